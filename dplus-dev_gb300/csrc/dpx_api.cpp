@@ -1,0 +1,769 @@
+// dpx_api.cpp — host side of libdpx: the C-ABI (include/dpx.h), device-resident
+// grids, form-factor tables, bracket plans and the drop-in wrappers with the
+// reference's argument meaning.  No entry point throws or traps; failures are
+// status codes with a per-thread message.
+#include "dpx.h"
+#include "dpx_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+#include <unordered_map>
+
+using dpx::Geom;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(DPX_ERR_OOM, "%s: %s", where, cudaGetErrorString(e));
+    }
+    return fail(DPX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+#define DPX_CUDA(call)                                          \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);     \
+    } while (0)
+
+const double kPi = 3.14159265358979323846;
+
+// Grow-only device buffer owned by a context.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+}  // namespace
+
+struct dpx_ctx_s {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    int fill_cpt = 4, fill_threads = 256;
+    DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs;
+    std::vector<char> host_stage;
+};
+
+struct dpx_grid_s {
+    dpx_ctx ctx;
+    int grid_size;
+    double qmax;
+    int precision;
+    Geom g;
+    void* cells;
+};
+
+namespace {
+
+int set_device(dpx_ctx ctx) {
+    int cur = -1;
+    DPX_CUDA(cudaGetDevice(&cur));
+    if (cur != ctx->device) DPX_CUDA(cudaSetDevice(ctx->device));
+    return DPX_OK;
+}
+
+size_t cell_bytes(int precision) { return precision == DPX_FP64 ? sizeof(double4_32a) : sizeof(float4); }
+
+// Unique-ion form factors minus the Gaussian dummy-atom solvent
+// (Atomic Form Factor.cpp:91-115, 121-176; r_m :11-27) for shells 0..Lp,
+// layout [U][Lp+1].
+void aff_table(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed,
+               double c1, int Lp, double step, std::vector<double>& out) {
+    double s3 = 0, n = 0;
+    for (int u = 0; u < U; ++u) {
+        s3 += rads[u] * rads[u] * rads[u] * api[u];
+        n += api[u];
+    }
+    const double rm = std::cbrt(s3 / n);
+    out.assign((size_t)U * (Lp + 1), 0.0);
+    for (int l = 0; l <= Lp; ++l) {
+        const double q = l * step;
+        const double s2 = q * q / (100.0 * 157.913670417429737901351855998);
+        for (int u = 0; u < U; ++u) {
+            double f = 0;
+            if (flags & DPX_CALC_ATOMIC_FORMFACTORS) {
+                for (int k = 0; k < 4; ++k) f += coeffs[u + 2 * k * U] * std::exp(-s2 * coeffs[u + (2 * k + 1) * U]);
+                f += coeffs[u + 8 * U];
+            }
+            double solvent = 0;
+            if (flags & DPX_CALC_DUMMY_SOLVENT) {
+                const double r = rads[u];
+                solvent = 4.1887902047863909846 * r * r * r * std::exp(-(rm * rm) * (q * q) * 0.2067834969664667) *
+                          sol_ed * c1 * c1 * c1 *
+                          std::exp(-0.6822178052976590 * q * q * rm * rm * (c1 * c1 - 1.0));
+            }
+            out[(size_t)u * (Lp + 1) + l] = f - solvent;
+        }
+    }
+}
+
+// Tait-Bryan X1Y2Z3 rotation (the reference's EulerD, Amplitude.h:557-573).
+void euler(double a, double b, double c, double R[9]) {
+    const double c1 = std::cos(a), s1 = std::sin(a), c2 = std::cos(b), s2 = std::sin(b), c3 = std::cos(c),
+                 s3 = std::sin(c);
+    R[0] = c2 * c3; R[1] = -c2 * s3; R[2] = s2;
+    R[3] = c1 * s3 + c3 * s1 * s2; R[4] = c1 * c3 - s1 * s2 * s3; R[5] = -c2 * s1;
+    R[6] = s1 * s3 - c1 * c3 * s2; R[7] = c3 * s1 + c1 * s2 * s3; R[8] = c1 * c2;
+}
+
+// Bracket assignment of IntegrateLayersTogether (Amplitude.cpp:1184-1217);
+// where two brackets claim one q, the later layer wins.
+void q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q) {
+    const int L = grid_size / 2;
+    const double step = 2 * qmax / grid_size;
+    for (int k = 0; k < nq; ++k) layer_of_q[k] = -1;
+    if (nq == 0) return;
+    int tmp = 0;
+    while (Q[0] > (tmp + 1) * step) tmp++;
+    for (int layer = tmp; layer < L; ++layer) {
+        int qb = 0;
+        while (qb < nq && Q[qb] <= layer * step) qb++;
+        if (qb >= nq) continue;
+        int qe = qb + 1;
+        if (qe == nq) qe--;
+        while (qe + 1 != nq && Q[qe] <= (layer + 1) * step) qe++;
+        if (qe + 1 != nq) qe--;
+        for (int k = qb; k <= qe; ++k) layer_of_q[k] = layer;
+    }
+}
+
+int grid_from_voxels(int64_t voxels, int thDivs, int phDivs, double stepSize, int* grid_size, double* qmax) {
+    if (thDivs != 3 || phDivs != 6) return fail(DPX_ERR_ARG, "only thDivs=3, phDivs=6 grids exist");
+    for (int lp = 4; lp < 4096; ++lp) {
+        const int64_t P = 6 * (int64_t)lp * (lp + 1) * (lp + 1) + 1;
+        if (P == voxels) {
+            *grid_size = 2 * (lp - 3);
+            *qmax = stepSize * (lp - 3);
+            return DPX_OK;
+        }
+        if (P > voxels) break;
+    }
+    return fail(DPX_ERR_ARG, "voxels=%lld is not a Jacobian sphere grid size", (long long)voxels);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dpx_last_error(void) { return g_err.c_str(); }
+int dpx_version(void) { return 1; }
+
+int dpx_ctx_create(int device, dpx_ctx* out) {
+    if (!out) return fail(DPX_ERR_ARG, "out is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(DPX_ERR_NODEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n) return fail(DPX_ERR_ARG, "device %d out of range", device);
+    DPX_CUDA(cudaSetDevice(device));
+    dpx_ctx c = new dpx_ctx_s();
+    c->device = device;
+    e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    c->stream = c->own;
+    *out = c;
+    return DPX_OK;
+}
+
+int dpx_ctx_destroy(dpx_ctx ctx) {
+    if (!ctx) return DPX_OK;
+    set_device(ctx);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
+                      &ctx->result, &ctx->dirs})
+        b->release();
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return DPX_OK;
+}
+
+int dpx_ctx_set_stream(dpx_ctx ctx, void* stream) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+    return DPX_OK;
+}
+
+void* dpx_ctx_get_stream(dpx_ctx ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int dpx_ctx_synchronize(dpx_ctx ctx) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    DPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return DPX_OK;
+}
+
+int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cpt, int threads) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    static const int ok[][2] = {{1, 128}, {2, 128}, {4, 128}, {8, 128}, {1, 256}, {2, 256},
+                                {4, 256}, {8, 256}, {2, 512}, {4, 512}};
+    for (auto& s : ok)
+        if (s[0] == cpt && s[1] == threads) {
+            ctx->fill_cpt = cpt;
+            ctx->fill_threads = threads;
+            return DPX_OK;
+        }
+    return fail(DPX_ERR_ARG, "unsupported fill shape %d x %d", cpt, threads);
+}
+
+int64_t dpx_grid_cells(int grid_size) {
+    if (grid_size < 2) return -1;
+    return dpx::make_geom(grid_size, 1.0).P;
+}
+
+int64_t dpx_grid_bytes(int grid_size, int precision) {
+    const int64_t p = dpx_grid_cells(grid_size);
+    return p < 0 ? -1 : p * (int64_t)cell_bytes(precision);
+}
+
+int dpx_grid_create(dpx_ctx ctx, int grid_size, double qmax, int precision, dpx_grid* out) {
+    if (!ctx || !out) return fail(DPX_ERR_ARG, "NULL argument");
+    if (grid_size < 2 || (grid_size & 1)) return fail(DPX_ERR_ARG, "grid_size must be even and >= 2");
+    if (!(qmax > 0)) return fail(DPX_ERR_ARG, "qmax must be positive");
+    if (precision != DPX_FP32 && precision != DPX_FP64) return fail(DPX_ERR_ARG, "bad precision");
+    if (int rc = set_device(ctx)) return rc;
+    dpx_grid g = new dpx_grid_s();
+    g->ctx = ctx;
+    g->grid_size = grid_size;
+    g->qmax = qmax;
+    g->precision = precision;
+    g->g = dpx::make_geom(grid_size, qmax);
+    cudaError_t e = cudaMalloc(&g->cells, (size_t)g->g.P * cell_bytes(precision));
+    if (e != cudaSuccess) {
+        delete g;
+        return cuda_fail(e, "cudaMalloc(grid)");
+    }
+    e = cudaMemsetAsync(g->cells, 0, (size_t)g->g.P * cell_bytes(precision), ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(g->cells);
+        delete g;
+        return cuda_fail(e, "cudaMemset(grid)");
+    }
+    *out = g;
+    return DPX_OK;
+}
+
+int dpx_grid_destroy(dpx_grid g) {
+    if (!g) return DPX_OK;
+    set_device(g->ctx);
+    cudaStreamSynchronize(g->ctx->stream);
+    cudaFree(g->cells);
+    delete g;
+    return DPX_OK;
+}
+
+void* dpx_grid_device_ptr(dpx_grid g) { return g ? g->cells : nullptr; }
+
+int dpx_grid_info(dpx_grid g, int* grid_size, double* qmax, int* precision, int64_t* cells) {
+    if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
+    if (grid_size) *grid_size = g->grid_size;
+    if (qmax) *qmax = g->qmax;
+    if (precision) *precision = g->precision;
+    if (cells) *cells = g->g.P;
+    return DPX_OK;
+}
+
+int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms_on_device, int n_ions,
+                      const int* atoms_per_ion, const double* coeffs, const double* ion_rads, int flags,
+                      double solvent_ed, double c1, double scale, const double* center) {
+    if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
+    if (n_atoms <= 0 || !atoms) return fail(DPX_ERR_ARG, "no atoms");
+    if (n_atoms > INT_MAX) return fail(DPX_ERR_ARG, "too many atoms (%lld)", (long long)n_atoms);
+    if (n_ions <= 0 || n_ions > 256 || !atoms_per_ion || !coeffs || !ion_rads)
+        return fail(DPX_ERR_ARG, "bad ion description");
+    int64_t tot = 0;
+    for (int u = 0; u < n_ions; ++u) {
+        if (atoms_per_ion[u] < 0) return fail(DPX_ERR_ARG, "negative atoms_per_ion");
+        tot += atoms_per_ion[u];
+    }
+    if (tot != n_atoms) return fail(DPX_ERR_ARG, "atoms_per_ion sums to %lld, n_atoms=%lld", (long long)tot,
+                                    (long long)n_atoms);
+    dpx_ctx ctx = g->ctx;
+    if (int rc = set_device(ctx)) return rc;
+    const Geom& G = g->g;
+    cudaStream_t s = ctx->stream;
+
+    // centring: atoms are shifted by c on the host; the kernel restores e^{i q.c}
+    double cen[3] = {0, 0, 0};
+    if (center) {
+        for (int k = 0; k < 3; ++k) cen[k] = center[k];
+    } else if (!atoms_on_device && g->precision == DPX_FP32) {
+        double acc[3] = {0, 0, 0};
+        for (int64_t j = 0; j < n_atoms; ++j)
+            for (int k = 0; k < 3; ++k) acc[k] += atoms[4 * j + k];
+        for (int k = 0; k < 3; ++k) cen[k] = acc[k] / double(n_atoms);
+    }
+    if (g->precision == DPX_FP64) cen[0] = cen[1] = cen[2] = 0.0;  // exact FP64 phases need no centring
+    const bool shift = (cen[0] != 0.0 || cen[1] != 0.0 || cen[2] != 0.0);
+
+    const float4* d_atoms = reinterpret_cast<const float4*>(atoms);
+    if (!atoms_on_device || shift) {
+        if (atoms_on_device) return fail(DPX_ERR_ARG, "an explicit centre needs host atoms");
+        DPX_CUDA(ctx->atoms.reserve((size_t)n_atoms * sizeof(float4)));
+        ctx->host_stage.resize((size_t)n_atoms * sizeof(float4));
+        float4* h = reinterpret_cast<float4*>(ctx->host_stage.data());
+        for (int64_t j = 0; j < n_atoms; ++j) {
+            h[j].x = (float)((double)atoms[4 * j] - cen[0]);
+            h[j].y = (float)((double)atoms[4 * j + 1] - cen[1]);
+            h[j].z = (float)((double)atoms[4 * j + 2] - cen[2]);
+            h[j].w = 0.f;
+        }
+        DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h, (size_t)n_atoms * sizeof(float4), cudaMemcpyHostToDevice, s));
+        d_atoms = reinterpret_cast<const float4*>(ctx->atoms.p);
+        DPX_CUDA(cudaStreamSynchronize(s));  // host_stage is reused by the next call
+    }
+
+    std::vector<int> off(n_ions + 1, 0);
+    for (int u = 0; u < n_ions; ++u) off[u + 1] = off[u] + atoms_per_ion[u];
+    std::vector<double> aff;
+    aff_table(n_ions, atoms_per_ion, coeffs, ion_rads, flags, solvent_ed, c1, G.Lp, G.step, aff);
+    const size_t tb = aff.size() * (g->precision == DPX_FP64 ? sizeof(double) : sizeof(float));
+    DPX_CUDA(ctx->table.reserve(tb));
+    DPX_CUDA(ctx->ions.reserve(off.size() * sizeof(int)));
+    std::vector<float> affF;
+    if (g->precision == DPX_FP32) affF.assign(aff.begin(), aff.end());
+    DPX_CUDA(cudaMemcpyAsync(ctx->table.p, g->precision == DPX_FP64 ? (const void*)aff.data() : (const void*)affF.data(),
+                             tb, cudaMemcpyHostToDevice, s));
+    DPX_CUDA(cudaMemcpyAsync(ctx->ions.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+
+    cudaError_t e;
+    if (g->precision == DPX_FP64)
+        e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, scale,
+                                 (double4_32a*)g->cells, 0, G.P);
+    else
+        e = dpx::launch_fill_f32(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const float*)ctx->table.p, G, cen,
+                                 (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads, 0, G.P);
+    if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
+    // the host vectors above are consumed by the async copies: wait before they go
+    DPX_CUDA(cudaStreamSynchronize(s));
+    return DPX_OK;
+}
+
+int dpx_grid_compute_splines(dpx_grid g) {
+    if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
+    if (int rc = set_device(g->ctx)) return rc;
+    cudaError_t e = g->precision == DPX_FP64 ? dpx::launch_splines_f64(g->ctx->stream, g->g, (double4_32a*)g->cells)
+                                             : dpx::launch_splines_f32(g->ctx->stream, g->g, (float4*)g->cells);
+    if (e != cudaSuccess) return cuda_fail(e, "spline launch");
+    return DPX_OK;
+}
+
+int dpx_grid_read(dpx_grid g, double* values, double* coeffs) {
+    if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
+    dpx_ctx ctx = g->ctx;
+    if (int rc = set_device(ctx)) return rc;
+    const size_t n = (size_t)g->g.P * 2 * sizeof(double);
+    DPX_CUDA(ctx->partial.reserve(n));
+    for (int which = 0; which < 2; ++which) {
+        double* dst = which ? coeffs : values;
+        if (!dst) continue;
+        cudaError_t e;
+        if (g->precision == DPX_FP64)
+            e = which ? dpx::launch_pack_ders_f64(ctx->stream, (double4_32a*)g->cells, g->g.P, (double*)ctx->partial.p)
+                      : dpx::launch_pack_values_f64(ctx->stream, (double4_32a*)g->cells, g->g.P, (double*)ctx->partial.p);
+        else
+            e = which ? dpx::launch_pack_ders_f32(ctx->stream, (float4*)g->cells, g->g.P, (double*)ctx->partial.p)
+                      : dpx::launch_pack_values_f32(ctx->stream, (float4*)g->cells, g->g.P, (double*)ctx->partial.p);
+        if (e != cudaSuccess) return cuda_fail(e, "pack launch");
+        DPX_CUDA(cudaMemcpyAsync(dst, ctx->partial.p, n, cudaMemcpyDeviceToHost, ctx->stream));
+        DPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return DPX_OK;
+}
+
+int dpx_grid_write(dpx_grid g, const double* values, const double* coeffs) {
+    if (!g || !values) return fail(DPX_ERR_ARG, "NULL argument");
+    dpx_ctx ctx = g->ctx;
+    if (int rc = set_device(ctx)) return rc;
+    const size_t n = (size_t)g->g.P * 2 * sizeof(double);
+    DPX_CUDA(ctx->partial.reserve(2 * n));
+    double* dv = (double*)ctx->partial.p;
+    double* dd = coeffs ? dv + 2 * g->g.P : nullptr;
+    DPX_CUDA(cudaMemcpyAsync(dv, values, n, cudaMemcpyHostToDevice, ctx->stream));
+    if (coeffs) DPX_CUDA(cudaMemcpyAsync(dd, coeffs, n, cudaMemcpyHostToDevice, ctx->stream));
+    cudaError_t e = g->precision == DPX_FP64 ? dpx::launch_unpack_f64(ctx->stream, dv, dd, g->g.P, (double4_32a*)g->cells)
+                                             : dpx::launch_unpack_f32(ctx->stream, dv, dd, g->g.P, (float4*)g->cells);
+    if (e != cudaSuccess) return cuda_fail(e, "unpack launch");
+    DPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return DPX_OK;
+}
+
+int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                            const int* n_copies, const double* copy_rot, const double* copy_tr,
+                            const double* sym_scale, int nq, const double* Q, const double* dirs, int dirs_on_device,
+                            int64_t dir_layer_stride, int64_t n_samples, double eps, double* res) {
+    if (!ctx || n_models <= 0 || !grids || nq <= 0 || !Q || !dirs || !res)
+        return fail(DPX_ERR_ARG, "NULL or empty argument");
+    if (n_samples <= 0) return fail(DPX_ERR_ARG, "n_samples must be positive");
+    const int grid_size = grids[0]->grid_size;
+    const double qmax = grids[0]->qmax;
+    const int prec = grids[0]->precision;
+    for (int m = 0; m < n_models; ++m)
+        if (!grids[m] || grids[m]->grid_size != grid_size || grids[m]->qmax != qmax || grids[m]->precision != prec)
+            return fail(DPX_ERR_ARG, "all models must share grid_size, qmax and precision");
+    for (int k = 1; k < nq; ++k)
+        if (!(Q[k] >= Q[k - 1])) return fail(DPX_ERR_ARG, "Q must be ascending");
+    if (Q[0] < 0) return fail(DPX_ERR_ARG, "negative q");
+    const Geom& G = grids[0]->g;
+    if (Q[nq - 1] > G.L * G.step * (1.0 + 1e-12))
+        return fail(DPX_ERR_ARG, "q=%g beyond the grid's qmax=%g", Q[nq - 1], G.L * G.step);
+    if (int rc = set_device(ctx)) return rc;
+    cudaStream_t s = ctx->stream;
+
+    // models and docked groups
+    std::vector<dpx::ModelDev> md(n_models);
+    std::vector<double> gR, gT;
+    std::vector<int> gOff;
+    std::vector<int> model_group_base(n_models), model_toff_base(n_models);
+    int copy_base = 0;
+    for (int m = 0; m < n_models; ++m) {
+        dpx::ModelDev& M = md[m];
+        M.grid = grids[m]->cells;
+        euler(rot ? rot[3 * m] : 0, rot ? rot[3 * m + 1] : 0, rot ? rot[3 * m + 2] : 0, M.R);
+        for (int k = 0; k < 3; ++k) M.tr[k] = tr ? tr[3 * m + k] : 0.0;
+        const int nc = n_copies ? n_copies[m] : 0;
+        M.sym_scale = sym_scale ? sym_scale[m] : 1.0;
+        model_group_base[m] = (int)gOff.size();
+        // group copies by identical Euler triples, first-appearance order
+        std::vector<int> rep;
+        std::vector<std::vector<int>> members;
+        for (int c = 0; c < nc; ++c) {
+            const double* r = copy_rot + 3 * (copy_base + c);
+            int found = -1;
+            for (size_t gi = 0; gi < rep.size(); ++gi) {
+                const double* r0 = copy_rot + 3 * (copy_base + rep[gi]);
+                if (r0[0] == r[0] && r0[1] == r[1] && r0[2] == r[2]) { found = (int)gi; break; }
+            }
+            if (found < 0) { rep.push_back(c); members.push_back({c}); }
+            else members[found].push_back(c);
+        }
+        M.n_groups = (int)rep.size();
+        model_toff_base[m] = (int)(gT.size() / 3);
+        for (size_t gi = 0; gi < rep.size(); ++gi) {
+            double R[9];
+            const double* r = copy_rot + 3 * (copy_base + rep[gi]);
+            euler(r[0], r[1], r[2], R);
+            gR.insert(gR.end(), R, R + 9);
+            gOff.push_back((int)(gT.size() / 3) - model_toff_base[m]);
+            for (int c : members[gi]) {
+                const double* t = copy_tr + 3 * (copy_base + c);
+                gT.insert(gT.end(), t, t + 3);
+            }
+        }
+        gOff.push_back((int)(gT.size() / 3) - model_toff_base[m]);
+        copy_base += nc;
+    }
+    // device layout of the group tables: [R (doubles)] [T (doubles)] [off (ints)]
+    const size_t bytesR = gR.size() * sizeof(double), bytesT = gT.size() * sizeof(double),
+                 bytesO = gOff.size() * sizeof(int);
+    DPX_CUDA(ctx->groups.reserve(bytesR + bytesT + bytesO + 64));
+    char* gbase = (char*)ctx->groups.p;
+    double* dR = (double*)gbase;
+    double* dT = (double*)(gbase + bytesR);
+    int* dO = (int*)(gbase + bytesR + bytesT);
+    std::vector<char> gstage(bytesR + bytesT + bytesO);
+    if (bytesR) std::memcpy(gstage.data(), gR.data(), bytesR);
+    if (bytesT) std::memcpy(gstage.data() + bytesR, gT.data(), bytesT);
+    if (bytesO) std::memcpy(gstage.data() + bytesR + bytesT, gOff.data(), bytesO);
+    int groups_seen = 0;
+    for (int m = 0; m < n_models; ++m) {
+        dpx::ModelDev& M = md[m];
+        M.group_R = dR + 9 * groups_seen;
+        M.group_off = dO + model_group_base[m];
+        M.trans = dT + 3 * model_toff_base[m];
+        groups_seen += M.n_groups;
+    }
+
+    // brackets
+    std::vector<int> layer_of_q(nq);
+    q_brackets(grid_size, qmax, nq, Q, layer_of_q.data());
+    std::vector<int> br_layer, br_off{0}, br_qidx;
+    std::vector<double> br_q;
+    int max_q = 1;
+    for (int l = 0; l < G.L; ++l) {
+        int cnt = 0;
+        for (int k = 0; k < nq; ++k)
+            if (layer_of_q[k] == l) {
+                br_q.push_back(Q[k]);
+                br_qidx.push_back(k);
+                cnt++;
+            }
+        if (cnt) {
+            br_layer.push_back(l);
+            br_off.push_back((int)br_q.size());
+            max_q = std::max(max_q, cnt);
+        }
+    }
+    const int nbr = (int)br_layer.size();
+    dpx::AvgPlan plan{};
+    plan.n_brackets = nbr;
+    plan.max_q = max_q;
+    plan.n_samples = n_samples;
+    plan.chunk = eps > 0.0 ? 100 : 128;
+    plan.chunk_off = eps > 0.0 ? 99 : 0;
+    plan.n_chunks = (n_samples + plan.chunk_off + plan.chunk - 1) / plan.chunk;
+    plan.dir_stride = dir_layer_stride;
+    const size_t pb = br_layer.size() * sizeof(int) + br_off.size() * sizeof(int) + br_qidx.size() * sizeof(int) +
+                      br_q.size() * sizeof(double) + 64;
+    DPX_CUDA(ctx->plan.reserve(pb + md.size() * sizeof(dpx::ModelDev) + 64));
+    std::vector<char> stage(pb + md.size() * sizeof(dpx::ModelDev) + 64);
+    size_t o = 0;
+    auto put = [&](const void* src, size_t n) -> size_t {
+        size_t at = (o + 15) & ~size_t(15);
+        if (n) std::memcpy(stage.data() + at, src, n);
+        o = at + n;
+        return at;
+    };
+    const size_t oQ = put(br_q.data(), br_q.size() * sizeof(double));
+    const size_t oL = put(br_layer.data(), br_layer.size() * sizeof(int));
+    const size_t oO = put(br_off.data(), br_off.size() * sizeof(int));
+    const size_t oI = put(br_qidx.data(), br_qidx.size() * sizeof(int));
+    const size_t oM = put(md.data(), md.size() * sizeof(dpx::ModelDev));
+    char* pbase = (char*)ctx->plan.p;
+    plan.br_q = (const double*)(pbase + oQ);
+    plan.br_layer = (const int*)(pbase + oL);
+    plan.br_q_off = (const int*)(pbase + oO);
+    plan.br_qidx = (const int*)(pbase + oI);
+    const dpx::ModelDev* d_models = (const dpx::ModelDev*)(pbase + oM);
+
+    // directions
+    if (dirs_on_device) {
+        plan.dirs = dirs;
+    } else {
+        const int64_t nd = (dir_layer_stride ? (int64_t)(G.L - 1) * dir_layer_stride : 0) + n_samples;
+        DPX_CUDA(ctx->dirs.reserve((size_t)nd * 2 * sizeof(double)));
+        DPX_CUDA(cudaMemcpyAsync(ctx->dirs.p, dirs, (size_t)nd * 2 * sizeof(double), cudaMemcpyHostToDevice, s));
+        plan.dirs = (const double*)ctx->dirs.p;
+    }
+    const size_t part = ((size_t)nbr * plan.n_chunks + (size_t)nbr * 5) * max_q * sizeof(double) + 64;
+    DPX_CUDA(ctx->partial.reserve(part));
+    plan.partial = (double*)ctx->partial.p;
+    DPX_CUDA(ctx->result.reserve((size_t)nq * sizeof(double)));
+    DPX_CUDA(cudaMemcpyAsync(ctx->plan.p, stage.data(), o, cudaMemcpyHostToDevice, s));
+    DPX_CUDA(cudaMemcpyAsync(ctx->groups.p, gstage.data(), gstage.size(), cudaMemcpyHostToDevice, s));
+    DPX_CUDA(cudaMemsetAsync(ctx->result.p, 0, (size_t)nq * sizeof(double), s));
+
+    cudaError_t e = dpx::launch_average(s, prec == DPX_FP64, G, n_models, d_models, plan);
+    if (e != cudaSuccess) return cuda_fail(e, "average launch");
+    e = dpx::launch_finalize(s, plan, eps, (double*)ctx->result.p);
+    if (e != cudaSuccess) return cuda_fail(e, "finalize launch");
+    DPX_CUDA(cudaMemcpyAsync(res, ctx->result.p, (size_t)nq * sizeof(double), cudaMemcpyDeviceToHost, s));
+
+    // q == 0: |sum of leaves at the origin|^2 (Amplitude.cpp:1176-1182)
+    std::vector<double> origin(4 * n_models, 0.0);
+    for (int m = 0; m < n_models; ++m) {
+        if (prec == DPX_FP64) {
+            DPX_CUDA(cudaMemcpyAsync(&origin[4 * m], grids[m]->cells, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        } else {
+            float2 v;
+            DPX_CUDA(cudaMemcpyAsync(&v, grids[m]->cells, sizeof(float2), cudaMemcpyDeviceToHost, s));
+            DPX_CUDA(cudaStreamSynchronize(s));
+            origin[4 * m] = v.x;
+            origin[4 * m + 1] = v.y;
+        }
+    }
+    DPX_CUDA(cudaStreamSynchronize(s));
+    if (Q[0] == 0.0) {
+        double ar = 0, ai = 0;
+        for (int m = 0; m < n_models; ++m) {
+            double w = 1.0;
+            if (md[m].n_groups > 0) w = (n_copies ? n_copies[m] : 0) * md[m].sym_scale;
+            ar += w * origin[4 * m];
+            ai += w * origin[4 * m + 1];
+        }
+        res[0] = ar * ar + ai * ai;
+    }
+    return DPX_OK;
+}
+
+int dpx_mc_directions(uint32_t seed, int64_t D, double* theta_phi) {
+    if (D < 0 || (D > 0 && !theta_phi)) return fail(DPX_ERR_ARG, "bad direction buffer");
+    std::mt19937 rng;
+    rng.seed(seed);
+    std::uniform_real_distribution<double> u(0.0, 2.0);
+    for (int64_t i = 0; i < D; ++i) {
+        const double u2 = u(rng);
+        const double v2 = u(rng);
+        theta_phi[2 * i + 1] = u2 * kPi;
+        theta_phi[2 * i] = std::acos(v2 - 1.0);
+    }
+    return DPX_OK;
+}
+
+int dpx_layer_seeds(uint32_t master, int nq, int n_layers, uint32_t* seeds) {
+    if (!seeds || nq < 0 || n_layers < 0) return fail(DPX_ERR_ARG, "bad arguments");
+    std::mt19937 gen;
+    std::uniform_int_distribution<unsigned int> draw(0, UINT_MAX);
+    gen.seed(master);
+    for (int i = 0; i < nq; ++i) (void)draw(gen);
+    for (int i = 0; i <= n_layers; ++i) seeds[i] = draw(gen);
+    return DPX_OK;
+}
+
+int dpx_q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q) {
+    if (grid_size < 2 || nq < 0 || (nq > 0 && (!Q || !layer_of_q))) return fail(DPX_ERR_ARG, "bad arguments");
+    q_brackets(grid_size, qmax, nq, Q, layer_of_q);
+    return DPX_OK;
+}
+
+int dpx_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xyz, int* elem) {
+    if (n_atoms <= 0 || !(radius_nm > 0) || !xyz || !elem) return fail(DPX_ERR_ARG, "bad arguments");
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U01(0.0, 1.0);
+    const double step = 0.15, min_d = 0.1, cell = 0.2;
+    const double R = radius_nm;
+    const int nc = (int)std::ceil(2 * R / cell) + 2;
+    auto key = [&](double x, double y, double z) -> int64_t {
+        int64_t ix = (int64_t)std::floor((x + R) / cell) + 1, iy = (int64_t)std::floor((y + R) / cell) + 1,
+                iz = (int64_t)std::floor((z + R) / cell) + 1;
+        return (ix * nc + iy) * nc + iz;
+    };
+    std::unordered_map<int64_t, std::vector<int64_t>> cells;
+    cells.reserve((size_t)n_atoms * 2);
+    auto free_at = [&](double x, double y, double z) -> bool {
+        const int64_t ix = (int64_t)std::floor((x + R) / cell) + 1, iy = (int64_t)std::floor((y + R) / cell) + 1,
+                      iz = (int64_t)std::floor((z + R) / cell) + 1;
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dz = -1; dz <= 1; ++dz) {
+                    auto it = cells.find(((ix + dx) * nc + (iy + dy)) * nc + (iz + dz));
+                    if (it == cells.end()) continue;
+                    for (int64_t j : it->second) {
+                        const double ex = xyz[3 * j] - x, ey = xyz[3 * j + 1] - y, ez = xyz[3 * j + 2] - z;
+                        if (ex * ex + ey * ey + ez * ez < min_d * min_d) return false;
+                    }
+                }
+        return true;
+    };
+    double px = 0, py = 0, pz = 0;
+    for (int64_t i = 0; i < n_atoms; ++i) {
+        double x = px, y = py, z = pz;
+        if (i > 0) {
+            bool placed = false;
+            for (int attempt = 0; attempt < 64 && !placed; ++attempt) {
+                const double ct = 2 * U01(rng) - 1, ph = 2 * kPi * U01(rng), st = std::sqrt(1 - ct * ct);
+                x = px + step * st * std::cos(ph);
+                y = py + step * st * std::sin(ph);
+                z = pz + step * ct;
+                if (x * x + y * y + z * z > R * R) continue;
+                placed = free_at(x, y, z);
+            }
+            if (!placed) {
+                // dead end: restart the chain at a random free point inside the sphere
+                for (int attempt = 0; attempt < 100000; ++attempt) {
+                    x = (2 * U01(rng) - 1) * R;
+                    y = (2 * U01(rng) - 1) * R;
+                    z = (2 * U01(rng) - 1) * R;
+                    if (x * x + y * y + z * z <= R * R && free_at(x, y, z)) { placed = true; break; }
+                }
+                if (!placed) return fail(DPX_ERR_ARG, "globule of radius %g nm cannot hold %lld atoms", R,
+                                         (long long)n_atoms);
+            }
+        }
+        xyz[3 * i] = (float)x;
+        xyz[3 * i + 1] = (float)y;
+        xyz[3 * i + 2] = (float)z;
+        cells[key(x, y, z)].push_back(i);
+        px = x; py = y; pz = z;
+        const double r = U01(rng);
+        elem[i] = r < 0.63 ? 0 : (r < 0.80 ? 1 : (r < 0.99 ? 2 : 3));
+    }
+    return DPX_OK;
+}
+
+int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
+                                    const float* atomLocations, int64_t numAtoms, int numUniqueIons,
+                                    const int* atomsPerIon, const float* coeffs, const float* ionRads,
+                                    int bitCombination, float solventED, float c1, double scale, int precision,
+                                    int* pStop) {
+    if (!outData || !atomLocations) return fail(DPX_ERR_ARG, "NULL buffer");
+    int grid_size;
+    double qmax;
+    if (int rc = grid_from_voxels((int64_t)voxels, thDivs, phDivs, stepSize, &grid_size, &qmax)) return rc;
+    if (pStop && *pStop) return fail(DPX_ERR_STOPPED, "stopped");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dpx_ctx ctx;
+    if (int rc = dpx_ctx_create(dev, &ctx)) return rc;
+    dpx_grid g;
+    int rc = dpx_grid_create(ctx, grid_size, qmax, precision, &g);
+    if (rc) { dpx_ctx_destroy(ctx); return rc; }
+    std::vector<double> cd(9 * numUniqueIons), rd(numUniqueIons);
+    for (int k = 0; k < 9 * numUniqueIons; ++k) cd[k] = coeffs[k];
+    for (int k = 0; k < numUniqueIons; ++k) rd[k] = ionRads ? ionRads[k] : 0.0;
+    rc = dpx_grid_fill_pdb(g, numAtoms, atomLocations, 0, numUniqueIons, atomsPerIon, cd.data(), rd.data(),
+                           bitCombination, solventED, c1, scale, nullptr);
+    if (!rc && pStop && *pStop) rc = fail(DPX_ERR_STOPPED, "stopped");
+    if (!rc) rc = dpx_grid_read(g, outData, nullptr);
+    dpx_grid_destroy(g);
+    dpx_ctx_destroy(ctx);
+    return rc;
+}
+
+int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* inAmp,
+                             const double* inD, const double* qs, double* intensities, int qPoints, int64_t maxIters,
+                             double convergence, const double* dirs, int64_t dir_layer_stride, int precision,
+                             int* pStop) {
+    if (!inAmp || !inD || !qs || !intensities || !dirs) return fail(DPX_ERR_ARG, "NULL buffer");
+    int grid_size;
+    double qmax;
+    if (int rc = grid_from_voxels(voxels, thDivs, phDivs, stepSz, &grid_size, &qmax)) return rc;
+    if (pStop && *pStop) return fail(DPX_ERR_STOPPED, "stopped");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dpx_ctx ctx;
+    if (int rc = dpx_ctx_create(dev, &ctx)) return rc;
+    dpx_grid g;
+    int rc = dpx_grid_create(ctx, grid_size, qmax, precision, &g);
+    if (rc) { dpx_ctx_destroy(ctx); return rc; }
+    rc = dpx_grid_write(g, inAmp, inD);
+    if (!rc)
+        rc = dpx_orientation_average(ctx, 1, &g, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, qPoints, qs, dirs,
+                                     0, dir_layer_stride, maxIters, convergence, intensities);
+    if (!rc && pStop && *pStop) rc = fail(DPX_ERR_STOPPED, "stopped");
+    dpx_grid_destroy(g);
+    dpx_ctx_destroy(ctx);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+// dpx_internal.h — shared declarations between the host side (dpx_api.cpp)
+// and the sm_103a kernels (dpx_kernels.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dpx {
+
+// Jacobian sphere grid geometry (D+ Grid.cpp:169-200): shell i in 1..Lp holds
+// (3i+1) theta rows of 6i phi points; cell 0 is the origin.
+struct Geom {
+    int L;        // radial layers (grid_size / 2)
+    int Lp;       // layers including the 3 extra shells
+    double step;  // qmax / L
+    int64_t P;    // complex cells
+};
+
+inline Geom make_geom(int grid_size, double qmax) {
+    Geom g;
+    g.L = grid_size / 2;
+    g.Lp = g.L + 3;
+    g.step = qmax / double(g.L);
+    int64_t lp = g.Lp;
+    g.P = 6 * lp * (lp + 1) * (lp + 1) + 1;
+    return g;
+}
+
+__host__ __device__ inline int64_t shell_base(int64_t i) { return 1 + 6 * (i - 1) * i * i; }
+
+// One placed view of a grid for the orientation average: the leaf's own
+// rotation/translation and, for a docked assembly, groups of copies that share
+// a rotation (ManualSymmetry translationsPerOrientation).
+struct ModelDev {
+    const void* grid;      // float4* (FP32) or double4_32a* (FP64): {re, im, dre, dim} per cell
+    double R[9];           // leaf RotMat (row-major)
+    double tr[3];          // leaf translation
+    int n_groups;          // 0 = plain leaf
+    const double* group_R; // [9 n_groups] rotation per group (row-major)
+    const int* group_off;  // [n_groups + 1] into trans
+    const double* trans;   // [3 K]
+    double sym_scale;
+};
+
+struct AvgPlan {
+    int n_brackets;
+    const int* br_layer;     // [nbr] layer index of the bracket
+    const int* br_q_off;     // [nbr + 1] offsets into br_q / br_qidx
+    const double* br_q;      // q values, bracket-major
+    const int* br_qidx;      // index into the result vector
+    int max_q;               // max q per bracket
+    const double* dirs;      // [D x 2] theta, phi
+    int64_t dir_stride;      // per-layer stride in directions (0 = shared)
+    int64_t n_samples;       // samples per bracket
+    int chunk;               // samples per chunk
+    int chunk_off;           // first chunk holds chunk - chunk_off samples
+    int64_t n_chunks;
+    double* partial;         // [nbr][n_chunks][max_q]
+};
+
+// kernels (dpx_kernels.cu)
+cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
+                            const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,
+                            int block, int64_t cell_lo, int64_t cell_hi);
+cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
+                            const Geom& g, double scale, double4_32a* grid, int64_t cell_lo, int64_t cell_hi);
+cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid);
+cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid);
+cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                           const AvgPlan& plan);
+cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
+cudaError_t launch_pack_values_f32(cudaStream_t s, const float4* grid, int64_t P, double* out);
+cudaError_t launch_pack_values_f64(cudaStream_t s, const double4_32a* grid, int64_t P, double* out);
+cudaError_t launch_unpack_f64(cudaStream_t s, const double* vals, const double* ders, int64_t P, double4_32a* grid);
+cudaError_t launch_unpack_f32(cudaStream_t s, const double* vals, const double* ders, int64_t P, float4* grid);
+cudaError_t launch_pack_ders_f32(cudaStream_t s, const float4* grid, int64_t P, double* out);
+cudaError_t launch_pack_ders_f64(cudaStream_t s, const double4_32a* grid, int64_t P, double* out);
+
+}  // namespace dpx

@@ -1,0 +1,663 @@
+// dpx_kernels.cu — sm_103a kernels of the D+ scattering hot path.
+//
+//   amplitude grid fill   F(q) = sum_ions aff_u(|q|) sum_{j in u} e^{i q.r_j}
+//                         (D+ PDBAmplitude.cpp:243-317 / Grid.cpp:760-826)
+//   periodic phi splines  circ(1,4,1) d = 3 (y[k+1] - y[k-1]) per theta row
+//                         (D+ PeriodicSplineSolver.h:7-67, Grid.cpp:1113-1151)
+//   orientation average   4-plane / 4-row Hermite interpolation + docked sum,
+//                         |A|^2 summed per (bracket, chunk, q)
+//                         (D+ Grid.cpp:61-134, 551-721; Amplitude.cpp:2746-2822,
+//                          3553-3600; Symmetries.cpp:1079-1166)
+//
+// Grid cells are stored interleaved {re, im, d_re, d_im} (float4 or double4_32a) so
+// that one interpolation node is one 16 B / 32 B sector.
+#include "dpx_internal.h"
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <cstdint>
+
+namespace dpx {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double k2Pi = 6.28318530717958647692528676656;
+
+// --------------------------------------------------------------------------
+// cell index -> (shell, theta row, phi column)
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void cell_indices(int64_t idx, int& qi, int& ti, int& pi) {
+    if (idx == 0) { qi = 0; ti = 0; pi = 0; return; }
+    int64_t i = (int64_t)cbrtf((float)idx * (1.0f / 6.0f));
+    if (i < 1) i = 1;
+    while (i > 1 && shell_base(i) > idx) --i;
+    while (shell_base(i + 1) <= idx) ++i;
+    int64_t rem = idx - shell_base(i);
+    qi = (int)i;
+    ti = (int)(rem / (6 * i));
+    pi = (int)(rem - (int64_t)ti * 6 * i);
+}
+
+__device__ __forceinline__ void next_cell(int& qi, int& ti, int& pi) {
+    if (qi == 0) { qi = 1; ti = 0; pi = 0; return; }
+    if (++pi == 6 * qi) {
+        pi = 0;
+        if (++ti == 3 * qi + 1) { ti = 0; ++qi; }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Amplitude fill, FP32 bulk.  Atoms (centred, sorted by ion) are staged in
+// shared memory one tile per block; every thread owns CPT consecutive cells
+// and accumulates sum cos / sum sin per ion in FP32 (tile partial sums keep the
+// accumulation error at the tile level), then multiplies by the ion's form
+// factor at the cell's shell.  An optional per-cell phase e^{i q.c} (FP64)
+// restores the centring translation.
+// --------------------------------------------------------------------------
+template <int CPT, int THREADS>
+__global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restrict__ atoms,
+                                                           const int* __restrict__ ion_off, int U,
+                                                           const float* __restrict__ aff, int Lp, double step,
+                                                           double cx, double cy, double cz, int use_center,
+                                                           float scale, float4* __restrict__ grid,
+                                                           int64_t cell_lo, int64_t cell_hi) {
+    __shared__ float4 s_atoms[THREADS];
+    const int64_t first = cell_lo + ((int64_t)blockIdx.x * THREADS + threadIdx.x) * CPT;
+
+    float qx[CPT], qy[CPT], qz[CPT], accR[CPT], accI[CPT];
+    int layer[CPT];
+    {
+        int qi, ti, pi;
+        cell_indices(first < cell_hi ? first : 0, qi, ti, pi);
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            layer[c] = qi;
+            if (qi == 0) {
+                qx[c] = qy[c] = qz[c] = 0.f;
+            } else {
+                const float inv = 1.0f / (float)(3 * qi);
+                float st, ct, sp, cp;
+                sincospif((float)ti * inv, &st, &ct);
+                sincospif((float)pi * inv, &sp, &cp);
+                const float qI = (float)((double)qi * step);
+                qx[c] = qI * st * cp;
+                qy[c] = qI * st * sp;
+                qz[c] = qI * ct;
+            }
+            accR[c] = 0.f;
+            accI[c] = 0.f;
+            if (layer[c] > Lp) layer[c] = Lp;  // cells past the grid end are never stored
+            next_cell(qi, ti, pi);
+        }
+    }
+
+    for (int u = 0; u < U; ++u) {
+        const int a0 = ion_off[u], a1 = ion_off[u + 1];
+        float sR[CPT], sI[CPT];
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) { sR[c] = 0.f; sI[c] = 0.f; }
+        for (int t0 = a0; t0 < a1; t0 += THREADS) {
+            const int n = min(THREADS, a1 - t0);
+            __syncthreads();
+            if (threadIdx.x < n) s_atoms[threadIdx.x] = atoms[t0 + threadIdx.x];
+            __syncthreads();
+            float tR[CPT], tI[CPT];
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) { tR[c] = 0.f; tI[c] = 0.f; }
+#pragma unroll 4
+            for (int j = 0; j < n; ++j) {
+                const float4 a = s_atoms[j];
+#pragma unroll
+                for (int c = 0; c < CPT; ++c) {
+                    const float ph = fmaf(qz[c], a.z, fmaf(qy[c], a.y, qx[c] * a.x));
+                    float sn, cs;
+                    __sincosf(ph, &sn, &cs);
+                    tR[c] += cs;
+                    tI[c] += sn;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) { sR[c] += tR[c]; sI[c] += tI[c]; }
+        }
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            const float f = aff[(int64_t)u * (Lp + 1) + layer[c]];
+            accR[c] = fmaf(f, sR[c], accR[c]);
+            accI[c] = fmaf(f, sI[c], accI[c]);
+        }
+    }
+
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+        const int64_t cell = first + c;
+        if (cell >= cell_hi) break;
+        float re = accR[c] * scale, im = accI[c] * scale;
+        if (use_center) {
+            const double ph = (double)qx[c] * cx + (double)qy[c] * cy + (double)qz[c] * cz;
+            double sn, cs;
+            sincos(ph, &sn, &cs);
+            const float fs = (float)sn, fc = (float)cs;
+            const float r2 = re * fc - im * fs, i2 = re * fs + im * fc;
+            re = r2;
+            im = i2;
+        }
+        reinterpret_cast<float2*>(grid + cell)[0] = make_float2(re, im);
+    }
+}
+
+// --------------------------------------------------------------------------
+// Amplitude fill, plain FP64: FP64 q vector, FP64 phase, FP64 sincos, FP64
+// accumulation.  Same tiling, one cell per thread.
+// --------------------------------------------------------------------------
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restrict__ atoms,
+                                                           const int* __restrict__ ion_off, int U,
+                                                           const double* __restrict__ aff, int Lp, double step,
+                                                           double scale, double4_32a* __restrict__ grid,
+                                                           int64_t cell_lo, int64_t cell_hi) {
+    __shared__ double4_32a s_atoms[THREADS];
+    const int64_t cell = cell_lo + (int64_t)blockIdx.x * THREADS + threadIdx.x;
+    int qi, ti, pi;
+    cell_indices(cell < cell_hi ? cell : 0, qi, ti, pi);
+    double qx = 0, qy = 0, qz = 0;
+    if (qi > 0) {
+        const double inv = 1.0 / (double)(3 * qi);
+        double st, ct, sp, cp;
+        sincospi((double)ti * inv, &st, &ct);
+        sincospi((double)pi * inv, &sp, &cp);
+        const double qI = (double)qi * step;
+        qx = qI * st * cp;
+        qy = qI * st * sp;
+        qz = qI * ct;
+    }
+    const int layer = qi > Lp ? Lp : qi;
+    double accR = 0, accI = 0;
+    for (int u = 0; u < U; ++u) {
+        const int a0 = ion_off[u], a1 = ion_off[u + 1];
+        double sR = 0, sI = 0;
+        for (int t0 = a0; t0 < a1; t0 += THREADS) {
+            const int n = min(THREADS, a1 - t0);
+            __syncthreads();
+            if (threadIdx.x < n) {
+                const float4 a = atoms[t0 + threadIdx.x];
+                s_atoms[threadIdx.x] = make_double4_32a(a.x, a.y, a.z, 0.0);
+            }
+            __syncthreads();
+            for (int j = 0; j < n; ++j) {
+                const double4_32a a = s_atoms[j];
+                const double ph = qx * a.x + qy * a.y + qz * a.z;
+                double sn, cs;
+                sincos(ph, &sn, &cs);
+                sR += cs;
+                sI += sn;
+            }
+        }
+        const double f = aff[(int64_t)u * (Lp + 1) + layer];
+        accR += f * sR;
+        accI += f * sI;
+    }
+    if (cell < cell_hi) reinterpret_cast<double2*>(grid + cell)[0] = make_double2(accR * scale, accI * scale);
+}
+
+// --------------------------------------------------------------------------
+// Periodic cubic-spline derivatives along each theta row.  The inverse of the
+// circulant circ(1,4,1) is a two-sided geometric kernel G(m) = C(a^m + a^(n-m))
+// / (1 - a^n), a = sqrt(3) - 2, C = 1/(2 sqrt 3); folding the right-hand side
+// 3(y[k+1]-y[k-1]) into it gives d_k = sum_s H(s) (y[k-s] - y[k+s]) with
+// H(s) = 3C a^(s-1) (a^2 - 1).  Long rows use the K-term truncation (|a|^K
+// below the type's epsilon); short rows use the exact periodic kernel.
+// --------------------------------------------------------------------------
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { typedef float4 type; typedef float2 half; };
+template <> struct Vec4<double> { typedef double4_32a type; typedef double2 half; };
+
+template <typename T, int K>
+__global__ void splines_kernel(typename Vec4<T>::type* __restrict__ grid, int64_t P) {
+    typedef typename Vec4<T>::half H2;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= P) return;
+    if (idx == 0) {
+        reinterpret_cast<H2*>(grid)[1] = H2{T(0), T(0)};
+        return;
+    }
+    int qi, ti, pi;
+    cell_indices(idx, qi, ti, pi);
+    const int n = 6 * qi;
+    const int64_t row = shell_base(qi) + (int64_t)ti * n;
+    const double alpha = -0.26794919243112270647;  // sqrt(3) - 2
+    const double C = 0.28867513459481288225;        // 1 / (2 sqrt 3)
+    T dr = 0, di = 0;
+    if (n > 2 * K + 2) {
+        double w = 3.0 * C * (alpha * alpha - 1.0);
+        for (int s = 1; s <= K; ++s) {
+            int lo = pi - s; if (lo < 0) lo += n;
+            int hi = pi + s; if (hi >= n) hi -= n;
+            const typename Vec4<T>::type a = grid[row + lo];
+            const typename Vec4<T>::type b = grid[row + hi];
+            dr += T(w) * (a.x - b.x);
+            di += T(w) * (a.y - b.y);
+            w *= alpha;
+        }
+    } else {
+        const double an = pow(alpha, (double)n);
+        const double denom = 1.0 / (1.0 - an);
+        for (int s = 0; s < n; ++s) {
+            int m1 = s + 1; if (m1 >= n) m1 -= n;
+            int m0 = s - 1; if (m0 < 0) m0 += n;
+            const double g1 = C * (pow(alpha, (double)m1) + pow(alpha, (double)(n - m1))) * denom;
+            const double g0 = C * (pow(alpha, (double)m0) + pow(alpha, (double)(n - m0))) * denom;
+            const double h = 3.0 * (g1 - g0);
+            int k = pi - s; if (k < 0) k += n;
+            const typename Vec4<T>::type a = grid[row + k];
+            dr += T(h) * a.x;
+            di += T(h) * a.y;
+        }
+    }
+    reinterpret_cast<H2*>(grid + idx)[1] = H2{dr, di};
+}
+
+// --------------------------------------------------------------------------
+// Interpolation on the Jacobian sphere grid.
+// --------------------------------------------------------------------------
+template <typename T>
+struct Cx {
+    T r, i;
+};
+template <typename T> __device__ __forceinline__ Cx<T> cadd(Cx<T> a, Cx<T> b) { return {a.r + b.r, a.i + b.i}; }
+template <typename T> __device__ __forceinline__ Cx<T> csub(Cx<T> a, Cx<T> b) { return {a.r - b.r, a.i - b.i}; }
+template <typename T> __device__ __forceinline__ Cx<T> cscale(Cx<T> a, T s) { return {a.r * s, a.i * s}; }
+template <typename T> __device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
+    return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> hermite(Cx<T> p1, Cx<T> p2, Cx<T> d1, Cx<T> d2, T t) {
+    // p1 + d1 t + (3(p2-p1) - 2 d1 - d2) t^2 + (2(p1-p2) + d1 + d2) t^3
+    const T t2 = t * t, t3 = t2 * t;
+    Cx<T> c2 = csub(csub(cscale(csub(p2, p1), T(3)), cscale(d1, T(2))), d2);
+    Cx<T> c3 = cadd(cadd(cscale(csub(p1, p2), T(2)), d1), d2);
+    return cadd(cadd(cadd(p1, cscale(d1, t)), cscale(c2, t2)), cscale(c3, t3));
+}
+
+template <typename T>
+__device__ __forceinline__ void four_point(Cx<T> y1, Cx<T> y2, Cx<T> y3, Cx<T> y4, Cx<T>& d2, Cx<T>& d3) {
+    // Ginsburg et al. 2019, eqs 35-36
+    const Cx<T> a = csub(y2, y1), b = csub(y3, y1), c = csub(y4, y2), d = csub(y4, y3);
+    d2 = cadd(cadd(cadd(cscale(a, T(-7. / 15.)), cscale(b, T(14. / 15.))), cscale(c, T(-4. / 15.))),
+              cscale(d, T(2. / 15.)));
+    d3 = cadd(cadd(cadd(cscale(a, T(2. / 15.)), cscale(b, T(-4. / 15.))), cscale(c, T(14. / 15.))),
+              cscale(d, T(-7. / 15.)));
+}
+
+template <typename T>
+__device__ __forceinline__ void load_cell(const typename Vec4<T>::type* __restrict__ g, int64_t c, Cx<T>& v,
+                                          Cx<T>& d);
+template <>
+__device__ __forceinline__ void load_cell<float>(const float4* __restrict__ g, int64_t c, Cx<float>& v,
+                                                 Cx<float>& d) {
+    const float4 x = __ldg(g + c);
+    v = {x.x, x.y};
+    d = {x.z, x.w};
+}
+template <>
+__device__ __forceinline__ void load_cell<double>(const double4_32a* __restrict__ g, int64_t c, Cx<double>& v,
+                                                  Cx<double>& d) {
+    const double2* p = reinterpret_cast<const double2*>(g + c);
+    const double2 a = __ldg(p), b = __ldg(p + 1);
+    v = {a.x, a.y};
+    d = {b.x, b.y};
+}
+
+// One theta-phi plane at shell ri (Grid.cpp:61-134 with IndicesFromRadians :1220-1256).
+template <typename T>
+__device__ Cx<T> interp_plane(const typename Vec4<T>::type* __restrict__ g, int ri, double theta, double phi) {
+    const int64_t base = shell_base(ri);
+    const int64_t phiPoints = 6 * (int64_t)ri, thePoints = 3 * (int64_t)ri;
+    const double edge = k2Pi / (double)phiPoints;
+    const int64_t tI = (int64_t)((theta / kPi) * (double)thePoints);
+    int64_t pI = (int64_t)((phi / k2Pi) * (double)phiPoints);
+    double tTh = (theta / edge) - (double)tI;
+    double tPh = (phi / edge) - (double)pI;
+    if (fabs(tTh) < 1.0e-10) tTh = 0.0;
+    if (fabs(tPh) < 1.0e-10) tPh = 0.0;
+    if (pI == phiPoints) pI = 0;
+    const int64_t pI1 = (pI + 1) % phiPoints;
+    Cx<T> nodes[4];
+#pragma unroll
+    for (int i = -1; i < 3; ++i) {
+        int64_t theInd = (thePoints + 1 + tI + i) % (thePoints + 1);
+        int64_t c1, c2;
+        if (theInd == tI + i) {
+            c1 = base + phiPoints * theInd + pI;
+            c2 = base + phiPoints * theInd + pI1;
+        } else {
+            // wrapped theta row: shifted by half a ring (Grid.cpp:95-105)
+            if (tI + i > thePoints) theInd = (tI + i) - (thePoints + 1);
+            c1 = base + phiPoints * theInd + pI;
+            c2 = base + phiPoints * theInd + pI1;
+            c1 += ((2 * pI >= phiPoints) ? -phiPoints : phiPoints) / 2;
+            c2 += ((2 * pI1 >= phiPoints) ? -phiPoints : phiPoints) / 2;
+        }
+        Cx<T> v1, d1, v2, d2;
+        load_cell<T>(g, c1, v1, d1);
+        load_cell<T>(g, c2, v2, d2);
+        nodes[i + 1] = hermite<T>(v1, v2, d1, d2, (T)tPh);
+    }
+    Cx<T> ds1, ds2;
+    four_point<T>(nodes[0], nodes[1], nodes[2], nodes[3], ds1, ds2);
+    return hermite<T>(nodes[1], nodes[2], ds1, ds2, (T)tTh);
+}
+
+__device__ __forceinline__ double bump8(double x) {
+    return __longlong_as_double(__double_as_longlong(x) + 8);
+}
+
+// GetSplineBetweenPlanes (Grid.cpp:551-607) for a known plane index.
+template <typename T>
+__device__ void planes(const typename Vec4<T>::type* __restrict__ g, int Lp, int fInd, double th, double ph,
+                       Cx<T>& pl1, Cx<T>& pl2, Cx<T>& d1, Cx<T>& d2) {
+    Cx<T> origin, od;
+    load_cell<T>(g, 0, origin, od);
+    Cx<T> p1, p2, p3, p4;
+    if (fInd == 0) {
+        double nth = kPi - th;
+        double nph = ph + kPi;
+        if (nph < 0) nph = k2Pi + (nph - (double)(int)(nph / k2Pi) * k2Pi);
+        if (nph >= k2Pi) nph = nph - (double)(int)(nph / k2Pi) * k2Pi;
+        if (nth < 0) nth = 0.;
+        if (nth > kPi) nth = kPi;
+        p1 = interp_plane<T>(g, 1, nth, nph);
+    } else if (fInd == 1) {
+        p1 = origin;
+    } else {
+        p1 = interp_plane<T>(g, fInd - 1, th, ph);
+    }
+    p2 = (fInd > 0) ? interp_plane<T>(g, fInd, th, ph) : origin;
+    p3 = interp_plane<T>(g, fInd + 1, th, ph);
+    p4 = (fInd + 2 < Lp) ? interp_plane<T>(g, fInd + 2, th, ph) : p3;
+    four_point<T>(p1, p2, p3, p4, d1, d2);
+    pl1 = p2;
+    pl2 = p3;
+}
+
+__device__ __forceinline__ void dir_angles(double x, double y, double z, double& th, double& ph) {
+    if (z > 1.0) z = 1.0;
+    if (z < -1.0) z = -1.0;
+    th = acos(z);
+    ph = atan2(y, x);
+    if (ph < 0.0) ph += 2.0 * kPi;
+}
+
+template <typename T> __device__ __forceinline__ Cx<T> expi(double phase);
+template <> __device__ __forceinline__ Cx<double> expi<double>(double phase) {
+    double s, c;
+    sincos(phase, &s, &c);
+    return {c, s};
+}
+template <> __device__ __forceinline__ Cx<float> expi<float>(double phase) {
+    // FP64 reduction of the phase to one turn, FP32 evaluation of the turn.
+    double t = phase * (1.0 / k2Pi);
+    t -= rint(t);
+    float s, c;
+    sincospif((float)(2.0 * t), &s, &c);
+    return {c, s};
+}
+
+// --------------------------------------------------------------------------
+// Orientation average: one block = one chunk of samples of one bracket.
+// Each thread evaluates one direction: for every model and every docked
+// rotation group, the leaf's 4 planes at the rotated direction, then the
+// radial Hermite per q, the leaf phase and the group's translation phases.
+// |A_q|^2 is reduced over the block in FP64 and stored per (bracket, chunk, q).
+// --------------------------------------------------------------------------
+template <typename T, int MQ>
+__global__ void __launch_bounds__(128) average_kernel(int Lp, double step, const ModelDev* __restrict__ models,
+                                                      int n_models, AvgPlan plan) {
+    typedef typename Vec4<T>::type V4;
+    const int b = blockIdx.y;
+    const int64_t chunk = blockIdx.x;
+    const int layer = plan.br_layer[b];
+    const int q0 = plan.br_q_off[b], q1 = plan.br_q_off[b + 1];
+    const int m = q1 - q0;
+    const int64_t s = chunk * plan.chunk - plan.chunk_off + threadIdx.x;
+    const bool valid = (threadIdx.x < plan.chunk) && s >= 0 && s < plan.n_samples;
+
+    __shared__ double red[4][MQ];
+
+    double theta = 0, phi = 0;
+    if (valid) {
+        const double* d = plan.dirs + 2 * ((int64_t)layer * plan.dir_stride + s);
+        theta = d[0];
+        phi = d[1];
+    }
+    const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+    const double dir[3] = {st * cp, st * sp, ct};
+    const int fInd = (m > 0) ? (int)bump8(plan.br_q[q0] / step) : 0;
+
+    for (int qc = 0; qc < m; qc += MQ) {
+        const int mq = min(MQ, m - qc);
+        Cx<T> A[MQ];
+        T frac[MQ];
+        double qv[MQ];
+#pragma unroll
+        for (int k = 0; k < MQ; ++k) {
+            A[k] = {T(0), T(0)};
+            qv[k] = (k < mq) ? plan.br_q[q0 + qc + k] : 0.0;
+            frac[k] = (T)(bump8(qv[k] / step) - (double)fInd);
+        }
+        if (valid) {
+            for (int mi = 0; mi < n_models; ++mi) {
+                const ModelDev& M = models[mi];
+                const V4* g = reinterpret_cast<const V4*>(M.grid);
+                const int ng = M.n_groups > 0 ? M.n_groups : 1;
+                for (int gi = 0; gi < ng; ++gi) {
+                    double n0 = dir[0], n1 = dir[1], n2 = dir[2];
+                    if (M.n_groups > 0) {
+                        const double* Rg = M.group_R + 9 * gi;
+                        double a0 = n0 * Rg[0] + n1 * Rg[3] + n2 * Rg[6];
+                        double a1 = n0 * Rg[1] + n1 * Rg[4] + n2 * Rg[7];
+                        double a2 = n0 * Rg[2] + n1 * Rg[5] + n2 * Rg[8];
+                        const double nr = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+                        n0 = a0 / nr; n1 = a1 / nr; n2 = a2 / nr;
+                    }
+                    // leaf placement (Amplitude.cpp:3553-3579)
+                    const double t0 = n0 * M.R[0] + n1 * M.R[3] + n2 * M.R[6];
+                    const double t1 = n0 * M.R[1] + n1 * M.R[4] + n2 * M.R[7];
+                    const double t2 = n0 * M.R[2] + n1 * M.R[5] + n2 * M.R[8];
+                    const double dotR = t0 * M.tr[0] + t1 * M.tr[1] + t2 * M.tr[2];
+                    double nth, nph;
+                    dir_angles(t0, t1, t2, nth, nph);
+                    Cx<T> pl1, pl2, d1, d2;
+                    planes<T>(g, Lp, fInd, nth, nph, pl1, pl2, d1, d2);
+                    Cx<T> val[MQ];
+#pragma unroll
+                    for (int k = 0; k < MQ; ++k) {
+                        if (k < mq) {
+                            val[k] = hermite<T>(pl1, pl2, d1, d2, frac[k]);
+                            if (dotR != 0.0) val[k] = cmul(val[k], expi<T>(dotR * qv[k]));
+                        }
+                    }
+                    if (M.n_groups > 0) {
+                        Cx<T> tp[MQ];
+#pragma unroll
+                        for (int k = 0; k < MQ; ++k) tp[k] = {T(0), T(0)};
+                        for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
+                            const double* tt = M.trans + 3 * c;
+                            const double a = dir[0] * tt[0] + dir[1] * tt[1] + dir[2] * tt[2];
+#pragma unroll
+                            for (int k = 0; k < MQ; ++k)
+                                if (k < mq) tp[k] = cadd(tp[k], expi<T>(a * qv[k]));
+                        }
+#pragma unroll
+                        for (int k = 0; k < MQ; ++k)
+                            if (k < mq) val[k] = cscale(cmul(val[k], tp[k]), (T)M.sym_scale);
+                    }
+#pragma unroll
+                    for (int k = 0; k < MQ; ++k)
+                        if (k < mq) A[k] = cadd(A[k], val[k]);
+                }
+            }
+        }
+        // |A|^2, block reduction in FP64
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+        for (int k = 0; k < MQ; ++k) {
+            double v = valid ? (double)A[k].r * (double)A[k].r + (double)A[k].i * (double)A[k].i : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp][k] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < mq) {
+            const int k = threadIdx.x;
+            const double v = ((red[0][k] + red[1][k]) + red[2][k]) + red[3][k];
+            plan.partial[((int64_t)b * plan.n_chunks + chunk) * plan.max_q + qc + k] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// Sequential convergence scan per bracket (AverageIntensitiesBetweenLayers,
+// Amplitude.cpp:2773-2815): running sums chunk by chunk; with eps > 0 the
+// reference's 4-column history is tested at every 100th sample.
+__global__ void finalize_kernel(AvgPlan plan, double eps, double* __restrict__ res) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= plan.n_brackets) return;
+    const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
+    const double* part = plan.partial + (int64_t)b * plan.n_chunks * plan.max_q;
+    double* out = plan.partial + ((int64_t)plan.n_brackets * plan.n_chunks) * plan.max_q +
+                  (int64_t)b * plan.max_q * 5;  // scratch: run[max_q] + hist[4][max_q]
+    double* run = out;
+    double* hist = out + plan.max_q;
+    for (int k = 0; k < m; ++k) run[k] = 0.0;
+    for (int64_t c = 0; c < plan.n_chunks; ++c) {
+        for (int k = 0; k < m; ++k) run[k] += part[c * plan.max_q + k];
+        if (eps > 0.0) {
+            const int64_t i = c * plan.chunk - plan.chunk_off + plan.chunk - 1;  // last sample of chunk
+            if (i >= plan.n_samples) break;
+            const int pos = (int)(c % 4);
+            for (int k = 0; k < m; ++k) hist[pos * plan.max_q + k] = run[k] / (double)(i + 1);
+            if (i >= 400) {
+                bool conv = true;
+                for (int j = 0; conv && j < 4; ++j)
+                    for (int k = 0; k < m; ++k)
+                        if (!(fabs(1.0 - hist[j * plan.max_q + k] / hist[k]) < eps)) { conv = false; break; }
+                if (conv) {
+                    for (int k = 0; k < m; ++k) res[plan.br_qidx[q0 + k]] = hist[pos * plan.max_q + k];
+                    return;
+                }
+            }
+        }
+    }
+    for (int k = 0; k < m; ++k) res[plan.br_qidx[q0 + k]] = run[k] / (double)plan.n_samples;
+}
+
+template <typename V4>
+__global__ void pack_values_kernel(const V4* __restrict__ g, int64_t P, double* __restrict__ out, int which) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const V4 x = g[i];
+    out[2 * i] = which ? (double)x.z : (double)x.x;
+    out[2 * i + 1] = which ? (double)x.w : (double)x.y;
+}
+
+template <typename V4, typename T>
+__global__ void unpack_kernel(const double* __restrict__ vals, const double* __restrict__ ders, int64_t P,
+                              V4* __restrict__ g) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    V4 x;
+    x.x = (T)vals[2 * i];
+    x.y = (T)vals[2 * i + 1];
+    x.z = ders ? (T)ders[2 * i] : T(0);
+    x.w = ders ? (T)ders[2 * i + 1] : T(0);
+    g[i] = x;
+}
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
+                            const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,
+                            int block, int64_t cell_lo, int64_t cell_hi) {
+    const int64_t n = cell_hi - cell_lo;
+    if (n <= 0) return cudaSuccess;
+    const int use_center = (center[0] != 0.0 || center[1] != 0.0 || center[2] != 0.0);
+#define DPX_FILL_CASE(CPT, TH)                                                                                   \
+    if (cells_per_thread == CPT && block == TH) {                                                              \
+        fill_f32_kernel<CPT, TH><<<blocks_for(n, CPT * TH), TH, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step,  \
+                                                                       center[0], center[1], center[2],        \
+                                                                       use_center, scale, grid, cell_lo,       \
+                                                                       cell_hi);                               \
+        return cudaGetLastError();                                                                             \
+    }
+    DPX_FILL_CASE(1, 128) DPX_FILL_CASE(2, 128) DPX_FILL_CASE(4, 128) DPX_FILL_CASE(8, 128)
+    DPX_FILL_CASE(1, 256) DPX_FILL_CASE(2, 256) DPX_FILL_CASE(4, 256) DPX_FILL_CASE(8, 256)
+    DPX_FILL_CASE(2, 512) DPX_FILL_CASE(4, 512)
+#undef DPX_FILL_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
+                            const Geom& g, double scale, double4_32a* grid, int64_t cell_lo, int64_t cell_hi) {
+    const int64_t n = cell_hi - cell_lo;
+    if (n <= 0) return cudaSuccess;
+    fill_f64_kernel<128><<<blocks_for(n, 128), 128, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step, scale, grid,
+                                                           cell_lo, cell_hi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid) {
+    splines_kernel<float, 14><<<blocks_for(g.P, 256), 256, 0, s>>>(grid, g.P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid) {
+    splines_kernel<double, 32><<<blocks_for(g.P, 256), 256, 0, s>>>(grid, g.P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                           const AvgPlan& plan) {
+    if (plan.n_brackets == 0 || plan.n_chunks == 0) return cudaSuccess;
+    if (plan.n_chunks > 0x7fffffff || plan.n_brackets > 65535) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)plan.n_chunks, (unsigned)plan.n_brackets);
+    if (fp64) average_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, g.step, d_models, n_models, plan);
+    else average_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, g.step, d_models, n_models, plan);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res) {
+    finalize_kernel<<<blocks_for(plan.n_brackets, 64), 64, 0, s>>>(plan, eps, d_res);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_values_f32(cudaStream_t s, const float4* grid, int64_t P, double* out) {
+    pack_values_kernel<float4><<<blocks_for(P, 256), 256, 0, s>>>(grid, P, out, 0);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack_values_f64(cudaStream_t s, const double4_32a* grid, int64_t P, double* out) {
+    pack_values_kernel<double4_32a><<<blocks_for(P, 256), 256, 0, s>>>(grid, P, out, 0);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack_ders_f32(cudaStream_t s, const float4* grid, int64_t P, double* out) {
+    pack_values_kernel<float4><<<blocks_for(P, 256), 256, 0, s>>>(grid, P, out, 1);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack_ders_f64(cudaStream_t s, const double4_32a* grid, int64_t P, double* out) {
+    pack_values_kernel<double4_32a><<<blocks_for(P, 256), 256, 0, s>>>(grid, P, out, 1);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack_f64(cudaStream_t s, const double* vals, const double* ders, int64_t P, double4_32a* grid) {
+    unpack_kernel<double4_32a, double><<<blocks_for(P, 256), 256, 0, s>>>(vals, ders, P, grid);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack_f32(cudaStream_t s, const double* vals, const double* ders, int64_t P, float4* grid) {
+    unpack_kernel<float4, float><<<blocks_for(P, 256), 256, 0, s>>>(vals, ders, P, grid);
+    return cudaGetLastError();
+}
+
+}  // namespace dpx

@@ -1,0 +1,103 @@
+"""ctypes binding of libdpx.so (the C-ABI declared in include/dpx.h).
+
+The library is the only compute path: if it is missing, every entry point
+raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from ._build import LIB_PATH
+
+_lib = None
+
+DPX_OK = 0
+DPX_FP64 = 0
+DPX_FP32 = 1
+DPX_CALC_ATOMIC_FORMFACTORS = 1
+DPX_CALC_DUMMY_SOLVENT = 2
+
+_STATUS = {-1: "DPX_ERR_ARG", -2: "DPX_ERR_CUDA", -3: "DPX_ERR_OOM", -4: "DPX_ERR_STOPPED",
+           -5: "DPX_ERR_NODEVICE"}
+
+
+class DpxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int)
+_U32 = C.POINTER(C.c_uint32)
+
+_SIGS = {
+    "dpx_last_error": (C.c_char_p, []),
+    "dpx_version": (C.c_int, []),
+    "dpx_ctx_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
+    "dpx_ctx_destroy": (C.c_int, [_P]),
+    "dpx_ctx_set_stream": (C.c_int, [_P, _P]),
+    "dpx_ctx_get_stream": (_P, [_P]),
+    "dpx_ctx_synchronize": (C.c_int, [_P]),
+    "dpx_ctx_set_fill_shape": (C.c_int, [_P, C.c_int, C.c_int]),
+    "dpx_grid_cells": (C.c_int64, [C.c_int]),
+    "dpx_grid_bytes": (C.c_int64, [C.c_int, C.c_int]),
+    "dpx_grid_create": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.POINTER(_P)]),
+    "dpx_grid_destroy": (C.c_int, [_P]),
+    "dpx_grid_device_ptr": (_P, [_P]),
+    "dpx_grid_info": (C.c_int, [_P, _I, _D, _I, C.POINTER(C.c_int64)]),
+    "dpx_grid_fill_pdb": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, _I, _D, _D, C.c_int, C.c_double,
+                                    C.c_double, C.c_double, _D]),
+    "dpx_grid_compute_splines": (C.c_int, [_P]),
+    "dpx_grid_read": (C.c_int, [_P, _D, _D]),
+    "dpx_grid_write": (C.c_int, [_P, _D, _D]),
+    "dpx_orientation_average": (C.c_int, [_P, C.c_int, C.POINTER(_P), _D, _D, _I, _D, _D, _D, C.c_int, _D, _P,
+                                          C.c_int, C.c_int64, C.c_int64, C.c_double, _D]),
+    "dpx_mc_directions": (C.c_int, [C.c_uint32, C.c_int64, _D]),
+    "dpx_layer_seeds": (C.c_int, [C.c_uint32, C.c_int, C.c_int, _U32]),
+    "dpx_q_brackets": (C.c_int, [C.c_int, C.c_double, C.c_int, _D, _I]),
+    "dpx_make_globule": (C.c_int, [C.c_int64, C.c_double, C.c_uint64, _F, _I]),
+    "dpx_pdb_jacobian_grid_amplitude": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.c_double, _D, _F, C.c_int64,
+                                                  C.c_int, _I, _F, _F, C.c_int, C.c_float, C.c_float, C.c_double,
+                                                  C.c_int, _I]),
+    "dpx_calc_mcoa_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, C.c_int,
+                                           C.c_int64, C.c_double, _D, C.c_int64, C.c_int, _I]),
+}
+
+EXPORTED = sorted(_SIGS)
+
+
+def lib() -> C.CDLL:
+    """Load libdpx.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libdpx.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != DPX_OK:
+        raise DpxError(rc, lib().dpx_last_error().decode(errors="replace"))
+
+
+def dptr(a):
+    """double* of a contiguous float64 numpy array (or None)."""
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def fptr(a):
+    return None if a is None else a.ctypes.data_as(_F)
+
+
+def iptr(a):
+    return None if a is None else a.ctypes.data_as(_I)

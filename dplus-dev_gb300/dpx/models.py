@@ -1,0 +1,289 @@
+"""Host-side mirror of D+'s operator interface for the scattering hot path.
+
+The classes keep the reference's names and argument meaning so that a caller
+of D+'s backend finds the same operations:
+
+* ``PDBAmplitude``  — PDBAmplitude::PreCalculate / calculateGrid
+  (Backend/Backend/PDBAmplitude.cpp:1199-1336, 319-435)
+* ``ManualSymmetry`` — explicit docked copies (Backend/DefaultModels/Symmetries.cpp:670-716, 1079-1166)
+* ``DomainModel``   — DomainModel::CalculateIntensityVector with the Monte Carlo
+  orientation average between layers (Backend/Backend/Amplitude.cpp:701-842, 1168-1247, 2746-2822)
+
+All arithmetic runs in libdpx on the GPU; nothing here computes amplitudes or
+intensities.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import math
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, iptr, lib
+from .elements import ion
+
+# radius types (Common/Common.h:371-378)
+RAD_UNINITIALIZED, RAD_VDW, RAD_EMP, RAD_CALC, RAD_DUMMY_ATOMS_ONLY, RAD_DUMMY_ATOMS_RADII = range(6)
+
+FP64 = _lib.DPX_FP64
+FP32 = _lib.DPX_FP32
+
+
+class Context:
+    """One device + one stream + the library's grow-only device scratch."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().dpx_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(lib().dpx_ctx_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    def set_fill_shape(self, cells_per_thread: int, threads: int) -> None:
+        check(lib().dpx_ctx_set_fill_shape(self.handle, cells_per_thread, threads))
+
+    def synchronize(self) -> None:
+        check(lib().dpx_ctx_synchronize(self.handle))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().dpx_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Grid:
+    """Device-resident JacobianSphereGrid (values + phi-spline derivatives)."""
+
+    def __init__(self, ctx: Context, grid_size: int, qmax: float, precision: int = FP32):
+        h = C.c_void_p()
+        check(lib().dpx_grid_create(ctx.handle, grid_size, float(qmax), precision, C.byref(h)))
+        self.handle = h
+        self.ctx = ctx
+        self.grid_size = grid_size
+        self.qmax = float(qmax)
+        self.precision = precision
+        self.cells = lib().dpx_grid_cells(grid_size)
+
+    @property
+    def device_ptr(self) -> int:
+        return lib().dpx_grid_device_ptr(self.handle)
+
+    def compute_splines(self) -> None:
+        check(lib().dpx_grid_compute_splines(self.handle))
+
+    def read(self, values: bool = True, coeffs: bool = True):
+        v = np.empty(2 * self.cells) if values else None
+        d = np.empty(2 * self.cells) if coeffs else None
+        check(lib().dpx_grid_read(self.handle, dptr(v), dptr(d)))
+        return v, d
+
+    def write(self, values: np.ndarray, coeffs: np.ndarray | None = None) -> None:
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        coeffs = None if coeffs is None else np.ascontiguousarray(coeffs, dtype=np.float64)
+        check(lib().dpx_grid_write(self.handle, dptr(values), dptr(coeffs)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().dpx_grid_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def euler_deg_to_rad(a, b, g):
+    return (math.radians(a), math.radians(b), math.radians(g))
+
+
+class PDBAmplitude:
+    """A PDB leaf: atoms, form factors and Gaussian dummy-atom solvent.
+
+    ``extra`` follows D+'s 10 PDB ExtraParameters (PDBAmplitude.cpp:1205-1214):
+    [scale, solventED, c1, voxelStep, solventRad, solvationThickness,
+    outerSolventED, fillHoles, solventOnly, radType].
+    """
+
+    def __init__(self, symbols: Sequence[str], xyz_nm: np.ndarray, extra: Sequence[float] | None = None,
+                 centered: bool = False, location: Sequence[float] = (0, 0, 0, 0, 0, 0)):
+        xyz = np.asarray(xyz_nm, dtype=np.float64).reshape(-1, 3)
+        if len(symbols) != len(xyz):
+            raise ValueError("symbols and coordinates differ in length")
+        if len(xyz) == 0:
+            raise ValueError("a PDB leaf needs at least one atom")
+        ions = [ion(s) for s in symbols]
+        # coordinates are stored as float, as the reference does (PDBAmplitude.h:15)
+        xyz = xyz.astype(np.float32).astype(np.float64)
+        if centered:  # moveCOMToOrigin (PDBReaderLib.cpp:271-293)
+            w = np.array([i.weight for i in ions])
+            com = (xyz * w[:, None]).sum(0) / w.sum()
+            xyz = (xyz - com).astype(np.float32).astype(np.float64)
+        order = sorted(range(len(ions)), key=lambda k: ions[k].ion_key)  # stable, as std::sort by ion index
+        self.symbols = [ions[k].symbol for k in order]
+        self.xyz = xyz[order]
+        keys = [ions[k].ion_key for k in order]
+        uniq, self.atoms_per_ion = [], []
+        for k, s in zip(keys, self.symbols):
+            if not uniq or uniq[-1][0] != k:
+                uniq.append((k, s))
+                self.atoms_per_ion.append(0)
+            self.atoms_per_ion[-1] += 1
+        self.unique = [ion(s) for _, s in uniq]
+        self.atoms_per_ion = np.array(self.atoms_per_ion, dtype=np.int32)
+        U = len(self.unique)
+        self.coeffs = np.zeros(9 * U)
+        for u, io in enumerate(self.unique):
+            for k in range(9):
+                self.coeffs[u + k * U] = io.coeffs[k]
+        self.ion_rads = np.array([io.dummy_radius for io in self.unique])
+        self.location = tuple(float(v) for v in location)  # x, y, z (nm), alpha, beta, gamma (radians)
+        self.set_extra(extra if extra is not None else [1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0])
+        self._grid = None
+        self._grid_key = None
+
+    def set_extra(self, p: Sequence[float]) -> None:
+        """PreCalculate's parameter unpacking and flag logic (PDBAmplitude.cpp:1205-1272)."""
+        p = list(p) + [0] * (10 - len(p))
+        self.scale, self.solventED, self.c1 = float(p[0]), float(p[1]), float(p[2])
+        self.voxelStep, self.solventRad, self.solvationThickness = float(p[3]), float(p[4]), float(p[5])
+        self.outerSolventED = float(p[6])
+        self.fillHoles = abs(p[7] - 1.0) < 1e-6
+        self.solventOnly = abs(p[8] - 1.0) < 1e-6
+        self.radType = int(p[9] + 0.1)
+        flags = 0
+        if not self.solventOnly:
+            flags |= _lib.DPX_CALC_ATOMIC_FORMFACTORS
+        if self.radType == RAD_DUMMY_ATOMS_ONLY and self.solventED != 0.0:
+            flags |= _lib.DPX_CALC_DUMMY_SOLVENT
+        voxel = ((self.solventED != 0.0 and self.radType in (RAD_CALC, RAD_EMP, RAD_DUMMY_ATOMS_RADII, RAD_VDW))
+                 or (self.outerSolventED != 0.0 and self.radType in (RAD_CALC, RAD_EMP, RAD_DUMMY_ATOMS_RADII,
+                                                                      RAD_VDW, RAD_DUMMY_ATOMS_ONLY)))
+        if voxel:
+            raise NotImplementedError("voxelized solvent / solvation layer is not available in this build")
+        self.flags = flags
+
+    def atoms_float4(self) -> np.ndarray:
+        a = np.zeros((len(self.xyz), 4), dtype=np.float32)
+        a[:, :3] = self.xyz
+        return a
+
+    def hash(self) -> str:
+        h = hashlib.sha1()
+        for arr in (self.xyz, self.coeffs, self.ion_rads, self.atoms_per_ion):
+            h.update(np.ascontiguousarray(arr).tobytes())
+        h.update(repr((self.scale, self.solventED, self.c1, self.flags)).encode())
+        return h.hexdigest()
+
+    def calculateGrid(self, ctx: Context, qmax: float, gridSize: int, precision: int = FP32) -> Grid:
+        """Fill (or reuse) the device-resident amplitude grid and its splines."""
+        key = (self.hash(), int(gridSize), float(qmax), int(precision), ctx.device)
+        if self._grid is not None and self._grid_key == key:
+            return self._grid
+        g = Grid(ctx, gridSize, qmax, precision)
+        a = self.atoms_float4()
+        check(lib().dpx_grid_fill_pdb(g.handle, len(a), a.ctypes.data_as(C.c_void_p), 0, len(self.unique),
+                                      iptr(self.atoms_per_ion), dptr(self.coeffs), dptr(self.ion_rads), self.flags,
+                                      self.solventED, self.c1, self.scale, None))
+        g.compute_splines()
+        self._grid, self._grid_key = g, key
+        return g
+
+
+class ManualSymmetry:
+    """Docked copies of one child: rows (x, y, z [nm], alpha, beta, gamma [degrees]),
+    as ManualSymmetry::PreCalculate reads them (Symmetries.cpp:670-695)."""
+
+    def __init__(self, child: PDBAmplitude, rows: Sequence[Sequence[float]], scale: float = 1.0):
+        r = np.asarray(rows, dtype=np.float64).reshape(-1, 6)
+        self.child = child
+        self.trans = np.ascontiguousarray(r[:, :3])
+        self.rot = np.ascontiguousarray(np.radians(r[:, 3:6]))
+        self.scale = float(scale)
+
+
+class DomainModel:
+    """DomainModel::CalculateIntensityVector for leaves on grids with the Monte
+    Carlo orientation average between layers."""
+
+    def __init__(self, amps: Sequence, gridSize: int, qMax: float, precision: int = FP32):
+        self.amps = list(amps)
+        self.gridSize = int(gridSize)
+        self.qMax = float(qMax)
+        self.precision = precision
+
+    def grids(self, ctx: Context):
+        out = []
+        for a in self.amps:
+            leaf = a.child if isinstance(a, ManualSymmetry) else a
+            out.append(leaf.calculateGrid(ctx, self.qMax, self.gridSize, self.precision))
+        return out
+
+    def CalculateIntensityVector(self, ctx: Context, Q: Sequence[float], epsi: float, iterations: int,
+                                 dirs: np.ndarray, dir_layer_stride: int = 0) -> np.ndarray:
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        grids = self.grids(ctx)
+        n = len(self.amps)
+        rot = np.zeros(3 * n)
+        tr = np.zeros(3 * n)
+        ncop = np.zeros(n, dtype=np.int32)
+        crot, ctr, sscale = [], [], np.ones(n)
+        for m, a in enumerate(self.amps):
+            leaf = a.child if isinstance(a, ManualSymmetry) else a
+            tr[3 * m:3 * m + 3] = leaf.location[:3]
+            rot[3 * m:3 * m + 3] = leaf.location[3:]
+            if isinstance(a, ManualSymmetry):
+                ncop[m] = len(a.trans)
+                crot.append(a.rot.ravel())
+                ctr.append(a.trans.ravel())
+                sscale[m] = a.scale
+        crot = np.ascontiguousarray(np.concatenate(crot) if crot else np.zeros(3))
+        ctr = np.ascontiguousarray(np.concatenate(ctr) if ctr else np.zeros(3))
+        gh = (C.c_void_p * n)(*[g.handle.value for g in grids])
+        res = np.zeros(len(Q))
+        d = np.ascontiguousarray(dirs, dtype=np.float64)
+        check(lib().dpx_orientation_average(ctx.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
+                                            dptr(sscale), len(Q), dptr(Q), d.ctypes.data_as(C.c_void_p), 0,
+                                            dir_layer_stride, iterations, epsi, dptr(res)))
+        return res
+
+
+# ---- seeded inputs -------------------------------------------------------
+
+def mc_directions(seed: int, D: int) -> np.ndarray:
+    """(theta, phi) pairs of the reference's mt19937 draw order."""
+    out = np.empty((D, 2))
+    check(lib().dpx_mc_directions(seed & 0xFFFFFFFF, D, dptr(out)))
+    return out
+
+
+def layer_seeds(master: int, nq: int, n_layers: int) -> np.ndarray:
+    out = np.empty(n_layers + 1, dtype=np.uint32)
+    check(lib().dpx_layer_seeds(master & 0xFFFFFFFF, nq, n_layers, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return out
+
+
+def layer_directions(master: int, nq: int, n_layers: int, D: int) -> np.ndarray:
+    """Per-layer direction streams [n_layers, D, 2] as IntegrateLayersTogether draws them."""
+    seeds = layer_seeds(master, nq, n_layers)
+    return np.stack([mc_directions(int(seeds[l]), D) for l in range(n_layers)])
+
+
+def make_globule(n_atoms: int, radius_nm: float, seed: int):
+    xyz = np.empty((n_atoms, 3), dtype=np.float32)
+    el = np.empty(n_atoms, dtype=np.int32)
+    check(lib().dpx_make_globule(n_atoms, radius_nm, seed, xyz.ctypes.data_as(C.POINTER(C.c_float)), iptr(el)))
+    from .elements import GLOBULE_CODES
+    return [GLOBULE_CODES[e] for e in el], xyz.astype(np.float64)

@@ -1,0 +1,148 @@
+/*
+ * dpx.h — C-ABI of the GB300-native D+ scattering hot path (libdpx.so).
+ *
+ * Plain pointers, sizes and status codes; no C++ or torch types cross this
+ * boundary, and no entry point throws, traps or falls back to the CPU.  Every
+ * entry point returns DPX_OK (0) or a negative dpx_status; the message of the
+ * last failure on the calling thread is dpx_last_error().
+ *
+ * Reference interfaces replaced (uri-raviv-lab/dplus-dev):
+ *   dpx_pdb_jacobian_grid_amplitude  <- PDBJacobianGridAmplitudeCalculation
+ *                                       (Backend/Backend/PDBAmplitudeCUDA.h:7-13,
+ *                                        impl PDBAmplitudeCUDA.cu:442-458)
+ *   dpx_calc_mcoa_jacob_sphr         <- GPUCalcMCOAJacobSphrDD
+ *                                       (Backend/GPU/GPUHeader.h:236, OAJacob.cu:387-399)
+ *   dpx_grid_compute_splines         <- JacobianSphereGrid::CalculateSplines
+ *                                       (Backend/Backend/Grid.cpp:1113-1151)
+ *   dpx_grid_fill_pdb                <- PDBAmplitude::calculateGrid GPU branch
+ *                                       (Backend/Backend/PDBAmplitude.cpp:319-435)
+ *   dpx_orientation_average          <- DomainModel::IntegrateLayersTogether /
+ *                                       AverageIntensitiesBetweenLayers
+ *                                       (Backend/Backend/Amplitude.cpp:1168-1247, 2746-2822)
+ *                                       and the hybrid ManualSymmetry docked sum
+ *                                       (Backend/DefaultModels/Symmetries.cpp:1079-1166,
+ *                                        GPUHybridCalc.cu:467-578)
+ *   dpx_mc_directions / dpx_layer_seeds <- the mt19937 draws of
+ *                                       Amplitude.cpp:757-767, 1171-1173, 2764-2780
+ */
+#ifndef DPX_H
+#define DPX_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum dpx_status {
+    DPX_OK = 0,
+    DPX_ERR_ARG = -1,       /* invalid argument / inconsistent sizes */
+    DPX_ERR_CUDA = -2,      /* CUDA runtime error (message in dpx_last_error) */
+    DPX_ERR_OOM = -3,       /* device allocation failed */
+    DPX_ERR_STOPPED = -4,   /* *pStop was set by the caller */
+    DPX_ERR_NODEVICE = -5   /* no CUDA device */
+} dpx_status;
+
+typedef enum dpx_precision {
+    DPX_FP64 = 0,   /* plain FP64: FP64 phases, sincos, accumulation, FP64 grid */
+    DPX_FP32 = 1    /* FP32 bulk: FP32 phases/SFU sincos/accumulation, FP32 grid,
+                       FP64 centring and translation phases, FP64 reductions */
+} dpx_precision;
+
+/* form-factor flags (same bits as the reference's atomicFormDefines.h:5-9) */
+#define DPX_CALC_ATOMIC_FORMFACTORS 1
+#define DPX_CALC_DUMMY_SOLVENT 2
+
+typedef struct dpx_ctx_s* dpx_ctx;
+typedef struct dpx_grid_s* dpx_grid;
+
+const char* dpx_last_error(void);
+int dpx_version(void);
+
+/* ---- context: one device, one stream, grow-only device scratch ---- */
+int dpx_ctx_create(int device, dpx_ctx* out);
+int dpx_ctx_destroy(dpx_ctx ctx);
+/* Use an external cudaStream_t (NULL = the context's own stream). */
+int dpx_ctx_set_stream(dpx_ctx ctx, void* stream);
+void* dpx_ctx_get_stream(dpx_ctx ctx);
+int dpx_ctx_synchronize(dpx_ctx ctx);
+/* Amplitude-kernel launch shape (cells per thread x threads per block);
+ * chosen by the autotuner, defaults 4 x 256. */
+int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cells_per_thread, int threads);
+
+/* ---- grid geometry (Grid.cpp:169-200): P = 6 L'(L'+1)^2 + 1, L' = grid_size/2 + 3 ---- */
+int64_t dpx_grid_cells(int grid_size);
+int64_t dpx_grid_bytes(int grid_size, int precision);
+
+/* ---- device-resident JacobianSphereGrid (values + phi-spline derivatives) ---- */
+int dpx_grid_create(dpx_ctx ctx, int grid_size, double qmax, int precision, dpx_grid* out);
+int dpx_grid_destroy(dpx_grid g);
+void* dpx_grid_device_ptr(dpx_grid g);     /* float4 / double4 {re, im, dre, dim} per cell */
+int dpx_grid_info(dpx_grid g, int* grid_size, double* qmax, int* precision, int64_t* cells);
+
+/* Amplitude of a PDB leaf on every cell (atoms + Gaussian dummy-atom solvent):
+ *   F(q) = scale * sum_u aff_u(|q|) sum_{j in u} e^{i q.r_j}
+ * atoms: float4 (x, y, z, ignored) in nm, sorted by ion; host or device memory.
+ * coeffs: [9 x n_ions], coeffs[u + k*n_ions] = (a1,b1,a2,b2,a3,b3,a4,b4,c)[k]
+ * (the reference's sortedCoeffs layout); ion_rads: [n_ions] dummy-atom radii (nm).
+ * center: optional [3] translation restored as a per-cell phase (NULL: the host
+ * atoms' centroid is used, or 0 for device atoms). */
+int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms_on_device, int n_ions,
+                      const int* atoms_per_ion, const double* coeffs, const double* ion_rads, int flags,
+                      double solvent_ed, double c1, double scale, const double* center);
+/* Periodic cubic-spline phi derivatives of every theta row. */
+int dpx_grid_compute_splines(dpx_grid g);
+/* Host copies in the reference's layout: interleaved complex double [2P] each;
+ * either pointer may be NULL. */
+int dpx_grid_read(dpx_grid g, double* values, double* coeffs);
+int dpx_grid_write(dpx_grid g, const double* values, const double* coeffs);
+
+/* ---- orientation average ----
+ * A model is a leaf grid placed by Euler angles rot[3] (radians, Tait-Bryan
+ * X1Y2Z3 as EulerD) and a translation tr[3] (nm), optionally docked n_copies
+ * times (ManualSymmetry rows: copy_rot[3 n] radians, copy_tr[3 n] nm, scale
+ * sym_scale).  All models share grid_size and qmax.
+ * Q: [nq] ascending q (nm^-1).  Directions: (theta, phi) pairs; layer l uses
+ * dirs + 2*l*dir_layer_stride (0 = one shared set); dirs_on_device selects
+ * host or device memory.  n_samples per bracket; eps > 0 applies the
+ * reference's convergence test every 100 samples.  res: [nq] host. */
+int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot,
+                            const double* tr, const int* n_copies, const double* copy_rot,
+                            const double* copy_tr, const double* sym_scale, int nq, const double* Q,
+                            const double* dirs, int dirs_on_device, int64_t dir_layer_stride,
+                            int64_t n_samples, double eps, double* res);
+
+/* ---- seeded direction streams (product-side restatement of the reference's draws) ---- */
+/* D pairs (theta, phi) from std::mt19937(seed) with u2, v2 ~ U[0,2): phi = pi u2, theta = acos(v2 - 1) */
+int dpx_mc_directions(uint32_t seed, int64_t D, double* theta_phi);
+/* Per-layer seeds derived from a master seed the way CalculateIntensityVector
+ * and IntegrateLayersTogether draw them (nq draws discarded, then n_layers+1). */
+int dpx_layer_seeds(uint32_t master, int nq, int n_layers, uint32_t* seeds);
+/* Which layer's bracket computes each q (-1 for q == 0), as IntegrateLayersTogether. */
+int dpx_q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q);
+
+/* ---- synthetic structures ----
+ * Seeded self-avoiding random walk (0.15 nm steps) folded into a sphere of
+ * radius_nm; elements drawn C 63 % / N 17 % / O 19 % / S 1 % (codes 0..3). */
+int dpx_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xyz, int* elem);
+
+/* ---- drop-in replacements with the reference's argument meaning ---- */
+/* PDBJacobianGridAmplitudeCalculation: outData is a caller-owned host buffer of
+ * 2*voxels doubles in grid-index order; splines are left to the caller, as in
+ * the reference.  Returns 0 or a negative status (the reference returns
+ * -3000-err / -1000-err; callers test != 0). */
+int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
+                                    const float* atomLocations, int64_t numAtoms, int numUniqueIons,
+                                    const int* atomsPerIon, const float* coeffs, const float* ionRads,
+                                    int bitCombination, float solventED, float c1, double scale, int precision,
+                                    int* pStop);
+/* GPUCalcMCOAJacobSphrDD with explicit directions: inAmp / inD are the grid's
+ * values and spline derivatives [2 voxels]; intensities [qPoints]. */
+int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* inAmp,
+                             const double* inD, const double* qs, double* intensities, int qPoints,
+                             int64_t maxIters, double convergence, const double* dirs, int64_t dir_layer_stride,
+                             int precision, int* pStop);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
