@@ -333,12 +333,12 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
             for (int k = 0; k < 3; ++k) acc[k] += atoms[4 * j + k];
         for (int k = 0; k < 3; ++k) cen[k] = acc[k] / double(n_atoms);
     }
-    if (g->precision == DPX_FP64) cen[0] = cen[1] = cen[2] = 0.0;  // exact FP64 phases need no centring
-    const bool shift = (cen[0] != 0.0 || cen[1] != 0.0 || cen[2] != 0.0);
+    if (g->precision == DPX_FP64 && !atoms_on_device) cen[0] = cen[1] = cen[2] = 0.0;  // FP64 phases need no centring
 
+    // host atoms are shifted by the centre here; device atoms are taken as
+    // already shifted by the caller (r_device = r - center)
     const float4* d_atoms = reinterpret_cast<const float4*>(atoms);
-    if (!atoms_on_device || shift) {
-        if (atoms_on_device) return fail(DPX_ERR_ARG, "an explicit centre needs host atoms");
+    if (!atoms_on_device) {
         DPX_CUDA(ctx->atoms.reserve((size_t)n_atoms * sizeof(float4)));
         ctx->host_stage.resize((size_t)n_atoms * sizeof(float4));
         float4* h = reinterpret_cast<float4*>(ctx->host_stage.data());
@@ -368,8 +368,8 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
 
     cudaError_t e;
     if (g->precision == DPX_FP64)
-        e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, scale,
-                                 (double4_32a*)g->cells, 0, G.P);
+        e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, cen,
+                                 scale, (double4_32a*)g->cells, 0, G.P);
     else
         e = dpx::launch_fill_f32(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const float*)ctx->table.p, G, cen,
                                  (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads, 0, G.P);

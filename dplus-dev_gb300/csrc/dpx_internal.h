@@ -62,7 +62,7 @@ cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_
                             const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,
                             int block, int64_t cell_lo, int64_t cell_hi);
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
-                            const Geom& g, double scale, double4_32a* grid, int64_t cell_lo, int64_t cell_hi);
+                            const Geom& g, const double center[3], double scale, double4_32a* grid, int64_t cell_lo, int64_t cell_hi);
 cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid);
 cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid);
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,

@@ -154,8 +154,9 @@ template <int THREADS>
 __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restrict__ atoms,
                                                            const int* __restrict__ ion_off, int U,
                                                            const double* __restrict__ aff, int Lp, double step,
-                                                           double scale, double4_32a* __restrict__ grid,
-                                                           int64_t cell_lo, int64_t cell_hi) {
+                                                           double cx, double cy, double cz, double scale,
+                                                           double4_32a* __restrict__ grid, int64_t cell_lo,
+                                                           int64_t cell_hi) {
     __shared__ double4_32a s_atoms[THREADS];
     const int64_t cell = cell_lo + (int64_t)blockIdx.x * THREADS + threadIdx.x;
     int qi, ti, pi;
@@ -197,7 +198,15 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
         accR += f * sR;
         accI += f * sI;
     }
-    if (cell < cell_hi) reinterpret_cast<double2*>(grid + cell)[0] = make_double2(accR * scale, accI * scale);
+    double re = accR * scale, im = accI * scale;
+    if (cx != 0.0 || cy != 0.0 || cz != 0.0) {
+        double sn, cs;
+        sincos(qx * cx + qy * cy + qz * cz, &sn, &cs);
+        const double r2 = re * cs - im * sn, i2 = re * sn + im * cs;
+        re = r2;
+        im = i2;
+    }
+    if (cell < cell_hi) reinterpret_cast<double2*>(grid + cell)[0] = make_double2(re, im);
 }
 
 // --------------------------------------------------------------------------
@@ -315,13 +324,19 @@ __device__ Cx<T> interp_plane(const typename Vec4<T>::type* __restrict__ g, int 
     const int64_t base = shell_base(ri);
     const int64_t phiPoints = 6 * (int64_t)ri, thePoints = 3 * (int64_t)ri;
     const double edge = k2Pi / (double)phiPoints;
+    // angles outside [0, pi] x [0, 2 pi] (or NaN) are clamped so that every
+    // node index below stays inside shell ri
+    if (!(theta >= 0.0)) theta = 0.0;
+    if (theta > kPi) theta = kPi;
+    if (!(phi >= 0.0)) phi = 0.0;
+    if (phi > k2Pi) phi = k2Pi;
     const int64_t tI = (int64_t)((theta / kPi) * (double)thePoints);
     int64_t pI = (int64_t)((phi / k2Pi) * (double)phiPoints);
     double tTh = (theta / edge) - (double)tI;
     double tPh = (phi / edge) - (double)pI;
     if (fabs(tTh) < 1.0e-10) tTh = 0.0;
     if (fabs(tPh) < 1.0e-10) tPh = 0.0;
-    if (pI == phiPoints) pI = 0;
+    if (pI >= phiPoints) pI = 0;
     const int64_t pI1 = (pI + 1) % phiPoints;
     Cx<T> nodes[4];
 #pragma unroll
@@ -602,11 +617,12 @@ cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_
 }
 
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
-                            const Geom& g, double scale, double4_32a* grid, int64_t cell_lo, int64_t cell_hi) {
+                            const Geom& g, const double center[3], double scale, double4_32a* grid, int64_t cell_lo,
+                            int64_t cell_hi) {
     const int64_t n = cell_hi - cell_lo;
     if (n <= 0) return cudaSuccess;
-    fill_f64_kernel<128><<<blocks_for(n, 128), 128, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step, scale, grid,
-                                                           cell_lo, cell_hi);
+    fill_f64_kernel<128><<<blocks_for(n, 128), 128, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step, center[0],
+                                                           center[1], center[2], scale, grid, cell_lo, cell_hi);
     return cudaGetLastError();
 }
 

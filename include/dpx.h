@@ -84,8 +84,10 @@ int dpx_grid_info(dpx_grid g, int* grid_size, double* qmax, int* precision, int6
  * atoms: float4 (x, y, z, ignored) in nm, sorted by ion; host or device memory.
  * coeffs: [9 x n_ions], coeffs[u + k*n_ions] = (a1,b1,a2,b2,a3,b3,a4,b4,c)[k]
  * (the reference's sortedCoeffs layout); ion_rads: [n_ions] dummy-atom radii (nm).
- * center: optional [3] translation restored as a per-cell phase (NULL: the host
- * atoms' centroid is used, or 0 for device atoms). */
+ * center: optional [3] centring translation c restored as a per-cell phase
+ * e^{i q.c}.  Host atoms are shifted by c here (NULL: their centroid for FP32
+ * grids, 0 for FP64 grids); device atoms are taken as already shifted by the
+ * caller (r_device = r - c; NULL: c = 0). */
 int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms_on_device, int n_ions,
                       const int* atoms_per_ion, const double* coeffs, const double* ion_rads, int flags,
                       double solvent_ed, double c1, double scale, const double* center);

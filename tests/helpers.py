@@ -1,0 +1,29 @@
+"""Shared builders for the parity tests (seeded inputs; the oracle is the checker)."""
+import numpy as np
+
+import oracle as O
+from dpx import models as M
+
+SOLVENT = [1, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 4]
+VACUUM = [1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0]
+
+
+def globule(n, radius, seed, extra=SOLVENT, centered=False):
+    sym, xyz = M.make_globule(n, radius, seed)
+    return M.PDBAmplitude(sym, xyz, extra, centered=centered)
+
+
+def oracle_grid(amp, gs, qmax, mode=O.FP64):
+    s = O.Struct.from_pdb(amp)
+    data = O.grid_fill(s, gs, qmax, mode)
+    return data, O.grid_splines(gs, data, mode)
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def rel_to_max(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
