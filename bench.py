@@ -123,7 +123,8 @@ def run_dpx(args):
     torch.cuda.set_device(lrank)
     L = dpx.lib()
     ctx = M.Context(lrank)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a real stream: CUDA events on it see every libdpx launch
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     if args.fill_shape:
         c, t = (int(x) for x in args.fill_shape.split("x"))

@@ -74,6 +74,8 @@ struct DevBuf {
 
 struct dpx_ctx_s {
     int device = 0;
+    int refs = 1;  // the caller's handle + one per live grid
+    bool closed = false;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     int fill_cpt = 4, fill_threads = 256;
@@ -207,8 +209,10 @@ int dpx_ctx_create(int device, dpx_ctx* out) {
     return DPX_OK;
 }
 
-int dpx_ctx_destroy(dpx_ctx ctx) {
-    if (!ctx) return DPX_OK;
+namespace {
+// Frees the context once the caller has destroyed it and no grid uses it.
+void ctx_release(dpx_ctx ctx) {
+    if (--ctx->refs > 0) return;
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
@@ -216,6 +220,14 @@ int dpx_ctx_destroy(dpx_ctx ctx) {
         b->release();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
+}
+}  // namespace
+
+int dpx_ctx_destroy(dpx_ctx ctx) {
+    if (!ctx) return DPX_OK;
+    if (ctx->closed) return fail(DPX_ERR_ARG, "context destroyed twice");
+    ctx->closed = true;
+    ctx_release(ctx);
     return DPX_OK;
 }
 
@@ -279,6 +291,7 @@ int dpx_grid_create(dpx_ctx ctx, int grid_size, double qmax, int precision, dpx_
         delete g;
         return cuda_fail(e, "cudaMemset(grid)");
     }
+    ctx->refs++;
     *out = g;
     return DPX_OK;
 }
@@ -288,7 +301,9 @@ int dpx_grid_destroy(dpx_grid g) {
     set_device(g->ctx);
     cudaStreamSynchronize(g->ctx->stream);
     cudaFree(g->cells);
+    dpx_ctx ctx = g->ctx;
     delete g;
+    ctx_release(ctx);
     return DPX_OK;
 }
 
@@ -369,10 +384,11 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
     cudaError_t e;
     if (g->precision == DPX_FP64)
         e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, cen,
-                                 scale, (double4_32a*)g->cells, 0, G.P);
+                                 scale, (double4_32a*)g->cells, 0, dpx::source_cells(G));
     else
         e = dpx::launch_fill_f32(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const float*)ctx->table.p, G, cen,
-                                 (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads, 0, G.P);
+                                 (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads, 0,
+                                 dpx::source_cells(G));
     if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
     // the host vectors above are consumed by the async copies: wait before they go
     DPX_CUDA(cudaStreamSynchronize(s));

@@ -27,6 +27,13 @@ inline Geom make_geom(int grid_size, double qmax) {
 
 __host__ __device__ inline int64_t shell_base(int64_t i) { return 1 + 6 * (i - 1) * i * i; }
 
+// Cells the amplitude fill evaluates: the origin plus the first 3i(3i+1) cells
+// of every shell; the rest are their Friedel antipodes (F(-q) = conj F(q)).
+inline int64_t source_cells(const Geom& g) {
+    const int64_t lp = g.Lp;
+    return 3 * lp * (lp + 1) * (lp + 1) + 1;
+}
+
 // One placed view of a grid for the orientation average: the leaf's own
 // rotation/translation and, for a docked assembly, groups of copies that share
 // a rotation (ManualSymmetry translationsPerOrientation).
@@ -57,7 +64,7 @@ struct AvgPlan {
     double* partial;         // [nbr][n_chunks][max_q]
 };
 
-// kernels (dpx_kernels.cu)
+// kernels (dpx_kernels.cu); the fill launchers take a range of source cells
 cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
                             const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,
                             int block, int64_t cell_lo, int64_t cell_hi);

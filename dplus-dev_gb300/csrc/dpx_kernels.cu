@@ -39,12 +39,50 @@ __device__ __forceinline__ void cell_indices(int64_t idx, int& qi, int& ti, int&
     pi = (int)(rem - (int64_t)ti * 6 * i);
 }
 
-__device__ __forceinline__ void next_cell(int& qi, int& ti, int& pi) {
-    if (qi == 0) { qi = 1; ti = 0; pi = 0; return; }
-    if (++pi == 6 * qi) {
-        pi = 0;
-        if (++ti == 3 * qi + 1) { ti = 0; ++qi; }
-    }
+// --------------------------------------------------------------------------
+// Friedel half of the grid.  With real form factors F(-q) = conj F(q), and the
+// antipode of cell (i, t, p) is the cell (i, 3i - t, (p + 3i) mod 6i).  The
+// first 3i(3i+1) cells of every shell (rows t < 3i/2 plus half of the equator
+// row when 3i is even) together with their antipodes cover the shell exactly
+// once, so the fill evaluates only that prefix: source index s (0 = origin)
+// maps to shell i with 1 + 3(i-1)i^2 <= s < 1 + 3i(i+1)^2.
+// --------------------------------------------------------------------------
+__host__ __device__ inline int64_t src_base(int64_t i) { return 1 + 3 * (i - 1) * i * i; }
+
+struct SrcCell {
+    int qi, ti, pi, o;  // shell, row, column, offset in the shell's source prefix
+};
+
+__device__ __forceinline__ SrcCell src_cell(int64_t s) {
+    SrcCell c{0, 0, 0, 0};
+    if (s == 0) return c;
+    int64_t i = (int64_t)cbrtf((float)s * (1.0f / 3.0f));
+    if (i < 1) i = 1;
+    while (i > 1 && src_base(i) > s) --i;
+    while (src_base(i + 1) <= s) ++i;
+    const int64_t o = s - src_base(i);
+    c.qi = (int)i;
+    c.o = (int)o;
+    c.ti = (int)(o / (6 * i));
+    c.pi = (int)(o - (int64_t)c.ti * 6 * i);
+    return c;
+}
+
+__device__ __forceinline__ void next_src(SrcCell& c) {
+    if (c.qi == 0) { c.qi = 1; c.ti = 0; c.pi = 0; c.o = 0; return; }
+    ++c.o;
+    if (c.o == 3 * c.qi * (3 * c.qi + 1)) { ++c.qi; c.ti = 0; c.pi = 0; c.o = 0; return; }
+    if (++c.pi == 6 * c.qi) { c.pi = 0; ++c.ti; }
+}
+
+// cell index of a source cell and of its antipode
+__device__ __forceinline__ void src_targets(const SrcCell& c, int64_t& cell, int64_t& anti) {
+    if (c.qi == 0) { cell = anti = 0; return; }
+    const int64_t b = shell_base(c.qi), n = 6 * (int64_t)c.qi;
+    cell = b + c.o;
+    int64_t p2 = c.pi + 3 * (int64_t)c.qi;
+    if (p2 >= n) p2 -= n;
+    anti = b + (3 * (int64_t)c.qi - c.ti) * n + p2;
 }
 
 // --------------------------------------------------------------------------
@@ -67,28 +105,30 @@ __global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restr
 
     float qx[CPT], qy[CPT], qz[CPT], accR[CPT], accI[CPT];
     int layer[CPT];
+    int64_t dst[CPT], anti[CPT];
     {
-        int qi, ti, pi;
-        cell_indices(first < cell_hi ? first : 0, qi, ti, pi);
+        SrcCell sc = src_cell(first < cell_hi ? first : 0);
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
+            const int qi = sc.qi;
             layer[c] = qi;
             if (qi == 0) {
                 qx[c] = qy[c] = qz[c] = 0.f;
             } else {
                 const float inv = 1.0f / (float)(3 * qi);
                 float st, ct, sp, cp;
-                sincospif((float)ti * inv, &st, &ct);
-                sincospif((float)pi * inv, &sp, &cp);
+                sincospif((float)sc.ti * inv, &st, &ct);
+                sincospif((float)sc.pi * inv, &sp, &cp);
                 const float qI = (float)((double)qi * step);
                 qx[c] = qI * st * cp;
                 qy[c] = qI * st * sp;
                 qz[c] = qI * ct;
             }
+            src_targets(sc, dst[c], anti[c]);
             accR[c] = 0.f;
             accI[c] = 0.f;
-            if (layer[c] > Lp) layer[c] = Lp;  // cells past the grid end are never stored
-            next_cell(qi, ti, pi);
+            if (layer[c] > Lp) layer[c] = Lp;  // source cells past the grid end are never stored
+            next_src(sc);
         }
     }
 
@@ -142,7 +182,8 @@ __global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restr
             re = r2;
             im = i2;
         }
-        reinterpret_cast<float2*>(grid + cell)[0] = make_float2(re, im);
+        reinterpret_cast<float2*>(grid + dst[c])[0] = make_float2(re, im);
+        if (anti[c] != dst[c]) reinterpret_cast<float2*>(grid + anti[c])[0] = make_float2(re, -im);
     }
 }
 
@@ -159,14 +200,14 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
                                                            int64_t cell_hi) {
     __shared__ double4_32a s_atoms[THREADS];
     const int64_t cell = cell_lo + (int64_t)blockIdx.x * THREADS + threadIdx.x;
-    int qi, ti, pi;
-    cell_indices(cell < cell_hi ? cell : 0, qi, ti, pi);
+    const SrcCell sc = src_cell(cell < cell_hi ? cell : 0);
+    const int qi = sc.qi;
     double qx = 0, qy = 0, qz = 0;
     if (qi > 0) {
         const double inv = 1.0 / (double)(3 * qi);
         double st, ct, sp, cp;
-        sincospi((double)ti * inv, &st, &ct);
-        sincospi((double)pi * inv, &sp, &cp);
+        sincospi((double)sc.ti * inv, &st, &ct);
+        sincospi((double)sc.pi * inv, &sp, &cp);
         const double qI = (double)qi * step;
         qx = qI * st * cp;
         qy = qI * st * sp;
@@ -206,7 +247,12 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
         re = r2;
         im = i2;
     }
-    if (cell < cell_hi) reinterpret_cast<double2*>(grid + cell)[0] = make_double2(re, im);
+    if (cell < cell_hi) {
+        int64_t dst, anti;
+        src_targets(sc, dst, anti);
+        reinterpret_cast<double2*>(grid + dst)[0] = make_double2(re, im);
+        if (anti != dst) reinterpret_cast<double2*>(grid + anti)[0] = make_double2(re, -im);
+    }
 }
 
 // --------------------------------------------------------------------------

@@ -60,7 +60,9 @@ def test_splines_match_oracle(ctx, prec, tol):
     g.compute_splines()
     v, d = g.read()
     ref_d = O.grid_splines(gs, v, O.FP64)
-    assert rel_to_max(d, ref_d) <= tol
+    # derivatives enter the Hermite interpolation next to the values: bound the
+    # error on the amplitude scale (FP32 storage rounds y at 6e-8 |y|)
+    assert np.max(np.abs(d - ref_d)) <= tol * np.max(np.abs(v))
 
 
 def _avg(ctx, amp, gs, qmax, Q, dirs, prec, eps=0.0, stride=0, n=None):
