@@ -92,6 +92,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def apply_profile_shape(spec: str) -> None:
+    """--profile-shape atoms,layers,dirs,nq: a reduced case for ncu captures
+    (never a bench line: the JSON says so)."""
+    global N_ATOMS, RADIUS, GRID_SIZE, N_DIRS, NQ, CONFIG
+    a, l, d, q = (int(x) for x in spec.split(","))
+    N_ATOMS, GRID_SIZE, N_DIRS, NQ = a, 2 * l, d, q
+    RADIUS = 5.0 * (a / 20000.0) ** (1.0 / 3.0)
+    CONFIG = dict(CONFIG, workload=f"profile shape: {a} atoms, {l} layers, {d} directions, {q} q",
+                  atoms=a, grid_layers=l, mc_directions=d, q_points=q)
+
+
 def build_inputs():
     from dpx import models as M
     sym, xyz = M.make_globule(N_ATOMS, RADIUS, SEED)
@@ -231,12 +242,14 @@ def run_dpx(args):
         avg_ms = float(np.median(times["average"]))
         spl_ms = float(np.median(times["splines"]))
         P = L.dpx_grid_cells(GRID_SIZE)
-        pairs = float(N_ATOMS) * P
-        # SFU roofline: 2 MUFU ops (sin, cos) per atom-cell pair, 16 MUFU lanes/SM/clk, 152 SMs
-        sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-        sfu_peak = 152 * 16 / 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e9  # Gpair/s at max clock
+        lp = GRID_SIZE // 2 + 3
+        P_src = 3 * lp * (lp + 1) ** 2 + 1  # Friedel half actually evaluated
+        pairs = float(N_ATOMS) * P_src
+        # SFU roofline: 2 MUFU ops (sin, cos) per evaluated atom-cell pair,
+        # 16 MUFU lanes/SM/clk, 152 SMs, at the maximum SM clock
+        sfu_peak = 152 * 16 / 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e9  # Gpair/s
         achieved = pairs / (fill_ms / 1e3) / 1e9
-        n_brackets = 200
+        n_brackets = GRID_SIZE // 2
         interp_bytes = float(N_DIRS) * n_brackets * (4 * 4 * 2 * 16)  # 4 planes x 4 rows x 2 nodes x 16 B
         out = {
             "metric": "I(q) solves/s (FP32-bulk, 20k-atom subunit, L=200, 500 q)",
@@ -249,7 +262,9 @@ def run_dpx(args):
             "gpu_launches": args.steps * 4,
             "roofline": {"bound": "sfu", "kernel": "fill_f32_kernel", "achieved": achieved, "peak": sfu_peak,
                          "unit": "Gpair/s", "frac": achieved / sfu_peak, "traffic": None,
-                         "note": "peak = 152 SM x 16 MUFU/clk / 2 MUFU per pair at sm_max_mhz"},
+                         "note": "evaluated pairs = atoms x Friedel-half cells; peak = 152 SM x 16 MUFU/clk / "
+                                 "2 MUFU per pair at sm_max_mhz (derived, not in MEASURED_PEAKS.json)",
+                         "algorithmic_pairs_per_s": float(N_ATOMS) * P / (fill_ms / 1e3)},
             "roofline_average": {"bound": "hbm", "kernel": "average_kernel",
                                  "achieved": interp_bytes / (avg_ms / 1e3) / 1e9, "peak": peaks["hbm_gbs"],
                                  "unit": "GB/s", "frac": interp_bytes / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"],
@@ -340,7 +355,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--check-error", action="store_true")
+    ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
     args = ap.parse_args()
+    if args.profile_shape:
+        apply_profile_shape(args.profile_shape)
+        args.no_cpu_baseline = True
     if args.impl == "reference":
         out = run_reference(args)
     else:
