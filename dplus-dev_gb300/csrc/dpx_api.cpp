@@ -145,9 +145,13 @@ void euler(double a, double b, double c, double R[9]) {
     R[6] = s1 * s3 - c1 * c3 * s2; R[7] = c3 * s1 + c1 * s2 * s3; R[8] = c1 * c2;
 }
 
+}  // namespace
+
+int dpx::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 // Bracket assignment of IntegrateLayersTogether (Amplitude.cpp:1184-1217);
 // where two brackets claim one q, the later layer wins.
-void q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q) {
+void dpx::q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q) {
     const int L = grid_size / 2;
     const double step = 2 * qmax / grid_size;
     for (int k = 0; k < nq; ++k) layer_of_q[k] = -1;
@@ -165,6 +169,9 @@ void q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_
         for (int k = qb; k <= qe; ++k) layer_of_q[k] = layer;
     }
 }
+
+namespace {
+using dpx::q_brackets;
 
 int grid_from_voxels(int64_t voxels, int thDivs, int phDivs, double stepSize, int* grid_size, double* qmax) {
     if (thDivs != 3 || phDivs != 6) return fail(DPX_ERR_ARG, "only thDivs=3, phDivs=6 grids exist");

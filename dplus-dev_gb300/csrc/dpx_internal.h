@@ -64,6 +64,10 @@ struct AvgPlan {
     double* partial;         // [nbr][n_chunks][max_q]
 };
 
+// host helpers (dpx_api.cpp)
+void q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q);
+int set_error(int code, const char* msg);  // records the per-thread message, returns code
+
 // kernels (dpx_kernels.cu); the fill launchers take a range of source cells
 cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
                             const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,

@@ -65,6 +65,8 @@ _SIGS = {
                                                   C.c_int, _I]),
     "dpx_calc_mcoa_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, C.c_int,
                                            C.c_int64, C.c_double, _D, C.c_int64, C.c_int, _I]),
+    "dpx_mc_average_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, _D, _P, C.c_int64, C.c_double,
+                                         _P, _P]),
 }
 
 EXPORTED = sorted(_SIGS)

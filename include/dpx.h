@@ -144,6 +144,37 @@ int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
                              int64_t maxIters, double convergence, const double* dirs, int64_t dir_layer_stride,
                              int precision, int* pStop);
 
+/* ---- allocation-free orientation average ----
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc /
+ * cudaFree: applications whose device memory is pre-reserved by their own pool
+ * or caching allocator, and latency-bound serving loops in which a cudaFree
+ * (which synchronizes the whole device) would stall other streams.
+ *
+ * The Monte Carlo orientation average of one device-resident grid at identity
+ * placement (the computation of dpx_calc_mcoa_jacob_sphr / GPUCalcMCOAJacobSphrDD
+ * on device data).  The caller passes every input and output:
+ *   grid_cells  device cells of the grid (dpx_grid_device_ptr layout: float4 for
+ *               DPX_FP32, 32-byte double4 for DPX_FP64, values + spline derivatives)
+ *   Q           host, nq ascending q values within the grid's qmax
+ *   dirs        device, n_samples (theta, phi) pairs used by every layer bracket
+ *   res         device, nq doubles, written in full
+ *   stream      cudaStream_t the work is queued on (NULL = legacy default stream);
+ *               the call returns without waiting for the results.
+ * Nothing is allocated on the device: bracket tables and partial sums live in
+ * one static scratch array of DPX_NOALLOC_SCRATCH_BYTES compiled into libdpx,
+ * which every GPU that loads the library holds until the process exits.
+ * Requests needing more (about 8 B x brackets x ceil(n_samples/128) x max q per
+ * bracket) return DPX_ERR_ARG.  The first call on a device looks up the scratch
+ * array's device address (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture.  All calls on a device share the
+ * array and it keeps the last call's contents: calls whose work overlaps on the
+ * GPU (different streams, or different host threads) race on it and must be
+ * serialized by the caller. */
+#define DPX_NOALLOC_SCRATCH_BYTES (16u << 20)
+int dpx_mc_average_noalloc(const void* grid_cells, int grid_size, double qmax, int precision, int nq,
+                           const double* Q, const double* dirs, int64_t n_samples, double eps, double* res,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif
