@@ -78,7 +78,7 @@ struct dpx_ctx_s {
     bool closed = false;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
-    int fill_cpt = 4, fill_threads = 256;
+    int fill_cpt = 8, fill_threads = 128;  // autotuned on GB300 (bench workload)
     DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs;
     std::vector<char> host_stage;
 };
@@ -254,15 +254,14 @@ int dpx_ctx_synchronize(dpx_ctx ctx) {
 
 int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cpt, int threads) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
-    static const int ok[][2] = {{1, 128}, {2, 128}, {4, 128}, {8, 128}, {1, 256}, {2, 256},
-                                {4, 256}, {8, 256}, {2, 512}, {4, 512}};
+    static const int ok[][2] = {{2, 256}, {4, 128}, {4, 256}, {6, 128}, {6, 256}, {8, 128}, {8, 256}};
     for (auto& s : ok)
         if (s[0] == cpt && s[1] == threads) {
             ctx->fill_cpt = cpt;
             ctx->fill_threads = threads;
             return DPX_OK;
         }
-    return fail(DPX_ERR_ARG, "unsupported fill shape %d x %d", cpt, threads);
+    return fail(DPX_ERR_ARG, "unsupported fill shape %d cells x %d threads", cpt, threads);
 }
 
 int64_t dpx_grid_cells(int grid_size) {
@@ -381,21 +380,27 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
     aff_table(n_ions, atoms_per_ion, coeffs, ion_rads, flags, solvent_ed, c1, G.Lp, G.step, aff);
     const size_t tb = aff.size() * (g->precision == DPX_FP64 ? sizeof(double) : sizeof(float));
     DPX_CUDA(ctx->table.reserve(tb));
-    DPX_CUDA(ctx->ions.reserve(off.size() * sizeof(int)));
     std::vector<float> affF;
     if (g->precision == DPX_FP32) affF.assign(aff.begin(), aff.end());
     DPX_CUDA(cudaMemcpyAsync(ctx->table.p, g->precision == DPX_FP64 ? (const void*)aff.data() : (const void*)affF.data(),
                              tb, cudaMemcpyHostToDevice, s));
+    // work-item prefix of the row-factored fill, placed after the ion offsets
+    const int cpt = g->precision == DPX_FP64 ? dpx::kFill64Cells : ctx->fill_cpt;
+    std::vector<int64_t> pref(G.Lp + 1);
+    const int64_t n_items = dpx::fill_items(G, cpt, pref.data());
+    const size_t off_bytes = (off.size() * sizeof(int) + 15) & ~size_t(15);
+    DPX_CUDA(ctx->ions.reserve(off_bytes + pref.size() * sizeof(int64_t)));
     DPX_CUDA(cudaMemcpyAsync(ctx->ions.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    const int64_t* d_pref = reinterpret_cast<const int64_t*>(static_cast<char*>(ctx->ions.p) + off_bytes);
+    DPX_CUDA(cudaMemcpyAsync((void*)d_pref, pref.data(), pref.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
 
     cudaError_t e;
     if (g->precision == DPX_FP64)
-        e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, cen,
-                                 scale, (double4_32a*)g->cells, 0, dpx::source_cells(G));
+        e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, d_pref,
+                                 n_items, cen, scale, (double4_32a*)g->cells);
     else
-        e = dpx::launch_fill_f32(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const float*)ctx->table.p, G, cen,
-                                 (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads, 0,
-                                 dpx::source_cells(G));
+        e = dpx::launch_fill_f32(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const float*)ctx->table.p, G, d_pref,
+                                 n_items, cen, (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads);
     if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
     // the host vectors above are consumed by the async copies: wait before they go
     DPX_CUDA(cudaStreamSynchronize(s));
@@ -451,30 +456,16 @@ int dpx_grid_write(dpx_grid g, const double* values, const double* coeffs) {
     return DPX_OK;
 }
 
-int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
-                            const int* n_copies, const double* copy_rot, const double* copy_tr,
-                            const double* sym_scale, int nq, const double* Q, const double* dirs, int dirs_on_device,
-                            int64_t dir_layer_stride, int64_t n_samples, double eps, double* res) {
-    if (!ctx || n_models <= 0 || !grids || nq <= 0 || !Q || !dirs || !res)
-        return fail(DPX_ERR_ARG, "NULL or empty argument");
-    if (n_samples <= 0) return fail(DPX_ERR_ARG, "n_samples must be positive");
-    const int grid_size = grids[0]->grid_size;
-    const double qmax = grids[0]->qmax;
-    const int prec = grids[0]->precision;
-    for (int m = 0; m < n_models; ++m)
-        if (!grids[m] || grids[m]->grid_size != grid_size || grids[m]->qmax != qmax || grids[m]->precision != prec)
-            return fail(DPX_ERR_ARG, "all models must share grid_size, qmax and precision");
-    for (int k = 1; k < nq; ++k)
-        if (!(Q[k] >= Q[k - 1])) return fail(DPX_ERR_ARG, "Q must be ascending");
-    if (Q[0] < 0) return fail(DPX_ERR_ARG, "negative q");
-    const Geom& G = grids[0]->g;
-    if (Q[nq - 1] > G.L * G.step * (1.0 + 1e-12))
-        return fail(DPX_ERR_ARG, "q=%g beyond the grid's qmax=%g", Q[nq - 1], G.L * G.step);
-    if (int rc = set_device(ctx)) return rc;
-    cudaStream_t s = ctx->stream;
+}  // extern "C"
 
-    // models and docked groups
-    std::vector<dpx::ModelDev> md(n_models);
+namespace {
+// Model structs and docked rotation groups (ManualSymmetry translationsPerOrientation
+// grouped by identical Euler triples, first-appearance order); group tables are
+// staged for ctx->groups, model structs point into it.
+int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                   const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                   std::vector<dpx::ModelDev>& md, std::vector<char>& gstage) {
+    md.assign(n_models, dpx::ModelDev{});
     std::vector<double> gR, gT;
     std::vector<int> gOff;
     std::vector<int> model_group_base(n_models), model_toff_base(n_models);
@@ -486,6 +477,9 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
         for (int k = 0; k < 3; ++k) M.tr[k] = tr ? tr[3 * m + k] : 0.0;
         const int nc = n_copies ? n_copies[m] : 0;
         M.sym_scale = sym_scale ? sym_scale[m] : 1.0;
+        M.plain = (M.R[0] == 1.0 && M.R[4] == 1.0 && M.R[8] == 1.0 && M.R[1] == 0.0 && M.R[2] == 0.0 &&
+                   M.R[3] == 0.0 && M.R[5] == 0.0 && M.R[6] == 0.0 && M.R[7] == 0.0 && M.tr[0] == 0.0 &&
+                   M.tr[1] == 0.0 && M.tr[2] == 0.0);
         model_group_base[m] = (int)gOff.size();
         // group copies by identical Euler triples, first-appearance order
         std::vector<int> rep;
@@ -524,7 +518,7 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
     double* dR = (double*)gbase;
     double* dT = (double*)(gbase + bytesR);
     int* dO = (int*)(gbase + bytesR + bytesT);
-    std::vector<char> gstage(bytesR + bytesT + bytesO);
+    gstage.assign(bytesR + bytesT + bytesO, 0);
     if (bytesR) std::memcpy(gstage.data(), gR.data(), bytesR);
     if (bytesT) std::memcpy(gstage.data() + bytesR, gT.data(), bytesT);
     if (bytesO) std::memcpy(gstage.data() + bytesR + bytesT, gOff.data(), bytesO);
@@ -536,6 +530,40 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
         M.trans = dT + 3 * model_toff_base[m];
         groups_seen += M.n_groups;
     }
+    return DPX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                            const int* n_copies, const double* copy_rot, const double* copy_tr,
+                            const double* sym_scale, int nq, const double* Q, const double* dirs, int dirs_on_device,
+                            int64_t dir_layer_stride, int64_t n_samples, double eps, double* res) {
+    if (!ctx || n_models <= 0 || !grids || nq <= 0 || !Q || !dirs || !res)
+        return fail(DPX_ERR_ARG, "NULL or empty argument");
+    if (n_samples <= 0) return fail(DPX_ERR_ARG, "n_samples must be positive");
+    const int grid_size = grids[0]->grid_size;
+    const double qmax = grids[0]->qmax;
+    const int prec = grids[0]->precision;
+    for (int m = 0; m < n_models; ++m)
+        if (!grids[m] || grids[m]->grid_size != grid_size || grids[m]->qmax != qmax || grids[m]->precision != prec)
+            return fail(DPX_ERR_ARG, "all models must share grid_size, qmax and precision");
+    for (int k = 1; k < nq; ++k)
+        if (!(Q[k] >= Q[k - 1])) return fail(DPX_ERR_ARG, "Q must be ascending");
+    if (Q[0] < 0) return fail(DPX_ERR_ARG, "negative q");
+    const Geom& G = grids[0]->g;
+    if (Q[nq - 1] > G.L * G.step * (1.0 + 1e-12))
+        return fail(DPX_ERR_ARG, "q=%g beyond the grid's qmax=%g", Q[nq - 1], G.L * G.step);
+    if (int rc = set_device(ctx)) return rc;
+    cudaStream_t s = ctx->stream;
+
+    std::vector<dpx::ModelDev> md;
+    std::vector<char> gstage;
+    if (int rc = prepare_models(ctx, n_models, grids, rot, tr, n_copies, copy_rot, copy_tr, sym_scale, md, gstage))
+        return rc;
+
 
     // brackets
     std::vector<int> layer_of_q(nq);
@@ -566,6 +594,9 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
     plan.chunk_off = eps > 0.0 ? 99 : 0;
     plan.n_chunks = (n_samples + plan.chunk_off + plan.chunk - 1) / plan.chunk;
     plan.dir_stride = dir_layer_stride;
+    plan.need_dir = 0;
+    for (const auto& M : md)
+        if (!M.plain || M.n_groups > 0) plan.need_dir = 1;
     const size_t pb = br_layer.size() * sizeof(int) + br_off.size() * sizeof(int) + br_qidx.size() * sizeof(int) +
                       br_q.size() * sizeof(double) + 64;
     DPX_CUDA(ctx->plan.reserve(pb + md.size() * sizeof(dpx::ModelDev) + 64));
@@ -636,6 +667,108 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
         }
         res[0] = ar * ar + ai * ai;
     }
+    return DPX_OK;
+}
+
+int dpx_vegas_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                        const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                        int nq, const double* Q, uint64_t seed, int points_per_iter, int64_t max_points, double eps,
+                        double* res) {
+    if (!ctx || n_models <= 0 || !grids || nq <= 0 || !Q || !res) return fail(DPX_ERR_ARG, "NULL or empty argument");
+    if (points_per_iter <= 0 || points_per_iter % 1024)
+        return fail(DPX_ERR_ARG, "points_per_iter must be a positive multiple of 1024 (32 x 32 bins)");
+    if (max_points <= 0) return fail(DPX_ERR_ARG, "max_points must be positive");
+    const int grid_size = grids[0]->grid_size;
+    const double qmax = grids[0]->qmax;
+    const int prec = grids[0]->precision;
+    for (int m = 0; m < n_models; ++m)
+        if (!grids[m] || grids[m]->grid_size != grid_size || grids[m]->qmax != qmax || grids[m]->precision != prec)
+            return fail(DPX_ERR_ARG, "all models must share grid_size, qmax and precision");
+    for (int k = 1; k < nq; ++k)
+        if (!(Q[k] >= Q[k - 1])) return fail(DPX_ERR_ARG, "Q must be ascending");
+    if (!(Q[0] >= 0)) return fail(DPX_ERR_ARG, "negative q");
+    const Geom& G = grids[0]->g;
+    if (Q[nq - 1] > G.L * G.step * (1.0 + 1e-12))
+        return fail(DPX_ERR_ARG, "q=%g beyond the grid's qmax=%g", Q[nq - 1], G.L * G.step);
+    if (int rc = set_device(ctx)) return rc;
+    cudaStream_t s = ctx->stream;
+
+    std::vector<dpx::ModelDev> md;
+    std::vector<char> gstage;
+    if (int rc = prepare_models(ctx, n_models, grids, rot, tr, n_copies, copy_rot, copy_tr, sym_scale, md, gstage))
+        return rc;
+    int need_dir = 0;
+    for (const auto& M : md)
+        if (!M.plain || M.n_groups > 0) need_dir = 1;
+
+    // brackets of the hybrid path (GPUHybridCalc.cu:363-375), q = 0 included
+    struct Br { int q0, m; };
+    std::vector<Br> brs;
+    int max_m = 1;
+    for (int qInd = 0, lower = 0; qInd < nq;) {
+        while (Q[qInd] > double(lower + 1) * G.step) lower++;
+        int qEnd;
+        for (qEnd = qInd + 1; qEnd < nq; qEnd++)
+            if (Q[qEnd] > double(lower + 1) * G.step) break;
+        qEnd--;
+        brs.push_back({qInd, qEnd - qInd + 1});
+        max_m = std::max(max_m, qEnd - qInd + 1);
+        qInd = qEnd + 1;
+        lower++;
+    }
+    const int n_iter = (int)((max_points + points_per_iter - 1) / points_per_iter);
+
+    // device layout in ctx->plan: [models][bounds 66][q nq][qidx nq][done nbr][hist n_iter x max_m]; I in ctx->partial
+    std::vector<int> qidx(nq);
+    for (int k = 0; k < nq; ++k) qidx[k] = k;
+    std::vector<double> bounds(2 * 32 + 2);
+    for (int i = 0; i <= 32; ++i) bounds[i] = double(i) / 32;
+    for (int i = 0; i <= 32; ++i) bounds[33 + i] = double(i) / 32;
+    std::vector<char> stage;
+    size_t o = 0;
+    auto put = [&](const void* src, size_t n) -> size_t {
+        size_t at = (o + 31) & ~size_t(31);
+        stage.resize(at + n);
+        if (n) std::memcpy(stage.data() + at, src, n);
+        o = at + n;
+        return at;
+    };
+    const size_t oM = put(md.data(), md.size() * sizeof(dpx::ModelDev));
+    const size_t oB = put(bounds.data(), bounds.size() * sizeof(double));
+    const size_t oQ = put(Q, (size_t)nq * sizeof(double));
+    const size_t oI = put(qidx.data(), qidx.size() * sizeof(int));
+    std::vector<int> zeros(brs.size(), 0);
+    const size_t oD = put(zeros.data(), zeros.size() * sizeof(int));
+    const size_t oH = (o + 31) & ~size_t(31);
+    const size_t total = oH + (size_t)n_iter * max_m * sizeof(double);
+    DPX_CUDA(ctx->plan.reserve(total));
+    DPX_CUDA(ctx->partial.reserve((size_t)points_per_iter * max_m * sizeof(double)));
+    DPX_CUDA(ctx->result.reserve((size_t)nq * sizeof(double)));
+    char* base = (char*)ctx->plan.p;
+    DPX_CUDA(cudaMemcpyAsync(base, stage.data(), o, cudaMemcpyHostToDevice, s));
+    DPX_CUDA(cudaMemcpyAsync(ctx->groups.p, gstage.data(), gstage.size(), cudaMemcpyHostToDevice, s));
+    const dpx::ModelDev* d_models = (const dpx::ModelDev*)(base + oM);
+    double* d_bounds = (double*)(base + oB);
+    const double* d_q = (const double*)(base + oQ);
+    const int* d_qidx = (const int*)(base + oI);
+    int* d_done = (int*)(base + oD);
+    double* d_hist = (double*)(base + oH);
+    double* d_I = (double*)ctx->partial.p;
+    double* d_res = (double*)ctx->result.p;
+    for (size_t b = 0; b < brs.size(); ++b) {
+        for (int it = 0; it < n_iter; ++it) {
+            const uint64_t key = (uint64_t(b) << 32) | uint64_t(it);
+            cudaError_t e = dpx::launch_vegas_points(s, prec == DPX_FP64, G, n_models, d_models, need_dir,
+                                                     d_q + brs[b].q0, brs[b].m, points_per_iter, seed, key, d_bounds,
+                                                     d_done + b, d_I);
+            if (e == cudaSuccess)
+                e = dpx::launch_vegas_update(s, d_bounds, d_I, brs[b].m, points_per_iter, it, eps, d_hist, d_done + b,
+                                             d_res, d_qidx + brs[b].q0);
+            if (e != cudaSuccess) return cuda_fail(e, "VEGAS launch");
+        }
+    }
+    DPX_CUDA(cudaMemcpyAsync(res, d_res, (size_t)nq * sizeof(double), cudaMemcpyDeviceToHost, s));
+    DPX_CUDA(cudaStreamSynchronize(s));
     return DPX_OK;
 }
 

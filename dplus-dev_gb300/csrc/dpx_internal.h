@@ -27,12 +27,8 @@ inline Geom make_geom(int grid_size, double qmax) {
 
 __host__ __device__ inline int64_t shell_base(int64_t i) { return 1 + 6 * (i - 1) * i * i; }
 
-// Cells the amplitude fill evaluates: the origin plus the first 3i(3i+1) cells
-// of every shell; the rest are their Friedel antipodes (F(-q) = conj F(q)).
-inline int64_t source_cells(const Geom& g) {
-    const int64_t lp = g.Lp;
-    return 3 * lp * (lp + 1) * (lp + 1) + 1;
-}
+// Cells per work item of the FP64 fill (the FP32 fill takes it from the context).
+constexpr int kFill64Cells = 2;
 
 // One placed view of a grid for the orientation average: the leaf's own
 // rotation/translation and, for a docked assembly, groups of copies that share
@@ -46,6 +42,7 @@ struct ModelDev {
     const int* group_off;  // [n_groups + 1] into trans
     const double* trans;   // [3 K]
     double sym_scale;
+    int plain;             // R is the identity and tr is zero
 };
 
 struct AvgPlan {
@@ -62,18 +59,33 @@ struct AvgPlan {
     int chunk_off;           // first chunk holds chunk - chunk_off samples
     int64_t n_chunks;
     double* partial;         // [nbr][n_chunks][max_q]
+    int need_dir;            // some model is placed or docked: the kernel needs the direction vector
 };
 
 // host helpers (dpx_api.cpp)
 void q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q);
 int set_error(int code, const char* msg);  // records the per-thread message, returns code
 
-// kernels (dpx_kernels.cu); the fill launchers take a range of source cells
+// amplitude fill (dpx_fill.cu).  fill_items writes the work-item prefix
+// pref[0..Lp] (origin, then per shell (floor(3i/2)+1) rows x ceil(3i/cpt)
+// column chunks) and returns the item count.
+int64_t fill_items(const Geom& g, int cpt, int64_t* pref);
 cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
-                            const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,
-                            int block, int64_t cell_lo, int64_t cell_hi);
+                            const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
+                            float scale, float4* grid, int cells_per_thread, int block);
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
-                            const Geom& g, const double center[3], double scale, double4_32a* grid, int64_t cell_lo, int64_t cell_hi);
+                            const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
+                            double scale, double4_32a* grid);
+
+// VEGAS (dpx_kernels.cu): points of one iteration of one bracket, then the
+// single-block reduction / bin refinement / running mean / convergence test.
+cudaError_t launch_vegas_points(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                                int need_dir, const double* d_q, int m, int ppi, uint64_t seed, uint64_t key,
+                                const double* d_bounds, const int* d_done, double* d_I);
+cudaError_t launch_vegas_update(cudaStream_t s, double* d_bounds, const double* d_I, int m, int ppi, int it,
+                                double eps, double* d_hist, int* d_done, double* d_res, const int* d_qidx);
+
+// other kernels (dpx_kernels.cu)
 cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid);
 cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid);
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,

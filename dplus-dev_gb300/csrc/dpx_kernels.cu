@@ -39,221 +39,6 @@ __device__ __forceinline__ void cell_indices(int64_t idx, int& qi, int& ti, int&
     pi = (int)(rem - (int64_t)ti * 6 * i);
 }
 
-// --------------------------------------------------------------------------
-// Friedel half of the grid.  With real form factors F(-q) = conj F(q), and the
-// antipode of cell (i, t, p) is the cell (i, 3i - t, (p + 3i) mod 6i).  The
-// first 3i(3i+1) cells of every shell (rows t < 3i/2 plus half of the equator
-// row when 3i is even) together with their antipodes cover the shell exactly
-// once, so the fill evaluates only that prefix: source index s (0 = origin)
-// maps to shell i with 1 + 3(i-1)i^2 <= s < 1 + 3i(i+1)^2.
-// --------------------------------------------------------------------------
-__host__ __device__ inline int64_t src_base(int64_t i) { return 1 + 3 * (i - 1) * i * i; }
-
-struct SrcCell {
-    int qi, ti, pi, o;  // shell, row, column, offset in the shell's source prefix
-};
-
-__device__ __forceinline__ SrcCell src_cell(int64_t s) {
-    SrcCell c{0, 0, 0, 0};
-    if (s == 0) return c;
-    int64_t i = (int64_t)cbrtf((float)s * (1.0f / 3.0f));
-    if (i < 1) i = 1;
-    while (i > 1 && src_base(i) > s) --i;
-    while (src_base(i + 1) <= s) ++i;
-    const int64_t o = s - src_base(i);
-    c.qi = (int)i;
-    c.o = (int)o;
-    c.ti = (int)(o / (6 * i));
-    c.pi = (int)(o - (int64_t)c.ti * 6 * i);
-    return c;
-}
-
-__device__ __forceinline__ void next_src(SrcCell& c) {
-    if (c.qi == 0) { c.qi = 1; c.ti = 0; c.pi = 0; c.o = 0; return; }
-    ++c.o;
-    if (c.o == 3 * c.qi * (3 * c.qi + 1)) { ++c.qi; c.ti = 0; c.pi = 0; c.o = 0; return; }
-    if (++c.pi == 6 * c.qi) { c.pi = 0; ++c.ti; }
-}
-
-// cell index of a source cell and of its antipode
-__device__ __forceinline__ void src_targets(const SrcCell& c, int64_t& cell, int64_t& anti) {
-    if (c.qi == 0) { cell = anti = 0; return; }
-    const int64_t b = shell_base(c.qi), n = 6 * (int64_t)c.qi;
-    cell = b + c.o;
-    int64_t p2 = c.pi + 3 * (int64_t)c.qi;
-    if (p2 >= n) p2 -= n;
-    anti = b + (3 * (int64_t)c.qi - c.ti) * n + p2;
-}
-
-// --------------------------------------------------------------------------
-// Amplitude fill, FP32 bulk.  Atoms (centred, sorted by ion) are staged in
-// shared memory one tile per block; every thread owns CPT consecutive cells
-// and accumulates sum cos / sum sin per ion in FP32 (tile partial sums keep the
-// accumulation error at the tile level), then multiplies by the ion's form
-// factor at the cell's shell.  An optional per-cell phase e^{i q.c} (FP64)
-// restores the centring translation.
-// --------------------------------------------------------------------------
-template <int CPT, int THREADS>
-__global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restrict__ atoms,
-                                                           const int* __restrict__ ion_off, int U,
-                                                           const float* __restrict__ aff, int Lp, double step,
-                                                           double cx, double cy, double cz, int use_center,
-                                                           float scale, float4* __restrict__ grid,
-                                                           int64_t cell_lo, int64_t cell_hi) {
-    __shared__ float4 s_atoms[THREADS];
-    const int64_t first = cell_lo + ((int64_t)blockIdx.x * THREADS + threadIdx.x) * CPT;
-
-    float qx[CPT], qy[CPT], qz[CPT], accR[CPT], accI[CPT];
-    int layer[CPT];
-    int64_t dst[CPT], anti[CPT];
-    {
-        SrcCell sc = src_cell(first < cell_hi ? first : 0);
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-            const int qi = sc.qi;
-            layer[c] = qi;
-            if (qi == 0) {
-                qx[c] = qy[c] = qz[c] = 0.f;
-            } else {
-                const float inv = 1.0f / (float)(3 * qi);
-                float st, ct, sp, cp;
-                sincospif((float)sc.ti * inv, &st, &ct);
-                sincospif((float)sc.pi * inv, &sp, &cp);
-                const float qI = (float)((double)qi * step);
-                qx[c] = qI * st * cp;
-                qy[c] = qI * st * sp;
-                qz[c] = qI * ct;
-            }
-            src_targets(sc, dst[c], anti[c]);
-            accR[c] = 0.f;
-            accI[c] = 0.f;
-            if (layer[c] > Lp) layer[c] = Lp;  // source cells past the grid end are never stored
-            next_src(sc);
-        }
-    }
-
-    for (int u = 0; u < U; ++u) {
-        const int a0 = ion_off[u], a1 = ion_off[u + 1];
-        float sR[CPT], sI[CPT];
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) { sR[c] = 0.f; sI[c] = 0.f; }
-        for (int t0 = a0; t0 < a1; t0 += THREADS) {
-            const int n = min(THREADS, a1 - t0);
-            __syncthreads();
-            if (threadIdx.x < n) s_atoms[threadIdx.x] = atoms[t0 + threadIdx.x];
-            __syncthreads();
-            float tR[CPT], tI[CPT];
-#pragma unroll
-            for (int c = 0; c < CPT; ++c) { tR[c] = 0.f; tI[c] = 0.f; }
-#pragma unroll 4
-            for (int j = 0; j < n; ++j) {
-                const float4 a = s_atoms[j];
-#pragma unroll
-                for (int c = 0; c < CPT; ++c) {
-                    const float ph = fmaf(qz[c], a.z, fmaf(qy[c], a.y, qx[c] * a.x));
-                    float sn, cs;
-                    __sincosf(ph, &sn, &cs);
-                    tR[c] += cs;
-                    tI[c] += sn;
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < CPT; ++c) { sR[c] += tR[c]; sI[c] += tI[c]; }
-        }
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-            const float f = aff[(int64_t)u * (Lp + 1) + layer[c]];
-            accR[c] = fmaf(f, sR[c], accR[c]);
-            accI[c] = fmaf(f, sI[c], accI[c]);
-        }
-    }
-
-#pragma unroll
-    for (int c = 0; c < CPT; ++c) {
-        const int64_t cell = first + c;
-        if (cell >= cell_hi) break;
-        float re = accR[c] * scale, im = accI[c] * scale;
-        if (use_center) {
-            const double ph = (double)qx[c] * cx + (double)qy[c] * cy + (double)qz[c] * cz;
-            double sn, cs;
-            sincos(ph, &sn, &cs);
-            const float fs = (float)sn, fc = (float)cs;
-            const float r2 = re * fc - im * fs, i2 = re * fs + im * fc;
-            re = r2;
-            im = i2;
-        }
-        reinterpret_cast<float2*>(grid + dst[c])[0] = make_float2(re, im);
-        if (anti[c] != dst[c]) reinterpret_cast<float2*>(grid + anti[c])[0] = make_float2(re, -im);
-    }
-}
-
-// --------------------------------------------------------------------------
-// Amplitude fill, plain FP64: FP64 q vector, FP64 phase, FP64 sincos, FP64
-// accumulation.  Same tiling, one cell per thread.
-// --------------------------------------------------------------------------
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restrict__ atoms,
-                                                           const int* __restrict__ ion_off, int U,
-                                                           const double* __restrict__ aff, int Lp, double step,
-                                                           double cx, double cy, double cz, double scale,
-                                                           double4_32a* __restrict__ grid, int64_t cell_lo,
-                                                           int64_t cell_hi) {
-    __shared__ double4_32a s_atoms[THREADS];
-    const int64_t cell = cell_lo + (int64_t)blockIdx.x * THREADS + threadIdx.x;
-    const SrcCell sc = src_cell(cell < cell_hi ? cell : 0);
-    const int qi = sc.qi;
-    double qx = 0, qy = 0, qz = 0;
-    if (qi > 0) {
-        const double inv = 1.0 / (double)(3 * qi);
-        double st, ct, sp, cp;
-        sincospi((double)sc.ti * inv, &st, &ct);
-        sincospi((double)sc.pi * inv, &sp, &cp);
-        const double qI = (double)qi * step;
-        qx = qI * st * cp;
-        qy = qI * st * sp;
-        qz = qI * ct;
-    }
-    const int layer = qi > Lp ? Lp : qi;
-    double accR = 0, accI = 0;
-    for (int u = 0; u < U; ++u) {
-        const int a0 = ion_off[u], a1 = ion_off[u + 1];
-        double sR = 0, sI = 0;
-        for (int t0 = a0; t0 < a1; t0 += THREADS) {
-            const int n = min(THREADS, a1 - t0);
-            __syncthreads();
-            if (threadIdx.x < n) {
-                const float4 a = atoms[t0 + threadIdx.x];
-                s_atoms[threadIdx.x] = make_double4_32a(a.x, a.y, a.z, 0.0);
-            }
-            __syncthreads();
-            for (int j = 0; j < n; ++j) {
-                const double4_32a a = s_atoms[j];
-                const double ph = qx * a.x + qy * a.y + qz * a.z;
-                double sn, cs;
-                sincos(ph, &sn, &cs);
-                sR += cs;
-                sI += sn;
-            }
-        }
-        const double f = aff[(int64_t)u * (Lp + 1) + layer];
-        accR += f * sR;
-        accI += f * sI;
-    }
-    double re = accR * scale, im = accI * scale;
-    if (cx != 0.0 || cy != 0.0 || cz != 0.0) {
-        double sn, cs;
-        sincos(qx * cx + qy * cy + qz * cz, &sn, &cs);
-        const double r2 = re * cs - im * sn, i2 = re * sn + im * cs;
-        re = r2;
-        im = i2;
-    }
-    if (cell < cell_hi) {
-        int64_t dst, anti;
-        src_targets(sc, dst, anti);
-        reinterpret_cast<double2*>(grid + dst)[0] = make_double2(re, im);
-        if (anti != dst) reinterpret_cast<double2*>(grid + anti)[0] = make_double2(re, -im);
-    }
-}
 
 // --------------------------------------------------------------------------
 // Periodic cubic-spline derivatives along each theta row.  The inverse of the
@@ -368,26 +153,31 @@ __device__ __forceinline__ void load_cell<double>(const double4_32a* __restrict_
 template <typename T>
 __device__ Cx<T> interp_plane(const typename Vec4<T>::type* __restrict__ g, int ri, double theta, double phi) {
     const int64_t base = shell_base(ri);
-    const int64_t phiPoints = 6 * (int64_t)ri, thePoints = 3 * (int64_t)ri;
-    const double edge = k2Pi / (double)phiPoints;
+    const int phiPoints = 6 * ri, thePoints = 3 * ri;
     // angles outside [0, pi] x [0, 2 pi] (or NaN) are clamped so that every
     // node index below stays inside shell ri
     if (!(theta >= 0.0)) theta = 0.0;
     if (theta > kPi) theta = kPi;
     if (!(phi >= 0.0)) phi = 0.0;
     if (phi > k2Pi) phi = k2Pi;
-    const int64_t tI = (int64_t)((theta / kPi) * (double)thePoints);
-    int64_t pI = (int64_t)((phi / k2Pi) * (double)phiPoints);
-    double tTh = (theta / edge) - (double)tI;
-    double tPh = (phi / edge) - (double)pI;
+    // theta and phi share the step pi / (3 ri): one scale gives both cell
+    // coordinates (the reference divides by pi and by the edge separately;
+    // the two agree to the last bit except on exact cell boundaries)
+    const double cells_per_rad = (double)thePoints * (1.0 / kPi);
+    const double xt = theta * cells_per_rad, xp = phi * cells_per_rad;
+    const int tI = (int)xt;
+    int pI = (int)xp;
+    double tTh = xt - (double)tI;
+    double tPh = xp - (double)pI;
     if (fabs(tTh) < 1.0e-10) tTh = 0.0;
     if (fabs(tPh) < 1.0e-10) tPh = 0.0;
     if (pI >= phiPoints) pI = 0;
-    const int64_t pI1 = (pI + 1) % phiPoints;
+    const int pI1 = (pI + 1 == phiPoints) ? 0 : pI + 1;
     Cx<T> nodes[4];
 #pragma unroll
     for (int i = -1; i < 3; ++i) {
-        int64_t theInd = (thePoints + 1 + tI + i) % (thePoints + 1);
+        const int v = tI + i;
+        int theInd = v < 0 ? v + thePoints + 1 : (v > thePoints ? v - (thePoints + 1) : v);
         int64_t c1, c2;
         if (theInd == tI + i) {
             c1 = base + phiPoints * theInd + pI;
@@ -466,6 +256,73 @@ template <> __device__ __forceinline__ Cx<float> expi<float>(double phase) {
 }
 
 // --------------------------------------------------------------------------
+// Amplitude of every model at one direction for up to MQ q values of a
+// bracket (plane index fInd, radial fractions frac): for every model and
+// docked rotation group, the leaf's 4 planes at the rotated direction, the
+// radial Hermite per q, the leaf phase and the group's translation phases
+// (Amplitude.cpp:3553-3600, Symmetries.cpp:1079-1166).  A is accumulated.
+// --------------------------------------------------------------------------
+template <typename T, int MQ>
+__device__ void sample_amps(const ModelDev* __restrict__ models, int n_models, int Lp, int fInd, double theta,
+                            double phi, const double dir[3], int mq, const double* qv, const T* frac, Cx<T>* A) {
+    typedef typename Vec4<T>::type V4;
+    for (int mi = 0; mi < n_models; ++mi) {
+        const ModelDev& M = models[mi];
+        const V4* g = reinterpret_cast<const V4*>(M.grid);
+        const int ng = M.n_groups > 0 ? M.n_groups : 1;
+        for (int gi = 0; gi < ng; ++gi) {
+            double n0 = dir[0], n1 = dir[1], n2 = dir[2];
+            if (M.n_groups > 0) {
+                const double* Rg = M.group_R + 9 * gi;
+                double a0 = n0 * Rg[0] + n1 * Rg[3] + n2 * Rg[6];
+                double a1 = n0 * Rg[1] + n1 * Rg[4] + n2 * Rg[7];
+                double a2 = n0 * Rg[2] + n1 * Rg[5] + n2 * Rg[8];
+                const double nr = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+                n0 = a0 / nr; n1 = a1 / nr; n2 = a2 / nr;
+            }
+            // leaf placement (Amplitude.cpp:3553-3579); an unplaced leaf
+            // reads the sample's own angles
+            double nth = theta, nph = phi, dotR = 0.0;
+            if (!(M.plain && M.n_groups == 0)) {
+                const double t0 = n0 * M.R[0] + n1 * M.R[3] + n2 * M.R[6];
+                const double t1 = n0 * M.R[1] + n1 * M.R[4] + n2 * M.R[7];
+                const double t2 = n0 * M.R[2] + n1 * M.R[5] + n2 * M.R[8];
+                dotR = t0 * M.tr[0] + t1 * M.tr[1] + t2 * M.tr[2];
+                dir_angles(t0, t1, t2, nth, nph);
+            }
+            Cx<T> pl1, pl2, d1, d2;
+            planes<T>(g, Lp, fInd, nth, nph, pl1, pl2, d1, d2);
+            Cx<T> val[MQ];
+#pragma unroll
+            for (int k = 0; k < MQ; ++k) {
+                if (k < mq) {
+                    val[k] = hermite<T>(pl1, pl2, d1, d2, frac[k]);
+                    if (dotR != 0.0) val[k] = cmul(val[k], expi<T>(dotR * qv[k]));
+                }
+            }
+            if (M.n_groups > 0) {
+                Cx<T> tp[MQ];
+#pragma unroll
+                for (int k = 0; k < MQ; ++k) tp[k] = {T(0), T(0)};
+                for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
+                    const double* tt = M.trans + 3 * c;
+                    const double a = dir[0] * tt[0] + dir[1] * tt[1] + dir[2] * tt[2];
+#pragma unroll
+                    for (int k = 0; k < MQ; ++k)
+                        if (k < mq) tp[k] = cadd(tp[k], expi<T>(a * qv[k]));
+                }
+#pragma unroll
+                for (int k = 0; k < MQ; ++k)
+                    if (k < mq) val[k] = cscale(cmul(val[k], tp[k]), (T)M.sym_scale);
+            }
+#pragma unroll
+            for (int k = 0; k < MQ; ++k)
+                if (k < mq) A[k] = cadd(A[k], val[k]);
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
 // Orientation average: one block = one chunk of samples of one bracket.
 // Each thread evaluates one direction: for every model and every docked
 // rotation group, the leaf's 4 planes at the rotated direction, then the
@@ -492,8 +349,15 @@ __global__ void __launch_bounds__(128) average_kernel(int Lp, double step, const
         theta = d[0];
         phi = d[1];
     }
-    const double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
-    const double dir[3] = {st * cp, st * sp, ct};
+    double dir[3] = {0.0, 0.0, 1.0};
+    if (plan.need_dir) {
+        double st, ct, sp, cp;
+        sincos(theta, &st, &ct);
+        sincos(phi, &sp, &cp);
+        dir[0] = st * cp;
+        dir[1] = st * sp;
+        dir[2] = ct;
+    }
     const int fInd = (m > 0) ? (int)bump8(plan.br_q[q0] / step) : 0;
 
     for (int qc = 0; qc < m; qc += MQ) {
@@ -507,59 +371,7 @@ __global__ void __launch_bounds__(128) average_kernel(int Lp, double step, const
             qv[k] = (k < mq) ? plan.br_q[q0 + qc + k] : 0.0;
             frac[k] = (T)(bump8(qv[k] / step) - (double)fInd);
         }
-        if (valid) {
-            for (int mi = 0; mi < n_models; ++mi) {
-                const ModelDev& M = models[mi];
-                const V4* g = reinterpret_cast<const V4*>(M.grid);
-                const int ng = M.n_groups > 0 ? M.n_groups : 1;
-                for (int gi = 0; gi < ng; ++gi) {
-                    double n0 = dir[0], n1 = dir[1], n2 = dir[2];
-                    if (M.n_groups > 0) {
-                        const double* Rg = M.group_R + 9 * gi;
-                        double a0 = n0 * Rg[0] + n1 * Rg[3] + n2 * Rg[6];
-                        double a1 = n0 * Rg[1] + n1 * Rg[4] + n2 * Rg[7];
-                        double a2 = n0 * Rg[2] + n1 * Rg[5] + n2 * Rg[8];
-                        const double nr = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
-                        n0 = a0 / nr; n1 = a1 / nr; n2 = a2 / nr;
-                    }
-                    // leaf placement (Amplitude.cpp:3553-3579)
-                    const double t0 = n0 * M.R[0] + n1 * M.R[3] + n2 * M.R[6];
-                    const double t1 = n0 * M.R[1] + n1 * M.R[4] + n2 * M.R[7];
-                    const double t2 = n0 * M.R[2] + n1 * M.R[5] + n2 * M.R[8];
-                    const double dotR = t0 * M.tr[0] + t1 * M.tr[1] + t2 * M.tr[2];
-                    double nth, nph;
-                    dir_angles(t0, t1, t2, nth, nph);
-                    Cx<T> pl1, pl2, d1, d2;
-                    planes<T>(g, Lp, fInd, nth, nph, pl1, pl2, d1, d2);
-                    Cx<T> val[MQ];
-#pragma unroll
-                    for (int k = 0; k < MQ; ++k) {
-                        if (k < mq) {
-                            val[k] = hermite<T>(pl1, pl2, d1, d2, frac[k]);
-                            if (dotR != 0.0) val[k] = cmul(val[k], expi<T>(dotR * qv[k]));
-                        }
-                    }
-                    if (M.n_groups > 0) {
-                        Cx<T> tp[MQ];
-#pragma unroll
-                        for (int k = 0; k < MQ; ++k) tp[k] = {T(0), T(0)};
-                        for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
-                            const double* tt = M.trans + 3 * c;
-                            const double a = dir[0] * tt[0] + dir[1] * tt[1] + dir[2] * tt[2];
-#pragma unroll
-                            for (int k = 0; k < MQ; ++k)
-                                if (k < mq) tp[k] = cadd(tp[k], expi<T>(a * qv[k]));
-                        }
-#pragma unroll
-                        for (int k = 0; k < MQ; ++k)
-                            if (k < mq) val[k] = cscale(cmul(val[k], tp[k]), (T)M.sym_scale);
-                    }
-#pragma unroll
-                    for (int k = 0; k < MQ; ++k)
-                        if (k < mq) A[k] = cadd(A[k], val[k]);
-                }
-            }
-        }
+        if (valid) sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
         // |A|^2, block reduction in FP64
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
@@ -636,42 +448,204 @@ __global__ void unpack_kernel(const double* __restrict__ vals, const double* __r
     g[i] = x;
 }
 
+// --------------------------------------------------------------------------
+// VEGAS over (u, v) in [0,1)^2, theta = acos(1 - 2u), phi = 2 pi v, with
+// 32 x 32 bins (HybridOA.cu:182-501, GPUHybridCalc.cu:581-720).  Uniforms come
+// from a keyed counter (SplitMix64 finalizer, Steele, Lea & Flood 2014) so the
+// points are reproducible: u01(seed, (bracket << 32) | iteration, n).
+// --------------------------------------------------------------------------
+constexpr int kVegasBins = 32;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double uniform01(uint64_t seed, uint64_t key, uint64_t n) {
+    const uint64_t s = mix64(seed ^ (key * 0xD1342543DE82EF95ull));
+    return (double)(mix64(s + n) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// One thread per point: its bin, its (theta, phi), |A(q)|^2 for the bracket's q.
+template <typename T, int MQ>
+__global__ void __launch_bounds__(128) vegas_points_kernel(int Lp, double step, const ModelDev* __restrict__ models,
+                                                           int n_models, int need_dir, const double* __restrict__ q,
+                                                           int m, int ppi, int ppb, uint64_t seed, uint64_t key,
+                                                           const double* __restrict__ bounds,
+                                                           const int* __restrict__ done, double* __restrict__ I) {
+    if (*done) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= ppi) return;
+    const int bin = p / ppb, th = bin / kVegasBins, ph = bin % kVegasBins;
+    const double* tb = bounds;
+    const double* pb = bounds + kVegasBins + 1;
+    const double r1 = uniform01(seed, key, 2 * (uint64_t)p), r2 = uniform01(seed, key, 2 * (uint64_t)p + 1);
+    const double theta = acos(1. - 2. * (r1 * (tb[th + 1] - tb[th]) + tb[th]));
+    const double phi = (r2 * (pb[ph + 1] - pb[ph]) + pb[ph]) * 2. * kPi;
+    double dir[3] = {0.0, 0.0, 1.0};
+    if (need_dir) {
+        double st, ct, sp, cp;
+        sincos(theta, &st, &ct);
+        sincos(phi, &sp, &cp);
+        dir[0] = st * cp;
+        dir[1] = st * sp;
+        dir[2] = ct;
+    }
+    const int fInd = (int)bump8(q[0] / step);
+    for (int qc = 0; qc < m; qc += MQ) {
+        const int mq = min(MQ, m - qc);
+        Cx<T> A[MQ];
+        T frac[MQ];
+        double qv[MQ];
+#pragma unroll
+        for (int k = 0; k < MQ; ++k) {
+            A[k] = {T(0), T(0)};
+            qv[k] = (k < mq) ? q[qc + k] : 0.0;
+            frac[k] = (T)(bump8(qv[k] / step) - (double)fInd);
+        }
+        sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+#pragma unroll
+        for (int k = 0; k < MQ; ++k)
+            if (k < mq)
+                I[(int64_t)p * m + qc + k] = (double)A[k].r * (double)A[k].r + (double)A[k].i * (double)A[k].i;
+    }
+}
+
+// ResizeVegasPoints (HybridOA.cu:182-268) for one dimension, one thread.
+__device__ void vegas_resize(double* bounds, const double* var, int n, double* w, double* nb) {
+    double total = 0;
+    for (int i = 0; i < n; ++i) total += var[i];
+    if (total == 0.) return;
+    for (int i = 0; i < n; ++i) {
+        const double b = (i == 0) ? (var[0] + var[1]) / 2.
+                                  : (i == n - 1 ? (var[n - 1] + var[n - 2]) / 2. : (var[i - 1] + var[i] + var[i + 1]) / 3.);
+        const double r = total / b;
+        double wi = pow((r - 1.) / (r * log(r)), 1.5);
+        if (wi != wi) wi = 0.;
+        w[i] = wi;
+        nb[i] = bounds[n];
+    }
+    double tw = 0;
+    for (int i = 0; i < n; ++i) tw += w[i];
+    double xold, xnew = 0., dw = 0., pts = tw / n;
+    int j = 0;
+    for (int i = 0; i < n; ++i) {
+        dw += w[i];
+        xold = xnew;
+        xnew = bounds[i + 1];
+        for (; dw > pts; ++j) {
+            dw -= pts;
+            if (j < n) nb[j] = xnew - dw * (xnew - xold) / w[i];
+        }
+    }
+    for (int k = 0; k < n - 1; ++k) bounds[1 + k] = nb[k];
+}
+
+// One block of 32 x 32 threads (one per bin): the bracket's estimate
+// (HybridVEGASBinReduceToIKernel), the per-bin variances
+// (HybridVEGASBinReduceKernel), the bin refinement, the running mean over
+// iterations and the convergence test (checkConvergenceOA).
+__global__ void __launch_bounds__(1024) vegas_update_kernel(double* __restrict__ bounds, const double* __restrict__ I,
+                                                            int m, int ppb, int it, double eps, double* __restrict__ hist,
+                                                            int* __restrict__ done, double* __restrict__ res,
+                                                            const int* __restrict__ qidx) {
+    if (*done) return;
+    constexpr int NB = kVegasBins * kVegasBins;
+    __shared__ double sb[2 * kVegasBins + 2];
+    __shared__ double red[NB];
+    __shared__ double m2[NB];
+    __shared__ double var[2 * kVegasBins];
+    __shared__ double scratch[4 * kVegasBins];
+    const int bin = threadIdx.x, th = bin / kVegasBins, ph = bin % kVegasBins;
+    if (bin < 2 * kVegasBins + 2) sb[bin] = bounds[bin];
+    __syncthreads();
+    const double* tb = sb;
+    const double* pb = sb + kVegasBins + 1;
+    const double vol = (tb[th + 1] - tb[th]) * (pb[ph + 1] - pb[ph]);
+    const double* Ib = I + (int64_t)bin * ppb * m;
+    for (int k = 0; k < m; ++k) {
+        double s = 0;
+        for (int p = 0; p < ppb; ++p) s += Ib[(int64_t)p * m + k];
+        red[bin] = s * (vol / ppb);
+        __syncthreads();
+        for (int o = NB / 2; o > 0; o >>= 1) {
+            if (bin < o) red[bin] += red[bin + o];
+            __syncthreads();
+        }
+        if (bin == 0) {
+            const double est = red[0];
+            const double run = (it == 0) ? est : (hist[(int64_t)(it - 1) * m + k] * it + est) / (it + 1);
+            hist[(int64_t)it * m + k] = run;
+            res[qidx[k]] = run;
+        }
+        __syncthreads();
+    }
+    double mean = 0, M2 = 0;
+    for (int p = 0; p < ppb; ++p) {
+        double sq = 0;
+        for (int k = 0; k < m; ++k) sq += Ib[(int64_t)p * m + k];
+        const double diff = vol * sq - mean;
+        mean += diff / (double)(p + 1);
+        M2 += diff * diff * (double)p / (double)(p + 1);
+    }
+    m2[bin] = M2 * ppb;
+    __syncthreads();
+    if (bin < kVegasBins) {
+        double a = 0;
+        for (int j = 0; j < kVegasBins; ++j) a += m2[bin * kVegasBins + j];
+        var[bin] = a;
+    } else if (bin < 2 * kVegasBins) {
+        const int c = bin - kVegasBins;
+        double a = 0;
+        for (int j = 0; j < kVegasBins; ++j) a += m2[j * kVegasBins + c];
+        var[bin] = a;
+    }
+    __syncthreads();
+    if (bin == 0) {
+        double* sbw = const_cast<double*>(sb);
+        vegas_resize(sbw, var, kVegasBins, scratch, scratch + kVegasBins);
+        vegas_resize(sbw + kVegasBins + 1, var + kVegasBins, kVegasBins, scratch + 2 * kVegasBins,
+                     scratch + 3 * kVegasBins);
+        for (int j = 0; j < 2 * kVegasBins + 2; ++j) bounds[j] = sb[j];
+        if (it > 2 && eps > 0.0) {
+            bool conv = true;
+            for (int k = 0; k < m && conv; ++k) {
+                const double r = hist[(int64_t)it * m + k];
+                for (int d = 1; d <= 3; ++d)
+                    if (fabs(1.0 - r / hist[(int64_t)(it - d) * m + k]) > eps) { conv = false; break; }
+            }
+            if (conv) *done = 1;
+        }
+    }
+}
+
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
-                            const Geom& g, const double center[3], float scale, float4* grid, int cells_per_thread,
-                            int block, int64_t cell_lo, int64_t cell_hi) {
-    const int64_t n = cell_hi - cell_lo;
-    if (n <= 0) return cudaSuccess;
-    const int use_center = (center[0] != 0.0 || center[1] != 0.0 || center[2] != 0.0);
-#define DPX_FILL_CASE(CPT, TH)                                                                                   \
-    if (cells_per_thread == CPT && block == TH) {                                                              \
-        fill_f32_kernel<CPT, TH><<<blocks_for(n, CPT * TH), TH, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step,  \
-                                                                       center[0], center[1], center[2],        \
-                                                                       use_center, scale, grid, cell_lo,       \
-                                                                       cell_hi);                               \
-        return cudaGetLastError();                                                                             \
-    }
-    DPX_FILL_CASE(1, 128) DPX_FILL_CASE(2, 128) DPX_FILL_CASE(4, 128) DPX_FILL_CASE(8, 128)
-    DPX_FILL_CASE(1, 256) DPX_FILL_CASE(2, 256) DPX_FILL_CASE(4, 256) DPX_FILL_CASE(8, 256)
-    DPX_FILL_CASE(2, 512) DPX_FILL_CASE(4, 512)
-#undef DPX_FILL_CASE
-    return cudaErrorInvalidValue;
-}
-
-cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
-                            const Geom& g, const double center[3], double scale, double4_32a* grid, int64_t cell_lo,
-                            int64_t cell_hi) {
-    const int64_t n = cell_hi - cell_lo;
-    if (n <= 0) return cudaSuccess;
-    fill_f64_kernel<128><<<blocks_for(n, 128), 128, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step, center[0],
-                                                           center[1], center[2], scale, grid, cell_lo, cell_hi);
+cudaError_t launch_vegas_points(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                                int need_dir, const double* d_q, int m, int ppi, uint64_t seed, uint64_t key,
+                                const double* d_bounds, const int* d_done, double* d_I) {
+    const int ppb = ppi / (kVegasBins * kVegasBins);
+    if (fp64)
+        vegas_points_kernel<double, 4><<<blocks_for(ppi, 128), 128, 0, s>>>(
+            g.Lp, g.step, d_models, n_models, need_dir, d_q, m, ppi, ppb, seed, key, d_bounds, d_done, d_I);
+    else
+        vegas_points_kernel<float, 4><<<blocks_for(ppi, 128), 128, 0, s>>>(
+            g.Lp, g.step, d_models, n_models, need_dir, d_q, m, ppi, ppb, seed, key, d_bounds, d_done, d_I);
     return cudaGetLastError();
 }
 
+cudaError_t launch_vegas_update(cudaStream_t s, double* d_bounds, const double* d_I, int m, int ppi, int it,
+                                double eps, double* d_hist, int* d_done, double* d_res, const int* d_qidx) {
+    vegas_update_kernel<<<1, kVegasBins * kVegasBins, 0, s>>>(d_bounds, d_I, m, ppi / (kVegasBins * kVegasBins), it,
+                                                              eps, d_hist, d_done, d_res, d_qidx);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid) {
     splines_kernel<float, 14><<<blocks_for(g.P, 256), 256, 0, s>>>(grid, g.P);
     return cudaGetLastError();

@@ -231,9 +231,7 @@ class DomainModel:
             out.append(leaf.calculateGrid(ctx, self.qMax, self.gridSize, self.precision))
         return out
 
-    def CalculateIntensityVector(self, ctx: Context, Q: Sequence[float], epsi: float, iterations: int,
-                                 dirs: np.ndarray, dir_layer_stride: int = 0) -> np.ndarray:
-        Q = np.ascontiguousarray(Q, dtype=np.float64)
+    def _model_args(self, ctx: Context):
         grids = self.grids(ctx)
         n = len(self.amps)
         rot = np.zeros(3 * n)
@@ -252,11 +250,31 @@ class DomainModel:
         crot = np.ascontiguousarray(np.concatenate(crot) if crot else np.zeros(3))
         ctr = np.ascontiguousarray(np.concatenate(ctr) if ctr else np.zeros(3))
         gh = (C.c_void_p * n)(*[g.handle.value for g in grids])
+        # the arrays must stay alive for the call: return them together
+        return (n, gh, rot, tr, ncop, crot, ctr, sscale), (grids,)
+
+    def CalculateIntensityVector(self, ctx: Context, Q: Sequence[float], epsi: float, iterations: int,
+                                 dirs: np.ndarray | None = None, dir_layer_stride: int = 0, method: str = "MC",
+                                 seed: int = 0, points_per_iter: int = 4096) -> np.ndarray:
+        """I(q) by the orientation method of Amplitude.cpp:736-842: "MC" averages
+        over the given directions (``iterations`` per bracket); "VEGAS" iterates
+        ``points_per_iter`` points until ``iterations`` points or convergence."""
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        (n, gh, rot, tr, ncop, crot, ctr, sscale), keep = self._model_args(ctx)
         res = np.zeros(len(Q))
-        d = np.ascontiguousarray(dirs, dtype=np.float64)
-        check(lib().dpx_orientation_average(ctx.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
-                                            dptr(sscale), len(Q), dptr(Q), d.ctypes.data_as(C.c_void_p), 0,
-                                            dir_layer_stride, iterations, epsi, dptr(res)))
+        if method == "MC":
+            d = np.ascontiguousarray(dirs, dtype=np.float64)
+            check(lib().dpx_orientation_average(ctx.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot),
+                                                dptr(ctr), dptr(sscale), len(Q), dptr(Q),
+                                                d.ctypes.data_as(C.c_void_p), 0, dir_layer_stride, iterations, epsi,
+                                                dptr(res)))
+        elif method == "VEGAS":
+            check(lib().dpx_vegas_intensity(ctx.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
+                                            dptr(sscale), len(Q), dptr(Q), seed, points_per_iter, iterations, epsi,
+                                            dptr(res)))
+        else:
+            raise ValueError(f"unknown orientation method {method!r}")
+        del keep
         return res
 
 

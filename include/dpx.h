@@ -65,8 +65,9 @@ int dpx_ctx_destroy(dpx_ctx ctx);
 int dpx_ctx_set_stream(dpx_ctx ctx, void* stream);
 void* dpx_ctx_get_stream(dpx_ctx ctx);
 int dpx_ctx_synchronize(dpx_ctx ctx);
-/* Amplitude-kernel launch shape (cells per thread x threads per block);
- * chosen by the autotuner, defaults 4 x 256. */
+/* FP32 amplitude-kernel launch shape: phi cells per work item x threads per
+ * block, chosen by the autotuner (default 8 x 128).  Supported: 2x256, 4x128,
+ * 4x256, 6x128, 6x256, 8x128, 8x256. */
 int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cells_per_thread, int threads);
 
 /* ---- grid geometry (Grid.cpp:169-200): P = 6 L'(L'+1)^2 + 1, L' = grid_size/2 + 3 ---- */
@@ -112,6 +113,20 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
                             const double* copy_tr, const double* sym_scale, int nq, const double* Q,
                             const double* dirs, int dirs_on_device, int64_t dir_layer_stride,
                             int64_t n_samples, double eps, double* res);
+
+/* VEGAS orientation average (the reference's GPU-only method,
+ * HybridOA.cu:182-501 / GPUHybridCalc.cu:581-720, driven by
+ * DomainModel::CalculateIntensityVector, Amplitude.cpp:737-754): 32 x 32 bins over
+ * (u, v), theta = acos(1 - 2u), phi = 2 pi v; points_per_iter points per
+ * iteration (a multiple of 1024; the reference uses 4096), iterations until
+ * max_points or the reference's 3-iteration convergence test at eps; the bin
+ * grid carries over between brackets as in the reference.  Uniforms come from
+ * a counter-based stream keyed by (seed, bracket, iteration), so results are
+ * reproducible.  Model arguments as dpx_orientation_average. */
+int dpx_vegas_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                        const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                        int nq, const double* Q, uint64_t seed, int points_per_iter, int64_t max_points, double eps,
+                        double* res);
 
 /* ---- seeded direction streams (product-side restatement of the reference's draws) ---- */
 /* D pairs (theta, phi) from std::mt19937(seed) with u2, v2 ~ U[0,2): phi = pi u2, theta = acos(v2 - 1) */

@@ -380,10 +380,10 @@ inline void dir_to_angles(const double v[3], double& th, double& ph) {
 void leaf_amps(const GridView& G, const double Rm[9], const double tr[3], int nq, const double* qs,
                double theta, double phi, cd* out, std::vector<cd>& tmp) {
     double st = std::sin(theta), ct = std::cos(theta), sp = std::sin(phi), cp = std::cos(phi);
-    double Q = qs[0];
-    double qc[3] = {Q * st * cp, Q * st * sp, Q * ct}, qt[3];
+    /* the reference forms Q (st cp, st sp, ct) R / Q; the unit direction gives
+     * the same vector and stays defined at q = 0 */
+    double qc[3] = {st * cp, st * sp, ct}, qt[3];
     row_times(qc, Rm, qt);
-    qt[0] /= Q; qt[1] /= Q; qt[2] /= Q;
     double nth, nph;
     dir_to_angles(qt, nth, nph);
     double dotR = qt[0] * tr[0] + qt[1] * tr[1] + qt[2] * tr[2];
@@ -774,6 +774,135 @@ void orc_direct_intensity(int64_t N, const double* xyz, int U, const int* atoms_
         }
         res[k] = acc / double(D);
     }
+}
+
+double orc_uniform(uint64_t seed, uint64_t key, uint64_t n) {
+    /* SplitMix64 finalizer (Steele, Lea & Flood 2014) over a keyed counter */
+    auto mix = [](uint64_t x) {
+        x += 0x9E3779B97F4A7C15ull;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        return x ^ (x >> 31);
+    };
+    const uint64_t s = mix(seed ^ (key * 0xD1342543DE82EF95ull));
+    return double(mix(s + n) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+namespace {
+/* ResizeVegasPoints (HybridOA.cu:182-268) for one dimension of n bins */
+void vegas_resize(double* bounds, const double* var, int n) {
+    double total = 0;
+    for (int i = 0; i < n; i++) total += var[i];
+    if (total == 0.) return;
+    std::vector<double> w(n), nb(n, bounds[n]);
+    for (int i = 0; i < n; i++) {
+        double b;
+        if (i == 0) b = (var[0] + var[1]) / 2.;
+        else if (i == n - 1) b = (var[n - 1] + var[n - 2]) / 2.;
+        else b = (var[i - 1] + var[i] + var[i + 1]) / 3.;
+        double r = total / b;
+        w[i] = std::pow((r - 1.) / (r * std::log(r)), 1.5);
+        if (w[i] != w[i]) w[i] = 0.;
+    }
+    double tw = 0;
+    for (int i = 0; i < n; i++) tw += w[i];
+    double xold, xnew = 0., dw = 0., pts = tw / n;
+    int j = 0;
+    for (int i = 0; i < n; i++) {
+        dw += w[i];
+        xold = xnew;
+        xnew = bounds[i + 1];
+        for (; dw > pts; j++) {
+            dw -= pts;
+            if (j < n) nb[j] = xnew - dw * (xnew - xold) / w[i];
+        }
+    }
+    for (int k = 0; k < n - 1; k++) bounds[1 + k] = nb[k];
+}
+}  // namespace
+
+int orc_vegas_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq, const double* Q,
+                        uint64_t seed, int points_per_iter, int64_t max_points, double eps, double* res) {
+    const int TB = 32, PB = 32, NB = TB * PB;
+    if (points_per_iter <= 0 || points_per_iter % NB) return -1;
+    const int ppb = points_per_iter / NB;
+    std::vector<LeafModel> models;
+    for (int l = 0; l < n_leaves; l++) models.push_back(make_model(grid_size, qmax, leaves[l]));
+    const double step = qmax / (grid_size / 2);
+    std::vector<double> bounds(TB + PB + 2);
+    for (int i = 0; i <= TB; i++) bounds[i] = double(i) / TB;
+    for (int i = 0; i <= PB; i++) bounds[1 + TB + i] = double(i) / PB;
+    double* tb = bounds.data();
+    double* pb = bounds.data() + TB + 1;
+    int qInd = 0, lower = 0, bracket = 0;
+    std::vector<cd> t1, t2, one, amp;
+    do {
+        /* GPUHybridCalc.cu:365-375 */
+        while (Q[qInd] > double(lower + 1) * step) lower++;
+        int qEnd;
+        for (qEnd = qInd + 1; qEnd < nq; qEnd++)
+            if (Q[qEnd] > double(lower + 1) * step) break;
+        qEnd--;
+        const int m = qEnd - qInd + 1;
+        const double* qs = Q + qInd;
+        std::vector<double> I((size_t)points_per_iter * m), run(m, 0.0);
+        std::vector<std::vector<double>> hist;
+        one.resize(m);
+        amp.resize(m);
+        for (int it = 0;; it++) {
+            const uint64_t key = (uint64_t(bracket) << 32) | uint64_t(it);
+            for (int p = 0; p < points_per_iter; p++) {
+                const int bin = p / ppb, th = bin / PB, ph = bin % PB;
+                const double r1 = orc_uniform(seed, key, 2 * uint64_t(p)), r2 = orc_uniform(seed, key, 2 * uint64_t(p) + 1);
+                const double theta = std::acos(1. - 2. * (r1 * (tb[th + 1] - tb[th]) + tb[th]));
+                const double phi = (r2 * (pb[ph + 1] - pb[ph]) + pb[ph]) * 2. * kPi;
+                for (int k = 0; k < m; k++) amp[k] = 0;
+                for (auto& M : models) {
+                    model_amps(M, m, qs, theta, phi, one.data(), t1, t2);
+                    for (int k = 0; k < m; k++) amp[k] += one[k];
+                }
+                for (int k = 0; k < m; k++) I[(size_t)p * m + k] = std::real(amp[k] * std::conj(amp[k]));
+            }
+            /* HybridVEGASBinReduceToIKernel / HybridVEGASBinReduceKernel (HybridOA.cu:301-449) */
+            std::vector<double> est(m, 0.0), thv(TB, 0.0), phv(PB, 0.0);
+            for (int bin = 0; bin < NB; bin++) {
+                const int th = bin / PB, ph = bin % PB;
+                const double vol = (tb[th + 1] - tb[th]) * (pb[ph + 1] - pb[ph]);
+                for (int k = 0; k < m; k++) {
+                    double s = 0;
+                    for (int p = 0; p < ppb; p++) s += I[(size_t)(bin * ppb + p) * m + k];
+                    est[k] += s * (vol / ppb);
+                }
+                double mean = 0, m2 = 0;
+                for (int p = 0; p < ppb; p++) {
+                    double sq = 0;
+                    for (int k = 0; k < m; k++) sq += I[(size_t)(bin * ppb + p) * m + k];
+                    const double diff = vol * sq - mean;
+                    mean += diff / double(p + 1);
+                    m2 += diff * diff * double(p) / double(p + 1);
+                }
+                thv[th] += m2 * ppb;
+                phv[ph] += m2 * ppb;
+            }
+            vegas_resize(tb, thv.data(), TB);
+            if (PB > 2) vegas_resize(pb, phv.data(), PB);
+            for (int k = 0; k < m; k++) run[k] = (it == 0) ? est[k] : (run[k] * it + est[k]) / (it + 1);
+            hist.push_back(run);
+            bool conv = false;
+            if (it > 2 && eps > 0.0) { /* checkConvergenceOA (GPUHybridCalc.cu:706-720) */
+                conv = true;
+                for (int k = 0; k < m && conv; k++)
+                    for (int d = 1; d <= 3; d++)
+                        if (std::fabs(1.0 - run[k] / hist[it - d][k]) > eps) { conv = false; break; }
+            }
+            if (conv || int64_t(it + 1) * points_per_iter >= max_points) break;
+        }
+        for (int k = 0; k < m; k++) res[qInd + k] = run[k];
+        qInd = qEnd + 1;
+        lower++;
+        bracket++;
+    } while (qInd < nq);
+    return 0;
 }
 
 double orc_gk_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, double q, double eps,

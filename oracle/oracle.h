@@ -104,6 +104,17 @@ int orc_integrate_layers(int grid_size, double qmax, int n_leaves, const orc_lea
  * layers win where two brackets claim the same q. */
 void orc_q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q);
 
+/* ---- VEGAS (restated from the reference's GPU-only implementation,
+ * HybridOA.cu:182-501 and GPUHybridCalc.cu:326-333, 363-375, 581-720) ----
+ * 32 x 32 bins over (u, v) in [0,1)^2 with theta = acos(1 - 2u), phi = 2 pi v;
+ * points_per_iter points per iteration (a multiple of 1024), uniforms from the
+ * counter-based stream orc_uniform(seed, (bracket << 32) | iteration, n); the
+ * bin grid carries over from bracket to bracket, as in the reference.
+ * Brackets follow the hybrid path's rule (GPUHybridCalc.cu:363-375). */
+double orc_uniform(uint64_t seed, uint64_t key, uint64_t n);
+int orc_vegas_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq, const double* Q,
+                        uint64_t seed, int points_per_iter, int64_t max_points, double eps, double* res);
+
 /* ---- FP64 direct-sum oracle (no grid) ----
  * F(q n) = sum_j f_j(q) e^{i q n.r_j} for a placed leaf with optional docked
  * copies; I(q) = mean over the given directions of |F|^2. */
