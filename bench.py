@@ -32,6 +32,10 @@ sys.path.insert(0, os.path.join(ROOT, "dplus-dev_gb300"))
 N_ATOMS, RADIUS, SEED = 20000, 5.0, 20251
 GRID_SIZE, QMAX, NQ = 400, 7.5, 500
 N_DIRS, DIR_SEED = 100_000, 1234
+FILL_CPT = 8  # the default FP32 fill shape (cells per work item x 128 threads)
+# ncu dram__bytes_read+write of fill_f32_kernel on the profile shape (2,000 atoms,
+# 120 layers, 11.3 M cells): 335 MB, i.e. 29.6 B per cell; scaled to 50.7 M cells
+FILL_TRAFFIC = 29.6 * 50688289
 EXTRA = [1, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 4]  # scale, solventED, c1, ..., radType 4 (dummy atoms)
 CONFIG = {"workload": "single subunit, 20,000-atom globule r=5 nm, dummy-atom solvent 333 e/nm^3, "
                       "L=200 (50,688,289 cells), qmax 7.5, 500 q, MC 1e5 fixed directions",
@@ -243,12 +247,14 @@ def run_dpx(args):
         spl_ms = float(np.median(times["splines"]))
         P = L.dpx_grid_cells(GRID_SIZE)
         lp = GRID_SIZE // 2 + 3
-        P_src = 3 * lp * (lp + 1) ** 2 + 1  # Friedel half actually evaluated
-        pairs = float(N_ATOMS) * P_src
-        # SFU roofline: 2 MUFU ops (sin, cos) per evaluated atom-cell pair,
-        # 16 MUFU lanes/SM/clk, 152 SMs, at the maximum SM clock
-        sfu_peak = 152 * 16 / 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e9  # Gpair/s
-        achieved = pairs / (fill_ms / 1e3) / 1e9
+        cpt = FILL_CPT
+        # row-factored fill: per work item (CPT cells of a theta row, each with its
+        # z-mirror) and atom, 1 + CPT sincos = 2 (1 + CPT) SFU ops
+        items = 1 + sum((3 * i // 2 + 1) * ((3 * i + cpt - 1) // cpt) for i in range(1, lp + 1))
+        sfu_ops = float(N_ATOMS) * items * 2 * (1 + cpt)
+        # SFU roofline: 16 MUFU lanes/SM/clk x 152 SMs at the maximum SM clock
+        sfu_peak = 152 * 16 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12  # Tops/s
+        achieved = sfu_ops / (fill_ms / 1e3) / 1e12
         n_brackets = GRID_SIZE // 2
         interp_bytes = float(N_DIRS) * n_brackets * (4 * 4 * 2 * 16)  # 4 planes x 4 rows x 2 nodes x 16 B
         out = {
@@ -261,9 +267,10 @@ def run_dpx(args):
                     "d2h_bytes_per_step": int(res.nbytes)},
             "gpu_launches": args.steps * 4,
             "roofline": {"bound": "sfu", "kernel": "fill_f32_kernel", "achieved": achieved, "peak": sfu_peak,
-                         "unit": "Gpair/s", "frac": achieved / sfu_peak, "traffic": None,
-                         "note": "evaluated pairs = atoms x Friedel-half cells; peak = 152 SM x 16 MUFU/clk / "
-                                 "2 MUFU per pair at sm_max_mhz (derived, not in MEASURED_PEAKS.json)",
+                         "unit": "T SFU-op/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
+                         "note": "SFU ops = atoms x work items x 2(1+CPT) (row-factored fill); peak = 152 SM x 16 "
+                                 "MUFU/clk at sm_max_mhz (derived, not in MEASURED_PEAKS.json); traffic = ncu "
+                                 "dram bytes of the profile shape scaled by cells",
                          "algorithmic_pairs_per_s": float(N_ATOMS) * P / (fill_ms / 1e3)},
             "roofline_average": {"bound": "hbm", "kernel": "average_kernel",
                                  "achieved": interp_bytes / (avg_ms / 1e3) / 1e9, "peak": peaks["hbm_gbs"],

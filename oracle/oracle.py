@@ -224,3 +224,22 @@ def direct_intensity(s: Struct, Q, dirs, copy_rot=None, copy_tr=None, nthreads=0
 def gk_intensity(grid_size, qmax, leaves, q, eps, max_depth):
     arr = (Leaf * len(leaves))(*leaves)
     return lib().orc_gk_intensity(grid_size, qmax, len(leaves), arr, q, eps, max_depth)
+
+
+def vegas_intensity(grid_size, qmax, leaves, Q, seed, points_per_iter, max_points, eps):
+    L = lib()
+    if not getattr(L, "_vegas_typed", False):
+        L.orc_vegas_intensity.restype = C.c_int
+        L.orc_vegas_intensity.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(Leaf), C.c_int, _D, C.c_uint64,
+                                          C.c_int, C.c_int64, C.c_double, _D]
+        L.orc_uniform.restype = C.c_double
+        L.orc_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
+        L._vegas_typed = True
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    arr = (Leaf * len(leaves))(*leaves)
+    res = np.zeros(len(Q))
+    rc = L.orc_vegas_intensity(grid_size, qmax, len(leaves), arr, len(Q), Q.ctypes.data_as(_D), seed,
+                               points_per_iter, max_points, eps, res.ctypes.data_as(_D))
+    if rc != 0:
+        raise ValueError("bad VEGAS arguments")
+    return res

@@ -246,3 +246,35 @@ def test_grid_reuse_is_device_resident(ctx):
     amp.set_extra([2, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 4])
     g3 = amp.calculateGrid(ctx, 3.0, 12, M.FP32)
     assert g3 is not g1
+
+
+@pytest.mark.parametrize("prec,tol,docked", [(M.FP64, TOL64, False), (M.FP32, TOL32, False), (M.FP64, TOL64, True),
+                                             (M.FP32, TOL32, True)])
+def test_vegas_matches_oracle(ctx, prec, tol, docked):
+    """VEGAS: same points (keyed counter stream), same bin refinement carried
+    across brackets, same running mean and convergence test as the restatement."""
+    amp = globule(250, 1.1, seed=21)
+    gs, qmax = 24, 4.0
+    Q = np.linspace(0, 4, 37)
+    if docked:
+        rows = [[0, 0, 0, 0, 0, 0], [2.5, 0, 0, 0, 0, 90], [0, 3.0, 1.0, 45, 30, 10]]
+        model = M.ManualSymmetry(amp, rows, scale=1.3)
+    else:
+        model = amp
+    dom = M.DomainModel([model], gs, qmax, prec)
+    I = dom.CalculateIntensityVector(ctx, Q, 1e-3, 6 * 2048, method="VEGAS", seed=99, points_per_iter=2048)
+    data, co = oracle_grid(amp, gs, qmax)
+    keep = []
+    if docked:
+        leaf = O.make_leaf(data, co, copy_rot=model.rot, copy_tr=model.trans, sym_scale=1.3, keep=keep)
+    else:
+        leaf = O.make_leaf(data, co)
+    ref = O.vegas_intensity(gs, qmax, [leaf], Q, 99, 2048, 6 * 2048, 1e-3)
+    assert rel(I, ref) <= tol
+
+
+def test_vegas_rejects_bad_point_counts(ctx):
+    amp = globule(50, 0.6, seed=22)
+    dom = M.DomainModel([amp], 10, 3.0, M.FP32)
+    with pytest.raises(dpx.DpxError):
+        dom.CalculateIntensityVector(ctx, np.linspace(0, 3, 5), 0.0, 5000, method="VEGAS", points_per_iter=1000)
