@@ -772,6 +772,145 @@ int dpx_vegas_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const 
     return DPX_OK;
 }
 
+int dpx_gk_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                     const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                     int nq, const double* Q, double eps, int64_t max_depth, double* res) {
+    if (!ctx || n_models <= 0 || !grids || nq <= 0 || !Q || !res) return fail(DPX_ERR_ARG, "NULL or empty argument");
+    const int grid_size = grids[0]->grid_size;
+    const double qmax = grids[0]->qmax;
+    const int prec = grids[0]->precision;
+    for (int m = 0; m < n_models; ++m)
+        if (!grids[m] || grids[m]->grid_size != grid_size || grids[m]->qmax != qmax || grids[m]->precision != prec)
+            return fail(DPX_ERR_ARG, "all models must share grid_size, qmax and precision");
+    for (int k = 0; k < nq; ++k)
+        if (!(Q[k] >= 0)) return fail(DPX_ERR_ARG, "negative q");
+    const Geom& G = grids[0]->g;
+    for (int k = 0; k < nq; ++k)
+        if (Q[k] > G.L * G.step * (1.0 + 1e-12)) return fail(DPX_ERR_ARG, "q=%g beyond the grid's qmax", Q[k]);
+    if (int rc = set_device(ctx)) return rc;
+    cudaStream_t s = ctx->stream;
+    std::vector<dpx::ModelDev> md;
+    std::vector<char> gstage;
+    if (int rc = prepare_models(ctx, n_models, grids, rot, tr, n_copies, copy_rot, copy_tr, sym_scale, md, gstage))
+        return rc;
+    DPX_CUDA(ctx->models.reserve(md.size() * sizeof(dpx::ModelDev)));
+    DPX_CUDA(cudaMemcpyAsync(ctx->models.p, md.data(), md.size() * sizeof(dpx::ModelDev), cudaMemcpyHostToDevice, s));
+    DPX_CUDA(cudaMemcpyAsync(ctx->groups.p, gstage.data(), gstage.size(), cudaMemcpyHostToDevice, s));
+    const dpx::ModelDev* d_models = (const dpx::ModelDev*)ctx->models.p;
+
+    // the 7/15 rule (the standard published Gauss-Kronrod pair)
+    static const double x15[15] = {
+        -0.9914553711208126392068547, -0.9491079123427585245261897, -0.8648644233597690727897128,
+        -0.7415311855993944398638648, -0.5860872354676911302941448, -0.4058451513773971669066064,
+        -0.2077849550078984676006894, 0.0, 0.2077849550078984676006894, 0.4058451513773971669066064,
+        0.5860872354676911302941448, 0.7415311855993944398638648, 0.8648644233597690727897128,
+        0.9491079123427585245261897, 0.9914553711208126392068547};
+    static const double w15[15] = {
+        0.0229353220105292249637320, 0.0630920926299785532907007, 0.1047900103222501838398763,
+        0.1406532597155259187451896, 0.1690047266392679028265834, 0.1903505780647854099132564,
+        0.2044329400752988924141620, 0.2094821410847278280129992, 0.2044329400752988924141620,
+        0.1903505780647854099132564, 0.1690047266392679028265834, 0.1406532597155259187451896,
+        0.1047900103222501838398763, 0.0630920926299785532907007, 0.0229353220105292249637320};
+    static const double w7[7] = {0.1294849661688696932706114, 0.2797053914892766679014678,
+                                 0.3818300505051189449503698, 0.4179591836734693877551020,
+                                 0.3818300505051189449503698, 0.2797053914892766679014678,
+                                 0.1294849661688696932706114};
+    struct ThetaIv { int q; double tmin, tmax; int64_t depth; };
+    struct Node { double st, ct, sum; };
+    struct PhiIv { int node; double pmin, pmax; int64_t depth; };
+    const int64_t kMaxTasks = 1 << 24;
+    std::vector<double> acc(nq, 0.0);
+    std::vector<ThetaIv> thetas;
+    for (int k = 0; k < nq; ++k)
+        if (Q[k] > 0.0) thetas.push_back({k, 0.0, kPi / 2, max_depth - 1});  // GaussKron2DSphereRecurs
+    std::vector<dpx::GKTask> tasks;
+    std::vector<double2> kg;
+    while (!thetas.empty()) {
+        std::vector<Node> nodes(thetas.size() * 15);
+        std::vector<PhiIv> phis;
+        for (size_t t = 0; t < thetas.size(); ++t) {
+            const double ba2 = (thetas[t].tmax - thetas[t].tmin) * 0.5, apb2 = (thetas[t].tmax + thetas[t].tmin) * 0.5;
+            for (int i = 0; i < 15; ++i) {
+                const double tv = apb2 + ba2 * x15[i];
+                nodes[t * 15 + i] = {std::sin(tv), std::cos(tv), 0.0};
+                phis.push_back({(int)(t * 15 + i), 0.0, 2.0 * kPi, thetas[t].depth});
+            }
+        }
+        while (!phis.empty()) {
+            if ((int64_t)phis.size() > kMaxTasks)
+                return fail(DPX_ERR_ARG, "Gauss-Kronrod needs more than %lld phi intervals at once; raise eps or "
+                                         "lower max_depth", (long long)kMaxTasks);
+            tasks.resize(phis.size());
+            for (size_t p = 0; p < phis.size(); ++p) {
+                const Node& nd = nodes[phis[p].node];
+                tasks[p] = {Q[thetas[phis[p].node / 15].q], nd.st, nd.ct, phis[p].pmin, phis[p].pmax};
+            }
+            kg.resize(phis.size());
+            DPX_CUDA(ctx->plan.reserve(tasks.size() * sizeof(dpx::GKTask)));
+            DPX_CUDA(ctx->partial.reserve(kg.size() * sizeof(double2)));
+            DPX_CUDA(cudaMemcpyAsync(ctx->plan.p, tasks.data(), tasks.size() * sizeof(dpx::GKTask),
+                                     cudaMemcpyHostToDevice, s));
+            cudaError_t e = dpx::launch_gk_phi(s, prec == DPX_FP64, G, n_models, d_models,
+                                               (const dpx::GKTask*)ctx->plan.p, (int)tasks.size(),
+                                               (double2*)ctx->partial.p);
+            if (e != cudaSuccess) return cuda_fail(e, "Gauss-Kronrod launch");
+            DPX_CUDA(cudaMemcpyAsync(kg.data(), ctx->partial.p, kg.size() * sizeof(double2), cudaMemcpyDeviceToHost,
+                                     s));
+            DPX_CUDA(cudaStreamSynchronize(s));
+            std::vector<PhiIv> next;
+            for (size_t p = 0; p < phis.size(); ++p) {
+                const double kv = kg[p].x, gv = kg[p].y;
+                // GaussLegPhi acceptance (Amplitude.cpp:1460)
+                if (phis[p].depth < 0 || std::fabs(1.0 - gv / kv) <= eps || gv == kv) {
+                    nodes[phis[p].node].sum += kv;
+                } else {
+                    const double mid = (phis[p].pmin + phis[p].pmax) * 0.5;
+                    next.push_back({phis[p].node, phis[p].pmin, mid, phis[p].depth - 1});
+                    next.push_back({phis[p].node, mid, phis[p].pmax, phis[p].depth - 1});
+                }
+            }
+            phis.swap(next);
+        }
+        std::vector<ThetaIv> next_t;
+        for (size_t t = 0; t < thetas.size(); ++t) {
+            const double ba2 = (thetas[t].tmax - thetas[t].tmin) * 0.5;
+            double kv = 0, gv = 0;
+            for (int i = 0; i < 15; ++i) {
+                const Node& nd = nodes[t * 15 + i];
+                kv += nd.sum * w15[i] * ba2 * nd.st;
+                if (i % 2 == 1) gv += nd.sum * w7[i / 2] * ba2 * nd.st;
+            }
+            // GaussLegTheta acceptance (Amplitude.cpp:1434)
+            if (thetas[t].depth < 0 || std::fabs(1.0 - gv / kv) <= eps || gv == kv) {
+                acc[thetas[t].q] += kv;
+            } else {
+                const double mid = (thetas[t].tmax + thetas[t].tmin) / 2.0;
+                next_t.push_back({thetas[t].q, thetas[t].tmin, mid, thetas[t].depth - 1});
+                next_t.push_back({thetas[t].q, mid, thetas[t].tmax, thetas[t].depth - 1});
+            }
+        }
+        thetas.swap(next_t);
+    }
+    // q == 0: |sum of models at the origin|^2 (CalculateIntensity, Amplitude.cpp:1477-1482)
+    double o_r = 0, o_i = 0;
+    for (int m = 0; m < n_models; ++m) {
+        double v[2] = {0, 0};
+        if (prec == DPX_FP64) {
+            DPX_CUDA(cudaMemcpy(v, grids[m]->cells, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+        } else {
+            float f[2];
+            DPX_CUDA(cudaMemcpy(f, grids[m]->cells, 2 * sizeof(float), cudaMemcpyDeviceToHost));
+            v[0] = f[0];
+            v[1] = f[1];
+        }
+        const double w = md[m].n_groups > 0 ? (n_copies ? n_copies[m] : 0) * md[m].sym_scale : 1.0;
+        o_r += w * v[0];
+        o_i += w * v[1];
+    }
+    for (int k = 0; k < nq; ++k) res[k] = (Q[k] > 0.0) ? acc[k] / (2.0 * kPi) : o_r * o_r + o_i * o_i;
+    return DPX_OK;
+}
+
 int dpx_mc_directions(uint32_t seed, int64_t D, double* theta_phi) {
     if (D < 0 || (D > 0 && !theta_phi)) return fail(DPX_ERR_ARG, "bad direction buffer");
     std::mt19937 rng;

@@ -85,6 +85,13 @@ cudaError_t launch_vegas_points(cudaStream_t s, bool fp64, const Geom& g, int n_
 cudaError_t launch_vegas_update(cudaStream_t s, double* d_bounds, const double* d_I, int m, int ppi, int it,
                                 double eps, double* d_hist, int* d_done, double* d_res, const int* d_qidx);
 
+// Gauss-Kronrod: one phi interval of one theta node of one q.
+struct GKTask {
+    double q, st, ct, pmin, pmax;
+};
+cudaError_t launch_gk_phi(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                          const GKTask* d_tasks, int n, double2* d_kg);
+
 // other kernels (dpx_kernels.cu)
 cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid);
 cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid);

@@ -621,9 +621,150 @@ __global__ void __launch_bounds__(1024) vegas_update_kernel(double* __restrict__
     }
 }
 
+// --------------------------------------------------------------------------
+// Adaptive Gauss-Kronrod (7,15) over (theta, phi) (DomainModel::GaussLegTheta /
+// GaussLegPhi, Amplitude.cpp:1416-1467).  The integrand is |sum of models|^2
+// through the single-q GetCart / GetSphr path (Grid.cpp:384-392, 487-548;
+// Amplitude::getAmplitude, Amplitude.cpp:3035-3056: the leaf phase uses the
+// q vector before the leaf rotation; ManualSymmetry::calcAmplitude,
+// Symmetries.cpp:697-716).  The host drives the recursion; this kernel
+// evaluates the 15 Kronrod nodes of a batch of phi intervals.
+// --------------------------------------------------------------------------
+__constant__ double c_x15[15] = {
+    -0.9914553711208126392068547, -0.9491079123427585245261897, -0.8648644233597690727897128,
+    -0.7415311855993944398638648, -0.5860872354676911302941448, -0.4058451513773971669066064,
+    -0.2077849550078984676006894, 0.0, 0.2077849550078984676006894, 0.4058451513773971669066064,
+    0.5860872354676911302941448, 0.7415311855993944398638648, 0.8648644233597690727897128,
+    0.9491079123427585245261897, 0.9914553711208126392068547};
+__constant__ double c_w15[15] = {
+    0.0229353220105292249637320, 0.0630920926299785532907007, 0.1047900103222501838398763,
+    0.1406532597155259187451896, 0.1690047266392679028265834, 0.1903505780647854099132564,
+    0.2044329400752988924141620, 0.2094821410847278280129992, 0.2044329400752988924141620,
+    0.1903505780647854099132564, 0.1690047266392679028265834, 0.1406532597155259187451896,
+    0.1047900103222501838398763, 0.0630920926299785532907007, 0.0229353220105292249637320};
+__constant__ double c_w7[7] = {0.1294849661688696932706114, 0.2797053914892766679014678, 0.3818300505051189449503698,
+                               0.4179591836734693877551020, 0.3818300505051189449503698, 0.2797053914892766679014678,
+                               0.1294849661688696932706114};
+
+// GetSphr (Grid.cpp:487-548)
+template <typename T>
+__device__ Cx<T> sphr_amp(const typename Vec4<T>::type* __restrict__ g, int Lp, double step, double r, double th,
+                          double ph) {
+    Cx<T> origin, od;
+    load_cell<T>(g, 0, origin, od);
+    if (r == 0.0) return origin;
+    const double frc = bump8(r / step);
+    const int fInd = (int)frc;
+    const double frac = frc - (double)fInd;
+    if (frac < 1.e-9) return (fInd > 0) ? interp_plane<T>(g, fInd, th, ph) : origin;
+    Cx<T> pl1, pl2, d1, d2;
+    planes<T>(g, Lp, fInd, th, ph, pl1, pl2, d1, d2);
+    return hermite<T>(pl1, pl2, d1, d2, (T)frac);
+}
+
+template <typename T>
+__device__ double gk_integrand(const ModelDev* __restrict__ models, int n_models, int Lp, double step, double q,
+                               double st, double ct, double phi) {
+    typedef typename Vec4<T>::type V4;
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    const double n[3] = {st * cp, st * sp, ct};
+    double ar = 0, ai = 0;
+    for (int mi = 0; mi < n_models; ++mi) {
+        const ModelDev& M = models[mi];
+        const V4* g = reinterpret_cast<const V4*>(M.grid);
+        const int ng = M.n_groups > 0 ? M.n_groups : 1;
+        double mr = 0, mim = 0;
+        for (int gi = 0; gi < ng; ++gi) {
+            double v0 = n[0], v1 = n[1], v2 = n[2];
+            if (M.n_groups > 0) {  // Q^T R_copy, not normalised (calcAmplitude)
+                const double* Rg = M.group_R + 9 * gi;
+                v0 = n[0] * Rg[0] + n[1] * Rg[3] + n[2] * Rg[6];
+                v1 = n[0] * Rg[1] + n[1] * Rg[4] + n[2] * Rg[7];
+                v2 = n[0] * Rg[2] + n[1] * Rg[5] + n[2] * Rg[8];
+            }
+            // leaf: Qt = Q^T RotMat, phase from Q (pre-rotation) . t
+            const double t0 = v0 * M.R[0] + v1 * M.R[3] + v2 * M.R[6];
+            const double t1 = v0 * M.R[1] + v1 * M.R[4] + v2 * M.R[7];
+            const double t2 = v0 * M.R[2] + v1 * M.R[5] + v2 * M.R[8];
+            double r = q * sqrt(t0 * t0 + t1 * t1 + t2 * t2);
+            const double z = q * t2;
+            if (fabs(z) > r) r = fabs(z);
+            const double th = (r == 0.0) ? 0.0 : acos(z / r);
+            double ph = atan2(q * t1, q * t0);
+            if (ph < 0.0) ph += 2.0 * kPi;
+            const Cx<T> a = sphr_amp<T>(g, Lp, step, r, th, ph);
+            double vr = (double)a.r, vi = (double)a.i;
+            const double lp = q * (v0 * M.tr[0] + v1 * M.tr[1] + v2 * M.tr[2]);
+            if (lp != 0.0) {
+                double s, c;
+                sincos(lp, &s, &c);
+                const double xr = vr * c - vi * s, xi = vr * s + vi * c;
+                vr = xr;
+                vi = xi;
+            }
+            if (M.n_groups > 0) {
+                double pr = 0, pi = 0;
+                for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
+                    const double* tt = M.trans + 3 * c;
+                    double s, cc;
+                    sincos(q * (n[0] * tt[0] + n[1] * tt[1] + n[2] * tt[2]), &s, &cc);
+                    pr += cc;
+                    pi += s;
+                }
+                const double xr = vr * pr - vi * pi, xi = vr * pi + vi * pr;
+                vr = xr * M.sym_scale;
+                vi = xi * M.sym_scale;
+            }
+            mr += vr;
+            mim += vi;
+        }
+        ar += mr;
+        ai += mim;
+    }
+    return ar * ar + ai * ai;
+}
+
+// 16 lanes per phi interval (lane 15 idle): node values, then the Kronrod and
+// Gauss sums of GaussLegPhi.
+template <typename T>
+__global__ void __launch_bounds__(128) gk_phi_kernel(const ModelDev* __restrict__ models, int n_models, int Lp,
+                                                     double step, const GKTask* __restrict__ tasks, int n,
+                                                     double2* __restrict__ kg) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = tid >> 4, j = tid & 15;
+    const bool valid = task < n && j < 15;
+    double kv = 0, gv = 0;
+    if (valid) {
+        const GKTask t = tasks[task];
+        const double ba2 = (t.pmax - t.pmin) * 0.5, apb2 = (t.pmax + t.pmin) * 0.5;
+        const double f = gk_integrand<T>(models, n_models, Lp, step, t.q, t.st, t.ct, apb2 + ba2 * c_x15[j]);
+        kv = f * ba2 * c_w15[j];
+        gv = (j & 1) ? f * ba2 * c_w7[j >> 1] : 0.0;
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+        kv += __shfl_down_sync(0xffffffffu, kv, o, 16);
+        gv += __shfl_down_sync(0xffffffffu, gv, o, 16);
+    }
+    if (task < n && j == 0) kg[task] = make_double2(kv, gv);
+}
+
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 }  // namespace
+
+cudaError_t launch_gk_phi(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                          const GKTask* d_tasks, int n, double2* d_kg) {
+    if (n <= 0) return cudaSuccess;
+    if (fp64)
+        gk_phi_kernel<double><<<blocks_for((int64_t)n * 16, 128), 128, 0, s>>>(d_models, n_models, g.Lp, g.step,
+                                                                              d_tasks, n, d_kg);
+    else
+        gk_phi_kernel<float><<<blocks_for((int64_t)n * 16, 128), 128, 0, s>>>(d_models, n_models, g.Lp, g.step,
+                                                                             d_tasks, n, d_kg);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_vegas_points(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
                                 int need_dir, const double* d_q, int m, int ppi, uint64_t seed, uint64_t key,

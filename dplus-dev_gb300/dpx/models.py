@@ -268,6 +268,9 @@ class DomainModel:
                                                 dptr(ctr), dptr(sscale), len(Q), dptr(Q),
                                                 d.ctypes.data_as(C.c_void_p), 0, dir_layer_stride, iterations, epsi,
                                                 dptr(res)))
+        elif method == "GK":  # iterations is the depth budget, as in the reference
+            check(lib().dpx_gk_intensity(ctx.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
+                                         dptr(sscale), len(Q), dptr(Q), epsi, iterations, dptr(res)))
         elif method == "VEGAS":
             check(lib().dpx_vegas_intensity(ctx.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
                                             dptr(sscale), len(Q), dptr(Q), seed, points_per_iter, iterations, epsi,

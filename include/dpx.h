@@ -128,6 +128,18 @@ int dpx_vegas_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const 
                         int nq, const double* Q, uint64_t seed, int points_per_iter, int64_t max_points, double eps,
                         double* res);
 
+/* Adaptive Gauss-Kronrod (7,15) orientation average (DomainModel::
+ * GaussKron2DSphereRecurs / GaussLegTheta / GaussLegPhi, Amplitude.cpp:1416-1467,
+ * CPU-only in the reference): theta in [0, pi/2], phi in [0, 2 pi], bisection
+ * until |1 - G7/K15| <= eps or the depth budget max_depth (the reference's
+ * "iterations") is spent, result / 2 pi.  The recursion runs on the host; each
+ * level's phi intervals are evaluated in one batched launch through the single-q
+ * GetSphr interpolation.  Q need not be sorted.  Model arguments as
+ * dpx_orientation_average. */
+int dpx_gk_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                     const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                     int nq, const double* Q, double eps, int64_t max_depth, double* res);
+
 /* ---- seeded direction streams (product-side restatement of the reference's draws) ---- */
 /* D pairs (theta, phi) from std::mt19937(seed) with u2, v2 ~ U[0,2): phi = pi u2, theta = acos(v2 - 1) */
 int dpx_mc_directions(uint32_t seed, int64_t D, double* theta_phi);

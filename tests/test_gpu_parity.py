@@ -273,6 +273,29 @@ def test_vegas_matches_oracle(ctx, prec, tol, docked):
     assert rel(I, ref) <= tol
 
 
+@pytest.mark.parametrize("prec,tol,docked", [(M.FP64, TOL64, False), (M.FP32, TOL32, False), (M.FP64, TOL64, True)])
+def test_gauss_kronrod_matches_oracle(ctx, prec, tol, docked):
+    """Adaptive GK 7/15: same rule, same acceptance test and depth budget as the
+    recursion of DomainModel::GaussLegTheta / GaussLegPhi."""
+    amp = globule(150, 0.9, seed=23)
+    amp.location = (0.3, -0.2, 0.5, 0.2, 0.4, -0.3)
+    gs, qmax = 20, 4.0
+    Q = np.array([0.0, 0.45, 1.3, 2.2, 3.9])
+    if docked:
+        model = M.ManualSymmetry(amp, [[0, 0, 0, 0, 0, 0], [2.0, 0.5, 0, 30, 0, 60]], scale=0.8)
+    else:
+        model = amp
+    dom = M.DomainModel([model], gs, qmax, prec)
+    I = dom.CalculateIntensityVector(ctx, Q, 1e-3, 6, method="GK")
+    data, co = oracle_grid(amp, gs, qmax)
+    keep = []
+    kw = dict(rot=amp.location[3:], tr=amp.location[:3], keep=keep)
+    leaf = O.make_leaf(data, co, copy_rot=model.rot, copy_tr=model.trans, sym_scale=0.8, **kw) if docked \
+        else O.make_leaf(data, co, **kw)
+    ref = np.array([O.gk_intensity(gs, qmax, [leaf], q, 1e-3, 6) for q in Q])
+    assert rel(I, ref) <= tol
+
+
 def test_vegas_rejects_bad_point_counts(ctx):
     amp = globule(50, 0.6, seed=22)
     dom = M.DomainModel([amp], 10, 3.0, M.FP32)

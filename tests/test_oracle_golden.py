@@ -179,6 +179,22 @@ def test_single_atom_known_answers_vegas(idx):
     assert np.max(np.abs(np.sqrt(I) - np.sqrt(ref))) <= 2e-6 * np.sqrt(ref.max())
 
 
+@pytest.mark.parametrize("idx", [1, 12])
+def test_single_atom_known_answers_gauss_kronrod(idx):
+    """Adaptive GK on an orientation-independent amplitude: G7 and K15 agree on
+    the first level and the integral / 2 pi is |f - dummy|^2."""
+    f = _load("single_atom.json")["fixtures"][idx]
+    amp = M.PDBAmplitude([f["ion"]], [[0.037, -1.1639, 3.8862]], f["extra"], centered=f["centered"])
+    s = O.Struct.from_pdb(amp)
+    gs, qmax = f["gridSize"], f["qMax"]
+    data = O.grid_fill(s, gs, qmax, O.FP64)
+    co = O.grid_splines(gs, data, O.FP64)
+    q = np.array(f["q"])[::40]
+    ref = np.array(f["I"])[::40]
+    I = np.array([O.gk_intensity(gs, qmax, [O.make_leaf(data, co)], x, 1e-5, 8) for x in q])
+    assert np.max(np.abs(np.sqrt(I) - np.sqrt(ref))) <= 2e-6 * np.sqrt(ref.max())
+
+
 def test_vegas_refines_bins_toward_variance():
     """The bin refinement moves boundaries: a strongly anisotropic model gets a
     different estimate sequence than a fixed grid would, and converges."""
