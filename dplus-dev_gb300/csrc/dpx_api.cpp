@@ -772,6 +772,33 @@ int dpx_vegas_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const 
     return DPX_OK;
 }
 
+int dpx_grid_assemble(dpx_grid dst, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                      const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                      const double* lattice, double scale) {
+    if (!dst || n_models <= 0 || !grids) return fail(DPX_ERR_ARG, "NULL or empty argument");
+    for (int m = 0; m < n_models; ++m) {
+        if (!grids[m] || grids[m]->grid_size != dst->grid_size || grids[m]->qmax != dst->qmax ||
+            grids[m]->precision != dst->precision)
+            return fail(DPX_ERR_ARG, "source grids must share the destination's grid_size, qmax and precision");
+        if (grids[m] == dst) return fail(DPX_ERR_ARG, "the destination cannot also be a source");
+    }
+    dpx_ctx ctx = dst->ctx;
+    if (int rc = set_device(ctx)) return rc;
+    cudaStream_t s = ctx->stream;
+    std::vector<dpx::ModelDev> md;
+    std::vector<char> gstage;
+    if (int rc = prepare_models(ctx, n_models, grids, rot, tr, n_copies, copy_rot, copy_tr, sym_scale, md, gstage))
+        return rc;
+    DPX_CUDA(ctx->models.reserve(md.size() * sizeof(dpx::ModelDev)));
+    DPX_CUDA(cudaMemcpyAsync(ctx->models.p, md.data(), md.size() * sizeof(dpx::ModelDev), cudaMemcpyHostToDevice, s));
+    DPX_CUDA(cudaMemcpyAsync(ctx->groups.p, gstage.data(), gstage.size(), cudaMemcpyHostToDevice, s));
+    cudaError_t e = dpx::launch_assemble(s, dst->precision == DPX_FP64, dst->g, n_models,
+                                         (const dpx::ModelDev*)ctx->models.p, lattice, scale, dst->cells);
+    if (e != cudaSuccess) return cuda_fail(e, "assembly launch");
+    DPX_CUDA(cudaStreamSynchronize(s));  // the staged host vectors go out of scope
+    return DPX_OK;
+}
+
 int dpx_gk_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
                      const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
                      int nq, const double* Q, double eps, int64_t max_depth, double* res) {

@@ -92,6 +92,11 @@ struct GKTask {
 cudaError_t launch_gk_phi(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
                           const GKTask* d_tasks, int n, double2* d_kg);
 
+// Grid-path assembly: dst += scale * lattice * sum of models (GetCart path).
+// lattice: NULL or {a[3], b[3], c[3], Na, Nb, Nc}.
+cudaError_t launch_assemble(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                            const double* lattice, double scale, void* dst);
+
 // other kernels (dpx_kernels.cu)
 cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid);
 cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid);

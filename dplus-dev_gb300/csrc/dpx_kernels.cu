@@ -662,14 +662,13 @@ __device__ Cx<T> sphr_amp(const typename Vec4<T>::type* __restrict__ g, int Lp, 
     return hermite<T>(pl1, pl2, d1, d2, (T)frac);
 }
 
+// Sum of the models' amplitudes at q n (n a unit vector) through the GetCart path.
 template <typename T>
-__device__ double gk_integrand(const ModelDev* __restrict__ models, int n_models, int Lp, double step, double q,
-                               double st, double ct, double phi) {
+__device__ void cart_amp(const ModelDev* __restrict__ models, int n_models, int Lp, double step, double q,
+                         const double n[3], double& ar, double& ai) {
     typedef typename Vec4<T>::type V4;
-    double sp, cp;
-    sincos(phi, &sp, &cp);
-    const double n[3] = {st * cp, st * sp, ct};
-    double ar = 0, ai = 0;
+    ar = 0;
+    ai = 0;
     for (int mi = 0; mi < n_models; ++mi) {
         const ModelDev& M = models[mi];
         const V4* g = reinterpret_cast<const V4*>(M.grid);
@@ -722,7 +721,86 @@ __device__ double gk_integrand(const ModelDev* __restrict__ models, int n_models
         ar += mr;
         ai += mim;
     }
+}
+
+template <typename T>
+__device__ double gk_integrand(const ModelDev* __restrict__ models, int n_models, int Lp, double step, double q,
+                               double st, double ct, double phi) {
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    const double n[3] = {st * cp, st * sp, ct};
+    double ar, ai;
+    cart_amp<T>(models, n_models, Lp, step, q, n, ar, ai);
     return ar * ar + ai * ai;
+}
+
+// --------------------------------------------------------------------------
+// Grid-path assembly: dst[cell] += scale * lattice(q) * sum of models at q,
+// one thread per destination cell.  Covers ManualSymmetry::calculateGrid
+// (Symmetries.cpp:879-962, GPU ManSymGenJacob.cu:36-124), the sum of placed
+// grids (SumGridsJacobian.cu:44-130) and the space-filling lattice factor of
+// GridSymmetry::calcAmplitude (Symmetries.cpp:105-137, SymmetryGenJacob.cu).
+// Destination cells sit on shell radii, so every source read is a single
+// theta-phi plane (GetSphr with frac = 0).
+// --------------------------------------------------------------------------
+struct Lattice {
+    double a[3], b[3], c[3];
+    double na, nb, nc;
+    int on;
+};
+
+__device__ __forceinline__ void lattice_factor(double dot, double N, double& fr, double& fi) {
+    // (1 - e^{i N x}) / (1 - e^{i x}), or N where x ~ 0 (closeToZero, mathfuncs.h:60-63)
+    if (fabs(dot) < 100.0 * 2.220446049250313e-16 || N == 1.0) {
+        fr = N;
+        fi = 0;
+        return;
+    }
+    double s1, c1, sN, cN;
+    sincos(dot, &s1, &c1);
+    sincos(dot * N, &sN, &cN);
+    const double ur = 1.0 - cN, ui = -sN, dr = 1.0 - c1, di = -s1;
+    const double den = dr * dr + di * di;
+    fr = (ur * dr + ui * di) / den;
+    fi = (ui * dr - ur * di) / den;
+}
+
+template <typename T>
+__global__ void assemble_kernel(const ModelDev* __restrict__ models, int n_models, int Lp, double step, int64_t P,
+                                Lattice lat, double scale, typename Vec4<T>::type* __restrict__ dst) {
+    typedef typename Vec4<T>::type V4;
+    const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P) return;
+    int qi, ti, pi;
+    cell_indices(cell, qi, ti, pi);
+    double n[3] = {0.0, 0.0, 1.0};
+    const double q = (double)qi * step;
+    if (qi > 0) {
+        double st, ct, sp, cp;
+        sincospi((double)ti / (double)(3 * qi), &st, &ct);
+        sincospi((double)pi / (double)(3 * qi), &sp, &cp);
+        n[0] = st * cp;
+        n[1] = st * sp;
+        n[2] = ct;
+    }
+    double ar, ai;
+    cart_amp<T>(models, n_models, Lp, step, q, n, ar, ai);
+    if (lat.on) {
+        const double* vs[3] = {lat.a, lat.b, lat.c};
+        const double Ns[3] = {lat.na, lat.nb, lat.nc};
+        for (int k = 0; k < 3; ++k) {
+            const double dot = q * (n[0] * vs[k][0] + n[1] * vs[k][1] + n[2] * vs[k][2]);
+            double fr, fi;
+            lattice_factor(dot, Ns[k], fr, fi);
+            const double xr = ar * fr - ai * fi, xi = ar * fi + ai * fr;
+            ar = xr;
+            ai = xi;
+        }
+    }
+    V4 v = dst[cell];
+    v.x = (T)((double)v.x + scale * ar);
+    v.y = (T)((double)v.y + scale * ai);
+    dst[cell] = v;
 }
 
 // 16 lanes per phi interval (lane 15 idle): node values, then the Kronrod and
@@ -753,6 +831,29 @@ __global__ void __launch_bounds__(128) gk_phi_kernel(const ModelDev* __restrict_
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 }  // namespace
+
+cudaError_t launch_assemble(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
+                            const double* lattice, double scale, void* dst) {
+    Lattice lat{};
+    if (lattice) {
+        for (int k = 0; k < 3; ++k) {
+            lat.a[k] = lattice[k];
+            lat.b[k] = lattice[3 + k];
+            lat.c[k] = lattice[6 + k];
+        }
+        lat.na = lattice[9];
+        lat.nb = lattice[10];
+        lat.nc = lattice[11];
+        lat.on = 1;
+    }
+    if (fp64)
+        assemble_kernel<double><<<blocks_for(g.P, 128), 128, 0, s>>>(d_models, n_models, g.Lp, g.step, g.P, lat, scale,
+                                                                     (double4_32a*)dst);
+    else
+        assemble_kernel<float><<<blocks_for(g.P, 128), 128, 0, s>>>(d_models, n_models, g.Lp, g.step, g.P, lat, scale,
+                                                                    (float4*)dst);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_gk_phi(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
                           const GKTask* d_tasks, int n, double2* d_kg) {

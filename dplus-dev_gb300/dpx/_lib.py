@@ -58,6 +58,7 @@ _SIGS = {
                                           C.c_int, C.c_int64, C.c_int64, C.c_double, _D]),
     "dpx_vegas_intensity": (C.c_int, [_P, C.c_int, C.POINTER(_P), _D, _D, _I, _D, _D, _D, C.c_int, _D, C.c_uint64,
                                       C.c_int, C.c_int64, C.c_double, _D]),
+    "dpx_grid_assemble": (C.c_int, [_P, C.c_int, C.POINTER(_P), _D, _D, _I, _D, _D, _D, _D, C.c_double]),
     "dpx_gk_intensity": (C.c_int, [_P, C.c_int, C.POINTER(_P), _D, _D, _I, _D, _D, _D, C.c_int, _D, C.c_double,
                                    C.c_int64, _D]),
     "dpx_mc_directions": (C.c_int, [C.c_uint32, C.c_int64, _D]),

@@ -202,21 +202,117 @@ class PDBAmplitude:
         return g
 
 
+def _pack_models(placements):
+    """C-ABI model arrays from (grid, location[6], copies or None, sym_scale) tuples."""
+    n = len(placements)
+    rot = np.zeros(3 * n)
+    tr = np.zeros(3 * n)
+    ncop = np.zeros(n, dtype=np.int32)
+    crot, ctr, sscale = [], [], np.ones(n)
+    for m, (g, loc, copies, sc) in enumerate(placements):
+        tr[3 * m:3 * m + 3] = loc[:3]
+        rot[3 * m:3 * m + 3] = loc[3:]
+        if copies is not None:
+            ncop[m] = len(copies[1])
+            crot.append(np.ravel(copies[0]))
+            ctr.append(np.ravel(copies[1]))
+        sscale[m] = sc
+    crot = np.ascontiguousarray(np.concatenate(crot) if crot else np.zeros(3))
+    ctr = np.ascontiguousarray(np.concatenate(ctr) if ctr else np.zeros(3))
+    gh = (C.c_void_p * n)(*[p[0].handle.value for p in placements])
+    return n, gh, rot, tr, ncop, crot, ctr, sscale
+
+
 class ManualSymmetry:
     """Docked copies of one child: rows (x, y, z [nm], alpha, beta, gamma [degrees]),
-    as ManualSymmetry::PreCalculate reads them (Symmetries.cpp:670-695)."""
+    as ManualSymmetry::PreCalculate reads them (Symmetries.cpp:670-695).
 
-    def __init__(self, child: PDBAmplitude, rows: Sequence[Sequence[float]], scale: float = 1.0):
+    ``use_grid=False`` is the hybrid path: the docked sum is evaluated per
+    orientation sample (HybridOA.cu, Symmetries.cpp:1079-1166).  ``use_grid=True``
+    builds the assembly grid once (ManualSymmetry::calculateGrid,
+    Symmetries.cpp:879-962) and averages it like a leaf."""
+
+    def __init__(self, child: PDBAmplitude, rows: Sequence[Sequence[float]], scale: float = 1.0,
+                 use_grid: bool = False, location: Sequence[float] = (0, 0, 0, 0, 0, 0)):
         r = np.asarray(rows, dtype=np.float64).reshape(-1, 6)
         self.child = child
         self.trans = np.ascontiguousarray(r[:, :3])
         self.rot = np.ascontiguousarray(np.radians(r[:, 3:6]))
         self.scale = float(scale)
+        self.use_grid = bool(use_grid)
+        self.location = tuple(float(v) for v in location)
+        self._grid = None
+        self._grid_key = None
+
+    def calculateGrid(self, ctx: Context, qmax: float, gridSize: int, precision: int = FP32) -> Grid:
+        child = self.child.calculateGrid(ctx, qmax, gridSize, precision)
+        key = (self.child.hash(), self.child.location, self.trans.tobytes(), self.rot.tobytes(), self.scale,
+               int(gridSize), float(qmax), int(precision))
+        if self._grid is not None and self._grid_key == key:
+            return self._grid
+        g = Grid(ctx, gridSize, qmax, precision)
+        n, gh, rot, tr, ncop, crot, ctr, sscale = _pack_models(
+            [(child, self.child.location, (self.rot, self.trans), self.scale)])
+        check(lib().dpx_grid_assemble(g.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
+                                      dptr(sscale), None, 1.0))
+        g.compute_splines()
+        self._grid, self._grid_key = g, key
+        return g
+
+    def placement(self, ctx, qmax, gridSize, precision):
+        if self.use_grid:
+            return (self.calculateGrid(ctx, qmax, gridSize, precision), self.location, None, 1.0)
+        return (self.child.calculateGrid(ctx, qmax, gridSize, precision), self.child.location,
+                (self.rot, self.trans), self.scale)
+
+
+class SpaceFillingSymmetry:
+    """GridSymmetry (Symmetries.cpp:30-137): children repeated on a lattice of
+    Na x Nb x Nc cells with edges da, db, dc (nm) and angles alpha, beta, gamma
+    (degrees); evaluated on the grid path."""
+
+    def __init__(self, children: Sequence, da, db, dc, alpha, beta, gamma, Na, Nb, Nc, scale: float = 1.0,
+                 location: Sequence[float] = (0, 0, 0, 0, 0, 0)):
+        a, b, c = (math.radians(x) for x in (alpha, beta, gamma))
+        if (a == 0 or b == 0 or c == 0 or any(abs(abs(x) - math.pi) < 1e-6 for x in (a, b, c))):
+            raise ValueError("Angles in a Space-filling Symmetry cannot be zero or 180.")
+        if abs(a) + abs(b) <= abs(c) or abs(c) + abs(b) <= abs(a) or abs(a) + abs(c) <= abs(b):
+            raise ValueError("In the Space-filling Symmetry, the sum of any two angles must be greater than the third.")
+        sa, sb, sc = math.sin(a), math.sin(b), math.sin(c)
+        ca, cb, cc = math.cos(a), math.cos(b), math.cos(c)
+        cat = (ca - cb * cc) / (sb * sc)
+        if abs(cat) > 1.0:
+            raise ValueError("In the Space-filling Symmetry, the angles don't form a valid basis.")
+        # GridSymmetry::PreCalculate (Symmetries.cpp:89-101)
+        self.lattice = np.array([da, 0.0, 0.0, db * cc, db * sc, 0.0, dc * cb, dc * sb * cat,
+                                 dc * sb * math.sin(math.acos(cat)), Na, Nb, Nc], dtype=np.float64)
+        self.children = list(children)
+        self.scale = float(scale)
+        self.location = tuple(float(v) for v in location)
+        self._grid = None
+        self._grid_key = None
+
+    def calculateGrid(self, ctx: Context, qmax: float, gridSize: int, precision: int = FP32) -> Grid:
+        placements = [c.placement(ctx, qmax, gridSize, precision) if hasattr(c, "placement")
+                      else (c.calculateGrid(ctx, qmax, gridSize, precision), c.location, None, 1.0)
+                      for c in self.children]
+        key = (tuple(id(p[0]) for p in placements), self.lattice.tobytes(), self.scale)
+        if self._grid is not None and self._grid_key == key:
+            return self._grid
+        g = Grid(ctx, gridSize, qmax, precision)
+        n, gh, rot, tr, ncop, crot, ctr, sscale = _pack_models(placements)
+        check(lib().dpx_grid_assemble(g.handle, n, gh, dptr(rot), dptr(tr), iptr(ncop), dptr(crot), dptr(ctr),
+                                      dptr(sscale), dptr(self.lattice), self.scale))
+        g.compute_splines()
+        self._grid, self._grid_key = g, key
+        return g
+
+    def placement(self, ctx, qmax, gridSize, precision):
+        return (self.calculateGrid(ctx, qmax, gridSize, precision), self.location, None, 1.0)
 
 
 class DomainModel:
-    """DomainModel::CalculateIntensityVector for leaves on grids with the Monte
-    Carlo orientation average between layers."""
+    """DomainModel::CalculateIntensityVector over its top-level amplitudes."""
 
     def __init__(self, amps: Sequence, gridSize: int, qMax: float, precision: int = FP32):
         self.amps = list(amps)
@@ -224,34 +320,19 @@ class DomainModel:
         self.qMax = float(qMax)
         self.precision = precision
 
-    def grids(self, ctx: Context):
+    def placements(self, ctx: Context):
         out = []
         for a in self.amps:
-            leaf = a.child if isinstance(a, ManualSymmetry) else a
-            out.append(leaf.calculateGrid(ctx, self.qMax, self.gridSize, self.precision))
+            if hasattr(a, "placement"):
+                out.append(a.placement(ctx, self.qMax, self.gridSize, self.precision))
+            else:
+                out.append((a.calculateGrid(ctx, self.qMax, self.gridSize, self.precision), a.location, None, 1.0))
         return out
 
     def _model_args(self, ctx: Context):
-        grids = self.grids(ctx)
-        n = len(self.amps)
-        rot = np.zeros(3 * n)
-        tr = np.zeros(3 * n)
-        ncop = np.zeros(n, dtype=np.int32)
-        crot, ctr, sscale = [], [], np.ones(n)
-        for m, a in enumerate(self.amps):
-            leaf = a.child if isinstance(a, ManualSymmetry) else a
-            tr[3 * m:3 * m + 3] = leaf.location[:3]
-            rot[3 * m:3 * m + 3] = leaf.location[3:]
-            if isinstance(a, ManualSymmetry):
-                ncop[m] = len(a.trans)
-                crot.append(a.rot.ravel())
-                ctr.append(a.trans.ravel())
-                sscale[m] = a.scale
-        crot = np.ascontiguousarray(np.concatenate(crot) if crot else np.zeros(3))
-        ctr = np.ascontiguousarray(np.concatenate(ctr) if ctr else np.zeros(3))
-        gh = (C.c_void_p * n)(*[g.handle.value for g in grids])
+        placements = self.placements(ctx)
         # the arrays must stay alive for the call: return them together
-        return (n, gh, rot, tr, ncop, crot, ctr, sscale), (grids,)
+        return _pack_models(placements), (placements,)
 
     def CalculateIntensityVector(self, ctx: Context, Q: Sequence[float], epsi: float, iterations: int,
                                  dirs: np.ndarray | None = None, dir_layer_stride: int = 0, method: str = "MC",

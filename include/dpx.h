@@ -128,6 +128,20 @@ int dpx_vegas_intensity(dpx_ctx ctx, int n_models, const dpx_grid* grids, const 
                         int nq, const double* Q, uint64_t seed, int points_per_iter, int64_t max_points, double eps,
                         double* res);
 
+/* Grid-path assembly: dst[cell] += scale * lattice(q) * sum of the placed (and
+ * docked) source grids at the cell's q, through the single-q GetCart path.
+ * Replaces ManualSymmetry::calculateGrid / GPUCalcManSymJacobSphrDD
+ * (Symmetries.cpp:879-962, GPUHeader.h:185, ManSymGenJacob.cu:36-124), the
+ * grid sum GPUSumGridsJacobSphrDD (GPUHeader.h:255, SumGridsJacobian.cu:44-130)
+ * and the space-filling GridSymmetry (Symmetries.cpp:60-137,
+ * GPUCalcSpcFillSymJacobSphrDD, GPUHeader.h:214): lattice = NULL or the 12
+ * doubles {a[3], b[3], c[3], Na, Nb, Nc} giving sum_n e^{i n q.a} per axis.
+ * The destination accumulates, as the reference's outputs do; compute its
+ * splines afterwards.  Sources share the destination's size, qmax, precision. */
+int dpx_grid_assemble(dpx_grid dst, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                      const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                      const double* lattice, double scale);
+
 /* Adaptive Gauss-Kronrod (7,15) orientation average (DomainModel::
  * GaussKron2DSphereRecurs / GaussLegTheta / GaussLegPhi, Amplitude.cpp:1416-1467,
  * CPU-only in the reference): theta in [0, pi/2], phi in [0, 2 pi], bisection

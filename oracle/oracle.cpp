@@ -905,6 +905,38 @@ int orc_vegas_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf
     return 0;
 }
 
+void orc_assemble_grid(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, const double* lattice,
+                       double scale, int nthreads, double* out) {
+    std::vector<LeafModel> models;
+    for (int l = 0; l < n_leaves; l++) models.push_back(make_model(grid_size, qmax, leaves[l]));
+    Geom g = make_geom(grid_size, qmax);
+    const cd One(1.0, 0.0), Im(0.0, 1.0);
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    /* Grid::Fill over ManualSymmetry / Amplitude::getAmplitude (Symmetries.cpp:697-716,
+     * Amplitude.cpp:3035-3056) and GridSymmetry::calcAmplitude (Symmetries.cpp:105-137) */
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t ind = 0; ind < g.P; ind++) {
+        int qi; int64_t ti, pi;
+        orc_indices_from_index(ind, &qi, &ti, &pi);
+        double qx, qy, qz;
+        cell_qvec(g, qi, ti, pi, qx, qy, qz);
+        cd amp(0, 0);
+        for (auto& M : models) amp += leaf_amp_cart(M, qx, qy, qz);
+        if (lattice) {
+            for (int a = 0; a < 3; a++) {
+                const double* v = lattice + 3 * a;
+                const double N = lattice[9 + a];
+                const double dot = qx * v[0] + qy * v[1] + qz * v[2];
+                if (std::fabs(dot) < 100.0 * 2.220446049250313e-16 || N == 1.0) amp *= N;
+                else amp *= (One - std::exp(Im * dot * N)) / (One - std::exp(Im * dot));
+            }
+        }
+        amp *= scale;
+        out[2 * ind] += amp.real();
+        out[2 * ind + 1] += amp.imag();
+    }
+}
+
 double orc_gk_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, double q, double eps,
                         int64_t max_depth) {
     std::vector<LeafModel> models;

@@ -115,6 +115,13 @@ double orc_uniform(uint64_t seed, uint64_t key, uint64_t n);
 int orc_vegas_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq, const double* Q,
                         uint64_t seed, int points_per_iter, int64_t max_points, double eps, double* res);
 
+/* ---- grid-path assembly: out[cell] += scale * lattice(q) * sum_leaves amplitude(q)
+ * through GetCart, as Grid::Fill evaluates ManualSymmetry / GridSymmetry
+ * calcAmplitude (Symmetries.cpp:105-137, 697-716, 879-962).  lattice: NULL or
+ * {a[3], b[3], c[3], Na, Nb, Nc}. */
+void orc_assemble_grid(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, const double* lattice,
+                       double scale, int nthreads, double* out);
+
 /* ---- FP64 direct-sum oracle (no grid) ----
  * F(q n) = sum_j f_j(q) e^{i q n.r_j} for a placed leaf with optional docked
  * copies; I(q) = mean over the given directions of |F|^2. */

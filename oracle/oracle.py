@@ -226,6 +226,18 @@ def gk_intensity(grid_size, qmax, leaves, q, eps, max_depth):
     return lib().orc_gk_intensity(grid_size, qmax, len(leaves), arr, q, eps, max_depth)
 
 
+def assemble_grid(grid_size, qmax, leaves, lattice=None, scale=1.0, out=None):
+    L = lib()
+    L.orc_assemble_grid.restype = None
+    L.orc_assemble_grid.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(Leaf), _D, C.c_double, C.c_int, _D]
+    if out is None:
+        out = np.zeros(2 * grid_cells(grid_size))
+    arr = (Leaf * len(leaves))(*leaves)
+    lat = None if lattice is None else np.ascontiguousarray(lattice, dtype=np.float64)
+    L.orc_assemble_grid(grid_size, qmax, len(leaves), arr, _d(lat), scale, 0, out.ctypes.data_as(_D))
+    return out
+
+
 def vegas_intensity(grid_size, qmax, leaves, Q, seed, points_per_iter, max_points, eps):
     L = lib()
     if not getattr(L, "_vegas_typed", False):

@@ -296,6 +296,44 @@ def test_gauss_kronrod_matches_oracle(ctx, prec, tol, docked):
     assert rel(I, ref) <= tol
 
 
+@pytest.mark.parametrize("prec,tol", [(M.FP64, TOL64), (M.FP32, 2e-6)])
+def test_assembly_grid_matches_oracle(ctx, prec, tol):
+    """Grid-path ManualSymmetry: the assembled grid cell by cell (tolerance on the
+    amplitude scale), then its MC average."""
+    amp = globule(200, 1.0, seed=24)
+    amp.location = (0.2, 0.1, -0.3, 0.1, 0.2, 0.3)
+    rows = [[0, 0, 0, 0, 0, 0], [2.0, 0, 0, 0, 0, 90], [0, 2.5, 0.5, 45, 30, 10], [-1.5, 1.0, 0, 45, 30, 10]]
+    sym = M.ManualSymmetry(amp, rows, scale=0.9, use_grid=True)
+    gs, qmax = 24, 4.0
+    g = sym.calculateGrid(ctx, qmax, gs, prec)
+    v, _ = g.read(True, False)
+    data, co = oracle_grid(amp, gs, qmax)
+    keep = []
+    leaf = O.make_leaf(data, co, rot=amp.location[3:], tr=amp.location[:3], copy_rot=sym.rot, copy_tr=sym.trans,
+                       sym_scale=0.9, keep=keep)
+    ref = O.assemble_grid(gs, qmax, [leaf])
+    assert np.max(np.abs(v - ref)) <= tol * np.max(np.abs(ref))
+    if prec == M.FP64:
+        Q = np.linspace(0, 4, 41)
+        dirs = M.mc_directions(51, 400)
+        I = M.DomainModel([sym], gs, qmax, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+        rco = O.grid_splines(gs, ref, O.FP64)
+        refI = O.integrate_layers(gs, qmax, [O.make_leaf(ref, rco)], Q, dirs, 0, len(dirs), 0.0)
+        assert rel(I, refI) <= TOL64
+
+
+@pytest.mark.parametrize("prec,tol", [(M.FP64, TOL64), (M.FP32, 2e-6)])
+def test_space_filling_grid_matches_oracle(ctx, prec, tol):
+    amp = globule(120, 0.8, seed=25)
+    sf = M.SpaceFillingSymmetry([amp], 3.0, 3.5, 4.0, 90, 80, 100, 3, 2, 4, scale=0.5)
+    gs, qmax = 20, 3.0
+    g = sf.calculateGrid(ctx, qmax, gs, prec)
+    v, _ = g.read(True, False)
+    data, co = oracle_grid(amp, gs, qmax)
+    ref = O.assemble_grid(gs, qmax, [O.make_leaf(data, co)], lattice=sf.lattice, scale=0.5)
+    assert np.max(np.abs(v - ref)) <= tol * np.max(np.abs(ref))
+
+
 def test_vegas_rejects_bad_point_counts(ctx):
     amp = globule(50, 0.6, seed=22)
     dom = M.DomainModel([amp], 10, 3.0, M.FP32)
