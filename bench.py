@@ -32,7 +32,6 @@ sys.path.insert(0, os.path.join(ROOT, "dplus-dev_gb300"))
 N_ATOMS, RADIUS, SEED = 20000, 5.0, 20251
 GRID_SIZE, QMAX, NQ = 400, 7.5, 500
 N_DIRS, DIR_SEED = 100_000, 1234
-FILL_CPT = 8  # the default FP32 fill shape (cells per work item x 128 threads)
 # ncu dram__bytes_read+write of fill_f32_kernel on the profile shape (2,000 atoms,
 # 120 layers, 11.3 M cells): 335 MB, i.e. 29.6 B per cell; scaled to 50.7 M cells
 FILL_TRAFFIC = 29.6 * 50688289
@@ -141,11 +140,18 @@ def run_dpx(args):
     stream = torch.cuda.Stream()  # a real stream: CUDA events on it see every libdpx launch
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
-    if args.fill_shape:
-        c, t = (int(x) for x in args.fill_shape.split("x"))
+    if args.fill_shape:  # CxT, suffix "p" = persistent schedule
+        spec = args.fill_shape
+        c, t = (int(x) for x in spec.rstrip("p").split("x"))
         ctx.set_fill_shape(c, t)
+        ctx.set_fill_schedule(spec.endswith("p"))
 
     amp, Q, dirs = build_inputs()
+    tune = None
+    if args.autotune:  # sweep every fill shape on this workload's leaf, keep the fastest
+        best, table = M.autotune_fill(ctx, [amp], QMAX, GRID_SIZE, repeats=1)
+        tune = {"best": "%dx%d%s" % (best[0], best[1], "p" if best[2] else ""),
+                "fill_ms": {"%dx%d%s" % (k[0], k[1], "p" if k[2] else ""): round(v, 3) for k, v in table.items()}}
     atoms_h = amp.atoms_float4()
     # device-resident inputs for the kernel-level number (centred on the host once)
     cen = amp.xyz.mean(0)
@@ -247,7 +253,7 @@ def run_dpx(args):
         spl_ms = float(np.median(times["splines"]))
         P = L.dpx_grid_cells(GRID_SIZE)
         lp = GRID_SIZE // 2 + 3
-        cpt = FILL_CPT
+        cpt = ctx.fill_shape()[0]
         # row-factored fill: per work item (CPT cells of a theta row, each with its
         # z-mirror) and atom, 1 + CPT sincos = 2 (1 + CPT) SFU ops
         items = 1 + sum((3 * i // 2 + 1) * ((3 * i + cpt - 1) // cpt) for i in range(1, lp + 1))
@@ -266,7 +272,10 @@ def run_dpx(args):
                                                                                dirs.nbytes),
                     "d2h_bytes_per_step": int(res.nbytes)},
             "gpu_launches": args.steps * 4,
-            "roofline": {"bound": "sfu", "kernel": "fill_f32_kernel", "achieved": achieved, "peak": sfu_peak,
+            "roofline": {"bound": "sfu", "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] else "flat"),
+                         "fill_shape": "%dx%d%s" % (ctx.fill_shape()[0], ctx.fill_shape()[1],
+                                                    "p" if ctx.fill_shape()[2] else ""),
+                         "achieved": achieved, "peak": sfu_peak,
                          "unit": "T SFU-op/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
                          "note": "SFU ops = atoms x work items x 2(1+CPT) (row-factored fill); peak = 152 SM x 16 "
                                  "MUFU/clk at sm_max_mhz (derived, not in MEASURED_PEAKS.json); traffic = ncu "
@@ -279,6 +288,8 @@ def run_dpx(args):
             "split_ms": {"fill": fill_ms, "splines": spl_ms, "average": avg_ms},
             "clocks": clocks,
         }
+        if tune:
+            out["autotune"] = tune
         if args.check_error:
             out["max_rel_err_vs_fp64"] = fp64_error(ctx, amp, Q, dirs, I_fp32)
         if not args.no_cpu_baseline and world == 1:
@@ -358,7 +369,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dpx", choices=["dpx", "reference"])
-    ap.add_argument("--fill-shape", default="")
+    ap.add_argument("--fill-shape", default="", help="CxT or CxTp (persistent)")
+    ap.add_argument("--autotune", action="store_true", help="sweep the fill shapes first and use the fastest")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--check-error", action="store_true")

@@ -2,8 +2,7 @@
 // grids, form-factor tables, bracket plans and the drop-in wrappers with the
 // reference's argument meaning.  No entry point throws or traps; failures are
 // status codes with a per-thread message.
-#include "dpx.h"
-#include "dpx_internal.h"
+#include "dpx_host.h"
 
 #include <cuda_runtime.h>
 
@@ -19,8 +18,9 @@
 #include <unordered_map>
 
 using dpx::Geom;
+using namespace dpxh;
 
-namespace {
+namespace dpxh {
 
 thread_local std::string g_err;
 
@@ -42,57 +42,9 @@ int cuda_fail(cudaError_t e, const char* where) {
     return fail(DPX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
 }
 
-#define DPX_CUDA(call)                                          \
-    do {                                                        \
-        cudaError_t e_ = (call);                                \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);     \
-    } while (0)
+}  // namespace dpxh
 
-const double kPi = 3.14159265358979323846;
-
-// Grow-only device buffer owned by a context.
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    cudaError_t reserve(size_t n) {
-        if (n <= bytes) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e == cudaSuccess) bytes = n;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-};
-
-}  // namespace
-
-struct dpx_ctx_s {
-    int device = 0;
-    int refs = 1;  // the caller's handle + one per live grid
-    bool closed = false;
-    cudaStream_t own = nullptr;
-    cudaStream_t stream = nullptr;
-    int fill_cpt = 8, fill_threads = 128;  // autotuned on GB300 (bench workload)
-    DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs;
-    std::vector<char> host_stage;
-};
-
-struct dpx_grid_s {
-    dpx_ctx ctx;
-    int grid_size;
-    double qmax;
-    int precision;
-    Geom g;
-    void* cells;
-};
-
-namespace {
+namespace dpxh {
 
 int set_device(dpx_ctx ctx) {
     int cur = -1;
@@ -102,6 +54,13 @@ int set_device(dpx_ctx ctx) {
 }
 
 size_t cell_bytes(int precision) { return precision == DPX_FP64 ? sizeof(double4_32a) : sizeof(float4); }
+
+// FP32 fill launch shapes the autotuner sweeps: {cells per work item, threads
+// per block (= atoms per shared-memory tile), persistent schedule}.
+extern const int kFillShape[][3] = {{2, 256, 0}, {2, 256, 1}, {4, 128, 0}, {4, 128, 1}, {4, 256, 0}, {4, 256, 1},
+                             {6, 128, 0}, {6, 128, 1}, {6, 256, 0}, {6, 256, 1}, {8, 128, 0}, {8, 128, 1},
+                             {8, 256, 0}, {8, 256, 1}};
+extern const int kFillShapes = 14;
 
 // Unique-ion form factors minus the Gaussian dummy-atom solvent
 // (Atomic Form Factor.cpp:91-115, 121-176; r_m :11-27) for shells 0..Lp,
@@ -145,7 +104,7 @@ void euler(double a, double b, double c, double R[9]) {
     R[6] = s1 * s3 - c1 * c3 * s2; R[7] = c3 * s1 + c1 * s2 * s3; R[8] = c1 * c2;
 }
 
-}  // namespace
+}  // namespace dpxh
 
 int dpx::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
@@ -216,7 +175,11 @@ int dpx_ctx_create(int device, dpx_ctx* out) {
     return DPX_OK;
 }
 
-namespace {
+}  // extern "C"
+
+namespace dpxh {
+void ctx_retain(dpx_ctx ctx) { ++ctx->refs; }
+
 // Frees the context once the caller has destroyed it and no grid uses it.
 void ctx_release(dpx_ctx ctx) {
     if (--ctx->refs > 0) return;
@@ -228,7 +191,9 @@ void ctx_release(dpx_ctx ctx) {
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
-}  // namespace
+}  // namespace dpxh
+
+extern "C" {
 
 int dpx_ctx_destroy(dpx_ctx ctx) {
     if (!ctx) return DPX_OK;
@@ -254,14 +219,34 @@ int dpx_ctx_synchronize(dpx_ctx ctx) {
 
 int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cpt, int threads) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
-    static const int ok[][2] = {{2, 256}, {4, 128}, {4, 256}, {6, 128}, {6, 256}, {8, 128}, {8, 256}};
-    for (auto& s : ok)
-        if (s[0] == cpt && s[1] == threads) {
+    for (int k = 0; k < kFillShapes; k += 2)
+        if (kFillShape[k][0] == cpt && kFillShape[k][1] == threads) {
             ctx->fill_cpt = cpt;
             ctx->fill_threads = threads;
             return DPX_OK;
         }
     return fail(DPX_ERR_ARG, "unsupported fill shape %d cells x %d threads", cpt, threads);
+}
+
+int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    ctx->fill_persistent = persistent != 0;
+    return DPX_OK;
+}
+
+int dpx_ctx_get_fill_shape(dpx_ctx ctx, int* shape) {
+    if (!ctx || !shape) return fail(DPX_ERR_ARG, "NULL argument");
+    shape[0] = ctx->fill_cpt;
+    shape[1] = ctx->fill_threads;
+    shape[2] = ctx->fill_persistent;
+    return DPX_OK;
+}
+
+int dpx_fill_shapes(int* shapes) {
+    if (shapes)
+        for (int k = 0; k < kFillShapes; ++k)
+            for (int j = 0; j < 3; ++j) shapes[3 * k + j] = kFillShape[k][j];
+    return kFillShapes;
 }
 
 int64_t dpx_grid_cells(int grid_size) {
@@ -324,87 +309,222 @@ int dpx_grid_info(dpx_grid g, int* grid_size, double* qmax, int* precision, int6
     return DPX_OK;
 }
 
+}  // extern "C"
+
+namespace dpxh {
+
+// Validate one leaf description; returns DPX_OK or an argument error.
+int check_pdb(const dpx_pdb_desc& d) {
+    if (d.n_atoms <= 0 || !d.atoms) return fail(DPX_ERR_ARG, "no atoms");
+    if (d.n_atoms > INT_MAX) return fail(DPX_ERR_ARG, "too many atoms (%lld)", (long long)d.n_atoms);
+    if (d.n_ions <= 0 || d.n_ions > 256 || !d.atoms_per_ion || !d.coeffs || !d.ion_rads)
+        return fail(DPX_ERR_ARG, "bad ion description");
+    int64_t tot = 0;
+    for (int u = 0; u < d.n_ions; ++u) {
+        if (d.atoms_per_ion[u] < 0) return fail(DPX_ERR_ARG, "negative atoms_per_ion");
+        tot += d.atoms_per_ion[u];
+    }
+    if (tot != d.n_atoms)
+        return fail(DPX_ERR_ARG, "atoms_per_ion sums to %lld, n_atoms=%lld", (long long)tot, (long long)d.n_atoms);
+    return DPX_OK;
+}
+
+// Batched fill with an explicit FP32 launch shape; ev0/ev1 (optional) bracket
+// the FP32 fill launch on the context's stream.
+int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int cpt, int threads, bool persistent,
+                    cudaEvent_t ev0, cudaEvent_t ev1) {
+    if (n <= 0 || !grids || !pdbs) return fail(DPX_ERR_ARG, "empty batch");
+    dpx_ctx ctx = grids[0] ? grids[0]->ctx : nullptr;
+    for (int j = 0; j < n; ++j) {
+        if (!grids[j] || grids[j]->ctx != ctx) return fail(DPX_ERR_ARG, "every grid of a batch needs the same context");
+        if (int rc = check_pdb(pdbs[j])) return rc;
+        for (int k = 0; k < j; ++k)
+            if (grids[k] == grids[j]) return fail(DPX_ERR_ARG, "a grid appears twice in one batch");
+    }
+    if (int rc = set_device(ctx)) return rc;
+    cudaStream_t s = ctx->stream;
+
+    // host staging: centred host atoms, then per job [ion offsets][aff][item prefix]
+    std::vector<double> cen(3 * n, 0.0);
+    size_t atom_bytes = 0;
+    std::vector<size_t> atom_off(n, SIZE_MAX), tab_off(n);
+    std::vector<int64_t> n_items(n);
+    std::vector<std::vector<int64_t>> prefs(n);
+    size_t tab_bytes = 0;
+    for (int j = 0; j < n; ++j) {
+        const dpx_pdb_desc& d = pdbs[j];
+        const bool fp32 = grids[j]->precision == DPX_FP32;
+        if (d.center) {
+            for (int k = 0; k < 3; ++k) cen[3 * j + k] = d.center[k];
+        } else if (!d.atoms_on_device && fp32) {  // centroid of the host atoms
+            double acc[3] = {0, 0, 0};
+            for (int64_t a = 0; a < d.n_atoms; ++a)
+                for (int k = 0; k < 3; ++k) acc[k] += d.atoms[4 * a + k];
+            for (int k = 0; k < 3; ++k) cen[3 * j + k] = acc[k] / double(d.n_atoms);
+        }
+        if (!fp32 && !d.atoms_on_device) cen[3 * j] = cen[3 * j + 1] = cen[3 * j + 2] = 0.0;  // exact FP64 phases
+        if (!d.atoms_on_device) {
+            atom_off[j] = atom_bytes;
+            atom_bytes = al16(atom_bytes + (size_t)d.n_atoms * sizeof(float4));
+        }
+        prefs[j].resize(grids[j]->g.Lp + 1);
+        n_items[j] = dpx::fill_items(grids[j]->g, fp32 ? cpt : dpx::kFill64Cells, prefs[j].data());
+        tab_off[j] = tab_bytes;
+        tab_bytes = al16(tab_bytes + (d.n_ions + 1) * sizeof(int));
+        tab_bytes = al16(tab_bytes + (size_t)d.n_ions * (grids[j]->g.Lp + 1) * (fp32 ? sizeof(float) : sizeof(double)));
+        tab_bytes = al16(tab_bytes + prefs[j].size() * sizeof(int64_t));
+    }
+    const size_t jobs_off = al16(atom_bytes + tab_bytes);
+    const size_t counter_off = al16(jobs_off + (size_t)n * sizeof(dpx::FillJob));
+    const size_t total = counter_off + 64;
+    DPX_CUDA(ctx->atoms.reserve(total));
+    ctx->host_stage.assign(total, 0);
+    char* h = ctx->host_stage.data();
+    char* dbase = (char*)ctx->atoms.p;
+    std::vector<dpx::FillJob> jobs;
+    int64_t tiles = 0;
+    std::vector<double> aff;
+    for (int j = 0; j < n; ++j) {
+        const dpx_pdb_desc& d = pdbs[j];
+        const Geom& G = grids[j]->g;
+        const bool fp32 = grids[j]->precision == DPX_FP32;
+        const float4* d_atoms = reinterpret_cast<const float4*>(d.atoms);
+        if (!d.atoms_on_device) {
+            float4* ha = reinterpret_cast<float4*>(h + atom_off[j]);
+            for (int64_t a = 0; a < d.n_atoms; ++a) {
+                ha[a].x = (float)((double)d.atoms[4 * a] - cen[3 * j]);
+                ha[a].y = (float)((double)d.atoms[4 * a + 1] - cen[3 * j + 1]);
+                ha[a].z = (float)((double)d.atoms[4 * a + 2] - cen[3 * j + 2]);
+                ha[a].w = 0.f;
+            }
+            d_atoms = reinterpret_cast<const float4*>(dbase + atom_off[j]);
+        }
+        size_t o = atom_bytes + tab_off[j];
+        int* off = reinterpret_cast<int*>(h + o);
+        off[0] = 0;
+        for (int u = 0; u < d.n_ions; ++u) off[u + 1] = off[u] + d.atoms_per_ion[u];
+        const int* d_off = reinterpret_cast<const int*>(dbase + o);
+        o = al16(o + (d.n_ions + 1) * sizeof(int));
+        aff_table(d.n_ions, d.atoms_per_ion, d.coeffs, d.ion_rads, d.flags, d.solvent_ed, d.c1, G.Lp, G.step, aff);
+        const void* d_aff = dbase + o;
+        if (fp32) {
+            float* af = reinterpret_cast<float*>(h + o);
+            for (size_t k = 0; k < aff.size(); ++k) af[k] = (float)aff[k];
+            o = al16(o + aff.size() * sizeof(float));
+        } else {
+            std::memcpy(h + o, aff.data(), aff.size() * sizeof(double));
+            o = al16(o + aff.size() * sizeof(double));
+        }
+        std::memcpy(h + o, prefs[j].data(), prefs[j].size() * sizeof(int64_t));
+        const int64_t* d_pref = reinterpret_cast<const int64_t*>(dbase + o);
+        if (fp32) {
+            dpx::FillJob J{};
+            J.atoms = d_atoms;
+            J.ion_off = d_off;
+            J.aff_f32 = (const float*)d_aff;
+            J.pref = d_pref;
+            J.grid = (float4*)grids[j]->cells;
+            J.n_items = n_items[j];
+            J.tile_start = tiles;
+            J.step = G.step;
+            J.cx = cen[3 * j];
+            J.cy = cen[3 * j + 1];
+            J.cz = cen[3 * j + 2];
+            J.use_center = (J.cx != 0.0 || J.cy != 0.0 || J.cz != 0.0);
+            J.U = d.n_ions;
+            J.Lp = G.Lp;
+            J.scale = (float)d.scale;
+            jobs.push_back(J);
+            tiles += (n_items[j] + threads - 1) / threads;
+        }
+    }
+    if (!jobs.empty()) std::memcpy(h + jobs_off, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
+    DPX_CUDA(cudaMemcpyAsync(dbase, h, counter_off, cudaMemcpyHostToDevice, s));
+    if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
+    cudaError_t e = dpx::launch_fill_f32_batch(s, (const dpx::FillJob*)(dbase + jobs_off), (int)jobs.size(), tiles,
+                                               (unsigned long long*)(dbase + counter_off), cpt, threads, persistent);
+    if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
+    if (ev1) DPX_CUDA(cudaEventRecord(ev1, s));
+    for (int j = 0; j < n; ++j) {  // the plain FP64 path: one launch per leaf
+        if (grids[j]->precision != DPX_FP64) continue;
+        const dpx_pdb_desc& d = pdbs[j];
+        const size_t o = atom_bytes + tab_off[j];
+        const size_t oa = al16(o + (d.n_ions + 1) * sizeof(int));
+        const size_t op = al16(oa + (size_t)d.n_ions * (grids[j]->g.Lp + 1) * sizeof(double));
+        const float4* d_atoms = d.atoms_on_device ? reinterpret_cast<const float4*>(d.atoms)
+                                                  : reinterpret_cast<const float4*>(dbase + atom_off[j]);
+        e = dpx::launch_fill_f64(s, d_atoms, (const int*)(dbase + o), d.n_ions, (const double*)(dbase + oa),
+                                 grids[j]->g, (const int64_t*)(dbase + op), n_items[j], &cen[3 * j], d.scale,
+                                 (double4_32a*)grids[j]->cells);
+        if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
+    }
+    // the staging buffer is reused by the next call: wait for the copy and the kernels
+    DPX_CUDA(cudaStreamSynchronize(s));
+    return DPX_OK;
+}
+
+}  // namespace dpxh
+
+extern "C" {
+
+int dpx_grid_fill_pdb_batch(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs) {
+    if (n <= 0 || !grids || !grids[0]) return fail(DPX_ERR_ARG, "empty batch");
+    const dpx_ctx ctx = grids[0]->ctx;
+    return fill_batch_impl(n, grids, pdbs, ctx->fill_cpt, ctx->fill_threads, ctx->fill_persistent, nullptr,
+                           nullptr);
+}
+
+int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int repeats, int* best,
+                      float* times_ms) {
+    if (n <= 0 || !grids || !grids[0] || !pdbs) return fail(DPX_ERR_ARG, "empty batch");
+    if (repeats <= 0) return fail(DPX_ERR_ARG, "repeats must be positive");
+    const dpx_ctx ctx = grids[0]->ctx;
+    if (int rc = set_device(ctx)) return rc;
+    cudaEvent_t e0, e1;
+    DPX_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(DPX_ERR_CUDA, "cudaEventCreate");
+    }
+    int rc = DPX_OK, bi = -1;
+    float bt = 0.f;
+    for (int k = 0; k < kFillShapes && !rc; ++k) {
+        float tot = 0.f;
+        for (int r = 0; r <= repeats && !rc; ++r) {  // r = 0 warms up
+            rc = fill_batch_impl(n, grids, pdbs, kFillShape[k][0], kFillShape[k][1], kFillShape[k][2] != 0, e0, e1);
+            float ms = 0.f;
+            if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = fail(DPX_ERR_CUDA, "event timing");
+            if (r > 0) tot += ms;
+        }
+        const float avg = tot / repeats;
+        if (times_ms) times_ms[k] = avg;
+        if (!rc && (bi < 0 || avg < bt)) {
+            bi = k;
+            bt = avg;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    ctx->fill_cpt = kFillShape[bi][0];
+    ctx->fill_threads = kFillShape[bi][1];
+    ctx->fill_persistent = kFillShape[bi][2] != 0;
+    if (best) {
+        best[0] = ctx->fill_cpt;
+        best[1] = ctx->fill_threads;
+        best[2] = ctx->fill_persistent;
+    }
+    // leave the grids filled with the chosen shape (every shape gives the same cells)
+    return DPX_OK;
+}
+
 int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms_on_device, int n_ions,
                       const int* atoms_per_ion, const double* coeffs, const double* ion_rads, int flags,
                       double solvent_ed, double c1, double scale, const double* center) {
     if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
-    if (n_atoms <= 0 || !atoms) return fail(DPX_ERR_ARG, "no atoms");
-    if (n_atoms > INT_MAX) return fail(DPX_ERR_ARG, "too many atoms (%lld)", (long long)n_atoms);
-    if (n_ions <= 0 || n_ions > 256 || !atoms_per_ion || !coeffs || !ion_rads)
-        return fail(DPX_ERR_ARG, "bad ion description");
-    int64_t tot = 0;
-    for (int u = 0; u < n_ions; ++u) {
-        if (atoms_per_ion[u] < 0) return fail(DPX_ERR_ARG, "negative atoms_per_ion");
-        tot += atoms_per_ion[u];
-    }
-    if (tot != n_atoms) return fail(DPX_ERR_ARG, "atoms_per_ion sums to %lld, n_atoms=%lld", (long long)tot,
-                                    (long long)n_atoms);
-    dpx_ctx ctx = g->ctx;
-    if (int rc = set_device(ctx)) return rc;
-    const Geom& G = g->g;
-    cudaStream_t s = ctx->stream;
-
-    // centring: atoms are shifted by c on the host; the kernel restores e^{i q.c}
-    double cen[3] = {0, 0, 0};
-    if (center) {
-        for (int k = 0; k < 3; ++k) cen[k] = center[k];
-    } else if (!atoms_on_device && g->precision == DPX_FP32) {
-        double acc[3] = {0, 0, 0};
-        for (int64_t j = 0; j < n_atoms; ++j)
-            for (int k = 0; k < 3; ++k) acc[k] += atoms[4 * j + k];
-        for (int k = 0; k < 3; ++k) cen[k] = acc[k] / double(n_atoms);
-    }
-    if (g->precision == DPX_FP64 && !atoms_on_device) cen[0] = cen[1] = cen[2] = 0.0;  // FP64 phases need no centring
-
-    // host atoms are shifted by the centre here; device atoms are taken as
-    // already shifted by the caller (r_device = r - center)
-    const float4* d_atoms = reinterpret_cast<const float4*>(atoms);
-    if (!atoms_on_device) {
-        DPX_CUDA(ctx->atoms.reserve((size_t)n_atoms * sizeof(float4)));
-        ctx->host_stage.resize((size_t)n_atoms * sizeof(float4));
-        float4* h = reinterpret_cast<float4*>(ctx->host_stage.data());
-        for (int64_t j = 0; j < n_atoms; ++j) {
-            h[j].x = (float)((double)atoms[4 * j] - cen[0]);
-            h[j].y = (float)((double)atoms[4 * j + 1] - cen[1]);
-            h[j].z = (float)((double)atoms[4 * j + 2] - cen[2]);
-            h[j].w = 0.f;
-        }
-        DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h, (size_t)n_atoms * sizeof(float4), cudaMemcpyHostToDevice, s));
-        d_atoms = reinterpret_cast<const float4*>(ctx->atoms.p);
-        DPX_CUDA(cudaStreamSynchronize(s));  // host_stage is reused by the next call
-    }
-
-    std::vector<int> off(n_ions + 1, 0);
-    for (int u = 0; u < n_ions; ++u) off[u + 1] = off[u] + atoms_per_ion[u];
-    std::vector<double> aff;
-    aff_table(n_ions, atoms_per_ion, coeffs, ion_rads, flags, solvent_ed, c1, G.Lp, G.step, aff);
-    const size_t tb = aff.size() * (g->precision == DPX_FP64 ? sizeof(double) : sizeof(float));
-    DPX_CUDA(ctx->table.reserve(tb));
-    std::vector<float> affF;
-    if (g->precision == DPX_FP32) affF.assign(aff.begin(), aff.end());
-    DPX_CUDA(cudaMemcpyAsync(ctx->table.p, g->precision == DPX_FP64 ? (const void*)aff.data() : (const void*)affF.data(),
-                             tb, cudaMemcpyHostToDevice, s));
-    // work-item prefix of the row-factored fill, placed after the ion offsets
-    const int cpt = g->precision == DPX_FP64 ? dpx::kFill64Cells : ctx->fill_cpt;
-    std::vector<int64_t> pref(G.Lp + 1);
-    const int64_t n_items = dpx::fill_items(G, cpt, pref.data());
-    const size_t off_bytes = (off.size() * sizeof(int) + 15) & ~size_t(15);
-    DPX_CUDA(ctx->ions.reserve(off_bytes + pref.size() * sizeof(int64_t)));
-    DPX_CUDA(cudaMemcpyAsync(ctx->ions.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    const int64_t* d_pref = reinterpret_cast<const int64_t*>(static_cast<char*>(ctx->ions.p) + off_bytes);
-    DPX_CUDA(cudaMemcpyAsync((void*)d_pref, pref.data(), pref.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-
-    cudaError_t e;
-    if (g->precision == DPX_FP64)
-        e = dpx::launch_fill_f64(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const double*)ctx->table.p, G, d_pref,
-                                 n_items, cen, scale, (double4_32a*)g->cells);
-    else
-        e = dpx::launch_fill_f32(s, d_atoms, (const int*)ctx->ions.p, n_ions, (const float*)ctx->table.p, G, d_pref,
-                                 n_items, cen, (float)scale, (float4*)g->cells, ctx->fill_cpt, ctx->fill_threads);
-    if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
-    // the host vectors above are consumed by the async copies: wait before they go
-    DPX_CUDA(cudaStreamSynchronize(s));
-    return DPX_OK;
+    dpx_pdb_desc d{n_atoms, atoms, atoms_on_device, n_ions, atoms_per_ion, coeffs, ion_rads, flags,
+                   solvent_ed, c1, scale, center};
+    return dpx_grid_fill_pdb_batch(1, &g, &d);
 }
 
 int dpx_grid_compute_splines(dpx_grid g) {
@@ -458,10 +578,30 @@ int dpx_grid_write(dpx_grid g, const double* values, const double* coeffs) {
 
 }  // extern "C"
 
-namespace {
+namespace dpxh {
 // Model structs and docked rotation groups (ManualSymmetry translationsPerOrientation
 // grouped by identical Euler triples, first-appearance order); group tables are
 // staged for ctx->groups, model structs point into it.
+void make_brackets(const dpx::Geom& G, int grid_size, double qmax, int nq, const double* Q, Brackets& b) {
+    std::vector<int> layer_of_q(nq);
+    dpx::q_brackets(grid_size, qmax, nq, Q, layer_of_q.data());
+    b = Brackets{};
+    for (int l = 0; l < G.L; ++l) {
+        int cnt = 0;
+        for (int k = 0; k < nq; ++k)
+            if (layer_of_q[k] == l) {
+                b.q.push_back(Q[k]);
+                b.qidx.push_back(k);
+                cnt++;
+            }
+        if (cnt) {
+            b.layer.push_back(l);
+            b.off.push_back((int)b.q.size());
+            b.max_q = std::max(b.max_q, cnt);
+        }
+    }
+}
+
 int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
                    const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
                    std::vector<dpx::ModelDev>& md, std::vector<char>& gstage) {
@@ -533,7 +673,7 @@ int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const doubl
     return DPX_OK;
 }
 
-}  // namespace
+}  // namespace dpxh
 
 extern "C" {
 
@@ -566,25 +706,11 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
 
 
     // brackets
-    std::vector<int> layer_of_q(nq);
-    q_brackets(grid_size, qmax, nq, Q, layer_of_q.data());
-    std::vector<int> br_layer, br_off{0}, br_qidx;
-    std::vector<double> br_q;
-    int max_q = 1;
-    for (int l = 0; l < G.L; ++l) {
-        int cnt = 0;
-        for (int k = 0; k < nq; ++k)
-            if (layer_of_q[k] == l) {
-                br_q.push_back(Q[k]);
-                br_qidx.push_back(k);
-                cnt++;
-            }
-        if (cnt) {
-            br_layer.push_back(l);
-            br_off.push_back((int)br_q.size());
-            max_q = std::max(max_q, cnt);
-        }
-    }
+    Brackets B;
+    make_brackets(G, grid_size, qmax, nq, Q, B);
+    const std::vector<int>&br_layer = B.layer, &br_off = B.off, &br_qidx = B.qidx;
+    const std::vector<double>& br_q = B.q;
+    const int max_q = B.max_q;
     const int nbr = (int)br_layer.size();
     dpx::AvgPlan plan{};
     plan.n_brackets = nbr;
@@ -1086,6 +1212,95 @@ int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
     dpx_grid_destroy(g);
     dpx_ctx_destroy(ctx);
     return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Shared body of the host-buffer assembly drop-ins: source grids from host
+// (values, derivatives) pairs, destination from outData (values only), one
+// dpx_grid_assemble, values copied back.  accumulate = 0 starts from zero
+// (GPUSumGridsJacobSphr overwrites its output).
+int assemble_host(int64_t voxels, int thDivs, int phDivs, double stepSize, int n, const double* const* inAmp,
+                  const double* const* inD, const double* rot, const double* tr, const int* n_copies,
+                  const double* copy_rot, const double* copy_tr, const double* sym_scale, const double* lattice,
+                  double scale, double* outData, bool accumulate, int precision, int* pStop) {
+    if (!outData || !inAmp || !inD || n <= 0) return fail(DPX_ERR_ARG, "NULL buffer");
+    for (int m = 0; m < n; ++m)
+        if (!inAmp[m] || !inD[m]) return fail(DPX_ERR_ARG, "NULL source grid");
+    int grid_size;
+    double qmax;
+    if (int rc = grid_from_voxels(voxels, thDivs, phDivs, stepSize, &grid_size, &qmax)) return rc;
+    if (pStop && *pStop) return fail(DPX_ERR_STOPPED, "stopped");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dpx_ctx ctx;
+    if (int rc = dpx_ctx_create(dev, &ctx)) return rc;
+    std::vector<dpx_grid> src(n, nullptr);
+    dpx_grid dst = nullptr;
+    int rc = dpx_grid_create(ctx, grid_size, qmax, precision, &dst);
+    for (int m = 0; m < n && !rc; ++m) {
+        rc = dpx_grid_create(ctx, grid_size, qmax, precision, &src[m]);
+        if (!rc) rc = dpx_grid_write(src[m], inAmp[m], inD[m]);
+    }
+    if (!rc && accumulate) rc = dpx_grid_write(dst, outData, nullptr);
+    if (!rc) rc = dpx_grid_assemble(dst, n, src.data(), rot, tr, n_copies, copy_rot, copy_tr, sym_scale, lattice, scale);
+    if (!rc) rc = dpx_grid_read(dst, outData, nullptr);
+    if (!rc && pStop && *pStop) rc = fail(DPX_ERR_STOPPED, "stopped");
+    for (dpx_grid g : src)
+        if (g) dpx_grid_destroy(g);
+    if (dst) dpx_grid_destroy(dst);
+    dpx_ctx_destroy(ctx);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dpx_calc_man_sym_jacob_sphr(int64_t voxels, int thDivs, int phDivs, int numCopies, double stepSize,
+                                const double* inModel, double* outData, const double* ds, const double* locX,
+                                const double* locY, const double* locZ, const double* locA, const double* locB,
+                                const double* locC, double scale, int precision, int* pStop) {
+    if (numCopies <= 0) return fail(DPX_ERR_ARG, "numCopies must be positive");
+    if (!locX || !locY || !locZ || !locA || !locB || !locC) return fail(DPX_ERR_ARG, "NULL location array");
+    // entry 0 places the inner object; entries 1..numCopies are the copies
+    const double rot[3] = {locA[0], locB[0], locC[0]}, tr[3] = {locX[0], locY[0], locZ[0]};
+    std::vector<double> crot(3 * (size_t)numCopies), ctr(3 * (size_t)numCopies);
+    for (int k = 0; k < numCopies; ++k) {
+        crot[3 * k] = locA[k + 1];
+        crot[3 * k + 1] = locB[k + 1];
+        crot[3 * k + 2] = locC[k + 1];
+        ctr[3 * k] = locX[k + 1];
+        ctr[3 * k + 1] = locY[k + 1];
+        ctr[3 * k + 2] = locZ[k + 1];
+    }
+    return assemble_host(voxels, thDivs, phDivs, stepSize, 1, &inModel, &ds, rot, tr, &numCopies, crot.data(),
+                         ctr.data(), &scale, nullptr, 1.0, outData, true, precision, pStop);
+}
+
+int dpx_calc_spc_fill_sym_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSize, const double* inModel,
+                                     double* outData, const double* ds, const double* vectorMatrix,
+                                     const double* repeats, const double* innerRots, const double* innerTrans,
+                                     double scale, int precision, int* pStop) {
+    if (!vectorMatrix || !repeats || !innerRots || !innerTrans) return fail(DPX_ERR_ARG, "NULL lattice argument");
+    // SymmetryGenJacob.cu:83-125 multiplies by sum_n e^{-i n q.a}, the complex
+    // conjugate of GridSymmetry::calcAmplitude's sum_n e^{+i n q.a}; the same
+    // lattice sum over -a reproduces it
+    double lat[12];
+    for (int k = 0; k < 9; ++k) lat[k] = -vectorMatrix[k];
+    for (int k = 0; k < 3; ++k) lat[9 + k] = repeats[k];
+    return assemble_host(voxels, thDivs, phDivs, stepSize, 1, &inModel, &ds, innerRots, innerTrans, nullptr, nullptr,
+                         nullptr, nullptr, lat, scale, outData, true, precision, pStop);
+}
+
+int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* const* inAmpData,
+                             const double* const* inD, const double* trans, const double* rots, int numGrids,
+                             double* outAmpData, int precision, int* pStop) {
+    if (numGrids <= 0 || !trans || !rots) return fail(DPX_ERR_ARG, "bad grid list");
+    return assemble_host(voxels, thDivs, phDivs, stepSz, numGrids, inAmpData, inD, rots, trans, nullptr, nullptr,
+                         nullptr, nullptr, nullptr, 1.0, outAmpData, false, precision, pStop);
 }
 
 }  // extern "C"

@@ -1,4 +1,4 @@
-// dpx_fill.cu — amplitude grid fill of a PDB leaf on the JacobianSphereGrid,
+// dpx_fill.cu — amplitude grid fill of PDB leaves on the JacobianSphereGrid,
 //   F(q) = scale * sum_u aff_u(|q|) sum_{j in u} e^{i q.r_j}
 // (D+ PDBAmplitude.cpp:243-317 evaluated on every cell by Grid.cpp:760-826;
 // the reference GPU kernel is PDBAmplitudeCUDA.cu:134-186).
@@ -16,7 +16,10 @@
 // Sin/cos evaluations per cell drop from 1 to (1 + 1/CPT) / 4.
 //
 // Work items: origin first, then per shell (floor(3i/2)+1) rows x ceil(3i/CPT)
-// column chunks of CPT cells; item_pref[i] is the first item after shell i.
+// column chunks of CPT cells; a job's item_pref[i] is the first item after
+// shell i.  The FP32 fill is one persistent launch over a batch of jobs
+// (structures of any size, on grids of any size): blocks take tiles of THREADS
+// items of one job from an atomic counter until the batch is done.
 #include "dpx_internal.h"
 
 #include <cuda_runtime.h>
@@ -69,17 +72,16 @@ __device__ __forceinline__ void store_quad(V2* __restrict__ g2, int i, int t, in
 // FP32 bulk: FP32 phases, SFU __sincosf, FP32 sums (per atom tile, then scaled
 // by the ion's form factor into the cell accumulators); the centring
 // translation c is restored per cell as e^{i q.c} in FP64.
+// fill_tile computes THREADS consecutive work items of one job; the job's
+// fields arrive as scalar __restrict__ arguments so that the inner loop keeps
+// them in registers.
 // --------------------------------------------------------------------------
 template <int CPT, int THREADS>
-__global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restrict__ atoms,
-                                                           const int* __restrict__ ion_off, int U,
-                                                           const float* __restrict__ aff, int Lp, double step,
-                                                           const int64_t* __restrict__ pref, double cx, double cy,
-                                                           double cz, int use_center, float scale,
-                                                           float4* __restrict__ grid) {
-    __shared__ float4 s_atoms[THREADS];
-    const int64_t w = (int64_t)blockIdx.x * THREADS + threadIdx.x;
-    const int64_t n_items = pref[Lp];
+__device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, const int* __restrict__ ion_off, int U,
+                                          const float* __restrict__ aff, const int64_t* __restrict__ pref,
+                                          float4* __restrict__ grid, int64_t n_items, int Lp, double step, double cx,
+                                          double cy, double cz, int use_center, float scale, int64_t w,
+                                          float4* __restrict__ s_atoms) {
     const bool active = w < n_items;
     Item it{0, 0, 0};
     if (active && w > 0) it = find_item(w, pref, Lp, CPT);
@@ -102,7 +104,6 @@ __global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restr
 #pragma unroll
         for (int k = 0; k < CPT; ++k) qx[k] = qy[k] = 0.f;
     }
-    const int layer = i;
 
     float fR[CPT], fI[CPT], gR[CPT], gI[CPT];
 #pragma unroll
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restr
 
     for (int u = 0; u < U; ++u) {
         const int a0 = ion_off[u], a1 = ion_off[u + 1];
-        const float f = aff[(int64_t)u * (Lp + 1) + layer];
+        const float f = aff[(int64_t)u * (Lp + 1) + i];
         for (int t0 = a0; t0 < a1; t0 += THREADS) {
             const int n = min(THREADS, a1 - t0);
             __syncthreads();
@@ -169,8 +170,59 @@ __global__ void __launch_bounds__(THREADS) fill_f32_kernel(const float4* __restr
     }
 }
 
+__device__ __forceinline__ int job_of_tile(const FillJob* __restrict__ jobs, int n_jobs, int64_t tile) {
+    int lo = 0, hi = n_jobs - 1;  // last job with tile_start <= tile
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].tile_start <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int CPT, int THREADS>
+__device__ __forceinline__ void run_tile(const FillJob& J, int64_t tile, float4* s_atoms) {
+    fill_tile<CPT, THREADS>(J.atoms, J.ion_off, J.U, J.aff_f32, J.pref, J.grid, J.n_items, J.Lp, J.step, J.cx, J.cy,
+                            J.cz, J.use_center, J.scale, (tile - J.tile_start) * THREADS + threadIdx.x, s_atoms);
+}
+
+// Persistent form: one CTA per resident slot, tiles of every job pulled from
+// an atomic counter; the job record is staged once per tile in shared memory.
+template <int CPT, int THREADS>
+__global__ void __launch_bounds__(THREADS) fill_f32_persistent(const FillJob* __restrict__ jobs, int n_jobs,
+                                                               int64_t total_tiles,
+                                                               unsigned long long* __restrict__ counter) {
+    __shared__ float4 s_atoms[THREADS];
+    __shared__ FillJob s_job;
+    __shared__ long long s_tile;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const long long t = (long long)atomicAdd(counter, 1ull);
+            s_tile = t;
+            if (t < total_tiles) s_job = jobs[job_of_tile(jobs, n_jobs, t)];
+        }
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= total_tiles) break;
+        const FillJob J = s_job;
+        run_tile<CPT, THREADS>(J, tile, s_atoms);
+    }
+}
+
+// Flat form: one CTA per tile over the whole batch; the hardware block
+// scheduler hands out the tiles in order.
+template <int CPT, int THREADS>
+__global__ void __launch_bounds__(THREADS) fill_f32_flat(const FillJob* __restrict__ jobs, int n_jobs) {
+    __shared__ float4 s_atoms[THREADS];
+    const int64_t tile = blockIdx.x;
+    const FillJob J = jobs[job_of_tile(jobs, n_jobs, tile)];
+    run_tile<CPT, THREADS>(J, tile, s_atoms);
+}
+
 // --------------------------------------------------------------------------
 // Plain FP64: FP64 q vector (sincospi), FP64 phases, FP64 sincos, FP64 sums.
+// One job per launch.
 // --------------------------------------------------------------------------
 template <int CPT, int THREADS>
 __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restrict__ atoms,
@@ -272,6 +324,28 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
 
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+template <int CPT, int TH>
+cudaError_t launch_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
+                         unsigned long long* d_counter, bool persistent) {
+    if (!persistent) {
+        if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+        fill_f32_flat<CPT, TH><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
+        return cudaGetLastError();
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_f32_persistent<CPT, TH>, TH, 0);
+    if (e != cudaSuccess) return e;
+    int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (blocks > total_tiles) blocks = total_tiles;
+    e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    fill_f32_persistent<CPT, TH><<<(unsigned)blocks, TH, 0, s>>>(d_jobs, n_jobs, total_tiles, d_counter);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 int64_t fill_items(const Geom& g, int cpt, int64_t* pref) {
@@ -280,18 +354,12 @@ int64_t fill_items(const Geom& g, int cpt, int64_t* pref) {
     return pref[g.Lp];
 }
 
-cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
-                            const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
-                            float scale, float4* grid, int cells_per_thread, int block) {
-    if (n_items <= 0) return cudaSuccess;
-    const int use_center = (center[0] != 0.0 || center[1] != 0.0 || center[2] != 0.0);
-#define DPX_FILL_CASE(CPT, TH)                                                                                  \
-    if (cells_per_thread == CPT && block == TH) {                                                              \
-        fill_f32_kernel<CPT, TH><<<blocks_for(n_items, TH), TH, 0, s>>>(atoms, ion_off, U, aff, g.Lp, g.step,  \
-                                                                       d_pref, center[0], center[1], center[2], \
-                                                                       use_center, scale, grid);               \
-        return cudaGetLastError();                                                                             \
-    }
+cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
+                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent) {
+    if (n_jobs <= 0 || total_tiles <= 0) return cudaSuccess;
+#define DPX_FILL_CASE(CPT, TH) \
+    if (cells_per_thread == CPT && block == TH)     \
+        return launch_batch<CPT, TH>(s, d_jobs, n_jobs, total_tiles, d_counter, persistent);
     DPX_FILL_CASE(2, 256) DPX_FILL_CASE(4, 128) DPX_FILL_CASE(4, 256) DPX_FILL_CASE(6, 128) DPX_FILL_CASE(6, 256)
     DPX_FILL_CASE(8, 128) DPX_FILL_CASE(8, 256)
 #undef DPX_FILL_CASE

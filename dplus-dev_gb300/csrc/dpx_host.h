@@ -1,0 +1,102 @@
+// dpx_host.h — host-side internals shared by the libdpx translation units
+// (dpx_api.cpp, dpx_batch.cpp, dpx_server.cpp): the context and grid handles,
+// status helpers and the staging routines.  Not part of the C-ABI.
+#pragma once
+#include "dpx.h"
+#include "dpx_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+namespace dpxh {
+
+// Records the per-thread message returned by dpx_last_error; returns code.
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* where);
+
+#define DPX_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return dpxh::cuda_fail(e_, #call);   \
+    } while (0)
+
+constexpr double kPi = 3.14159265358979323846;
+
+// Grow-only device buffer owned by a context.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
+
+}  // namespace dpxh
+
+struct dpx_ctx_s {
+    int device = 0;
+    int refs = 1;  // the caller's handle + one per live grid / batch / server
+    bool closed = false;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    int fill_cpt = 8, fill_threads = 128;  // FP32 fill shape (dpx_autotune_fill)
+    bool fill_persistent = false;
+    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs;
+    std::vector<char> host_stage;
+};
+
+struct dpx_grid_s {
+    dpx_ctx ctx;
+    int grid_size;
+    double qmax;
+    int precision;
+    dpx::Geom g;
+    void* cells;
+};
+
+namespace dpxh {
+
+int set_device(dpx_ctx ctx);
+void ctx_retain(dpx_ctx ctx);
+void ctx_release(dpx_ctx ctx);
+size_t cell_bytes(int precision);
+extern const int kFillShape[][3];
+extern const int kFillShapes;
+
+// Unique-ion form factors minus the dummy-atom solvent for shells 0..Lp, [U][Lp+1].
+void aff_table(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed,
+               double c1, int Lp, double step, std::vector<double>& out);
+// Tait-Bryan X1Y2Z3 rotation (EulerD).
+void euler(double a, double b, double c, double R[9]);
+int check_pdb(const dpx_pdb_desc& d);
+
+// Model structs for the kernels; group tables staged in gstage for ctx->groups.
+int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                   const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                   std::vector<dpx::ModelDev>& md, std::vector<char>& gstage);
+
+// Bracket tables of one orientation average (IntegrateLayersTogether).
+struct Brackets {
+    std::vector<int> layer, off{0}, qidx;
+    std::vector<double> q;
+    int max_q = 1;
+};
+void make_brackets(const dpx::Geom& G, int grid_size, double qmax, int nq, const double* Q, Brackets& b);
+
+}  // namespace dpxh

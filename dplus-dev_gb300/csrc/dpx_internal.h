@@ -70,9 +70,27 @@ int set_error(int code, const char* msg);  // records the per-thread message, re
 // pref[0..Lp] (origin, then per shell (floor(3i/2)+1) rows x ceil(3i/cpt)
 // column chunks) and returns the item count.
 int64_t fill_items(const Geom& g, int cpt, int64_t* pref);
-cudaError_t launch_fill_f32(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const float* aff,
-                            const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
-                            float scale, float4* grid, int cells_per_thread, int block);
+
+// One structure on one grid in a batched FP32 fill.  Its items occupy tiles
+// [tile_start, tile_start + ceil(n_items / threads)); jobs are in ascending
+// tile_start order.
+struct FillJob {
+    const float4* atoms;    // centred, sorted by ion
+    const int* ion_off;     // [U + 1]
+    const float* aff_f32;   // [U][Lp + 1]
+    const int64_t* pref;    // [Lp + 1] item prefix
+    float4* grid;
+    int64_t n_items;
+    int64_t tile_start;
+    double step;
+    double cx, cy, cz;
+    int U, Lp, use_center;
+    float scale;
+};
+// One launch over every tile of every job: persistent (one CTA per resident
+// slot, atomic tile counter d_counter) or flat (one CTA per tile).
+cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
+                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent);
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
                             const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
                             double scale, double4_32a* grid);

@@ -34,6 +34,13 @@ _F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int)
 _U32 = C.POINTER(C.c_uint32)
 
+
+class PdbDesc(C.Structure):
+    """dpx_pdb_desc: one leaf of dpx_grid_fill_pdb_batch."""
+    _fields_ = [("n_atoms", C.c_int64), ("atoms", _P), ("atoms_on_device", C.c_int), ("n_ions", C.c_int),
+                ("atoms_per_ion", _I), ("coeffs", _D), ("ion_rads", _D), ("flags", C.c_int),
+                ("solvent_ed", C.c_double), ("c1", C.c_double), ("scale", C.c_double), ("center", _D)]
+
 _SIGS = {
     "dpx_last_error": (C.c_char_p, []),
     "dpx_version": (C.c_int, []),
@@ -43,6 +50,9 @@ _SIGS = {
     "dpx_ctx_get_stream": (_P, [_P]),
     "dpx_ctx_synchronize": (C.c_int, [_P]),
     "dpx_ctx_set_fill_shape": (C.c_int, [_P, C.c_int, C.c_int]),
+    "dpx_ctx_set_fill_schedule": (C.c_int, [_P, C.c_int]),
+    "dpx_ctx_get_fill_shape": (C.c_int, [_P, _I]),
+    "dpx_fill_shapes": (C.c_int, [_I]),
     "dpx_grid_cells": (C.c_int64, [C.c_int]),
     "dpx_grid_bytes": (C.c_int64, [C.c_int, C.c_int]),
     "dpx_grid_create": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.POINTER(_P)]),
@@ -51,6 +61,8 @@ _SIGS = {
     "dpx_grid_info": (C.c_int, [_P, _I, _D, _I, C.POINTER(C.c_int64)]),
     "dpx_grid_fill_pdb": (C.c_int, [_P, C.c_int64, _P, C.c_int, C.c_int, _I, _D, _D, C.c_int, C.c_double,
                                     C.c_double, C.c_double, _D]),
+    "dpx_grid_fill_pdb_batch": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(PdbDesc)]),
+    "dpx_autotune_fill": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(PdbDesc), C.c_int, _I, _F]),
     "dpx_grid_compute_splines": (C.c_int, [_P]),
     "dpx_grid_read": (C.c_int, [_P, _D, _D]),
     "dpx_grid_write": (C.c_int, [_P, _D, _D]),
@@ -70,6 +82,12 @@ _SIGS = {
                                                   C.c_int, _I]),
     "dpx_calc_mcoa_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, C.c_int,
                                            C.c_int64, C.c_double, _D, C.c_int64, C.c_int, _I]),
+    "dpx_calc_man_sym_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, _D,
+                                              _D, _D, _D, _D, C.c_double, C.c_int, _I]),
+    "dpx_calc_spc_fill_sym_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, _D, _D,
+                                                   _D, C.c_double, C.c_int, _I]),
+    "dpx_sum_grids_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, C.POINTER(_D), C.POINTER(_D),
+                                           _D, _D, C.c_int, _D, C.c_int, _I]),
     "dpx_mc_average_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, _D, _P, C.c_int64, C.c_double,
                                          _P, _P]),
 }

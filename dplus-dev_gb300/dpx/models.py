@@ -44,6 +44,15 @@ class Context:
     def set_stream(self, stream_ptr: int | None) -> None:
         check(lib().dpx_ctx_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
 
+    def set_fill_schedule(self, persistent: bool) -> None:
+        check(lib().dpx_ctx_set_fill_schedule(self.handle, int(bool(persistent))))
+
+    def fill_shape(self):
+        """(cells_per_thread, threads, persistent) of the FP32 fill."""
+        out = np.zeros(3, dtype=np.int32)
+        check(lib().dpx_ctx_get_fill_shape(self.handle, iptr(out)))
+        return tuple(int(v) for v in out)
+
     def set_fill_shape(self, cells_per_thread: int, threads: int) -> None:
         check(lib().dpx_ctx_set_fill_shape(self.handle, cells_per_thread, threads))
 
@@ -187,19 +196,75 @@ class PDBAmplitude:
         h.update(repr((self.scale, self.solventED, self.c1, self.flags)).encode())
         return h.hexdigest()
 
+    def _key(self, ctx: Context, qmax: float, gridSize: int, precision: int):
+        return (self.hash(), int(gridSize), float(qmax), int(precision), ctx.device)
+
     def calculateGrid(self, ctx: Context, qmax: float, gridSize: int, precision: int = FP32) -> Grid:
         """Fill (or reuse) the device-resident amplitude grid and its splines."""
-        key = (self.hash(), int(gridSize), float(qmax), int(precision), ctx.device)
-        if self._grid is not None and self._grid_key == key:
-            return self._grid
-        g = Grid(ctx, gridSize, qmax, precision)
-        a = self.atoms_float4()
-        check(lib().dpx_grid_fill_pdb(g.handle, len(a), a.ctypes.data_as(C.c_void_p), 0, len(self.unique),
-                                      iptr(self.atoms_per_ion), dptr(self.coeffs), dptr(self.ion_rads), self.flags,
-                                      self.solventED, self.c1, self.scale, None))
-        g.compute_splines()
-        self._grid, self._grid_key = g, key
-        return g
+        return calculate_grids(ctx, [self], qmax, gridSize, precision)[0]
+
+
+def pdb_descs(leaves: Sequence[PDBAmplitude]):
+    """dpx_pdb_desc array of PDB leaves (host atoms, centroid centring) and the
+    numpy arrays it points into, which must outlive the call."""
+    keep, descs = [], (_lib.PdbDesc * len(leaves))()
+    for d, a in zip(descs, leaves):
+        at = a.atoms_float4()
+        keep += [at, a.atoms_per_ion, a.coeffs, a.ion_rads]
+        d.n_atoms, d.atoms, d.atoms_on_device, d.n_ions = len(at), at.ctypes.data, 0, len(a.unique)
+        d.atoms_per_ion, d.coeffs, d.ion_rads = iptr(a.atoms_per_ion), dptr(a.coeffs), dptr(a.ion_rads)
+        d.flags, d.solvent_ed, d.c1, d.scale, d.center = a.flags, a.solventED, a.c1, a.scale, None
+    return descs, keep
+
+
+def autotune_fill(ctx: Context, leaves: Sequence[PDBAmplitude], qmax: float, gridSize: int, repeats: int = 2):
+    """Project autotuner: time every FP32 fill shape on these leaves and keep
+    the fastest in the context.  Returns (best (cpt, threads, persistent),
+    {shape: ms})."""
+    n_shapes = lib().dpx_fill_shapes(None)
+    shapes = np.zeros(3 * n_shapes, dtype=np.int32)
+    lib().dpx_fill_shapes(iptr(shapes))
+    grids = [Grid(ctx, gridSize, qmax, FP32) for _ in leaves]
+    descs, keep = pdb_descs(leaves)
+    handles = (C.c_void_p * len(grids))(*[g.handle.value for g in grids])
+    best = np.zeros(3, dtype=np.int32)
+    times = np.zeros(n_shapes, dtype=np.float32)
+    check(lib().dpx_autotune_fill(len(grids), handles, descs, int(repeats), iptr(best),
+                                  times.ctypes.data_as(C.POINTER(C.c_float))))
+    for g in grids:
+        g.close()
+    table = {tuple(int(v) for v in shapes[3 * k:3 * k + 3]): float(times[k]) for k in range(n_shapes)}
+    return tuple(int(v) for v in best), table
+
+
+def calculate_grids(ctx: Context, leaves: Sequence[PDBAmplitude], qmax: float, gridSize: int,
+                    precision: int = FP32) -> list:
+    """Grids of several PDB leaves; the ones not cached are filled by ONE
+    dpx_grid_fill_pdb_batch call (a single persistent launch for FP32)."""
+    todo, seen = [], set()
+    for a in leaves:
+        key = a._key(ctx, qmax, gridSize, precision)
+        if (a._grid is None or a._grid_key != key) and id(a) not in seen:
+            todo.append((a, key))
+            seen.add(id(a))
+    if todo:
+        grids = [Grid(ctx, gridSize, qmax, precision) for _ in todo]
+        descs, keep = pdb_descs([a for a, _ in todo])
+        handles = (C.c_void_p * len(todo))(*[g.handle.value for g in grids])
+        check(lib().dpx_grid_fill_pdb_batch(len(todo), handles, descs))
+        for g, (a, key) in zip(grids, todo):
+            g.compute_splines()
+            a._grid, a._grid_key = g, key
+    return [a._grid for a in leaves]
+
+
+def _pdb_leaves(node, out: list) -> list:
+    """Every PDBAmplitude under a model tree node."""
+    if isinstance(node, PDBAmplitude):
+        out.append(node)
+    for c in ([node.child] if hasattr(node, "child") else []) + list(getattr(node, "children", [])):
+        _pdb_leaves(c, out)
+    return out
 
 
 def _pack_models(placements):
@@ -321,6 +386,11 @@ class DomainModel:
         self.precision = precision
 
     def placements(self, ctx: Context):
+        leaves = []
+        for a in self.amps:
+            _pdb_leaves(a, leaves)
+        if leaves:  # fill every missing leaf grid in one batched launch
+            calculate_grids(ctx, leaves, self.qMax, self.gridSize, self.precision)
         out = []
         for a in self.amps:
             if hasattr(a, "placement"):

@@ -22,6 +22,9 @@
  *                                       and the hybrid ManualSymmetry docked sum
  *                                       (Backend/DefaultModels/Symmetries.cpp:1079-1166,
  *                                        GPUHybridCalc.cu:467-578)
+ *   dpx_calc_man_sym_jacob_sphr      <- GPUCalcManSymJacobSphrDD (Backend/GPU/GPUHeader.h:185)
+ *   dpx_calc_spc_fill_sym_jacob_sphr <- GPUCalcSpcFillSymJacobSphrDD (GPUHeader.h:214)
+ *   dpx_sum_grids_jacob_sphr         <- GPUSumGridsJacobSphrDD (GPUHeader.h:255)
  *   dpx_mc_directions / dpx_layer_seeds <- the mt19937 draws of
  *                                       Amplitude.cpp:757-767, 1171-1173, 2764-2780
  */
@@ -66,9 +69,19 @@ int dpx_ctx_set_stream(dpx_ctx ctx, void* stream);
 void* dpx_ctx_get_stream(dpx_ctx ctx);
 int dpx_ctx_synchronize(dpx_ctx ctx);
 /* FP32 amplitude-kernel launch shape: phi cells per work item x threads per
- * block, chosen by the autotuner (default 8 x 128).  Supported: 2x256, 4x128,
- * 4x256, 6x128, 6x256, 8x128, 8x256. */
+ * block (the threads also set the atoms per shared-memory tile), chosen by
+ * dpx_autotune_fill (default 8 x 128, flat).  Supported: 2x256, 4x128, 4x256,
+ * 6x128, 6x256, 8x128, 8x256. */
 int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cells_per_thread, int threads);
+/* FP32 fill schedule: 0 = flat (one CTA per tile of THREADS work items, the
+ * hardware hands them out), 1 = persistent (one CTA per resident slot pulling
+ * tiles from an atomic counter). */
+int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent);
+/* shape[3] = {cells_per_thread, threads, persistent} in use. */
+int dpx_ctx_get_fill_shape(dpx_ctx ctx, int* shape);
+/* The shapes the autotuner sweeps: writes 3 ints per shape (if shapes != NULL)
+ * and returns their number. */
+int dpx_fill_shapes(int* shapes);
 
 /* ---- grid geometry (Grid.cpp:169-200): P = 6 L'(L'+1)^2 + 1, L' = grid_size/2 + 3 ---- */
 int64_t dpx_grid_cells(int grid_size);
@@ -92,6 +105,34 @@ int dpx_grid_info(dpx_grid g, int* grid_size, double* qmax, int* precision, int6
 int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms_on_device, int n_ions,
                       const int* atoms_per_ion, const double* coeffs, const double* ion_rads, int flags,
                       double solvent_ed, double c1, double scale, const double* center);
+/* One PDB leaf of a batched fill: the arguments of dpx_grid_fill_pdb after the grid. */
+typedef struct dpx_pdb_desc {
+    int64_t n_atoms;
+    const float* atoms;
+    int atoms_on_device;
+    int n_ions;
+    const int* atoms_per_ion;
+    const double* coeffs;
+    const double* ion_rads;
+    int flags;
+    double solvent_ed;
+    double c1;
+    double scale;
+    const double* center;
+} dpx_pdb_desc;
+/* Fills n grids (distinct, one context) from n leaves.  The FP32 grids of the
+ * batch share ONE persistent launch that pulls tiles of every leaf from a
+ * common counter, so small leaves no longer leave SMs idle; FP64 grids get a
+ * launch each.  Same results as n calls of dpx_grid_fill_pdb.  The reference
+ * fills each PDBAmplitude in its own call (Amplitude.cpp PDBAmplitude::calculateGrid). */
+int dpx_grid_fill_pdb_batch(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs);
+/* Autotuner (no counterpart in the reference): fills the batch once per shape
+ * of dpx_fill_shapes (after one warm-up fill), times the FP32 fill launch with
+ * CUDA events, averages over `repeats`, and keeps the fastest shape in the
+ * context.  best[3] (optional) receives it, times_ms[dpx_fill_shapes()]
+ * (optional) the average time of each.  The grids end up filled. */
+int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int repeats, int* best,
+                      float* times_ms);
 /* Periodic cubic-spline phi derivatives of every theta row. */
 int dpx_grid_compute_splines(dpx_grid g);
 /* Host copies in the reference's layout: interleaved complex double [2P] each;
@@ -184,6 +225,29 @@ int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
                              const double* inD, const double* qs, double* intensities, int qPoints,
                              int64_t maxIters, double convergence, const double* dirs, int64_t dir_layer_stride,
                              int precision, int* pStop);
+/* GPUCalcManSymJacobSphrDD (Backend/GPU/GPUHeader.h:185, ManSymGenJacob.cu:36-124,
+ * called by ManualSymmetry::calculateGrid Symmetries.cpp:943-945).  loc*
+ * arrays hold numCopies + 1 entries: entry 0 places the inner object, entries
+ * 1..numCopies are the copies (nm, radians).  outData [2 voxels] is
+ * accumulated: outData += scale * sum_k R_k A(R_k^T q) e^{i q.t_k}. */
+int dpx_calc_man_sym_jacob_sphr(int64_t voxels, int thDivs, int phDivs, int numCopies, double stepSize,
+                                const double* inModel, double* outData, const double* ds, const double* locX,
+                                const double* locY, const double* locZ, const double* locA, const double* locB,
+                                const double* locC, double scale, int precision, int* pStop);
+/* GPUCalcSpcFillSymJacobSphrDD (GPUHeader.h:214, SymmetryGenJacob.cu:33-140):
+ * vectorMatrix [9] = the three unit-cell vectors a, b, c (nm), repeats [3],
+ * innerRots [3] (radians), innerTrans [3] (nm); outData is accumulated with
+ * the kernel's lattice sum  sum_{n<N} e^{-i n q.a}  per vector. */
+int dpx_calc_spc_fill_sym_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSize, const double* inModel,
+                                     double* outData, const double* ds, const double* vectorMatrix,
+                                     const double* repeats, const double* innerRots, const double* innerTrans,
+                                     double scale, int precision, int* pStop);
+/* GPUSumGridsJacobSphrDD (GPUHeader.h:255, SumGridsJacobian.cu:44-256):
+ * outAmpData [2 voxels] = sum over numGrids placed grids (trans [3 n] nm,
+ * rots [3 n] radians); the output is overwritten, as in the reference. */
+int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* const* inAmpData,
+                             const double* const* inD, const double* trans, const double* rots, int numGrids,
+                             double* outAmpData, int precision, int* pStop);
 
 /* ---- allocation-free orientation average ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc /

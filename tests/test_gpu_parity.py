@@ -339,3 +339,168 @@ def test_vegas_rejects_bad_point_counts(ctx):
     dom = M.DomainModel([amp], 10, 3.0, M.FP32)
     with pytest.raises(dpx.DpxError):
         dom.CalculateIntensityVector(ctx, np.linspace(0, 3, 5), 0.0, 5000, method="VEGAS", points_per_iter=1000)
+
+
+def test_batched_fill_equals_single_fills(ctx):
+    """dpx_grid_fill_pdb_batch: one persistent FP32 launch over several leaves
+    gives bit-identical cells to one call per leaf; FP64 leaves in the same
+    batch match the oracle."""
+    gs, qmax = 30, 5.0
+    leaves = [globule(900, 2.0, seed=41, extra=VACUUM), globule(150, 1.0, seed=42, extra=SOLVENT),
+              globule(2500, 2.6, seed=43, extra=SOLVENT), globule(300, 1.2, seed=44, extra=VACUUM)]
+    precs = [M.FP32, M.FP32, M.FP32, M.FP64]
+    singles = []
+    for amp, p in zip(leaves, precs):
+        g = M.Grid(ctx, gs, qmax, p)
+        a = amp.atoms_float4()
+        _lib.check(dpx.lib().dpx_grid_fill_pdb(g.handle, len(a), a.ctypes.data_as(C.c_void_p), 0, len(amp.unique),
+                                               _lib.iptr(amp.atoms_per_ion), _lib.dptr(amp.coeffs),
+                                               _lib.dptr(amp.ion_rads), amp.flags, amp.solventED, amp.c1,
+                                               amp.scale, None))
+        singles.append(g.read(True, False)[0])
+    grids = [M.Grid(ctx, gs, qmax, p) for p in precs]
+    descs = (_lib.PdbDesc * len(leaves))()
+    keep = []
+    for d, amp in zip(descs, leaves):
+        a = amp.atoms_float4()
+        keep.append(a)
+        d.n_atoms, d.atoms, d.atoms_on_device, d.n_ions = len(a), a.ctypes.data, 0, len(amp.unique)
+        d.atoms_per_ion, d.coeffs, d.ion_rads = _lib.iptr(amp.atoms_per_ion), _lib.dptr(amp.coeffs), \
+            _lib.dptr(amp.ion_rads)
+        d.flags, d.solvent_ed, d.c1, d.scale, d.center = amp.flags, amp.solventED, amp.c1, amp.scale, None
+    handles = (C.c_void_p * len(grids))(*[g.handle.value for g in grids])
+    _lib.check(dpx.lib().dpx_grid_fill_pdb_batch(len(grids), handles, descs))
+    for g, ref in zip(grids, singles):
+        assert np.array_equal(g.read(True, False)[0], ref)
+    ref64 = O.grid_fill(O.Struct.from_pdb(leaves[3]), gs, qmax, O.FP64)
+    assert rel_to_max(singles[3], ref64) <= TOL64
+    # the same grid twice in one batch is refused
+    dup = (C.c_void_p * 2)(grids[0].handle.value, grids[0].handle.value)
+    assert dpx.lib().dpx_grid_fill_pdb_batch(2, dup, descs) == -1
+
+
+def test_domain_model_batches_leaf_fills(ctx):
+    """DomainModel fills all missing leaf grids in one batch; I(q) equals the
+    one-leaf-at-a-time result exactly."""
+    gs, qmax = 24, 4.0
+    Q = np.linspace(0.1, 3.9, 40)
+    dirs = M.mc_directions(5, 300)
+    def mk():
+        a, b = globule(400, 1.4, seed=51, extra=VACUUM), globule(250, 1.1, seed=52, extra=SOLVENT)
+        a.location, b.location = (0.5, 0, 0, 0.2, 0, 0), (-0.5, 0.3, 0, 0, 0.4, 0.1)
+        return [a, b]
+    a1 = mk()
+    for a in a1:  # one fill per leaf
+        a.calculateGrid(ctx, qmax, gs, M.FP32)
+    I1 = M.DomainModel(a1, gs, qmax, M.FP32).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    a2 = mk()
+    I2 = M.DomainModel(a2, gs, qmax, M.FP32).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    assert np.array_equal(I1, I2)
+
+
+def _cell_qvectors(gs, qmax):
+    """q vectors of every cell in grid-index order (Grid.cpp:169-200 layout)."""
+    Lp, step = gs // 2 + 3, qmax / (gs // 2)
+    out = [np.zeros((1, 3))]
+    for i in range(1, Lp + 1):
+        t, p = np.meshgrid(np.arange(3 * i + 1), np.arange(6 * i), indexing="ij")
+        th, ph = np.pi * t / (3 * i), np.pi * p / (3 * i)
+        q = i * step
+        out.append(np.stack([q * np.sin(th) * np.cos(ph), q * np.sin(th) * np.sin(ph), q * np.cos(th)],
+                            -1).reshape(-1, 3))
+    return np.concatenate(out)
+
+
+def test_dropin_manual_symmetry_grid(ctx):
+    """dpx_calc_man_sym_jacob_sphr: host buffers, loc arrays with the inner
+    placement at entry 0, outData accumulated."""
+    amp = globule(150, 0.9, seed=61)
+    gs, qmax = 20, 3.0
+    data, co = oracle_grid(amp, gs, qmax)
+    P = len(data) // 2
+    rng = np.random.default_rng(3)
+    loc = rng.uniform(-1.5, 1.5, (6, 4))  # x, y, z, a, b, c; 1 inner + 3 copies
+    loc[3:] = rng.uniform(0, 2 * np.pi, (3, 4))
+    loc[3:, 3] = loc[3:, 2]  # two copies share a rotation
+    out = rng.normal(size=2 * P)
+    out0 = out.copy()
+    rc = dpx.lib().dpx_calc_man_sym_jacob_sphr(P, 3, 6, 3, qmax / (gs // 2), _lib.dptr(data), _lib.dptr(out),
+                                               _lib.dptr(co), *[_lib.dptr(np.ascontiguousarray(r)) for r in loc],
+                                               0.8, M.FP64, None)
+    _lib.check(rc)
+    keep = []
+    leaf = O.make_leaf(data, co, rot=loc[3:, 0], tr=loc[:3, 0], copy_rot=loc[3:, 1:].T.copy(),
+                       copy_tr=loc[:3, 1:].T.copy(), sym_scale=0.8, keep=keep)
+    ref = O.assemble_grid(gs, qmax, [leaf])
+    assert np.max(np.abs(out - out0 - ref)) <= TOL64 * np.max(np.abs(ref))
+
+
+def test_dropin_space_filling_grid(ctx):
+    """dpx_calc_spc_fill_sym_jacob_sphr reproduces SymmetryGenJacob.cu's lattice
+    sum sin(N x/2)/sin(x/2) e^{-i (N-1) x/2} (restated here in numpy)."""
+    amp = globule(120, 0.8, seed=62)
+    gs, qmax = 18, 3.0
+    data, co = oracle_grid(amp, gs, qmax)
+    P = len(data) // 2
+    vm = np.array([3.0, 0.0, 0.0, 0.4, 3.5, 0.0, 0.2, -0.3, 4.0])
+    reps = np.array([3.0, 2.0, 4.0])
+    irot, itr = np.array([0.3, -0.2, 0.5]), np.array([0.4, 0.1, -0.2])
+    out = np.random.default_rng(4).normal(size=2 * P)
+    out0 = out.copy()
+    _lib.check(dpx.lib().dpx_calc_spc_fill_sym_jacob_sphr(P, 3, 6, qmax / (gs // 2), _lib.dptr(data),
+                                                          _lib.dptr(out), _lib.dptr(co), _lib.dptr(vm),
+                                                          _lib.dptr(reps), _lib.dptr(irot), _lib.dptr(itr), 0.6,
+                                                          M.FP64, None))
+    child = O.assemble_grid(gs, qmax, [O.make_leaf(data, co, rot=irot, tr=itr)])
+    A = child[0::2] + 1j * child[1::2]
+    qv = _cell_qvectors(gs, qmax)
+    for k in range(3):
+        x, N = qv @ vm[3 * k:3 * k + 3], reps[k]
+        small = np.abs(x) < 100 * np.finfo(float).eps
+        xs = np.where(small, 1.0, x)
+        S = np.sin(N * xs / 2) / np.sin(xs / 2) * np.exp(-0.5j * (N - 1) * xs)
+        A = A * np.where(small | (N == 1), N, S)
+    got = (out - out0)[0::2] + 1j * (out - out0)[1::2]
+    assert np.max(np.abs(got - 0.6 * A)) <= 1e-9 * np.max(np.abs(A))
+
+
+def test_dropin_sum_grids(ctx):
+    """dpx_sum_grids_jacob_sphr overwrites its output with the sum of the placed grids."""
+    gs, qmax = 18, 3.0
+    a, b = globule(100, 0.8, seed=63), globule(140, 0.9, seed=64)
+    (da, ca), (db, cb) = oracle_grid(a, gs, qmax), oracle_grid(b, gs, qmax)
+    P = len(da) // 2
+    trans = np.array([0.5, 0.0, 0.2, -0.4, 0.3, 0.0])
+    rots = np.array([0.1, 0.2, 0.3, 1.0, -0.5, 2.0])
+    out = np.full(2 * P, 7.0)
+    amps = (_lib._D * 2)(_lib.dptr(da), _lib.dptr(db))
+    ders = (_lib._D * 2)(_lib.dptr(ca), _lib.dptr(cb))
+    _lib.check(dpx.lib().dpx_sum_grids_jacob_sphr(P, 3, 6, qmax / (gs // 2), amps, ders, _lib.dptr(trans),
+                                                  _lib.dptr(rots), 2, _lib.dptr(out), M.FP64, None))
+    keep = []
+    ref = O.assemble_grid(gs, qmax, [O.make_leaf(da, ca, rot=rots[:3], tr=trans[:3], keep=keep),
+                                     O.make_leaf(db, cb, rot=rots[3:], tr=trans[3:], keep=keep)])
+    assert np.max(np.abs(out - ref)) <= TOL64 * np.max(np.abs(ref))
+
+
+def test_fill_schedules_and_autotuner(ctx):
+    """Flat and persistent FP32 fills give identical cells for every shape; the
+    autotuner keeps one of the swept shapes and its grids match a fill with it."""
+    gs, qmax = 26, 4.0
+    leaves = [globule(700, 1.8, seed=71, extra=SOLVENT), globule(90, 0.7, seed=72, extra=VACUUM)]
+    for cpt, th in [(2, 256), (4, 128), (8, 128), (8, 256)]:
+        ctx.set_fill_shape(cpt, th)
+        got = []
+        for persistent in (False, True):
+            ctx.set_fill_schedule(persistent)
+            for a in leaves:
+                a._grid = None
+            got.append([g.read(True, False)[0] for g in M.calculate_grids(ctx, leaves, qmax, gs, M.FP32)])
+        for x, y in zip(*got):
+            assert np.array_equal(x, y)
+    best, table = M.autotune_fill(ctx, leaves, qmax, gs, repeats=1)
+    assert best in table and len(table) == dpx.lib().dpx_fill_shapes(None)
+    assert ctx.fill_shape() == best
+    assert all(t > 0 for t in table.values())
+    ctx.set_fill_shape(8, 128)
+    ctx.set_fill_schedule(False)
