@@ -299,6 +299,144 @@ def run_dpx(args):
     return out
 
 
+BATCH_NQ, BATCH_DIRS = 200, 100_000
+
+
+def run_batch(args):
+    """Independent solves of uneven size in one batch (dpx_batch: one CUDA graph
+    per wave, one FP32 fill launch per wave); FP32-bulk for the whole mix, the
+    plain FP64 path on a seeded subsample of it for the speed ratio and the
+    error."""
+    import torch
+    from dpx import models as M
+    from dpx import workloads as W
+
+    rank, world, lrank = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(lrank)
+    ctx = M.Context(lrank)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    mix = W.batch_mix(args.batch_size)
+    # every rank solves its own copy of the mix (replicas: no exchange on this path)
+    t0 = time.perf_counter()
+    leaves = [s.leaf() for s in mix]
+    gen_s = time.perf_counter() - t0
+    Qs = [np.linspace(0.0, s.qmax, BATCH_NQ) for s in mix]
+    dirs = M.mc_directions(DIR_SEED, BATCH_DIRS)
+    gss = [s.grid_size for s in mix]
+    qms = [s.qmax for s in mix]
+    tune = None
+    if args.autotune:  # on a seeded sample of four mid-sized structures of the mix
+        rng = np.random.default_rng(7)
+        mids = sorted(range(len(mix)), key=lambda j: mix[j].pairs())[len(mix) // 4: 3 * len(mix) // 4]
+        pick = [mids[k] for k in rng.choice(len(mids), size=min(4, len(mids)), replace=False)]
+        # the sample shares one grid: the largest of the four
+        j0 = max(pick, key=lambda j: mix[j].layers)
+        best, table = M.autotune_fill(ctx, [leaves[j] for j in pick], mix[j0].qmax, mix[j0].grid_size, repeats=1)
+        tune = {"best": "%dx%d%s" % (best[0], best[1], "p" if best[2] else ""), "sample": pick,
+                "fill_ms": {"%dx%d%s" % (k[0], k[1], "p" if k[2] else ""): round(v, 3) for k, v in table.items()}}
+
+    def build(idx, prec):
+        return M.SolveBatch(ctx, [leaves[j] for j in idx], [gss[j] for j in idx], [qms[j] for j in idx],
+                            [Qs[j] for j in idx], dirs, precision=prec)
+
+    allidx = list(range(len(mix)))
+    b = build(allidx, M.FP32)
+    waves, launches, pool = b.info()
+    for _ in range(args.warmup):
+        b.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(lrank) as clk:
+        barrier_sync(world)
+        e0.record(stream)
+        for _ in range(args.steps):
+            b.launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dev_ms = e0.elapsed_time(e1)
+    dev_ms = max_over_ranks(dev_ms, world)
+    I32 = b.results()
+    b.close()
+    # end to end: build from host leaves (upload, graph recording), run, read back
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        b = build(allidx, M.FP32)
+        b.run()
+        _ = b.results()
+        b.close()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    n_tot = len(mix) * world
+    value = n_tot * args.steps / (dev_ms / 1e3)
+    pairs = float(sum(s.pairs() for s in mix))
+    out = {
+        "metric": "I(q) solves/s (FP32-bulk, uneven batch of independent structures)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded globules)",
+        "config": {"workload": "batch of %d independent structures: atoms log-uniform [500, 200000], qmax U[2,10], "
+                               "layers U[40,250], half with dummy-atom solvent; %d q in [0, qmax], MC %d shared "
+                               "directions" % (len(mix), BATCH_NQ, BATCH_DIRS),
+                   "structures": len(mix), "atom_cell_pairs": pairs, "waves": waves, "grid_pool_bytes": pool,
+                   "l2": "every grid >= 8 MB and the wave's grids together >> 129 MB L2"},
+        "e2e": {"value": n_tot / e2e_s, "unit": "solves/s",
+                "h2d_bytes_per_step": int(sum(16 * s.atoms for s in mix) + dirs.nbytes + sum(q.nbytes for q in Qs)),
+                "d2h_bytes_per_step": int(sum(q.nbytes for q in Qs))},
+        "gpu_launches": int(launches) * args.steps,
+        "roofline": {"bound": "sfu", "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] else "flat"),
+                     "algorithmic_pairs_per_s": pairs * args.steps / (dev_ms / 1e3),
+                     "note": "whole-batch time (fill + splines + average); per-kernel split in the subunit line"},
+        "generation_s": gen_s,
+    }
+    if tune:
+        out["autotune"] = tune
+    out["clocks"] = clk.summary()
+    if args.fp64_sample > 0 and rank == 0:
+        rng = np.random.default_rng(11)
+        sub = sorted(rng.choice(len(mix), size=min(args.fp64_sample, len(mix)), replace=False).tolist())
+        b32, b64 = build(sub, M.FP32), build(sub, M.FP64)
+        b32.run()
+        b64.run()
+        torch.cuda.synchronize()
+        t = {}
+        for name, bb in (("fp32", b32), ("fp64", b64)):
+            e0.record(stream)
+            bb.launch()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t[name] = e0.elapsed_time(e1)
+        r32, r64 = b32.results(), b64.results()
+        err = max(float(np.max(np.abs(x - y) / np.abs(y))) for x, y in zip(r32, r64))
+        out["fp64_plain"] = {"sample": sub, "atom_cell_pairs": float(sum(mix[j].pairs() for j in sub)),
+                             "fp32_ms": t["fp32"], "fp64_ms": t["fp64"], "speedup_fp32_vs_fp64": t["fp64"] / t["fp32"],
+                             "fp64_solves_per_s": len(sub) / (t["fp64"] / 1e3),
+                             "max_rel_err_fp32_vs_fp64": err}
+        b32.close()
+        b64.close()
+    ctx.close()
+    return out if rank == 0 else None
+
+
+def barrier_sync(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ms, world):
+    if world == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def fp64_error(ctx, amp, Q, dirs, I32):
     """FP32-bulk I(q) against the plain FP64 GPU path on the same inputs."""
     from dpx import models as M
@@ -375,6 +513,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--check-error", action="store_true")
     ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
+    ap.add_argument("--workload", default="subunit", choices=["subunit", "batch"])
+    ap.add_argument("--batch-size", type=int, default=512)
+    ap.add_argument("--fp64-sample", type=int, default=0, help="batch: FP64 comparison on this many structures")
+    ap.add_argument("--e2e-steps", type=int, default=1)
     args = ap.parse_args()
     if args.profile_shape:
         apply_profile_shape(args.profile_shape)
@@ -384,7 +526,7 @@ def main():
     else:
         from dpx import _build
         _build.build_libdpx()
-        out = run_dpx(args)
+        out = run_batch(args) if args.workload == "batch" else run_dpx(args)
     if out is not None:
         print(json.dumps(out))
 

@@ -1,0 +1,414 @@
+// dpx_batch.cpp — many independent I(q) solves (one PDB leaf each, its own
+// grid size, qmax and q list) prepared once and replayed as CUDA graphs.
+//
+// A solve is the reference's per-structure sequence PDBAmplitude::calculateGrid
+// (PDBAmplitude.cpp:319-435) -> CalculateSplines (Grid.cpp:1113-1151) ->
+// DomainModel::CalculateIntensityVector's MC between layers (Amplitude.cpp:
+// 1168-1247, 2746-2822), which the reference runs one structure at a time.
+// Here the solves are packed into waves whose grids fit a device-memory
+// budget.  Each wave is one CUDA graph:
+//   one FP32 fill launch over every structure of the wave (FP64: one per structure),
+//   per structure: splines, MC average, finalize, the q = 0 term,
+//   one device-to-host copy of the wave's I(q) into pinned memory.
+// All inputs (atoms, form-factor tables, item prefixes, bracket tables and the
+// shared direction set) are uploaded once at creation; the grids of a wave
+// live in one pool reused by every wave.
+#include "dpx_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+using dpx::Geom;
+using namespace dpxh;
+
+struct dpx_batch_s {
+    dpx_ctx ctx = nullptr;
+    int precision = DPX_FP32;
+    int n = 0;
+    double eps = 0.0;
+    std::vector<int> nq;
+    std::vector<size_t> res_off;  // into the result arrays (doubles)
+    size_t res_total = 0;
+    std::vector<int> wave_first;  // solves [wave_first[w], wave_first[w+1])
+    size_t pool_bytes = 0;
+    int64_t launches = 0;  // kernels per run
+    void* arena = nullptr;
+    void* pool = nullptr;
+    double* partial = nullptr;
+    double* d_res = nullptr;
+    double* h_res = nullptr;  // pinned
+    std::vector<cudaGraph_t> graphs;
+    std::vector<cudaGraphExec_t> execs;
+};
+
+namespace {
+
+void batch_free(dpx_batch b) {
+    if (!b) return;
+    set_device(b->ctx);
+    cudaStreamSynchronize(b->ctx->stream);
+    for (cudaGraphExec_t e : b->execs) cudaGraphExecDestroy(e);
+    for (cudaGraph_t g : b->graphs) cudaGraphDestroy(g);
+    if (b->arena) cudaFree(b->arena);
+    if (b->pool) cudaFree(b->pool);
+    if (b->partial) cudaFree(b->partial);
+    if (b->d_res) cudaFree(b->d_res);
+    if (b->h_res) cudaFreeHost(b->h_res);
+    ctx_release(b->ctx);
+    delete b;
+}
+
+// Host staging of one byte arena: returns the offset of the copied block.
+struct Stage {
+    std::vector<char> h;
+    size_t put(const void* src, size_t n) {
+        const size_t at = al16(h.size());
+        h.resize(at + n);
+        if (n) std::memcpy(h.data() + at, src, n);
+        return at;
+    }
+};
+
+struct SolvePlan {
+    Geom G;
+    int grid_size;
+    double qmax;
+    size_t grid_off;  // in the pool
+    size_t o_atoms, o_off, o_aff, o_pref, o_model, o_bq, o_bl, o_bo, o_bi;
+    int64_t n_items;
+    double cen[3];
+    bool origin;  // Q[0] == 0
+    int U;
+    float scale32;
+    double scale;
+    dpx::AvgPlan plan;  // pointers filled once the arena exists
+};
+
+}  // namespace
+
+extern "C" {
+
+int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int precision, const double* dirs,
+                     int64_t n_samples, double eps, int64_t grid_budget_bytes, dpx_batch* out) {
+    if (!ctx || n <= 0 || !solves || !dirs || !out) return fail(DPX_ERR_ARG, "NULL or empty argument");
+    if (precision != DPX_FP32 && precision != DPX_FP64) return fail(DPX_ERR_ARG, "bad precision");
+    if (n_samples <= 0) return fail(DPX_ERR_ARG, "n_samples must be positive");
+    *out = nullptr;
+    for (int j = 0; j < n; ++j) {
+        const dpx_solve_desc& d = solves[j];
+        if (int rc = check_pdb(d.pdb)) return rc;
+        if (d.grid_size < 2 || (d.grid_size & 1)) return fail(DPX_ERR_ARG, "solve %d: grid_size must be even", j);
+        if (!(d.qmax > 0)) return fail(DPX_ERR_ARG, "solve %d: qmax must be positive", j);
+        if (d.nq <= 0 || !d.Q) return fail(DPX_ERR_ARG, "solve %d: no q values", j);
+        for (int k = 1; k < d.nq; ++k)
+            if (!(d.Q[k] >= d.Q[k - 1])) return fail(DPX_ERR_ARG, "solve %d: Q must be ascending", j);
+        if (d.Q[0] < 0) return fail(DPX_ERR_ARG, "solve %d: negative q", j);
+        if (d.Q[d.nq - 1] > d.qmax * (1.0 + 1e-12)) return fail(DPX_ERR_ARG, "solve %d: q beyond qmax", j);
+    }
+    if (int rc = set_device(ctx)) return rc;
+    const bool fp32 = precision == DPX_FP32;
+    const int cpt = fp32 ? ctx->fill_cpt : dpx::kFill64Cells, threads = ctx->fill_threads;
+    const bool persistent = ctx->fill_persistent;
+    if (grid_budget_bytes <= 0) {
+        size_t fr = 0, tot = 0;
+        DPX_CUDA(cudaMemGetInfo(&fr, &tot));
+        grid_budget_bytes = (int64_t)(fr / 2);
+    }
+
+    auto* b = new dpx_batch_s;
+    b->ctx = ctx;
+    ctx_retain(ctx);
+    b->precision = precision;
+    b->n = n;
+    b->eps = eps;
+
+    // waves: solves in order, grid bytes of a wave within the budget
+    std::vector<SolvePlan> sp(n);
+    b->wave_first.push_back(0);
+    size_t wave_bytes = 0;
+    for (int j = 0; j < n; ++j) {
+        SolvePlan& p = sp[j];
+        p.grid_size = solves[j].grid_size;
+        p.qmax = solves[j].qmax;
+        p.G = dpx::make_geom(p.grid_size, p.qmax);
+        const size_t gb = al16((size_t)p.G.P * cell_bytes(precision));
+        if (wave_bytes > 0 && (int64_t)(wave_bytes + gb) > grid_budget_bytes) {
+            b->pool_bytes = std::max(b->pool_bytes, wave_bytes);
+            b->wave_first.push_back(j);
+            wave_bytes = 0;
+        }
+        p.grid_off = wave_bytes;
+        wave_bytes += gb;
+    }
+    b->pool_bytes = std::max(b->pool_bytes, wave_bytes);
+    b->wave_first.push_back(n);
+    const int n_waves = (int)b->wave_first.size() - 1;
+
+    // staging of every input table
+    Stage st;
+    size_t partial_max = 0;
+    std::vector<double> aff;
+    std::vector<float> affF;
+    std::vector<float4> atoms;
+    for (int j = 0; j < n; ++j) {
+        const dpx_solve_desc& d = solves[j];
+        const dpx_pdb_desc& pd = d.pdb;
+        SolvePlan& p = sp[j];
+        const Geom& G = p.G;
+        // centring: FP32 grids shift host atoms by their centroid (restored as a
+        // per-cell phase), FP64 grids take them as they are
+        for (int k = 0; k < 3; ++k) p.cen[k] = 0.0;
+        if (pd.center) {
+            for (int k = 0; k < 3; ++k) p.cen[k] = pd.center[k];
+        } else if (!pd.atoms_on_device && fp32) {
+            double acc[3] = {0, 0, 0};
+            for (int64_t a = 0; a < pd.n_atoms; ++a)
+                for (int k = 0; k < 3; ++k) acc[k] += pd.atoms[4 * a + k];
+            for (int k = 0; k < 3; ++k) p.cen[k] = acc[k] / double(pd.n_atoms);
+        }
+        if (!fp32 && !pd.atoms_on_device) p.cen[0] = p.cen[1] = p.cen[2] = 0.0;
+        if (pd.atoms_on_device) {
+            p.o_atoms = SIZE_MAX;
+        } else {
+            atoms.resize(pd.n_atoms);
+            for (int64_t a = 0; a < pd.n_atoms; ++a)
+                atoms[a] = make_float4((float)((double)pd.atoms[4 * a] - p.cen[0]),
+                                       (float)((double)pd.atoms[4 * a + 1] - p.cen[1]),
+                                       (float)((double)pd.atoms[4 * a + 2] - p.cen[2]), 0.f);
+            p.o_atoms = st.put(atoms.data(), atoms.size() * sizeof(float4));
+        }
+        std::vector<int> off(pd.n_ions + 1, 0);
+        for (int u = 0; u < pd.n_ions; ++u) off[u + 1] = off[u] + pd.atoms_per_ion[u];
+        p.o_off = st.put(off.data(), off.size() * sizeof(int));
+        aff_table(pd.n_ions, pd.atoms_per_ion, pd.coeffs, pd.ion_rads, pd.flags, pd.solvent_ed, pd.c1, G.Lp, G.step,
+                  aff);
+        if (fp32) {
+            affF.assign(aff.begin(), aff.end());
+            p.o_aff = st.put(affF.data(), affF.size() * sizeof(float));
+        } else {
+            p.o_aff = st.put(aff.data(), aff.size() * sizeof(double));
+        }
+        std::vector<int64_t> pref(G.Lp + 1);
+        p.n_items = dpx::fill_items(G, cpt, pref.data());
+        p.o_pref = st.put(pref.data(), pref.size() * sizeof(int64_t));
+        p.U = pd.n_ions;
+        p.scale = pd.scale;
+        p.scale32 = (float)pd.scale;
+        // brackets and the plain identity model
+        Brackets B;
+        make_brackets(G, p.grid_size, p.qmax, d.nq, d.Q, B);
+        p.o_bq = st.put(B.q.data(), B.q.size() * sizeof(double));
+        p.o_bl = st.put(B.layer.data(), B.layer.size() * sizeof(int));
+        p.o_bo = st.put(B.off.data(), B.off.size() * sizeof(int));
+        p.o_bi = st.put(B.qidx.data(), B.qidx.size() * sizeof(int));
+        dpx::ModelDev M{};
+        M.R[0] = M.R[4] = M.R[8] = 1.0;
+        M.sym_scale = 1.0;
+        M.plain = 1;
+        p.o_model = st.put(&M, sizeof M);  // grid pointer patched below
+        dpx::AvgPlan& P = p.plan;
+        P = dpx::AvgPlan{};
+        P.n_brackets = (int)B.layer.size();
+        P.max_q = B.max_q;
+        P.n_samples = n_samples;
+        P.chunk = eps > 0.0 ? 100 : 128;
+        P.chunk_off = eps > 0.0 ? 99 : 0;
+        P.n_chunks = (n_samples + P.chunk_off + P.chunk - 1) / P.chunk;
+        P.dir_stride = 0;
+        P.need_dir = 0;
+        partial_max = std::max(partial_max, ((size_t)P.n_brackets * P.n_chunks + (size_t)P.n_brackets * 5) *
+                                                P.max_q * sizeof(double) + 64);
+        p.origin = d.Q[0] == 0.0;
+        b->nq.push_back(d.nq);
+        b->res_off.push_back(b->res_total);
+        b->res_total += (size_t)d.nq;
+    }
+    const size_t o_dirs = st.put(dirs, (size_t)n_samples * 2 * sizeof(double));
+    // per-wave FP32 job tables and tile counters
+    std::vector<size_t> o_jobs(n_waves, 0), o_counter(n_waves, 0);
+    std::vector<int64_t> wave_tiles(n_waves, 0);
+    const size_t jobs_base = al16(st.h.size());
+    {
+        size_t o = jobs_base;
+        for (int w = 0; w < n_waves; ++w) {
+            o_jobs[w] = o;
+            o = al16(o + (size_t)(b->wave_first[w + 1] - b->wave_first[w]) * sizeof(dpx::FillJob));
+            o_counter[w] = o;
+            o = al16(o + 64);
+        }
+        st.h.resize(o, 0);
+    }
+
+    // device allocations
+    int rc = DPX_OK;
+    cudaError_t e = cudaMalloc(&b->arena, st.h.size());
+    if (e == cudaSuccess) e = cudaMalloc(&b->pool, b->pool_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->partial, partial_max);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_res, b->res_total * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_res, b->res_total * sizeof(double));
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "batch allocation");
+        batch_free(b);
+        return rc;
+    }
+    char* A = static_cast<char*>(b->arena);
+    char* pool = static_cast<char*>(b->pool);
+
+    // patch device pointers into the staged models and job tables
+    for (int w = 0; w < n_waves; ++w) {
+        int64_t tiles = 0;
+        std::vector<dpx::FillJob> jobs;
+        for (int j = b->wave_first[w]; j < b->wave_first[w + 1]; ++j) {
+            SolvePlan& p = sp[j];
+            dpx::ModelDev* M = reinterpret_cast<dpx::ModelDev*>(st.h.data() + p.o_model);
+            M->grid = pool + p.grid_off;
+            if (fp32) {
+                dpx::FillJob J{};
+                J.atoms = p.o_atoms == SIZE_MAX ? reinterpret_cast<const float4*>(solves[j].pdb.atoms)
+                                                : reinterpret_cast<const float4*>(A + p.o_atoms);
+                J.ion_off = reinterpret_cast<const int*>(A + p.o_off);
+                J.aff_f32 = reinterpret_cast<const float*>(A + p.o_aff);
+                J.pref = reinterpret_cast<const int64_t*>(A + p.o_pref);
+                J.grid = reinterpret_cast<float4*>(pool + p.grid_off);
+                J.n_items = p.n_items;
+                J.tile_start = tiles;
+                J.step = p.G.step;
+                J.cx = p.cen[0];
+                J.cy = p.cen[1];
+                J.cz = p.cen[2];
+                J.use_center = (p.cen[0] != 0.0 || p.cen[1] != 0.0 || p.cen[2] != 0.0);
+                J.U = p.U;
+                J.Lp = p.G.Lp;
+                J.scale = p.scale32;
+                jobs.push_back(J);
+                tiles += (p.n_items + threads - 1) / threads;
+            }
+            dpx::AvgPlan& P = p.plan;
+            P.br_q = reinterpret_cast<const double*>(A + p.o_bq);
+            P.br_layer = reinterpret_cast<const int*>(A + p.o_bl);
+            P.br_q_off = reinterpret_cast<const int*>(A + p.o_bo);
+            P.br_qidx = reinterpret_cast<const int*>(A + p.o_bi);
+            P.dirs = reinterpret_cast<const double*>(A + o_dirs);
+            P.partial = b->partial;
+        }
+        if (!jobs.empty()) std::memcpy(st.h.data() + o_jobs[w], jobs.data(), jobs.size() * sizeof(dpx::FillJob));
+        wave_tiles[w] = tiles;
+    }
+    cudaStream_t s = ctx->stream;
+    e = cudaMemcpyAsync(b->arena, st.h.data(), st.h.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "batch upload");
+        batch_free(b);
+        return rc;
+    }
+
+    // record one graph per wave
+    for (int w = 0; w < n_waves && !rc; ++w) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "cudaStreamBeginCapture");
+            break;
+        }
+        int64_t launches = 0;
+        const int j0 = b->wave_first[w], j1 = b->wave_first[w + 1];
+        if (fp32) {
+            e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(A + o_jobs[w]), j1 - j0,
+                                           wave_tiles[w], reinterpret_cast<unsigned long long*>(A + o_counter[w]),
+                                           cpt, threads, persistent);
+            launches++;
+        } else {
+            for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
+                const SolvePlan& p = sp[j];
+                const float4* at = p.o_atoms == SIZE_MAX ? reinterpret_cast<const float4*>(solves[j].pdb.atoms)
+                                                         : reinterpret_cast<const float4*>(A + p.o_atoms);
+                e = dpx::launch_fill_f64(s, at, reinterpret_cast<const int*>(A + p.o_off), p.U,
+                                         reinterpret_cast<const double*>(A + p.o_aff), p.G,
+                                         reinterpret_cast<const int64_t*>(A + p.o_pref), p.n_items, p.cen, p.scale,
+                                         reinterpret_cast<double4_32a*>(pool + p.grid_off));
+                launches++;
+            }
+        }
+        for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
+            const SolvePlan& p = sp[j];
+            void* grid = pool + p.grid_off;
+            e = fp32 ? dpx::launch_splines_f32(s, p.G, reinterpret_cast<float4*>(grid))
+                     : dpx::launch_splines_f64(s, p.G, reinterpret_cast<double4_32a*>(grid));
+            double* r = b->d_res + b->res_off[j];
+            if (e == cudaSuccess) e = cudaMemsetAsync(r, 0, (size_t)b->nq[j] * sizeof(double), s);
+            if (e == cudaSuccess)
+                e = dpx::launch_average(s, !fp32, p.G, 1, reinterpret_cast<const dpx::ModelDev*>(A + p.o_model),
+                                        p.plan);
+            if (e == cudaSuccess) e = dpx::launch_finalize(s, p.plan, eps, r);
+            if (e == cudaSuccess && p.origin) {
+                e = dpx::launch_origin_intensity(s, !fp32, grid, r);
+                launches++;
+            }
+            launches += 3;
+        }
+        const size_t r0 = b->res_off[j0], r1 = (j1 < n) ? b->res_off[j1] : b->res_total;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->h_res + r0, b->d_res + r0, (r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost, s);
+        const cudaError_t ec = cudaStreamEndCapture(s, &g);
+        if (e == cudaSuccess) e = ec;
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            rc = cuda_fail(e, "batch graph capture");
+            break;
+        }
+        b->graphs.push_back(g);
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "cudaGraphInstantiate");
+            break;
+        }
+        b->execs.push_back(x);
+        b->launches += launches;
+    }
+    if (rc) {
+        batch_free(b);
+        return rc;
+    }
+    *out = b;
+    return DPX_OK;
+}
+
+int dpx_batch_launch(dpx_batch b) {
+    if (!b) return fail(DPX_ERR_ARG, "batch is NULL");
+    if (int rc = set_device(b->ctx)) return rc;
+    for (cudaGraphExec_t x : b->execs) DPX_CUDA(cudaGraphLaunch(x, b->ctx->stream));
+    return DPX_OK;
+}
+
+int dpx_batch_run(dpx_batch b) {
+    if (int rc = dpx_batch_launch(b)) return rc;
+    DPX_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    return DPX_OK;
+}
+
+int dpx_batch_info(dpx_batch b, int* n_waves, int64_t* kernels_per_run, int64_t* pool_bytes) {
+    if (!b) return fail(DPX_ERR_ARG, "batch is NULL");
+    if (n_waves) *n_waves = (int)b->execs.size();
+    if (kernels_per_run) *kernels_per_run = b->launches;
+    if (pool_bytes) *pool_bytes = (int64_t)b->pool_bytes;
+    return DPX_OK;
+}
+
+int dpx_batch_result(dpx_batch b, int j, double* res) {
+    if (!b || !res) return fail(DPX_ERR_ARG, "NULL argument");
+    if (j < 0 || j >= b->n) return fail(DPX_ERR_ARG, "solve %d out of range", j);
+    std::memcpy(res, b->h_res + b->res_off[j], (size_t)b->nq[j] * sizeof(double));
+    return DPX_OK;
+}
+
+int dpx_batch_destroy(dpx_batch b) {
+    if (!b) return fail(DPX_ERR_ARG, "batch is NULL");
+    batch_free(b);
+    return DPX_OK;
+}
+
+}  // extern "C"

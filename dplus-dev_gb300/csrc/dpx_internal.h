@@ -121,6 +121,8 @@ cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid)
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
                            const AvgPlan& plan);
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
+// d_res[0] = |origin cell|^2 (I at q = 0 of one plain leaf)
+cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res);
 cudaError_t launch_pack_values_f32(cudaStream_t s, const float4* grid, int64_t P, double* out);
 cudaError_t launch_pack_values_f64(cudaStream_t s, const double4_32a* grid, int64_t P, double* out);
 cudaError_t launch_unpack_f64(cudaStream_t s, const double* vals, const double* ders, int64_t P, double4_32a* grid);

@@ -908,6 +908,28 @@ cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_model
     return cudaGetLastError();
 }
 
+namespace {
+// I(0) = |A(0)|^2 of one plain leaf (Amplitude.cpp:1176-1182): the origin cell.
+__global__ void origin_intensity_kernel(const void* grid, int fp64, double* res) {
+    double re, im;
+    if (fp64) {
+        const double* g = static_cast<const double*>(grid);
+        re = g[0];
+        im = g[1];
+    } else {
+        const float* g = static_cast<const float*>(grid);
+        re = g[0];
+        im = g[1];
+    }
+    res[0] = re * re + im * im;
+}
+}  // namespace
+
+cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res) {
+    origin_intensity_kernel<<<1, 1, 0, s>>>(grid, fp64 ? 1 : 0, d_res);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res) {
     finalize_kernel<<<blocks_for(plan.n_brackets, 64), 64, 0, s>>>(plan, eps, d_res);
     return cudaGetLastError();

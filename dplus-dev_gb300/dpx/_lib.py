@@ -41,6 +41,11 @@ class PdbDesc(C.Structure):
                 ("atoms_per_ion", _I), ("coeffs", _D), ("ion_rads", _D), ("flags", C.c_int),
                 ("solvent_ed", C.c_double), ("c1", C.c_double), ("scale", C.c_double), ("center", _D)]
 
+class SolveDesc(C.Structure):
+    """dpx_solve_desc: one solve of a dpx_batch."""
+    _fields_ = [("pdb", PdbDesc), ("grid_size", C.c_int), ("qmax", C.c_double), ("nq", C.c_int), ("Q", _D)]
+
+
 _SIGS = {
     "dpx_last_error": (C.c_char_p, []),
     "dpx_version": (C.c_int, []),
@@ -88,6 +93,13 @@ _SIGS = {
                                                    _D, C.c_double, C.c_int, _I]),
     "dpx_sum_grids_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, C.POINTER(_D), C.POINTER(_D),
                                            _D, _D, C.c_int, _D, C.c_int, _I]),
+    "dpx_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(SolveDesc), C.c_int, _D, C.c_int64, C.c_double,
+                                   C.c_int64, C.POINTER(_P)]),
+    "dpx_batch_launch": (C.c_int, [_P]),
+    "dpx_batch_run": (C.c_int, [_P]),
+    "dpx_batch_result": (C.c_int, [_P, C.c_int, _D]),
+    "dpx_batch_info": (C.c_int, [_P, _I, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "dpx_batch_destroy": (C.c_int, [_P]),
     "dpx_mc_average_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, _D, _P, C.c_int64, C.c_double,
                                          _P, _P]),
 }

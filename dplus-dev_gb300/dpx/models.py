@@ -258,6 +258,63 @@ def calculate_grids(ctx: Context, leaves: Sequence[PDBAmplitude], qmax: float, g
     return [a._grid for a in leaves]
 
 
+class SolveBatch:
+    """Many independent I(q) solves, one PDB leaf each (dpx_batch): every leaf
+    on its own grid (gridSize, qMax) with its own q list, Monte Carlo over one
+    shared direction set.  Built once (inputs uploaded, CUDA graphs recorded),
+    then ``run()`` replays it."""
+
+    def __init__(self, ctx: Context, leaves: Sequence[PDBAmplitude], grid_sizes: Sequence[int],
+                 qmaxes: Sequence[float], Qs: Sequence[np.ndarray], dirs: np.ndarray, n_samples: int | None = None,
+                 eps: float = 0.0, precision: int = FP32, grid_budget_bytes: int = 0):
+        n = len(leaves)
+        if not (len(grid_sizes) == len(qmaxes) == len(Qs) == n):
+            raise ValueError("leaves, grid_sizes, qmaxes and Qs must have the same length")
+        self.ctx = ctx
+        self._Qs = [np.ascontiguousarray(q, dtype=np.float64) for q in Qs]
+        pdbs, keep = pdb_descs(leaves)
+        descs = (_lib.SolveDesc * n)()
+        for d, pd, gs, qm, q in zip(descs, pdbs, grid_sizes, qmaxes, self._Qs):
+            d.pdb, d.grid_size, d.qmax, d.nq, d.Q = pd, int(gs), float(qm), len(q), dptr(q)
+        dirs = np.ascontiguousarray(dirs, dtype=np.float64)
+        n_samples = len(dirs) if n_samples is None else int(n_samples)
+        h = C.c_void_p()
+        check(lib().dpx_batch_create(ctx.handle, n, descs, int(precision), dptr(dirs), n_samples, float(eps),
+                                     int(grid_budget_bytes), C.byref(h)))
+        self.handle = h
+
+    def run(self) -> None:
+        check(lib().dpx_batch_run(self.handle))
+
+    def launch(self) -> None:
+        check(lib().dpx_batch_launch(self.handle))
+
+    def result(self, j: int) -> np.ndarray:
+        out = np.zeros(len(self._Qs[j]))
+        check(lib().dpx_batch_result(self.handle, int(j), dptr(out)))
+        return out
+
+    def results(self) -> list:
+        return [self.result(j) for j in range(len(self._Qs))]
+
+    def info(self):
+        """(waves, kernel launches per run, grid-pool bytes)."""
+        w, k, b = C.c_int(), C.c_int64(), C.c_int64()
+        check(lib().dpx_batch_info(self.handle, C.byref(w), C.byref(k), C.byref(b)))
+        return w.value, k.value, b.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().dpx_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _pdb_leaves(node, out: list) -> list:
     """Every PDBAmplitude under a model tree node."""
     if isinstance(node, PDBAmplitude):

@@ -249,6 +249,37 @@ int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
                              const double* const* inD, const double* trans, const double* rots, int numGrids,
                              double* outAmpData, int precision, int* pStop);
 
+/* ---- batched independent solves (no counterpart in the reference, which
+ * solves one structure per call) ----
+ * Each solve is one PDB leaf on its own grid (grid_size, qmax) with its own
+ * ascending q list: fill -> splines -> Monte Carlo average over the shared
+ * direction set (n_samples (theta, phi) pairs, host), eps as in
+ * dpx_orientation_average.  dpx_batch_create uploads every input once, packs
+ * the solves in order into waves whose grids fit grid_budget_bytes (<= 0: half
+ * the free device memory) and records one CUDA graph per wave: one FP32 fill
+ * launch over the wave's structures (FP64: one per structure), then splines,
+ * average, finalize and the q = 0 term per structure, then one copy of the
+ * wave's I(q) to pinned host memory.  Host atoms are read only during create;
+ * device atoms (atoms_on_device) must stay valid while the batch lives. */
+typedef struct dpx_solve_desc {
+    dpx_pdb_desc pdb;
+    int grid_size;
+    double qmax;
+    int nq;
+    const double* Q;
+} dpx_solve_desc;
+typedef struct dpx_batch_s* dpx_batch;
+int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int precision, const double* dirs,
+                     int64_t n_samples, double eps, int64_t grid_budget_bytes, dpx_batch* out);
+/* Launch every wave's graph on the context stream (returns at once) / and wait. */
+int dpx_batch_launch(dpx_batch b);
+int dpx_batch_run(dpx_batch b);
+/* I(q) of solve j after a completed run: res [nq of solve j]. */
+int dpx_batch_result(dpx_batch b, int j, double* res);
+/* Waves, kernel launches per run, bytes of the grid pool. */
+int dpx_batch_info(dpx_batch b, int* n_waves, int64_t* kernels_per_run, int64_t* pool_bytes);
+int dpx_batch_destroy(dpx_batch b);
+
 /* ---- allocation-free orientation average ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc /
  * cudaFree: applications whose device memory is pre-reserved by their own pool

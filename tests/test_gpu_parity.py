@@ -504,3 +504,41 @@ def test_fill_schedules_and_autotuner(ctx):
     assert all(t > 0 for t in table.values())
     ctx.set_fill_shape(8, 128)
     ctx.set_fill_schedule(False)
+
+
+def _batch_case(seed0=80):
+    rng = np.random.default_rng(seed0)
+    leaves, gss, qms, Qs = [], [], [], []
+    for k in range(5):
+        n = int(rng.integers(60, 900))
+        leaves.append(globule(n, 0.5 + 0.02 * n ** (1 / 3) * 3, seed=seed0 + k, extra=SOLVENT if k % 2 else VACUUM))
+        gss.append(int(rng.integers(6, 16)) * 2)
+        qms.append(float(rng.uniform(2.0, 6.0)))
+        lo = 0.0 if k % 2 == 0 else 0.3
+        Qs.append(np.linspace(lo, qms[-1], int(rng.integers(20, 60))))
+    return leaves, gss, qms, Qs
+
+
+@pytest.mark.parametrize("prec", [M.FP32, M.FP64])
+def test_solve_batch_equals_single_solves(ctx, prec):
+    """dpx_batch (one graph per wave, one fill launch per wave) gives the same
+    I(q) as one DomainModel solve per structure, also when the grid budget
+    splits the batch into several waves; replaying the graphs is stable."""
+    leaves, gss, qms, Qs = _batch_case()
+    dirs = M.mc_directions(9, 500)
+    singles = [M.DomainModel([a], gs, qm, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+               for a, gs, qm, Q in zip(leaves, gss, qms, Qs)]
+    for budget in (0, 1):  # 1 byte: every structure is its own wave
+        b = M.SolveBatch(ctx, leaves, gss, qms, Qs, dirs, precision=prec, grid_budget_bytes=budget)
+        waves, launches, _ = b.info()
+        assert waves == (5 if budget == 1 else 1)
+        assert launches > 0
+        for _ in range(2):
+            b.run()
+            for r, s in zip(b.results(), singles):
+                assert np.allclose(r, s, rtol=1e-12, atol=0)
+        b.close()
+    if prec == M.FP64:  # pin one structure to the oracle
+        data, co = oracle_grid(leaves[0], gss[0], qms[0])
+        ref = O.integrate_layers(gss[0], qms[0], [O.make_leaf(data, co)], Qs[0], dirs, 0, len(dirs), 0.0)
+        assert rel(singles[0], ref) <= TOL64
