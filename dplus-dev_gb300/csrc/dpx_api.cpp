@@ -602,9 +602,10 @@ void make_brackets(const dpx::Geom& G, int grid_size, double qmax, int nq, const
     }
 }
 
-int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
-                   const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
-                   std::vector<dpx::ModelDev>& md, std::vector<char>& gstage) {
+int build_models(int n_models, const void* const* cells, const double* rot, const double* tr, const int* n_copies,
+                 const double* copy_rot, const double* copy_tr, const double* sym_scale, ModelTables& t) {
+    std::vector<dpx::ModelDev>& md = t.md;
+    std::vector<char>& gstage = t.gstage;
     md.assign(n_models, dpx::ModelDev{});
     std::vector<double> gR, gT;
     std::vector<int> gOff;
@@ -612,7 +613,7 @@ int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const doubl
     int copy_base = 0;
     for (int m = 0; m < n_models; ++m) {
         dpx::ModelDev& M = md[m];
-        M.grid = grids[m]->cells;
+        M.grid = cells[m];
         euler(rot ? rot[3 * m] : 0, rot ? rot[3 * m + 1] : 0, rot ? rot[3 * m + 2] : 0, M.R);
         for (int k = 0; k < 3; ++k) M.tr[k] = tr ? tr[3 * m + k] : 0.0;
         const int nc = n_copies ? n_copies[m] : 0;
@@ -653,23 +654,42 @@ int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const doubl
     // device layout of the group tables: [R (doubles)] [T (doubles)] [off (ints)]
     const size_t bytesR = gR.size() * sizeof(double), bytesT = gT.size() * sizeof(double),
                  bytesO = gOff.size() * sizeof(int);
-    DPX_CUDA(ctx->groups.reserve(bytesR + bytesT + bytesO + 64));
-    char* gbase = (char*)ctx->groups.p;
-    double* dR = (double*)gbase;
-    double* dT = (double*)(gbase + bytesR);
-    int* dO = (int*)(gbase + bytesR + bytesT);
     gstage.assign(bytesR + bytesT + bytesO, 0);
     if (bytesR) std::memcpy(gstage.data(), gR.data(), bytesR);
     if (bytesT) std::memcpy(gstage.data() + bytesR, gT.data(), bytesT);
     if (bytesO) std::memcpy(gstage.data() + bytesR + bytesT, gOff.data(), bytesO);
+    t.oR.assign(n_models, 0);
+    t.oT.assign(n_models, 0);
+    t.oO.assign(n_models, 0);
     int groups_seen = 0;
     for (int m = 0; m < n_models; ++m) {
-        dpx::ModelDev& M = md[m];
-        M.group_R = dR + 9 * groups_seen;
-        M.group_off = dO + model_group_base[m];
-        M.trans = dT + 3 * model_toff_base[m];
-        groups_seen += M.n_groups;
+        t.oR[m] = 9 * sizeof(double) * (size_t)groups_seen;
+        t.oO[m] = bytesR + bytesT + sizeof(int) * (size_t)model_group_base[m];
+        t.oT[m] = bytesR + 3 * sizeof(double) * (size_t)model_toff_base[m];
+        groups_seen += md[m].n_groups;
     }
+    return DPX_OK;
+}
+
+void place_models(ModelTables& t, char* dbase) {
+    for (size_t m = 0; m < t.md.size(); ++m) {
+        t.md[m].group_R = reinterpret_cast<const double*>(dbase + t.oR[m]);
+        t.md[m].group_off = reinterpret_cast<const int*>(dbase + t.oO[m]);
+        t.md[m].trans = reinterpret_cast<const double*>(dbase + t.oT[m]);
+    }
+}
+
+int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
+                   const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
+                   std::vector<dpx::ModelDev>& md, std::vector<char>& gstage) {
+    std::vector<const void*> cells(n_models);
+    for (int m = 0; m < n_models; ++m) cells[m] = grids[m]->cells;
+    ModelTables t;
+    if (int rc = build_models(n_models, cells.data(), rot, tr, n_copies, copy_rot, copy_tr, sym_scale, t)) return rc;
+    DPX_CUDA(ctx->groups.reserve(t.gstage.size() + 64));
+    place_models(t, (char*)ctx->groups.p);
+    md.swap(t.md);
+    gstage.swap(t.gstage);
     return DPX_OK;
 }
 

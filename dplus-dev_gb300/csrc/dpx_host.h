@@ -86,6 +86,17 @@ void aff_table(int U, const int* api, const double* coeffs, const double* rads, 
 void euler(double a, double b, double c, double R[9]);
 int check_pdb(const dpx_pdb_desc& d);
 
+// Model structs of one average and their docked-copy group tables.  build_models
+// stages the tables on the host (gstage) with offsets; place_models points the
+// structs at the tables' device copy.
+struct ModelTables {
+    std::vector<dpx::ModelDev> md;
+    std::vector<char> gstage;
+    std::vector<size_t> oR, oT, oO;
+};
+int build_models(int n_models, const void* const* cells, const double* rot, const double* tr, const int* n_copies,
+                 const double* copy_rot, const double* copy_tr, const double* sym_scale, ModelTables& t);
+void place_models(ModelTables& t, char* dbase);
 // Model structs for the kernels; group tables staged in gstage for ctx->groups.
 int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const double* rot, const double* tr,
                    const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,

@@ -123,6 +123,8 @@ cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_model
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
 // d_res[0] = |origin cell|^2 (I at q = 0 of one plain leaf)
 cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res);
+// d_res[0] = |sum_m w_m A_m(0)|^2 over placed (and docked) models
+cudaError_t launch_origin_models(cudaStream_t s, bool fp64, const ModelDev* d_models, int n_models, double* d_res);
 cudaError_t launch_pack_values_f32(cudaStream_t s, const float4* grid, int64_t P, double* out);
 cudaError_t launch_pack_values_f64(cudaStream_t s, const double4_32a* grid, int64_t P, double* out);
 cudaError_t launch_unpack_f64(cudaStream_t s, const double* vals, const double* ders, int64_t P, double4_32a* grid);

@@ -925,6 +925,36 @@ __global__ void origin_intensity_kernel(const void* grid, int fp64, double* res)
 }
 }  // namespace
 
+namespace {
+// I(0) = |sum_m w_m A_m(0)|^2 over placed models (Amplitude.cpp:1176-1182);
+// a docked model weighs K copies x its symmetry scale.
+__global__ void origin_models_kernel(const ModelDev* __restrict__ models, int n_models, int fp64, double* res) {
+    double ar = 0, ai = 0;
+    for (int m = 0; m < n_models; ++m) {
+        const ModelDev& M = models[m];
+        double re, im;
+        if (fp64) {
+            const double* g = static_cast<const double*>(M.grid);
+            re = g[0];
+            im = g[1];
+        } else {
+            const float* g = static_cast<const float*>(M.grid);
+            re = g[0];
+            im = g[1];
+        }
+        const double w = M.n_groups > 0 ? (double)M.group_off[M.n_groups] * M.sym_scale : 1.0;
+        ar += w * re;
+        ai += w * im;
+    }
+    res[0] = ar * ar + ai * ai;
+}
+}  // namespace
+
+cudaError_t launch_origin_models(cudaStream_t s, bool fp64, const ModelDev* d_models, int n_models, double* d_res) {
+    origin_models_kernel<<<1, 1, 0, s>>>(d_models, n_models, fp64 ? 1 : 0, d_res);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res) {
     origin_intensity_kernel<<<1, 1, 0, s>>>(grid, fp64 ? 1 : 0, d_res);
     return cudaGetLastError();

@@ -17,7 +17,7 @@ INCLUDE_DIR = os.path.join(REPO_DIR, "include")
 BUILD_DIR = os.path.join(os.path.dirname(PKG_DIR), "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libdpx.so")
 
-SOURCES = ["dpx_fill.cu", "dpx_kernels.cu", "dpx_api.cpp", "dpx_batch.cpp", "dpx_noalloc.cu"]
+SOURCES = ["dpx_fill.cu", "dpx_kernels.cu", "dpx_api.cpp", "dpx_batch.cpp", "dpx_server.cpp", "dpx_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

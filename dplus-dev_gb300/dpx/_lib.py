@@ -46,6 +46,21 @@ class SolveDesc(C.Structure):
     _fields_ = [("pdb", PdbDesc), ("grid_size", C.c_int), ("qmax", C.c_double), ("nq", C.c_int), ("Q", _D)]
 
 
+class Request(C.Structure):
+    """dpx_request: one I(q) solve submitted to a dpx_server."""
+    _fields_ = [("n_leaves", C.c_int), ("leaves", C.POINTER(PdbDesc)), ("leaf_keys", C.POINTER(C.c_uint64)),
+                ("n_models", C.c_int), ("model_leaf", _I), ("rot", _D), ("tr", _D), ("n_copies", _I),
+                ("copy_rot", _D), ("copy_tr", _D), ("sym_scale", _D), ("grid_size", C.c_int), ("qmax", C.c_double),
+                ("precision", C.c_int), ("nq", C.c_int), ("Q", _D), ("n_samples", C.c_int64), ("eps", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """dpx_server_stats."""
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "completed", "failed", "grid_fills", "grid_hits",
+                                         "fill_launches", "steps", "evictions", "bytes_in_use", "bytes_peak",
+                                         "budget", "cached_grids")]
+
+
 _SIGS = {
     "dpx_last_error": (C.c_char_p, []),
     "dpx_version": (C.c_int, []),
@@ -100,6 +115,12 @@ _SIGS = {
     "dpx_batch_result": (C.c_int, [_P, C.c_int, _D]),
     "dpx_batch_info": (C.c_int, [_P, _I, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "dpx_batch_destroy": (C.c_int, [_P]),
+    "dpx_server_create": (C.c_int, [_P, C.c_int64, C.c_int, C.c_int, _D, C.c_int64, C.POINTER(_P)]),
+    "dpx_server_submit": (C.c_int, [_P, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "dpx_server_poll": (C.c_int, [_P, C.c_uint64]),
+    "dpx_server_wait": (C.c_int, [_P, C.c_uint64, _D, _D]),
+    "dpx_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "dpx_server_destroy": (C.c_int, [_P]),
     "dpx_mc_average_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, _D, _P, C.c_int64, C.c_double,
                                          _P, _P]),
 }

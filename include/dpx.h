@@ -280,6 +280,64 @@ int dpx_batch_result(dpx_batch b, int j, double* res);
 int dpx_batch_info(dpx_batch b, int* n_waves, int64_t* kernels_per_run, int64_t* pool_bytes);
 int dpx_batch_destroy(dpx_batch b);
 
+/* ---- serving engine (no counterpart in the reference, which runs one job
+ * at a time on its job thread, JobManager.cpp:151-206) ----
+ * A request is an I(q) solve of placed, optionally docked PDB leaves on one
+ * grid (grid_size, qmax, precision): models name a leaf, a placement (rot,
+ * tr: [3 n_models] radians / nm, NULL = identity) and optional copies as in
+ * dpx_orientation_average.  Inputs are copied at submission.  One worker
+ * thread admits requests in arrival order while the device-memory budget
+ * holds (grids not yet resident + scratch; unpinned cached grids are evicted
+ * least-recently-used first; a request that does not fit yet lets later
+ * ones pass), fills all grids the admitted requests miss in one batched
+ * launch, and runs each request's Monte Carlo average on one of n_streams
+ * streams, so requests that arrive while others run overlap with them.  Grids
+ * stay resident keyed by leaf content (or leaf_keys[l] != 0) and grid
+ * parameters: requests that change only placements reuse them.  The shared
+ * direction set (n_dirs (theta, phi) pairs) is given once; a request uses its
+ * first n_samples. */
+typedef struct dpx_request {
+    int n_leaves;
+    const dpx_pdb_desc* leaves;   /* host atoms */
+    const uint64_t* leaf_keys;    /* NULL or per leaf; 0 = key by content */
+    int n_models;
+    const int* model_leaf;        /* [n_models] leaf index per model */
+    const double* rot;
+    const double* tr;
+    const int* n_copies;          /* NULL = no docked copies */
+    const double* copy_rot;
+    const double* copy_tr;
+    const double* sym_scale;      /* NULL = 1 */
+    int grid_size;
+    double qmax;
+    int precision;
+    int nq;
+    const double* Q;              /* ascending, within [0, qmax] */
+    int64_t n_samples;
+    double eps;
+} dpx_request;
+typedef struct dpx_server_stats {
+    int64_t submitted, completed, failed;
+    int64_t grid_fills;           /* leaves filled */
+    int64_t grid_hits;            /* leaves found resident */
+    int64_t fill_launches, steps, evictions;
+    int64_t bytes_in_use, bytes_peak, budget;
+    int64_t cached_grids;
+} dpx_server_stats;
+typedef struct dpx_server_s* dpx_server;
+/* hbm_budget_bytes <= 0: 80% of the free device memory. */
+int dpx_server_create(dpx_ctx ctx, int64_t hbm_budget_bytes, int max_inflight, int n_streams, const double* dirs,
+                      int64_t n_dirs, dpx_server* out);
+int dpx_server_submit(dpx_server s, const dpx_request* r, uint64_t* ticket);
+/* 1 when the request has finished (or failed), 0 while it waits or runs. */
+int dpx_server_poll(dpx_server s, uint64_t ticket);
+/* Blocks until the request finishes; res [nq]; latency_ms = submission to
+ * completion.  Returns the request's status; the ticket is then released. */
+int dpx_server_wait(dpx_server s, uint64_t ticket, double* res, double* latency_ms);
+int dpx_server_stats_get(dpx_server s, dpx_server_stats* st);
+/* Finishes every submitted request, then frees the server. */
+int dpx_server_destroy(dpx_server s);
+
 /* ---- allocation-free orientation average ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc /
  * cudaFree: applications whose device memory is pre-reserved by their own pool
