@@ -35,11 +35,15 @@ N_DIRS, DIR_SEED = 100_000, 1234
 # ncu dram__bytes_read+write of fill_f32_kernel on the profile shape (2,000 atoms,
 # 120 layers, 11.3 M cells): 335 MB, i.e. 29.6 B per cell; scaled to 50.7 M cells
 FILL_TRAFFIC = 29.6 * 50688289
-EXTRA = [1, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 4]  # scale, solventED, c1, ..., radType 4 (dummy atoms)
-CONFIG = {"workload": "single subunit, 20,000-atom globule r=5 nm, dummy-atom solvent 333 e/nm^3, "
-                      "L=200 (50,688,289 cells), qmax 7.5, 500 q, MC 1e5 fixed directions",
+# scale, solventED, c1, voxelStep, probe radius, solvation thickness, outer (layer) ED, fillHoles,
+# solventOnly, radius type 4 (dummy atoms): dummy-atom solvent at 333 e/nm^3 and a 0.3 nm voxelized
+# solvation layer at 400 e/nm^3
+EXTRA = [1, 333, 1, 0.05, 0.14, 0.3, 400, 0, 0, 4]
+CONFIG = {"workload": "single subunit, 20,000-atom globule r=5 nm, dummy-atom solvent 333 e/nm^3, 0.3 nm "
+                      "voxelized solvation layer at 400 e/nm^3 (0.05 nm voxels), L=200 (50,688,289 cells), "
+                      "qmax 7.5, 500 q, MC 1e5 fixed directions",
           "atoms": N_ATOMS, "grid_layers": GRID_SIZE // 2, "qmax": QMAX, "q_points": NQ, "mc_directions": N_DIRS,
-          "precision": "fp32-bulk", "solvation_layer": "not included (voxelized layer not built)",
+          "precision": "fp32-bulk", "solvation_layer": "0.3 nm at 400 e/nm^3, voxel 0.05 nm",
           "l2": "grid 811 MB written and read per step (> 129 MB L2)"}
 
 
@@ -152,6 +156,10 @@ def run_dpx(args):
         best, table = M.autotune_fill(ctx, [amp], QMAX, GRID_SIZE, repeats=1)
         tune = {"best": "%dx%d%s" % (best[0], best[1], "p" if best[2] else ""),
                 "fill_ms": {"%dx%d%s" % (k[0], k[1], "p" if k[2] else ""): round(v, 3) for k, v in table.items()}}
+    t_vox = time.perf_counter()
+    boxes = amp.solvent_boxes()  # voxelization: host, once per structure (PreCalculate)
+    voxelize_s = time.perf_counter() - t_vox
+    n_boxes = 0 if boxes is None else len(boxes)
     atoms_h = amp.atoms_float4()
     # device-resident inputs for the kernel-level number (centred on the host once)
     cen = amp.xyz.mean(0)
@@ -169,18 +177,19 @@ def run_dpx(args):
           for k in ("fill", "splines", "average")}
     times = {k: [] for k in ev}
 
+    desc_dev, keep_dev = M.pdb_descs([amp])
+    desc_dev[0].atoms, desc_dev[0].atoms_on_device = d_atoms.data_ptr(), 1  # centred, resident
+    desc_dev[0].center = _lib.dptr(cen_arr)
+
     def solve(device_inputs: bool, timed_parts: bool = False):
         if timed_parts:
             ev["fill"][0].record(stream)
         if device_inputs:
             # atoms already centred and resident; the centring phase is restored per cell
-            _lib.check(L.dpx_grid_fill_pdb(grid.handle, N_ATOMS, C.c_void_p(d_atoms.data_ptr()), 1, len(api),
-                                           _lib.iptr(api), _lib.dptr(co), _lib.dptr(rads), amp.flags,
-                                           amp.solventED, amp.c1, amp.scale, _lib.dptr(cen_arr)))
+            _lib.check(L.dpx_grid_fill_pdb_batch(1, gh, desc_dev))
         else:
-            _lib.check(L.dpx_grid_fill_pdb(grid.handle, N_ATOMS, atoms_h.ctypes.data_as(C.c_void_p), 0, len(api),
-                                           _lib.iptr(api), _lib.dptr(co), _lib.dptr(rads), amp.flags,
-                                           amp.solventED, amp.c1, amp.scale, None))
+            desc_h, keep_h = M.pdb_descs([amp])  # host atoms and boxes, staged by the call
+            _lib.check(L.dpx_grid_fill_pdb_batch(1, gh, desc_h))
         if timed_parts:
             ev["fill"][1].record(stream)
             ev["splines"][0].record(stream)
@@ -256,8 +265,9 @@ def run_dpx(args):
         cpt = ctx.fill_shape()[0]
         # row-factored fill: per work item (CPT cells of a theta row, each with its
         # z-mirror) and atom, 1 + CPT sincos = 2 (1 + CPT) SFU ops
+        # (solvent boxes cost the same per work item: their extent factors are cached)
         items = 1 + sum((3 * i // 2 + 1) * ((3 * i + cpt - 1) // cpt) for i in range(1, lp + 1))
-        sfu_ops = float(N_ATOMS) * items * 2 * (1 + cpt)
+        sfu_ops = float(N_ATOMS + n_boxes) * items * 2 * (1 + cpt)
         # SFU roofline: 16 MUFU lanes/SM/clk x 152 SMs at the maximum SM clock
         sfu_peak = 152 * 16 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12  # Tops/s
         achieved = sfu_ops / (fill_ms / 1e3) / 1e12
@@ -269,18 +279,21 @@ def run_dpx(args):
             "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded globule)", "config": CONFIG,
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(atoms_h.nbytes + Q.nbytes +
-                                                                               dirs.nbytes),
-                    "d2h_bytes_per_step": int(res.nbytes)},
+                                                                               dirs.nbytes + 32 * n_boxes),
+                    "d2h_bytes_per_step": int(res.nbytes),
+                    "note": "voxelization (host, once per structure) excluded: voxelize_s"},
+            "voxelize_s": voxelize_s, "solvent_boxes": n_boxes,
             "gpu_launches": args.steps * 4,
             "roofline": {"bound": "sfu", "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] else "flat"),
                          "fill_shape": "%dx%d%s" % (ctx.fill_shape()[0], ctx.fill_shape()[1],
                                                     "p" if ctx.fill_shape()[2] else ""),
                          "achieved": achieved, "peak": sfu_peak,
                          "unit": "T SFU-op/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
-                         "note": "SFU ops = atoms x work items x 2(1+CPT) (row-factored fill); peak = 152 SM x 16 "
+                         "note": "SFU ops = (atoms + solvent boxes) x work items x 2(1+CPT) (row-factored fill); "
+                                 "peak = 152 SM x 16 "
                                  "MUFU/clk at sm_max_mhz (derived, not in MEASURED_PEAKS.json); traffic = ncu "
                                  "dram bytes of the profile shape scaled by cells",
-                         "algorithmic_pairs_per_s": float(N_ATOMS) * P / (fill_ms / 1e3)},
+                         "algorithmic_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)},
             "roofline_average": {"bound": "hbm", "kernel": "average_kernel",
                                  "achieved": interp_bytes / (avg_ms / 1e3) / 1e9, "peak": peaks["hbm_gbs"],
                                  "unit": "GB/s", "frac": interp_bytes / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"],
@@ -586,9 +599,10 @@ def cpu_baseline(seconds: float):
     t_spl = time.perf_counter() - t0
     solve_s = t_fill + t_spl
     return {"value": 1.0 / solve_s, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": f"outer {shells} shell(s) of the grid fill ({cells} cells x {N_ATOMS} atoms, "
-                      f"{dt:.1f} s) scaled by cells to {P}; splines timed in full; orientation average "
-                      f"not included (<1%)"}
+            "sample": f"outer {shells} shell(s) of the grid fill ({cells} cells x ({N_ATOMS} atoms + "
+                      f"{0 if s.boxes is None else len(s.boxes)} solvent boxes), {dt:.1f} s) scaled by cells to "
+                      f"{P}; splines timed in full; orientation average not included (<1%); voxelization "
+                      f"(host, once per structure) not included"}
 
 
 def run_reference(args):

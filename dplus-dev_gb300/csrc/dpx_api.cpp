@@ -344,118 +344,39 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     if (int rc = set_device(ctx)) return rc;
     cudaStream_t s = ctx->stream;
 
-    // host staging: centred host atoms, then per job [ion offsets][aff][item prefix]
-    std::vector<double> cen(3 * n, 0.0);
-    size_t atom_bytes = 0;
-    std::vector<size_t> atom_off(n, SIZE_MAX), tab_off(n);
-    std::vector<int64_t> n_items(n);
-    std::vector<std::vector<int64_t>> prefs(n);
-    size_t tab_bytes = 0;
+    // host staging of every leaf, then the FP32 job table and the tile counter
+    std::vector<char>& h = ctx->host_stage;
+    h.clear();
+    std::vector<LeafTables> lt(n);
     for (int j = 0; j < n; ++j) {
-        const dpx_pdb_desc& d = pdbs[j];
         const bool fp32 = grids[j]->precision == DPX_FP32;
-        if (d.center) {
-            for (int k = 0; k < 3; ++k) cen[3 * j + k] = d.center[k];
-        } else if (!d.atoms_on_device && fp32) {  // centroid of the host atoms
-            double acc[3] = {0, 0, 0};
-            for (int64_t a = 0; a < d.n_atoms; ++a)
-                for (int k = 0; k < 3; ++k) acc[k] += d.atoms[4 * a + k];
-            for (int k = 0; k < 3; ++k) cen[3 * j + k] = acc[k] / double(d.n_atoms);
-        }
-        if (!fp32 && !d.atoms_on_device) cen[3 * j] = cen[3 * j + 1] = cen[3 * j + 2] = 0.0;  // exact FP64 phases
-        if (!d.atoms_on_device) {
-            atom_off[j] = atom_bytes;
-            atom_bytes = al16(atom_bytes + (size_t)d.n_atoms * sizeof(float4));
-        }
-        prefs[j].resize(grids[j]->g.Lp + 1);
-        n_items[j] = dpx::fill_items(grids[j]->g, fp32 ? cpt : dpx::kFill64Cells, prefs[j].data());
-        tab_off[j] = tab_bytes;
-        tab_bytes = al16(tab_bytes + (d.n_ions + 1) * sizeof(int));
-        tab_bytes = al16(tab_bytes + (size_t)d.n_ions * (grids[j]->g.Lp + 1) * (fp32 ? sizeof(float) : sizeof(double)));
-        tab_bytes = al16(tab_bytes + prefs[j].size() * sizeof(int64_t));
+        stage_leaf(h, pdbs[j], grids[j]->g, fp32, fp32 ? cpt : dpx::kFill64Cells, lt[j]);
     }
-    const size_t jobs_off = al16(atom_bytes + tab_bytes);
+    const size_t jobs_off = al16(h.size());
     const size_t counter_off = al16(jobs_off + (size_t)n * sizeof(dpx::FillJob));
-    const size_t total = counter_off + 64;
-    DPX_CUDA(ctx->atoms.reserve(total));
-    ctx->host_stage.assign(total, 0);
-    char* h = ctx->host_stage.data();
-    char* dbase = (char*)ctx->atoms.p;
+    h.resize(counter_off + 64, 0);
+    DPX_CUDA(ctx->atoms.reserve(h.size()));
+    const char* dbase = (const char*)ctx->atoms.p;
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
-    std::vector<double> aff;
     for (int j = 0; j < n; ++j) {
-        const dpx_pdb_desc& d = pdbs[j];
-        const Geom& G = grids[j]->g;
-        const bool fp32 = grids[j]->precision == DPX_FP32;
-        const float4* d_atoms = reinterpret_cast<const float4*>(d.atoms);
-        if (!d.atoms_on_device) {
-            float4* ha = reinterpret_cast<float4*>(h + atom_off[j]);
-            for (int64_t a = 0; a < d.n_atoms; ++a) {
-                ha[a].x = (float)((double)d.atoms[4 * a] - cen[3 * j]);
-                ha[a].y = (float)((double)d.atoms[4 * a + 1] - cen[3 * j + 1]);
-                ha[a].z = (float)((double)d.atoms[4 * a + 2] - cen[3 * j + 2]);
-                ha[a].w = 0.f;
-            }
-            d_atoms = reinterpret_cast<const float4*>(dbase + atom_off[j]);
-        }
-        size_t o = atom_bytes + tab_off[j];
-        int* off = reinterpret_cast<int*>(h + o);
-        off[0] = 0;
-        for (int u = 0; u < d.n_ions; ++u) off[u + 1] = off[u] + d.atoms_per_ion[u];
-        const int* d_off = reinterpret_cast<const int*>(dbase + o);
-        o = al16(o + (d.n_ions + 1) * sizeof(int));
-        aff_table(d.n_ions, d.atoms_per_ion, d.coeffs, d.ion_rads, d.flags, d.solvent_ed, d.c1, G.Lp, G.step, aff);
-        const void* d_aff = dbase + o;
-        if (fp32) {
-            float* af = reinterpret_cast<float*>(h + o);
-            for (size_t k = 0; k < aff.size(); ++k) af[k] = (float)aff[k];
-            o = al16(o + aff.size() * sizeof(float));
-        } else {
-            std::memcpy(h + o, aff.data(), aff.size() * sizeof(double));
-            o = al16(o + aff.size() * sizeof(double));
-        }
-        std::memcpy(h + o, prefs[j].data(), prefs[j].size() * sizeof(int64_t));
-        const int64_t* d_pref = reinterpret_cast<const int64_t*>(dbase + o);
-        if (fp32) {
-            dpx::FillJob J{};
-            J.atoms = d_atoms;
-            J.ion_off = d_off;
-            J.aff_f32 = (const float*)d_aff;
-            J.pref = d_pref;
-            J.grid = (float4*)grids[j]->cells;
-            J.n_items = n_items[j];
-            J.tile_start = tiles;
-            J.step = G.step;
-            J.cx = cen[3 * j];
-            J.cy = cen[3 * j + 1];
-            J.cz = cen[3 * j + 2];
-            J.use_center = (J.cx != 0.0 || J.cy != 0.0 || J.cz != 0.0);
-            J.U = d.n_ions;
-            J.Lp = G.Lp;
-            J.scale = (float)d.scale;
-            jobs.push_back(J);
-            tiles += (n_items[j] + threads - 1) / threads;
-        }
+        if (grids[j]->precision != DPX_FP32) continue;
+        jobs.push_back(make_job(pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, tiles));
+        tiles += (lt[j].items + threads - 1) / threads;
     }
-    if (!jobs.empty()) std::memcpy(h + jobs_off, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
-    DPX_CUDA(cudaMemcpyAsync(dbase, h, counter_off, cudaMemcpyHostToDevice, s));
+    if (!jobs.empty()) std::memcpy(h.data() + jobs_off, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
+    DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h.data(), counter_off, cudaMemcpyHostToDevice, s));
     if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
+    bool boxes = false;
+    for (const dpx::FillJob& J : jobs) boxes |= J.n_boxes > 0;
     cudaError_t e = dpx::launch_fill_f32_batch(s, (const dpx::FillJob*)(dbase + jobs_off), (int)jobs.size(), tiles,
-                                               (unsigned long long*)(dbase + counter_off), cpt, threads, persistent);
+                                               (unsigned long long*)(dbase + counter_off), cpt, threads, persistent,
+                                               boxes);
     if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
     if (ev1) DPX_CUDA(cudaEventRecord(ev1, s));
     for (int j = 0; j < n; ++j) {  // the plain FP64 path: one launch per leaf
         if (grids[j]->precision != DPX_FP64) continue;
-        const dpx_pdb_desc& d = pdbs[j];
-        const size_t o = atom_bytes + tab_off[j];
-        const size_t oa = al16(o + (d.n_ions + 1) * sizeof(int));
-        const size_t op = al16(oa + (size_t)d.n_ions * (grids[j]->g.Lp + 1) * sizeof(double));
-        const float4* d_atoms = d.atoms_on_device ? reinterpret_cast<const float4*>(d.atoms)
-                                                  : reinterpret_cast<const float4*>(dbase + atom_off[j]);
-        e = dpx::launch_fill_f64(s, d_atoms, (const int*)(dbase + o), d.n_ions, (const double*)(dbase + oa),
-                                 grids[j]->g, (const int64_t*)(dbase + op), n_items[j], &cen[3 * j], d.scale,
-                                 (double4_32a*)grids[j]->cells);
+        e = launch_leaf_f64(s, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells);
         if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
     }
     // the staging buffer is reused by the next call: wait for the copy and the kernels
@@ -523,7 +444,7 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
                       double solvent_ed, double c1, double scale, const double* center) {
     if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
     dpx_pdb_desc d{n_atoms, atoms, atoms_on_device, n_ions, atoms_per_ion, coeffs, ion_rads, flags,
-                   solvent_ed, c1, scale, center};
+                   solvent_ed, c1, scale, center, 0, nullptr};
     return dpx_grid_fill_pdb_batch(1, &g, &d);
 }
 

@@ -76,13 +76,9 @@ struct SolvePlan {
     int grid_size;
     double qmax;
     size_t grid_off;  // in the pool
-    size_t o_atoms, o_off, o_aff, o_pref, o_model, o_bq, o_bl, o_bo, o_bi;
-    int64_t n_items;
-    double cen[3];
+    LeafTables lt;  // offsets in the arena
+    size_t o_model, o_bq, o_bl, o_bo, o_bi;
     bool origin;  // Q[0] == 0
-    int U;
-    float scale32;
-    double scale;
     dpx::AvgPlan plan;  // pointers filled once the arena exists
 };
 
@@ -149,53 +145,12 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     // staging of every input table
     Stage st;
     size_t partial_max = 0;
-    std::vector<double> aff;
-    std::vector<float> affF;
-    std::vector<float4> atoms;
     for (int j = 0; j < n; ++j) {
         const dpx_solve_desc& d = solves[j];
         const dpx_pdb_desc& pd = d.pdb;
         SolvePlan& p = sp[j];
         const Geom& G = p.G;
-        // centring: FP32 grids shift host atoms by their centroid (restored as a
-        // per-cell phase), FP64 grids take them as they are
-        for (int k = 0; k < 3; ++k) p.cen[k] = 0.0;
-        if (pd.center) {
-            for (int k = 0; k < 3; ++k) p.cen[k] = pd.center[k];
-        } else if (!pd.atoms_on_device && fp32) {
-            double acc[3] = {0, 0, 0};
-            for (int64_t a = 0; a < pd.n_atoms; ++a)
-                for (int k = 0; k < 3; ++k) acc[k] += pd.atoms[4 * a + k];
-            for (int k = 0; k < 3; ++k) p.cen[k] = acc[k] / double(pd.n_atoms);
-        }
-        if (!fp32 && !pd.atoms_on_device) p.cen[0] = p.cen[1] = p.cen[2] = 0.0;
-        if (pd.atoms_on_device) {
-            p.o_atoms = SIZE_MAX;
-        } else {
-            atoms.resize(pd.n_atoms);
-            for (int64_t a = 0; a < pd.n_atoms; ++a)
-                atoms[a] = make_float4((float)((double)pd.atoms[4 * a] - p.cen[0]),
-                                       (float)((double)pd.atoms[4 * a + 1] - p.cen[1]),
-                                       (float)((double)pd.atoms[4 * a + 2] - p.cen[2]), 0.f);
-            p.o_atoms = st.put(atoms.data(), atoms.size() * sizeof(float4));
-        }
-        std::vector<int> off(pd.n_ions + 1, 0);
-        for (int u = 0; u < pd.n_ions; ++u) off[u + 1] = off[u] + pd.atoms_per_ion[u];
-        p.o_off = st.put(off.data(), off.size() * sizeof(int));
-        aff_table(pd.n_ions, pd.atoms_per_ion, pd.coeffs, pd.ion_rads, pd.flags, pd.solvent_ed, pd.c1, G.Lp, G.step,
-                  aff);
-        if (fp32) {
-            affF.assign(aff.begin(), aff.end());
-            p.o_aff = st.put(affF.data(), affF.size() * sizeof(float));
-        } else {
-            p.o_aff = st.put(aff.data(), aff.size() * sizeof(double));
-        }
-        std::vector<int64_t> pref(G.Lp + 1);
-        p.n_items = dpx::fill_items(G, cpt, pref.data());
-        p.o_pref = st.put(pref.data(), pref.size() * sizeof(int64_t));
-        p.U = pd.n_ions;
-        p.scale = pd.scale;
-        p.scale32 = (float)pd.scale;
+        stage_leaf(st.h, pd, G, fp32, cpt, p.lt);
         // brackets and the plain identity model
         Brackets B;
         make_brackets(G, p.grid_size, p.qmax, d.nq, d.Q, B);
@@ -265,25 +220,8 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
             dpx::ModelDev* M = reinterpret_cast<dpx::ModelDev*>(st.h.data() + p.o_model);
             M->grid = pool + p.grid_off;
             if (fp32) {
-                dpx::FillJob J{};
-                J.atoms = p.o_atoms == SIZE_MAX ? reinterpret_cast<const float4*>(solves[j].pdb.atoms)
-                                                : reinterpret_cast<const float4*>(A + p.o_atoms);
-                J.ion_off = reinterpret_cast<const int*>(A + p.o_off);
-                J.aff_f32 = reinterpret_cast<const float*>(A + p.o_aff);
-                J.pref = reinterpret_cast<const int64_t*>(A + p.o_pref);
-                J.grid = reinterpret_cast<float4*>(pool + p.grid_off);
-                J.n_items = p.n_items;
-                J.tile_start = tiles;
-                J.step = p.G.step;
-                J.cx = p.cen[0];
-                J.cy = p.cen[1];
-                J.cz = p.cen[2];
-                J.use_center = (p.cen[0] != 0.0 || p.cen[1] != 0.0 || p.cen[2] != 0.0);
-                J.U = p.U;
-                J.Lp = p.G.Lp;
-                J.scale = p.scale32;
-                jobs.push_back(J);
-                tiles += (p.n_items + threads - 1) / threads;
+                jobs.push_back(make_job(solves[j].pdb, p.lt, A, p.G, pool + p.grid_off, tiles));
+                tiles += (p.lt.items + threads - 1) / threads;
             }
             dpx::AvgPlan& P = p.plan;
             P.br_q = reinterpret_cast<const double*>(A + p.o_bq);
@@ -316,19 +254,16 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         int64_t launches = 0;
         const int j0 = b->wave_first[w], j1 = b->wave_first[w + 1];
         if (fp32) {
+            bool boxes = false;
+            for (int j = j0; j < j1; ++j) boxes |= sp[j].lt.n_boxes > 0;
             e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(A + o_jobs[w]), j1 - j0,
                                            wave_tiles[w], reinterpret_cast<unsigned long long*>(A + o_counter[w]),
-                                           cpt, threads, persistent);
+                                           cpt, threads, persistent, boxes);
             launches++;
         } else {
             for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
                 const SolvePlan& p = sp[j];
-                const float4* at = p.o_atoms == SIZE_MAX ? reinterpret_cast<const float4*>(solves[j].pdb.atoms)
-                                                         : reinterpret_cast<const float4*>(A + p.o_atoms);
-                e = dpx::launch_fill_f64(s, at, reinterpret_cast<const int*>(A + p.o_off), p.U,
-                                         reinterpret_cast<const double*>(A + p.o_aff), p.G,
-                                         reinterpret_cast<const int64_t*>(A + p.o_pref), p.n_items, p.cen, p.scale,
-                                         reinterpret_cast<double4_32a*>(pool + p.grid_off));
+                e = launch_leaf_f64(s, solves[j].pdb, p.lt, A, p.G, pool + p.grid_off);
                 launches++;
             }
         }

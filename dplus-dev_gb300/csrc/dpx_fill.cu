@@ -76,12 +76,65 @@ __device__ __forceinline__ void store_quad(V2* __restrict__ g2, int i, int t, in
 // fields arrive as scalar __restrict__ arguments so that the inner loop keeps
 // them in registers.
 // --------------------------------------------------------------------------
+// Voxelized-solvent boxes (PDBAmplitude.cpp:277-314): each adds
+//   w prod_a [L_a sinc(q_a L_a / 2)] e^{i q.c}
+// with the same row factoring as the atoms: the z factor and e^{+-i q_z c_z}
+// are shared by the row, the mirror cell differs only in the sign of q_z.
+// Boxes arrive sorted by extent, so the per-column x * y factor and the z
+// factor are recomputed only when an extent changes (as the reference kernel
+// caches its x factor, PDBAmplitudeCUDA.cu:50-58); each box then costs one
+// sincos per row and one per column.  Boxes are staged THREADS / 2 at a time
+// (two float4 each) in the atom tile.
+__device__ __forceinline__ float sinc_f(float h) { return h == 0.f ? 1.f : __fdividef(__sinf(h), h); }
+
 template <int CPT, int THREADS>
+__device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, int n_boxes, const float (&qx)[CPT],
+                                            const float (&qy)[CPT], float qz, float (&fR)[CPT], float (&fI)[CPT],
+                                            float (&gR)[CPT], float (&gI)[CPT], float4* __restrict__ s_box) {
+    float fxy[CPT], fz = 0.f;
+    float lx = -1.f, ly = -1.f, lz = -1.f;
+    for (int b0 = 0; b0 < n_boxes; b0 += THREADS / 2) {
+        const int nb = min(THREADS / 2, n_boxes - b0);
+        __syncthreads();
+        if (threadIdx.x < 2 * nb) s_box[threadIdx.x] = boxes[2 * (int64_t)b0 + threadIdx.x];
+        __syncthreads();
+        for (int j = 0; j < nb; ++j) {
+            const float4 c = s_box[2 * j], L = s_box[2 * j + 1];
+            if (L.x != lx || L.y != ly) {
+                lx = L.x;
+                ly = L.y;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k)
+                    fxy[k] = L.x * sinc_f(0.5f * qx[k] * L.x) * L.y * sinc_f(0.5f * qy[k] * L.y);
+            }
+            if (L.z != lz) {
+                lz = L.z;
+                fz = L.z * sinc_f(0.5f * qz * L.z);
+            }
+            const float wz = c.w * fz;
+            float sz, cz;
+            __sincosf(qz * c.z, &sz, &cz);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) {
+                const float a = wz * fxy[k];
+                float sn, cs;
+                __sincosf(fmaf(qy[k], c.y, qx[k] * c.x), &sn, &cs);
+                const float ar = a * cs, ai = a * sn;
+                fR[k] = fmaf(-ai, sz, fmaf(ar, cz, fR[k]));
+                fI[k] = fmaf(ar, sz, fmaf(ai, cz, fI[k]));
+                gR[k] = fmaf(ai, sz, fmaf(ar, cz, gR[k]));
+                gI[k] = fmaf(-ar, sz, fmaf(ai, cz, gI[k]));
+            }
+        }
+    }
+}
+
+template <int CPT, int THREADS, bool BOXES>
 __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, const int* __restrict__ ion_off, int U,
                                           const float* __restrict__ aff, const int64_t* __restrict__ pref,
-                                          float4* __restrict__ grid, int64_t n_items, int Lp, double step, double cx,
-                                          double cy, double cz, int use_center, float scale, int64_t w,
-                                          float4* __restrict__ s_atoms) {
+                                          const float4* __restrict__ boxes, int n_boxes, float4* __restrict__ grid,
+                                          int64_t n_items, int Lp, double step, double cx, double cy, double cz,
+                                          int use_center, float scale, int64_t w, float4* __restrict__ s_atoms) {
     const bool active = w < n_items;
     Item it{0, 0, 0};
     if (active && w > 0) it = find_item(w, pref, Lp, CPT);
@@ -145,6 +198,7 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
             }
         }
     }
+    if (BOXES && n_boxes > 0) box_sum_f32<CPT, THREADS>(boxes, n_boxes, qx, qy, qz, fR, fI, gR, gI, s_atoms);
     if (!active) return;
 
     float2* g2 = reinterpret_cast<float2*>(grid);
@@ -180,10 +234,11 @@ __device__ __forceinline__ int job_of_tile(const FillJob* __restrict__ jobs, int
     return lo;
 }
 
-template <int CPT, int THREADS>
+template <int CPT, int THREADS, bool BOXES>
 __device__ __forceinline__ void run_tile(const FillJob& J, int64_t tile, float4* s_atoms) {
-    fill_tile<CPT, THREADS>(J.atoms, J.ion_off, J.U, J.aff_f32, J.pref, J.grid, J.n_items, J.Lp, J.step, J.cx, J.cy,
-                            J.cz, J.use_center, J.scale, (tile - J.tile_start) * THREADS + threadIdx.x, s_atoms);
+    fill_tile<CPT, THREADS, BOXES>(J.atoms, J.ion_off, J.U, J.aff_f32, J.pref, J.boxes, J.n_boxes, J.grid, J.n_items, J.Lp,
+                            J.step, J.cx, J.cy, J.cz, J.use_center, J.scale,
+                            (tile - J.tile_start) * THREADS + threadIdx.x, s_atoms);
 }
 
 // Persistent form: one CTA per resident slot, tiles of every job pulled from
@@ -206,18 +261,20 @@ __global__ void __launch_bounds__(THREADS) fill_f32_persistent(const FillJob* __
         const int64_t tile = s_tile;
         if (tile >= total_tiles) break;
         const FillJob J = s_job;
-        run_tile<CPT, THREADS>(J, tile, s_atoms);
+        run_tile<CPT, THREADS, false>(J, tile, s_atoms);
     }
 }
 
 // Flat form: one CTA per tile over the whole batch; the hardware block
-// scheduler hands out the tiles in order.
-template <int CPT, int THREADS>
-__global__ void __launch_bounds__(THREADS) fill_f32_flat(const FillJob* __restrict__ jobs, int n_jobs) {
+// scheduler hands out the tiles in order.  BOXES compiles the voxelized-solvent
+// sum in (a batch with boxes runs this form; without, the leaner code keeps
+// the atom loop's registers free).
+template <int CPT, int THREADS, bool BOXES>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS) fill_f32_flat(const FillJob* __restrict__ jobs, int n_jobs) {
     __shared__ float4 s_atoms[THREADS];
     const int64_t tile = blockIdx.x;
     const FillJob J = jobs[job_of_tile(jobs, n_jobs, tile)];
-    run_tile<CPT, THREADS>(J, tile, s_atoms);
+    run_tile<CPT, THREADS, BOXES>(J, tile, s_atoms);
 }
 
 // --------------------------------------------------------------------------
@@ -229,7 +286,8 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
                                                            const int* __restrict__ ion_off, int U,
                                                            const double* __restrict__ aff, int Lp, double step,
                                                            const int64_t* __restrict__ pref, double cx, double cy,
-                                                           double cz, double scale, double4_32a* __restrict__ grid) {
+                                                           double cz, double scale, const float4* __restrict__ boxes,
+                                                           int n_boxes, double4_32a* __restrict__ grid) {
     __shared__ double4_32a s_atoms[THREADS];
     const int64_t w = (int64_t)blockIdx.x * THREADS + threadIdx.x;
     const int64_t n_items = pref[Lp];
@@ -297,6 +355,55 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
             gI[k] += f * sGi[k];
         }
     }
+    // voxelized-solvent boxes in FP64 (box data are the reference's floats),
+    // extent factors cached across boxes sorted by extent
+    double fx[CPT], fy[CPT], fz = 0.0, lx = -1.0, ly = -1.0, lz = -1.0;
+    for (int b0 = 0; b0 < n_boxes; b0 += THREADS / 2) {
+        const int nb = min(THREADS / 2, n_boxes - b0);
+        __syncthreads();
+        if (threadIdx.x < 2 * nb) {
+            const float4 v = boxes[2 * (int64_t)b0 + threadIdx.x];
+            s_atoms[threadIdx.x] = make_double4_32a(v.x, v.y, v.z, v.w);
+        }
+        __syncthreads();
+        for (int j = 0; j < nb; ++j) {
+            const double4_32a c = s_atoms[2 * j], L = s_atoms[2 * j + 1];
+            if (L.x != lx) {
+                lx = L.x;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) {
+                    const double h = 0.5 * qx[k] * L.x;
+                    fx[k] = L.x * (h == 0.0 ? 1.0 : sin(h) / h);
+                }
+            }
+            if (L.y != ly) {
+                ly = L.y;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) {
+                    const double h = 0.5 * qy[k] * L.y;
+                    fy[k] = L.y * (h == 0.0 ? 1.0 : sin(h) / h);
+                }
+            }
+            if (L.z != lz) {
+                lz = L.z;
+                const double h = 0.5 * qz * L.z;
+                fz = L.z * (h == 0.0 ? 1.0 : sin(h) / h);
+            }
+            const double wz = c.w * fz;
+            double sz, cz;
+            sincos(qz * c.z, &sz, &cz);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) {
+                const double a = wz * fx[k] * fy[k];
+                double sn, cs;
+                sincos(qx[k] * c.x + qy[k] * c.y, &sn, &cs);
+                fR[k] += a * (cs * cz - sn * sz);
+                fI[k] += a * (sn * cz + cs * sz);
+                gR[k] += a * (cs * cz + sn * sz);
+                gI[k] += a * (sn * cz - cs * sz);
+            }
+        }
+    }
     if (!active) return;
 
     double2* g2 = reinterpret_cast<double2*>(grid);
@@ -326,10 +433,11 @@ inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + thre
 
 template <int CPT, int TH>
 cudaError_t launch_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
-                         unsigned long long* d_counter, bool persistent) {
-    if (!persistent) {
+                         unsigned long long* d_counter, bool persistent, bool boxes) {
+    if (!persistent || boxes) {
         if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-        fill_f32_flat<CPT, TH><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
+        if (boxes) fill_f32_flat<CPT, TH, true><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
+        else fill_f32_flat<CPT, TH, false><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
         return cudaGetLastError();
     }
     int dev = 0, sms = 0, per_sm = 0;
@@ -355,11 +463,12 @@ int64_t fill_items(const Geom& g, int cpt, int64_t* pref) {
 }
 
 cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
-                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent) {
+                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent,
+                                  bool boxes) {
     if (n_jobs <= 0 || total_tiles <= 0) return cudaSuccess;
 #define DPX_FILL_CASE(CPT, TH) \
     if (cells_per_thread == CPT && block == TH)     \
-        return launch_batch<CPT, TH>(s, d_jobs, n_jobs, total_tiles, d_counter, persistent);
+        return launch_batch<CPT, TH>(s, d_jobs, n_jobs, total_tiles, d_counter, persistent, boxes);
     DPX_FILL_CASE(2, 256) DPX_FILL_CASE(4, 128) DPX_FILL_CASE(4, 256) DPX_FILL_CASE(6, 128) DPX_FILL_CASE(6, 256)
     DPX_FILL_CASE(8, 128) DPX_FILL_CASE(8, 256)
 #undef DPX_FILL_CASE
@@ -368,10 +477,10 @@ cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_j
 
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
                             const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
-                            double scale, double4_32a* grid) {
+                            double scale, const float4* boxes, int n_boxes, double4_32a* grid) {
     if (n_items <= 0) return cudaSuccess;
     fill_f64_kernel<kFill64Cells, 128><<<blocks_for(n_items, 128), 128, 0, s>>>(
-        atoms, ion_off, U, aff, g.Lp, g.step, d_pref, center[0], center[1], center[2], scale, grid);
+        atoms, ion_off, U, aff, g.Lp, g.step, d_pref, center[0], center[1], center[2], scale, boxes, n_boxes, grid);
     return cudaGetLastError();
 }
 

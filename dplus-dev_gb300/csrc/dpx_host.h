@@ -102,6 +102,22 @@ int prepare_models(dpx_ctx ctx, int n_models, const dpx_grid* grids, const doubl
                    const int* n_copies, const double* copy_rot, const double* copy_tr, const double* sym_scale,
                    std::vector<dpx::ModelDev>& md, std::vector<char>& gstage);
 
+// Device tables of one leaf in a staging buffer (offsets from its start).
+struct LeafTables {
+    size_t atoms = SIZE_MAX;  // SIZE_MAX: the caller's device atoms
+    size_t off = 0, aff = 0, pref = 0, boxes = SIZE_MAX;
+    int64_t items = 0, n_boxes = 0;
+    double cen[3] = {0, 0, 0};
+};
+// Appends leaf d's tables for grid G (FP32 with cpt cells per item, or FP64).
+void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t);
+// The FP32 fill job of a staged leaf whose buffer sits at device address dbase.
+dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
+                      int64_t tile_start);
+// The FP64 fill launch of a staged leaf.
+cudaError_t launch_leaf_f64(cudaStream_t s, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase,
+                            const dpx::Geom& G, void* grid);
+
 // Bracket tables of one orientation average (IntegrateLayersTogether).
 struct Brackets {
     std::vector<int> layer, off{0}, qidx;

@@ -79,21 +79,25 @@ struct FillJob {
     const int* ion_off;     // [U + 1]
     const float* aff_f32;   // [U][Lp + 1]
     const int64_t* pref;    // [Lp + 1] item prefix
+    const float4* boxes;    // [2 n_boxes]: {cx, cy, cz, weight}, {Lx, Ly, Lz, 0} (centred, nm, e/nm^3)
     float4* grid;
     int64_t n_items;
     int64_t tile_start;
     double step;
     double cx, cy, cz;
     int U, Lp, use_center;
+    int n_boxes;
     float scale;
 };
 // One launch over every tile of every job: persistent (one CTA per resident
-// slot, atomic tile counter d_counter) or flat (one CTA per tile).
+// slot, atomic tile counter d_counter) or flat (one CTA per tile).  boxes: some
+// job carries voxelized-solvent boxes (always the flat form, box code compiled in).
 cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
-                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent);
+                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent,
+                                  bool boxes);
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
                             const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
-                            double scale, double4_32a* grid);
+                            double scale, const float4* boxes, int n_boxes, double4_32a* grid);
 
 // VEGAS (dpx_kernels.cu): points of one iteration of one bracket, then the
 // single-block reduction / bin refinement / running mean / convergence test.

@@ -57,6 +57,7 @@ struct LeafCopy {
     double sol_ed = 0, c1 = 1, scale = 1;
     bool has_center = false;
     double center[3] = {0, 0, 0};
+    std::vector<float> boxes;  // 8 per voxelized-solvent box
     uint64_t key = 0;  // content (or caller) key, before the grid parameters
 };
 
@@ -338,51 +339,28 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
     const int cpt32 = ctx->fill_cpt, threads = ctx->fill_threads;
     std::vector<char>& h = S->host;
     h.clear();
-    Upload U{h};
-    struct Off {
-        size_t atoms, off, aff, pref;
-        int64_t items;
-        double cen[3];
-    };
-    std::vector<Off> o(fresh.size());
-    std::vector<double> aff;
-    std::vector<float> affF;
-    std::vector<float4> at;
+    std::vector<dpx_pdb_desc> descs(fresh.size());
+    std::vector<LeafTables> lt(fresh.size());
     for (size_t j = 0; j < fresh.size(); ++j) {
         const GridEntry& g = *fresh[j];
         const LeafCopy& l = *g.src;
+        dpx_pdb_desc& d = descs[j];
+        d = dpx_pdb_desc{};
+        d.n_atoms = (int64_t)l.atoms.size() / 4;
+        d.atoms = l.atoms.data();
+        d.n_ions = l.n_ions;
+        d.atoms_per_ion = l.api.data();
+        d.coeffs = l.coeffs.data();
+        d.ion_rads = l.rads.data();
+        d.flags = l.flags;
+        d.solvent_ed = l.sol_ed;
+        d.c1 = l.c1;
+        d.scale = l.scale;
+        d.center = l.has_center ? l.center : nullptr;
+        d.n_boxes = (int64_t)l.boxes.size() / 8;
+        d.boxes = l.boxes.empty() ? nullptr : l.boxes.data();
         const bool fp32 = g.precision == DPX_FP32;
-        const int64_t n = (int64_t)l.atoms.size() / 4;
-        for (int k = 0; k < 3; ++k) o[j].cen[k] = 0.0;
-        if (l.has_center) {
-            for (int k = 0; k < 3; ++k) o[j].cen[k] = l.center[k];
-        } else if (fp32) {
-            double acc[3] = {0, 0, 0};
-            for (int64_t a = 0; a < n; ++a)
-                for (int k = 0; k < 3; ++k) acc[k] += l.atoms[4 * a + k];
-            for (int k = 0; k < 3; ++k) o[j].cen[k] = acc[k] / double(n);
-        }
-        if (!fp32) o[j].cen[0] = o[j].cen[1] = o[j].cen[2] = 0.0;
-        at.resize(n);
-        for (int64_t a = 0; a < n; ++a)
-            at[a] = make_float4((float)((double)l.atoms[4 * a] - o[j].cen[0]),
-                                (float)((double)l.atoms[4 * a + 1] - o[j].cen[1]),
-                                (float)((double)l.atoms[4 * a + 2] - o[j].cen[2]), 0.f);
-        o[j].atoms = U.put(at.data(), at.size() * sizeof(float4));
-        std::vector<int> off(l.n_ions + 1, 0);
-        for (int u = 0; u < l.n_ions; ++u) off[u + 1] = off[u] + l.api[u];
-        o[j].off = U.put(off.data(), off.size() * sizeof(int));
-        aff_table(l.n_ions, l.api.data(), l.coeffs.data(), l.rads.data(), l.flags, l.sol_ed, l.c1, g.G.Lp, g.G.step,
-                  aff);
-        if (fp32) {
-            affF.assign(aff.begin(), aff.end());
-            o[j].aff = U.put(affF.data(), affF.size() * sizeof(float));
-        } else {
-            o[j].aff = U.put(aff.data(), aff.size() * sizeof(double));
-        }
-        std::vector<int64_t> pref(g.G.Lp + 1);
-        o[j].items = dpx::fill_items(g.G, fp32 ? cpt32 : dpx::kFill64Cells, pref.data());
-        o[j].pref = U.put(pref.data(), pref.size() * sizeof(int64_t));
+        stage_leaf(h, d, g.G, fp32, fp32 ? cpt32 : dpx::kFill64Cells, lt[j]);
     }
     const size_t jobs_at = al16(h.size());
     const size_t n32 = std::count_if(fresh.begin(), fresh.end(), [](GridEntry* g) { return g->precision == DPX_FP32; });
@@ -390,35 +368,15 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
     const size_t counter_at = al16(h.size());
     h.resize(counter_at + 64, 0);
     // device: grids, then one staging block (freed in stream order after the launches)
-    for (GridEntry* g : fresh) {
-        DPX_CUDA(cudaMallocAsync(&g->cells, g->bytes, s));
-        DPX_CUDA(cudaMemsetAsync(g->cells, 0, g->bytes, s));
-    }
+    for (GridEntry* g : fresh) DPX_CUDA(cudaMallocAsync(&g->cells, g->bytes, s));
     char* d = nullptr;
     DPX_CUDA(cudaMallocAsync((void**)&d, h.size(), s));
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
     for (size_t j = 0; j < fresh.size(); ++j) {
-        const GridEntry& g = *fresh[j];
-        if (g.precision != DPX_FP32) continue;
-        dpx::FillJob J{};
-        J.atoms = reinterpret_cast<const float4*>(d + o[j].atoms);
-        J.ion_off = reinterpret_cast<const int*>(d + o[j].off);
-        J.aff_f32 = reinterpret_cast<const float*>(d + o[j].aff);
-        J.pref = reinterpret_cast<const int64_t*>(d + o[j].pref);
-        J.grid = reinterpret_cast<float4*>(g.cells);
-        J.n_items = o[j].items;
-        J.tile_start = tiles;
-        J.step = g.G.step;
-        J.cx = o[j].cen[0];
-        J.cy = o[j].cen[1];
-        J.cz = o[j].cen[2];
-        J.use_center = (J.cx != 0.0 || J.cy != 0.0 || J.cz != 0.0);
-        J.U = g.src->n_ions;
-        J.Lp = g.G.Lp;
-        J.scale = (float)g.src->scale;
-        jobs.push_back(J);
-        tiles += (o[j].items + threads - 1) / threads;
+        if (fresh[j]->precision != DPX_FP32) continue;
+        jobs.push_back(make_job(descs[j], lt[j], d, fresh[j]->G, fresh[j]->cells, tiles));
+        tiles += (lt[j].items + threads - 1) / threads;
     }
     if (!jobs.empty()) std::memcpy(h.data() + jobs_at, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
     size_t cap = 0;
@@ -427,22 +385,18 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
     std::memcpy(hp, h.data(), h.size());
     DPX_CUDA(cudaMemcpyAsync(d, hp, h.size(), cudaMemcpyHostToDevice, s));
     S->pinned.put(hp, s);
+    bool boxes = false;
+    for (const dpx::FillJob& J : jobs) boxes |= J.n_boxes > 0;
     cudaError_t e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(d + jobs_at), (int)jobs.size(),
                                                tiles, reinterpret_cast<unsigned long long*>(d + counter_at), cpt32,
-                                               threads, ctx->fill_persistent);
+                                               threads, ctx->fill_persistent, boxes);
     if (e != cudaSuccess) return cuda_fail(e, "fill launch");
     if (!jobs.empty()) dl.fill_launches++;
     for (size_t j = 0; j < fresh.size(); ++j) {
-        GridEntry& g = *fresh[j];
-        if (g.precision == DPX_FP64) {
-            e = dpx::launch_fill_f64(s, reinterpret_cast<const float4*>(d + o[j].atoms),
-                                     reinterpret_cast<const int*>(d + o[j].off), g.src->n_ions,
-                                     reinterpret_cast<const double*>(d + o[j].aff), g.G,
-                                     reinterpret_cast<const int64_t*>(d + o[j].pref), o[j].items, o[j].cen,
-                                     g.src->scale, reinterpret_cast<double4_32a*>(g.cells));
-            if (e != cudaSuccess) return cuda_fail(e, "fill launch");
-            dl.fill_launches++;
-        }
+        if (fresh[j]->precision != DPX_FP64) continue;
+        e = launch_leaf_f64(s, descs[j], lt[j], d, fresh[j]->G, fresh[j]->cells);
+        if (e != cudaSuccess) return cuda_fail(e, "fill launch");
+        dl.fill_launches++;
     }
     DPX_CUDA(cudaFreeAsync(d, s));
     for (GridEntry* g : fresh) {
@@ -674,6 +628,7 @@ int dpx_server_submit(dpx_server S, const dpx_request* q, uint64_t* ticket) {
         c.has_center = d.center != nullptr;
         if (d.center)
             for (int k = 0; k < 3; ++k) c.center[k] = d.center[k];
+        if (d.n_boxes > 0 && d.boxes) c.boxes.assign(d.boxes, d.boxes + 8 * d.n_boxes);
         uint64_t h = q->leaf_keys && q->leaf_keys[l] ? q->leaf_keys[l] : 0;
         if (!h) {  // content key
             h = 1469598103934665603ull;
@@ -684,6 +639,7 @@ int dpx_server_submit(dpx_server S, const dpx_request* q, uint64_t* ticket) {
             const double p[4] = {c.sol_ed, c.c1, c.scale, (double)c.flags};
             h = fnv(h, p, sizeof p);
             if (c.has_center) h = fnv(h, c.center, sizeof c.center);
+            h = fnv(h, c.boxes.data(), c.boxes.size() * sizeof(float));
         }
         c.key = h;
     }

@@ -17,7 +17,8 @@ INCLUDE_DIR = os.path.join(REPO_DIR, "include")
 BUILD_DIR = os.path.join(os.path.dirname(PKG_DIR), "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libdpx.so")
 
-SOURCES = ["dpx_fill.cu", "dpx_kernels.cu", "dpx_api.cpp", "dpx_batch.cpp", "dpx_server.cpp", "dpx_noalloc.cu"]
+SOURCES = ["dpx_fill.cu", "dpx_kernels.cu", "dpx_api.cpp", "dpx_batch.cpp", "dpx_server.cpp", "dpx_stage.cpp",
+           "dpx_voxel.cpp", "dpx_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -30,8 +31,10 @@ def nvcc() -> str:
 
 def _compile(src: str) -> str:
     obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+    # host code without floating-point contraction: the same results on x86 and Arm hosts
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-           "-I", INCLUDE_DIR, "-I", SRC_DIR, "-c", os.path.join(SRC_DIR, src), "-o", obj]
+           "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE_DIR, "-I", SRC_DIR, "-c", os.path.join(SRC_DIR, src),
+           "-o", obj]
     if src.endswith(".cu"):
         cmd[3:3] = ["-Xptxas", "-v"] if os.environ.get("DPX_PTXAS_VERBOSE") else []
     subprocess.run(cmd, check=True)
@@ -41,7 +44,7 @@ def _compile(src: str) -> str:
 def build_libdpx(force: bool = False) -> str:
     """Compile libdpx.so if any source is newer than the library."""
     srcs = [os.path.join(SRC_DIR, s) for s in SOURCES] + [
-        os.path.join(SRC_DIR, "dpx_internal.h"), os.path.join(INCLUDE_DIR, "dpx.h")]
+        os.path.join(SRC_DIR, "dpx_internal.h"), os.path.join(SRC_DIR, "dpx_host.h"), os.path.join(INCLUDE_DIR, "dpx.h")]
     if (not force and os.path.exists(LIB_PATH)
             and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs)):
         return LIB_PATH

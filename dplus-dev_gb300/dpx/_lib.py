@@ -39,7 +39,8 @@ class PdbDesc(C.Structure):
     """dpx_pdb_desc: one leaf of dpx_grid_fill_pdb_batch."""
     _fields_ = [("n_atoms", C.c_int64), ("atoms", _P), ("atoms_on_device", C.c_int), ("n_ions", C.c_int),
                 ("atoms_per_ion", _I), ("coeffs", _D), ("ion_rads", _D), ("flags", C.c_int),
-                ("solvent_ed", C.c_double), ("c1", C.c_double), ("scale", C.c_double), ("center", _D)]
+                ("solvent_ed", C.c_double), ("c1", C.c_double), ("scale", C.c_double), ("center", _D),
+                ("n_boxes", C.c_int64), ("boxes", _F)]
 
 class SolveDesc(C.Structure):
     """dpx_solve_desc: one solve of a dpx_batch."""
@@ -121,6 +122,12 @@ _SIGS = {
     "dpx_server_wait": (C.c_int, [_P, C.c_uint64, _D, _D]),
     "dpx_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "dpx_server_destroy": (C.c_int, [_P]),
+    "dpx_voxel_solvent": (C.c_int, [C.c_int64, _F, _F, C.c_double, C.c_double, C.c_double, C.c_int,
+                                    C.POINTER(_P)]),
+    "dpx_boxes_count": (C.c_int64, [_P, C.c_int]),
+    "dpx_boxes_get": (C.c_int, [_P, C.c_int, _F, _I]),
+    "dpx_boxes_space": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "dpx_boxes_free": (C.c_int, [_P]),
     "dpx_mc_average_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, _D, _P, C.c_int64, C.c_double,
                                          _P, _P]),
 }

@@ -177,12 +177,69 @@ class PDBAmplitude:
             flags |= _lib.DPX_CALC_ATOMIC_FORMFACTORS
         if self.radType == RAD_DUMMY_ATOMS_ONLY and self.solventED != 0.0:
             flags |= _lib.DPX_CALC_DUMMY_SOLVENT
-        voxel = ((self.solventED != 0.0 and self.radType in (RAD_CALC, RAD_EMP, RAD_DUMMY_ATOMS_RADII, RAD_VDW))
-                 or (self.outerSolventED != 0.0 and self.radType in (RAD_CALC, RAD_EMP, RAD_DUMMY_ATOMS_RADII,
-                                                                      RAD_VDW, RAD_DUMMY_ATOMS_ONLY)))
-        if voxel:
-            raise NotImplementedError("voxelized solvent / solvation layer is not available in this build")
+        # voxelized solvent (PDBAmplitude.cpp:1248-1256): excluded-volume boxes
+        # for the radius-table types, solvation-layer boxes when outerSolventED != 0
+        self.voxel_excluded = self.solventED != 0.0 and self.radType in (RAD_CALC, RAD_EMP, RAD_DUMMY_ATOMS_RADII,
+                                                                          RAD_VDW)
+        self.voxel_layer = self.outerSolventED != 0.0 and self.radType in (RAD_CALC, RAD_EMP, RAD_DUMMY_ATOMS_RADII,
+                                                                            RAD_VDW, RAD_DUMMY_ATOMS_ONLY)
+        if (self.voxel_excluded or self.voxel_layer) and self.radType not in (RAD_DUMMY_ATOMS_ONLY,
+                                                                             RAD_DUMMY_ATOMS_RADII):
+            raise NotImplementedError("voxelized solvent needs the dummy-atom radius table (radius types 4, 5); "
+                                      "the van der Waals / empirical / calculated tables are not carried")
         self.flags = flags
+        self._boxes_key = None
+        self._boxes = None
+
+    def atom_radii(self) -> np.ndarray:
+        """Per-atom radius (nm) of the leaf's radius type (svgRad for types 4, 5)."""
+        return np.array([ion(sym).dummy_radius for sym in self.symbols], dtype=np.float32)
+
+    def voxel_boxes(self):
+        """dpx_voxel_solvent on the leaf's atoms: (excluded com, excluded dims,
+        layer com, layer dims), centres in nm, extents in voxels."""
+        xyz = np.ascontiguousarray(self.xyz, dtype=np.float32)
+        rad = self.atom_radii()
+        h = C.c_void_p()
+        check(lib().dpx_voxel_solvent(len(xyz), xyz.ctypes.data_as(C.POINTER(C.c_float)),
+                                      rad.ctypes.data_as(C.POINTER(C.c_float)), self.voxelStep, self.solventRad,
+                                      self.solvationThickness, int(self.fillHoles), C.byref(h)))
+        out = []
+        try:
+            for which in (0, 1):
+                n = lib().dpx_boxes_count(h, which)
+                com = np.zeros((n, 3), dtype=np.float32)
+                dims = np.zeros((n, 3), dtype=np.int32)
+                if n:
+                    check(lib().dpx_boxes_get(h, which, com.ctypes.data_as(C.POINTER(C.c_float)), iptr(dims)))
+                out += [com, dims]
+        finally:
+            lib().dpx_boxes_free(h)
+        return tuple(out)
+
+    def solvent_boxes(self):
+        """[n, 8] float32 {cx, cy, cz, weight, Lx, Ly, Lz, 0} of the voxelized
+        solvent (PDBAmplitude.cpp:277-314): excluded volume at -solventED,
+        solvation layer at outerSolventED - solventED; None without voxels."""
+        if not (self.voxel_excluded or self.voxel_layer):
+            return None
+        key = (self.voxelStep, self.solventRad, self.solvationThickness, self.fillHoles, self.radType,
+               self.solventED, self.outerSolventED, self.voxel_excluded, self.voxel_layer)
+        if self._boxes_key != key:
+            ec, ed, lc, ld = self.voxel_boxes()
+            step = np.float32(self.voxelStep)
+            parts = []
+            for on, com, dims, w in ((self.voxel_excluded, ec, ed, -self.solventED),
+                                     (self.voxel_layer, lc, ld, self.outerSolventED - self.solventED)):
+                if on and len(com):
+                    b = np.zeros((len(com), 8), dtype=np.float32)
+                    b[:, :3] = com
+                    b[:, 3] = np.float32(w)
+                    b[:, 4:7] = step * dims.astype(np.float32)
+                    parts.append(b)
+            self._boxes = np.ascontiguousarray(np.concatenate(parts)) if parts else None
+            self._boxes_key = key
+        return self._boxes
 
     def atoms_float4(self) -> np.ndarray:
         a = np.zeros((len(self.xyz), 4), dtype=np.float32)
@@ -193,7 +250,9 @@ class PDBAmplitude:
         h = hashlib.sha1()
         for arr in (self.xyz, self.coeffs, self.ion_rads, self.atoms_per_ion):
             h.update(np.ascontiguousarray(arr).tobytes())
-        h.update(repr((self.scale, self.solventED, self.c1, self.flags)).encode())
+        h.update(repr((self.scale, self.solventED, self.c1, self.flags, self.voxel_excluded, self.voxel_layer,
+                       self.voxelStep, self.solventRad, self.solvationThickness, self.outerSolventED,
+                       self.fillHoles)).encode())
         return h.hexdigest()
 
     def _key(self, ctx: Context, qmax: float, gridSize: int, precision: int):
@@ -214,6 +273,10 @@ def pdb_descs(leaves: Sequence[PDBAmplitude]):
         d.n_atoms, d.atoms, d.atoms_on_device, d.n_ions = len(at), at.ctypes.data, 0, len(a.unique)
         d.atoms_per_ion, d.coeffs, d.ion_rads = iptr(a.atoms_per_ion), dptr(a.coeffs), dptr(a.ion_rads)
         d.flags, d.solvent_ed, d.c1, d.scale, d.center = a.flags, a.solventED, a.c1, a.scale, None
+        boxes = a.solvent_boxes()
+        if boxes is not None:
+            keep.append(boxes)
+            d.n_boxes, d.boxes = len(boxes), boxes.ctypes.data_as(C.POINTER(C.c_float))
     return descs, keep
 
 

@@ -119,6 +119,13 @@ typedef struct dpx_pdb_desc {
     double c1;
     double scale;
     const double* center;
+    /* voxelized solvent (dpx_voxel_solvent), 0 / NULL for none: n_boxes
+     * records of 8 floats {cx, cy, cz, weight (e/nm^3), Lx, Ly, Lz, 0} in nm,
+     * in the frame of the host atoms; each adds
+     * weight * prod_a [L_a sinc(q_a L_a / 2)] e^{i q.c} (PDBAmplitude.cpp:277-314)
+     * before the scale. */
+    int64_t n_boxes;
+    const float* boxes;
 } dpx_pdb_desc;
 /* Fills n grids (distinct, one context) from n leaves.  The FP32 grids of the
  * batch share ONE persistent launch that pulls tiles of every leaf from a
@@ -248,6 +255,24 @@ int dpx_calc_spc_fill_sym_jacob_sphr(int64_t voxels, int thDivs, int phDivs, dou
 int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* const* inAmpData,
                              const double* const* inD, const double* trans, const double* rots, int numGrids,
                              double* outAmpData, int precision, int* pStop);
+
+/* ---- voxelized solvent (PDBAmplitude::FindPDBRanges PDBAmplitude.cpp:710-749,
+ * CalculateSolventSpace VoxelizedSolvent.cpp:4-190) ----
+ * Voxelizes the space around n_atoms atoms (xyz: 3 floats per atom, nm;
+ * radii: per atom, nm — the radius table of the leaf's radius type) with
+ * voxel_step, marks the excluded volume, a probe shell (probe_radius) and the
+ * solvation layer (solvation_thickness), optionally fills enclosed cavities,
+ * and reduces both regions to boxes in the reference's greedy scan order.
+ * Box set 0 = excluded volume, 1 = solvation layer: centres (3 floats, nm)
+ * and extents in voxels (3 ints).  Host computation. */
+typedef struct dpx_boxes_s* dpx_boxes;
+int dpx_voxel_solvent(int64_t n_atoms, const float* xyz, const float* radii, double voxel_step, double probe_radius,
+                      double solvation_thickness, int fill_holes, dpx_boxes* out);
+int64_t dpx_boxes_count(dpx_boxes b, int which);
+int dpx_boxes_get(dpx_boxes b, int which, float* com, int* dims);
+/* dims[3] = the voxel space (x, y, z padded to a multiple of 16) */
+int dpx_boxes_space(dpx_boxes b, int64_t* dims);
+int dpx_boxes_free(dpx_boxes b);
 
 /* ---- batched independent solves (no counterpart in the reference, which
  * solves one structure per call) ----

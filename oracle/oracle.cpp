@@ -607,6 +607,69 @@ void orc_grid_fill(int grid_size, double qmax, int64_t N, const double* xyz, int
                          scale, mode, nthreads, 0, g.Lp, data);
 }
 
+/* Voxelized-solvent boxes added to every cell (PDBAmplitude.cpp:277-314):
+ *   data += scale * sum_b w_b prod_a [L_a sinc(q_a L_a / 2)] e^{i q.c_b}
+ * boxes: 8 floats per box {cx, cy, cz, w, Lx, Ly, Lz, 0}.  FP64 mode promotes
+ * the box floats to double; reference-exact mode evaluates in float as the
+ * reference's Eigen float arrays do (sinc = sin(x)/x, 1 where that is NaN). */
+void orc_grid_add_boxes_shells(int grid_size, double qmax, int64_t n_boxes, const float* boxes, double scale,
+                               int mode, int nthreads, int shell_lo, int shell_hi, double* data) {
+    Geom g = make_geom(grid_size, qmax);
+    int64_t lo = (shell_lo <= 0) ? 0 : shell_base(shell_lo);
+    int64_t hi = shell_base(int64_t(shell_hi) + 1); /* exclusive */
+    if (hi > g.P) hi = g.P;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t ind = lo; ind < hi; ind++) {
+        int qi; int64_t ti, pi;
+        orc_indices_from_index(ind, &qi, &ti, &pi);
+        double qx, qy, qz;
+        cell_qvec(g, qi, ti, pi, qx, qy, qz);
+        double re = 0, im = 0;
+        if (mode == ORC_REFEXACT) {
+            const float q[3] = {float(qx), float(qy), float(qz)};
+            float fr = 0.f, fi = 0.f;
+            for (int64_t b = 0; b < n_boxes; b++) {
+                const float* B = boxes + 8 * b;
+                float va = 1.f, ph = 0.f;
+                for (int a = 0; a < 3; a++) {
+                    const float x = B[4 + a] * (0.5f * q[a]);
+                    float sc = std::sin(x) / x;
+                    if (sc != sc) sc = 1.f;
+                    va *= sc * B[4 + a];
+                    ph += B[a] * q[a];
+                }
+                va *= B[3];
+                fr += va * std::cos(ph);
+                fi += va * std::sin(ph);
+            }
+            re = fr;
+            im = fi;
+        } else {
+            const double q[3] = {qx, qy, qz};
+            for (int64_t b = 0; b < n_boxes; b++) {
+                const float* B = boxes + 8 * b;
+                double va = B[3], ph = 0;
+                for (int a = 0; a < 3; a++) {
+                    const double L = B[4 + a], x = 0.5 * q[a] * L;
+                    va *= L * (x == 0.0 ? 1.0 : std::sin(x) / x);
+                    ph += q[a] * double(B[a]);
+                }
+                re += va * std::cos(ph);
+                im += va * std::sin(ph);
+            }
+        }
+        data[2 * ind] += scale * re;
+        data[2 * ind + 1] += scale * im;
+    }
+}
+
+void orc_grid_add_boxes(int grid_size, double qmax, int64_t n_boxes, const float* boxes, double scale, int mode,
+                        int nthreads, double* data) {
+    Geom g = make_geom(grid_size, qmax);
+    orc_grid_add_boxes_shells(grid_size, qmax, n_boxes, boxes, scale, mode, nthreads, 0, g.Lp, data);
+}
+
 void orc_grid_splines(int grid_size, const double* data, double* coeffs, int mode, int nthreads) {
     Geom g = make_geom(grid_size, 1.0);
     coeffs[0] = coeffs[1] = 0.0;

@@ -59,6 +59,13 @@ void orc_grid_fill_shells(int grid_size, double qmax, int64_t N, const double* x
                           double* data);
 
 /* ---- periodic phi splines (Grid.cpp:1113-1151, PeriodicSplineSolver.h:7-67) ---- */
+/* Voxelized-solvent boxes {cx, cy, cz, w, Lx, Ly, Lz, 0} added to every cell
+ * (PDBAmplitude.cpp:277-314), times scale. */
+void orc_grid_add_boxes(int grid_size, double qmax, int64_t n_boxes, const float* boxes, double scale, int mode,
+                        int nthreads, double* data);
+/* The same over shells [shell_lo, shell_hi] only. */
+void orc_grid_add_boxes_shells(int grid_size, double qmax, int64_t n_boxes, const float* boxes, double scale,
+                               int mode, int nthreads, int shell_lo, int shell_hi, double* data);
 void orc_grid_splines(int grid_size, const double* data, double* coeffs, int mode, int nthreads);
 
 /* ---- interpolation (Grid.cpp:61-134, 487-607, 677-721) ----

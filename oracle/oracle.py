@@ -58,6 +58,9 @@ def lib():
                                            C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                            _D]
         L.orc_grid_splines.argtypes = [C.c_int, _D, _D, C.c_int, C.c_int]
+        L.orc_grid_add_boxes.argtypes = [C.c_int, C.c_double, C.c_int64, _F, C.c_double, C.c_int, C.c_int, _D]
+        L.orc_grid_add_boxes_shells.argtypes = [C.c_int, C.c_double, C.c_int64, _F, C.c_double, C.c_int, C.c_int,
+                                                C.c_int, C.c_int, _D]
         L.orc_grid_amplitudes_at_points.argtypes = [C.c_int, C.c_double, _D, _D, C.c_int, _D, C.c_double,
                                                     C.c_double, _D]
         L.orc_mc_directions.argtypes = [C.c_uint32, C.c_int64, _D]
@@ -99,17 +102,20 @@ def ref():
 class Struct:
     """Oracle-side view of a PDB leaf (atoms sorted by ion)."""
 
-    def __init__(self, xyz, atoms_per_ion, coeffs, ion_rads, flags, sol_ed=0.0, c1=1.0, scale=1.0):
+    def __init__(self, xyz, atoms_per_ion, coeffs, ion_rads, flags, sol_ed=0.0, c1=1.0, scale=1.0, boxes=None):
         self.xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         self.api = np.ascontiguousarray(atoms_per_ion, dtype=np.int32)
         self.coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
         self.rads = np.ascontiguousarray(ion_rads, dtype=np.float64)
         self.flags, self.sol_ed, self.c1, self.scale = int(flags), float(sol_ed), float(c1), float(scale)
+        # voxelized-solvent boxes: [n, 8] float32 {cx, cy, cz, w, Lx, Ly, Lz, 0}
+        self.boxes = None if boxes is None or len(boxes) == 0 else \
+            np.ascontiguousarray(boxes, dtype=np.float32).reshape(-1, 8)
 
     @classmethod
     def from_pdb(cls, amp):
         return cls(amp.xyz, amp.atoms_per_ion, amp.coeffs, amp.ion_rads, amp.flags, amp.solventED, amp.c1,
-                   amp.scale)
+                   amp.scale, getattr(amp, "solvent_boxes", lambda: None)())
 
 
 def grid_cells(grid_size):
@@ -120,6 +126,9 @@ def grid_fill(s: Struct, grid_size, qmax, mode=FP64, nthreads=0):
     out = np.zeros(2 * grid_cells(grid_size))
     lib().orc_grid_fill(grid_size, qmax, len(s.xyz), _d(s.xyz), len(s.api), s.api.ctypes.data_as(_I), _d(s.coeffs),
                         _d(s.rads), s.flags, s.sol_ed, s.c1, s.scale, mode, nthreads, out.ctypes.data_as(_D))
+    if s.boxes is not None:
+        lib().orc_grid_add_boxes(grid_size, qmax, len(s.boxes), s.boxes.ctypes.data_as(_F), s.scale, mode, nthreads,
+                                 out.ctypes.data_as(_D))
     return out
 
 
@@ -129,6 +138,9 @@ def grid_fill_shells(s: Struct, grid_size, qmax, lo, hi, mode=FP64, nthreads=0, 
     lib().orc_grid_fill_shells(grid_size, qmax, len(s.xyz), _d(s.xyz), len(s.api), s.api.ctypes.data_as(_I),
                                _d(s.coeffs), _d(s.rads), s.flags, s.sol_ed, s.c1, s.scale, mode, nthreads, lo, hi,
                                out.ctypes.data_as(_D))
+    if s.boxes is not None:
+        lib().orc_grid_add_boxes_shells(grid_size, qmax, len(s.boxes), s.boxes.ctypes.data_as(_F), s.scale, mode,
+                                        nthreads, lo, hi, out.ctypes.data_as(_D))
     return out
 
 

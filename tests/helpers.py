@@ -6,6 +6,10 @@ from dpx import models as M
 
 SOLVENT = [1, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 4]
 VACUUM = [1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0]
+# dummy-atom solvent plus a 0.3 nm voxelized solvation layer at 400 e/nm^3
+LAYER = [1, 333, 1, 0.05, 0.14, 0.3, 400, 0, 0, 4]
+# radius-table solvent (type 5): excluded-volume boxes and the layer, cavities filled
+BOXES5 = [1, 334, 1, 0.05, 0.14, 0.28, 364, 1, 0, 5]
 
 
 def globule(n, radius, seed, extra=SOLVENT, centered=False):

@@ -84,8 +84,9 @@ def test_bad_arguments_are_rejected():
     out = np.zeros(4, dtype=np.int32)
     assert dpx.lib().dpx_q_brackets(1, 1.0, 4, None, _lib.iptr(out)) == -1
     assert dpx.lib().dpx_make_globule(0, 1.0, 1, None, None) == -1
-    with pytest.raises(NotImplementedError):
-        M.PDBAmplitude(["C"], [[0, 0, 0]], [1, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 5])  # voxel solvent
+    with pytest.raises(NotImplementedError):  # voxel solvent with the van der Waals radius table
+        M.PDBAmplitude(["C"], [[0, 0, 0]], [1, 333, 1, 0.05, 0.14, 0.28, 0, 0, 0, 1])
+    assert dpx.lib().dpx_voxel_solvent(0, None, None, 0.05, 0.14, 0.28, 0, None) == -1
 
 
 def test_pdb_amplitude_mirrors_precalculate():

@@ -15,7 +15,7 @@ import oracle as O
 import dpx
 from dpx import _lib
 from dpx import models as M
-from helpers import SOLVENT, VACUUM, globule, oracle_grid, rel, rel_to_max
+from helpers import BOXES5, LAYER, SOLVENT, VACUUM, globule, oracle_grid, rel, rel_to_max
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -511,7 +511,8 @@ def _batch_case(seed0=80):
     leaves, gss, qms, Qs = [], [], [], []
     for k in range(5):
         n = int(rng.integers(60, 900))
-        leaves.append(globule(n, 0.5 + 0.02 * n ** (1 / 3) * 3, seed=seed0 + k, extra=SOLVENT if k % 2 else VACUUM))
+        extra = LAYER if k == 3 else (SOLVENT if k % 2 else VACUUM)
+        leaves.append(globule(n, 0.5 + 0.02 * n ** (1 / 3) * 3, seed=seed0 + k, extra=extra))
         gss.append(int(rng.integers(6, 16)) * 2)
         qms.append(float(rng.uniform(2.0, 6.0)))
         lo = 0.0 if k % 2 == 0 else 0.3
@@ -542,3 +543,35 @@ def test_solve_batch_equals_single_solves(ctx, prec):
         data, co = oracle_grid(leaves[0], gss[0], qms[0])
         ref = O.integrate_layers(gss[0], qms[0], [O.make_leaf(data, co)], Qs[0], dirs, 0, len(dirs), 0.0)
         assert rel(singles[0], ref) <= TOL64
+
+
+@pytest.mark.parametrize("extra", [LAYER, BOXES5])
+@pytest.mark.parametrize("prec,tol", [(M.FP64, TOL64), (M.FP32, 2e-5)])
+def test_grid_fill_voxel_solvent_matches_oracle(ctx, extra, prec, tol):
+    """Atoms plus voxelized-solvent boxes (solvation layer; excluded volume for
+    radius type 5), fused into the fill, against the oracle's FP64 box sum.
+    FP32 bound on the amplitude scale: the box terms use the SFU sine and
+    divide; the I(q) bar (1e-4) is checked in the next test."""
+    amp = globule(250, 1.1, seed=91, extra=extra)
+    assert amp.solvent_boxes() is not None and len(amp.solvent_boxes()) > 100
+    gs, qmax = 24, 5.0
+    g = amp.calculateGrid(ctx, qmax, gs, prec)
+    v, _ = g.read(True, False)
+    ref = O.grid_fill(O.Struct.from_pdb(amp), gs, qmax, O.FP64)
+    assert rel_to_max(v, ref) <= tol
+
+
+def test_intensity_with_solvation_layer(ctx):
+    """I(q) of a leaf with the voxelized layer: FP32 bulk within 1e-4 of the
+    FP64 oracle, and the layer changes I(q) by far more than that."""
+    amp = globule(300, 1.2, seed=92, extra=LAYER)
+    bare = globule(300, 1.2, seed=92, extra=SOLVENT)
+    gs, qmax = 30, 4.0
+    Q = np.linspace(0.05, 4.0, 60)
+    dirs = M.mc_directions(93, 500)
+    I = M.DomainModel([amp], gs, qmax, M.FP32).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    I0 = M.DomainModel([bare], gs, qmax, M.FP32).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    data, co = oracle_grid(amp, gs, qmax)
+    ref = O.integrate_layers(gs, qmax, [O.make_leaf(data, co)], Q, dirs, 0, len(dirs), 0.0)
+    assert rel(I, ref) <= TOL32
+    assert rel(I, I0) > 1e-3

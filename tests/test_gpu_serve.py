@@ -6,7 +6,7 @@ import pytest
 
 from dpx import models as M
 from dpx.serve import Server
-from helpers import SOLVENT, VACUUM, globule
+from helpers import LAYER, SOLVENT, VACUUM, globule
 
 pytestmark = pytest.mark.gpu
 
@@ -15,7 +15,7 @@ def _mix():
     """(amps, grid_size, qmax, Q, precision) per request; leaves shared by repeats."""
     a = globule(500, 1.5, seed=101, extra=SOLVENT)
     b = globule(300, 1.2, seed=102, extra=VACUUM)
-    c = globule(800, 1.9, seed=103, extra=SOLVENT)
+    c = globule(800, 1.9, seed=103, extra=LAYER)
     d = globule(200, 1.0, seed=104, extra=VACUUM)
     b2 = globule(300, 1.2, seed=102, extra=VACUUM)  # same content as b: same cache key
     b2.location = (0.4, -0.2, 0.1, 0.3, 0.2, 0.1)
