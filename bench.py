@@ -151,6 +151,9 @@ def run_dpx(args):
         ctx.set_fill_schedule(spec.endswith("p"))
 
     amp, Q, dirs = build_inputs()
+    sfu_c = C.c_double()
+    _lib.check(L.dpx_measure_sfu_peak(ctx.handle, C.byref(sfu_c)))
+    sfu_measured = sfu_c.value
     tune = None
     if args.autotune:  # sweep every fill shape on this workload's leaf, keep the fastest
         best, table = M.autotune_fill(ctx, [amp], QMAX, GRID_SIZE, repeats=1)
@@ -268,8 +271,10 @@ def run_dpx(args):
         # (solvent boxes cost the same per work item: their extent factors are cached)
         items = 1 + sum((3 * i // 2 + 1) * ((3 * i + cpt - 1) // cpt) for i in range(1, lp + 1))
         sfu_ops = float(N_ATOMS + n_boxes) * items * 2 * (1 + cpt)
-        # SFU roofline: 16 MUFU lanes/SM/clk x 152 SMs at the maximum SM clock
-        sfu_peak = 152 * 16 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12  # Tops/s
+        # SFU roofline: the MUFU throughput this GPU sustains on a calibration
+        # kernel of independent sincos chains (measured here, with the clocks above)
+        sfu_peak = sfu_measured / 1e12  # Tops/s
+        sfu_nominal = 152 * 16 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
         achieved = sfu_ops / (fill_ms / 1e3) / 1e12
         n_brackets = GRID_SIZE // 2
         interp_bytes = float(N_DIRS) * n_brackets * (4 * 4 * 2 * 16)  # 4 planes x 4 rows x 2 nodes x 16 B
@@ -284,15 +289,16 @@ def run_dpx(args):
                     "note": "voxelization (host, once per structure) excluded: voxelize_s"},
             "voxelize_s": voxelize_s, "solvent_boxes": n_boxes,
             "gpu_launches": args.steps * 4,
-            "roofline": {"bound": "sfu", "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] else "flat"),
+            "roofline": {"bound": "sfu",
+                         "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] and not n_boxes else "flat"),
                          "fill_shape": "%dx%d%s" % (ctx.fill_shape()[0], ctx.fill_shape()[1],
                                                     "p" if ctx.fill_shape()[2] else ""),
                          "achieved": achieved, "peak": sfu_peak,
                          "unit": "T SFU-op/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
+                         "peak_kind": "measured (sincos calibration kernel, dpx_measure_sfu_peak)",
+                         "peak_nominal_16_per_sm_clk": sfu_nominal,
                          "note": "SFU ops = (atoms + solvent boxes) x work items x 2(1+CPT) (row-factored fill); "
-                                 "peak = 152 SM x 16 "
-                                 "MUFU/clk at sm_max_mhz (derived, not in MEASURED_PEAKS.json); traffic = ncu "
-                                 "dram bytes of the profile shape scaled by cells",
+                                 "traffic = ncu dram bytes of the profile shape scaled by cells",
                          "algorithmic_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)},
             "roofline_average": {"bound": "hbm", "kernel": "average_kernel",
                                  "achieved": interp_bytes / (avg_ms / 1e3) / 1e9, "peak": peaks["hbm_gbs"],

@@ -85,12 +85,20 @@ __device__ __forceinline__ void store_quad(V2* __restrict__ g2, int i, int t, in
 // caches its x factor, PDBAmplitudeCUDA.cu:50-58); each box then costs one
 // sincos per row and one per column.  Boxes are staged THREADS / 2 at a time
 // (two float4 each) in the atom tile.
-__device__ __forceinline__ float sinc_f(float h) { return h == 0.f ? 1.f : __fdividef(__sinf(h), h); }
+// sin(h)/h.  The SFU sine has an absolute error near 1e-7-1e-6, which is a
+// large RELATIVE error of sin(h)/h for small h (low q, where every box adds in
+// phase): below |h| = 0.5 the Taylor series 1 - h^2/6 + h^4/120 - h^6/5040
+// (truncation < 1.1e-8) is used instead.
+__device__ __forceinline__ float sinc_f(float h) {
+    const float h2 = h * h;
+    if (h2 < 0.25f) return fmaf(h2, fmaf(h2, fmaf(h2, -1.f / 5040.f, 1.f / 120.f), -1.f / 6.f), 1.f);
+    return __fdividef(__sinf(h), h);
+}
 
 template <int CPT, int THREADS>
 __device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, int n_boxes, const float (&qx)[CPT],
-                                            const float (&qy)[CPT], float qz, float (&fR)[CPT], float (&fI)[CPT],
-                                            float (&gR)[CPT], float (&gI)[CPT], float4* __restrict__ s_box) {
+                                            const float (&qy)[CPT], float qz, float (&cc)[CPT], float (&ss)[CPT],
+                                            float (&sc)[CPT], float (&cs)[CPT], float4* __restrict__ s_box) {
     float fxy[CPT], fz = 0.f;
     float lx = -1.f, ly = -1.f, lz = -1.f;
     for (int b0 = 0; b0 < n_boxes; b0 += THREADS / 2) {
@@ -98,6 +106,11 @@ __device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, in
         __syncthreads();
         if (threadIdx.x < 2 * nb) s_box[threadIdx.x] = boxes[2 * (int64_t)b0 + threadIdx.x];
         __syncthreads();
+        // per-tile partial sums: near q = 0 every box adds in phase, and adding
+        // each small term straight to the running sum would round 1e5 times
+        float tcc[CPT], tss[CPT], tsc[CPT], tcs[CPT];
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) tcc[k] = tss[k] = tsc[k] = tcs[k] = 0.f;
         for (int j = 0; j < nb; ++j) {
             const float4 c = s_box[2 * j], L = s_box[2 * j + 1];
             if (L.x != lx || L.y != ly) {
@@ -111,20 +124,26 @@ __device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, in
                 lz = L.z;
                 fz = L.z * sinc_f(0.5f * qz * L.z);
             }
-            const float wz = c.w * fz;
             float sz, cz;
             __sincosf(qz * c.z, &sz, &cz);
+            const float wz = c.w * fz, wcz = wz * cz, wsz = wz * sz;
 #pragma unroll
             for (int k = 0; k < CPT; ++k) {
-                const float a = wz * fxy[k];
-                float sn, cs;
-                __sincosf(fmaf(qy[k], c.y, qx[k] * c.x), &sn, &cs);
-                const float ar = a * cs, ai = a * sn;
-                fR[k] = fmaf(-ai, sz, fmaf(ar, cz, fR[k]));
-                fI[k] = fmaf(ar, sz, fmaf(ai, cz, fI[k]));
-                gR[k] = fmaf(ai, sz, fmaf(ar, cz, gR[k]));
-                gI[k] = fmaf(-ar, sz, fmaf(ai, cz, gI[k]));
+                float sn, cn;
+                __sincosf(fmaf(qy[k], c.y, qx[k] * c.x), &sn, &cn);
+                const float tc = fxy[k] * cn, ts = fxy[k] * sn;
+                tcc[k] = fmaf(tc, wcz, tcc[k]);
+                tss[k] = fmaf(ts, wsz, tss[k]);
+                tsc[k] = fmaf(ts, wcz, tsc[k]);
+                tcs[k] = fmaf(tc, wsz, tcs[k]);
             }
+        }
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            cc[k] += tcc[k];
+            ss[k] += tss[k];
+            sc[k] += tsc[k];
+            cs[k] += tcs[k];
         }
     }
 }
@@ -134,7 +153,8 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
                                           const float* __restrict__ aff, const int64_t* __restrict__ pref,
                                           const float4* __restrict__ boxes, int n_boxes, float4* __restrict__ grid,
                                           int64_t n_items, int Lp, double step, double cx, double cy, double cz,
-                                          int use_center, float scale, int64_t w, float4* __restrict__ s_atoms) {
+                                          int use_center, float scale, double origin, int64_t w,
+                                          float4* __restrict__ s_atoms) {
     const bool active = w < n_items;
     Item it{0, 0, 0};
     if (active && w > 0) it = find_item(w, pref, Lp, CPT);
@@ -158,9 +178,14 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
         for (int k = 0; k < CPT; ++k) qx[k] = qy[k] = 0.f;
     }
 
-    float fR[CPT], fI[CPT], gR[CPT], gI[CPT];
+    // Four product sums per column instead of two complex accumulators:
+    //   cc = sum f c cz, ss = sum f s sz, sc = sum f s cz, cs = sum f c sz
+    // with (c, s) = e^{i Pxy}, (cz, sz) = e^{i Pz}; then
+    //   F = (cc - ss) + i (sc + cs),  G = (cc + ss) + i (sc - cs),
+    // four FMAs per atom and column where the complex products take eight.
+    float cc[CPT], ss[CPT], sc[CPT], cs[CPT];
 #pragma unroll
-    for (int k = 0; k < CPT; ++k) fR[k] = fI[k] = gR[k] = gI[k] = 0.f;
+    for (int k = 0; k < CPT; ++k) cc[k] = ss[k] = sc[k] = cs[k] = 0.f;
 
     for (int u = 0; u < U; ++u) {
         const int a0 = ion_off[u], a1 = ion_off[u + 1];
@@ -170,9 +195,9 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
             __syncthreads();
             if (threadIdx.x < n) s_atoms[threadIdx.x] = atoms[t0 + threadIdx.x];
             __syncthreads();
-            float tFr[CPT], tFi[CPT], tGr[CPT], tGi[CPT];
+            float tcc[CPT], tss[CPT], tsc[CPT], tcs[CPT];
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) tFr[k] = tFi[k] = tGr[k] = tGi[k] = 0.f;
+            for (int k = 0; k < CPT; ++k) tcc[k] = tss[k] = tsc[k] = tcs[k] = 0.f;
 #pragma unroll 2
             for (int j = 0; j < n; ++j) {
                 const float4 a = s_atoms[j];
@@ -180,30 +205,38 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
                 __sincosf(qz * a.z, &sz, &cz);
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) {
-                    float s, c;
-                    __sincosf(fmaf(qy[k], a.y, qx[k] * a.x), &s, &c);
-                    // e^{i Pxy} e^{+-i Pz}
-                    tFr[k] = fmaf(-s, sz, fmaf(c, cz, tFr[k]));
-                    tFi[k] = fmaf(c, sz, fmaf(s, cz, tFi[k]));
-                    tGr[k] = fmaf(s, sz, fmaf(c, cz, tGr[k]));
-                    tGi[k] = fmaf(-c, sz, fmaf(s, cz, tGi[k]));
+                    float sn, cn;
+                    __sincosf(fmaf(qy[k], a.y, qx[k] * a.x), &sn, &cn);
+                    tcc[k] = fmaf(cn, cz, tcc[k]);
+                    tss[k] = fmaf(sn, sz, tss[k]);
+                    tsc[k] = fmaf(sn, cz, tsc[k]);
+                    tcs[k] = fmaf(cn, sz, tcs[k]);
                 }
             }
 #pragma unroll
             for (int k = 0; k < CPT; ++k) {
-                fR[k] = fmaf(f, tFr[k], fR[k]);
-                fI[k] = fmaf(f, tFi[k], fI[k]);
-                gR[k] = fmaf(f, tGr[k], gR[k]);
-                gI[k] = fmaf(f, tGi[k], gI[k]);
+                cc[k] = fmaf(f, tcc[k], cc[k]);
+                ss[k] = fmaf(f, tss[k], ss[k]);
+                sc[k] = fmaf(f, tsc[k], sc[k]);
+                cs[k] = fmaf(f, tcs[k], cs[k]);
             }
         }
     }
-    if (BOXES && n_boxes > 0) box_sum_f32<CPT, THREADS>(boxes, n_boxes, qx, qy, qz, fR, fI, gR, gI, s_atoms);
+    if (BOXES && n_boxes > 0) box_sum_f32<CPT, THREADS>(boxes, n_boxes, qx, qy, qz, cc, ss, sc, cs, s_atoms);
     if (!active) return;
 
+    float fR[CPT], fI[CPT], gR[CPT], gI[CPT];
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        fR[k] = cc[k] - ss[k];
+        fI[k] = sc[k] + cs[k];
+        gR[k] = cc[k] + ss[k];
+        gI[k] = sc[k] - cs[k];
+    }
+
     float2* g2 = reinterpret_cast<float2*>(grid);
-    if (i == 0) {  // origin: every phase is zero
-        g2[0] = make_float2(fR[0] * scale, fI[0] * scale);
+    if (i == 0) {  // origin: every phase is zero; the host's FP64 sum avoids 1e5 in-phase roundings
+        g2[0] = make_float2((float)origin, 0.f);
         return;
     }
 #pragma unroll
@@ -237,7 +270,7 @@ __device__ __forceinline__ int job_of_tile(const FillJob* __restrict__ jobs, int
 template <int CPT, int THREADS, bool BOXES>
 __device__ __forceinline__ void run_tile(const FillJob& J, int64_t tile, float4* s_atoms) {
     fill_tile<CPT, THREADS, BOXES>(J.atoms, J.ion_off, J.U, J.aff_f32, J.pref, J.boxes, J.n_boxes, J.grid, J.n_items, J.Lp,
-                            J.step, J.cx, J.cy, J.cz, J.use_center, J.scale,
+                            J.step, J.cx, J.cy, J.cz, J.use_center, J.scale, J.origin,
                             (tile - J.tile_start) * THREADS + threadIdx.x, s_atoms);
 }
 
@@ -314,15 +347,16 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
         for (int k = 0; k < CPT; ++k) qx[k] = qy[k] = 0.0;
     }
 
-    double fR[CPT], fI[CPT], gR[CPT], gI[CPT];
+    // the four product sums of the FP32 fill, in FP64
+    double cc[CPT], ss[CPT], sc[CPT], cs[CPT];
 #pragma unroll
-    for (int k = 0; k < CPT; ++k) fR[k] = fI[k] = gR[k] = gI[k] = 0.0;
+    for (int k = 0; k < CPT; ++k) cc[k] = ss[k] = sc[k] = cs[k] = 0.0;
 
     for (int u = 0; u < U; ++u) {
         const int a0 = ion_off[u], a1 = ion_off[u + 1];
-        double sFr[CPT], sFi[CPT], sGr[CPT], sGi[CPT];
+        double tcc[CPT], tss[CPT], tsc[CPT], tcs[CPT];
 #pragma unroll
-        for (int k = 0; k < CPT; ++k) sFr[k] = sFi[k] = sGr[k] = sGi[k] = 0.0;
+        for (int k = 0; k < CPT; ++k) tcc[k] = tss[k] = tsc[k] = tcs[k] = 0.0;
         for (int t0 = a0; t0 < a1; t0 += THREADS) {
             const int n = min(THREADS, a1 - t0);
             __syncthreads();
@@ -337,27 +371,27 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
                 sincos(qz * a.z, &sz, &cz);
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) {
-                    double s, c;
-                    sincos(qx[k] * a.x + qy[k] * a.y, &s, &c);
-                    sFr[k] += c * cz - s * sz;
-                    sFi[k] += s * cz + c * sz;
-                    sGr[k] += c * cz + s * sz;
-                    sGi[k] += s * cz - c * sz;
+                    double sn, cn;
+                    sincos(qx[k] * a.x + qy[k] * a.y, &sn, &cn);
+                    tcc[k] = fma(cn, cz, tcc[k]);
+                    tss[k] = fma(sn, sz, tss[k]);
+                    tsc[k] = fma(sn, cz, tsc[k]);
+                    tcs[k] = fma(cn, sz, tcs[k]);
                 }
             }
         }
         const double f = aff[(int64_t)u * (Lp + 1) + i];
 #pragma unroll
         for (int k = 0; k < CPT; ++k) {
-            fR[k] += f * sFr[k];
-            fI[k] += f * sFi[k];
-            gR[k] += f * sGr[k];
-            gI[k] += f * sGi[k];
+            cc[k] = fma(f, tcc[k], cc[k]);
+            ss[k] = fma(f, tss[k], ss[k]);
+            sc[k] = fma(f, tsc[k], sc[k]);
+            cs[k] = fma(f, tcs[k], cs[k]);
         }
     }
     // voxelized-solvent boxes in FP64 (box data are the reference's floats),
-    // extent factors cached across boxes sorted by extent
-    double fx[CPT], fy[CPT], fz = 0.0, lx = -1.0, ly = -1.0, lz = -1.0;
+    // the x * y and z extent factors cached across boxes sorted by extent
+    double fxy[CPT], fz = 0.0, lx = -1.0, ly = -1.0, lz = -1.0;
     for (int b0 = 0; b0 < n_boxes; b0 += THREADS / 2) {
         const int nb = min(THREADS / 2, n_boxes - b0);
         __syncthreads();
@@ -368,20 +402,13 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
         __syncthreads();
         for (int j = 0; j < nb; ++j) {
             const double4_32a c = s_atoms[2 * j], L = s_atoms[2 * j + 1];
-            if (L.x != lx) {
+            if (L.x != lx || L.y != ly) {
                 lx = L.x;
-#pragma unroll
-                for (int k = 0; k < CPT; ++k) {
-                    const double h = 0.5 * qx[k] * L.x;
-                    fx[k] = L.x * (h == 0.0 ? 1.0 : sin(h) / h);
-                }
-            }
-            if (L.y != ly) {
                 ly = L.y;
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) {
-                    const double h = 0.5 * qy[k] * L.y;
-                    fy[k] = L.y * (h == 0.0 ? 1.0 : sin(h) / h);
+                    const double hx = 0.5 * qx[k] * L.x, hy = 0.5 * qy[k] * L.y;
+                    fxy[k] = L.x * (hx == 0.0 ? 1.0 : sin(hx) / hx) * L.y * (hy == 0.0 ? 1.0 : sin(hy) / hy);
                 }
             }
             if (L.z != lz) {
@@ -389,20 +416,28 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
                 const double h = 0.5 * qz * L.z;
                 fz = L.z * (h == 0.0 ? 1.0 : sin(h) / h);
             }
-            const double wz = c.w * fz;
             double sz, cz;
             sincos(qz * c.z, &sz, &cz);
+            const double wz = c.w * fz, wcz = wz * cz, wsz = wz * sz;
 #pragma unroll
             for (int k = 0; k < CPT; ++k) {
-                const double a = wz * fx[k] * fy[k];
-                double sn, cs;
-                sincos(qx[k] * c.x + qy[k] * c.y, &sn, &cs);
-                fR[k] += a * (cs * cz - sn * sz);
-                fI[k] += a * (sn * cz + cs * sz);
-                gR[k] += a * (cs * cz + sn * sz);
-                gI[k] += a * (sn * cz - cs * sz);
+                double sn, cn;
+                sincos(qx[k] * c.x + qy[k] * c.y, &sn, &cn);
+                const double tc = fxy[k] * cn, ts = fxy[k] * sn;
+                cc[k] = fma(tc, wcz, cc[k]);
+                ss[k] = fma(ts, wsz, ss[k]);
+                sc[k] = fma(ts, wcz, sc[k]);
+                cs[k] = fma(tc, wsz, cs[k]);
             }
         }
+    }
+    double fR[CPT], fI[CPT], gR[CPT], gI[CPT];
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+        fR[k] = cc[k] - ss[k];
+        fI[k] = sc[k] + cs[k];
+        gR[k] = cc[k] + ss[k];
+        gI[k] = sc[k] - cs[k];
     }
     if (!active) return;
 

@@ -108,6 +108,7 @@ struct LeafTables {
     size_t off = 0, aff = 0, pref = 0, boxes = SIZE_MAX;
     int64_t items = 0, n_boxes = 0;
     double cen[3] = {0, 0, 0};
+    double origin = 0;  // F(0) = scale (sum_u aff_u(0) N_u + sum_b w_b V_b), FP64
 };
 // Appends leaf d's tables for grid G (FP32 with cpt cells per item, or FP64).
 void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t);

@@ -85,6 +85,7 @@ struct FillJob {
     int64_t tile_start;
     double step;
     double cx, cy, cz;
+    double origin;          // F(q = 0), summed in FP64 on the host (every term adds in phase there)
     int U, Lp, use_center;
     int n_boxes;
     float scale;
@@ -125,6 +126,8 @@ cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid)
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
                            const AvgPlan& plan);
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
+// SFU calibration: blocks x 256 threads x iters x 8 __sincosf (2 MUFU ops each)
+cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);
 // d_res[0] = |origin cell|^2 (I at q = 0 of one plain leaf)
 cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res);
 // d_res[0] = |sum_m w_m A_m(0)|^2 over placed (and docked) models

@@ -955,6 +955,33 @@ cudaError_t launch_origin_models(cudaStream_t s, bool fp64, const ModelDev* d_mo
     return cudaGetLastError();
 }
 
+namespace {
+// SFU calibration: eight independent __sincosf chains per thread; each step is
+// two MUFU operations and one FMA, so the loop is bound by the MUFU pipe.
+__global__ void __launch_bounds__(256) sfu_probe_kernel(int iters, float* out) {
+    float x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = 0.001f * (threadIdx.x + 1) + 0.1f * c;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            float sn, cs;
+            __sincosf(x[c], &sn, &cs);
+            x[c] = fmaf(sn, 0.5f, cs);
+        }
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc += x[c];
+    if (acc == 12345.678f) out[0] = acc;  // keeps the chains live; never true for these inputs
+}
+}  // namespace
+
+cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out) {
+    sfu_probe_kernel<<<blocks, 256, 0, s>>>(iters, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res) {
     origin_intensity_kernel<<<1, 1, 0, s>>>(grid, fp64 ? 1 : 0, d_res);
     return cudaGetLastError();

@@ -53,6 +53,8 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
     } else {
         t.aff = put(h, aff.data(), aff.size() * sizeof(double));
     }
+    double origin = 0.0;  // F(0): the form factors at shell 0 times the ion counts, plus the box volumes
+    for (int u = 0; u < d.n_ions; ++u) origin += aff[(size_t)u * (G.Lp + 1)] * d.atoms_per_ion[u];
     std::vector<int64_t> pref(G.Lp + 1);
     t.items = dpx::fill_items(G, cpt, pref.data());
     t.pref = put(h, pref.data(), pref.size() * sizeof(int64_t));
@@ -78,7 +80,12 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
                                    (float)((double)s[2] - t.cen[2]), s[3]);
             b[2 * i + 1] = make_float4(s[4], s[5], s[6], 0.f);
         }
+        for (int64_t i = 0; i < t.n_boxes; ++i) {
+            const float* s = d.boxes + 8 * i;
+            origin += (double)s[3] * (double)s[4] * (double)s[5] * (double)s[6];
+        }
     }
+    t.origin = origin * d.scale;
 }
 
 dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
@@ -102,6 +109,7 @@ dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* db
     J.U = d.n_ions;
     J.Lp = G.Lp;
     J.scale = (float)d.scale;
+    J.origin = t.origin;
     return J;
 }
 

@@ -256,6 +256,12 @@ int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
                              const double* const* inD, const double* trans, const double* rots, int numGrids,
                              double* outAmpData, int precision, int* pStop);
 
+/* SFU calibration (no counterpart in the reference): times a kernel of
+ * independent __sincosf chains and returns the MUFU operations per second this
+ * GPU sustains (sin and cos count one each) — the denominator of the amplitude
+ * fill's roofline. */
+int dpx_measure_sfu_peak(dpx_ctx ctx, double* ops_per_s);
+
 /* ---- voxelized solvent (PDBAmplitude::FindPDBRanges PDBAmplitude.cpp:710-749,
  * CalculateSolventSpace VoxelizedSolvent.cpp:4-190) ----
  * Voxelizes the space around n_atoms atoms (xyz: 3 floats per atom, nm;
