@@ -247,11 +247,7 @@ def run_dpx(args):
         barrier()
     I_fp32 = res.copy()
 
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([dev_ms, e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, e2e_ms = t.tolist()
+    dev_ms, e2e_ms = max_over_ranks([dev_ms, e2e_ms], world)
 
     out = None
     if rank == 0:
@@ -557,13 +553,18 @@ def barrier_sync(world):
 
 
 def max_over_ranks(ms, world):
+    """Max over the ranks of a time (or a list of times): replicas report the
+    slowest rank.  NCCL ranks reduce on their GPU, gloo ranks on the CPU."""
     if world == 1:
         return ms
     import torch
     import torch.distributed as dist
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    vals = ms if isinstance(ms, (list, tuple)) else [ms]
+    t = torch.tensor(list(vals), dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    out = [float(x) for x in t.tolist()]
+    return out if isinstance(ms, (list, tuple)) else out[0]
 
 
 def fp64_error(ctx, amp, Q, dirs, I32):

@@ -1136,9 +1136,28 @@ int dpx_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xy
 int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
                                     const float* atomLocations, int64_t numAtoms, int numUniqueIons,
                                     const int* atomsPerIon, const float* coeffs, const float* ionRads,
-                                    int bitCombination, float solventED, float c1, double scale, int precision,
-                                    int* pStop) {
+                                    int bitCombination, float solventED, float c1, const float* solCOM,
+                                    const int* solDims, int64_t nSol, double voxStep, const float* outSolCOM,
+                                    const int* outSolDims, int64_t nOutSol, double outerSolED, double scale,
+                                    int precision, int* pStop) {
     if (!outData || !atomLocations) return fail(DPX_ERR_ARG, "NULL buffer");
+    if ((nSol > 0 && (!solCOM || !solDims)) || (nOutSol > 0 && (!outSolCOM || !outSolDims)))
+        return fail(DPX_ERR_ARG, "NULL voxel arrays");
+    // voxel boxes as PDBJacobianGridAmplitudeCalculation applies them
+    // (PDBAmplitudeCUDA.cu:363-389): excluded volume at -solvED when the
+    // CALC_VOXELIZED_SOLVENT bit (1 << 3) is set, the outer layer at
+    // outerSolED - solvED, each only with more than four boxes
+    std::vector<float> boxes;
+    auto add = [&](const float* com, const int* dims, int64_t n, double w) {
+        for (int64_t b = 0; b < n; ++b) {
+            const float rec[8] = {com[4 * b], com[4 * b + 1], com[4 * b + 2], (float)w,
+                                  (float)voxStep * (float)dims[4 * b], (float)voxStep * (float)dims[4 * b + 1],
+                                  (float)voxStep * (float)dims[4 * b + 2], 0.f};
+            boxes.insert(boxes.end(), rec, rec + 8);
+        }
+    };
+    if (solventED != 0.0f && (bitCombination & (1 << 3)) && nSol > 4) add(solCOM, solDims, nSol, -solventED);
+    if (outerSolED != 0.0 && nOutSol > 4) add(outSolCOM, outSolDims, nOutSol, outerSolED - solventED);
     int grid_size;
     double qmax;
     if (int rc = grid_from_voxels((int64_t)voxels, thDivs, phDivs, stepSize, &grid_size, &qmax)) return rc;
@@ -1153,8 +1172,10 @@ int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, dou
     std::vector<double> cd(9 * numUniqueIons), rd(numUniqueIons);
     for (int k = 0; k < 9 * numUniqueIons; ++k) cd[k] = coeffs[k];
     for (int k = 0; k < numUniqueIons; ++k) rd[k] = ionRads ? ionRads[k] : 0.0;
-    rc = dpx_grid_fill_pdb(g, numAtoms, atomLocations, 0, numUniqueIons, atomsPerIon, cd.data(), rd.data(),
-                           bitCombination, solventED, c1, scale, nullptr);
+    dpx_pdb_desc d{numAtoms, atomLocations, 0, numUniqueIons, atomsPerIon, cd.data(), rd.data(),
+                   bitCombination & 3, solventED, c1, scale, nullptr, (int64_t)boxes.size() / 8,
+                   boxes.empty() ? nullptr : boxes.data()};
+    rc = dpx_grid_fill_pdb_batch(1, &g, &d);
     if (!rc && pStop && *pStop) rc = fail(DPX_ERR_STOPPED, "stopped");
     if (!rc) rc = dpx_grid_read(g, outData, nullptr);
     dpx_grid_destroy(g);

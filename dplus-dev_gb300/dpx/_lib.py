@@ -99,7 +99,8 @@ _SIGS = {
     "dpx_q_brackets": (C.c_int, [C.c_int, C.c_double, C.c_int, _D, _I]),
     "dpx_make_globule": (C.c_int, [C.c_int64, C.c_double, C.c_uint64, _F, _I]),
     "dpx_pdb_jacobian_grid_amplitude": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.c_double, _D, _F, C.c_int64,
-                                                  C.c_int, _I, _F, _F, C.c_int, C.c_float, C.c_float, C.c_double,
+                                                  C.c_int, _I, _F, _F, C.c_int, C.c_float, C.c_float, _F, _I,
+                                                  C.c_int64, C.c_double, _F, _I, C.c_int64, C.c_double, C.c_double,
                                                   C.c_int, _I]),
     "dpx_calc_mcoa_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, C.c_int,
                                            C.c_int64, C.c_double, _D, C.c_int64, C.c_int, _I]),

@@ -219,13 +219,20 @@ int dpx_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xy
 /* ---- drop-in replacements with the reference's argument meaning ---- */
 /* PDBJacobianGridAmplitudeCalculation: outData is a caller-owned host buffer of
  * 2*voxels doubles in grid-index order; splines are left to the caller, as in
- * the reference.  Returns 0 or a negative status (the reference returns
- * -3000-err / -1000-err; callers test != 0). */
+ * the reference.  Voxelized solvent as the reference passes it: solCOM /
+ * outSolCOM float4 box centres (nm), solDims / outSolDims int4 extents in
+ * voxels of voxStep nm; excluded-volume boxes count at -solventED when
+ * bitCombination has CALC_VOXELIZED_SOLVENT (1 << 3), solvation boxes at
+ * outerSolED - solventED, each set only with more than four boxes.  Returns 0
+ * or a negative status (the reference returns -3000-err / -1000-err; callers
+ * test != 0). */
 int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
                                     const float* atomLocations, int64_t numAtoms, int numUniqueIons,
                                     const int* atomsPerIon, const float* coeffs, const float* ionRads,
-                                    int bitCombination, float solventED, float c1, double scale, int precision,
-                                    int* pStop);
+                                    int bitCombination, float solventED, float c1, const float* solCOM,
+                                    const int* solDims, int64_t nSol, double voxStep, const float* outSolCOM,
+                                    const int* outSolDims, int64_t nOutSol, double outerSolED, double scale,
+                                    int precision, int* pStop);
 /* GPUCalcMCOAJacobSphrDD with explicit directions: inAmp / inD are the grid's
  * values and spline derivatives [2 voxels]; intensities [qPoints]. */
 int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* inAmp,

@@ -190,8 +190,8 @@ def test_drop_in_grid_amplitude_entry(ctx):
     rf = amp.ion_rads.astype(np.float32)
     rc = dpx.lib().dpx_pdb_jacobian_grid_amplitude(P, 3, 6, qmax / (gs // 2), _lib.dptr(out), _lib.fptr(a), len(a),
                                                    len(amp.unique), _lib.iptr(amp.atoms_per_ion), _lib.fptr(cf),
-                                                   _lib.fptr(rf), amp.flags, amp.solventED, amp.c1, amp.scale,
-                                                   M.FP64, None)
+                                                   _lib.fptr(rf), amp.flags, amp.solventED, amp.c1, None, None, 0,
+                                                   0.0, None, None, 0, 0.0, amp.scale, M.FP64, None)
     _lib.check(rc)
     s = O.Struct(amp.xyz, amp.atoms_per_ion, cf.astype(np.float64), rf.astype(np.float64), amp.flags,
                  amp.solventED, amp.c1, amp.scale)
@@ -199,12 +199,13 @@ def test_drop_in_grid_amplitude_entry(ctx):
     stop = C.c_int(1)
     assert dpx.lib().dpx_pdb_jacobian_grid_amplitude(P, 3, 6, qmax / (gs // 2), _lib.dptr(out), _lib.fptr(a), len(a),
                                                      len(amp.unique), _lib.iptr(amp.atoms_per_ion), _lib.fptr(cf),
-                                                     _lib.fptr(rf), amp.flags, amp.solventED, amp.c1, amp.scale,
-                                                     M.FP64, C.byref(stop)) == -4
+                                                     _lib.fptr(rf), amp.flags, amp.solventED, amp.c1, None, None,
+                                                     0, 0.0, None, None, 0, 0.0, amp.scale, M.FP64,
+                                                     C.byref(stop)) == -4
     assert dpx.lib().dpx_pdb_jacobian_grid_amplitude(P + 1, 3, 6, 0.5, _lib.dptr(out), _lib.fptr(a), len(a),
                                                      len(amp.unique), _lib.iptr(amp.atoms_per_ion), _lib.fptr(cf),
-                                                     _lib.fptr(rf), amp.flags, amp.solventED, amp.c1, amp.scale,
-                                                     M.FP64, None) == -1
+                                                     _lib.fptr(rf), amp.flags, amp.solventED, amp.c1, None, None,
+                                                     0, 0.0, None, None, 0, 0.0, amp.scale, M.FP64, None) == -1
 
 
 def test_drop_in_mcoa_entry(ctx):
@@ -590,3 +591,29 @@ def test_layer_fp32_error_with_many_boxes(ctx):
     amp._grid = None
     I64 = M.DomainModel([amp], gs, qmax, M.FP64).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
     assert rel(I32, I64) <= TOL32
+
+
+def test_drop_in_grid_fill_with_voxel_boxes(ctx):
+    """The grid-fill drop-in with the reference's float4 / int4 voxel arrays
+    gives the grid of the Python leaf with the same boxes (solvation layer)."""
+    amp = globule(250, 1.1, seed=97, extra=LAYER)
+    gs, qmax = 22, 4.5
+    P = dpx.lib().dpx_grid_cells(gs)
+    ec, ed, lc, ld = amp.voxel_boxes()
+    com4 = np.zeros((len(lc), 4), dtype=np.float32)
+    com4[:, :3] = lc
+    dim4 = np.zeros((len(ld), 4), dtype=np.int32)
+    dim4[:, :3] = ld
+    a = amp.atoms_float4()
+    cf = amp.coeffs.astype(np.float32)
+    rf = amp.ion_rads.astype(np.float32)
+    out = np.zeros(2 * P)
+    _lib.check(dpx.lib().dpx_pdb_jacobian_grid_amplitude(P, 3, 6, qmax / (gs // 2), _lib.dptr(out), _lib.fptr(a),
+                                                         len(a), len(amp.unique), _lib.iptr(amp.atoms_per_ion),
+                                                         _lib.fptr(cf), _lib.fptr(rf), amp.flags, amp.solventED,
+                                                         amp.c1, None, None, 0, amp.voxelStep, _lib.fptr(com4),
+                                                         _lib.iptr(dim4), len(lc), amp.outerSolventED, amp.scale,
+                                                         M.FP64, None))
+    s = O.Struct(amp.xyz, amp.atoms_per_ion, cf.astype(np.float64), rf.astype(np.float64), amp.flags,
+                 amp.solventED, amp.c1, amp.scale, amp.solvent_boxes())
+    assert rel_to_max(out, O.grid_fill(s, gs, qmax, O.FP64)) <= TOL64
