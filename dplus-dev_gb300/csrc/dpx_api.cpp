@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
@@ -523,14 +524,41 @@ void make_brackets(const dpx::Geom& G, int grid_size, double qmax, int nq, const
     }
 }
 
+namespace {
+struct TripleHash {
+    size_t operator()(const std::array<double, 3>& a) const {
+        uint64_t h = 1469598103934665603ull;
+        for (double v : a) {
+            uint64_t b;
+            std::memcpy(&b, &v, sizeof b);
+            h = (h ^ b) * 1099511628211ull;
+        }
+        return (size_t)h;
+    }
+};
+
+// Translations t_m = t_0 + m d (m = 0..M-1) to 1e-9 nm on every axis, in the
+// order given: the group's phase sum then has a closed form (the FP32 path uses it).
+bool arithmetic_progression(const std::vector<double>& T, size_t first, size_t M, double d[3]) {
+    if (M < 3) return false;
+    const double* t0 = &T[3 * first];
+    const double* tl = &T[3 * (first + M - 1)];
+    for (int a = 0; a < 3; ++a) d[a] = (tl[a] - t0[a]) / double(M - 1);
+    for (size_t m = 1; m + 1 < M; ++m)
+        for (int a = 0; a < 3; ++a)
+            if (std::fabs(T[3 * (first + m) + a] - (t0[a] + double(m) * d[a])) > 1e-9) return false;
+    return true;
+}
+}  // namespace
+
 int build_models(int n_models, const void* const* cells, const double* rot, const double* tr, const int* n_copies,
                  const double* copy_rot, const double* copy_tr, const double* sym_scale, ModelTables& t) {
     std::vector<dpx::ModelDev>& md = t.md;
     std::vector<char>& gstage = t.gstage;
     md.assign(n_models, dpx::ModelDev{});
-    std::vector<double> gR, gT;
-    std::vector<int> gOff;
-    std::vector<int> model_group_base(n_models), model_toff_base(n_models);
+    std::vector<double> gR, gT, gS;
+    std::vector<int> gOff, gA;
+    std::vector<int> model_group_base(n_models), model_toff_base(n_models), model_gidx_base(n_models);
     int copy_base = 0;
     for (int m = 0; m < n_models; ++m) {
         dpx::ModelDev& M = md[m];
@@ -543,49 +571,65 @@ int build_models(int n_models, const void* const* cells, const double* rot, cons
                    M.R[3] == 0.0 && M.R[5] == 0.0 && M.R[6] == 0.0 && M.R[7] == 0.0 && M.tr[0] == 0.0 &&
                    M.tr[1] == 0.0 && M.tr[2] == 0.0);
         model_group_base[m] = (int)gOff.size();
+        model_gidx_base[m] = (int)gA.size();
         // group copies by identical Euler triples, first-appearance order
-        std::vector<int> rep;
+        // (ManualSymmetry translationsPerOrientation, Symmetries.cpp:670-695)
+        std::unordered_map<std::array<double, 3>, int, TripleHash> where;
         std::vector<std::vector<int>> members;
         for (int c = 0; c < nc; ++c) {
             const double* r = copy_rot + 3 * (copy_base + c);
-            int found = -1;
-            for (size_t gi = 0; gi < rep.size(); ++gi) {
-                const double* r0 = copy_rot + 3 * (copy_base + rep[gi]);
-                if (r0[0] == r[0] && r0[1] == r[1] && r0[2] == r[2]) { found = (int)gi; break; }
+            const std::array<double, 3> key{r[0], r[1], r[2]};
+            auto f = where.find(key);
+            if (f == where.end()) {
+                where.emplace(key, (int)members.size());
+                members.push_back({c});
+            } else {
+                members[f->second].push_back(c);
             }
-            if (found < 0) { rep.push_back(c); members.push_back({c}); }
-            else members[found].push_back(c);
         }
-        M.n_groups = (int)rep.size();
+        M.n_groups = (int)members.size();
         model_toff_base[m] = (int)(gT.size() / 3);
-        for (size_t gi = 0; gi < rep.size(); ++gi) {
+        for (size_t gi = 0; gi < members.size(); ++gi) {
             double R[9];
-            const double* r = copy_rot + 3 * (copy_base + rep[gi]);
+            const double* r = copy_rot + 3 * (copy_base + members[gi][0]);
             euler(r[0], r[1], r[2], R);
             gR.insert(gR.end(), R, R + 9);
-            gOff.push_back((int)(gT.size() / 3) - model_toff_base[m]);
+            const size_t first = gT.size() / 3;
+            gOff.push_back((int)first - model_toff_base[m]);
             for (int c : members[gi]) {
-                const double* t = copy_tr + 3 * (copy_base + c);
-                gT.insert(gT.end(), t, t + 3);
+                const double* tt = copy_tr + 3 * (copy_base + c);
+                gT.insert(gT.end(), tt, tt + 3);
             }
+            double d[3] = {0, 0, 0};
+            const bool ap = arithmetic_progression(gT, first, members[gi].size(), d);
+            gS.insert(gS.end(), d, d + 3);
+            gA.push_back(ap ? (int)members[gi].size() : 0);
         }
         gOff.push_back((int)(gT.size() / 3) - model_toff_base[m]);
         copy_base += nc;
     }
-    // device layout of the group tables: [R (doubles)] [T (doubles)] [off (ints)]
+    // device layout of the group tables: [R][T][step] (doubles) [off][ap] (ints)
     const size_t bytesR = gR.size() * sizeof(double), bytesT = gT.size() * sizeof(double),
-                 bytesO = gOff.size() * sizeof(int);
-    gstage.assign(bytesR + bytesT + bytesO, 0);
-    if (bytesR) std::memcpy(gstage.data(), gR.data(), bytesR);
-    if (bytesT) std::memcpy(gstage.data() + bytesR, gT.data(), bytesT);
-    if (bytesO) std::memcpy(gstage.data() + bytesR + bytesT, gOff.data(), bytesO);
+                 bytesS = gS.size() * sizeof(double), bytesO = gOff.size() * sizeof(int),
+                 bytesA = gA.size() * sizeof(int);
+    gstage.assign(bytesR + bytesT + bytesS + bytesO + bytesA, 0);
+    char* h = gstage.data();
+    if (bytesR) std::memcpy(h, gR.data(), bytesR);
+    if (bytesT) std::memcpy(h + bytesR, gT.data(), bytesT);
+    if (bytesS) std::memcpy(h + bytesR + bytesT, gS.data(), bytesS);
+    if (bytesO) std::memcpy(h + bytesR + bytesT + bytesS, gOff.data(), bytesO);
+    if (bytesA) std::memcpy(h + bytesR + bytesT + bytesS + bytesO, gA.data(), bytesA);
     t.oR.assign(n_models, 0);
     t.oT.assign(n_models, 0);
     t.oO.assign(n_models, 0);
+    t.oS.assign(n_models, 0);
+    t.oA.assign(n_models, 0);
     int groups_seen = 0;
     for (int m = 0; m < n_models; ++m) {
         t.oR[m] = 9 * sizeof(double) * (size_t)groups_seen;
-        t.oO[m] = bytesR + bytesT + sizeof(int) * (size_t)model_group_base[m];
+        t.oS[m] = bytesR + bytesT + 3 * sizeof(double) * (size_t)groups_seen;
+        t.oO[m] = bytesR + bytesT + bytesS + sizeof(int) * (size_t)model_group_base[m];
+        t.oA[m] = bytesR + bytesT + bytesS + bytesO + sizeof(int) * (size_t)model_gidx_base[m];
         t.oT[m] = bytesR + 3 * sizeof(double) * (size_t)model_toff_base[m];
         groups_seen += md[m].n_groups;
     }
@@ -597,6 +641,8 @@ void place_models(ModelTables& t, char* dbase) {
         t.md[m].group_R = reinterpret_cast<const double*>(dbase + t.oR[m]);
         t.md[m].group_off = reinterpret_cast<const int*>(dbase + t.oO[m]);
         t.md[m].trans = reinterpret_cast<const double*>(dbase + t.oT[m]);
+        t.md[m].group_step = reinterpret_cast<const double*>(dbase + t.oS[m]);
+        t.md[m].group_ap = reinterpret_cast<const int*>(dbase + t.oA[m]);
     }
 }
 

@@ -41,6 +41,8 @@ struct ModelDev {
     const double* group_R; // [9 n_groups] rotation per group (row-major)
     const int* group_off;  // [n_groups + 1] into trans
     const double* trans;   // [3 K]
+    const double* group_step;  // [3 n_groups] d of a group whose translations are t0 + m d
+    const int* group_ap;       // [n_groups] M of such a group (0: an arbitrary list)
     double sym_scale;
     int plain;             // R is the identity and tr is zero
 };

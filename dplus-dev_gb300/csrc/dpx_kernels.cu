@@ -255,6 +255,34 @@ template <> __device__ __forceinline__ Cx<float> expi<float>(double phase) {
     return {c, s};
 }
 
+// sum_{m < M} e^{i (p0 + m theta)}: the phase sum of M translations in
+// arithmetic progression (p0 = q n.t0, theta = q n.d).  With x = theta_r / 2,
+// theta_r = theta reduced to (-pi, pi] (the reduction's whole turns cancel
+// between the two factors below):
+//   e^{i (p0 + (M-1) x)} sin(M x) / sin(x)
+// where |M x| < 0.05 takes the series M [1 - (M^2-1) x^2 / 6
+// + (3M^4 - 10M^2 + 7) x^4 / 360] (truncation < 1e-11 relative), so the
+// Bragg condition x -> 0 keeps full relative accuracy.
+template <typename T>
+__device__ __forceinline__ Cx<T> ap_sum(double p0, double theta, int M) {
+    double t = theta * (1.0 / k2Pi);
+    t -= rint(t);
+    const double x = t * kPi;  // theta_r / 2, |x| <= pi / 2
+    const double Mx = (double)M * x;
+    double ratio;
+    if (fabs(Mx) < 0.05) {
+        const double m2 = (double)M * (double)M, x2 = x * x;
+        ratio = (double)M * (1.0 - (m2 - 1.0) * x2 / 6.0 + (3.0 * m2 * m2 - 10.0 * m2 + 7.0) * x2 * x2 / 360.0);
+    } else {
+        const Cx<T> sM = expi<T>(Mx);  // FP64 reduction of the long angle, then the turn
+        T sx, cx;
+        sincospi((T)t, &sx, &cx);     // sin(x) = sin(pi t), relative accuracy down to small x
+        ratio = (double)sM.i / (double)sx;
+    }
+    const Cx<T> e = expi<T>(p0 + (double)(M - 1) * x);
+    return {(T)(ratio * (double)e.r), (T)(ratio * (double)e.i)};
+}
+
 // --------------------------------------------------------------------------
 // Amplitude of every model at one direction for up to MQ q values of a
 // bracket (plane index fInd, radial fractions frac): for every model and
@@ -304,12 +332,24 @@ __device__ void sample_amps(const ModelDev* __restrict__ models, int n_models, i
                 Cx<T> tp[MQ];
 #pragma unroll
                 for (int k = 0; k < MQ; ++k) tp[k] = {T(0), T(0)};
-                for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
-                    const double* tt = M.trans + 3 * c;
-                    const double a = dir[0] * tt[0] + dir[1] * tt[1] + dir[2] * tt[2];
+                const int ap = (sizeof(T) == 4 && M.group_ap) ? M.group_ap[gi] : 0;
+                if (ap > 0) {
+                    // FP32 bulk: translations t0 + m d, m < M, summed in closed form
+                    const double* t0 = M.trans + 3 * M.group_off[gi];
+                    const double* dd = M.group_step + 3 * gi;
+                    const double a0 = dir[0] * t0[0] + dir[1] * t0[1] + dir[2] * t0[2];
+                    const double ad = dir[0] * dd[0] + dir[1] * dd[1] + dir[2] * dd[2];
 #pragma unroll
                     for (int k = 0; k < MQ; ++k)
-                        if (k < mq) tp[k] = cadd(tp[k], expi<T>(a * qv[k]));
+                        if (k < mq) tp[k] = ap_sum<T>(a0 * qv[k], ad * qv[k], ap);
+                } else {
+                    for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
+                        const double* tt = M.trans + 3 * c;
+                        const double a = dir[0] * tt[0] + dir[1] * tt[1] + dir[2] * tt[2];
+#pragma unroll
+                        for (int k = 0; k < MQ; ++k)
+                            if (k < mq) tp[k] = cadd(tp[k], expi<T>(a * qv[k]));
+                    }
                 }
 #pragma unroll
                 for (int k = 0; k < MQ; ++k)
