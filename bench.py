@@ -436,6 +436,122 @@ def run_batch(args):
     return out if rank == 0 else None
 
 
+ASM_NQ, ASM_DIRS, ASM_GRID, ASM_QMAX = 400, 1_000_000, 300, 4.0
+
+
+def run_assembly(args):
+    """Symmetry-docked assemblies of one 5,000-atom subunit (r = 3 nm, vacuum),
+    hybrid docked sum per orientation sample: the 60 rotations of the
+    icosahedral group with translations R_k (0, 0, 12 nm), and a 1,300-copy
+    helix (radius 12 nm, 13 per 8 nm turn, seeded subunit orientation turned
+    by each copy's azimuth).  150 layers, qmax 4, 400 q, FP32 bulk.  A step is
+    the subunit grid fill plus both MC averages over 1e6 fixed directions (two
+    solves); VEGAS (5 x 2e5 points) and Gauss-Kronrod (1e-5) are timed once
+    on the icosahedral assembly, and the plain FP64 path on 1e5 directions."""
+    import torch
+    from dpx import models as M
+    from dpx import workloads as W
+
+    rank, world, lrank = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(lrank)
+    ctx = M.Context(lrank)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    sym, xyz = M.make_globule(5000, 3.0, 2020)
+    leaf = M.PDBAmplitude(sym, xyz, W.VACUUM)
+    ir, it = W.icosahedral_copies(12.0)
+    hr, ht = W.helix_copies(1300, 12.0, 13, 8.0, seed=77)
+    rows_ico = np.concatenate([it, np.degrees(ir)], axis=1)
+    rows_hel = np.concatenate([ht, np.degrees(hr)], axis=1)
+    Q = np.linspace(0.0, ASM_QMAX, ASM_NQ)
+    dirs = M.mc_directions(DIR_SEED, ASM_DIRS)
+    d_dirs = torch.from_numpy(dirs).cuda()
+
+    def dom(rows, prec=M.FP32):
+        return M.DomainModel([M.ManualSymmetry(leaf, rows, use_grid=False)], ASM_GRID, ASM_QMAX, prec)
+
+    import ctypes as C
+    from dpx import _lib
+    L = M.lib()
+
+    def mc(d, ndirs=ASM_DIRS):
+        (n, gh, rot, tr, ncop, crot, ctr, sscale), keep = d._model_args(ctx)
+        res = np.zeros(len(Q))
+        _lib.check(L.dpx_orientation_average(ctx.handle, n, gh, _lib.dptr(rot), _lib.dptr(tr), _lib.iptr(ncop),
+                                             _lib.dptr(crot), _lib.dptr(ctr), _lib.dptr(sscale), len(Q),
+                                             _lib.dptr(Q), C.c_void_p(d_dirs.data_ptr()), 1, 0, ndirs, 0.0,
+                                             _lib.dptr(res)))
+        return res
+
+    d_ico, d_hel = dom(rows_ico), dom(rows_hel)
+
+    def step():
+        leaf._grid = None  # the subunit grid is refilled every step
+        return mc(d_ico), mc(d_hel)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(lrank) as clk:
+        barrier_sync(world)
+        e0.record(stream)
+        for _ in range(args.steps):
+            I_ico, I_hel = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dev_ms = e0.elapsed_time(e1)
+    dev_ms = max_over_ranks(dev_ms, world)
+    # end to end: host directions in, I(q) out, through DomainModel
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        leaf._grid = None
+        d_ico.CalculateIntensityVector(ctx, Q, 0.0, ASM_DIRS, dirs)
+        d_hel.CalculateIntensityVector(ctx, Q, 0.0, ASM_DIRS, dirs)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    solves = 2 * args.steps * world
+    value = solves / (dev_ms / 1e3)
+    out = {
+        "metric": "I(q) solves/s (FP32-bulk, symmetry-docked assemblies, hybrid MC 1e6 directions)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded globule, icosahedral and helical copies)",
+        "config": {"workload": "5,000-atom subunit r=3 nm; icosahedral 60 copies at 12 nm; helix 1,300 copies, "
+                               "r=12 nm, 13 per 8 nm turn; 150 layers, qmax 4, 400 q, MC 1e6 directions; a step "
+                               "= subunit fill + both averages (2 solves)",
+                   "copies": [60, 1300], "rotation_groups": [60, 13],
+                   "l2": "subunit grid 350 MB (> 129 MB L2) gathered per sample"},
+        "e2e": {"value": 2 * world / e2e_s, "unit": "solves/s",
+                "h2d_bytes_per_step": int(2 * dirs.nbytes + 16 * len(xyz) + 48 * (60 + 1300)),
+                "d2h_bytes_per_step": int(2 * Q.nbytes)},
+        "gpu_launches": 2 * 4 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_extras:
+        t0 = time.perf_counter()
+        d_ico.CalculateIntensityVector(ctx, Q, 0.0, 5 * 200704, method="VEGAS", seed=11, points_per_iter=200704)
+        out["vegas_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        Qg = np.linspace(0.05, ASM_QMAX, 40)
+        d_ico.CalculateIntensityVector(ctx, Qg, 1e-5, 6, method="GK")
+        out["gk_s_40q_depth6"] = time.perf_counter() - t0
+        errs = []
+        for rows, I32 in ((rows_ico, None), (rows_hel, None)):
+            leaf._grid = None
+            a32 = mc(dom(rows, M.FP32), 100_000)
+            leaf._grid = None
+            a64 = mc(dom(rows, M.FP64), 100_000)
+            errs.append(float(np.max(np.abs(a32 - a64) / np.abs(a64))))
+        out["max_rel_err_vs_fp64_1e5_dirs"] = errs
+        leaf._grid = None
+    ctx.close()
+    return out if rank == 0 else None
+
+
 SERVE_DIRS, SERVE_NQ = 10_000, 100
 
 
@@ -644,7 +760,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--check-error", action="store_true")
     ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
-    ap.add_argument("--workload", default="subunit", choices=["subunit", "batch", "serve"])
+    ap.add_argument("--workload", default="subunit", choices=["subunit", "batch", "serve", "assembly"])
+    ap.add_argument("--no-extras", action="store_true", help="assembly: skip the VEGAS / GK / FP64 extras")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--inflight", type=int, default=32)
@@ -660,7 +777,7 @@ def main():
     else:
         from dpx import _build
         _build.build_libdpx()
-        run = {"batch": run_batch, "serve": run_serve}.get(args.workload, run_dpx)
+        run = {"batch": run_batch, "serve": run_serve, "assembly": run_assembly}.get(args.workload, run_dpx)
         out = run(args)
     if out is not None:
         print(json.dumps(out))

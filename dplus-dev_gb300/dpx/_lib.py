@@ -130,6 +130,9 @@ _SIGS = {
     "dpx_boxes_space": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dpx_boxes_free": (C.c_int, [_P]),
     "dpx_measure_sfu_peak": (C.c_int, [_P, _D]),
+    "dpx_amp_write": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_double, _D]),
+    "dpx_amp_read_info": (C.c_int, [C.c_char_p, _I, _D, C.c_char_p, C.c_int64]),
+    "dpx_amp_read": (C.c_int, [C.c_char_p, _D]),
     "dpx_mc_average_noalloc": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, _D, _P, C.c_int64, C.c_double,
                                          _P, _P]),
 }

@@ -15,6 +15,7 @@ intensities.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import hashlib
 import math
 from typing import Sequence
@@ -102,6 +103,25 @@ class Grid:
         coeffs = None if coeffs is None else np.ascontiguousarray(coeffs, dtype=np.float64)
         check(lib().dpx_grid_write(self.handle, dptr(values), dptr(coeffs)))
 
+    def save_amp(self, path: str, header: str = "") -> None:
+        """D+'s binary .amp (version 13, Grid.cpp:847-891): the amplitudes only."""
+        v, _ = self.read(True, False)
+        check(lib().dpx_amp_write(os.fsencode(path), header.encode(), self.grid_size,
+                                  self.qmax / (self.grid_size // 2), dptr(v)))
+
+    def save_ampj(self, path: str, params: Sequence[float] = (), header: str = "") -> None:
+        """D+'s zipped grid (Amplitude::WriteAmplitudeToFile, Amplitude.cpp:3120-3212):
+        grid.dat (the raw amplitudes), criticalinfo.json and header.json, stored."""
+        import json
+        import zipfile
+        v, _ = self.read(True, False)
+        info = {"qmax": self.qmax, "qmin": 0, "gridSize": self.grid_size,
+                "stepSize": self.qmax / (self.grid_size // 2), "Params": [float(x) for x in params]}
+        with zipfile.ZipFile(path, "w", zipfile.ZIP_STORED) as z:
+            z.writestr("grid.dat", np.ascontiguousarray(v, dtype="<f8").tobytes())
+            z.writestr("criticalinfo.json", json.dumps(info))
+            z.writestr("header.json", json.dumps({"Old Header:": header, "Header": {}}))
+
     def close(self) -> None:
         if self.handle:
             lib().dpx_grid_destroy(self.handle)
@@ -112,6 +132,61 @@ class Grid:
             self.close()
         except Exception:
             pass
+
+
+def read_amp(path: str):
+    """(grid_size, qmax, header, values) of a .amp (binary v13) or .ampj (zip) file."""
+    if zipfile_like(path):
+        import json
+        import zipfile
+        with zipfile.ZipFile(path) as z:
+            info = json.loads(z.read("criticalinfo.json"))
+            values = np.frombuffer(z.read("grid.dat"), dtype="<f8").astype(np.float64)
+            header = ""
+            if "header.json" in z.namelist():
+                header = json.loads(z.read("header.json")).get("Old Header:", "")
+        gs, qmax = int(info["gridSize"]), float(info["qmax"])
+        if len(values) != 2 * lib().dpx_grid_cells(gs):
+            raise ValueError(f"{path}: grid.dat holds {len(values)} doubles, not 2 x {lib().dpx_grid_cells(gs)}")
+        return gs, qmax, header, values
+    gs, step = C.c_int(), C.c_double()
+    head = C.create_string_buffer(1 << 16)
+    check(lib().dpx_amp_read_info(os.fsencode(path), C.byref(gs), C.byref(step), head, len(head)))
+    values = np.empty(2 * lib().dpx_grid_cells(gs.value))
+    check(lib().dpx_amp_read(os.fsencode(path), dptr(values)))
+    return gs.value, step.value * (gs.value // 2), head.value.decode(errors="replace"), values
+
+
+def zipfile_like(path: str) -> bool:
+    with open(path, "rb") as f:
+        return f.read(4) == b"PK\x03\x04"
+
+
+class AmpGridAmplitude:
+    """A leaf read from a D+ amplitude file (AmpGridAmplitude, Amplitude.cpp:3682-3720,
+    3955-3970): the stored amplitudes times ``scale``, splines recomputed on
+    the device, placed by ``location`` like any leaf."""
+
+    def __init__(self, path: str, scale: float = 1.0, location: Sequence[float] = (0, 0, 0, 0, 0, 0)):
+        self.path = path
+        self.grid_size, self.qmax, self.header, self.values = read_amp(path)
+        self.scale = float(scale)
+        self.location = tuple(float(v) for v in location)
+        self._grid = None
+        self._grid_key = None
+
+    def calculateGrid(self, ctx: Context, qmax: float, gridSize: int, precision: int = FP32) -> Grid:
+        if int(gridSize) != self.grid_size or abs(float(qmax) - self.qmax) > 1e-12 * self.qmax:
+            raise ValueError(f"{self.path} holds a grid of size {self.grid_size}, qmax {self.qmax}; "
+                             f"the model asks for {gridSize}, {qmax}")
+        key = (self.scale, int(precision), ctx.device)
+        if self._grid is not None and self._grid_key == key:
+            return self._grid
+        g = Grid(ctx, self.grid_size, self.qmax, precision)
+        g.write(self.values * self.scale)
+        g.compute_splines()
+        self._grid, self._grid_key = g, key
+        return g
 
 
 def euler_deg_to_rad(a, b, g):

@@ -128,9 +128,9 @@ typedef struct dpx_pdb_desc {
     const float* boxes;
 } dpx_pdb_desc;
 /* Fills n grids (distinct, one context) from n leaves.  The FP32 grids of the
- * batch share ONE persistent launch that pulls tiles of every leaf from a
- * common counter, so small leaves no longer leave SMs idle; FP64 grids get a
- * launch each.  Same results as n calls of dpx_grid_fill_pdb.  The reference
+ * batch share ONE launch over the tiles of every leaf (flat: one CTA per tile;
+ * or persistent, dpx_ctx_set_fill_schedule), so small leaves no longer leave
+ * SMs idle; FP64 grids get a launch each.  Same results as n calls of dpx_grid_fill_pdb.  The reference
  * fills each PDBAmplitude in its own call (Amplitude.cpp PDBAmplitude::calculateGrid). */
 int dpx_grid_fill_pdb_batch(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs);
 /* Autotuner (no counterpart in the reference): fills the batch once per shape
@@ -268,6 +268,17 @@ int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
  * GPU sustains (sin and cos count one each) — the denominator of the amplitude
  * fill's roofline. */
 int dpx_measure_sfu_peak(dpx_ctx ctx, double* ops_per_s);
+
+/* ---- amplitude-grid files (D+'s binary .amp, version 13: JacobianSphereGrid::
+ * ExportBinaryData / ImportBinaryData, Backend/Backend/Grid.cpp:847-963) ----
+ * values: 2 * dpx_grid_cells(grid_size) doubles, the interleaved complex
+ * amplitudes in grid-index order (dpx_grid_read / dpx_grid_write layout);
+ * step = qmax / (grid_size / 2).  Host file I/O; spline coefficients are not
+ * stored (a reader recomputes them, as D+ does). */
+int dpx_amp_write(const char* path, const char* header, int grid_size, double step, const double* values);
+/* grid_size, step and the header text (NUL-terminated, truncated to header_cap). */
+int dpx_amp_read_info(const char* path, int* grid_size, double* step, char* header, int64_t header_cap);
+int dpx_amp_read(const char* path, double* values);
 
 /* ---- voxelized solvent (PDBAmplitude::FindPDBRanges PDBAmplitude.cpp:710-749,
  * CalculateSolventSpace VoxelizedSolvent.cpp:4-190) ----

@@ -642,3 +642,34 @@ def test_helical_assembly_closed_form_phase_sums(ctx):
             amp._grid = None
         assert rel(I[M.FP32], I[M.FP64]) <= TOL32
         assert abs(I[M.FP32][0] / I[M.FP64][0] - 1) < 1e-6  # q = 0: every copy in phase
+
+
+@pytest.mark.parametrize("ext", [".amp", ".ampj"])
+def test_amp_file_round_trip_as_a_leaf(ctx, tmp_path, ext):
+    """A grid saved as a D+ amplitude file and loaded as AmpGridAmplitude gives
+    the same I(q) as the leaf it came from; its scale multiplies the amplitude;
+    the same file read into an FP32 grid stays within the FP32 bound."""
+    amp = globule(300, 1.2, seed=111, extra=SOLVENT)
+    gs, qmax = 24, 4.0
+    Q = np.linspace(0, 4.0, 33)
+    dirs = M.mc_directions(112, 300)
+    g = amp.calculateGrid(ctx, qmax, gs, M.FP64)
+    p = str(tmp_path / ("leaf" + ext))
+    if ext == ".amp":
+        g.save_amp(p, "dpx test grid")
+    else:
+        g.save_ampj(p, params=[1, 333], header="dpx test grid")
+    I0 = M.DomainModel([amp], gs, qmax, M.FP64).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    leaf = M.AmpGridAmplitude(p)
+    assert leaf.header == "dpx test grid"
+    I1 = M.DomainModel([leaf], gs, qmax, M.FP64).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    assert rel(I1, I0) <= 1e-12
+    I2 = M.DomainModel([M.AmpGridAmplitude(p, scale=2.0)], gs, qmax, M.FP64).CalculateIntensityVector(
+        ctx, Q, 0.0, len(dirs), dirs)
+    assert rel(I2, 4.0 * I0) <= 1e-12
+    I3 = M.DomainModel([M.AmpGridAmplitude(p)], gs, qmax, M.FP32).CalculateIntensityVector(
+        ctx, Q, 0.0, len(dirs), dirs)
+    assert rel(I3, I0) <= TOL32
+    with pytest.raises(ValueError):
+        M.DomainModel([M.AmpGridAmplitude(p)], gs + 2, qmax, M.FP64).CalculateIntensityVector(
+            ctx, Q, 0.0, len(dirs), dirs)
