@@ -673,3 +673,44 @@ def test_amp_file_round_trip_as_a_leaf(ctx, tmp_path, ext):
     with pytest.raises(ValueError):
         M.DomainModel([M.AmpGridAmplitude(p)], gs + 2, qmax, M.FP64).CalculateIntensityVector(
             ctx, Q, 0.0, len(dirs), dirs)
+
+
+def test_json_state_runs_end_to_end(ctx, tmp_path):
+    """A D+ JSON state (two populations, a manual symmetry of a PDB file, an
+    amplitude-file leaf) decoded and run: Scale * sum_p w_p I_p + Constant of
+    the same models built by hand."""
+    import json
+    from dpx import state as S
+    amp = globule(120, 0.8, seed=121, extra=VACUUM)
+    pdb = tmp_path / "sub.pdb"
+    with open(pdb, "w") as f:
+        for k, (sym, p) in enumerate(zip(amp.symbols, amp.xyz * 10.0)):
+            f.write("ATOM  %5d  %-3s ALA A   1    %8.3f%8.3f%8.3f  1.00  0.00          %2s\n"
+                    % (k + 1, sym, p[0], p[1], p[2], sym))
+    gs, qmax = 20, 3.0
+    g = amp.calculateGrid(ctx, qmax, gs, M.FP64)
+    g.save_amp(str(tmp_path / "leaf.amp"))
+    loc = {"x": 0, "y": 0, "z": 0, "alpha": 0, "beta": 0, "gamma": 0}
+    leaf = {"Type": "PDB", "Filename": "C:\\\\data\\\\sub.pdb", "Centered": False, "Location": loc,
+            "ExtraParameters": [1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0], "Use_Grid": True}
+    rows = [[0, 0, 0, 0, 0, 0], [2.5, 0, 0, 0, 0, 60], [0, 2.5, 1, 30, 20, 10]]
+    sym = {"Type": ",26", "Location": loc, "Parameters": rows, "ExtraParameters": [0.8], "Children": [leaf],
+           "Use_Grid": False}
+    ampnode = {"Type": "AMP", "Filename": "leaf.amp", "Location": dict(loc, x=1.0), "ExtraParameters": [1.5]}
+    state = {"DomainPreferences": {"GridSize": gs, "qMax": qmax, "OrientationMethod": "Monte Carlo (Mersenne Twister)",
+                                   "OrientationIterations": 300, "Convergence": 0.0, "UseGrid": False},
+             "Domain": {"Scale": 2.0, "Constant": 0.25,
+                        "Populations": [{"PopulationSize": 1.0, "Models": [sym]},
+                                        {"PopulationSize": 0.5, "Models": [ampnode]}]}}
+    job = S.decode(json.dumps(state), base_dir=str(tmp_path))
+    Q = np.linspace(0, 3.0, 31)
+    dirs = M.mc_directions(122, 300)
+    I = job.intensity(ctx, Q, dirs, precision=M.FP64)
+    syms, xyz = S.read_pdb(str(pdb))  # the coordinates as the PDB file rounds them
+    same = M.PDBAmplitude(syms, xyz, [1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0])
+    by_hand1 = M.DomainModel([M.ManualSymmetry(same, rows, scale=0.8, use_grid=False)], gs, qmax, M.FP64)
+    by_hand2 = M.DomainModel([M.AmpGridAmplitude(str(tmp_path / "leaf.amp"), scale=1.5,
+                                                 location=(1.0, 0, 0, 0, 0, 0))], gs, qmax, M.FP64)
+    ref = 2.0 * (by_hand1.CalculateIntensityVector(ctx, Q, 0.0, 300, dirs)
+                 + 0.5 * by_hand2.CalculateIntensityVector(ctx, Q, 0.0, 300, dirs)) + 0.25
+    assert rel(I, ref) <= 1e-9
