@@ -556,7 +556,8 @@ int build_models(int n_models, const void* const* cells, const double* rot, cons
     std::vector<dpx::ModelDev>& md = t.md;
     std::vector<char>& gstage = t.gstage;
     md.assign(n_models, dpx::ModelDev{});
-    std::vector<double> gR, gT, gS;
+    std::vector<double> gR, gT, gS, gW;
+    std::vector<float> gRf;
     std::vector<int> gOff, gA;
     std::vector<int> model_group_base(n_models), model_toff_base(n_models), model_gidx_base(n_models);
     int copy_base = 0;
@@ -570,6 +571,8 @@ int build_models(int n_models, const void* const* cells, const double* rot, cons
         M.plain = (M.R[0] == 1.0 && M.R[4] == 1.0 && M.R[8] == 1.0 && M.R[1] == 0.0 && M.R[2] == 0.0 &&
                    M.R[3] == 0.0 && M.R[5] == 0.0 && M.R[6] == 0.0 && M.R[7] == 0.0 && M.tr[0] == 0.0 &&
                    M.tr[1] == 0.0 && M.tr[2] == 0.0);
+        for (int k = 0; k < 9; ++k) M.Rf[k] = (float)M.R[k];
+        for (int i = 0; i < 3; ++i) M.w[i] = M.R[3 * i] * M.tr[0] + M.R[3 * i + 1] * M.tr[1] + M.R[3 * i + 2] * M.tr[2];
         model_group_base[m] = (int)gOff.size();
         model_gidx_base[m] = (int)gA.size();
         // group copies by identical Euler triples, first-appearance order
@@ -594,6 +597,15 @@ int build_models(int n_models, const void* const* cells, const double* rot, cons
             const double* r = copy_rot + 3 * (copy_base + members[gi][0]);
             euler(r[0], r[1], r[2], R);
             gR.insert(gR.end(), R, R + 9);
+            // FP32 average: C = R_copy R_leaf (the sample's leaf frame is C^T n) and
+            // w = C t_leaf (its leaf phase is q n.w, kept in FP64)
+            double Cm[9], w[3];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    Cm[3 * i + j] = R[3 * i] * M.R[j] + R[3 * i + 1] * M.R[3 + j] + R[3 * i + 2] * M.R[6 + j];
+            for (int i = 0; i < 3; ++i) w[i] = Cm[3 * i] * M.tr[0] + Cm[3 * i + 1] * M.tr[1] + Cm[3 * i + 2] * M.tr[2];
+            for (int k = 0; k < 9; ++k) gRf.push_back((float)Cm[k]);
+            gW.insert(gW.end(), w, w + 3);
             const size_t first = gT.size() / 3;
             gOff.push_back((int)first - model_toff_base[m]);
             for (int c : members[gi]) {
@@ -609,27 +621,38 @@ int build_models(int n_models, const void* const* cells, const double* rot, cons
         copy_base += nc;
     }
     // device layout of the group tables: [R][T][step] (doubles) [off][ap] (ints)
+    // [R][T][step][w] (doubles) [C] (floats) [off][ap] (ints); the ints start at
+    // bytesD + bytesF
     const size_t bytesR = gR.size() * sizeof(double), bytesT = gT.size() * sizeof(double),
-                 bytesS = gS.size() * sizeof(double), bytesO = gOff.size() * sizeof(int),
+                 bytesS = gS.size() * sizeof(double), bytesW = gW.size() * sizeof(double),
+                 bytesF = gRf.size() * sizeof(float), bytesO0 = gOff.size() * sizeof(int),
                  bytesA = gA.size() * sizeof(int);
-    gstage.assign(bytesR + bytesT + bytesS + bytesO + bytesA, 0);
+    const size_t bytesD = bytesR + bytesT + bytesS + bytesW;
+    const size_t bytesO = bytesF + bytesO0;  // everything before the ap ints, after the doubles
+    gstage.assign(bytesD + bytesO + bytesA, 0);
     char* h = gstage.data();
     if (bytesR) std::memcpy(h, gR.data(), bytesR);
     if (bytesT) std::memcpy(h + bytesR, gT.data(), bytesT);
     if (bytesS) std::memcpy(h + bytesR + bytesT, gS.data(), bytesS);
-    if (bytesO) std::memcpy(h + bytesR + bytesT + bytesS, gOff.data(), bytesO);
-    if (bytesA) std::memcpy(h + bytesR + bytesT + bytesS + bytesO, gA.data(), bytesA);
+    if (bytesW) std::memcpy(h + bytesR + bytesT + bytesS, gW.data(), bytesW);
+    if (bytesF) std::memcpy(h + bytesD, gRf.data(), bytesF);
+    if (bytesO0) std::memcpy(h + bytesD + bytesF, gOff.data(), bytesO0);
+    if (bytesA) std::memcpy(h + bytesD + bytesO, gA.data(), bytesA);
     t.oR.assign(n_models, 0);
     t.oT.assign(n_models, 0);
     t.oO.assign(n_models, 0);
     t.oS.assign(n_models, 0);
     t.oA.assign(n_models, 0);
+    t.oW.assign(n_models, 0);
+    t.oF.assign(n_models, 0);
     int groups_seen = 0;
     for (int m = 0; m < n_models; ++m) {
         t.oR[m] = 9 * sizeof(double) * (size_t)groups_seen;
         t.oS[m] = bytesR + bytesT + 3 * sizeof(double) * (size_t)groups_seen;
-        t.oO[m] = bytesR + bytesT + bytesS + sizeof(int) * (size_t)model_group_base[m];
-        t.oA[m] = bytesR + bytesT + bytesS + bytesO + sizeof(int) * (size_t)model_gidx_base[m];
+        t.oW[m] = bytesR + bytesT + bytesS + 3 * sizeof(double) * (size_t)groups_seen;
+        t.oF[m] = bytesD + 9 * sizeof(float) * (size_t)groups_seen;
+        t.oO[m] = bytesD + bytesF + sizeof(int) * (size_t)model_group_base[m];
+        t.oA[m] = bytesD + bytesO + sizeof(int) * (size_t)model_gidx_base[m];
         t.oT[m] = bytesR + 3 * sizeof(double) * (size_t)model_toff_base[m];
         groups_seen += md[m].n_groups;
     }
@@ -643,6 +666,8 @@ void place_models(ModelTables& t, char* dbase) {
         t.md[m].trans = reinterpret_cast<const double*>(dbase + t.oT[m]);
         t.md[m].group_step = reinterpret_cast<const double*>(dbase + t.oS[m]);
         t.md[m].group_ap = reinterpret_cast<const int*>(dbase + t.oA[m]);
+        t.md[m].group_w = reinterpret_cast<const double*>(dbase + t.oW[m]);
+        t.md[m].group_Cf = reinterpret_cast<const float*>(dbase + t.oF[m]);
     }
 }
 

@@ -92,7 +92,7 @@ int check_pdb(const dpx_pdb_desc& d);
 struct ModelTables {
     std::vector<dpx::ModelDev> md;
     std::vector<char> gstage;
-    std::vector<size_t> oR, oT, oO, oS, oA;
+    std::vector<size_t> oR, oT, oO, oS, oA, oW, oF;
 };
 int build_models(int n_models, const void* const* cells, const double* rot, const double* tr, const int* n_copies,
                  const double* copy_rot, const double* copy_tr, const double* sym_scale, ModelTables& t);

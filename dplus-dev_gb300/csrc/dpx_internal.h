@@ -43,6 +43,12 @@ struct ModelDev {
     const double* trans;   // [3 K]
     const double* group_step;  // [3 n_groups] d of a group whose translations are t0 + m d
     const int* group_ap;       // [n_groups] M of such a group (0: an arbitrary list)
+    // FP32 average geometry: per group C = R_copy R_leaf as floats (row-major)
+    // and w = C t_leaf; for a model without groups Rf = R_leaf and w = R_leaf t_leaf
+    const float* group_Cf;     // [9 n_groups]
+    const double* group_w;     // [3 n_groups]
+    float Rf[9];
+    double w[3];
     double sym_scale;
     int plain;             // R is the identity and tr is zero
 };

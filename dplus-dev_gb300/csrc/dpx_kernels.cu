@@ -363,6 +363,155 @@ __device__ void sample_amps(const ModelDev* __restrict__ models, int n_models, i
 }
 
 // --------------------------------------------------------------------------
+// FP32-bulk geometry of the average.  The per-(sample, rotation group) work —
+// the rotated direction, its angles and the plane/node indices — runs in FP32
+// on the SFU-backed FP32 pipes instead of the slow FP64 pipe: the angles come
+// from atan2f (accurate at the poles, unlike acos), the node fractions carry
+// an error near 3e-5 of a cell at 450 cells, well inside the FP32-bulk I(q)
+// bar.  FP64 stays where the phases need it: the sample direction itself, the
+// leaf phase q n.(R_copy R_leaf t_leaf) and the translation phases.
+// --------------------------------------------------------------------------
+constexpr float kPiF = 3.14159265358979f;
+constexpr float k2PiF = 6.28318530717959f;
+
+__device__ Cx<float> interp_plane_f(const float4* __restrict__ g, int ri, float theta, float phi) {
+    const int64_t base = shell_base(ri);
+    const int phiPoints = 6 * ri, thePoints = 3 * ri;
+    // clamped as in interp_plane: every node index stays inside shell ri
+    if (!(theta >= 0.f)) theta = 0.f;
+    if (theta > kPiF) theta = kPiF;
+    if (!(phi >= 0.f)) phi = 0.f;
+    if (phi > k2PiF) phi = k2PiF;
+    const float cells_per_rad = (float)thePoints * (1.f / kPiF);
+    const float xt = theta * cells_per_rad, xp = phi * cells_per_rad;
+    int tI = (int)xt;
+    if (tI > thePoints) tI = thePoints;
+    int pI = (int)xp;
+    const float tTh = xt - (float)tI;
+    float tPh = xp - (float)pI;
+    if (pI >= phiPoints) {
+        pI = 0;
+        tPh = 0.f;
+    }
+    const int pI1 = (pI + 1 == phiPoints) ? 0 : pI + 1;
+    Cx<float> nodes[4];
+#pragma unroll
+    for (int i = -1; i < 3; ++i) {
+        const int v = tI + i;
+        int theInd = v < 0 ? v + thePoints + 1 : (v > thePoints ? v - (thePoints + 1) : v);
+        int64_t c1, c2;
+        if (theInd == tI + i) {
+            c1 = base + phiPoints * theInd + pI;
+            c2 = base + phiPoints * theInd + pI1;
+        } else {
+            if (tI + i > thePoints) theInd = (tI + i) - (thePoints + 1);
+            c1 = base + phiPoints * theInd + pI;
+            c2 = base + phiPoints * theInd + pI1;
+            c1 += ((2 * pI >= phiPoints) ? -phiPoints : phiPoints) / 2;
+            c2 += ((2 * pI1 >= phiPoints) ? -phiPoints : phiPoints) / 2;
+        }
+        Cx<float> v1, d1, v2, d2;
+        load_cell<float>(g, c1, v1, d1);
+        load_cell<float>(g, c2, v2, d2);
+        nodes[i + 1] = hermite<float>(v1, v2, d1, d2, tPh);
+    }
+    Cx<float> ds1, ds2;
+    four_point<float>(nodes[0], nodes[1], nodes[2], nodes[3], ds1, ds2);
+    return hermite<float>(nodes[1], nodes[2], ds1, ds2, tTh);
+}
+
+__device__ void planes_f(const float4* __restrict__ g, int Lp, int fInd, float th, float ph, Cx<float>& pl1,
+                         Cx<float>& pl2, Cx<float>& d1, Cx<float>& d2) {
+    Cx<float> origin, od;
+    load_cell<float>(g, 0, origin, od);
+    Cx<float> p1, p2, p3, p4;
+    if (fInd == 0) {  // the mirrored first shell (Grid.cpp:513-537)
+        float nth = kPiF - th;
+        float nph = ph + kPiF;
+        if (nph >= k2PiF) nph -= k2PiF;
+        if (nth < 0.f) nth = 0.f;
+        if (nth > kPiF) nth = kPiF;
+        p1 = interp_plane_f(g, 1, nth, nph);
+    } else if (fInd == 1) {
+        p1 = origin;
+    } else {
+        p1 = interp_plane_f(g, fInd - 1, th, ph);
+    }
+    p2 = (fInd > 0) ? interp_plane_f(g, fInd, th, ph) : origin;
+    p3 = interp_plane_f(g, fInd + 1, th, ph);
+    p4 = (fInd + 2 < Lp) ? interp_plane_f(g, fInd + 2, th, ph) : p3;
+    four_point<float>(p1, p2, p3, p4, d1, d2);
+    pl1 = p2;
+    pl2 = p3;
+}
+
+template <int MQ>
+__device__ void sample_amps_f32(const ModelDev* __restrict__ models, int n_models, int Lp, int fInd, double theta,
+                                double phi, const double dir[3], int mq, const double* qv, const float* frac,
+                                Cx<float>* A) {
+    const float n0 = (float)dir[0], n1 = (float)dir[1], n2 = (float)dir[2];
+    for (int mi = 0; mi < n_models; ++mi) {
+        const ModelDev& M = models[mi];
+        const float4* g = reinterpret_cast<const float4*>(M.grid);
+        const int ng = M.n_groups > 0 ? M.n_groups : 1;
+        for (int gi = 0; gi < ng; ++gi) {
+            float th = (float)theta, ph = (float)phi;
+            double dotR = 0.0;
+            if (!(M.plain && M.n_groups == 0)) {
+                const float* Cm = M.n_groups > 0 ? M.group_Cf + 9 * gi : M.Rf;
+                const double* w = M.n_groups > 0 ? M.group_w + 3 * gi : M.w;
+                const float t0 = n0 * Cm[0] + n1 * Cm[3] + n2 * Cm[6];
+                const float t1 = n0 * Cm[1] + n1 * Cm[4] + n2 * Cm[7];
+                const float t2 = n0 * Cm[2] + n1 * Cm[5] + n2 * Cm[8];
+                dotR = dir[0] * w[0] + dir[1] * w[1] + dir[2] * w[2];
+                th = atan2f(sqrtf(t0 * t0 + t1 * t1), t2);
+                ph = atan2f(t1, t0);
+                if (ph < 0.f) ph += k2PiF;
+            }
+            Cx<float> pl1, pl2, d1, d2;
+            planes_f(g, Lp, fInd, th, ph, pl1, pl2, d1, d2);
+            Cx<float> val[MQ];
+#pragma unroll
+            for (int k = 0; k < MQ; ++k) {
+                if (k < mq) {
+                    val[k] = hermite<float>(pl1, pl2, d1, d2, frac[k]);
+                    if (dotR != 0.0) val[k] = cmul(val[k], expi<float>(dotR * qv[k]));
+                }
+            }
+            if (M.n_groups > 0) {
+                Cx<float> tp[MQ];
+#pragma unroll
+                for (int k = 0; k < MQ; ++k) tp[k] = {0.f, 0.f};
+                const int ap = M.group_ap ? M.group_ap[gi] : 0;
+                if (ap > 0) {
+                    const double* t0 = M.trans + 3 * M.group_off[gi];
+                    const double* dd = M.group_step + 3 * gi;
+                    const double a0 = dir[0] * t0[0] + dir[1] * t0[1] + dir[2] * t0[2];
+                    const double ad = dir[0] * dd[0] + dir[1] * dd[1] + dir[2] * dd[2];
+#pragma unroll
+                    for (int k = 0; k < MQ; ++k)
+                        if (k < mq) tp[k] = ap_sum<float>(a0 * qv[k], ad * qv[k], ap);
+                } else {
+                    for (int c = M.group_off[gi]; c < M.group_off[gi + 1]; ++c) {
+                        const double* tt = M.trans + 3 * c;
+                        const double a = dir[0] * tt[0] + dir[1] * tt[1] + dir[2] * tt[2];
+#pragma unroll
+                        for (int k = 0; k < MQ; ++k)
+                            if (k < mq) tp[k] = cadd(tp[k], expi<float>(a * qv[k]));
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < MQ; ++k)
+                    if (k < mq) val[k] = cscale(cmul(val[k], tp[k]), (float)M.sym_scale);
+            }
+#pragma unroll
+            for (int k = 0; k < MQ; ++k)
+                if (k < mq) A[k] = cadd(A[k], val[k]);
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
 // Orientation average: one block = one chunk of samples of one bracket.
 // Each thread evaluates one direction: for every model and every docked
 // rotation group, the leaf's 4 planes at the rotated direction, then the
@@ -411,7 +560,12 @@ __global__ void __launch_bounds__(128) average_kernel(int Lp, double step, const
             qv[k] = (k < mq) ? plan.br_q[q0 + qc + k] : 0.0;
             frac[k] = (T)(bump8(qv[k] / step) - (double)fInd);
         }
-        if (valid) sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+        if (valid) {
+            if constexpr (sizeof(T) == 4)
+                sample_amps_f32<MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+            else
+                sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+        }
         // |A|^2, block reduction in FP64
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
