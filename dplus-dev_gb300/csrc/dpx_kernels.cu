@@ -699,7 +699,10 @@ __global__ void __launch_bounds__(128) vegas_points_kernel(int Lp, double step, 
             qv[k] = (k < mq) ? q[qc + k] : 0.0;
             frac[k] = (T)(bump8(qv[k] / step) - (double)fInd);
         }
-        sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+        if constexpr (sizeof(T) == 4)
+            sample_amps_f32<MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+        else
+            sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
 #pragma unroll
         for (int k = 0; k < MQ; ++k)
             if (k < mq)
