@@ -29,6 +29,7 @@ from typing import Sequence
 import numpy as np
 
 from . import models as M
+from . import pdb as P
 
 METHODS = {"Monte Carlo (Mersenne Twister)": "MC", "Adaptive (VEGAS) Monte Carlo": "VEGAS",
            "Adaptive Gauss Kronrod": "GK"}
@@ -49,24 +50,10 @@ def _euler_angles(R):
 
 
 def read_pdb(path: str):
-    """(symbols, xyz in nm) of the ATOM / HETATM records of a PDB file: the
-    coordinate columns 31-54 (Angstrom) and the element of columns 77-78, or of
-    the atom name when those are blank (PDBReaderLib.cpp reads the same fields)."""
-    syms, xyz = [], []
-    with open(path) as f:
-        for line in f:
-            if not (line.startswith("ATOM") or line.startswith("HETATM")):
-                continue
-            x, y, z = float(line[30:38]), float(line[38:46]), float(line[46:54])
-            el = line[76:78].strip() if len(line) >= 78 else ""
-            if not el:
-                name = line[12:16].strip()
-                el = "".join(ch for ch in name if ch.isalpha())[:1]
-            syms.append(el.upper())
-            xyz.append((x / 10.0, y / 10.0, z / 10.0))
-    if not syms:
-        raise ValueError(f"{path}: no ATOM / HETATM records")
-    return syms, np.array(xyz)
+    """(ions, xyz in nm) of a PDB file as D+ reads it (``dpx.pdb.read_pdb``:
+    alternate locations, element and charge columns, implicit-hydrogen groups)."""
+    atoms = P.read_pdb(path)
+    return atoms.symbols, atoms.xyz
 
 
 def _location(node):
@@ -135,10 +122,10 @@ class _Decoder:
     def leaf(self, node):
         t = node.get("Type")
         if t == "PDB":
-            syms, xyz = read_pdb(self.resolve(node["Filename"]))
+            atoms = P.read_pdb(self.resolve(node["Filename"]))
             extra = list(node.get("ExtraParameters", [1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0]))
-            return M.PDBAmplitude(syms, xyz, extra, centered=bool(node.get("Centered", False)),
-                                  location=_location(node))
+            return M.PDBAmplitude(atoms.symbols, atoms.xyz, extra, centered=bool(node.get("Centered", False)),
+                                  location=_location(node), bfactors=atoms.bfactor)
         if t == "AMP":
             extra = node.get("ExtraParameters", [1])
             return M.AmpGridAmplitude(self.resolve(node["Filename"]), scale=float(extra[0] if extra else 1.0),
