@@ -66,17 +66,17 @@ extern const int kFillShapes = 14;
 // Unique-ion form factors minus the Gaussian dummy-atom solvent
 // (Atomic Form Factor.cpp:91-115, 121-176; r_m :11-27) for shells 0..Lp,
 // layout [U][Lp+1].
-void aff_table(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed,
-               double c1, int Lp, double step, std::vector<double>& out) {
+void aff_at(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed, double c1,
+            int nq, const double* qs, std::vector<double>& out) {
     double s3 = 0, n = 0;
     for (int u = 0; u < U; ++u) {
         s3 += rads[u] * rads[u] * rads[u] * api[u];
         n += api[u];
     }
     const double rm = std::cbrt(s3 / n);
-    out.assign((size_t)U * (Lp + 1), 0.0);
-    for (int l = 0; l <= Lp; ++l) {
-        const double q = l * step;
+    out.assign((size_t)U * nq, 0.0);
+    for (int l = 0; l < nq; ++l) {
+        const double q = qs[l];
         const double s2 = q * q / (100.0 * 157.913670417429737901351855998);
         for (int u = 0; u < U; ++u) {
             double f = 0;
@@ -91,9 +91,16 @@ void aff_table(int U, const int* api, const double* coeffs, const double* rads, 
                           sol_ed * c1 * c1 * c1 *
                           std::exp(-0.6822178052976590 * q * q * rm * rm * (c1 * c1 - 1.0));
             }
-            out[(size_t)u * (Lp + 1) + l] = f - solvent;
+            out[(size_t)u * nq + l] = f - solvent;
         }
     }
+}
+
+void aff_table(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed,
+               double c1, int Lp, double step, std::vector<double>& out) {
+    std::vector<double> q(Lp + 1);
+    for (int l = 0; l <= Lp; ++l) q[l] = l * step;
+    aff_at(U, api, coeffs, rads, flags, sol_ed, c1, Lp + 1, q.data(), out);
 }
 
 // Tait-Bryan X1Y2Z3 rotation (the reference's EulerD, Amplitude.h:557-573).
@@ -187,7 +194,7 @@ void ctx_release(dpx_ctx ctx) {
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
-                      &ctx->result, &ctx->dirs})
+                      &ctx->result, &ctx->dirs, &ctx->debye})
         b->release();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;

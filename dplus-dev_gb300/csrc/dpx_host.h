@@ -57,7 +57,7 @@ struct dpx_ctx_s {
     cudaStream_t stream = nullptr;
     int fill_cpt = 8, fill_threads = 128;  // FP32 fill shape (dpx_autotune_fill)
     bool fill_persistent = false;
-    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs;
+    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye;
     std::vector<char> host_stage;
 };
 
@@ -82,6 +82,9 @@ extern const int kFillShapes;
 // Unique-ion form factors minus the dummy-atom solvent for shells 0..Lp, [U][Lp+1].
 void aff_table(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed,
                double c1, int Lp, double step, std::vector<double>& out);
+// The same at the nq values q[k], [U][nq].
+void aff_at(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed, double c1,
+            int nq, const double* q, std::vector<double>& out);
 // Tait-Bryan X1Y2Z3 rotation (EulerD).
 void euler(double a, double b, double c, double R[9]);
 int check_pdb(const dpx_pdb_desc& d);

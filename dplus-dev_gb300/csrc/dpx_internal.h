@@ -136,6 +136,28 @@ cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_model
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
 // SFU calibration: blocks x 256 threads x iters x 8 __sincosf (2 MUFU ops each)
 cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);
+
+// Debye sum of one leaf (dpx_debye.cu).  Atoms padded to a multiple of the
+// 128-atom tile; F tables [nq][npad] of the path's type; partial sums
+// [debye_pair_blocks(npad)][nq].
+struct DebyeArgs {
+    const float4* pos;      // [npad] (x, y, z, 0) nm, padding zero
+    const int* ion;         // [n] ion index per atom
+    const float* bfactor;   // [n] B factors (Debye-Waller) or nullptr
+    const float2* anom;     // [n] (f', f'') or nullptr
+    const double* ff;       // [U][nq] ion form factors minus the dummy-atom solvent
+    const double* q;        // [nq]
+    void* Fr;               // [nq][npad] per-atom form factors (real part)
+    void* Fi;               // [nq][npad] imaginary part (anomalous only)
+    double* partial;        // [pair blocks][nq]
+    double* out;            // [nq]
+    int64_t n, npad;
+    int nq;
+    double scale2;          // I is multiplied by scale^2
+};
+int64_t debye_padded_atoms(int64_t n);
+int debye_pair_blocks(int64_t npad);
+cudaError_t launch_debye(cudaStream_t s, bool fp64, bool anomalous, const DebyeArgs& a);
 // d_res[0] = |origin cell|^2 (I at q = 0 of one plain leaf)
 cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid, double* d_res);
 // d_res[0] = |sum_m w_m A_m(0)|^2 over placed (and docked) models

@@ -130,6 +130,10 @@ _SIGS = {
     "dpx_boxes_space": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dpx_boxes_free": (C.c_int, [_P]),
     "dpx_measure_sfu_peak": (C.c_int, [_P, _D]),
+    "dpx_debye_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), _F, _F, C.c_int, _D, C.c_int, _D]),
+    "dpx_calc_debye_v2": (C.c_int, [C.c_int, C.c_float, C.c_float, _D, C.c_int, _I, _F, C.POINTER(C.c_uint8), _F,
+                                    C.c_int, _F, _F, C.c_int, C.c_int, C.POINTER(C.c_char), _F, C.c_float, C.c_float,
+                                    C.c_int, _I]),
     "dpx_amp_write": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_double, _D]),
     "dpx_amp_read_info": (C.c_int, [C.c_char_p, _I, _D, C.c_char_p, C.c_int64]),
     "dpx_amp_read": (C.c_int, [C.c_char_p, _D]),

@@ -202,22 +202,25 @@ class PDBAmplitude:
     """
 
     def __init__(self, symbols: Sequence[str], xyz_nm: np.ndarray, extra: Sequence[float] | None = None,
-                 centered: bool = False, location: Sequence[float] = (0, 0, 0, 0, 0, 0)):
+                 centered: bool = False, location: Sequence[float] = (0, 0, 0, 0, 0, 0),
+                 bfactors: Sequence[float] | None = None):
         xyz = np.asarray(xyz_nm, dtype=np.float64).reshape(-1, 3)
         if len(symbols) != len(xyz):
             raise ValueError("symbols and coordinates differ in length")
         if len(xyz) == 0:
             raise ValueError("a PDB leaf needs at least one atom")
         ions = [ion(s) for s in symbols]
-        # coordinates are stored as float, as the reference does (PDBAmplitude.h:15)
-        xyz = xyz.astype(np.float32).astype(np.float64)
-        if centered:  # moveCOMToOrigin (PDBReaderLib.cpp:271-293)
+        if centered:  # moveCOMToOrigin (PDBReaderLib.cpp:271-293), on the coordinates as read
             w = np.array([i.weight for i in ions])
             com = (xyz * w[:, None]).sum(0) / w.sum()
-            xyz = (xyz - com).astype(np.float32).astype(np.float64)
+            xyz = xyz - com
+        # coordinates are stored as float, as the reference does (PDBAmplitude.h:15)
+        xyz = xyz.astype(np.float32).astype(np.float64)
         order = sorted(range(len(ions)), key=lambda k: ions[k].ion_key)  # stable, as std::sort by ion index
         self.symbols = [ions[k].symbol for k in order]
         self.xyz = xyz[order]
+        # B factors (Debye-Waller, used by the Debye sum), in the sorted order
+        self.bfactors = None if bfactors is None else np.asarray(bfactors, dtype=np.float64)[order]
         keys = [ions[k].ion_key for k in order]
         uniq, self.atoms_per_ion = [], []
         for k, s in zip(keys, self.symbols):
@@ -569,6 +572,44 @@ class SpaceFillingSymmetry:
 
     def placement(self, ctx, qmax, gridSize, precision):
         return (self.calculateGrid(ctx, qmax, gridSize, precision), self.location, None, 1.0)
+
+
+class DebyeCalTester:
+    """Debye sum of a PDB leaf (DebyeCalTester, PDBAmplitude.cpp:1586-1967; the
+    standalone DebyeCalculator, DebyeCalculator/DebyeCalculator.cpp:83-311): the
+    exact orientation average, no grid.  ``p`` = [solventED, Debye-Waller
+    flag, c1] as the reference's parameter vector (DebyeCalculator.cpp:239-243):
+    dummy-atom solvent when solventED != 0 (with the dummy-atom radii, as
+    PreCalculate selects RAD_DUMMY_ATOMS_ONLY), the leaf's B factors when the
+    flag is above 0.1.  ``anomalous``: [N, 2] (f', f'') per atom in the leaf's
+    ion-sorted order, or None (AnomDebyeCalTester)."""
+
+    def __init__(self, leaf: PDBAmplitude, anomalous: np.ndarray | None = None):
+        self.leaf = leaf
+        self.anomalous = None if anomalous is None else \
+            np.ascontiguousarray(anomalous, dtype=np.float32).reshape(len(leaf.xyz), 2)
+
+    def CalculateVector(self, ctx: Context, q, p: Sequence[float] = (0.0, 0.0, 1.0), precision: int = FP32):
+        pv = list(p) + [0.0, 0.0, 1.0][len(p):]
+        a = self.leaf
+        bf = None
+        if pv[1] > 0.1:
+            if a.bfactors is None:
+                raise ValueError("the Debye-Waller flag needs B factors on the leaf")
+            bf = np.ascontiguousarray(a.bfactors, dtype=np.float32)
+        at = a.atoms_float4()
+        d = _lib.PdbDesc()
+        d.n_atoms, d.atoms, d.atoms_on_device, d.n_ions = len(at), at.ctypes.data, 0, len(a.unique)
+        d.atoms_per_ion, d.coeffs, d.ion_rads = iptr(a.atoms_per_ion), dptr(a.coeffs), dptr(a.ion_rads)
+        d.flags = _lib.DPX_CALC_ATOMIC_FORMFACTORS | (_lib.DPX_CALC_DUMMY_SOLVENT if pv[0] != 0.0 else 0)
+        d.solvent_ed, d.c1, d.scale, d.center = float(pv[0]), float(pv[2]), 1.0, None
+        Q = np.ascontiguousarray(q, dtype=np.float64)
+        out = np.zeros(len(Q))
+        fptr = C.POINTER(C.c_float)
+        check(lib().dpx_debye_intensity(ctx.handle, C.byref(d), None if bf is None else bf.ctypes.data_as(fptr),
+                                        None if self.anomalous is None else self.anomalous.ctypes.data_as(fptr),
+                                        len(Q), dptr(Q), int(precision), dptr(out)))
+        return out
 
 
 class DomainModel:

@@ -27,6 +27,10 @@
  *   dpx_sum_grids_jacob_sphr         <- GPUSumGridsJacobSphrDD (GPUHeader.h:255)
  *   dpx_mc_directions / dpx_layer_seeds <- the mt19937 draws of
  *                                       Amplitude.cpp:757-767, 1171-1173, 2764-2780
+ *   dpx_debye_intensity              <- DebyeCalTester::Calculate / CalculateVectorGPU
+ *                                       (Backend/Backend/PDBAmplitude.cpp:1652-1716, 1789-1967)
+ *   dpx_calc_debye_v2                <- GPUCalcDebyeV2 (Backend/GPU/InternalGPUHeaders.h:61,
+ *                                       DebyeCalculator.cu:164-372)
  */
 #ifndef DPX_H
 #define DPX_H
@@ -239,6 +243,32 @@ int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
                              const double* inD, const double* qs, double* intensities, int qPoints,
                              int64_t maxIters, double convergence, const double* dirs, int64_t dir_layer_stride,
                              int precision, int* pStop);
+/* ---- Debye sum: the exact orientation average of a PDB leaf, no grid ----
+ *   I(q) = scale^2 [sum_i |f_i|^2 + 2 sum_{i<j} Re(f_i conj f_j) sin(q r_ij)/(q r_ij)]
+ * (DebyeCalTester::Calculate, PDBAmplitude.cpp:1789-1825; AnomDebyeCalTester,
+ * :2466-2512).  f_i is the ion's form factor minus its Gaussian dummy-atom
+ * solvent (d->flags, solvent_ed, c1, ion_rads as for the grid fill), plus
+ * anomalous[2i] + i anomalous[2i+1] (f', f'') when anomalous != NULL, times
+ * exp(-bfactors[i] (q/10)^2 / (16 pi^2)) when bfactors != NULL; per-atom
+ * arrays follow d->atoms' (ion-sorted) order.  d must carry no voxel boxes.
+ * Q, I: host [nq].  FP32: FP32 pair terms (SFU sine, Taylor series below
+ * q r = 0.5), FP64 per-tile and cross-block sums; FP64: every step in double.
+ * Device scratch: (nq x N x 4 B, twice with anomalous factors, FP64: 8 B)
+ * on the context, kept for reuse. */
+int dpx_debye_intensity(dpx_ctx ctx, const dpx_pdb_desc* d, const float* bfactors, const float* anomalous, int nq,
+                        const double* Q, int precision, double* I);
+/* GPUCalcDebyeV2 (DebyeCalculator.cu:350-372): numQValues q values
+ * qMin + k (qMax - qMin) / (numQValues - 1) (in float, as the reference);
+ * loc: float4 [numAtoms] nm sorted by ion; atomsPerIon read up to numAtoms;
+ * coeffs [9 x U]; anomalousVals: float2 [numAtoms] or NULL; dummy-atom solvent
+ * (bSol, solvED != 0) with ion radii atmRad[atmInd[first atom of the ion]];
+ * bSolOnly drops the atomic form factors; ionInd is unused (as in the
+ * reference).  B factors are applied when bBfactors is set, as the reference's
+ * CPU Debye does (its GPU kernel ignores them).  outData [numQValues]. */
+int dpx_calc_debye_v2(int numQValues, float qMin, float qMax, double* outData, int numAtoms, const int* atomsPerIon,
+                      const float* loc, const unsigned char* ionInd, const float* anomalousVals, int bBfactors,
+                      const float* BFactors, const float* coeffs, int bSol, int bSolOnly, const char* atmInd,
+                      const float* atmRad, float solvED, float c1, int precision, int* pStop);
 /* GPUCalcManSymJacobSphrDD (Backend/GPU/GPUHeader.h:185, ManSymGenJacob.cu:36-124,
  * called by ManualSymmetry::calculateGrid Symmetries.cpp:943-945).  loc*
  * arrays hold numCopies + 1 entries: entry 0 places the inner object, entries

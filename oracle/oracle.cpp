@@ -1000,6 +1000,99 @@ void orc_assemble_grid(int grid_size, double qmax, int n_leaves, const orc_leaf*
     }
 }
 
+/* Debye sum, DebyeCalTester::Calculate (PDBAmplitude.cpp:1789-1825) and its
+ * anomalous twin (PDBAmplitude.cpp:2466-2512): per-atom form factors at q
+ * (GetAllAFFs, Atomic Form Factor.cpp), plus f' + i f'' when given, times the
+ * Debye-Waller factor exp(-B (q/10)^2 / (16 pi^2)) when B factors are given;
+ * I = sum_i |f_i|^2 + 2 sum_{i<j} Re(f_i conj f_j) sinc(q r_ij).  FP64: every
+ * step in double.  REFEXACT: float form factors, float coordinates and
+ * distances, float sinc with sin(x)/x = NaN -> 1 (SincArrayXf, Amplitude.h:108),
+ * float pair products cast to double and summed in double, the self terms
+ * summed in float, as the reference's Eigen expressions do. */
+void orc_debye(int64_t N, const double* xyz, int U, const int* atoms_per_ion, const double* coeffs,
+               const double* ion_rads, int flags, double sol_ed, double c1, const double* bfactor,
+               const double* anom, int nq, const double* Q, int mode, int nthreads, double* out) {
+    std::vector<int> ion(N);
+    {
+        int64_t j = 0;
+        for (int u = 0; u < U; u++)
+            for (int k = 0; k < atoms_per_ion[u]; k++) ion[j++] = u;
+    }
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    const double rm = mean_radius<double>(U, atoms_per_ion, ion_rads);
+    const float rmf = mean_radius<float>(U, atoms_per_ion, ion_rads);
+    for (int k = 0; k < nq; k++) {
+        const double q = Q[k];
+        if (mode == ORC_REFEXACT) {
+            std::vector<float> aff(U), fr(N), fi(N, 0.f);
+            unique_affs<float>(U, coeffs, rmf, ion_rads, flags, sol_ed, c1, (float)q, aff.data());
+            for (int64_t i = 0; i < N; i++) {
+                fr[i] = aff[ion[i]];
+                if (anom) {
+                    fr[i] += (float)anom[2 * i];
+                    fi[i] = (float)anom[2 * i + 1];
+                }
+                if (bfactor) {
+                    const double q10 = q / 10.0;
+                    const double dw = std::exp(-(bfactor[i] * q10 * q10 / (16. * kPi * kPi)));
+                    fr[i] = (float)(fr[i] * dw);
+                    fi[i] = (float)(fi[i] * dw);
+                }
+            }
+            double res = 0.0;
+#pragma omp parallel for reduction(+ : res) schedule(dynamic, 64)
+            for (int64_t i = 1; i < N; i++) {
+                const float xi = (float)xyz[3 * i], yi = (float)xyz[3 * i + 1], zi = (float)xyz[3 * i + 2];
+                double row = 0.0;
+                for (int64_t j = 0; j < i; j++) {
+                    const float dx = (float)xyz[3 * j] - xi, dy = (float)xyz[3 * j + 1] - yi,
+                                dz = (float)xyz[3 * j + 2] - zi;
+                    const float x = (float)q * std::sqrt(dx * dx + dy * dy + dz * dz);
+                    float sc = std::sin(x) / x;
+                    if (sc != sc) sc = 1.f;
+                    row += (double)(fr[i] * fr[j] + fi[i] * fi[j]) * (double)sc;
+                }
+                res += 2.0 * row;
+            }
+            float self = 0.f;
+            for (int64_t i = 0; i < N; i++) self += fr[i] * fr[i] + fi[i] * fi[i];
+            out[k] = res + (double)self;
+        } else {
+            std::vector<double> aff(U), fr(N), fi(N, 0.0);
+            unique_affs<double>(U, coeffs, rm, ion_rads, flags, sol_ed, c1, q, aff.data());
+            for (int64_t i = 0; i < N; i++) {
+                fr[i] = aff[ion[i]];
+                if (anom) {
+                    fr[i] += anom[2 * i];
+                    fi[i] = anom[2 * i + 1];
+                }
+                if (bfactor) {
+                    const double q10 = q / 10.0;
+                    const double dw = std::exp(-(bfactor[i] * q10 * q10 / (16. * kPi * kPi)));
+                    fr[i] *= dw;
+                    fi[i] *= dw;
+                }
+            }
+            double res = 0.0;
+#pragma omp parallel for reduction(+ : res) schedule(dynamic, 64)
+            for (int64_t i = 1; i < N; i++) {
+                double row = 0.0;
+                for (int64_t j = 0; j < i; j++) {
+                    const double dx = xyz[3 * j] - xyz[3 * i], dy = xyz[3 * j + 1] - xyz[3 * i + 1],
+                                 dz = xyz[3 * j + 2] - xyz[3 * i + 2];
+                    const double x = q * std::sqrt(dx * dx + dy * dy + dz * dz);
+                    const double sc = x == 0.0 ? 1.0 : std::sin(x) / x;
+                    row += (fr[i] * fr[j] + fi[i] * fi[j]) * sc;
+                }
+                res += 2.0 * row;
+            }
+            double self = 0.0;
+            for (int64_t i = 0; i < N; i++) self += fr[i] * fr[i] + fi[i] * fi[i];
+            out[k] = res + self;
+        }
+    }
+}
+
 double orc_gk_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, double q, double eps,
                         int64_t max_depth) {
     std::vector<LeafModel> models;

@@ -144,6 +144,13 @@ void orc_direct_intensity(int64_t N, const double* xyz, int U, const int* atoms_
 double orc_gk_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves,
                         double q, double eps, int64_t max_depth);
 
+/* ---- Debye sum (DebyeCalTester::Calculate, PDBAmplitude.cpp:1789-1825) ----
+ * xyz [3N] nm sorted by ion; bfactor [N] (Debye-Waller) and anom [2N]
+ * (f', f'') per atom or NULL; out [nq].  mode ORC_FP64 / ORC_REFEXACT. */
+void orc_debye(int64_t N, const double* xyz, int U, const int* atoms_per_ion, const double* coeffs,
+               const double* ion_rads, int flags, double sol_ed, double c1, const double* bfactor,
+               const double* anom, int nq, const double* Q, int mode, int nthreads, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,8 @@ def lib():
         L.orc_q_brackets.argtypes = [C.c_int, C.c_double, C.c_int, _D, _I]
         L.orc_direct_intensity.argtypes = [C.c_int64, _D, C.c_int, _I, _D, _D, C.c_int, C.c_double, C.c_double,
                                            C.c_double, C.c_int, _D, _D, C.c_int, _D, C.c_int64, _D, C.c_int, _D]
+        L.orc_debye.argtypes = [C.c_int64, _D, C.c_int, _I, _D, _D, C.c_int, C.c_double, C.c_double, _D, _D,
+                                C.c_int, _D, C.c_int, C.c_int, _D]
         L.orc_gk_intensity.restype = C.c_double
         L.orc_gk_intensity.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(Leaf), C.c_double, C.c_double,
                                        C.c_int64]
@@ -231,6 +233,18 @@ def direct_intensity(s: Struct, Q, dirs, copy_rot=None, copy_tr=None, nthreads=0
                                Q.ctypes.data_as(_D), len(dirs), dirs.ctypes.data_as(_D), nthreads,
                                res.ctypes.data_as(_D))
     return res
+
+
+def debye(s: Struct, Q, bfactor=None, anom=None, mode=FP64, nthreads=0):
+    """Debye I(q) of a leaf (DebyeCalTester::Calculate); bfactor [N] and
+    anom [N, 2] (f', f'') per atom in the leaf's (ion-sorted) order."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    out = np.zeros(len(Q))
+    b = None if bfactor is None else np.ascontiguousarray(bfactor, dtype=np.float64)
+    a = None if anom is None else np.ascontiguousarray(anom, dtype=np.float64).reshape(-1)
+    lib().orc_debye(len(s.xyz), _d(s.xyz), len(s.api), s.api.ctypes.data_as(_I), _d(s.coeffs), _d(s.rads), s.flags,
+                    s.sol_ed, s.c1, _d(b), _d(a), len(Q), _d(Q), mode, nthreads, out.ctypes.data_as(_D))
+    return out
 
 
 def gk_intensity(grid_size, qmax, leaves, q, eps, max_depth):
