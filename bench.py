@@ -119,6 +119,26 @@ def build_inputs():
     return amp, Q, dirs
 
 
+def shape_label(shape) -> str:
+    """'CxT' + 'kN' (N phi columns on the FMA pipe) + 'p' (persistent)."""
+    c, t, persistent = shape[0], shape[1], shape[2]
+    poly = shape[3] if len(shape) > 3 else 0
+    return "%dx%d%s%s" % (c, t, "k%d" % poly if poly else "", "p" if persistent else "")
+
+
+def apply_fill_shape(ctx, spec: str) -> None:
+    """Set the FP32 fill shape from a shape_label string, e.g. 8x128k2."""
+    persistent = spec.endswith("p")
+    body = spec.rstrip("p")
+    poly = 0
+    if "k" in body:
+        body, k = body.split("k")
+        poly = int(k)
+    c, t = (int(x) for x in body.split("x"))
+    ctx.set_fill_shape(c, t, poly)
+    ctx.set_fill_schedule(persistent)
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -144,11 +164,10 @@ def run_dpx(args):
     stream = torch.cuda.Stream()  # a real stream: CUDA events on it see every libdpx launch
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
-    if args.fill_shape:  # CxT, suffix "p" = persistent schedule
-        spec = args.fill_shape
-        c, t = (int(x) for x in spec.rstrip("p").split("x"))
-        ctx.set_fill_shape(c, t)
-        ctx.set_fill_schedule(spec.endswith("p"))
+    if args.fill_shape:
+        apply_fill_shape(ctx, args.fill_shape)
+    if args.fill_method == "harmonic":
+        ctx.set_fill_method(_lib.DPX_FILL_HARMONIC)
 
     amp, Q, dirs = build_inputs()
     sfu_c = C.c_double()
@@ -157,8 +176,7 @@ def run_dpx(args):
     tune = None
     if args.autotune:  # sweep every fill shape on this workload's leaf, keep the fastest
         best, table = M.autotune_fill(ctx, [amp], QMAX, GRID_SIZE, repeats=1)
-        tune = {"best": "%dx%d%s" % (best[0], best[1], "p" if best[2] else ""),
-                "fill_ms": {"%dx%d%s" % (k[0], k[1], "p" if k[2] else ""): round(v, 3) for k, v in table.items()}}
+        tune = {"best": shape_label(best), "fill_ms": {shape_label(k): round(v, 3) for k, v in table.items()}}
     t_vox = time.perf_counter()
     boxes = amp.solvent_boxes()  # voxelization: host, once per structure (PreCalculate)
     voxelize_s = time.perf_counter() - t_vox
@@ -261,15 +279,18 @@ def run_dpx(args):
         spl_ms = float(np.median(times["splines"]))
         P = L.dpx_grid_cells(GRID_SIZE)
         lp = GRID_SIZE // 2 + 3
-        cpt = ctx.fill_shape()[0]
+        cpt, kp = ctx.fill_shape()[0], ctx.fill_shape()[3]
         # row-factored fill: per work item (CPT cells of a theta row, each with its
-        # z-mirror) and atom, 1 + CPT sincos = 2 (1 + CPT) SFU ops
+        # z-mirror) and atom, 1 + CPT sincos = 2 (1 + CPT) sin/cos evaluations
         # (solvent boxes cost the same per work item: their extent factors are cached)
         items = 1 + sum((3 * i // 2 + 1) * ((3 * i + cpt - 1) // cpt) for i in range(1, lp + 1))
         sfu_ops = float(N_ATOMS + n_boxes) * items * 2 * (1 + cpt)
         # SFU roofline: the MUFU throughput this GPU sustains on a calibration
-        # kernel of independent sincos chains (measured here, with the clocks above)
-        sfu_peak = sfu_measured / 1e12  # Tops/s
+        # kernel of independent sincos chains (measured here, with the clocks above).
+        # With kp of the 1 + CPT sincos per item on the FMA pipe, the SFU carries
+        # (1 + CPT - kp) of them, so the evaluation rate it allows is
+        # peak x (1 + CPT) / (1 + CPT - kp).
+        sfu_peak = sfu_measured / 1e12 * (1 + cpt) / (1 + cpt - kp)  # T evaluations/s
         sfu_nominal = 152 * 16 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
         achieved = sfu_ops / (fill_ms / 1e3) / 1e12
         n_brackets = GRID_SIZE // 2
@@ -287,11 +308,12 @@ def run_dpx(args):
             "gpu_launches": args.steps * 4,
             "roofline": {"bound": "sfu",
                          "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] and not n_boxes else "flat"),
-                         "fill_shape": "%dx%d%s" % (ctx.fill_shape()[0], ctx.fill_shape()[1],
-                                                    "p" if ctx.fill_shape()[2] else ""),
+                         "fill_shape": shape_label(ctx.fill_shape()),
                          "achieved": achieved, "peak": sfu_peak,
-                         "unit": "T SFU-op/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
-                         "peak_kind": "measured (sincos calibration kernel, dpx_measure_sfu_peak)",
+                         "unit": "T sin/cos-eval/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
+                         "peak_kind": "measured (sincos calibration kernel, dpx_measure_sfu_peak)"
+                                      + (", x (1+CPT)/(1+CPT-k): k sincos per item on the FMA pipe" if kp else ""),
+                         "sfu_measured": sfu_measured / 1e12,
                          "peak_nominal_16_per_sm_clk": sfu_nominal,
                          "note": "SFU ops = (atoms + solvent boxes) x work items x 2(1+CPT) (row-factored fill); "
                                  "traffic = ncu dram bytes of the profile shape scaled by cells",
@@ -754,7 +776,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dpx", choices=["dpx", "reference"])
-    ap.add_argument("--fill-shape", default="", help="CxT or CxTp (persistent)")
+    ap.add_argument("--fill-shape", default="", help="CxT[kN][p]: N phi columns on the FMA pipe, p = persistent")
+    ap.add_argument("--fill-method", default="direct", choices=["direct", "harmonic"],
+                    help="FP32 amplitude fill: direct sum, or multipole expansion")
     ap.add_argument("--autotune", action="store_true", help="sweep the fill shapes first and use the fastest")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -57,11 +57,13 @@ int set_device(dpx_ctx ctx) {
 size_t cell_bytes(int precision) { return precision == DPX_FP64 ? sizeof(double4_32a) : sizeof(float4); }
 
 // FP32 fill launch shapes the autotuner sweeps: {cells per work item, threads
-// per block (= atoms per shared-memory tile), persistent schedule}.
-extern const int kFillShape[][3] = {{2, 256, 0}, {2, 256, 1}, {4, 128, 0}, {4, 128, 1}, {4, 256, 0}, {4, 256, 1},
-                             {6, 128, 0}, {6, 128, 1}, {6, 256, 0}, {6, 256, 1}, {8, 128, 0}, {8, 128, 1},
-                             {8, 256, 0}, {8, 256, 1}};
-extern const int kFillShapes = 14;
+// per block (= atoms per shared-memory tile), persistent schedule, columns
+// whose sincos run on the FMA pipe}; flat and persistent forms pairwise.
+extern const int kFillShape[][4] = {{2, 256, 0, 0}, {2, 256, 1, 0}, {4, 128, 0, 0}, {4, 128, 1, 0}, {4, 256, 0, 0},
+                                    {4, 256, 1, 0}, {6, 128, 0, 0}, {6, 128, 1, 0}, {6, 256, 0, 0}, {6, 256, 1, 0},
+                                    {8, 128, 0, 0}, {8, 128, 1, 0}, {8, 256, 0, 0}, {8, 256, 1, 0}, {8, 128, 0, 1},
+                                    {8, 128, 1, 1}, {8, 128, 0, 2}, {8, 128, 1, 2}, {8, 128, 0, 3}, {8, 128, 1, 3}};
+extern const int kFillShapes = 20;
 
 // Unique-ion form factors minus the Gaussian dummy-atom solvent
 // (Atomic Form Factor.cpp:91-115, 121-176; r_m :11-27) for shells 0..Lp,
@@ -194,7 +196,7 @@ void ctx_release(dpx_ctx ctx) {
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
-                      &ctx->result, &ctx->dirs, &ctx->debye})
+                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic})
         b->release();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
@@ -231,10 +233,32 @@ int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cpt, int threads) {
         if (kFillShape[k][0] == cpt && kFillShape[k][1] == threads) {
             ctx->fill_cpt = cpt;
             ctx->fill_threads = threads;
+            ctx->fill_poly = 0;
             return DPX_OK;
         }
     return fail(DPX_ERR_ARG, "unsupported fill shape %d cells x %d threads", cpt, threads);
 }
+
+int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    for (int k = 0; k < kFillShapes; ++k)
+        if (kFillShape[k][0] == ctx->fill_cpt && kFillShape[k][1] == ctx->fill_threads &&
+            kFillShape[k][3] == poly_columns) {
+            ctx->fill_poly = poly_columns;
+            return DPX_OK;
+        }
+    return fail(DPX_ERR_ARG, "no %d x %d fill with %d FMA-pipe columns", ctx->fill_cpt, ctx->fill_threads,
+                poly_columns);
+}
+
+int dpx_ctx_set_fill_method(dpx_ctx ctx, int method) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    if (method != DPX_FILL_DIRECT && method != DPX_FILL_HARMONIC) return fail(DPX_ERR_ARG, "unknown fill method %d", method);
+    ctx->fill_method = method;
+    return DPX_OK;
+}
+
+int dpx_ctx_get_fill_method(dpx_ctx ctx) { return ctx ? ctx->fill_method : DPX_ERR_ARG; }
 
 int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
@@ -247,13 +271,14 @@ int dpx_ctx_get_fill_shape(dpx_ctx ctx, int* shape) {
     shape[0] = ctx->fill_cpt;
     shape[1] = ctx->fill_threads;
     shape[2] = ctx->fill_persistent;
+    shape[3] = ctx->fill_poly;
     return DPX_OK;
 }
 
 int dpx_fill_shapes(int* shapes) {
     if (shapes)
         for (int k = 0; k < kFillShapes; ++k)
-            for (int j = 0; j < 3; ++j) shapes[3 * k + j] = kFillShape[k][j];
+            for (int j = 0; j < 4; ++j) shapes[4 * k + j] = kFillShape[k][j];
     return kFillShapes;
 }
 
@@ -339,8 +364,8 @@ int check_pdb(const dpx_pdb_desc& d) {
 
 // Batched fill with an explicit FP32 launch shape; ev0/ev1 (optional) bracket
 // the FP32 fill launch on the context's stream.
-int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int cpt, int threads, bool persistent,
-                    cudaEvent_t ev0, cudaEvent_t ev1) {
+int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int cpt, int threads, int poly,
+                    bool persistent, cudaEvent_t ev0, cudaEvent_t ev1) {
     if (n <= 0 || !grids || !pdbs) return fail(DPX_ERR_ARG, "empty batch");
     dpx_ctx ctx = grids[0] ? grids[0]->ctx : nullptr;
     for (int j = 0; j < n; ++j) {
@@ -365,21 +390,34 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     h.resize(counter_off + 64, 0);
     DPX_CUDA(ctx->atoms.reserve(h.size()));
     const char* dbase = (const char*)ctx->atoms.p;
+    // the leaf tables first: the harmonic fills read their form factors
+    DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h.data(), jobs_off, cudaMemcpyHostToDevice, s));
+    if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
+    std::vector<char> done(n, 0);  // FP32 leaves filled by the harmonic method
+    if (ctx->fill_method == DPX_FILL_HARMONIC)
+        for (int j = 0; j < n; ++j) {
+            if (grids[j]->precision != DPX_FP32) continue;
+            const int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells);
+            if (rc < 0) return rc;
+            done[j] = rc == 0;
+        }
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
     for (int j = 0; j < n; ++j) {
-        if (grids[j]->precision != DPX_FP32) continue;
+        if (grids[j]->precision != DPX_FP32 || done[j]) continue;
         jobs.push_back(make_job(pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, tiles));
         tiles += (lt[j].items + threads - 1) / threads;
     }
-    if (!jobs.empty()) std::memcpy(h.data() + jobs_off, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
-    DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h.data(), counter_off, cudaMemcpyHostToDevice, s));
-    if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
+    if (!jobs.empty()) {
+        std::memcpy(h.data() + jobs_off, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
+        DPX_CUDA(cudaMemcpyAsync(static_cast<char*>(ctx->atoms.p) + jobs_off, h.data() + jobs_off, counter_off - jobs_off,
+                                 cudaMemcpyHostToDevice, s));
+    }
     bool boxes = false;
     for (const dpx::FillJob& J : jobs) boxes |= J.n_boxes > 0;
     cudaError_t e = dpx::launch_fill_f32_batch(s, (const dpx::FillJob*)(dbase + jobs_off), (int)jobs.size(), tiles,
-                                               (unsigned long long*)(dbase + counter_off), cpt, threads, persistent,
-                                               boxes);
+                                               (unsigned long long*)(dbase + counter_off), cpt, threads, poly,
+                                               persistent, boxes);
     if (e != cudaSuccess) return cuda_fail(e, "amplitude fill launch");
     if (ev1) DPX_CUDA(cudaEventRecord(ev1, s));
     for (int j = 0; j < n; ++j) {  // the plain FP64 path: one launch per leaf
@@ -399,8 +437,8 @@ extern "C" {
 int dpx_grid_fill_pdb_batch(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs) {
     if (n <= 0 || !grids || !grids[0]) return fail(DPX_ERR_ARG, "empty batch");
     const dpx_ctx ctx = grids[0]->ctx;
-    return fill_batch_impl(n, grids, pdbs, ctx->fill_cpt, ctx->fill_threads, ctx->fill_persistent, nullptr,
-                           nullptr);
+    return fill_batch_impl(n, grids, pdbs, ctx->fill_cpt, ctx->fill_threads, ctx->fill_poly, ctx->fill_persistent,
+                           nullptr, nullptr);
 }
 
 int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int repeats, int* best,
@@ -420,7 +458,8 @@ int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, in
     for (int k = 0; k < kFillShapes && !rc; ++k) {
         float tot = 0.f;
         for (int r = 0; r <= repeats && !rc; ++r) {  // r = 0 warms up
-            rc = fill_batch_impl(n, grids, pdbs, kFillShape[k][0], kFillShape[k][1], kFillShape[k][2] != 0, e0, e1);
+            rc = fill_batch_impl(n, grids, pdbs, kFillShape[k][0], kFillShape[k][1], kFillShape[k][3],
+                                 kFillShape[k][2] != 0, e0, e1);
             float ms = 0.f;
             if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = fail(DPX_ERR_CUDA, "event timing");
             if (r > 0) tot += ms;
@@ -438,12 +477,14 @@ int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, in
     ctx->fill_cpt = kFillShape[bi][0];
     ctx->fill_threads = kFillShape[bi][1];
     ctx->fill_persistent = kFillShape[bi][2] != 0;
-    if (best) {
-        best[0] = ctx->fill_cpt;
-        best[1] = ctx->fill_threads;
-        best[2] = ctx->fill_persistent;
-    }
-    // leave the grids filled with the chosen shape (every shape gives the same cells)
+    ctx->fill_poly = kFillShape[bi][3];
+    if (best)
+        for (int j = 0; j < 4; ++j) best[j] = kFillShape[bi][j];
+    // leave the grids filled with the chosen shape: shapes with FMA-pipe
+    // columns differ from the SFU ones in the last bits
+    if (bi != kFillShapes - 1)
+        return fill_batch_impl(n, grids, pdbs, ctx->fill_cpt, ctx->fill_threads, ctx->fill_poly, ctx->fill_persistent,
+                               nullptr, nullptr);
     return DPX_OK;
 }
 
@@ -452,7 +493,7 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
                       double solvent_ed, double c1, double scale, const double* center) {
     if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
     dpx_pdb_desc d{n_atoms, atoms, atoms_on_device, n_ions, atoms_per_ion, coeffs, ion_rads, flags,
-                   solvent_ed, c1, scale, center, 0, nullptr};
+                   solvent_ed, c1, scale, center, 0, nullptr, 0.0};
     return dpx_grid_fill_pdb_batch(1, &g, &d);
 }
 
@@ -1252,7 +1293,7 @@ int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, dou
     for (int k = 0; k < numUniqueIons; ++k) rd[k] = ionRads ? ionRads[k] : 0.0;
     dpx_pdb_desc d{numAtoms, atomLocations, 0, numUniqueIons, atomsPerIon, cd.data(), rd.data(),
                    bitCombination & 3, solventED, c1, scale, nullptr, (int64_t)boxes.size() / 8,
-                   boxes.empty() ? nullptr : boxes.data()};
+                   boxes.empty() ? nullptr : boxes.data(), voxStep};
     rc = dpx_grid_fill_pdb_batch(1, &g, &d);
     if (!rc && pStop && *pStop) rc = fail(DPX_ERR_STOPPED, "stopped");
     if (!rc) rc = dpx_grid_read(g, outData, nullptr);

@@ -107,6 +107,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     const bool fp32 = precision == DPX_FP32;
     const int cpt = fp32 ? ctx->fill_cpt : dpx::kFill64Cells, threads = ctx->fill_threads;
     const bool persistent = ctx->fill_persistent;
+    const int poly = ctx->fill_poly;
     if (grid_budget_bytes <= 0) {
         size_t fr = 0, tot = 0;
         DPX_CUDA(cudaMemGetInfo(&fr, &tot));
@@ -258,7 +259,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
             for (int j = j0; j < j1; ++j) boxes |= sp[j].lt.n_boxes > 0;
             e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(A + o_jobs[w]), j1 - j0,
                                            wave_tiles[w], reinterpret_cast<unsigned long long*>(A + o_counter[w]),
-                                           cpt, threads, persistent, boxes);
+                                           cpt, threads, poly, persistent, boxes);
             launches++;
         } else {
             for (int j = j0; j < j1 && e == cudaSuccess; ++j) {

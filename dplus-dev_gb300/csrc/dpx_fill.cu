@@ -95,7 +95,42 @@ __device__ __forceinline__ float sinc_f(float h) {
     return __fdividef(__sinf(h), h);
 }
 
-template <int CPT, int THREADS>
+// sin and cos of x on the FMA pipe, for the columns that the SFU does not
+// take (the SFU is the fill's bound; moving a few of the CPT sincos per item to
+// the FMA pipe, which the SFU path leaves half idle, balances the two).  x is
+// reduced by pi: n = round(x / pi) by the 1.5 * 2^23 shift, pi in two parts
+// (Cody and Waite), y in [-pi/2, pi/2]; sin y = y + y^3 P(y^2) and
+// cos y = 1 + y^2 Q(y^2) with P, Q of degree 3, coefficients fitted for this
+// kernel by error-weighted least squares on Chebyshev nodes (FP32 evaluation:
+// |error| <= 1.1e-7 for sin, 1.6e-7 for cos, against 2^-21.4 for the SFU);
+// then both carry (-1)^n, the low bit of the shifted n.
+__device__ __forceinline__ void sincos_fma(float x, float* s, float* c) {
+    const float nm = fmaf(x, 0.318309886183790672f, 12582912.f);
+    const float n = nm - 12582912.f;
+    float y = fmaf(-n, 3.140625f, x);
+    y = fmaf(-n, 9.67653589793116e-4f, y);
+    const float y2 = y * y;
+    float ps = fmaf(y2, 2.6000548e-06f, -1.98066147e-04f);
+    ps = fmaf(y2, ps, 8.33301712e-03f);
+    ps = fmaf(y2, ps, -1.66666567e-01f);
+    const float sv = fmaf(y * y2, ps, y);
+    float pc = fmaf(y2, 2.31943905e-05f, -1.38559274e-03f);
+    pc = fmaf(y2, pc, 4.16639894e-02f);
+    pc = fmaf(y2, pc, -4.99999315e-01f);
+    const float cv = fmaf(y2, pc, 1.0f);
+    const unsigned flip = __float_as_uint(nm) << 31;
+    *s = __uint_as_float(__float_as_uint(sv) ^ flip);
+    *c = __uint_as_float(__float_as_uint(cv) ^ flip);
+}
+
+// sincos of column k: the first KP columns on the FMA pipe, the rest on the SFU.
+template <int KP>
+__device__ __forceinline__ void column_sincos(int k, float x, float* s, float* c) {
+    if (k < KP) sincos_fma(x, s, c);
+    else __sincosf(x, s, c);
+}
+
+template <int CPT, int THREADS, int KP>
 __device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, int n_boxes, const float (&qx)[CPT],
                                             const float (&qy)[CPT], float qz, float (&cc)[CPT], float (&ss)[CPT],
                                             float (&sc)[CPT], float (&cs)[CPT], float4* __restrict__ s_box) {
@@ -130,7 +165,7 @@ __device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, in
 #pragma unroll
             for (int k = 0; k < CPT; ++k) {
                 float sn, cn;
-                __sincosf(fmaf(qy[k], c.y, qx[k] * c.x), &sn, &cn);
+                column_sincos<KP>(k, fmaf(qy[k], c.y, qx[k] * c.x), &sn, &cn);
                 const float tc = fxy[k] * cn, ts = fxy[k] * sn;
                 tcc[k] = fmaf(tc, wcz, tcc[k]);
                 tss[k] = fmaf(ts, wsz, tss[k]);
@@ -148,7 +183,7 @@ __device__ __forceinline__ void box_sum_f32(const float4* __restrict__ boxes, in
     }
 }
 
-template <int CPT, int THREADS, bool BOXES>
+template <int CPT, int THREADS, bool BOXES, int KP>
 __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, const int* __restrict__ ion_off, int U,
                                           const float* __restrict__ aff, const int64_t* __restrict__ pref,
                                           const float4* __restrict__ boxes, int n_boxes, float4* __restrict__ grid,
@@ -206,7 +241,7 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) {
                     float sn, cn;
-                    __sincosf(fmaf(qy[k], a.y, qx[k] * a.x), &sn, &cn);
+                    column_sincos<KP>(k, fmaf(qy[k], a.y, qx[k] * a.x), &sn, &cn);
                     tcc[k] = fmaf(cn, cz, tcc[k]);
                     tss[k] = fmaf(sn, sz, tss[k]);
                     tsc[k] = fmaf(sn, cz, tsc[k]);
@@ -222,7 +257,7 @@ __device__ __forceinline__ void fill_tile(const float4* __restrict__ atoms, cons
             }
         }
     }
-    if (BOXES && n_boxes > 0) box_sum_f32<CPT, THREADS>(boxes, n_boxes, qx, qy, qz, cc, ss, sc, cs, s_atoms);
+    if (BOXES && n_boxes > 0) box_sum_f32<CPT, THREADS, KP>(boxes, n_boxes, qx, qy, qz, cc, ss, sc, cs, s_atoms);
     if (!active) return;
 
     float fR[CPT], fI[CPT], gR[CPT], gI[CPT];
@@ -267,16 +302,16 @@ __device__ __forceinline__ int job_of_tile(const FillJob* __restrict__ jobs, int
     return lo;
 }
 
-template <int CPT, int THREADS, bool BOXES>
+template <int CPT, int THREADS, bool BOXES, int KP>
 __device__ __forceinline__ void run_tile(const FillJob& J, int64_t tile, float4* s_atoms) {
-    fill_tile<CPT, THREADS, BOXES>(J.atoms, J.ion_off, J.U, J.aff_f32, J.pref, J.boxes, J.n_boxes, J.grid, J.n_items, J.Lp,
+    fill_tile<CPT, THREADS, BOXES, KP>(J.atoms, J.ion_off, J.U, J.aff_f32, J.pref, J.boxes, J.n_boxes, J.grid, J.n_items, J.Lp,
                             J.step, J.cx, J.cy, J.cz, J.use_center, J.scale, J.origin,
                             (tile - J.tile_start) * THREADS + threadIdx.x, s_atoms);
 }
 
 // Persistent form: one CTA per resident slot, tiles of every job pulled from
 // an atomic counter; the job record is staged once per tile in shared memory.
-template <int CPT, int THREADS>
+template <int CPT, int THREADS, int KP>
 __global__ void __launch_bounds__(THREADS) fill_f32_persistent(const FillJob* __restrict__ jobs, int n_jobs,
                                                                int64_t total_tiles,
                                                                unsigned long long* __restrict__ counter) {
@@ -294,7 +329,7 @@ __global__ void __launch_bounds__(THREADS) fill_f32_persistent(const FillJob* __
         const int64_t tile = s_tile;
         if (tile >= total_tiles) break;
         const FillJob J = s_job;
-        run_tile<CPT, THREADS, false>(J, tile, s_atoms);
+        run_tile<CPT, THREADS, false, KP>(J, tile, s_atoms);
     }
 }
 
@@ -302,12 +337,12 @@ __global__ void __launch_bounds__(THREADS) fill_f32_persistent(const FillJob* __
 // scheduler hands out the tiles in order.  BOXES compiles the voxelized-solvent
 // sum in (a batch with boxes runs this form; without, the leaner code keeps
 // the atom loop's registers free).
-template <int CPT, int THREADS, bool BOXES>
+template <int CPT, int THREADS, bool BOXES, int KP>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS) fill_f32_flat(const FillJob* __restrict__ jobs, int n_jobs) {
     __shared__ float4 s_atoms[THREADS];
     const int64_t tile = blockIdx.x;
     const FillJob J = jobs[job_of_tile(jobs, n_jobs, tile)];
-    run_tile<CPT, THREADS, BOXES>(J, tile, s_atoms);
+    run_tile<CPT, THREADS, BOXES, KP>(J, tile, s_atoms);
 }
 
 // --------------------------------------------------------------------------
@@ -466,26 +501,26 @@ __global__ void __launch_bounds__(THREADS) fill_f64_kernel(const float4* __restr
 
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-template <int CPT, int TH>
+template <int CPT, int TH, int KP>
 cudaError_t launch_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
                          unsigned long long* d_counter, bool persistent, bool boxes) {
     if (!persistent || boxes) {
         if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-        if (boxes) fill_f32_flat<CPT, TH, true><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
-        else fill_f32_flat<CPT, TH, false><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
+        if (boxes) fill_f32_flat<CPT, TH, true, KP><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
+        else fill_f32_flat<CPT, TH, false, KP><<<(unsigned)total_tiles, TH, 0, s>>>(d_jobs, n_jobs);
         return cudaGetLastError();
     }
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_f32_persistent<CPT, TH>, TH, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_f32_persistent<CPT, TH, KP>, TH, 0);
     if (e != cudaSuccess) return e;
     int64_t blocks = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
     if (blocks > total_tiles) blocks = total_tiles;
     e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    fill_f32_persistent<CPT, TH><<<(unsigned)blocks, TH, 0, s>>>(d_jobs, n_jobs, total_tiles, d_counter);
+    fill_f32_persistent<CPT, TH, KP><<<(unsigned)blocks, TH, 0, s>>>(d_jobs, n_jobs, total_tiles, d_counter);
     return cudaGetLastError();
 }
 
@@ -498,14 +533,15 @@ int64_t fill_items(const Geom& g, int cpt, int64_t* pref) {
 }
 
 cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
-                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent,
-                                  bool boxes) {
+                                  unsigned long long* d_counter, int cells_per_thread, int block, int poly,
+                                  bool persistent, bool boxes) {
     if (n_jobs <= 0 || total_tiles <= 0) return cudaSuccess;
-#define DPX_FILL_CASE(CPT, TH) \
-    if (cells_per_thread == CPT && block == TH)     \
-        return launch_batch<CPT, TH>(s, d_jobs, n_jobs, total_tiles, d_counter, persistent, boxes);
-    DPX_FILL_CASE(2, 256) DPX_FILL_CASE(4, 128) DPX_FILL_CASE(4, 256) DPX_FILL_CASE(6, 128) DPX_FILL_CASE(6, 256)
-    DPX_FILL_CASE(8, 128) DPX_FILL_CASE(8, 256)
+#define DPX_FILL_CASE(CPT, TH, KP)                                    \
+    if (cells_per_thread == CPT && block == TH && poly == KP)         \
+        return launch_batch<CPT, TH, KP>(s, d_jobs, n_jobs, total_tiles, d_counter, persistent, boxes);
+    DPX_FILL_CASE(2, 256, 0) DPX_FILL_CASE(4, 128, 0) DPX_FILL_CASE(4, 256, 0) DPX_FILL_CASE(6, 128, 0)
+    DPX_FILL_CASE(6, 256, 0) DPX_FILL_CASE(8, 128, 0) DPX_FILL_CASE(8, 256, 0)
+    DPX_FILL_CASE(8, 128, 1) DPX_FILL_CASE(8, 128, 2) DPX_FILL_CASE(8, 128, 3)
 #undef DPX_FILL_CASE
     return cudaErrorInvalidValue;
 }

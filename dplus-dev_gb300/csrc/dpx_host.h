@@ -57,7 +57,9 @@ struct dpx_ctx_s {
     cudaStream_t stream = nullptr;
     int fill_cpt = 8, fill_threads = 128;  // FP32 fill shape (dpx_autotune_fill)
     bool fill_persistent = false;
-    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye;
+    int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
+    int fill_method = 0;  // DPX_FILL_DIRECT / DPX_FILL_HARMONIC
+    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     std::vector<char> host_stage;
 };
 
@@ -76,7 +78,7 @@ int set_device(dpx_ctx ctx);
 void ctx_retain(dpx_ctx ctx);
 void ctx_release(dpx_ctx ctx);
 size_t cell_bytes(int precision);
-extern const int kFillShape[][3];
+extern const int kFillShape[][4];
 extern const int kFillShapes;
 
 // Unique-ion form factors minus the dummy-atom solvent for shells 0..Lp, [U][Lp+1].
@@ -118,6 +120,12 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
 // The FP32 fill job of a staged leaf whose buffer sits at device address dbase.
 dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
                       int64_t tile_start);
+// Harmonic (multipole) FP32 fill of a staged leaf (dpx_harmonic_host.cpp).
+// Returns DPX_OK, 1 when the leaf cannot take it (boxes without their voxel
+// step, an expansion order above the kernels' limit: the caller uses the
+// direct sum), or a negative status.
+int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
+                  void* grid);
 // The FP64 fill launch of a staged leaf.
 cudaError_t launch_leaf_f64(cudaStream_t s, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase,
                             const dpx::Geom& G, void* grid);

@@ -102,8 +102,8 @@ struct FillJob {
 // slot, atomic tile counter d_counter) or flat (one CTA per tile).  boxes: some
 // job carries voxelized-solvent boxes (always the flat form, box code compiled in).
 cudaError_t launch_fill_f32_batch(cudaStream_t s, const FillJob* d_jobs, int n_jobs, int64_t total_tiles,
-                                  unsigned long long* d_counter, int cells_per_thread, int block, bool persistent,
-                                  bool boxes);
+                                  unsigned long long* d_counter, int cells_per_thread, int block, int poly,
+                                  bool persistent, bool boxes);
 cudaError_t launch_fill_f64(cudaStream_t s, const float4* atoms, const int* ion_off, int U, const double* aff,
                             const Geom& g, const int64_t* d_pref, int64_t n_items, const double center[3],
                             double scale, const float4* boxes, int n_boxes, double4_32a* grid);
@@ -136,6 +136,45 @@ cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_model
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
 // SFU calibration: blocks x 256 threads x iters x 8 __sincosf (2 MUFU ops each)
 cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);
+
+// Harmonic (multipole) FP32 fill of one leaf (dpx_harmonic.cu).  Points are
+// float4 (x, y, z nm about the centre, ion index for atoms / weight for voxels).
+struct HarmonicArgs {
+    const float4* pts;      // the point set
+    int64_t n;              // its points
+    int ch;                 // points per chunk (a multiple of 64)
+    int Lp, LM, K;          // shells 1..Lp, l <= LM, K = (LM+1)(LM+2)/2
+    double step;            // q step
+    const int* lmax;        // [Lp+1] l_i
+    const int* imin;        // [LM+1] first shell with l_i >= l
+    const int64_t* joff;    // [LM+1] first J row of order l
+    const float2* ab;       // [K] Legendre recurrence coefficients
+    const float* aff;       // [U][Lp+1] ion form factors (atoms)
+    float2* Y;              // [K][ch]
+    float* J;               // [rows][ch]
+};
+struct HarmonicSynth {
+    const int2* rows;       // (i, t) of every theta row t <= 3i/2, i >= 1
+    int n_rows;
+    const double2* Ca;      // [Lp+1][K] atoms
+    const double2* Cv;      // [Lp+1][K] voxels or nullptr
+    int K, Lp, lmax_host_outer;
+    const int* lmax;
+    const float2* ab;
+    double step;
+    float vox_s;            // voxel edge (nm)
+    double cx, cy, cz;
+    int use_center;
+    float scale;
+    double origin;
+    float4* grid;
+};
+int harmonic_max_l();
+// C [Lp+1][K] (FP64) += the expansion coefficients of points
+// [chunk_off, chunk_off + ch) of the set.
+cudaError_t launch_harmonic_chunk(cudaStream_t s, const HarmonicArgs& a, bool voxels, int64_t chunk_off,
+                                  double2* C);
+cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a);
 
 // Debye sum of one leaf (dpx_debye.cu).  Atoms padded to a multiple of the
 // 128-atom tile; F tables [nq][npad] of the path's type; partial sums

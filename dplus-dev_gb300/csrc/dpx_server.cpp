@@ -389,7 +389,7 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
     for (const dpx::FillJob& J : jobs) boxes |= J.n_boxes > 0;
     cudaError_t e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(d + jobs_at), (int)jobs.size(),
                                                tiles, reinterpret_cast<unsigned long long*>(d + counter_at), cpt32,
-                                               threads, ctx->fill_persistent, boxes);
+                                               threads, ctx->fill_poly, ctx->fill_persistent, boxes);
     if (e != cudaSuccess) return cuda_fail(e, "fill launch");
     if (!jobs.empty()) dl.fill_launches++;
     for (size_t j = 0; j < fresh.size(); ++j) {

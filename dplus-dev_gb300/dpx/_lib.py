@@ -17,6 +17,7 @@ DPX_FP64 = 0
 DPX_FP32 = 1
 DPX_CALC_ATOMIC_FORMFACTORS = 1
 DPX_CALC_DUMMY_SOLVENT = 2
+DPX_FILL_DIRECT, DPX_FILL_HARMONIC = 0, 1
 
 _STATUS = {-1: "DPX_ERR_ARG", -2: "DPX_ERR_CUDA", -3: "DPX_ERR_OOM", -4: "DPX_ERR_STOPPED",
            -5: "DPX_ERR_NODEVICE"}
@@ -40,7 +41,7 @@ class PdbDesc(C.Structure):
     _fields_ = [("n_atoms", C.c_int64), ("atoms", _P), ("atoms_on_device", C.c_int), ("n_ions", C.c_int),
                 ("atoms_per_ion", _I), ("coeffs", _D), ("ion_rads", _D), ("flags", C.c_int),
                 ("solvent_ed", C.c_double), ("c1", C.c_double), ("scale", C.c_double), ("center", _D),
-                ("n_boxes", C.c_int64), ("boxes", _F)]
+                ("n_boxes", C.c_int64), ("boxes", _F), ("voxel_step", C.c_double)]
 
 class SolveDesc(C.Structure):
     """dpx_solve_desc: one solve of a dpx_batch."""
@@ -72,6 +73,9 @@ _SIGS = {
     "dpx_ctx_synchronize": (C.c_int, [_P]),
     "dpx_ctx_set_fill_shape": (C.c_int, [_P, C.c_int, C.c_int]),
     "dpx_ctx_set_fill_schedule": (C.c_int, [_P, C.c_int]),
+    "dpx_ctx_set_fill_poly": (C.c_int, [_P, C.c_int]),
+    "dpx_ctx_set_fill_method": (C.c_int, [_P, C.c_int]),
+    "dpx_ctx_get_fill_method": (C.c_int, [_P]),
     "dpx_ctx_get_fill_shape": (C.c_int, [_P, _I]),
     "dpx_fill_shapes": (C.c_int, [_I]),
     "dpx_grid_cells": (C.c_int64, [C.c_int]),

@@ -49,13 +49,21 @@ class Context:
         check(lib().dpx_ctx_set_fill_schedule(self.handle, int(bool(persistent))))
 
     def fill_shape(self):
-        """(cells_per_thread, threads, persistent) of the FP32 fill."""
-        out = np.zeros(3, dtype=np.int32)
+        """(cells_per_thread, threads, persistent, poly_columns) of the FP32 fill."""
+        out = np.zeros(4, dtype=np.int32)
         check(lib().dpx_ctx_get_fill_shape(self.handle, iptr(out)))
         return tuple(int(v) for v in out)
 
-    def set_fill_shape(self, cells_per_thread: int, threads: int) -> None:
+    def set_fill_shape(self, cells_per_thread: int, threads: int, poly_columns: int = 0) -> None:
         check(lib().dpx_ctx_set_fill_shape(self.handle, cells_per_thread, threads))
+        check(lib().dpx_ctx_set_fill_poly(self.handle, poly_columns))
+
+    def set_fill_method(self, method: int) -> None:
+        """FP32 fill method: _lib.DPX_FILL_DIRECT or _lib.DPX_FILL_HARMONIC."""
+        check(lib().dpx_ctx_set_fill_method(self.handle, int(method)))
+
+    def fill_method(self) -> int:
+        return int(lib().dpx_ctx_get_fill_method(self.handle))
 
     def synchronize(self) -> None:
         check(lib().dpx_ctx_synchronize(self.handle))
@@ -355,26 +363,27 @@ def pdb_descs(leaves: Sequence[PDBAmplitude]):
         if boxes is not None:
             keep.append(boxes)
             d.n_boxes, d.boxes = len(boxes), boxes.ctypes.data_as(C.POINTER(C.c_float))
+            d.voxel_step = a.voxelStep
     return descs, keep
 
 
 def autotune_fill(ctx: Context, leaves: Sequence[PDBAmplitude], qmax: float, gridSize: int, repeats: int = 2):
     """Project autotuner: time every FP32 fill shape on these leaves and keep
-    the fastest in the context.  Returns (best (cpt, threads, persistent),
-    {shape: ms})."""
+    the fastest in the context.  Returns (best (cpt, threads, persistent,
+    poly_columns), {shape: ms})."""
     n_shapes = lib().dpx_fill_shapes(None)
-    shapes = np.zeros(3 * n_shapes, dtype=np.int32)
+    shapes = np.zeros(4 * n_shapes, dtype=np.int32)
     lib().dpx_fill_shapes(iptr(shapes))
     grids = [Grid(ctx, gridSize, qmax, FP32) for _ in leaves]
     descs, keep = pdb_descs(leaves)
     handles = (C.c_void_p * len(grids))(*[g.handle.value for g in grids])
-    best = np.zeros(3, dtype=np.int32)
+    best = np.zeros(4, dtype=np.int32)
     times = np.zeros(n_shapes, dtype=np.float32)
     check(lib().dpx_autotune_fill(len(grids), handles, descs, int(repeats), iptr(best),
                                   times.ctypes.data_as(C.POINTER(C.c_float))))
     for g in grids:
         g.close()
-    table = {tuple(int(v) for v in shapes[3 * k:3 * k + 3]): float(times[k]) for k in range(n_shapes)}
+    table = {tuple(int(v) for v in shapes[4 * k:4 * k + 4]): float(times[k]) for k in range(n_shapes)}
     return tuple(int(v) for v in best), table
 
 

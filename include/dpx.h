@@ -81,9 +81,27 @@ int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cells_per_thread, int threads);
  * hardware hands them out), 1 = persistent (one CTA per resident slot pulling
  * tiles from an atomic counter). */
 int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent);
-/* shape[3] = {cells_per_thread, threads, persistent} in use. */
+/* Phi columns per work item whose sin/cos run as polynomials on the FMA pipe
+ * instead of the SFU (0-3 for the 8 x 128 shape, 0 otherwise; reset to 0 by
+ * dpx_ctx_set_fill_shape).  The SFU bounds the fill and leaves the FMA pipe
+ * half idle, so a few such columns balance the two pipes. */
+int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns);
+/* FP32 fill method.  DPX_FILL_DIRECT: the direct sum over points and cells
+ * (the reference's algorithm, PDBAmplitude.cpp:243-317).  DPX_FILL_HARMONIC:
+ * the same amplitudes by multipole expansion (no counterpart in the
+ * reference): per shell i the plane-wave expansion is cut at order
+ * l_i = ceil(q_i R + 3 (q_i R)^(1/3) + 6) (R the largest point distance from
+ * the centre), the expansion coefficients are a GEMM-shaped sum over the
+ * points, and each theta row is synthesized from them; solvent boxes are
+ * expanded into their voxels (dpx_pdb_desc.voxel_step).  Leaves it cannot take
+ * (device atoms, boxes without a voxel step, orders above 175) use the direct
+ * sum.  FP64 grids always use the direct sum. */
+enum { DPX_FILL_DIRECT = 0, DPX_FILL_HARMONIC = 1 };
+int dpx_ctx_set_fill_method(dpx_ctx ctx, int method);
+int dpx_ctx_get_fill_method(dpx_ctx ctx);
+/* shape[4] = {cells_per_thread, threads, persistent, poly_columns} in use. */
 int dpx_ctx_get_fill_shape(dpx_ctx ctx, int* shape);
-/* The shapes the autotuner sweeps: writes 3 ints per shape (if shapes != NULL)
+/* The shapes the autotuner sweeps: writes 4 ints per shape (if shapes != NULL)
  * and returns their number. */
 int dpx_fill_shapes(int* shapes);
 
@@ -130,6 +148,9 @@ typedef struct dpx_pdb_desc {
      * before the scale. */
     int64_t n_boxes;
     const float* boxes;
+    /* the voxel edge (nm) the boxes were built on; 0 = unknown.  The
+     * harmonic fill expands boxes into voxels and needs it. */
+    double voxel_step;
 } dpx_pdb_desc;
 /* Fills n grids (distinct, one context) from n leaves.  The FP32 grids of the
  * batch share ONE launch over the tiles of every leaf (flat: one CTA per tile;
@@ -140,7 +161,7 @@ int dpx_grid_fill_pdb_batch(int n, const dpx_grid* grids, const dpx_pdb_desc* pd
 /* Autotuner (no counterpart in the reference): fills the batch once per shape
  * of dpx_fill_shapes (after one warm-up fill), times the FP32 fill launch with
  * CUDA events, averages over `repeats`, and keeps the fastest shape in the
- * context.  best[3] (optional) receives it, times_ms[dpx_fill_shapes()]
+ * context.  best[4] (optional) receives it, times_ms[dpx_fill_shapes()]
  * (optional) the average time of each.  The grids end up filled. */
 int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int repeats, int* best,
                       float* times_ms);

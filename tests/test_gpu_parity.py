@@ -499,12 +499,51 @@ def test_fill_schedules_and_autotuner(ctx):
             got.append([g.read(True, False)[0] for g in M.calculate_grids(ctx, leaves, qmax, gs, M.FP32)])
         for x, y in zip(*got):
             assert np.array_equal(x, y)
+    # FMA-pipe columns: flat and persistent identical as well
+    for kp in (1, 2, 3):
+        ctx.set_fill_shape(8, 128, kp)
+        got = []
+        for persistent in (False, True):
+            ctx.set_fill_schedule(persistent)
+            for a in leaves:
+                a._grid = None
+            got.append([g.read(True, False)[0] for g in M.calculate_grids(ctx, leaves, qmax, gs, M.FP32)])
+        for x, y in zip(*got):
+            assert np.array_equal(x, y)
+    ctx.set_fill_schedule(False)
     best, table = M.autotune_fill(ctx, leaves, qmax, gs, repeats=1)
     assert best in table and len(table) == dpx.lib().dpx_fill_shapes(None)
+    assert {(8, 128, 0, k) for k in range(4)} <= set(table)
     assert ctx.fill_shape() == best
     assert all(t > 0 for t in table.values())
     ctx.set_fill_shape(8, 128)
     ctx.set_fill_schedule(False)
+
+
+@pytest.mark.parametrize("kp", [1, 2, 3])
+@pytest.mark.parametrize("extra", [SOLVENT, LAYER])
+def test_fill_fma_pipe_columns_match_oracle(ctx, kp, extra):
+    """Phi columns whose sin/cos run as FMA-pipe polynomials: the grid within
+    the FP32 amplitude bound of the FP64 oracle (atoms, and atoms with the
+    voxelized layer), and I(q) within 1e-4 of the plain FP64 path."""
+    amp = globule(1500, 2.2, seed=90 + kp, extra=extra)
+    gs, qmax = 40, 5.0
+    ctx.set_fill_shape(8, 128, kp)
+    try:
+        g = amp.calculateGrid(ctx, qmax, gs, M.FP32)
+        v, _ = g.read(True, False)
+        ref = O.grid_fill(O.Struct.from_pdb(amp), gs, qmax, O.FP64)  # atoms and boxes
+        assert rel_to_max(v, ref) <= 2e-6
+        Q = np.linspace(0.0, qmax, 41)
+        dirs = M.mc_directions(91, 2000)
+        I = {}
+        for prec in (M.FP32, M.FP64):
+            amp._grid = None
+            I[prec] = M.DomainModel([amp], gs, qmax, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+        assert rel(I[M.FP32], I[M.FP64]) <= TOL32
+    finally:
+        ctx.set_fill_shape(8, 128, 0)
+        amp._grid = None
 
 
 def _batch_case(seed0=80):
