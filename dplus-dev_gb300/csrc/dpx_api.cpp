@@ -198,6 +198,7 @@ void ctx_release(dpx_ctx ctx) {
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
                       &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic})
         b->release();
+    ctx->pinned.release();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }

@@ -8,27 +8,31 @@
 // for real f, the m < 0 terms are the conjugates of the m > 0 ones).  Pbar_lm
 // are the orthonormal associated Legendre functions (Y_lm = Pbar_lm e^{i m phi}).
 // The series is cut at l_i = ceil(x + 3 x^(1/3) + 6), x = q_i R, R the largest
-// |r_j| about the centroid: beyond it j_l(x) is below 1e-7 of its peak.
+// |r_j| about the centre: beyond it j_l(x) is below 1e-7 of its peak.
 //
-// Cost: the direct fill spends one sincos per point and grid cell (divided by
-// four through the row and Friedel symmetries); here a point costs
-// sum_i (l_i + 1) Bessel values and (l_max + 1)^2 / 2 basis values, the
-// analysis is a GEMM-shaped sum (shells x (l, m)) over the points, and the
-// synthesis of a theta row costs O(l_i^2 + cells x l_i) independent of the
-// number of points.
+// Radial bins.  Points are grouped by radius into bins of width
+// delta = 0.7 / q_max (and, for atoms, by ion); within bin b (centre r_b) the
+// radial factor is a degree-5 polynomial in u = (r - r_b) / (delta / 2):
+//   j_l(q_i r) = sum_n T_n(i, b, l) u^n    (interpolation at 6 Chebyshev nodes,
+//                                           error below 2e-8 for q <= q_max)
+// so that C_lm(q_i) = sum_groups F_g(q_i) sum_n T_n(i, b_g, l) M_g[n][lm] with the
+// per-group moments M_g[n][lm] = sum_{j in g} w_j u_j^n Pbar_lm(cos theta_j)
+// e^{-i m phi_j}.  A point costs 6 (l_max+1)(l_max+2)/2 multiply-adds whatever
+// the number of shells, and the radial functions are evaluated once per
+// (shell, bin, node) instead of once per (shell, point).
 //
-// Kernels (per chunk of points, points being atoms or solvent voxels; a chunk
-// is sized so that its basis table stays in L2 while the GEMM re-reads it):
-//   hm_basis   Y[k][j] = Pbar_lm(cos theta_j) e^{-i m phi_j}, k = l(l+1)/2 + m
-//   hm_bessel  J_l[i][j] = f_j(q_i) j_l(q_i r_j)   (upward recurrence for
-//              l <= x, downward continued fraction above)
-//   hm_gemm    C[i][k] += sum_j J_l(k)[i][j] Y[k][j]: FP32 products in 64-point
-//              sub-tiles, Kahan-compensated across sub-tiles, FP64 across chunks
-// then hm_synth writes the grid: per
-// theta row t <= 3i/2 the B_m of both exponentials, the 6i cells by a table of
-// 6i-th roots of unity, the voxel form factor prod_a s sinc(q_a s / 2) on the
-// solvent part (a box of n voxels is exactly the sum of its voxels), the
-// centring phase e^{i q.c} in FP64, and the Friedel mirror row.
+// Kernels:
+//   hm_nodes     j_l at the Chebyshev nodes of every (shell, bin), FP64
+//   hm_fit       T_n(i, b, l) from the node values (inverse Vandermonde)
+//   hm_moments   per unit of <= 1024 points of one group: basis values of a
+//                tile of points in shared memory, then M_unit[n][k] (FP32)
+//   hm_groups    M_g = sum of its units, FP64, stored FP32
+//   hm_contract  C[i][k] = sum_g F_g(q_i) sum_n T_n M_g[n][k], FP64 across groups
+//   hm_synth     per theta row t <= 3i/2: the B_m of both exponentials, the 6i
+//                cells by a table of 6i-th roots of unity, the voxel form
+//                factor prod_a s sinc(q_a s / 2) on the solvent part (a box of
+//                n voxels is exactly the sum of its voxels), the centring
+//                phase e^{i q.c} in FP64, and the Friedel mirror row.
 #include "dpx_internal.h"
 
 #include <cstdint>
@@ -37,201 +41,264 @@ namespace dpx {
 namespace {
 
 constexpr float kFourPi = 12.566370614359172954f;
-constexpr int kGemmShells = 32;  // shells per GEMM block (8 groups of 4)
-constexpr int kGemmM = 64;       // m values per GEMM block (2 per lane)
-constexpr int kGemmSub = 64;     // points per shared-memory sub-tile
+constexpr int kNodes = 6;       // Chebyshev nodes per bin = polynomial degree + 1
+constexpr int kMaxL = 192;      // local recurrence arrays
+constexpr int kMomThreads = 512;  // threads per moments block
+constexpr int kSliceK = 2560;      // (l, m) per moments block: 5 per thread
 
 __device__ __forceinline__ int k_of(int l, int m) { return l * (l + 1) / 2 + m; }
-
-// ---------------------------------------------------------------------------
-// hm_basis: thread (point j of the chunk, order m); padding points write zeros.
-// ab[k] = {a_lm, b_lm} of the recurrence Pbar_lm = a (x Pbar_{l-1,m} - b Pbar_{l-2,m}).
-// ---------------------------------------------------------------------------
-__global__ void hm_basis(const float4* __restrict__ pts, int64_t n, int64_t chunk_off, int ch, int LM,
-                         const float2* __restrict__ ab, float2* __restrict__ Y) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int m = blockIdx.y;
-    if (j >= ch) return;
-    const int64_t g = chunk_off + j;
-    float ct = 1.f, st = 0.f, ph = 0.f;
-    const bool valid = g < n;
-    if (valid) {
-        const float4 p = pts[g];
-        const float rxy = sqrtf(fmaf(p.x, p.x, p.y * p.y));
-        const float r = sqrtf(fmaf(p.z, p.z, rxy * rxy));
-        if (r > 0.f) {
-            ct = p.z / r;
-            st = rxy / r;
-            ph = atan2f(p.y, p.x);
-        }
-    }
-    float pmm = 0.28209479177387814347f;  // 1 / sqrt(4 pi)
-    for (int mm = 1; mm <= m; ++mm) pmm = -sqrtf((2.f * mm + 1.f) / (2.f * mm)) * st * pmm;
-    float sm, cm;
-    sincosf((float)m * ph, &sm, &cm);  // e^{-i m phi}, accurate argument reduction
-    const float er = valid ? cm : 0.f, ei = valid ? -sm : 0.f;
-    float p2 = 0.f, p1 = pmm;
-    Y[(int64_t)k_of(m, m) * ch + j] = make_float2(p1 * er, p1 * ei);
-    for (int l = m + 1; l <= LM; ++l) {
-        const float2 c = ab[k_of(l, m)];
-        const float p0 = c.x * fmaf(ct, p1, -c.y * p2);
-        Y[(int64_t)k_of(l, m) * ch + j] = make_float2(p0 * er, p0 * ei);
-        p2 = p1;
-        p1 = p0;
-    }
+__device__ __forceinline__ int l_of(int k) {
+    int l = (int)((sqrtf(8.f * (float)k + 1.f) - 1.f) * 0.5f);
+    while (k_of(l + 1, 0) <= k) ++l;
+    while (k_of(l, 0) > k) --l;
+    return l;
 }
 
 // ---------------------------------------------------------------------------
-// hm_bessel: thread (point j of the chunk, shell i >= 1).  J_l rows are the
-// shells i >= imin[l]; J_l starts at joff[l] (in units of ch).
-// The weight of a point is its ion's form factor at q_i (atoms: w holds the
-// ion index) or its solvent weight in e/nm^3 (voxels).
+// hm_nodes: thread (shell i >= 1, bin b, node c).  j_l(x), l <= l_i, in FP64:
+// upward recurrence for l <= floor(x), the continued fraction
+// r_l = x / (2l + 1 - x r_{l+1}) (started 16 orders above) for the ratios above.
+// Jn[((i * nbins + b) * kNodes + c) * (LM + 1) + l].
 // ---------------------------------------------------------------------------
-constexpr int kMaxL = 192;
-
-template <bool VOXELS>
-__global__ void hm_bessel(const float4* __restrict__ pts, int64_t n, int64_t chunk_off, int ch, int Lp, double step,
-                          const int* __restrict__ lmax, const int* __restrict__ imin, const int64_t* __restrict__ joff,
-                          const float* __restrict__ aff, float* __restrict__ J) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y + 1;
-    if (j >= ch) return;
+__global__ void hm_nodes(int Lp, int nbins, int LM, double step, double delta, const int* __restrict__ lmax,
+                         const double* __restrict__ nodes, double* __restrict__ Jn) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)Lp * nbins * kNodes;
+    if (e >= total) return;
+    const int c = (int)(e % kNodes);
+    const int b = (int)((e / kNodes) % nbins);
+    const int i = (int)(e / ((int64_t)kNodes * nbins)) + 1;
     const int li = lmax[i];
-    const int64_t g = chunk_off + j;
-    float w = 0.f, r = 0.f;
-    if (g < n) {
-        const float4 p = pts[g];
-        r = sqrtf(fmaf(p.x, p.x, fmaf(p.y, p.y, p.z * p.z)));
-        w = VOXELS ? p.w : aff[(int64_t)(int)p.w * (Lp + 1) + i];
-    }
-    const float x = (float)((double)i * step) * r;
-    auto put = [&](int l, float v) { J[(joff[l] + (int64_t)(i - imin[l])) * ch + j] = w * v; };
-    if (w == 0.f) {
-        for (int l = 0; l <= li; ++l) put(l, 0.f);
+    double* out = Jn + (((int64_t)i * nbins + b) * kNodes + c) * (LM + 1);
+    const double x = (double)i * step * ((b + 0.5) * delta + nodes[c] * 0.5 * delta);
+    if (x < 1e-8) {
+        out[0] = 1.0;
+        for (int l = 1; l <= li; ++l) out[l] = 0.0;
         return;
     }
-    if (x < 1e-3f) {  // j_0 = 1 - x^2/6, j_1 = x/3, higher orders below 1e-10
-        put(0, 1.f - x * x / 6.f);
-        if (li >= 1) put(1, x / 3.f);
-        for (int l = 2; l <= li; ++l) put(l, 0.f);
-        return;
-    }
-    float s, c;
-    sincosf(x, &s, &c);
-    const float ix = 1.f / x;
-    const float j0 = s * ix;
-    // l <= L0 = floor(x): upward recurrence, stable below the turning point
+    double s, co;
+    sincos(x, &s, &co);
+    const double ix = 1.0 / x;
+    const double j0 = s * ix;
+    out[0] = j0;
     const int L0 = min((int)x, li);
-    put(0, j0);
-    float jm = j0, jc = 0.f;
+    double jm = j0, jc = j0;
     if (L0 >= 1) {
-        jc = (j0 - c) * ix;  // j_1
-        put(1, jc);
+        jc = (j0 - co) * ix;
+        out[1] = jc;
         for (int l = 1; l < L0; ++l) {
-            const float jn = (2.f * l + 1.f) * ix * jc - jm;
-            put(l + 1, jn);
+            const double jn = (2.0 * l + 1.0) * ix * jc - jm;
+            out[l + 1] = jn;
             jm = jc;
             jc = jn;
         }
-    } else {
-        jc = j0;
     }
     if (L0 >= li) return;
-    // l > L0: ratios r_l = j_l / j_{l-1} by the continued fraction
-    // r_l = x / (2l + 1 - x r_{l+1}), started 16 orders above the last one needed
     const int top = min(li + 16, kMaxL - 1);
-    float rr[kMaxL];
-    float rn = 0.f;
+    double rr[kMaxL];
+    double rn = 0.0;
     for (int l = top; l > L0; --l) {
-        rn = x / (2.f * l + 1.f - x * rn);
+        rn = x / (2.0 * l + 1.0 - x * rn);
         if (l <= li) rr[l] = rn;
     }
-    float v = jc;  // j_{L0}
+    double v = jc;
     for (int l = L0 + 1; l <= li; ++l) {
         v *= rr[l];
-        put(l, v);
+        out[l] = v;
     }
 }
 
+// hm_fit: thread (shell i >= 1, bin b, l <= l_i): T[((i nbins + b)(LM+1) + l) * 8 + n].
+__global__ void hm_fit(int Lp, int nbins, int LM, const int* __restrict__ lmax, const double* __restrict__ vinv,
+                       const double* __restrict__ Jn, float* __restrict__ T) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)Lp * nbins * (LM + 1);
+    if (e >= total) return;
+    const int l = (int)(e % (LM + 1));
+    const int b = (int)((e / (LM + 1)) % nbins);
+    const int i = (int)(e / ((int64_t)(LM + 1) * nbins)) + 1;
+    float* out = T + (((int64_t)i * nbins + b) * (LM + 1) + l) * 8;
+    if (l > lmax[i]) {
+        for (int n = 0; n < 8; ++n) out[n] = 0.f;
+        return;
+    }
+    const double* jn = Jn + (((int64_t)i * nbins + b) * kNodes) * (LM + 1) + l;
+    double v[kNodes];
+    for (int c = 0; c < kNodes; ++c) v[c] = jn[(int64_t)c * (LM + 1)];
+    for (int n = 0; n < kNodes; ++n) {
+        double t = 0.0;
+        for (int c = 0; c < kNodes; ++c) t += vinv[n * kNodes + c] * v[c];
+        out[n] = (float)t;
+    }
+    out[6] = out[7] = 0.f;
+}
+
 // ---------------------------------------------------------------------------
-// hm_gemm: block (m tile, shell tile, l); 256 threads = 8 shell groups of 4
-// shells x 32 lanes of 2 m each.  C[i][k] (FP64) += the chunk's sum; every
-// element has one owner per chunk and the chunks run in order.
+// hm_moments: block (unit, k slice); units[u] = {first point, count, bin, 0}.
+// Points: float4 (x, y, z, weight) about the centre, sorted by group.
+// MP[u][n][k] (FP32) = sum over the unit's points of w u^n Pbar_lm e^{-i m phi}.
+// Dynamic shared memory: tp x kk float2 basis values (kk = the slice width),
+// tp x 8 weights w u^n and tp x 4 angles.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) hm_gemm(const float* __restrict__ J, const float2* __restrict__ Y, int ch,
-                                               int Lp, int K, const int* __restrict__ imin,
-                                               const int64_t* __restrict__ joff, double2* __restrict__ C) {
-    __shared__ __align__(16) float sJ[kGemmSub][kGemmShells + 4];
-    __shared__ float2 sY[kGemmSub][kGemmM + 1];
-    const int l = blockIdx.z;
-    const int m0 = blockIdx.x * kGemmM;
-    if (m0 > l) return;
-    const int i_lo = imin[l];
-    const int rows = Lp - i_lo + 1;  // shells with l_i >= l
-    const int s0 = blockIdx.y * kGemmShells;
-    if (s0 >= rows) return;
-    const int t = threadIdx.x, lane = t & 31, grp = t >> 5;
-    const float* Jl = J + joff[l] * ch;
-    const int64_t kb = (int64_t)k_of(l, 0);
-    float ar[4][2], ai[4][2], sr[4][2], si[4][2], cr[4][2], ci[4][2];
+__global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units,
+                                                  int LM, int K, int kk, int tp, float delta,
+                                                  const float2* __restrict__ ab, const float* __restrict__ nmm,
+                                                  float2* __restrict__ MP) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    // regions at 16-byte boundaries: tp x kk float2 may be an odd multiple of 8 bytes
+    float2* sY = reinterpret_cast<float2*>(smem);
+    const size_t oW = ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16;
+    float* sW = reinterpret_cast<float*>(smem + oW);
+    float4* sA = reinterpret_cast<float4*>(smem + oW + (size_t)tp * 8 * sizeof(float));
+    const int4 un = units[blockIdx.x];
+    const int k_lo = blockIdx.y * kSliceK, k_hi = min(K, k_lo + kSliceK);
+    const float rb = (un.z + 0.5f) * delta, ih = 2.f / delta;
+    float2 acc[kSliceK / kMomThreads][kNodes];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int s = 0; s < kSliceK / kMomThreads; ++s)
 #pragma unroll
-        for (int b = 0; b < 2; ++b) ar[a][b] = ai[a][b] = sr[a][b] = si[a][b] = cr[a][b] = ci[a][b] = 0.f;
-    for (int j0 = 0; j0 < ch; j0 += kGemmSub) {
+        for (int n = 0; n < kNodes; ++n) acc[s][n] = make_float2(0.f, 0.f);
+    for (int p0 = 0; p0 < un.y; p0 += tp) {
+        const int np = min(tp, un.y - p0);
         __syncthreads();
-        // stage J rows s0..s0+31 and Y columns m0..m0+63 for points j0..j0+63
-        for (int e = t; e < kGemmSub * kGemmShells; e += 256) {
-            const int sh = e / kGemmSub, jj = e % kGemmSub;
-            sJ[jj][sh] = (s0 + sh < rows) ? Jl[(int64_t)(s0 + sh) * ch + j0 + jj] : 0.f;
-        }
-        for (int e = t; e < kGemmSub * kGemmM; e += 256) {
-            const int mm = e / kGemmSub, jj = e % kGemmSub;
-            sY[jj][mm] = (m0 + mm <= l) ? Y[(kb + m0 + mm) * ch + j0 + jj] : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int jj = 0; jj < kGemmSub; ++jj) {
-            const float4 jv = *reinterpret_cast<const float4*>(&sJ[jj][grp * 4]);
-            const float2 y0 = sY[jj][lane], y1 = sY[jj][lane + 32];
-            const float js[4] = {jv.x, jv.y, jv.z, jv.w};
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                ar[a][0] = fmaf(js[a], y0.x, ar[a][0]);
-                ai[a][0] = fmaf(js[a], y0.y, ai[a][0]);
-                ar[a][1] = fmaf(js[a], y1.x, ar[a][1]);
-                ai[a][1] = fmaf(js[a], y1.y, ai[a][1]);
+        // per point: angles and the weights w u^n
+        for (int p = threadIdx.x; p < np; p += blockDim.x) {
+            const float4 q = pts[un.x + p0 + p];
+            const float rxy = sqrtf(fmaf(q.x, q.x, q.y * q.y));
+            const float r = sqrtf(fmaf(q.z, q.z, rxy * rxy));
+            float4 a = make_float4(1.f, 0.f, 0.f, 0.f);  // cos theta, sin theta, phi
+            if (r > 0.f) a = make_float4(q.z / r, rxy / r, atan2f(q.y, q.x), 0.f);
+            sA[p] = a;
+            const float u = (r - rb) * ih;
+            float wn = q.w;
+            for (int n = 0; n < kNodes; ++n) {
+                sW[p * 8 + n] = wn;
+                wn *= u;
             }
         }
-        // Kahan-compensated running sums of the 64-point partial sums
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 2; ++b) {
-                float y = ar[a][b] - cr[a][b];
-                float tt = sr[a][b] + y;
-                cr[a][b] = (tt - sr[a][b]) - y;
-                sr[a][b] = tt;
-                y = ai[a][b] - ci[a][b];
-                tt = si[a][b] + y;
-                ci[a][b] = (tt - si[a][b]) - y;
-                si[a][b] = tt;
-                ar[a][b] = ai[a][b] = 0.f;
+        __syncthreads();
+        // basis columns (point p, orders m and LM - m in one thread: equal work):
+        // Pbar_mm = nmm[m] (-sin theta)^m, then the l recurrence over the slice
+        // items (column pair c, point p), p fastest: the lanes of a warp share
+        // one or two columns (broadcast coefficient loads) and write rows p of
+        // stride kk = 1 mod 16 float2 (no bank conflicts)
+        const int half = LM / 2 + 1;
+        for (int it = threadIdx.x; it < np * half; it += blockDim.x) {
+            const int p = it % np, cpair = it / np;
+            const float4 a = sA[p];
+            float2* y = sY + (size_t)p * kk - k_lo;
+            for (int side = 0; side < 2; ++side) {
+                const int m = side == 0 ? cpair : LM - cpair;
+                if (side == 1 && m == cpair) break;
+                if (k_of(LM, m) < k_lo || k_of(m, m) >= k_hi) continue;
+                float pw = nmm[m];
+                for (int mm = 0; mm < m; ++mm) pw *= -a.y;
+                float sm, cm;
+                sincosf((float)m * a.z, &sm, &cm);
+                float p2 = 0.f, p1 = pw;
+                int k = k_of(m, m);
+                if (k >= k_lo) y[k] = make_float2(p1 * cm, -p1 * sm);
+                for (int l = m + 1; l <= LM; ++l) {
+                    k = k_of(l, m);
+                    if (k >= k_hi) break;
+                    const float2 c = ab[k];
+                    const float pn = c.x * fmaf(a.x, p1, -c.y * p2);
+                    if (k >= k_lo) y[k] = make_float2(pn * cm, -pn * sm);
+                    p2 = p1;
+                    p1 = pn;
+                }
             }
+        }
+        __syncthreads();
+        for (int p = 0; p < np; ++p) {
+            float w[kNodes];
+#pragma unroll
+            for (int n = 0; n < kNodes; ++n) w[n] = sW[p * 8 + n];
+            const float2* yp = sY + (size_t)p * kk;
+#pragma unroll
+            for (int s = 0; s < kSliceK / kMomThreads; ++s) {
+                const int kl = s * kMomThreads + threadIdx.x;
+                if (k_lo + kl >= k_hi) continue;
+                const float2 y = yp[kl];
+#pragma unroll
+                for (int n = 0; n < kNodes; ++n) {
+                    acc[s][n].x = fmaf(w[n], y.x, acc[s][n].x);
+                    acc[s][n].y = fmaf(w[n], y.y, acc[s][n].y);
+                }
+            }
+        }
     }
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const int row = s0 + grp * 4 + a;
-        if (row >= rows) continue;
-        const int i = i_lo + row;
+    for (int s = 0; s < kSliceK / kMomThreads; ++s) {
+        const int k = k_lo + s * kMomThreads + threadIdx.x;
+        if (k >= k_hi) continue;
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const int m = m0 + lane + 32 * b;
-            if (m > l) continue;
-            double2& c = C[(int64_t)i * K + kb + m];
-            c.x += (double)sr[a][b] - (double)cr[a][b];
-            c.y += (double)si[a][b] - (double)ci[a][b];
+        for (int n = 0; n < kNodes; ++n) MP[((int64_t)blockIdx.x * kNodes + n) * K + k] = acc[s][n];
+    }
+}
+
+// hm_groups: M[g][n][k] = sum of MP over the units [gu[g], gu[g+1]) of group g, FP64.
+__global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, int G, int K,
+                          float2* __restrict__ M) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t per = (int64_t)kNodes * K;
+    if (e >= (int64_t)G * per) return;
+    const int g = (int)(e / per);
+    const int64_t r = e % per;
+    double re = 0.0, im = 0.0;
+    for (int u = gu[g]; u < gu[g + 1]; ++u) {
+        const float2 v = MP[(int64_t)u * per + r];
+        re += (double)v.x;
+        im += (double)v.y;
+    }
+    M[e] = make_float2((float)re, (float)im);
+}
+
+// ---------------------------------------------------------------------------
+// hm_contract: block (k slice of 128, tile of 8 shells); thread k.
+// groups[g] = {bin, ion (< 0: factor 1)}; C[i][k] = sum_g F sum_n T M.
+// ---------------------------------------------------------------------------
+constexpr int kContractShells = 8;
+
+__global__ void __launch_bounds__(128) hm_contract(const float2* __restrict__ M, const int2* __restrict__ groups, int G,
+                                                   const float* __restrict__ T, int nbins, int LM, int K, int Lp,
+                                                   const int* __restrict__ lmax, const float* __restrict__ aff,
+                                                   double2* __restrict__ C) {
+    const int k = blockIdx.x * 128 + threadIdx.x;
+    const int i0 = 1 + blockIdx.y * kContractShells;
+    if (k >= K) return;
+    const int l = l_of(k);
+    double cr[kContractShells], ci[kContractShells];
+#pragma unroll
+    for (int a = 0; a < kContractShells; ++a) cr[a] = ci[a] = 0.0;
+    for (int g = 0; g < G; ++g) {
+        const int2 gb = groups[g];
+        float2 mv[kNodes];
+#pragma unroll
+        for (int n = 0; n < kNodes; ++n) mv[n] = M[((int64_t)g * kNodes + n) * K + k];
+#pragma unroll
+        for (int a = 0; a < kContractShells; ++a) {
+            const int i = i0 + a;
+            if (i > Lp || lmax[i] < l) continue;
+            const float4* t4 = reinterpret_cast<const float4*>(T + (((int64_t)i * nbins + gb.x) * (LM + 1) + l) * 8);
+            const float4 ta = t4[0], tb = t4[1];
+            const float t[kNodes] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y};
+            float sr = 0.f, si = 0.f;
+#pragma unroll
+            for (int n = 0; n < kNodes; ++n) {
+                sr = fmaf(t[n], mv[n].x, sr);
+                si = fmaf(t[n], mv[n].y, si);
+            }
+            const float f = gb.y < 0 ? 1.f : aff[(int64_t)gb.y * (Lp + 1) + i];
+            cr[a] += (double)(f * sr);
+            ci[a] += (double)(f * si);
         }
+    }
+#pragma unroll
+    for (int a = 0; a < kContractShells; ++a) {
+        const int i = i0 + a;
+        if (i > Lp) continue;
+        C[(int64_t)i * K + k] = make_double2(cr[a], ci[a]);
     }
 }
 
@@ -247,7 +314,8 @@ __device__ __forceinline__ float sinc_h(float h) {
 // the 6i roots of unity.
 // ---------------------------------------------------------------------------
 __global__ void hm_synth(const int2* __restrict__ rows, const double2* __restrict__ Ca, const double2* __restrict__ Cv,
-                         int K, const int* __restrict__ lmax, const float2* __restrict__ ab, double step,
+                         int K, const int* __restrict__ lmax, const float2* __restrict__ ab,
+                         const float* __restrict__ nmm, double step,
                          float vox_s, double cx, double cy, double cz, int use_center, float scale, double origin,
                          float4* __restrict__ grid) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -267,8 +335,8 @@ __global__ void hm_synth(const int2* __restrict__ rows, const double2* __restric
     sincospif((float)t / (float)h, &st, &ct);
     // Legendre column m per thread
     for (int m = threadIdx.x; m <= li; m += blockDim.x) {
-        float pmm = 0.28209479177387814347f;
-        for (int mm = 1; mm <= m; ++mm) pmm = -sqrtf((2.f * mm + 1.f) / (2.f * mm)) * st * pmm;
+        float pmm = nmm[m];
+        for (int mm = 0; mm < m; ++mm) pmm *= -st;
         float p2 = 0.f, p1 = pmm;
         sP[k_of(m, m)] = p1;
         for (int l = m + 1; l <= li; ++l) {
@@ -379,20 +447,33 @@ __global__ void hm_synth(const int2* __restrict__ rows, const double2* __restric
 }  // namespace
 
 int harmonic_max_l() { return kMaxL - 17; }
+int harmonic_nodes() { return kNodes; }
 
-cudaError_t launch_harmonic_chunk(cudaStream_t s, const HarmonicArgs& a, bool voxels, int64_t chunk_off,
-                                  double2* C) {
-    const int ch = a.ch;
-    hm_basis<<<dim3((ch + 127) / 128, a.LM + 1), 128, 0, s>>>(a.pts, a.n, chunk_off, ch, a.LM, a.ab, a.Y);
-    if (voxels)
-        hm_bessel<true><<<dim3((ch + 127) / 128, a.Lp), 128, 0, s>>>(a.pts, a.n, chunk_off, ch, a.Lp, a.step, a.lmax,
-                                                                     a.imin, a.joff, a.aff, a.J);
-    else
-        hm_bessel<false><<<dim3((ch + 127) / 128, a.Lp), 128, 0, s>>>(a.pts, a.n, chunk_off, ch, a.Lp, a.step,
-                                                                      a.lmax, a.imin, a.joff, a.aff, a.J);
-    const int mt = (a.LM + kGemmM) / kGemmM;
-    const int st = (a.Lp + kGemmShells - 1) / kGemmShells;
-    hm_gemm<<<dim3(mt, st, a.LM + 1), 256, 0, s>>>(a.J, a.Y, ch, a.Lp, a.K, a.imin, a.joff, C);
+cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a) {
+    const int64_t nn = (int64_t)a.Lp * a.nbins * kNodes;
+    hm_nodes<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a.Lp, a.nbins, a.LM, a.step, a.delta, a.lmax, a.nodes, a.Jn);
+    const int64_t nf = (int64_t)a.Lp * a.nbins * (a.LM + 1);
+    hm_fit<<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(a.Lp, a.nbins, a.LM, a.lmax, a.vinv, a.Jn, a.T);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C) {
+    const int slices = (a.K + kSliceK - 1) / kSliceK;
+    int kk = a.K < kSliceK ? a.K : kSliceK;
+    kk += (17 - kk % 16) % 16;  // row stride = 1 mod 16 float2
+    // points per tile: about 200 KB of basis values, one 512-thread block per SM
+    int tp = (int)((200 * 1024) / ((size_t)kk * sizeof(float2) + 48));
+    tp = tp < 1 ? 1 : (tp > 16 ? 16 : tp);
+    const size_t smem = ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16 + (size_t)tp * 8 * sizeof(float) +
+                        (size_t)tp * sizeof(float4);
+    cudaError_t e = cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    hm_moments<<<dim3(a.n_units, slices), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp, (float)a.delta, a.ab,
+                                                         a.nmm, a.MP);
+    const int64_t ng = (int64_t)a.G * kNodes * a.K;
+    hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.G, a.K, a.M);
+    hm_contract<<<dim3((a.K + 127) / 128, (a.Lp + kContractShells - 1) / kContractShells), 128, 0, s>>>(
+        a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.aff, C);
     return cudaGetLastError();
 }
 
@@ -406,7 +487,7 @@ cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
         cudaError_t e = cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    hm_synth<<<a.n_rows, 256, smem, s>>>(a.rows, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.step, a.vox_s, a.cx, a.cy, a.cz,
+    hm_synth<<<a.n_rows, 256, smem, s>>>(a.rows, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step, a.vox_s, a.cx, a.cy, a.cz,
                                          a.use_center, a.scale, a.origin, a.grid);
     return cudaGetLastError();
 }

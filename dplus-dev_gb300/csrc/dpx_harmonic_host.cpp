@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace dpxh {
@@ -24,9 +25,124 @@ size_t put(std::vector<char>& h, const void* src, size_t n) {
 // Expansion order of shell i: l_i = ceil(x + 3 x^(1/3) + 6), x = q_i R.
 int order_of(double x) { return (int)std::ceil(x + 3.0 * std::cbrt(x) + 6.0); }
 
-// Basis table of a chunk kept under this many bytes, so that it stays in the
-// 129 MB L2 while the GEMM re-reads it once per tile of shells.
-constexpr size_t kChunkBasisBytes = size_t(80) << 20;
+// Radial bin width x q_max: the degree-5 interpolation of j_l(q r) over a bin
+// then errs by less than 2e-8.
+constexpr double kBinWidthTimesQmax = 0.7;
+// Points per moments block.
+constexpr int kUnitPoints = 1024;
+
+// Chebyshev nodes cos((2c+1) pi / 12) and the inverse of their Vandermonde
+// matrix V[c][n] = x_c^n (Gauss-Jordan in double).
+void chebyshev_fit(double nodes[6], double vinv[36]) {
+    double a[6][12];
+    for (int c = 0; c < 6; ++c) {
+        nodes[c] = std::cos((2 * c + 1) * 3.14159265358979323846 / 12.0);
+        double x = 1.0;
+        for (int n = 0; n < 6; ++n) {
+            a[c][n] = x;
+            a[c][6 + n] = c == n ? 1.0 : 0.0;
+            x *= nodes[c];
+        }
+    }
+    for (int col = 0; col < 6; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 6; ++r)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        for (int q = 0; q < 12; ++q) std::swap(a[col][q], a[piv][q]);
+        const double inv = 1.0 / a[col][col];
+        for (int q = 0; q < 12; ++q) a[col][q] *= inv;
+        for (int r = 0; r < 6; ++r)
+            if (r != col) {
+                const double f = a[r][col];
+                for (int q = 0; q < 12; ++q) a[r][q] -= f * a[col][q];
+            }
+    }
+    // T = V^-1 J: T_n = sum_c vinv[n][c] J_c
+    for (int n = 0; n < 6; ++n)
+        for (int c = 0; c < 6; ++c) vinv[n * 6 + c] = a[n][6 + c];
+}
+
+// The voxels of the solvent boxes about the centre t.cen, binned by radius
+// (bin width delta) in box order within a bin: two passes over the boxes on
+// host threads (counts per thread and bin, then the scatter), written into the
+// context's pinned buffer.  Units of <= kUnitPoints voxels per bin.
+int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s, double delta, int nbins,
+               std::vector<int4>& units, std::vector<int2>& groups, std::vector<int>& gu, const float4** out,
+               int64_t* n_out) {
+    const int64_t nb = t.n_boxes;
+    const int nth = (int)std::max<int64_t>(1, std::min<int64_t>(
+        std::min<int64_t>(16, (int64_t)std::max(1u, std::thread::hardware_concurrency())), nb / 4096 + 1));
+    std::vector<int64_t> cnt((size_t)nth * nbins, 0);
+    auto box_range = [&](int th, int64_t& b0, int64_t& b1) {
+        b0 = nb * th / nth;
+        b1 = nb * (th + 1) / nth;
+    };
+    auto for_voxels = [&](int64_t b, auto&& fn) {
+        const float* r = d.boxes + 8 * b;
+        const int nx = (int)std::lround(r[4] / s), ny = (int)std::lround(r[5] / s), nz = (int)std::lround(r[6] / s);
+        for (int ix = 0; ix < nx; ++ix) {
+            const float x = (float)((double)r[0] + ((ix + 0.5) * s - 0.5 * r[4]) - t.cen[0]);
+            for (int iy = 0; iy < ny; ++iy) {
+                const float y = (float)((double)r[1] + ((iy + 0.5) * s - 0.5 * r[5]) - t.cen[1]);
+                for (int iz = 0; iz < nz; ++iz) {
+                    const float z = (float)((double)r[2] + ((iz + 0.5) * s - 0.5 * r[6]) - t.cen[2]);
+                    const double rr = std::sqrt((double)x * x + (double)y * y + (double)z * z);
+                    fn(make_float4(x, y, z, r[3]), std::min(nbins - 1, (int)(rr / delta)));
+                }
+            }
+        }
+    };
+    {
+        std::vector<std::thread> pool;
+        for (int th = 0; th < nth; ++th)
+            pool.emplace_back([&, th] {
+                int64_t b0, b1;
+                box_range(th, b0, b1);
+                int64_t* c = cnt.data() + (size_t)th * nbins;
+                for (int64_t b = b0; b < b1; ++b) for_voxels(b, [&](const float4&, int bin) { ++c[bin]; });
+            });
+        for (auto& p : pool) p.join();
+    }
+    std::vector<int64_t> bin_start(nbins + 1, 0), off((size_t)nth * nbins);
+    for (int bin = 0; bin < nbins; ++bin) {
+        int64_t o = bin_start[bin];
+        for (int th = 0; th < nth; ++th) {
+            off[(size_t)th * nbins + bin] = o;
+            o += cnt[(size_t)th * nbins + bin];
+        }
+        bin_start[bin + 1] = o;
+    }
+    const int64_t n = bin_start[nbins];
+    if (n > INT32_MAX) return fail(DPX_ERR_ARG, "harmonic fill: %lld voxels", (long long)n);
+    if (cudaError_t e = ctx->pinned.reserve((size_t)n * sizeof(float4))) {
+        cudaGetLastError();
+        return fail(DPX_ERR_OOM, "pinned staging of %lld voxels (%s)", (long long)n, cudaGetErrorString(e));
+    }
+    float4* dst = static_cast<float4*>(ctx->pinned.p);
+    {
+        std::vector<std::thread> pool;
+        for (int th = 0; th < nth; ++th)
+            pool.emplace_back([&, th] {
+                int64_t b0, b1;
+                box_range(th, b0, b1);
+                int64_t* o = off.data() + (size_t)th * nbins;
+                for (int64_t b = b0; b < b1; ++b) for_voxels(b, [&](const float4& v, int bin) { dst[o[bin]++] = v; });
+            });
+        for (auto& p : pool) p.join();
+    }
+    for (int bin = 0; bin < nbins; ++bin) {
+        const int64_t c = bin_start[bin + 1] - bin_start[bin];
+        if (c == 0) continue;
+        gu.push_back((int)units.size());
+        groups.push_back(make_int2(bin, -1));
+        for (int64_t o = 0; o < c; o += kUnitPoints)
+            units.push_back(make_int4((int)(bin_start[bin] + o), (int)std::min<int64_t>(kUnitPoints, c - o), bin, 0));
+    }
+    gu.push_back((int)units.size());
+    *out = dst;
+    *n_out = n;
+    return DPX_OK;
+}
 
 }  // namespace
 
@@ -54,43 +170,25 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
                 atoms[j] = make_float4((float)((double)src[4 * j] - sh[0]), (float)((double)src[4 * j + 1] - sh[1]),
                                        (float)((double)src[4 * j + 2] - sh[2]), (float)u);
     }
-    std::vector<float4> vox;
+    // ---- R: the atoms and the corners of the solvent boxes ----
     const double s = d.voxel_step;
-    if (t.n_boxes > 0) {
-        for (int64_t b = 0; b < t.n_boxes; ++b) {
-            const float* r = d.boxes + 8 * b;
-            const int nx = (int)std::lround(r[4] / s), ny = (int)std::lround(r[5] / s), nz = (int)std::lround(r[6] / s);
-            for (int ix = 0; ix < nx; ++ix)
-                for (int iy = 0; iy < ny; ++iy)
-                    for (int iz = 0; iz < nz; ++iz)
-                        vox.push_back(make_float4(
-                            (float)((double)r[0] + ((ix + 0.5) * s - 0.5 * r[4]) - t.cen[0]),
-                            (float)((double)r[1] + ((iy + 0.5) * s - 0.5 * r[5]) - t.cen[1]),
-                            (float)((double)r[2] + ((iz + 0.5) * s - 0.5 * r[6]) - t.cen[2]), r[3]));
-        }
-    }
     double R = 0.0;
     for (const float4& p : atoms) R = std::max(R, std::sqrt((double)p.x * p.x + (double)p.y * p.y + (double)p.z * p.z));
-    for (const float4& p : vox) R = std::max(R, std::sqrt((double)p.x * p.x + (double)p.y * p.y + (double)p.z * p.z));
+    for (int64_t b = 0; b < t.n_boxes; ++b) {
+        const float* r = d.boxes + 8 * b;
+        double q = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const double e = std::fabs((double)r[k] - t.cen[k]) + 0.5 * r[4 + k];
+            q += e * e;
+        }
+        R = std::max(R, std::sqrt(q));
+    }
     // ---- orders ----
     std::vector<int> lmax(Lp + 1, 0);
     for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * R);
     const int LM = lmax[Lp];
     if (LM > dpx::harmonic_max_l()) return 1;
     const int K = (LM + 1) * (LM + 2) / 2;
-    std::vector<int> imin(LM + 1, Lp + 1);
-    for (int l = 0; l <= LM; ++l)
-        for (int i = 1; i <= Lp; ++i)
-            if (lmax[i] >= l) {
-                imin[l] = i;
-                break;
-            }
-    std::vector<int64_t> joff(LM + 1, 0);
-    int64_t rows_total = 0;
-    for (int l = 0; l <= LM; ++l) {
-        joff[l] = rows_total;
-        rows_total += Lp - imin[l] + 1;
-    }
     std::vector<float2> ab(K, make_float2(0.f, 0.f));
     for (int m = 0; m <= LM; ++m)
         for (int l = m + 1; l <= LM; ++l) {
@@ -98,29 +196,96 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
             const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
             ab[(size_t)l * (l + 1) / 2 + m] = make_float2((float)a, (float)b);
         }
+    std::vector<float> nmm(LM + 1);  // Pbar_mm = nmm[m] (-sin theta)^m, orthonormal
+    {
+        double v = 0.28209479177387814347;  // 1 / sqrt(4 pi)
+        for (int m = 0; m <= LM; ++m) {
+            if (m > 0) v *= std::sqrt((2.0 * m + 1.0) / (2.0 * m));
+            nmm[m] = (float)v;
+        }
+    }
     std::vector<int2> rows;
     for (int i = 1; i <= Lp; ++i)
         for (int tt = 0; tt <= 3 * i / 2; ++tt) rows.push_back(make_int2(i, tt));
-    // ---- chunking ----
-    const int64_t npts = std::max<int64_t>((int64_t)atoms.size(), (int64_t)vox.size());
-    int64_t ch = (int64_t)(kChunkBasisBytes / ((size_t)K * sizeof(float2))) / 64 * 64;
-    ch = std::max<int64_t>(64, std::min<int64_t>(ch, (npts + 63) / 64 * 64));
+    // ---- radial bins and the degree-5 interpolation on Chebyshev nodes ----
+    const double delta = kBinWidthTimesQmax / (Lp * G.step);
+    const int nbins = (int)(R / delta) + 1;
+    double nodes[6], vinv[36];
+    chebyshev_fit(nodes, vinv);
+    // ---- groups: (bin, ion) for atoms, bin for voxels; counting sort ----
+    struct Set {
+        std::vector<float4> pts;
+        std::vector<int4> units;
+        std::vector<int2> groups;
+        std::vector<int> gu;
+    };
+    auto make_set = [&](const std::vector<float4>& in, bool voxels, Set& out) {
+        const int nion = voxels ? 1 : d.n_ions;
+        const int ng = nbins * nion;
+        std::vector<int> gid(in.size()), count(ng + 1, 0);
+        for (size_t j = 0; j < in.size(); ++j) {
+            const float4& p = in[j];
+            const double r = std::sqrt((double)p.x * p.x + (double)p.y * p.y + (double)p.z * p.z);
+            const int b = std::min(nbins - 1, (int)(r / delta));
+            gid[j] = b * nion + (voxels ? 0 : (int)p.w);
+            count[gid[j] + 1]++;
+        }
+        for (int g = 0; g < ng; ++g) count[g + 1] += count[g];
+        out.pts.resize(in.size());
+        std::vector<int> fill(count.begin(), count.end() - 1);
+        for (size_t j = 0; j < in.size(); ++j) {
+            float4 p = in[j];
+            if (!voxels) p.w = 1.f;  // the ion's form factor is applied per shell
+            out.pts[fill[gid[j]]++] = p;
+        }
+        for (int g = 0; g < ng; ++g) {
+            const int n = count[g + 1] - count[g];
+            if (n == 0) continue;
+            out.gu.push_back((int)out.units.size());
+            out.groups.push_back(make_int2(g / nion, voxels ? -1 : g % nion));
+            for (int o = 0; o < n; o += kUnitPoints)
+                out.units.push_back(make_int4(count[g] + o, std::min(kUnitPoints, n - o), g / nion, 0));
+        }
+        out.gu.push_back((int)out.units.size());
+    };
+    Set sa, sv;
+    make_set(atoms, false, sa);
+    // voxels: binned on the host threads straight into pinned memory
+    int64_t n_vox = 0;
+    const float4* vox_pinned = nullptr;
+    if (t.n_boxes > 0) {
+        if (int rc = bin_voxels(ctx, d, t, s, delta, nbins, sv.units, sv.groups, sv.gu, &vox_pinned, &n_vox))
+            return rc;
+    }
     const size_t cell_set = (size_t)(Lp + 1) * K * sizeof(double2);
+    const size_t moments_per_unit = (size_t)6 * K * sizeof(float2);
     // ---- device arena ----
     std::vector<char> h;
-    const size_t oA = put(h, atoms.data(), atoms.size() * sizeof(float4));
-    const size_t oV = put(h, vox.data(), vox.size() * sizeof(float4));
     const size_t oL = put(h, lmax.data(), lmax.size() * sizeof(int));
-    const size_t oI = put(h, imin.data(), imin.size() * sizeof(int));
-    const size_t oJo = put(h, joff.data(), joff.size() * sizeof(int64_t));
     const size_t oAb = put(h, ab.data(), ab.size() * sizeof(float2));
+    const size_t oNm = put(h, nmm.data(), nmm.size() * sizeof(float));
     const size_t oR = put(h, rows.data(), rows.size() * sizeof(int2));
+    const size_t oNo = put(h, nodes, sizeof nodes);
+    const size_t oVi = put(h, vinv, sizeof vinv);
+    size_t oP[2], oU[2], oG[2], oGu[2];
+    Set* sets[2] = {&sa, &sv};
+    for (int k = 0; k < 2; ++k) {
+        oP[k] = put(h, sets[k]->pts.data(), sets[k]->pts.size() * sizeof(float4));  // voxels: empty here
+        oU[k] = put(h, sets[k]->units.data(), sets[k]->units.size() * sizeof(int4));
+        oG[k] = put(h, sets[k]->groups.data(), sets[k]->groups.size() * sizeof(int2));
+        oGu[k] = put(h, sets[k]->gu.data(), sets[k]->gu.size() * sizeof(int));
+    }
     const size_t staged = al16(h.size());
-    const size_t oY = staged;
-    const size_t oJ = al16(oY + (size_t)K * ch * sizeof(float2));
-    const size_t oCa = al16(oJ + (size_t)rows_total * ch * sizeof(float));
+    const size_t oVx = staged;  // the binned voxels, copied from pinned memory
+    const size_t oJn = al16(oVx + (size_t)n_vox * sizeof(float4));
+    const size_t oT = al16(oJn + (size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double));
+    const size_t oMP = al16(oT + (size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float));
+    const size_t max_units = std::max(sa.units.size(), sv.units.size());
+    const size_t max_groups = std::max(sa.groups.size(), sv.groups.size());
+    const size_t oM = al16(oMP + max_units * moments_per_unit);
+    const size_t oCa = al16(oM + max_groups * moments_per_unit);
     const size_t oCv = al16(oCa + cell_set);
-    const size_t total = oCv + (vox.empty() ? 0 : cell_set);
+    const size_t total = oCv + (n_vox == 0 ? 0 : cell_set);
     if (cudaError_t e = ctx->harmonic.reserve(total)) {
         cudaGetLastError();
         return fail(DPX_ERR_OOM, "harmonic fill needs %zu bytes (%s)", total, cudaGetErrorString(e));
@@ -128,31 +293,46 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     char* base = static_cast<char*>(ctx->harmonic.p);
     cudaStream_t st = ctx->stream;
     DPX_CUDA(cudaMemcpyAsync(base, h.data(), staged, cudaMemcpyHostToDevice, st));
-    dpx::HarmonicArgs a{};
-    a.ch = (int)ch;
-    a.Lp = Lp;
-    a.LM = LM;
-    a.K = K;
-    a.step = G.step;
-    a.lmax = reinterpret_cast<const int*>(base + oL);
-    a.imin = reinterpret_cast<const int*>(base + oI);
-    a.joff = reinterpret_cast<const int64_t*>(base + oJo);
-    a.ab = reinterpret_cast<const float2*>(base + oAb);
-    a.aff = reinterpret_cast<const float*>(dbase + t.aff);
-    a.Y = reinterpret_cast<float2*>(base + oY);
-    a.J = reinterpret_cast<float*>(base + oJ);
+    if (n_vox) DPX_CUDA(cudaMemcpyAsync(base + oVx, vox_pinned, (size_t)n_vox * sizeof(float4), cudaMemcpyHostToDevice, st));
+    const int* d_lmax = reinterpret_cast<const int*>(base + oL);
+    dpx::HarmonicTables tb{};
+    tb.Lp = Lp;
+    tb.nbins = nbins;
+    tb.LM = LM;
+    tb.step = G.step;
+    tb.delta = delta;
+    tb.lmax = d_lmax;
+    tb.nodes = reinterpret_cast<const double*>(base + oNo);
+    tb.vinv = reinterpret_cast<const double*>(base + oVi);
+    tb.Jn = reinterpret_cast<double*>(base + oJn);
+    tb.T = reinterpret_cast<float*>(base + oT);
+    DPX_CUDA(dpx::launch_harmonic_tables(st, tb));
     double2* Ca = reinterpret_cast<double2*>(base + oCa);
-    double2* Cv = vox.empty() ? nullptr : reinterpret_cast<double2*>(base + oCv);
-    DPX_CUDA(cudaMemsetAsync(Ca, 0, cell_set * (vox.empty() ? 1 : 2), st));
-    for (int set = 0; set < 2; ++set) {
-        const bool voxels = set == 1;
-        const int64_t n = voxels ? (int64_t)vox.size() : (int64_t)atoms.size();
-        if (n == 0) continue;
-        a.pts = reinterpret_cast<const float4*>(base + (voxels ? oV : oA));
-        a.n = n;
-        const int64_t nc = (n + ch - 1) / ch;
-        for (int64_t c = 0; c < nc; ++c)
-            DPX_CUDA(dpx::launch_harmonic_chunk(st, a, voxels, c * ch, voxels ? Cv : Ca));
+    double2* Cv = n_vox == 0 ? nullptr : reinterpret_cast<double2*>(base + oCv);
+    DPX_CUDA(cudaMemsetAsync(Ca, 0, cell_set * (n_vox == 0 ? 1 : 2), st));
+    for (int k = 0; k < 2; ++k) {
+        const Set& S = *sets[k];
+        if (S.units.empty()) continue;
+        dpx::HarmonicSet a{};
+        a.pts = reinterpret_cast<const float4*>(base + (k == 0 ? oP[0] : oVx));
+        a.units = reinterpret_cast<const int4*>(base + oU[k]);
+        a.n_units = (int)S.units.size();
+        a.groups = reinterpret_cast<const int2*>(base + oG[k]);
+        a.gu = reinterpret_cast<const int*>(base + oGu[k]);
+        a.G = (int)S.groups.size();
+        a.LM = LM;
+        a.K = K;
+        a.Lp = Lp;
+        a.nbins = nbins;
+        a.delta = delta;
+        a.ab = reinterpret_cast<const float2*>(base + oAb);
+        a.nmm = reinterpret_cast<const float*>(base + oNm);
+        a.T = tb.T;
+        a.lmax = d_lmax;
+        a.aff = reinterpret_cast<const float*>(dbase + t.aff);
+        a.MP = reinterpret_cast<float2*>(base + oMP);
+        a.M = reinterpret_cast<float2*>(base + oM);
+        DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
     }
     dpx::HarmonicSynth y{};
     y.rows = reinterpret_cast<const int2*>(base + oR);
@@ -162,8 +342,9 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     y.K = K;
     y.Lp = Lp;
     y.lmax_host_outer = LM;
-    y.lmax = a.lmax;
-    y.ab = a.ab;
+    y.lmax = d_lmax;
+    y.ab = reinterpret_cast<const float2*>(base + oAb);
+    y.nmm = reinterpret_cast<const float*>(base + oNm);
     y.step = G.step;
     y.vox_s = (float)s;
     y.cx = t.cen[0];
@@ -174,8 +355,8 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     y.origin = t.origin;
     y.grid = reinterpret_cast<float4*>(grid);
     DPX_CUDA(dpx::launch_harmonic_synth(st, y));
-    // the staging vectors are host-side; the copy above was from pageable
-    // memory and has completed, the arena stays owned by the context
+    // the staging vector was copied from pageable memory (the call returns once
+    // it is staged); the arena stays owned by the context
     return DPX_OK;
 }
 

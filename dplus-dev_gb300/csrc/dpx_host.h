@@ -45,6 +45,26 @@ struct DevBuf {
     }
 };
 
+// Grow-only pinned host buffer owned by a context.
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMallocHost(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
 inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
 }  // namespace dpxh
@@ -60,6 +80,7 @@ struct dpx_ctx_s {
     int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
     int fill_method = 0;  // DPX_FILL_DIRECT / DPX_FILL_HARMONIC
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
+    dpxh::HostBuf pinned;  // staging of the harmonic fill's voxels
     std::vector<char> host_stage;
 };
 

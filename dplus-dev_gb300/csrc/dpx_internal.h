@@ -138,20 +138,33 @@ cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, dou
 cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);
 
 // Harmonic (multipole) FP32 fill of one leaf (dpx_harmonic.cu).  Points are
-// float4 (x, y, z nm about the centre, ion index for atoms / weight for voxels).
-struct HarmonicArgs {
-    const float4* pts;      // the point set
-    int64_t n;              // its points
-    int ch;                 // points per chunk (a multiple of 64)
-    int Lp, LM, K;          // shells 1..Lp, l <= LM, K = (LM+1)(LM+2)/2
-    double step;            // q step
+// float4 (x, y, z nm about the centre, weight), sorted by group (radial bin,
+// and ion for atoms); a unit is <= 1024 points of one group.
+struct HarmonicTables {
+    int Lp, nbins, LM;
+    double step, delta;     // q step, bin width (nm)
     const int* lmax;        // [Lp+1] l_i
-    const int* imin;        // [LM+1] first shell with l_i >= l
-    const int64_t* joff;    // [LM+1] first J row of order l
+    const double* nodes;    // [6] Chebyshev nodes on [-1, 1]
+    const double* vinv;     // [6][6] inverse Vandermonde of the nodes
+    double* Jn;             // [Lp+1][nbins][6][LM+1] scratch
+    float* T;               // [Lp+1][nbins][LM+1][8] polynomial coefficients
+};
+struct HarmonicSet {
+    const float4* pts;
+    const int4* units;      // {first point, count, bin, 0}
+    int n_units;
+    const int2* groups;     // {bin, ion or -1}
+    const int* gu;          // [G+1] first unit of each group
+    int G;
+    int LM, K, Lp, nbins;
+    double delta;
     const float2* ab;       // [K] Legendre recurrence coefficients
+    const float* nmm;       // [LM+1] Pbar_mm = nmm[m] (-sin theta)^m
+    const float* T;
+    const int* lmax;
     const float* aff;       // [U][Lp+1] ion form factors (atoms)
-    float2* Y;              // [K][ch]
-    float* J;               // [rows][ch]
+    float2* MP;             // [n_units][6][K]
+    float2* M;              // [G][6][K]
 };
 struct HarmonicSynth {
     const int2* rows;       // (i, t) of every theta row t <= 3i/2, i >= 1
@@ -161,6 +174,7 @@ struct HarmonicSynth {
     int K, Lp, lmax_host_outer;
     const int* lmax;
     const float2* ab;
+    const float* nmm;
     double step;
     float vox_s;            // voxel edge (nm)
     double cx, cy, cz;
@@ -170,10 +184,10 @@ struct HarmonicSynth {
     float4* grid;
 };
 int harmonic_max_l();
-// C [Lp+1][K] (FP64) += the expansion coefficients of points
-// [chunk_off, chunk_off + ch) of the set.
-cudaError_t launch_harmonic_chunk(cudaStream_t s, const HarmonicArgs& a, bool voxels, int64_t chunk_off,
-                                  double2* C);
+int harmonic_nodes();
+cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a);
+// C [Lp+1][K] (FP64) = the expansion coefficients of one point set.
+cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C);
 cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a);
 
 // Debye sum of one leaf (dpx_debye.cu).  Atoms padded to a multiple of the
