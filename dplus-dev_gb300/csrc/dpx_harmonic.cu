@@ -137,22 +137,27 @@ __global__ void hm_fit(int Lp, int nbins, int LM, const int* __restrict__ lmax, 
 // hm_moments: block (unit, k slice); units[u] = {first point, count, bin, 0}.
 // Points: float4 (x, y, z, weight) about the centre, sorted by group.
 // MP[u][n][k] (FP32) = sum over the unit's points of w u^n Pbar_lm e^{-i m phi}.
-// Dynamic shared memory: tp x kk float2 basis values (kk = the slice width),
-// tp x 8 weights w u^n and tp x 4 angles.
+// Dynamic shared memory (16-byte aligned regions): the recurrence
+// coefficients of the slice's orders, tp x kk float2 basis values (kk = the
+// slice width rounded to 1 mod 16: rows without bank conflicts), tp x 8
+// weights w u^n and tp angle records.
 // ---------------------------------------------------------------------------
+template <bool FULL>
 __global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units,
-                                                  int LM, int K, int kk, int tp, float delta,
-                                                  const float2* __restrict__ ab, const float* __restrict__ nmm,
-                                                  float2* __restrict__ MP) {
+                                                          int LM, int K, int kk, int tp, float delta,
+                                                          const float2* __restrict__ ab, const float* __restrict__ nmm,
+                                                          float2* __restrict__ MP) {
     extern __shared__ __align__(16) unsigned char smem[];
-    // regions at 16-byte boundaries: tp x kk float2 may be an odd multiple of 8 bytes
-    float2* sY = reinterpret_cast<float2*>(smem);
-    const size_t oW = ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16;
-    float* sW = reinterpret_cast<float*>(smem + oW);
-    float4* sA = reinterpret_cast<float4*>(smem + oW + (size_t)tp * 8 * sizeof(float));
+    float2* sAb = reinterpret_cast<float2*>(smem);
+    const size_t oY = ((size_t)K * sizeof(float2) + 15) / 16 * 16;
+    float2* sY = reinterpret_cast<float2*>(smem + oY);
+    const size_t oW = oY + ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16;
+    float4* sW = reinterpret_cast<float4*>(smem + oW);  // two float4 per point: w u^0 .. w u^5, 0, 0
+    float4* sA = reinterpret_cast<float4*>(smem + oW + (size_t)tp * 2 * sizeof(float4));
     const int4 un = units[blockIdx.x];
-    const int k_lo = blockIdx.y * kSliceK, k_hi = min(K, k_lo + kSliceK);
+    const int k_lo = FULL ? 0 : blockIdx.y * kSliceK, k_hi = FULL ? K : min(K, k_lo + kSliceK);
     const float rb = (un.z + 0.5f) * delta, ih = 2.f / delta;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) sAb[k] = ab[k];
     float2 acc[kSliceK / kMomThreads][kNodes];
 #pragma unroll
     for (int s = 0; s < kSliceK / kMomThreads; ++s)
@@ -170,15 +175,15 @@ __global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restri
             if (r > 0.f) a = make_float4(q.z / r, rxy / r, atan2f(q.y, q.x), 0.f);
             sA[p] = a;
             const float u = (r - rb) * ih;
-            float wn = q.w;
-            for (int n = 0; n < kNodes; ++n) {
-                sW[p * 8 + n] = wn;
-                wn *= u;
-            }
+            float wn[8];
+            wn[0] = q.w;
+#pragma unroll
+            for (int n = 1; n < kNodes; ++n) wn[n] = wn[n - 1] * u;
+            wn[6] = wn[7] = 0.f;
+            sW[2 * p] = make_float4(wn[0], wn[1], wn[2], wn[3]);
+            sW[2 * p + 1] = make_float4(wn[4], wn[5], wn[6], wn[7]);
         }
         __syncthreads();
-        // basis columns (point p, orders m and LM - m in one thread: equal work):
-        // Pbar_mm = nmm[m] (-sin theta)^m, then the l recurrence over the slice
         // items (column pair c, point p), p fastest: the lanes of a warp share
         // one or two columns (broadcast coefficient loads) and write rows p of
         // stride kk = 1 mod 16 float2 (no bank conflicts)
@@ -190,20 +195,23 @@ __global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restri
             for (int side = 0; side < 2; ++side) {
                 const int m = side == 0 ? cpair : LM - cpair;
                 if (side == 1 && m == cpair) break;
-                if (k_of(LM, m) < k_lo || k_of(m, m) >= k_hi) continue;
+                if (!FULL && (k_of(LM, m) < k_lo || k_of(m, m) >= k_hi)) continue;
                 float pw = nmm[m];
                 for (int mm = 0; mm < m; ++mm) pw *= -a.y;
                 float sm, cm;
                 sincosf((float)m * a.z, &sm, &cm);
                 float p2 = 0.f, p1 = pw;
                 int k = k_of(m, m);
-                if (k >= k_lo) y[k] = make_float2(p1 * cm, -p1 * sm);
-                for (int l = m + 1; l <= LM; ++l) {
-                    k = k_of(l, m);
-                    if (k >= k_hi) break;
-                    const float2 c = ab[k];
+                if (FULL || k >= k_lo) y[k] = make_float2(p1 * cm, -p1 * sm);
+                // orders l = m+1 .. lend whose k stays below k_hi
+                int lend = LM;
+                if (!FULL)
+                    while (lend > m && k_of(lend, m) >= k_hi) --lend;
+                for (int l = m + 1; l <= lend; ++l) {
+                    k += l;  // k_of(l, m) = k_of(l - 1, m) + l
+                    const float2 c = sAb[k];
                     const float pn = c.x * fmaf(a.x, p1, -c.y * p2);
-                    if (k >= k_lo) y[k] = make_float2(pn * cm, -pn * sm);
+                    if (FULL || k >= k_lo) y[k] = make_float2(pn * cm, -pn * sm);
                     p2 = p1;
                     p1 = pn;
                 }
@@ -211,19 +219,18 @@ __global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restri
         }
         __syncthreads();
         for (int p = 0; p < np; ++p) {
-            float w[kNodes];
-#pragma unroll
-            for (int n = 0; n < kNodes; ++n) w[n] = sW[p * 8 + n];
+            const float4 w0 = sW[2 * p], w1 = sW[2 * p + 1];
+            const float w[kNodes] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y};
             const float2* yp = sY + (size_t)p * kk;
 #pragma unroll
             for (int s = 0; s < kSliceK / kMomThreads; ++s) {
                 const int kl = s * kMomThreads + threadIdx.x;
-                if (k_lo + kl >= k_hi) continue;
-                const float2 y = yp[kl];
+                if (k_lo + kl >= k_hi) break;
+                const float2 yv = yp[kl];
 #pragma unroll
                 for (int n = 0; n < kNodes; ++n) {
-                    acc[s][n].x = fmaf(w[n], y.x, acc[s][n].x);
-                    acc[s][n].y = fmaf(w[n], y.y, acc[s][n].y);
+                    acc[s][n].x = fmaf(w[n], yv.x, acc[s][n].x);
+                    acc[s][n].y = fmaf(w[n], yv.y, acc[s][n].y);
                 }
             }
         }
@@ -231,7 +238,7 @@ __global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restri
 #pragma unroll
     for (int s = 0; s < kSliceK / kMomThreads; ++s) {
         const int k = k_lo + s * kMomThreads + threadIdx.x;
-        if (k >= k_hi) continue;
+        if (k >= k_hi) break;
 #pragma unroll
         for (int n = 0; n < kNodes; ++n) MP[((int64_t)blockIdx.x * kNodes + n) * K + k] = acc[s][n];
     }
@@ -461,15 +468,25 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C
     const int slices = (a.K + kSliceK - 1) / kSliceK;
     int kk = a.K < kSliceK ? a.K : kSliceK;
     kk += (17 - kk % 16) % 16;  // row stride = 1 mod 16 float2
-    // points per tile: about 200 KB of basis values, one 512-thread block per SM
-    int tp = (int)((200 * 1024) / ((size_t)kk * sizeof(float2) + 48));
+    const size_t oY = ((size_t)a.K * sizeof(float2) + 15) / 16 * 16;
+    // points per tile: the basis rows within 200 KB of shared memory with the coefficients
+    const size_t budget = 200 * 1024 > oY + 4096 ? 200 * 1024 - oY : 4096;
+    int tp = (int)(budget / ((size_t)kk * sizeof(float2) + 48));
     tp = tp < 1 ? 1 : (tp > 16 ? 16 : tp);
-    const size_t smem = ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16 + (size_t)tp * 8 * sizeof(float) +
+    const size_t smem = oY + ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16 + (size_t)tp * 2 * sizeof(float4) +
                         (size_t)tp * sizeof(float4);
-    cudaError_t e = cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    hm_moments<<<dim3(a.n_units, slices), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp, (float)a.delta, a.ab,
-                                                         a.nmm, a.MP);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    if (slices == 1) {
+        cudaError_t e = cudaFuncSetAttribute(hm_moments<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        hm_moments<true><<<dim3(a.n_units, 1), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp,
+                                                                      (float)a.delta, a.ab, a.nmm, a.MP);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(hm_moments<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        hm_moments<false><<<dim3(a.n_units, slices), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp,
+                                                                           (float)a.delta, a.ab, a.nmm, a.MP);
+    }
     const int64_t ng = (int64_t)a.G * kNodes * a.K;
     hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.G, a.K, a.M);
     hm_contract<<<dim3((a.K + 127) / 128, (a.Lp + kContractShells - 1) / kContractShells), 128, 0, s>>>(
