@@ -196,9 +196,8 @@ void ctx_release(dpx_ctx ctx) {
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
-                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic})
+                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels})
         b->release();
-    ctx->pinned.release();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -382,9 +381,18 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     std::vector<char>& h = ctx->host_stage;
     h.clear();
     std::vector<LeafTables> lt(n);
+    std::vector<char> harm(n, 0);  // FP32 leaves the harmonic method takes
+    std::vector<std::vector<float>> host_atoms(n);
+    if (ctx->fill_method == DPX_FILL_HARMONIC)
+        for (int j = 0; j < n; ++j) {
+            if (grids[j]->precision != DPX_FP32) continue;
+            int status = DPX_OK;
+            harm[j] = harmonic_accepts(ctx, pdbs[j], grids[j]->g, host_atoms[j], &status);
+            if (status) return status;
+        }
     for (int j = 0; j < n; ++j) {
         const bool fp32 = grids[j]->precision == DPX_FP32;
-        stage_leaf(h, pdbs[j], grids[j]->g, fp32, fp32 ? cpt : dpx::kFill64Cells, lt[j]);
+        stage_leaf(h, pdbs[j], grids[j]->g, fp32, fp32 ? cpt : dpx::kFill64Cells, lt[j], !harm[j]);
     }
     const size_t jobs_off = al16(h.size());
     const size_t counter_off = al16(jobs_off + (size_t)n * sizeof(dpx::FillJob));
@@ -394,18 +402,14 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     // the leaf tables first: the harmonic fills read their form factors
     DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h.data(), jobs_off, cudaMemcpyHostToDevice, s));
     if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
-    std::vector<char> done(n, 0);  // FP32 leaves filled by the harmonic method
-    if (ctx->fill_method == DPX_FILL_HARMONIC)
-        for (int j = 0; j < n; ++j) {
-            if (grids[j]->precision != DPX_FP32) continue;
-            const int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells);
-            if (rc < 0) return rc;
-            done[j] = rc == 0;
-        }
+    for (int j = 0; j < n; ++j)
+        if (harm[j])
+            if (int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, host_atoms[j]))
+                return rc;
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
     for (int j = 0; j < n; ++j) {
-        if (grids[j]->precision != DPX_FP32 || done[j]) continue;
+        if (grids[j]->precision != DPX_FP32 || harm[j]) continue;
         jobs.push_back(make_job(pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, tiles));
         tiles += (lt[j].items + threads - 1) / threads;
     }

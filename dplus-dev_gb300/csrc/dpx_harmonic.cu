@@ -244,6 +244,94 @@ __global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restri
     }
 }
 
+// ---------------------------------------------------------------------------
+// Solvent boxes to voxels, binned by radius with a stable counting sort:
+// vx_expand (voxel v of box b: centre, weight; its bin; per-block histograms),
+// vx_bins (per bin: the total and its blocks' offsets), vx_scatter (the rank of
+// a voxel among the earlier voxels of its block and bin, by warp match and the
+// per-warp counts).  The order within a bin is the voxel order: deterministic.
+// boxes: float4 pairs {cx, cy, cz, w} about the centre, {Lx, Ly, Lz, 0};
+// vstart[b]: first voxel of box b (z fastest, then y, then x).
+// ---------------------------------------------------------------------------
+constexpr int kBinThreads = 256;
+constexpr int kMaxBins = 1024;
+
+__global__ void __launch_bounds__(kBinThreads) vx_expand(const float4* __restrict__ boxes,
+                                                         const int64_t* __restrict__ vstart, int64_t nb, int64_t nv,
+                                                         float vs, float delta, int nbins, float4* __restrict__ vox,
+                                                         int* __restrict__ vbin, int* __restrict__ hist, int nblk) {
+    __shared__ int sh[kMaxBins];
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0;
+    __syncthreads();
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nv) {
+        int64_t lo = 0, hi = nb - 1;  // the last box with vstart <= v
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (vstart[mid] <= v) lo = mid;
+            else hi = mid - 1;
+        }
+        const float4 c = boxes[2 * lo], L = boxes[2 * lo + 1];
+        const int ny = __float2int_rn(L.y / vs), nz = __float2int_rn(L.z / vs);
+        const int64_t local = v - vstart[lo];
+        const int iz = (int)(local % nz);
+        const int64_t rest = local / nz;
+        const int iy = (int)(rest % ny), ix = (int)(rest / ny);
+        const float4 p = make_float4(c.x + ((ix + 0.5f) * vs - 0.5f * L.x), c.y + ((iy + 0.5f) * vs - 0.5f * L.y),
+                                     c.z + ((iz + 0.5f) * vs - 0.5f * L.z), c.w);
+        vox[v] = p;
+        const float r = sqrtf(fmaf(p.x, p.x, fmaf(p.y, p.y, p.z * p.z)));
+        const int b = min(nbins - 1, (int)(r / delta));
+        vbin[v] = b;
+        atomicAdd(&sh[b], 1);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) hist[(int64_t)b * nblk + blockIdx.x] = sh[b];
+}
+
+// thread per bin: its total over the blocks
+__global__ void vx_totals(const int* __restrict__ hist, int nbins, int nblk, int64_t* __restrict__ total) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    int64_t t = 0;
+    for (int k = 0; k < nblk; ++k) t += hist[(int64_t)b * nblk + k];
+    total[b] = t;
+}
+
+// thread per bin: off[b][blk] = start of bin b + the counts of its earlier blocks
+__global__ void vx_offsets(const int* __restrict__ hist, const int64_t* __restrict__ total, int nbins, int nblk,
+                           int64_t* __restrict__ off) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    int64_t run = 0;
+    for (int c = 0; c < b; ++c) run += total[c];
+    for (int k = 0; k < nblk; ++k) {
+        off[(int64_t)b * nblk + k] = run;
+        run += hist[(int64_t)b * nblk + k];
+    }
+}
+
+__global__ void __launch_bounds__(kBinThreads) vx_scatter(const float4* __restrict__ vox, const int* __restrict__ vbin,
+                                                          int64_t nv, int nbins, int nblk,
+                                                          const int64_t* __restrict__ off, float4* __restrict__ out) {
+    __shared__ int wc[kBinThreads / 32][kMaxBins];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int e = threadIdx.x; e < (kBinThreads / 32) * nbins; e += blockDim.x) wc[e / nbins][e % nbins] = 0;
+    __syncthreads();
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = v < nv;
+    const int b = valid ? vbin[v] : -1 - lane;  // invalid lanes form groups of one
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank == 0) wc[w][b] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+        int pre = 0;
+        for (int k = 0; k < w; ++k) pre += wc[k][b];
+        out[off[(int64_t)b * nblk + blockIdx.x] + pre + rank] = vox[v];
+    }
+}
+
 // hm_groups: M[g][n][k] = sum of MP over the units [gu[g], gu[g+1]) of group g, FP64.
 __global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, int G, int K,
                           float2* __restrict__ M) {
@@ -491,6 +579,19 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C
     hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.G, a.K, a.M);
     hm_contract<<<dim3((a.K + 127) / 128, (a.Lp + kContractShells - 1) / kContractShells), 128, 0, s>>>(
         a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.aff, C);
+    return cudaGetLastError();
+}
+
+int harmonic_max_bins() { return kMaxBins; }
+
+cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
+    const int nblk = (int)((a.nv + kBinThreads - 1) / kBinThreads);
+    if (a.nbins > kMaxBins) return cudaErrorInvalidValue;
+    vx_expand<<<nblk, kBinThreads, 0, s>>>(a.boxes, a.vstart, a.nb, a.nv, a.vs, a.delta, a.nbins, a.tmp, a.vbin,
+                                           a.hist, nblk);
+    vx_totals<<<(a.nbins + 127) / 128, 128, 0, s>>>(a.hist, a.nbins, nblk, a.total);
+    vx_offsets<<<(a.nbins + 127) / 128, 128, 0, s>>>(a.hist, a.total, a.nbins, nblk, a.off);
+    vx_scatter<<<nblk, kBinThreads, 0, s>>>(a.tmp, a.vbin, a.nv, a.nbins, nblk, a.off, a.out);
     return cudaGetLastError();
 }
 

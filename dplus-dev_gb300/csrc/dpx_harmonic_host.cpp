@@ -8,7 +8,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <thread>
 #include <vector>
 
 namespace dpxh {
@@ -62,104 +61,137 @@ void chebyshev_fit(double nodes[6], double vinv[36]) {
         for (int c = 0; c < 6; ++c) vinv[n * 6 + c] = a[n][6 + c];
 }
 
-// The voxels of the solvent boxes about the centre t.cen, binned by radius
-// (bin width delta) in box order within a bin: two passes over the boxes on
-// host threads (counts per thread and bin, then the scatter), written into the
-// context's pinned buffer.  Units of <= kUnitPoints voxels per bin.
+// The voxels of the solvent boxes about the centre t.cen, expanded and
+// sorted by radius bin (bin width delta) on the device, in box order within a
+// bin (dpx::launch_voxel_bins); the bin totals come back to build the units of
+// <= kUnitPoints voxels per bin.
 int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s, double delta, int nbins,
                std::vector<int4>& units, std::vector<int2>& groups, std::vector<int>& gu, const float4** out,
                int64_t* n_out) {
     const int64_t nb = t.n_boxes;
-    const int nth = (int)std::max<int64_t>(1, std::min<int64_t>(
-        std::min<int64_t>(16, (int64_t)std::max(1u, std::thread::hardware_concurrency())), nb / 4096 + 1));
-    std::vector<int64_t> cnt((size_t)nth * nbins, 0);
-    auto box_range = [&](int th, int64_t& b0, int64_t& b1) {
-        b0 = nb * th / nth;
-        b1 = nb * (th + 1) / nth;
-    };
-    auto for_voxels = [&](int64_t b, auto&& fn) {
+    std::vector<float4> hb((size_t)2 * nb);
+    std::vector<int64_t> vstart(nb);
+    int64_t nv = 0;
+    for (int64_t b = 0; b < nb; ++b) {
         const float* r = d.boxes + 8 * b;
-        const int nx = (int)std::lround(r[4] / s), ny = (int)std::lround(r[5] / s), nz = (int)std::lround(r[6] / s);
-        for (int ix = 0; ix < nx; ++ix) {
-            const float x = (float)((double)r[0] + ((ix + 0.5) * s - 0.5 * r[4]) - t.cen[0]);
-            for (int iy = 0; iy < ny; ++iy) {
-                const float y = (float)((double)r[1] + ((iy + 0.5) * s - 0.5 * r[5]) - t.cen[1]);
-                for (int iz = 0; iz < nz; ++iz) {
-                    const float z = (float)((double)r[2] + ((iz + 0.5) * s - 0.5 * r[6]) - t.cen[2]);
-                    const double rr = std::sqrt((double)x * x + (double)y * y + (double)z * z);
-                    fn(make_float4(x, y, z, r[3]), std::min(nbins - 1, (int)(rr / delta)));
-                }
-            }
-        }
-    };
-    {
-        std::vector<std::thread> pool;
-        for (int th = 0; th < nth; ++th)
-            pool.emplace_back([&, th] {
-                int64_t b0, b1;
-                box_range(th, b0, b1);
-                int64_t* c = cnt.data() + (size_t)th * nbins;
-                for (int64_t b = b0; b < b1; ++b) for_voxels(b, [&](const float4&, int bin) { ++c[bin]; });
-            });
-        for (auto& p : pool) p.join();
+        hb[2 * b] = make_float4((float)((double)r[0] - t.cen[0]), (float)((double)r[1] - t.cen[1]),
+                                (float)((double)r[2] - t.cen[2]), r[3]);
+        hb[2 * b + 1] = make_float4(r[4], r[5], r[6], 0.f);
+        vstart[b] = nv;
+        nv += (int64_t)std::lround(r[4] / s) * std::lround(r[5] / s) * std::lround(r[6] / s);
     }
-    std::vector<int64_t> bin_start(nbins + 1, 0), off((size_t)nth * nbins);
-    for (int bin = 0; bin < nbins; ++bin) {
-        int64_t o = bin_start[bin];
-        for (int th = 0; th < nth; ++th) {
-            off[(size_t)th * nbins + bin] = o;
-            o += cnt[(size_t)th * nbins + bin];
-        }
-        bin_start[bin + 1] = o;
-    }
-    const int64_t n = bin_start[nbins];
-    if (n > INT32_MAX) return fail(DPX_ERR_ARG, "harmonic fill: %lld voxels", (long long)n);
-    if (cudaError_t e = ctx->pinned.reserve((size_t)n * sizeof(float4))) {
+    if (nv > INT32_MAX) return fail(DPX_ERR_ARG, "harmonic fill: %lld voxels", (long long)nv);
+    const int nblk = (int)((nv + 255) / 256);
+    std::vector<char> h;
+    const size_t oB = put(h, hb.data(), hb.size() * sizeof(float4));
+    const size_t oS = put(h, vstart.data(), vstart.size() * sizeof(int64_t));
+    const size_t staged = al16(h.size());
+    const size_t oTmp = staged;
+    const size_t oBin = al16(oTmp + (size_t)nv * sizeof(float4));
+    const size_t oHist = al16(oBin + (size_t)nv * sizeof(int));
+    const size_t oOff = al16(oHist + (size_t)nbins * nblk * sizeof(int));
+    const size_t oTot = al16(oOff + (size_t)nbins * nblk * sizeof(int64_t));
+    const size_t oOut = al16(oTot + (size_t)nbins * sizeof(int64_t));
+    const size_t total = oOut + (size_t)nv * sizeof(float4);
+    if (cudaError_t e = ctx->voxels.reserve(total)) {
         cudaGetLastError();
-        return fail(DPX_ERR_OOM, "pinned staging of %lld voxels (%s)", (long long)n, cudaGetErrorString(e));
+        return fail(DPX_ERR_OOM, "voxel binning needs %zu bytes (%s)", total, cudaGetErrorString(e));
     }
-    float4* dst = static_cast<float4*>(ctx->pinned.p);
-    {
-        std::vector<std::thread> pool;
-        for (int th = 0; th < nth; ++th)
-            pool.emplace_back([&, th] {
-                int64_t b0, b1;
-                box_range(th, b0, b1);
-                int64_t* o = off.data() + (size_t)th * nbins;
-                for (int64_t b = b0; b < b1; ++b) for_voxels(b, [&](const float4& v, int bin) { dst[o[bin]++] = v; });
-            });
-        for (auto& p : pool) p.join();
-    }
+    char* base = static_cast<char*>(ctx->voxels.p);
+    cudaStream_t st = ctx->stream;
+    DPX_CUDA(cudaMemcpyAsync(base, h.data(), staged, cudaMemcpyHostToDevice, st));
+    dpx::VoxelBinArgs a{};
+    a.boxes = reinterpret_cast<const float4*>(base + oB);
+    a.vstart = reinterpret_cast<const int64_t*>(base + oS);
+    a.nb = nb;
+    a.nv = nv;
+    a.vs = (float)s;
+    a.delta = (float)delta;
+    a.nbins = nbins;
+    a.tmp = reinterpret_cast<float4*>(base + oTmp);
+    a.vbin = reinterpret_cast<int*>(base + oBin);
+    a.hist = reinterpret_cast<int*>(base + oHist);
+    a.off = reinterpret_cast<int64_t*>(base + oOff);
+    a.total = reinterpret_cast<int64_t*>(base + oTot);
+    a.out = reinterpret_cast<float4*>(base + oOut);
+    DPX_CUDA(dpx::launch_voxel_bins(st, a));
+    std::vector<int64_t> tot(nbins);
+    DPX_CUDA(cudaMemcpyAsync(tot.data(), a.total, (size_t)nbins * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    DPX_CUDA(cudaStreamSynchronize(st));
+    int64_t start = 0;
     for (int bin = 0; bin < nbins; ++bin) {
-        const int64_t c = bin_start[bin + 1] - bin_start[bin];
-        if (c == 0) continue;
-        gu.push_back((int)units.size());
-        groups.push_back(make_int2(bin, -1));
-        for (int64_t o = 0; o < c; o += kUnitPoints)
-            units.push_back(make_int4((int)(bin_start[bin] + o), (int)std::min<int64_t>(kUnitPoints, c - o), bin, 0));
+        const int64_t c = tot[bin];
+        if (c > 0) {
+            gu.push_back((int)units.size());
+            groups.push_back(make_int2(bin, -1));
+            for (int64_t o = 0; o < c; o += kUnitPoints)
+                units.push_back(make_int4((int)(start + o), (int)std::min<int64_t>(kUnitPoints, c - o), bin, 0));
+        }
+        start += c;
     }
     gu.push_back((int)units.size());
-    *out = dst;
-    *n_out = n;
+    *out = a.out;
+    *n_out = nv;
     return DPX_OK;
 }
 
 }  // namespace
 
-int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid) {
-    const int Lp = G.Lp;
-    if (t.n_boxes > 0 && !(d.voxel_step > 0.0)) return 1;
-    // ---- point sets about the leaf's centre t.cen (device atoms arrive shifted) ----
+bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, std::vector<float>& host_atoms,
+                      int* status) {
+    *status = DPX_OK;
+    if (d.n_boxes > 0 && d.boxes && !(d.voxel_step > 0.0)) return false;
     const float* src = d.atoms;
-    std::vector<float> dev_copy;
-    if (d.atoms_on_device) {
-        dev_copy.resize((size_t)4 * d.n_atoms);
-        DPX_CUDA(cudaMemcpyAsync(dev_copy.data(), d.atoms, dev_copy.size() * sizeof(float), cudaMemcpyDeviceToHost,
-                                 ctx->stream));
-        DPX_CUDA(cudaStreamSynchronize(ctx->stream));
-        src = dev_copy.data();
+    if (d.atoms_on_device) {  // atoms already shifted by the centre
+        host_atoms.resize((size_t)4 * d.n_atoms);
+        cudaError_t e = cudaMemcpyAsync(host_atoms.data(), d.atoms, host_atoms.size() * sizeof(float),
+                                        cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) {
+            *status = cuda_fail(e, "harmonic fill: atoms to host");
+            return false;
+        }
+        src = host_atoms.data();
     }
+    // the centre of stage_leaf: the given one, else the host atoms' centroid
+    double c[3] = {0, 0, 0};
+    if (d.center) {
+        for (int k = 0; k < 3; ++k) c[k] = d.center[k];
+    } else if (!d.atoms_on_device) {
+        for (int64_t a = 0; a < d.n_atoms; ++a)
+            for (int k = 0; k < 3; ++k) c[k] += src[4 * a + k];
+        for (int k = 0; k < 3; ++k) c[k] /= (double)d.n_atoms;
+    }
+    const double ca[3] = {d.atoms_on_device ? 0.0 : c[0], d.atoms_on_device ? 0.0 : c[1],
+                          d.atoms_on_device ? 0.0 : c[2]};
+    double r2 = 0.0;
+    for (int64_t a = 0; a < d.n_atoms; ++a) {
+        double q = 0;
+        for (int k = 0; k < 3; ++k) q += (src[4 * a + k] - ca[k]) * (src[4 * a + k] - ca[k]);
+        r2 = std::max(r2, q);
+    }
+    const int64_t nb = d.n_boxes > 0 && d.boxes ? d.n_boxes : 0;
+    for (int64_t b = 0; b < nb; ++b) {
+        const float* r = d.boxes + 8 * b;
+        double q = 0;
+        for (int k = 0; k < 3; ++k) {
+            const double e = std::fabs((double)r[k] - c[k]) + 0.5 * r[4 + k];
+            q += e * e;
+        }
+        r2 = std::max(r2, q);
+    }
+    const double R = std::sqrt(r2) * (1.0 + 1e-6);  // the fill measures R on the rounded points
+    if (order_of(G.Lp * G.step * R) > dpx::harmonic_max_l()) return false;
+    const double delta = kBinWidthTimesQmax / (G.Lp * G.step);
+    if (nb > 0 && (int)(R / delta) + 1 > dpx::harmonic_max_bins()) return false;
+    return true;
+}
+
+int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
+                  void* grid, const std::vector<float>& host_atoms) {
+    const int Lp = G.Lp;
+    // ---- point sets about the leaf's centre t.cen (device atoms arrive shifted) ----
+    const float* src = d.atoms_on_device ? host_atoms.data() : d.atoms;
     const double sh[3] = {d.atoms_on_device ? 0.0 : t.cen[0], d.atoms_on_device ? 0.0 : t.cen[1],
                           d.atoms_on_device ? 0.0 : t.cen[2]};
     std::vector<float4> atoms(d.n_atoms);
@@ -187,7 +219,8 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     std::vector<int> lmax(Lp + 1, 0);
     for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * R);
     const int LM = lmax[Lp];
-    if (LM > dpx::harmonic_max_l()) return 1;
+    if (LM > dpx::harmonic_max_l()) return fail(DPX_ERR_ARG, "harmonic fill: order %d above %d", LM,
+                                                dpx::harmonic_max_l());
     const int K = (LM + 1) * (LM + 2) / 2;
     std::vector<float2> ab(K, make_float2(0.f, 0.f));
     for (int m = 0; m <= LM; ++m)
@@ -250,12 +283,13 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     };
     Set sa, sv;
     make_set(atoms, false, sa);
-    // voxels: binned on the host threads straight into pinned memory
+    // voxels: expanded and binned on the device
     int64_t n_vox = 0;
-    const float4* vox_pinned = nullptr;
+    const float4* vox_dev = nullptr;
     if (t.n_boxes > 0) {
-        if (int rc = bin_voxels(ctx, d, t, s, delta, nbins, sv.units, sv.groups, sv.gu, &vox_pinned, &n_vox))
-            return rc;
+        if (nbins > dpx::harmonic_max_bins())
+            return fail(DPX_ERR_ARG, "harmonic fill: %d radial bins above %d", nbins, dpx::harmonic_max_bins());
+        if (int rc = bin_voxels(ctx, d, t, s, delta, nbins, sv.units, sv.groups, sv.gu, &vox_dev, &n_vox)) return rc;
     }
     const size_t cell_set = (size_t)(Lp + 1) * K * sizeof(double2);
     const size_t moments_per_unit = (size_t)6 * K * sizeof(float2);
@@ -276,8 +310,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         oGu[k] = put(h, sets[k]->gu.data(), sets[k]->gu.size() * sizeof(int));
     }
     const size_t staged = al16(h.size());
-    const size_t oVx = staged;  // the binned voxels, copied from pinned memory
-    const size_t oJn = al16(oVx + (size_t)n_vox * sizeof(float4));
+    const size_t oJn = staged;
     const size_t oT = al16(oJn + (size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double));
     const size_t oMP = al16(oT + (size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float));
     const size_t max_units = std::max(sa.units.size(), sv.units.size());
@@ -293,7 +326,6 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     char* base = static_cast<char*>(ctx->harmonic.p);
     cudaStream_t st = ctx->stream;
     DPX_CUDA(cudaMemcpyAsync(base, h.data(), staged, cudaMemcpyHostToDevice, st));
-    if (n_vox) DPX_CUDA(cudaMemcpyAsync(base + oVx, vox_pinned, (size_t)n_vox * sizeof(float4), cudaMemcpyHostToDevice, st));
     const int* d_lmax = reinterpret_cast<const int*>(base + oL);
     dpx::HarmonicTables tb{};
     tb.Lp = Lp;
@@ -314,7 +346,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         const Set& S = *sets[k];
         if (S.units.empty()) continue;
         dpx::HarmonicSet a{};
-        a.pts = reinterpret_cast<const float4*>(base + (k == 0 ? oP[0] : oVx));
+        a.pts = k == 0 ? reinterpret_cast<const float4*>(base + oP[0]) : vox_dev;
         a.units = reinterpret_cast<const int4*>(base + oU[k]);
         a.n_units = (int)S.units.size();
         a.groups = reinterpret_cast<const int2*>(base + oG[k]);

@@ -45,26 +45,6 @@ struct DevBuf {
     }
 };
 
-// Grow-only pinned host buffer owned by a context.
-struct HostBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    cudaError_t reserve(size_t n) {
-        if (n <= bytes) return cudaSuccess;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMallocHost(&p, n);
-        if (e == cudaSuccess) bytes = n;
-        return e;
-    }
-    void release() {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-    }
-};
-
 inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
 }  // namespace dpxh
@@ -80,7 +60,7 @@ struct dpx_ctx_s {
     int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
     int fill_method = 0;  // DPX_FILL_DIRECT / DPX_FILL_HARMONIC
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
-    dpxh::HostBuf pinned;  // staging of the harmonic fill's voxels
+    dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
     std::vector<char> host_stage;
 };
 
@@ -137,16 +117,21 @@ struct LeafTables {
     double origin = 0;  // F(0) = scale (sum_u aff_u(0) N_u + sum_b w_b V_b), FP64
 };
 // Appends leaf d's tables for grid G (FP32 with cpt cells per item, or FP64).
-void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t);
+// direct_boxes = false leaves the boxes out of the staging (the harmonic fill
+// reads them from the descriptor); F(0) counts them either way.
+void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t,
+                bool direct_boxes = true);
 // The FP32 fill job of a staged leaf whose buffer sits at device address dbase.
 dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
                       int64_t tile_start);
 // Harmonic (multipole) FP32 fill of a staged leaf (dpx_harmonic_host.cpp).
-// Returns DPX_OK, 1 when the leaf cannot take it (boxes without their voxel
-// step, an expansion order above the kernels' limit: the caller uses the
-// direct sum), or a negative status.
+// harmonic_accepts decides before the staging: boxes need their voxel step,
+// and the expansion order and the radial bins must stay within the kernels'
+// limits (device atoms are copied to `host_atoms` to measure them).
+bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, std::vector<float>& host_atoms,
+                      int* status);
 int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid);
+                  void* grid, const std::vector<float>& host_atoms);
 // The FP64 fill launch of a staged leaf.
 cudaError_t launch_leaf_f64(cudaStream_t s, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase,
                             const dpx::Geom& G, void* grid);

@@ -185,6 +185,22 @@ struct HarmonicSynth {
 };
 int harmonic_max_l();
 int harmonic_nodes();
+int harmonic_max_bins();
+// Solvent boxes expanded into voxels and sorted by radius bin on the device.
+struct VoxelBinArgs {
+    const float4* boxes;    // [2 nb] {cx, cy, cz, w} about the centre, {Lx, Ly, Lz, 0}
+    const int64_t* vstart;  // [nb] first voxel of each box
+    int64_t nb, nv;
+    float vs, delta;        // voxel edge, bin width (nm)
+    int nbins;
+    float4* tmp;            // [nv] voxels in box order
+    int* vbin;              // [nv] their bins
+    int* hist;              // [nbins][blocks]
+    int64_t* off;           // [nbins][blocks]
+    int64_t* total;         // [nbins]
+    float4* out;            // [nv] voxels sorted by bin
+};
+cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a);
 cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a);
 // C [Lp+1][K] (FP64) = the expansion coefficients of one point set.
 cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C);

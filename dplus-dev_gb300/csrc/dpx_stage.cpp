@@ -19,7 +19,8 @@ size_t put(std::vector<char>& h, const void* src, size_t n) {
 }
 }  // namespace
 
-void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t) {
+void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t,
+                bool direct_boxes) {
     // centring: FP32 grids shift host atoms by the given centre or their
     // centroid, restored per cell as e^{i q.c}; FP64 grids take host atoms as
     // they are; device atoms arrive already shifted by the given centre
@@ -60,7 +61,7 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
     t.pref = put(h, pref.data(), pref.size() * sizeof(int64_t));
     t.n_boxes = d.n_boxes > 0 && d.boxes ? d.n_boxes : 0;
     t.boxes = SIZE_MAX;
-    if (t.n_boxes) {  // {cx, cy, cz, w}, {Lx, Ly, Lz, 0}, centres shifted like the atoms
+    if (t.n_boxes && direct_boxes) {  // {cx, cy, cz, w}, {Lx, Ly, Lz, 0}, centres shifted like the atoms
         // sorted by extent (as PrepareParametersForGPU sorts, PDBAmplitude.cpp:1351-1360) so
         // the fill recomputes its extent factors only where an extent changes
         std::vector<int64_t> order(t.n_boxes);
@@ -80,10 +81,10 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
                                    (float)((double)s[2] - t.cen[2]), s[3]);
             b[2 * i + 1] = make_float4(s[4], s[5], s[6], 0.f);
         }
-        for (int64_t i = 0; i < t.n_boxes; ++i) {
-            const float* s = d.boxes + 8 * i;
-            origin += (double)s[3] * (double)s[4] * (double)s[5] * (double)s[6];
-        }
+    }
+    for (int64_t i = 0; i < t.n_boxes; ++i) {
+        const float* s = d.boxes + 8 * i;
+        origin += (double)s[3] * (double)s[4] * (double)s[5] * (double)s[6];
     }
     t.origin = origin * d.scale;
 }
