@@ -35,6 +35,10 @@ N_DIRS, DIR_SEED = 100_000, 1234
 # ncu dram__bytes_read+write of fill_f32_kernel on the profile shape (2,000 atoms,
 # 120 layers, 11.3 M cells): 335 MB, i.e. 29.6 B per cell; scaled to 50.7 M cells
 FILL_TRAFFIC = 29.6 * 50688289
+# ncu dram__bytes_read+write of the voxel hm_moments launch per point (atoms and
+# voxels are read once, the per-unit moments written once): set from the capture
+# summarised under profiles/, None until then
+MOMENTS_TRAFFIC = None
 # scale, solventED, c1, voxelStep, probe radius, solvation thickness, outer (layer) ED, fillHoles,
 # solventOnly, radius type 4 (dummy atoms): dummy-atom solvent at 333 e/nm^3 and a 0.3 nm voxelized
 # solvation layer at 400 e/nm^3
@@ -120,8 +124,11 @@ def build_inputs():
 
 
 def shape_label(shape) -> str:
-    """'CxT' + 'kN' (N phi columns on the FMA pipe) + 'p' (persistent)."""
+    """'CxT' + 'kN' (N phi columns on the FMA pipe) + 'p' (persistent);
+    (0, 0, 0, 0) is the harmonic method."""
     c, t, persistent = shape[0], shape[1], shape[2]
+    if c == 0:
+        return "harmonic"
     poly = shape[3] if len(shape) > 3 else 0
     return "%dx%d%s%s" % (c, t, "k%d" % poly if poly else "", "p" if persistent else "")
 
@@ -166,8 +173,7 @@ def run_dpx(args):
     ctx.set_stream(stream.cuda_stream)
     if args.fill_shape:
         apply_fill_shape(ctx, args.fill_shape)
-    if args.fill_method == "harmonic":
-        ctx.set_fill_method(_lib.DPX_FILL_HARMONIC)
+    ctx.set_fill_method(_lib.DPX_FILL_HARMONIC if args.fill_method == "harmonic" else _lib.DPX_FILL_DIRECT)
 
     amp, Q, dirs = build_inputs()
     sfu_c = C.c_double()
@@ -249,12 +255,19 @@ def run_dpx(args):
         t1.record(stream)
         barrier()
         dev_ms = t0.elapsed_time(t1)
-        # per-kernel split (separate pass so that the timed loop has no extra events)
+        # per-kernel split (separate pass so that the timed loop has no extra events);
+        # the harmonic fill's own stage events give its moments kernels' time
+        _lib.check(L.dpx_ctx_set_timing(ctx.handle, 1))
+        stages = []
         for _ in range(max(1, min(3, args.steps))):
             solve(True, timed_parts=True)
             torch.cuda.synchronize()
             for k, (a, b) in ev.items():
                 times[k].append(a.elapsed_time(b))
+            st5 = np.zeros(5)
+            _lib.check(L.dpx_ctx_stage_times(ctx.handle, _lib.dptr(st5)))
+            stages.append(st5)
+        _lib.check(L.dpx_ctx_set_timing(ctx.handle, 0))
         # end-to-end through the C-ABI with host buffers (atoms in, I(q) out)
         barrier()
         w0 = time.perf_counter()
@@ -295,6 +308,35 @@ def run_dpx(args):
         achieved = sfu_ops / (fill_ms / 1e3) / 1e12
         n_brackets = GRID_SIZE // 2
         interp_bytes = float(N_DIRS) * n_brackets * (4 * 4 * 2 * 16)  # 4 planes x 4 rows x 2 nodes x 16 B
+        if ctx.fill_method() == _lib.DPX_FILL_HARMONIC and stages and stages[-1][2] > 0:
+            st5 = np.median(np.array(stages), axis=0)
+            mom_ms, syn_ms, harm_ms, n_pts, kk = (float(v) for v in st5)
+            # moments: per point and (l, m) six weights times a complex basis value = 24 flops
+            flops = n_pts * kk * 24.0
+            fp32_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+            roofline = {"bound": "fp32", "kernel": "hm_moments", "method": "harmonic",
+                        "achieved": flops / (mom_ms / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": flops / (mom_ms / 1e3) / 1e12 / fp32_peak, "traffic": MOMENTS_TRAFFIC,
+                        "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 flops x max SM clock): "
+                                     "no measured FP32 peak is on file",
+                        "note": "flops = points (atoms + solvent voxels) x K x 6 moments x 4 (complex "
+                                "multiply-add); the fill also holds the synthesis and the radial tables",
+                        "points": n_pts, "K": kk,
+                        "stage_ms": {"moments": mom_ms, "synthesis": syn_ms, "harmonic_fill": harm_ms},
+                        "equivalent_direct_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)}
+        else:
+            roofline = {"bound": "sfu",
+                        "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] and not n_boxes else "flat"),
+                        "method": "direct", "fill_shape": shape_label(ctx.fill_shape()),
+                        "achieved": achieved, "peak": sfu_peak,
+                        "unit": "T sin/cos-eval/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
+                        "peak_kind": "measured (sincos calibration kernel, dpx_measure_sfu_peak)"
+                                     + (", x (1+CPT)/(1+CPT-k): k sincos per item on the FMA pipe" if kp else ""),
+                        "sfu_measured": sfu_measured / 1e12,
+                        "peak_nominal_16_per_sm_clk": sfu_nominal,
+                        "note": "SFU ops = (atoms + solvent boxes) x work items x 2(1+CPT) (row-factored fill); "
+                                "traffic = ncu dram bytes of the profile shape scaled by cells",
+                        "algorithmic_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)}
         out = {
             "metric": "I(q) solves/s (FP32-bulk, 20k-atom subunit, L=200, 500 q)",
             "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -306,18 +348,7 @@ def run_dpx(args):
                     "note": "voxelization (host, once per structure) excluded: voxelize_s"},
             "voxelize_s": voxelize_s, "solvent_boxes": n_boxes,
             "gpu_launches": args.steps * 4,
-            "roofline": {"bound": "sfu",
-                         "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] and not n_boxes else "flat"),
-                         "fill_shape": shape_label(ctx.fill_shape()),
-                         "achieved": achieved, "peak": sfu_peak,
-                         "unit": "T sin/cos-eval/s", "frac": achieved / sfu_peak, "traffic": FILL_TRAFFIC,
-                         "peak_kind": "measured (sincos calibration kernel, dpx_measure_sfu_peak)"
-                                      + (", x (1+CPT)/(1+CPT-k): k sincos per item on the FMA pipe" if kp else ""),
-                         "sfu_measured": sfu_measured / 1e12,
-                         "peak_nominal_16_per_sm_clk": sfu_nominal,
-                         "note": "SFU ops = (atoms + solvent boxes) x work items x 2(1+CPT) (row-factored fill); "
-                                 "traffic = ncu dram bytes of the profile shape scaled by cells",
-                         "algorithmic_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)},
+            "roofline": roofline,
             "roofline_average": {"bound": "hbm", "kernel": "average_kernel",
                                  "achieved": interp_bytes / (avg_ms / 1e3) / 1e9, "peak": peaks["hbm_gbs"],
                                  "unit": "GB/s", "frac": interp_bytes / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"],
@@ -777,7 +808,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dpx", choices=["dpx", "reference"])
     ap.add_argument("--fill-shape", default="", help="CxT[kN][p]: N phi columns on the FMA pipe, p = persistent")
-    ap.add_argument("--fill-method", default="direct", choices=["direct", "harmonic"],
+    ap.add_argument("--fill-method", default="harmonic", choices=["direct", "harmonic"],
                     help="FP32 amplitude fill: direct sum, or multipole expansion")
     ap.add_argument("--autotune", action="store_true", help="sweep the fill shapes first and use the fastest")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

@@ -58,12 +58,14 @@ size_t cell_bytes(int precision) { return precision == DPX_FP64 ? sizeof(double4
 
 // FP32 fill launch shapes the autotuner sweeps: {cells per work item, threads
 // per block (= atoms per shared-memory tile), persistent schedule, columns
-// whose sincos run on the FMA pipe}; flat and persistent forms pairwise.
+// whose sincos run on the FMA pipe}; flat and persistent forms pairwise; the
+// row {0, 0, 0, 0} stands for the harmonic method.
 extern const int kFillShape[][4] = {{2, 256, 0, 0}, {2, 256, 1, 0}, {4, 128, 0, 0}, {4, 128, 1, 0}, {4, 256, 0, 0},
                                     {4, 256, 1, 0}, {6, 128, 0, 0}, {6, 128, 1, 0}, {6, 256, 0, 0}, {6, 256, 1, 0},
                                     {8, 128, 0, 0}, {8, 128, 1, 0}, {8, 256, 0, 0}, {8, 256, 1, 0}, {8, 128, 0, 1},
-                                    {8, 128, 1, 1}, {8, 128, 0, 2}, {8, 128, 1, 2}, {8, 128, 0, 3}, {8, 128, 1, 3}};
-extern const int kFillShapes = 20;
+                                    {8, 128, 1, 1}, {8, 128, 0, 2}, {8, 128, 1, 2}, {8, 128, 0, 3}, {8, 128, 1, 3},
+                                    {0, 0, 0, 0}};  // the last row: the harmonic method
+extern const int kFillShapes = 21;
 
 // Unique-ion form factors minus the Gaussian dummy-atom solvent
 // (Atomic Form Factor.cpp:91-115, 121-176; r_m :11-27) for shells 0..Lp,
@@ -198,6 +200,8 @@ void ctx_release(dpx_ctx ctx) {
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
                       &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels})
         b->release();
+    for (cudaEvent_t e : ctx->tev)
+        if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -229,8 +233,8 @@ int dpx_ctx_synchronize(dpx_ctx ctx) {
 
 int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cpt, int threads) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
-    for (int k = 0; k < kFillShapes; k += 2)
-        if (kFillShape[k][0] == cpt && kFillShape[k][1] == threads) {
+    for (int k = 0; k < kFillShapes; ++k)
+        if (cpt > 0 && kFillShape[k][0] == cpt && kFillShape[k][1] == threads) {
             ctx->fill_cpt = cpt;
             ctx->fill_threads = threads;
             ctx->fill_poly = 0;
@@ -249,6 +253,35 @@ int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns) {
         }
     return fail(DPX_ERR_ARG, "no %d x %d fill with %d FMA-pipe columns", ctx->fill_cpt, ctx->fill_threads,
                 poly_columns);
+}
+
+int dpx_ctx_set_timing(dpx_ctx ctx, int on) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    ctx->timing = on != 0;
+    ctx->tev_used = 0;
+    return DPX_OK;
+}
+
+int dpx_ctx_stage_times(dpx_ctx ctx, double* out) {
+    if (!ctx || !out) return fail(DPX_ERR_ARG, "NULL argument");
+    for (int k = 0; k < 5; ++k) out[k] = 0.0;
+    if (ctx->tev_used == 0) return DPX_OK;
+    if (int rc = set_device(ctx)) return rc;
+    DPX_CUDA(cudaEventSynchronize(ctx->tev[7]));
+    float ms = 0.f;
+    DPX_CUDA(cudaEventElapsedTime(&ms, ctx->tev[0], ctx->tev[1]));
+    out[0] = ms;
+    if (ctx->tev_used == 8) {
+        DPX_CUDA(cudaEventElapsedTime(&ms, ctx->tev[2], ctx->tev[3]));
+        out[0] += ms;
+    }
+    DPX_CUDA(cudaEventElapsedTime(&ms, ctx->tev[4], ctx->tev[5]));
+    out[1] = ms;
+    DPX_CUDA(cudaEventElapsedTime(&ms, ctx->tev[6], ctx->tev[7]));
+    out[2] = ms;
+    out[3] = ctx->stage_points;
+    out[4] = ctx->stage_k;
+    return DPX_OK;
 }
 
 int dpx_ctx_set_fill_method(dpx_ctx ctx, int method) {
@@ -460,11 +493,16 @@ int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, in
     }
     int rc = DPX_OK, bi = -1;
     float bt = 0.f;
+    const int method0 = ctx->fill_method;
     for (int k = 0; k < kFillShapes && !rc; ++k) {
         float tot = 0.f;
+        const bool harmonic = kFillShape[k][0] == 0;
+        ctx->fill_method = harmonic ? DPX_FILL_HARMONIC : DPX_FILL_DIRECT;
         for (int r = 0; r <= repeats && !rc; ++r) {  // r = 0 warms up
-            rc = fill_batch_impl(n, grids, pdbs, kFillShape[k][0], kFillShape[k][1], kFillShape[k][3],
-                                 kFillShape[k][2] != 0, e0, e1);
+            rc = harmonic ? fill_batch_impl(n, grids, pdbs, ctx->fill_cpt, ctx->fill_threads, ctx->fill_poly,
+                                            ctx->fill_persistent, e0, e1)
+                          : fill_batch_impl(n, grids, pdbs, kFillShape[k][0], kFillShape[k][1], kFillShape[k][3],
+                                            kFillShape[k][2] != 0, e0, e1);
             float ms = 0.f;
             if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = fail(DPX_ERR_CUDA, "event timing");
             if (r > 0) tot += ms;
@@ -478,11 +516,17 @@ int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, in
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    ctx->fill_method = method0;
     if (rc) return rc;
-    ctx->fill_cpt = kFillShape[bi][0];
-    ctx->fill_threads = kFillShape[bi][1];
-    ctx->fill_persistent = kFillShape[bi][2] != 0;
-    ctx->fill_poly = kFillShape[bi][3];
+    if (kFillShape[bi][0] == 0) {
+        ctx->fill_method = DPX_FILL_HARMONIC;
+    } else {
+        ctx->fill_method = DPX_FILL_DIRECT;
+        ctx->fill_cpt = kFillShape[bi][0];
+        ctx->fill_threads = kFillShape[bi][1];
+        ctx->fill_persistent = kFillShape[bi][2] != 0;
+        ctx->fill_poly = kFillShape[bi][3];
+    }
     if (best)
         for (int j = 0; j < 4; ++j) best[j] = kFillShape[bi][j];
     // leave the grids filled with the chosen shape: shapes with FMA-pipe

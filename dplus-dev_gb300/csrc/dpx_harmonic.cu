@@ -564,6 +564,10 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C
     const size_t smem = oY + ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16 + (size_t)tp * 2 * sizeof(float4) +
                         (size_t)tp * sizeof(float4);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    if (a.ev0) {
+        cudaError_t e = cudaEventRecord(a.ev0, s);
+        if (e != cudaSuccess) return e;
+    }
     if (slices == 1) {
         cudaError_t e = cudaFuncSetAttribute(hm_moments<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -574,6 +578,10 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C
         if (e != cudaSuccess) return e;
         hm_moments<false><<<dim3(a.n_units, slices), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp,
                                                                            (float)a.delta, a.ab, a.nmm, a.MP);
+    }
+    if (a.ev1) {
+        cudaError_t e = cudaEventRecord(a.ev1, s);
+        if (e != cudaSuccess) return e;
     }
     const int64_t ng = (int64_t)a.G * kNodes * a.K;
     hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.G, a.K, a.M);

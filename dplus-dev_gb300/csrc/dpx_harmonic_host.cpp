@@ -325,6 +325,16 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     }
     char* base = static_cast<char*>(ctx->harmonic.p);
     cudaStream_t st = ctx->stream;
+    cudaEvent_t* ev = nullptr;  // [0, 1] atoms' moments, [2, 3] voxels' moments, [4, 5] synthesis, [6, 7] fill
+    if (ctx->timing) {
+        for (cudaEvent_t& e : ctx->tev)
+            if (!e) DPX_CUDA(cudaEventCreate(&e));
+        ev = ctx->tev;
+        ctx->tev_used = n_vox ? 8 : 6;
+        ctx->stage_points = (double)atoms.size() + (double)n_vox;
+        ctx->stage_k = K;
+        DPX_CUDA(cudaEventRecord(ev[6], st));
+    }
     DPX_CUDA(cudaMemcpyAsync(base, h.data(), staged, cudaMemcpyHostToDevice, st));
     const int* d_lmax = reinterpret_cast<const int*>(base + oL);
     dpx::HarmonicTables tb{};
@@ -364,6 +374,8 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         a.aff = reinterpret_cast<const float*>(dbase + t.aff);
         a.MP = reinterpret_cast<float2*>(base + oMP);
         a.M = reinterpret_cast<float2*>(base + oM);
+        a.ev0 = ev ? ev[2 * k] : nullptr;
+        a.ev1 = ev ? ev[2 * k + 1] : nullptr;
         DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
     }
     dpx::HarmonicSynth y{};
@@ -386,7 +398,12 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     y.scale = (float)d.scale;
     y.origin = t.origin;
     y.grid = reinterpret_cast<float4*>(grid);
+    if (ev) DPX_CUDA(cudaEventRecord(ev[4], st));
     DPX_CUDA(dpx::launch_harmonic_synth(st, y));
+    if (ev) {
+        DPX_CUDA(cudaEventRecord(ev[5], st));
+        DPX_CUDA(cudaEventRecord(ev[7], st));
+    }
     // the staging vector was copied from pageable memory (the call returns once
     // it is staged); the arena stays owned by the context
     return DPX_OK;

@@ -58,7 +58,14 @@ struct dpx_ctx_s {
     int fill_cpt = 8, fill_threads = 128;  // FP32 fill shape (dpx_autotune_fill)
     bool fill_persistent = false;
     int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
-    int fill_method = 0;  // DPX_FILL_DIRECT / DPX_FILL_HARMONIC
+    int fill_method = 1;  // DPX_FILL_HARMONIC (default) / DPX_FILL_DIRECT
+    // stage timing of the last harmonic fill (dpx_ctx_set_timing): events
+    // around the moments of the atoms and of the voxels, the synthesis and the
+    // whole fill; the points and K of that fill
+    bool timing = false;
+    cudaEvent_t tev[8] = {};
+    int tev_used = 0;
+    double stage_points = 0, stage_k = 0;
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
     std::vector<char> host_stage;

@@ -165,6 +165,7 @@ struct HarmonicSet {
     const float* aff;       // [U][Lp+1] ion form factors (atoms)
     float2* MP;             // [n_units][6][K]
     float2* M;              // [G][6][K]
+    cudaEvent_t ev0, ev1;   // recorded around the moments launch when not null
 };
 struct HarmonicSynth {
     const int2* rows;       // (i, t) of every theta row t <= 3i/2, i >= 1

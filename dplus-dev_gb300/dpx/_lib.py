@@ -76,6 +76,8 @@ _SIGS = {
     "dpx_ctx_set_fill_poly": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_set_fill_method": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_get_fill_method": (C.c_int, [_P]),
+    "dpx_ctx_set_timing": (C.c_int, [_P, C.c_int]),
+    "dpx_ctx_stage_times": (C.c_int, [_P, _D]),
     "dpx_ctx_get_fill_shape": (C.c_int, [_P, _I]),
     "dpx_fill_shapes": (C.c_int, [_I]),
     "dpx_grid_cells": (C.c_int64, [C.c_int]),

@@ -83,22 +83,32 @@ int dpx_ctx_set_fill_shape(dpx_ctx ctx, int cells_per_thread, int threads);
 int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent);
 /* Phi columns per work item whose sin/cos run as polynomials on the FMA pipe
  * instead of the SFU (0-3 for the 8 x 128 shape, 0 otherwise; reset to 0 by
- * dpx_ctx_set_fill_shape).  The SFU bounds the fill and leaves the FMA pipe
- * half idle, so a few such columns balance the two pipes. */
+ * dpx_ctx_set_fill_shape): meant to share the work between the two pipes; on
+ * GB300 they measure slower than the SFU alone and the autotuner keeps 0. */
 int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns);
 /* FP32 fill method.  DPX_FILL_DIRECT: the direct sum over points and cells
- * (the reference's algorithm, PDBAmplitude.cpp:243-317).  DPX_FILL_HARMONIC:
- * the same amplitudes by multipole expansion (no counterpart in the
- * reference): per shell i the plane-wave expansion is cut at order
+ * (the reference's algorithm, PDBAmplitude.cpp:243-317).  DPX_FILL_HARMONIC
+ * (the default; no counterpart in the reference): the same amplitudes by
+ * multipole expansion.  Per shell i the plane-wave expansion is cut at order
  * l_i = ceil(q_i R + 3 (q_i R)^(1/3) + 6) (R the largest point distance from
- * the centre), the expansion coefficients are a GEMM-shaped sum over the
- * points, and each theta row is synthesized from them; solvent boxes are
- * expanded into their voxels (dpx_pdb_desc.voxel_step).  Leaves it cannot take
- * (device atoms, boxes without a voxel step, orders above 175) use the direct
- * sum.  FP64 grids always use the direct sum. */
+ * the centre); points are grouped by radius and their expansion coefficients
+ * summed per group; each theta row is synthesized from the coefficients; solvent
+ * boxes are expanded into their voxels (dpx_pdb_desc.voxel_step).  It serves
+ * dpx_grid_fill_pdb and dpx_grid_fill_pdb_batch; leaves it cannot take (boxes
+ * without a voxel step, orders above 175, more than 1024 radial bins of
+ * solvent) use the direct sum, as do FP64 grids and the batched-solve and
+ * serving fills.  dpx_autotune_fill times it beside the direct shapes (the
+ * row {0, 0, 0, 0} of dpx_fill_shapes). */
 enum { DPX_FILL_DIRECT = 0, DPX_FILL_HARMONIC = 1 };
 int dpx_ctx_set_fill_method(dpx_ctx ctx, int method);
 int dpx_ctx_get_fill_method(dpx_ctx ctx);
+/* Stage timing of harmonic fills (no counterpart in the reference): with
+ * timing on, the fill records CUDA events on the context's stream;
+ * dpx_ctx_stage_times then gives out[5] = {ms of the moments kernels, ms of
+ * the synthesis, ms of the whole harmonic fill, points (atoms + voxels), K}
+ * of the last harmonic fill (zeros when there was none). */
+int dpx_ctx_set_timing(dpx_ctx ctx, int on);
+int dpx_ctx_stage_times(dpx_ctx ctx, double* out);
 /* shape[4] = {cells_per_thread, threads, persistent, poly_columns} in use. */
 int dpx_ctx_get_fill_shape(dpx_ctx ctx, int* shape);
 /* The shapes the autotuner sweeps: writes 4 ints per shape (if shapes != NULL)

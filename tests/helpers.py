@@ -1,4 +1,6 @@
 """Shared builders for the parity tests (seeded inputs; the oracle is the checker)."""
+import contextlib
+
 import numpy as np
 
 import oracle as O
@@ -21,6 +23,18 @@ def oracle_grid(amp, gs, qmax, mode=O.FP64):
     s = O.Struct.from_pdb(amp)
     data = O.grid_fill(s, gs, qmax, mode)
     return data, O.grid_splines(gs, data, mode)
+
+
+@contextlib.contextmanager
+def fill_method(ctx, method):
+    """Run a block with the context's FP32 fill method set (the batched-solve
+    and serving engines fill with the direct sum)."""
+    before = ctx.fill_method()
+    ctx.set_fill_method(method)
+    try:
+        yield ctx
+    finally:
+        ctx.set_fill_method(before)
 
 
 def rel(a, b):

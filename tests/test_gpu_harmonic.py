@@ -18,9 +18,10 @@ TOL32 = 1e-4
 
 @pytest.fixture
 def harmonic(ctx):
+    before = ctx.fill_method()
     ctx.set_fill_method(_lib.DPX_FILL_HARMONIC)
     yield ctx
-    ctx.set_fill_method(_lib.DPX_FILL_DIRECT)
+    ctx.set_fill_method(before)
 
 
 @pytest.mark.parametrize("extra,centered", [(VACUUM, False), (SOLVENT, True), (SOLVENT, False), (LAYER, False)])
@@ -55,11 +56,12 @@ def test_harmonic_and_direct_fill_agree_in_a_batch(ctx):
     leaves = [globule(900, 1.7, seed=144, extra=LAYER), globule(300, 1.0, seed=145, extra=VACUUM)]
     qmax = 4.0
     got = {}
+    before = ctx.fill_method()
     for method in (_lib.DPX_FILL_DIRECT, _lib.DPX_FILL_HARMONIC):
         ctx.set_fill_method(method)
         for a in leaves:
             a._grid = None
         got[method] = [g.read(True, False)[0] for g in M.calculate_grids(ctx, leaves, qmax, 30, M.FP32)]
-    ctx.set_fill_method(_lib.DPX_FILL_DIRECT)
+    ctx.set_fill_method(before)
     for x, y in zip(got[_lib.DPX_FILL_DIRECT], got[_lib.DPX_FILL_HARMONIC]):
         assert rel_to_max(y, x) <= 2e-6

@@ -15,7 +15,7 @@ import oracle as O
 import dpx
 from dpx import _lib
 from dpx import models as M
-from helpers import BOXES5, LAYER, SOLVENT, VACUUM, globule, oracle_grid, rel, rel_to_max
+from helpers import BOXES5, LAYER, SOLVENT, VACUUM, fill_method, globule, oracle_grid, rel, rel_to_max
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -485,8 +485,9 @@ def test_dropin_sum_grids(ctx):
 
 
 def test_fill_schedules_and_autotuner(ctx):
-    """Flat and persistent FP32 fills give identical cells for every shape; the
-    autotuner keeps one of the swept shapes and its grids match a fill with it."""
+    """Direct sum: flat and persistent FP32 fills give identical cells for every
+    shape; the autotuner keeps one of the swept shapes (or the harmonic method)."""
+    ctx.set_fill_method(_lib.DPX_FILL_DIRECT)
     gs, qmax = 26, 4.0
     leaves = [globule(700, 1.8, seed=71, extra=SOLVENT), globule(90, 0.7, seed=72, extra=VACUUM)]
     for cpt, th in [(2, 256), (4, 128), (8, 128), (8, 256)]:
@@ -513,11 +514,15 @@ def test_fill_schedules_and_autotuner(ctx):
     ctx.set_fill_schedule(False)
     best, table = M.autotune_fill(ctx, leaves, qmax, gs, repeats=1)
     assert best in table and len(table) == dpx.lib().dpx_fill_shapes(None)
-    assert {(8, 128, 0, k) for k in range(4)} <= set(table)
-    assert ctx.fill_shape() == best
+    assert {(8, 128, 0, k) for k in range(4)} <= set(table) and (0, 0, 0, 0) in table
+    if best == (0, 0, 0, 0):
+        assert ctx.fill_method() == _lib.DPX_FILL_HARMONIC
+    else:
+        assert ctx.fill_method() == _lib.DPX_FILL_DIRECT and ctx.fill_shape() == best
     assert all(t > 0 for t in table.values())
     ctx.set_fill_shape(8, 128)
     ctx.set_fill_schedule(False)
+    ctx.set_fill_method(_lib.DPX_FILL_HARMONIC)
 
 
 @pytest.mark.parametrize("kp", [1, 2, 3])
@@ -528,6 +533,7 @@ def test_fill_fma_pipe_columns_match_oracle(ctx, kp, extra):
     voxelized layer), and I(q) within 1e-4 of the plain FP64 path."""
     amp = globule(1500, 2.2, seed=90 + kp, extra=extra)
     gs, qmax = 40, 5.0
+    ctx.set_fill_method(_lib.DPX_FILL_DIRECT)
     ctx.set_fill_shape(8, 128, kp)
     try:
         g = amp.calculateGrid(ctx, qmax, gs, M.FP32)
@@ -543,6 +549,7 @@ def test_fill_fma_pipe_columns_match_oracle(ctx, kp, extra):
         assert rel(I[M.FP32], I[M.FP64]) <= TOL32
     finally:
         ctx.set_fill_shape(8, 128, 0)
+        ctx.set_fill_method(_lib.DPX_FILL_HARMONIC)
         amp._grid = None
 
 
@@ -567,8 +574,9 @@ def test_solve_batch_equals_single_solves(ctx, prec):
     splits the batch into several waves; replaying the graphs is stable."""
     leaves, gss, qms, Qs = _batch_case()
     dirs = M.mc_directions(9, 500)
-    singles = [M.DomainModel([a], gs, qm, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
-               for a, gs, qm, Q in zip(leaves, gss, qms, Qs)]
+    with fill_method(ctx, _lib.DPX_FILL_DIRECT):  # the batch fills with the direct sum
+        singles = [M.DomainModel([a], gs, qm, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+                   for a, gs, qm, Q in zip(leaves, gss, qms, Qs)]
     for budget in (0, 1):  # 1 byte: every structure is its own wave
         b = M.SolveBatch(ctx, leaves, gss, qms, Qs, dirs, precision=prec, grid_budget_bytes=budget)
         waves, launches, _ = b.info()

@@ -4,9 +4,10 @@ budget admits and evicts, and requests that cannot fit fail cleanly."""
 import numpy as np
 import pytest
 
+from dpx import _lib
 from dpx import models as M
 from dpx.serve import Server
-from helpers import LAYER, SOLVENT, VACUUM, globule
+from helpers import LAYER, SOLVENT, VACUUM, fill_method, globule
 
 pytestmark = pytest.mark.gpu
 
@@ -38,8 +39,14 @@ def _mix():
 
 
 def _direct(ctx, req, dirs):
+    """One DomainModel solve, filled with the direct sum as the server fills."""
     amps, gs, qmax, Q, prec = req
-    return M.DomainModel(amps, gs, qmax, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
+    for a in amps:
+        for leaf in (a, getattr(a, "child", None)):
+            if leaf is not None:
+                leaf._grid = None
+    with fill_method(ctx, _lib.DPX_FILL_DIRECT):
+        return M.DomainModel(amps, gs, qmax, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
 
 
 def test_server_same_alone_and_in_the_mix(ctx):
