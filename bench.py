@@ -35,10 +35,10 @@ N_DIRS, DIR_SEED = 100_000, 1234
 # ncu dram__bytes_read+write of fill_f32_kernel on the profile shape (2,000 atoms,
 # 120 layers, 11.3 M cells): 335 MB, i.e. 29.6 B per cell; scaled to 50.7 M cells
 FILL_TRAFFIC = 29.6 * 50688289
-# ncu dram__bytes_read+write of the voxel hm_moments launch per point (atoms and
-# voxels are read once, the per-unit moments written once): set from the capture
-# summarised under profiles/, None until then
-MOMENTS_TRAFFIC = None
+# ncu dram__bytes_read+write of the voxel hm_moments launch on the profile shape
+# (about 452,000 voxels): 6.93 MB read, 0 written, i.e. 15.7 B per point (each
+# point read once); scaled to the points of the workload
+MOMENTS_BYTES_PER_POINT = 15.7
 # scale, solventED, c1, voxelStep, probe radius, solvation thickness, outer (layer) ED, fillHoles,
 # solventOnly, radius type 4 (dummy atoms): dummy-atom solvent at 333 e/nm^3 and a 0.3 nm voxelized
 # solvation layer at 400 e/nm^3
@@ -316,7 +316,8 @@ def run_dpx(args):
             fp32_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
             roofline = {"bound": "fp32", "kernel": "hm_moments", "method": "harmonic",
                         "achieved": flops / (mom_ms / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
-                        "frac": flops / (mom_ms / 1e3) / 1e12 / fp32_peak, "traffic": MOMENTS_TRAFFIC,
+                        "frac": flops / (mom_ms / 1e3) / 1e12 / fp32_peak,
+                        "traffic": MOMENTS_BYTES_PER_POINT * n_pts,
                         "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 flops x max SM clock): "
                                      "no measured FP32 peak is on file",
                         "note": "flops = points (atoms + solvent voxels) x K x 6 moments x 4 (complex "
