@@ -832,6 +832,7 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
     plan.need_dir = 0;
     for (const auto& M : md)
         if (!M.plain || M.n_groups > 0) plan.need_dir = 1;
+    plan.one_leaf = (n_models == 1 && md[0].n_groups == 0) ? 1 : 0;
     const size_t pb = br_layer.size() * sizeof(int) + br_off.size() * sizeof(int) + br_qidx.size() * sizeof(int) +
                       br_q.size() * sizeof(double) + 64;
     DPX_CUDA(ctx->plan.reserve(pb + md.size() * sizeof(dpx::ModelDev) + 64));

@@ -174,6 +174,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         P.n_chunks = (n_samples + P.chunk_off + P.chunk - 1) / P.chunk;
         P.dir_stride = 0;
         P.need_dir = 0;
+        P.one_leaf = 1;
         partial_max = std::max(partial_max, ((size_t)P.n_brackets * P.n_chunks + (size_t)P.n_brackets * 5) *
                                                 P.max_q * sizeof(double) + 64);
         p.origin = d.Q[0] == 0.0;

@@ -332,7 +332,17 @@ __global__ void __launch_bounds__(kBinThreads) vx_scatter(const float4* __restri
     }
 }
 
-// hm_groups: M[g][n][k] = sum of MP over the units [gu[g], gu[g+1]) of group g, FP64.
+// s += x with the rounding error of every addition carried in c (Knuth's
+// TwoSum): a compensated FP32 sum, about as accurate as an FP64 one.
+__device__ __forceinline__ void sum2(float& s, float& c, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+}
+
+// hm_groups: M[g][n][k] = sum of MP over the units [gu[g], gu[g+1]) of group g,
+// compensated.
 __global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, int G, int K,
                           float2* __restrict__ M) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,32 +350,33 @@ __global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__
     if (e >= (int64_t)G * per) return;
     const int g = (int)(e / per);
     const int64_t r = e % per;
-    double re = 0.0, im = 0.0;
+    float re = 0.f, rc = 0.f, im = 0.f, ic = 0.f;
     for (int u = gu[g]; u < gu[g + 1]; ++u) {
         const float2 v = MP[(int64_t)u * per + r];
-        re += (double)v.x;
-        im += (double)v.y;
+        sum2(re, rc, v.x);
+        sum2(im, ic, v.y);
     }
-    M[e] = make_float2((float)re, (float)im);
+    M[e] = make_float2(re + rc, im + ic);
 }
 
 // ---------------------------------------------------------------------------
 // hm_contract: block (k slice of 128, tile of 8 shells); thread k.
-// groups[g] = {bin, ion (< 0: factor 1)}; C[i][k] = sum_g F sum_n T M.
+// groups[g] = {bin, ion (< 0: factor 1)}; C[i][k] = sum_g F sum_n T M,
+// summed across groups with compensation.
 // ---------------------------------------------------------------------------
 constexpr int kContractShells = 8;
 
 __global__ void __launch_bounds__(128) hm_contract(const float2* __restrict__ M, const int2* __restrict__ groups, int G,
                                                    const float* __restrict__ T, int nbins, int LM, int K, int Lp,
                                                    const int* __restrict__ lmax, const float* __restrict__ aff,
-                                                   double2* __restrict__ C) {
+                                                   float2* __restrict__ C) {
     const int k = blockIdx.x * 128 + threadIdx.x;
     const int i0 = 1 + blockIdx.y * kContractShells;
     if (k >= K) return;
     const int l = l_of(k);
-    double cr[kContractShells], ci[kContractShells];
+    float cr[kContractShells], ci[kContractShells], er[kContractShells], ei[kContractShells];
 #pragma unroll
-    for (int a = 0; a < kContractShells; ++a) cr[a] = ci[a] = 0.0;
+    for (int a = 0; a < kContractShells; ++a) cr[a] = ci[a] = er[a] = ei[a] = 0.f;
     for (int g = 0; g < G; ++g) {
         const int2 gb = groups[g];
         float2 mv[kNodes];
@@ -385,15 +396,15 @@ __global__ void __launch_bounds__(128) hm_contract(const float2* __restrict__ M,
                 si = fmaf(t[n], mv[n].y, si);
             }
             const float f = gb.y < 0 ? 1.f : aff[(int64_t)gb.y * (Lp + 1) + i];
-            cr[a] += (double)(f * sr);
-            ci[a] += (double)(f * si);
+            sum2(cr[a], er[a], f * sr);
+            sum2(ci[a], ei[a], f * si);
         }
     }
 #pragma unroll
     for (int a = 0; a < kContractShells; ++a) {
         const int i = i0 + a;
         if (i > Lp) continue;
-        C[(int64_t)i * K + k] = make_double2(cr[a], ci[a]);
+        C[(int64_t)i * K + k] = make_float2(cr[a] + er[a], ci[a] + ei[a]);
     }
 }
 
@@ -405,27 +416,56 @@ __device__ __forceinline__ float sinc_h(float h) {
 
 // ---------------------------------------------------------------------------
 // hm_synth: one block per theta row (i, t <= 3i/2); rows[] lists (i, t).
-// Dynamic shared memory: P column values [K_i], B and B' (atoms, voxels),
-// the 6i roots of unity.
+// The row's 6i cells are F(p) = sum_{|m| <= l_i} G_m w^{mp}, w = e^{2 pi i/6i},
+// with G_m = 4 pi sum_l i^l P_lm C_lm and G_-m = 4 pi sum_l i^l P_lm conj(C_lm)
+// (m > 0).  Writing p = s i + j (sextant s < 6, column j < i):
+//   F(s i + j) = sum_{r < 6} e^{2 pi i r s / 6} D_r(j),
+//   D_r(j) = sum_{m = r mod 6} G_m w^{mj},
+// so a thread per column j sums the G_m once into six residue classes and
+// finishes its six cells with a 6-point DFT.
+// Dynamic shared memory: P column values [K_i], G (atoms, voxels) over
+// m in [m0, m0 + nG) with zero padding (m0 = -6 ceil(l_i/6)), the 6i roots
+// of unity.
 // ---------------------------------------------------------------------------
-__global__ void hm_synth(const int2* __restrict__ rows, const double2* __restrict__ Ca, const double2* __restrict__ Cv,
-                         int K, const int* __restrict__ lmax, const float2* __restrict__ ab,
-                         const float* __restrict__ nmm, double step,
-                         float vox_s, double cx, double cy, double cz, int use_center, float scale, double origin,
-                         float4* __restrict__ grid) {
+constexpr int kSynthThreads = 128;
+
+__device__ __forceinline__ int synth_pad(int li) { return 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6); }
+
+__device__ __forceinline__ float2 i_pow_times(int l, float2 c) {  // i^l c
+    switch (l & 3) {
+        case 0: return c;
+        case 1: return make_float2(-c.y, c.x);
+        case 2: return make_float2(-c.x, -c.y);
+        default: return make_float2(c.y, -c.x);
+    }
+}
+
+// x = hi + lo (the FP32 pair nearest the FP64 value)
+__device__ __forceinline__ float2 split_ff(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+__global__ void __launch_bounds__(kSynthThreads) hm_synth(const int2* __restrict__ rows, const float2* __restrict__ Ca,
+                                                          const float2* __restrict__ Cv, int K,
+                                                          const int* __restrict__ lmax, const float2* __restrict__ ab,
+                                                          const float* __restrict__ nmm, double step, float vox_s,
+                                                          double cx, double cy, double cz, int use_center, float scale,
+                                                          double origin, float4* __restrict__ grid) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ float2 sRow[3];
     const int2 row = rows[blockIdx.x];
     const int i = row.x, t = row.y;
     const int li = lmax[i];
     const int Ki = k_of(li, li) + 1;
     const int nph = 6 * i, h = 3 * i;
-    float* sP = reinterpret_cast<float*>(smem);
-    float2* sB = reinterpret_cast<float2*>(smem + ((size_t)Ki * 4 + 15) / 16 * 16);
-    float2* sBp = sB + (li + 1);
-    float2* sBv = sBp + (li + 1);
-    float2* sBpv = sBv + (li + 1);
-    float2* sW = sBpv + (li + 1);
+    const int nG = synth_pad(li);
+    const int m0 = -6 * ((li + 5) / 6);
     const bool vox = Cv != nullptr;
+    float* sP = reinterpret_cast<float*>(smem);
+    float2* sG = reinterpret_cast<float2*>(smem + ((size_t)Ki * 4 + 15) / 16 * 16);
+    float2* sGv = sG + nG;
+    float2* sW = sGv + nG;
     float st, ct;
     sincospif((float)t / (float)h, &st, &ct);
     // Legendre column m per thread
@@ -447,93 +487,133 @@ __global__ void hm_synth(const int2* __restrict__ rows, const double2* __restric
         sincospif(2.f * (float)n / (float)nph, &sw, &cw);
         sW[n] = make_float2(cw, sw);
     }
+    if (threadIdx.x == 0) {
+        const double inv2pi = 0.15915494309189533577;
+        double sd, cd;
+        sincospi((double)t / (double)h, &sd, &cd);
+        const double qd = (double)i * step;
+        sRow[0] = split_ff(qd * sd * cx * inv2pi);
+        sRow[1] = split_ff(qd * sd * cy * inv2pi);
+        sRow[2] = split_ff(qd * cd * cz * inv2pi);
+    }
+    for (int n = threadIdx.x; n < nG; n += blockDim.x) {  // the padding beyond |m| <= l_i
+        const int m = m0 + n;
+        if (m > li || m < -li) {
+            sG[n] = make_float2(0.f, 0.f);
+            sGv[n] = make_float2(0.f, 0.f);
+        }
+    }
     __syncthreads();
-    // B_m = 4 pi sum_l i^l P_lm C_lm ; B'_m = 4 pi sum_l i^l P_lm conj(C_lm)
-    const double2* Cai = Ca + (int64_t)i * K;
-    const double2* Cvi = vox ? Cv + (int64_t)i * K : nullptr;
+    const float2* Cai = Ca + (int64_t)i * K;
+    const float2* Cvi = vox ? Cv + (int64_t)i * K : nullptr;
     for (int m = threadIdx.x; m <= li; m += blockDim.x) {
         float br = 0.f, bi = 0.f, pr = 0.f, pi_ = 0.f;
         float vr = 0.f, vi = 0.f, qr = 0.f, qi = 0.f;
         for (int l = m; l <= li; ++l) {
             const int k = k_of(l, m);
             const float p = sP[k];
-            const double2 cd = Cai[k];
-            const float2 c = make_float2((float)cd.x, (float)cd.y);
-            // i^l (c.x + i c.y) and i^l (c.x - i c.y)
-            float ar, ai, er, ei;
-            switch (l & 3) {
-                case 0: ar = c.x; ai = c.y; er = c.x; ei = -c.y; break;
-                case 1: ar = -c.y; ai = c.x; er = c.y; ei = c.x; break;
-                case 2: ar = -c.x; ai = -c.y; er = -c.x; ei = c.y; break;
-                default: ar = c.y; ai = -c.x; er = -c.y; ei = -c.x; break;
-            }
-            br = fmaf(p, ar, br);
-            bi = fmaf(p, ai, bi);
-            pr = fmaf(p, er, pr);
-            pi_ = fmaf(p, ei, pi_);
+            const float2 c = Cai[k];
+            const float2 a = i_pow_times(l, c), e = i_pow_times(l, make_float2(c.x, -c.y));
+            br = fmaf(p, a.x, br);
+            bi = fmaf(p, a.y, bi);
+            pr = fmaf(p, e.x, pr);
+            pi_ = fmaf(p, e.y, pi_);
             if (vox) {
-                const double2 dd = Cvi[k];
-                const float2 d = make_float2((float)dd.x, (float)dd.y);
-                switch (l & 3) {
-                    case 0: ar = d.x; ai = d.y; er = d.x; ei = -d.y; break;
-                    case 1: ar = -d.y; ai = d.x; er = d.y; ei = d.x; break;
-                    case 2: ar = -d.x; ai = -d.y; er = -d.x; ei = d.y; break;
-                    default: ar = d.y; ai = -d.x; er = -d.y; ei = -d.x; break;
-                }
-                vr = fmaf(p, ar, vr);
-                vi = fmaf(p, ai, vi);
-                qr = fmaf(p, er, qr);
-                qi = fmaf(p, ei, qi);
+                const float2 d = Cvi[k];
+                const float2 av = i_pow_times(l, d), ev = i_pow_times(l, make_float2(d.x, -d.y));
+                vr = fmaf(p, av.x, vr);
+                vi = fmaf(p, av.y, vi);
+                qr = fmaf(p, ev.x, qr);
+                qi = fmaf(p, ev.y, qi);
             }
         }
-        sB[m] = make_float2(kFourPi * br, kFourPi * bi);
-        sBp[m] = make_float2(m > 0 ? kFourPi * pr : 0.f, m > 0 ? kFourPi * pi_ : 0.f);
+        sG[m - m0] = make_float2(kFourPi * br, kFourPi * bi);
+        if (m > 0) sG[-m - m0] = make_float2(kFourPi * pr, kFourPi * pi_);
         if (vox) {
-            sBv[m] = make_float2(kFourPi * vr, kFourPi * vi);
-            sBpv[m] = make_float2(m > 0 ? kFourPi * qr : 0.f, m > 0 ? kFourPi * qi : 0.f);
+            sGv[m - m0] = make_float2(kFourPi * vr, kFourPi * vi);
+            if (m > 0) sGv[-m - m0] = make_float2(kFourPi * qr, kFourPi * qi);
         }
     }
     __syncthreads();
     const float qI = (float)((double)i * step);
     const int64_t base = shell_base(i);
-    for (int p = threadIdx.x; p < nph; p += blockDim.x) {
-        float ar = 0.f, ai = 0.f, vr = 0.f, vi = 0.f;
-        int idx = 0;  // (m p) mod 6i
-        for (int m = 0; m <= li; ++m) {
-            const float2 w = sW[idx];
-            const float2 b = sB[m], bp = sBp[m];
-            // b w + bp conj(w)
-            ar += b.x * w.x - b.y * w.y + bp.x * w.x + bp.y * w.y;
-            ai += b.x * w.y + b.y * w.x + bp.y * w.x - bp.x * w.y;
-            if (vox) {
-                const float2 c = sBv[m], cp = sBpv[m];
-                vr += c.x * w.x - c.y * w.y + cp.x * w.x + cp.y * w.y;
-                vi += c.x * w.y + c.y * w.x + cp.y * w.x - cp.x * w.y;
+    // centring phase q.c / 2 pi = A cos(phi) + B sin(phi) + Z per cell, the
+    // row constants A, B, Z in FP64 (set before the barrier above), held as
+    // FP32 pairs
+    const float2 A2 = sRow[0], B2 = sRow[1], Z2 = sRow[2];
+    constexpr float kS3 = 0.86602540378443865f;  // sin(pi/3)
+    const float wr6[6] = {1.f, 0.5f, -0.5f, -1.f, -0.5f, 0.5f};
+    const float wi6[6] = {0.f, kS3, kS3, 0.f, -kS3, -kS3};
+    for (int j = threadIdx.x; j < i; j += blockDim.x) {
+        float2 D[6], Dv[6];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) D[r] = Dv[r] = make_float2(0.f, 0.f);
+        int idx = (int)(((int64_t)m0 * j) % nph);
+        if (idx < 0) idx += nph;
+        for (int u = 0; u < nG; u += 6) {
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const float2 w = sW[idx];
+                const float2 g = sG[u + r];
+                D[r].x = fmaf(g.x, w.x, fmaf(-g.y, w.y, D[r].x));
+                D[r].y = fmaf(g.x, w.y, fmaf(g.y, w.x, D[r].y));
+                if (vox) {
+                    const float2 gv = sGv[u + r];
+                    Dv[r].x = fmaf(gv.x, w.x, fmaf(-gv.y, w.y, Dv[r].x));
+                    Dv[r].y = fmaf(gv.x, w.y, fmaf(gv.y, w.x, Dv[r].y));
+                }
+                idx += j;  // idx, j < 6i
+                if (idx >= nph) idx -= nph;
             }
-            idx += p;  // idx, p < 6i
-            if (idx >= nph) idx -= nph;
         }
-        float sp, cp;
-        sincospif((float)p / (float)h, &sp, &cp);
-        const float qx = qI * st * cp, qy = qI * st * sp, qz = qI * ct;
-        if (vox) {
-            const float f = vox_s * sinc_h(0.5f * qx * vox_s) * vox_s * sinc_h(0.5f * qy * vox_s) * vox_s *
-                            sinc_h(0.5f * qz * vox_s);
-            ar = fmaf(f, vr, ar);
-            ai = fmaf(f, vi, ai);
-        }
-        float2 F = make_float2(ar * scale, ai * scale);
-        if (use_center) {
-            double s1, c1;
-            sincos((double)qx * cx + (double)qy * cy + (double)qz * cz, &s1, &c1);
-            F = make_float2((float)(F.x * c1 - F.y * s1), (float)(F.x * s1 + F.y * c1));
-        }
-        grid[base + (int64_t)t * nph + p] = make_float4(F.x, F.y, 0.f, 0.f);
-        // Friedel: the antipode (3i - t, p + 3i) holds the conjugate (the
-        // equator row is its own mirror and is written once per cell)
-        if (2 * t != h) {
-            const int pm = p < h ? p + h : p - h;
-            grid[base + (int64_t)(h - t) * nph + pm] = make_float4(F.x, -F.y, 0.f, 0.f);
+#pragma unroll
+        for (int sx = 0; sx < 6; ++sx) {
+            float ar = 0.f, ai = 0.f, vr = 0.f, vi = 0.f;
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const int e = (r * sx) % 6;
+                ar += D[r].x * wr6[e] - D[r].y * wi6[e];
+                ai += D[r].x * wi6[e] + D[r].y * wr6[e];
+                if (vox) {
+                    vr += Dv[r].x * wr6[e] - Dv[r].y * wi6[e];
+                    vi += Dv[r].x * wi6[e] + Dv[r].y * wr6[e];
+                }
+            }
+            const int p = sx * i + j;
+            const float2 w = sW[p];  // (cos, sin) of the cell's phi = p pi / 3i
+            const float cp = w.x, sp = w.y;
+            const float qx = qI * st * cp, qy = qI * st * sp, qz = qI * ct;
+            if (vox) {
+                const float f = vox_s * sinc_h(0.5f * qx * vox_s) * vox_s * sinc_h(0.5f * qy * vox_s) * vox_s *
+                                sinc_h(0.5f * qz * vox_s);
+                ar = fmaf(f, vr, ar);
+                ai = fmaf(f, vi, ai);
+            }
+            float2 F = make_float2(ar * scale, ai * scale);
+            if (use_center) {
+                // turns = A cp + B sp + Z in double-float (Dekker's two-product,
+                // Knuth's two-sum), reduced by its nearest integer
+                const float p1 = __fmul_rn(A2.x, cp), e1 = fmaf(A2.x, cp, -p1);
+                const float p2 = __fmul_rn(B2.x, sp), e2 = fmaf(B2.x, sp, -p2);
+                const float s1 = __fadd_rn(p1, p2);
+                const float b1 = __fsub_rn(s1, p1);
+                const float f1 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s1, b1)), __fsub_rn(p2, b1));
+                const float s2 = __fadd_rn(s1, Z2.x);
+                const float b2 = __fsub_rn(s2, s1);
+                const float f2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(Z2.x, b2));
+                const float lo = e1 + e2 + f1 + f2 + Z2.y + A2.y * cp + B2.y * sp;
+                const float rt = __fsub_rn(s2, rintf(s2)) + lo;
+                float s1n, c1n;
+                sincospif(2.f * rt, &s1n, &c1n);
+                F = make_float2(F.x * c1n - F.y * s1n, F.x * s1n + F.y * c1n);
+            }
+            grid[base + (int64_t)t * nph + p] = make_float4(F.x, F.y, 0.f, 0.f);
+            // Friedel: the antipode (3i - t, p + 3i) holds the conjugate (the
+            // equator row is its own mirror and is written once per cell)
+            if (2 * t != h) {
+                const int pm = p < h ? p + h : p - h;
+                grid[base + (int64_t)(h - t) * nph + pm] = make_float4(F.x, -F.y, 0.f, 0.f);
+            }
         }
     }
     if (i == 1 && t == 0 && threadIdx.x == 0) grid[0] = make_float4((float)origin, 0.f, 0.f, 0.f);
@@ -552,7 +632,7 @@ cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C) {
+cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C) {
     const int slices = (a.K + kSliceK - 1) / kSliceK;
     int kk = a.K < kSliceK ? a.K : kSliceK;
     kk += (17 - kk % 16) % 16;  // row stride = 1 mod 16 float2
@@ -607,14 +687,15 @@ cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
     // one launch; dynamic shared memory sized for the outermost shell
     const int li = a.lmax_host_outer;
     const int nph = 6 * a.Lp;
-    const size_t smem = ((size_t)((li + 1) * (li + 2) / 2) * 4 + 15) / 16 * 16 + (size_t)4 * (li + 1) * sizeof(float2) +
+    const int nG = 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6);
+    const size_t smem = ((size_t)((li + 1) * (li + 2) / 2) * 4 + 15) / 16 * 16 + (size_t)2 * nG * sizeof(float2) +
                         (size_t)nph * sizeof(float2);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    hm_synth<<<a.n_rows, 256, smem, s>>>(a.rows, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step, a.vox_s, a.cx, a.cy, a.cz,
-                                         a.use_center, a.scale, a.origin, a.grid);
+    hm_synth<<<a.n_rows, kSynthThreads, smem, s>>>(a.rows, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step, a.vox_s, a.cx,
+                                                   a.cy, a.cz, a.use_center, a.scale, a.origin, a.grid);
     return cudaGetLastError();
 }
 

@@ -291,7 +291,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
             return fail(DPX_ERR_ARG, "harmonic fill: %d radial bins above %d", nbins, dpx::harmonic_max_bins());
         if (int rc = bin_voxels(ctx, d, t, s, delta, nbins, sv.units, sv.groups, sv.gu, &vox_dev, &n_vox)) return rc;
     }
-    const size_t cell_set = (size_t)(Lp + 1) * K * sizeof(double2);
+    const size_t cell_set = (size_t)(Lp + 1) * K * sizeof(float2);
     const size_t moments_per_unit = (size_t)6 * K * sizeof(float2);
     // ---- device arena ----
     std::vector<char> h;
@@ -349,8 +349,8 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     tb.Jn = reinterpret_cast<double*>(base + oJn);
     tb.T = reinterpret_cast<float*>(base + oT);
     DPX_CUDA(dpx::launch_harmonic_tables(st, tb));
-    double2* Ca = reinterpret_cast<double2*>(base + oCa);
-    double2* Cv = n_vox == 0 ? nullptr : reinterpret_cast<double2*>(base + oCv);
+    float2* Ca = reinterpret_cast<float2*>(base + oCa);
+    float2* Cv = n_vox == 0 ? nullptr : reinterpret_cast<float2*>(base + oCv);
     DPX_CUDA(cudaMemsetAsync(Ca, 0, cell_set * (n_vox == 0 ? 1 : 2), st));
     for (int k = 0; k < 2; ++k) {
         const Set& S = *sets[k];

@@ -66,8 +66,11 @@ struct AvgPlan {
     int chunk;               // samples per chunk
     int chunk_off;           // first chunk holds chunk - chunk_off samples
     int64_t n_chunks;
-    double* partial;         // [nbr][n_chunks][max_q]
+    double* partial;         // [nbr][n_chunks][max_q] partial sums, then 5 nbr max_q doubles of
+                             // scratch: the average's bracket tables, then the finalize's sums
     int need_dir;            // some model is placed or docked: the kernel needs the direction vector
+    int one_leaf;            // one model without docked copies (ModelDev::n_groups == 0): with a
+                             // shared direction set the average slides its plane window
 };
 
 // host helpers (dpx_api.cpp)
@@ -170,8 +173,8 @@ struct HarmonicSet {
 struct HarmonicSynth {
     const int2* rows;       // (i, t) of every theta row t <= 3i/2, i >= 1
     int n_rows;
-    const double2* Ca;      // [Lp+1][K] atoms
-    const double2* Cv;      // [Lp+1][K] voxels or nullptr
+    const float2* Ca;       // [Lp+1][K] atoms
+    const float2* Cv;       // [Lp+1][K] voxels or nullptr
     int K, Lp, lmax_host_outer;
     const int* lmax;
     const float2* ab;
@@ -204,7 +207,7 @@ struct VoxelBinArgs {
 cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a);
 cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a);
 // C [Lp+1][K] (FP64) = the expansion coefficients of one point set.
-cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, double2* C);
+cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C);
 cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a);
 
 // Debye sum of one leaf (dpx_debye.cu).  Atoms padded to a multiple of the

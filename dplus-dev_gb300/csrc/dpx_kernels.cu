@@ -15,6 +15,8 @@
 
 #include <cuda_runtime.h>
 #include <math_constants.h>
+
+#include <algorithm>
 #include <cstdint>
 
 namespace dpx {
@@ -204,29 +206,37 @@ __device__ __forceinline__ double bump8(double x) {
     return __longlong_as_double(__double_as_longlong(x) + 8);
 }
 
-// GetSplineBetweenPlanes (Grid.cpp:551-607) for a known plane index.
+// Plane j of the radial window of GetSplineBetweenPlanes (Grid.cpp:551-607):
+// j = -1 is shell 1 read at the mirrored direction (Grid.cpp:513-537), j = 0
+// the origin cell, 1 <= j < Lp shell j at (th, ph).
 template <typename T>
-__device__ void planes(const typename Vec4<T>::type* __restrict__ g, int Lp, int fInd, double th, double ph,
-                       Cx<T>& pl1, Cx<T>& pl2, Cx<T>& d1, Cx<T>& d2) {
-    Cx<T> origin, od;
-    load_cell<T>(g, 0, origin, od);
-    Cx<T> p1, p2, p3, p4;
-    if (fInd == 0) {
+__device__ Cx<T> window_plane(const typename Vec4<T>::type* __restrict__ g, int j, double th, double ph) {
+    if (j == -1) {
         double nth = kPi - th;
         double nph = ph + kPi;
         if (nph < 0) nph = k2Pi + (nph - (double)(int)(nph / k2Pi) * k2Pi);
         if (nph >= k2Pi) nph = nph - (double)(int)(nph / k2Pi) * k2Pi;
         if (nth < 0) nth = 0.;
         if (nth > kPi) nth = kPi;
-        p1 = interp_plane<T>(g, 1, nth, nph);
-    } else if (fInd == 1) {
-        p1 = origin;
-    } else {
-        p1 = interp_plane<T>(g, fInd - 1, th, ph);
+        return interp_plane<T>(g, 1, nth, nph);
     }
-    p2 = (fInd > 0) ? interp_plane<T>(g, fInd, th, ph) : origin;
-    p3 = interp_plane<T>(g, fInd + 1, th, ph);
-    p4 = (fInd + 2 < Lp) ? interp_plane<T>(g, fInd + 2, th, ph) : p3;
+    if (j == 0) {
+        Cx<T> origin, od;
+        load_cell<T>(g, 0, origin, od);
+        return origin;
+    }
+    return interp_plane<T>(g, j, th, ph);
+}
+
+// The four planes around plane index fInd: fInd - 1 .. fInd + 2, the last
+// repeated at the outermost shell.
+template <typename T>
+__device__ void planes(const typename Vec4<T>::type* __restrict__ g, int Lp, int fInd, double th, double ph,
+                       Cx<T>& pl1, Cx<T>& pl2, Cx<T>& d1, Cx<T>& d2) {
+    const Cx<T> p1 = window_plane<T>(g, fInd - 1, th, ph);
+    const Cx<T> p2 = window_plane<T>(g, fInd, th, ph);
+    const Cx<T> p3 = window_plane<T>(g, fInd + 1, th, ph);
+    const Cx<T> p4 = (fInd + 2 < Lp) ? window_plane<T>(g, fInd + 2, th, ph) : p3;
     four_point<T>(p1, p2, p3, p4, d1, d2);
     pl1 = p2;
     pl2 = p3;
@@ -420,26 +430,30 @@ __device__ Cx<float> interp_plane_f(const float4* __restrict__ g, int ri, float 
     return hermite<float>(nodes[1], nodes[2], ds1, ds2, tTh);
 }
 
-__device__ void planes_f(const float4* __restrict__ g, int Lp, int fInd, float th, float ph, Cx<float>& pl1,
-                         Cx<float>& pl2, Cx<float>& d1, Cx<float>& d2) {
-    Cx<float> origin, od;
-    load_cell<float>(g, 0, origin, od);
-    Cx<float> p1, p2, p3, p4;
-    if (fInd == 0) {  // the mirrored first shell (Grid.cpp:513-537)
+// window_plane in FP32 angles.
+__device__ Cx<float> window_plane_f(const float4* __restrict__ g, int j, float th, float ph) {
+    if (j == -1) {  // the mirrored first shell (Grid.cpp:513-537)
         float nth = kPiF - th;
         float nph = ph + kPiF;
         if (nph >= k2PiF) nph -= k2PiF;
         if (nth < 0.f) nth = 0.f;
         if (nth > kPiF) nth = kPiF;
-        p1 = interp_plane_f(g, 1, nth, nph);
-    } else if (fInd == 1) {
-        p1 = origin;
-    } else {
-        p1 = interp_plane_f(g, fInd - 1, th, ph);
+        return interp_plane_f(g, 1, nth, nph);
     }
-    p2 = (fInd > 0) ? interp_plane_f(g, fInd, th, ph) : origin;
-    p3 = interp_plane_f(g, fInd + 1, th, ph);
-    p4 = (fInd + 2 < Lp) ? interp_plane_f(g, fInd + 2, th, ph) : p3;
+    if (j == 0) {
+        Cx<float> origin, od;
+        load_cell<float>(g, 0, origin, od);
+        return origin;
+    }
+    return interp_plane_f(g, j, th, ph);
+}
+
+__device__ void planes_f(const float4* __restrict__ g, int Lp, int fInd, float th, float ph, Cx<float>& pl1,
+                         Cx<float>& pl2, Cx<float>& d1, Cx<float>& d2) {
+    const Cx<float> p1 = window_plane_f(g, fInd - 1, th, ph);
+    const Cx<float> p2 = window_plane_f(g, fInd, th, ph);
+    const Cx<float> p3 = window_plane_f(g, fInd + 1, th, ph);
+    const Cx<float> p4 = (fInd + 2 < Lp) ? window_plane_f(g, fInd + 2, th, ph) : p3;
     four_point<float>(p1, p2, p3, p4, d1, d2);
     pl1 = p2;
     pl2 = p3;
@@ -512,33 +526,104 @@ __device__ void sample_amps_f32(const ModelDev* __restrict__ models, int n_model
 }
 
 // --------------------------------------------------------------------------
-// Orientation average: one block = one chunk of samples of one bracket.
-// Each thread evaluates one direction: for every model and every docked
-// rotation group, the leaf's 4 planes at the rotated direction, then the
-// radial Hermite per q, the leaf phase and the group's translation phases.
-// |A_q|^2 is reduced over the block in FP64 and stored per (bracket, chunk, q).
+// Bracket tables, once per average: the plane index fInd of each bracket and
+// the radial fraction of each of its q values (the +8-ULP guard and floor of
+// Grid.cpp:149-150), in the precision of the interpolation.
 // --------------------------------------------------------------------------
-template <typename T, int MQ>
-__global__ void __launch_bounds__(128) average_kernel(int Lp, double step, const ModelDev* __restrict__ models,
-                                                      int n_models, AvgPlan plan) {
-    typedef typename Vec4<T>::type V4;
-    const int b = blockIdx.y;
-    const int64_t chunk = blockIdx.x;
-    const int layer = plan.br_layer[b];
+template <typename T>
+__global__ void bracket_tables_kernel(AvgPlan plan, double step, int* __restrict__ find, T* __restrict__ frac) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= plan.n_brackets) return;
     const int q0 = plan.br_q_off[b], q1 = plan.br_q_off[b + 1];
-    const int m = q1 - q0;
-    const int64_t s = chunk * plan.chunk - plan.chunk_off + threadIdx.x;
-    const bool valid = (threadIdx.x < plan.chunk) && s >= 0 && s < plan.n_samples;
+    const int f = (q1 > q0) ? (int)bump8(plan.br_q[q0] / step) : 0;
+    find[b] = f;
+    for (int k = q0; k < q1; ++k) frac[k] = (T)(bump8(plan.br_q[k] / step) - (double)f);
+}
 
-    __shared__ double red[4][MQ];
+// The four radial planes of the bracket a thread is on.  Consecutive brackets
+// share three of them, so a thread that walks the brackets of one direction
+// in order interpolates one new plane per bracket.
+template <typename T>
+struct PlaneWindow {
+    Cx<T> p[4];
+    int f;  // the bracket plane index the window holds (-2: none)
+};
 
-    double theta = 0, phi = 0;
-    if (valid) {
-        const double* d = plan.dirs + 2 * ((int64_t)layer * plan.dir_stride + s);
-        theta = d[0];
-        phi = d[1];
+template <typename T, typename PlaneFn>
+__device__ __forceinline__ void window_to(PlaneWindow<T>& w, int f, int Lp, PlaneFn plane) {
+    if (f == w.f) return;
+    if (f == w.f + 1 && w.f + 2 < Lp) {  // w.p[3] is plane f + 1, not the repeated last one
+        w.p[0] = w.p[1];
+        w.p[1] = w.p[2];
+        w.p[2] = w.p[3];
+        w.p[3] = (f + 2 < Lp) ? plane(f + 2) : w.p[2];
+    } else {
+        w.p[0] = plane(f - 1);
+        w.p[1] = plane(f);
+        w.p[2] = plane(f + 1);
+        w.p[3] = (f + 2 < Lp) ? plane(f + 2) : w.p[2];
     }
-    double dir[3] = {0.0, 0.0, 1.0};
+    w.f = f;
+}
+
+// --------------------------------------------------------------------------
+// Orientation average.  One block = one chunk of samples (one direction per
+// thread) over a segment of consecutive brackets.  For every bracket: every
+// model and docked rotation group, the leaf's 4 planes at the rotated
+// direction, the radial Hermite per q, the leaf phase and the group's
+// translation phases; |A_q|^2 summed per warp (in the interpolation's
+// precision), the four warps in FP64, stored per (bracket, chunk, q).
+// --------------------------------------------------------------------------
+constexpr int kAvgSlots = 32;  // (bracket, q chunk) sums a block holds before storing them
+
+template <int MQ>
+struct AvgSums {
+    double red[kAvgSlots][4][MQ];
+    int b[kAvgSlots], q[kAvgSlots], m[kAvgSlots];
+};
+
+// Stores the block's filled slots.  Called block-uniformly.
+template <int MQ>
+__device__ __forceinline__ void avg_flush(AvgSums<MQ>& S, int& nslot, const AvgPlan& plan, int64_t chunk) {
+    if (nslot == 0) return;
+    __syncthreads();
+    for (int t = threadIdx.x; t < nslot * MQ; t += blockDim.x) {
+        const int sl = t / MQ, k = t - sl * MQ;
+        if (k < S.m[sl]) {
+            const double v = ((S.red[sl][0][k] + S.red[sl][1][k]) + S.red[sl][2][k]) + S.red[sl][3][k];
+            plan.partial[((int64_t)S.b[sl] * plan.n_chunks + chunk) * plan.max_q + S.q[sl] + k] = v;
+        }
+    }
+    __syncthreads();
+    nslot = 0;
+}
+
+// Per-warp sums of |A|^2 into the block's next slot, stored when the slots
+// are full.  Called block-uniformly.
+template <typename T, int MQ>
+__device__ __forceinline__ void avg_slot(AvgSums<MQ>& S, int& nslot, const Cx<T>* A, bool valid, int b, int qc, int mq,
+                                         const AvgPlan& plan, int64_t chunk) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < MQ; ++k) {
+        T v = valid ? A[k].r * A[k].r + A[k].i * A[k].i : T(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) S.red[nslot][warp][k] = (double)v;
+    }
+    if (threadIdx.x == 0) {
+        S.b[nslot] = b;
+        S.q[nslot] = qc;
+        S.m[nslot] = mq;
+    }
+    if (++nslot == kAvgSlots) avg_flush<MQ>(S, nslot, plan, chunk);
+}
+
+__device__ __forceinline__ void sample_direction(const AvgPlan& plan, int layer, int64_t s, double& theta,
+                                                 double& phi, double dir[3]) {
+    const double* d = plan.dirs + 2 * ((int64_t)layer * plan.dir_stride + s);
+    theta = d[0];
+    phi = d[1];
     if (plan.need_dir) {
         double st, ct, sp, cp;
         sincos(theta, &st, &ct);
@@ -547,40 +632,151 @@ __global__ void __launch_bounds__(128) average_kernel(int Lp, double step, const
         dir[1] = st * sp;
         dir[2] = ct;
     }
-    const int fInd = (m > 0) ? (int)bump8(plan.br_q[q0] / step) : 0;
+}
 
-    for (int qc = 0; qc < m; qc += MQ) {
-        const int mq = min(MQ, m - qc);
-        Cx<T> A[MQ];
-        T frac[MQ];
-        double qv[MQ];
-#pragma unroll
-        for (int k = 0; k < MQ; ++k) {
-            A[k] = {T(0), T(0)};
-            qv[k] = (k < mq) ? plan.br_q[q0 + qc + k] : 0.0;
-            frac[k] = (T)(bump8(qv[k] / step) - (double)fInd);
+template <typename T, int MQ>
+__global__ void __launch_bounds__(128) average_kernel(int Lp, const ModelDev* __restrict__ models, int n_models,
+                                                      AvgPlan plan, int seg_len, const int* __restrict__ find,
+                                                      const T* __restrict__ frac_tab) {
+    const int64_t chunk = blockIdx.x;
+    const int b0 = blockIdx.y * seg_len;
+    const int b1 = min(plan.n_brackets, b0 + seg_len);
+    const int64_t s = chunk * plan.chunk - plan.chunk_off + threadIdx.x;
+    const bool valid = (threadIdx.x < plan.chunk) && s >= 0 && s < plan.n_samples;
+    __shared__ AvgSums<MQ> S;
+    int nslot = 0;
+    double theta = 0, phi = 0;
+    double dir[3] = {0.0, 0.0, 1.0};
+    int cur_layer = -1;
+    for (int b = b0; b < b1; ++b) {
+        const int layer = plan.br_layer[b];
+        const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
+        const int fInd = find[b];
+        if (valid && layer != cur_layer && (cur_layer < 0 || plan.dir_stride != 0)) {
+            sample_direction(plan, layer, s, theta, phi, dir);
+            cur_layer = layer;
         }
+        for (int qc = 0; qc < m; qc += MQ) {
+            const int mq = min(MQ, m - qc);
+            Cx<T> A[MQ];
+            T frac[MQ];
+            double qv[MQ];
+#pragma unroll
+            for (int k = 0; k < MQ; ++k) {
+                A[k] = {T(0), T(0)};
+                qv[k] = (k < mq) ? plan.br_q[q0 + qc + k] : 0.0;
+                frac[k] = (k < mq) ? frac_tab[q0 + qc + k] : T(0);
+            }
+            if (valid) {
+                if constexpr (sizeof(T) == 4)
+                    sample_amps_f32<MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+                else
+                    sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+            }
+            avg_slot<T, MQ>(S, nslot, A, valid, b, qc, mq, plan, chunk);
+        }
+    }
+    avg_flush<MQ>(S, nslot, plan, chunk);
+}
+
+// One undocked leaf with one direction set for all layers: a thread walks
+// the brackets of its direction in order and keeps the leaf's planes in a
+// sliding window, one plane interpolation per bracket.  The planes, the
+// radial Hermite and the leaf phase are those of sample_amps /
+// sample_amps_f32, so the amplitudes are the same.
+template <typename T, int MQ>
+__global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelDev* __restrict__ models,
+                                                            AvgPlan plan, int seg_len, const int* __restrict__ find,
+                                                            const T* __restrict__ frac_tab) {
+    typedef typename Vec4<T>::type V4;
+    const int64_t chunk = blockIdx.x;
+    const int b0 = blockIdx.y * seg_len;
+    const int b1 = min(plan.n_brackets, b0 + seg_len);
+    const int64_t s = chunk * plan.chunk - plan.chunk_off + threadIdx.x;
+    const bool valid = (threadIdx.x < plan.chunk) && s >= 0 && s < plan.n_samples;
+    __shared__ AvgSums<MQ> S;
+    int nslot = 0;
+
+    const ModelDev& M = models[0];
+    const V4* g = reinterpret_cast<const V4*>(M.grid);
+    // the leaf's direction (Amplitude.cpp:3553-3579)
+    double th = 0, ph = 0, dotR = 0;
+    float thf = 0.f, phf = 0.f;
+    if (valid) {
+        double theta, phi, dir[3] = {0.0, 0.0, 1.0};
+        sample_direction(plan, 0, s, theta, phi, dir);
+        th = theta;
+        ph = phi;
+        thf = (float)theta;
+        phf = (float)phi;
+        if (!M.plain) {
+            if constexpr (sizeof(T) == 4) {
+                const float n0 = (float)dir[0], n1 = (float)dir[1], n2 = (float)dir[2];
+                const float* C = M.Rf;
+                const float t0 = n0 * C[0] + n1 * C[3] + n2 * C[6];
+                const float t1 = n0 * C[1] + n1 * C[4] + n2 * C[7];
+                const float t2 = n0 * C[2] + n1 * C[5] + n2 * C[8];
+                dotR = dir[0] * M.w[0] + dir[1] * M.w[1] + dir[2] * M.w[2];
+                thf = atan2f(sqrtf(t0 * t0 + t1 * t1), t2);
+                phf = atan2f(t1, t0);
+                if (phf < 0.f) phf += k2PiF;
+            } else {
+                const double t0 = dir[0] * M.R[0] + dir[1] * M.R[3] + dir[2] * M.R[6];
+                const double t1 = dir[0] * M.R[1] + dir[1] * M.R[4] + dir[2] * M.R[7];
+                const double t2 = dir[0] * M.R[2] + dir[1] * M.R[5] + dir[2] * M.R[8];
+                dotR = t0 * M.tr[0] + t1 * M.tr[1] + t2 * M.tr[2];
+                dir_angles(t0, t1, t2, th, ph);
+            }
+        }
+    }
+    PlaneWindow<T> win;
+    win.f = -2;
+    for (int b = b0; b < b1; ++b) {
+        const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
+        Cx<T> pl1{}, pl2{}, d1{}, d2{};
         if (valid) {
             if constexpr (sizeof(T) == 4)
-                sample_amps_f32<MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+                window_to(win, find[b], Lp, [&](int j) { return window_plane_f(g, j, thf, phf); });
             else
-                sample_amps<T, MQ>(models, n_models, Lp, fInd, theta, phi, dir, mq, qv, frac, A);
+                window_to(win, find[b], Lp, [&](int j) { return window_plane<T>(g, j, th, ph); });
+            four_point<T>(win.p[0], win.p[1], win.p[2], win.p[3], d1, d2);
+            pl1 = win.p[1];
+            pl2 = win.p[2];
         }
-        // |A|^2, block reduction in FP64
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int qc = 0; qc < m; qc += MQ) {
+            const int mq = min(MQ, m - qc);
+            Cx<T> A[MQ];
 #pragma unroll
-        for (int k = 0; k < MQ; ++k) {
-            double v = valid ? (double)A[k].r * (double)A[k].r + (double)A[k].i * (double)A[k].i : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) red[warp][k] = v;
+            for (int k = 0; k < MQ; ++k) {
+                A[k] = {T(0), T(0)};
+                if (valid && k < mq) {
+                    Cx<T> v = hermite<T>(pl1, pl2, d1, d2, frac_tab[q0 + qc + k]);
+                    if (dotR != 0.0) v = cmul(v, expi<T>(dotR * plan.br_q[q0 + qc + k]));
+                    A[k] = cadd(A[k], v);
+                }
+            }
+            avg_slot<T, MQ>(S, nslot, A, valid, b, qc, mq, plan, chunk);
         }
+    }
+    avg_flush<MQ>(S, nslot, plan, chunk);
+}
+
+// eps = 0: the sum of each bracket's chunk partials, in a fixed order.
+__global__ void __launch_bounds__(128) finalize_sum_kernel(AvgPlan plan, double* __restrict__ res) {
+    const int b = blockIdx.x;
+    const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
+    const double* part = plan.partial + (int64_t)b * plan.n_chunks * plan.max_q;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ double red[4];
+    for (int k = 0; k < m; ++k) {
+        double v = 0.0;
+        for (int64_t c = threadIdx.x; c < plan.n_chunks; c += blockDim.x) v += part[c * plan.max_q + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp] = v;
         __syncthreads();
-        if (threadIdx.x < mq) {
-            const int k = threadIdx.x;
-            const double v = ((red[0][k] + red[1][k]) + red[2][k]) + red[3][k];
-            plan.partial[((int64_t)b * plan.n_chunks + chunk) * plan.max_q + qc + k] = v;
-        }
+        if (threadIdx.x == 0)
+            res[plan.br_qidx[q0 + k]] = (((red[0] + red[1]) + red[2]) + red[3]) / (double)plan.n_samples;
         __syncthreads();
     }
 }
@@ -1098,10 +1294,36 @@ cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid)
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
                            const AvgPlan& plan) {
     if (plan.n_brackets == 0 || plan.n_chunks == 0) return cudaSuccess;
-    if (plan.n_chunks > 0x7fffffff || plan.n_brackets > 65535) return cudaErrorInvalidValue;
-    dim3 grid((unsigned)plan.n_chunks, (unsigned)plan.n_brackets);
-    if (fp64) average_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, g.step, d_models, n_models, plan);
-    else average_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, g.step, d_models, n_models, plan);
+    if (plan.n_chunks > 0x7fffffff) return cudaErrorInvalidValue;
+    // segments of consecutive brackets: enough blocks to fill the GPU a few
+    // times over, at most 64 brackets a segment
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t nbr = plan.n_brackets;
+    const int64_t target = (int64_t)sms * 16;
+    int64_t n_seg = std::max<int64_t>((nbr + 63) / 64, (target + plan.n_chunks - 1) / plan.n_chunks);
+    n_seg = std::min<int64_t>(n_seg, nbr);
+    const int seg_len = (int)((nbr + n_seg - 1) / n_seg);
+    n_seg = (nbr + seg_len - 1) / seg_len;
+    if (n_seg > 65535) return cudaErrorInvalidValue;
+    // the bracket tables live in the finalize scratch behind the partial sums
+    // (5 n_brackets max_q doubles, unused until the finalize): plane indices,
+    // then the fractions of every q
+    double* tab = plan.partial + (size_t)nbr * plan.n_chunks * plan.max_q;
+    int* find = reinterpret_cast<int*>(tab);
+    double* frac = tab + (nbr + 1) / 2;
+    dim3 grid((unsigned)plan.n_chunks, (unsigned)n_seg);
+    const bool slide = plan.one_leaf && n_models == 1 && plan.dir_stride == 0;
+    if (fp64) {
+        bracket_tables_kernel<double><<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, find, frac);
+        if (slide) average_slide_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, seg_len, find, frac);
+        else average_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, n_models, plan, seg_len, find, frac);
+    } else {
+        float* fracf = reinterpret_cast<float*>(frac);
+        bracket_tables_kernel<float><<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, find, fracf);
+        if (slide) average_slide_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, seg_len, find, fracf);
+        else average_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, n_models, plan, seg_len, find, fracf);
+    }
     return cudaGetLastError();
 }
 
@@ -1185,7 +1407,9 @@ cudaError_t launch_origin_intensity(cudaStream_t s, bool fp64, const void* grid,
 }
 
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res) {
-    finalize_kernel<<<blocks_for(plan.n_brackets, 64), 64, 0, s>>>(plan, eps, d_res);
+    if (plan.n_brackets == 0) return cudaSuccess;
+    if (eps > 0.0) finalize_kernel<<<blocks_for(plan.n_brackets, 64), 64, 0, s>>>(plan, eps, d_res);
+    else finalize_sum_kernel<<<plan.n_brackets, 128, 0, s>>>(plan, d_res);
     return cudaGetLastError();
 }
 

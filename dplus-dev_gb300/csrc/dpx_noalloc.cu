@@ -146,6 +146,7 @@ extern "C" int dpx_mc_average_noalloc(const void* grid_cells, int grid_size, dou
     md.sym_scale = 1.0;
     md.plain = 1;
     plan.need_dir = 0;
+    plan.one_leaf = 1;
     std::vector<char> stage(oP);
     std::memcpy(stage.data() + oQ, br_q.data(), br_q.size() * sizeof(double));
     std::memcpy(stage.data() + oL, br_layer.data(), br_layer.size() * sizeof(int));

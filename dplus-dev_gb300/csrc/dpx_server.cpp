@@ -439,6 +439,7 @@ int launch_request(dpx_server_s* S, Request* r) {
     P.need_dir = 0;
     for (const dpx::ModelDev& M : T.md)
         if (!M.plain || M.n_groups > 0) P.need_dir = 1;
+    P.one_leaf = (nm == 1 && T.md[0].n_groups == 0) ? 1 : 0;
     std::vector<char> h;
     Upload U{h};
     const size_t oG = U.put(T.gstage.data(), T.gstage.size());
