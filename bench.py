@@ -123,17 +123,22 @@ def build_inputs():
     return amp, Q, dirs
 
 
-def launches_per_solve(ctx, n_boxes):
-    """Kernel launches of one solve: the fill, the splines (1) and the average
-    (bracket tables, average, finalize: 3).  Harmonic fill: radial tables (2),
-    moments + group sums + contraction per point set (3 each), synthesis (1),
-    and with solvent voxels their expansion and binning (4); direct fill: one
-    launch (the boxes are sorted on the host)."""
+def fill_launches(ctx, n_boxes):
+    """Kernel launches of one leaf's fill with its spline derivatives.
+    Harmonic fill: radial tables (2), moments + group sums + contraction per
+    point set (3 each), synthesis (1, which also writes the spline
+    derivatives), and with solvent voxels their expansion and binning (4);
+    direct fill: one launch (the boxes are sorted on the host), then the
+    spline pass (1)."""
+    from dpx import _lib
     if ctx.fill_method() == _lib.DPX_FILL_HARMONIC:
-        fill = 2 + 3 + 1 + ((4 + 3) if n_boxes else 0)
-    else:
-        fill = 1
-    return fill + 1 + 3
+        return 2 + 3 + 1 + ((4 + 3) if n_boxes else 0)
+    return 1 + 1
+
+
+def launches_per_solve(ctx, n_boxes):
+    """One solve: the fill and the average (bracket tables, average, finalize)."""
+    return fill_launches(ctx, n_boxes) + 3
 
 
 def shape_label(shape) -> str:
@@ -602,7 +607,8 @@ def run_assembly(args):
         "e2e": {"value": 2 * world / e2e_s, "unit": "solves/s",
                 "h2d_bytes_per_step": int(2 * dirs.nbytes + 16 * len(xyz) + 48 * (60 + 1300)),
                 "d2h_bytes_per_step": int(2 * Q.nbytes)},
-        "gpu_launches": 2 * 4 * args.steps,
+        # the subunit fill, then two averages of 3 launches (bracket tables, average, finalize)
+        "gpu_launches": (fill_launches(ctx, 0) + 2 * 3) * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_extras:
@@ -714,7 +720,8 @@ def run_serve(args):
                 "h2d_bytes_per_step": int(sum(16 * len(r.leaf.xyz) + (0 if r.copies is None else 48 * len(r.copies[1]))
                                               for r in stream)),
                 "d2h_bytes_per_step": int(sum(r.Q.nbytes for r in stream))},
-        "gpu_launches": int(st["fill_launches"] + 2 * st["grid_fills"] + 3 * st["completed"]),
+        # per grid: its splines (+1); per request: bracket tables, average, finalize, I(0)
+        "gpu_launches": int(st["fill_launches"] + 2 * st["grid_fills"] + 4 * st["completed"]),
         "server": st, "generation_s": gen_s, "clocks": clk.summary(),
     }
     if args.fp64_sample > 0 and rank == 0:

@@ -200,6 +200,8 @@ void ctx_release(dpx_ctx ctx) {
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
                       &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels})
         b->release();
+    ctx->pin_boxes.release();
+    ctx->pin_plan.release();
     for (cudaEvent_t e : ctx->tev)
         if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -364,7 +366,11 @@ int dpx_grid_destroy(dpx_grid g) {
     return DPX_OK;
 }
 
-void* dpx_grid_device_ptr(dpx_grid g) { return g ? g->cells : nullptr; }
+void* dpx_grid_device_ptr(dpx_grid g) {
+    if (!g) return nullptr;
+    g->splines_current = false;  // the caller may write through it
+    return g->cells;
+}
 
 int dpx_grid_info(dpx_grid g, int* grid_size, double* qmax, int* precision, int64_t* cells) {
     if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
@@ -409,6 +415,7 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     }
     if (int rc = set_device(ctx)) return rc;
     cudaStream_t s = ctx->stream;
+    for (int j = 0; j < n; ++j) grids[j]->splines_current = false;
 
     // host staging of every leaf, then the FP32 job table and the tile counter
     std::vector<char>& h = ctx->host_stage;
@@ -416,11 +423,12 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     std::vector<LeafTables> lt(n);
     std::vector<char> harm(n, 0);  // FP32 leaves the harmonic method takes
     std::vector<std::vector<float>> host_atoms(n);
+    std::vector<double> harm_R(n, 0.0);
     if (ctx->fill_method == DPX_FILL_HARMONIC)
         for (int j = 0; j < n; ++j) {
             if (grids[j]->precision != DPX_FP32) continue;
             int status = DPX_OK;
-            harm[j] = harmonic_accepts(ctx, pdbs[j], grids[j]->g, host_atoms[j], &status);
+            harm[j] = harmonic_accepts(ctx, pdbs[j], grids[j]->g, host_atoms[j], &harm_R[j], &status);
             if (status) return status;
         }
     for (int j = 0; j < n; ++j) {
@@ -437,7 +445,8 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
     for (int j = 0; j < n; ++j)
         if (harm[j])
-            if (int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, host_atoms[j]))
+            if (int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, host_atoms[j],
+                                       harm_R[j]))
                 return rc;
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
@@ -465,6 +474,7 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     }
     // the staging buffer is reused by the next call: wait for the copy and the kernels
     DPX_CUDA(cudaStreamSynchronize(s));
+    for (int j = 0; j < n; ++j) grids[j]->splines_current = harm[j] != 0;  // the synthesis wrote them
     return DPX_OK;
 }
 
@@ -548,10 +558,12 @@ int dpx_grid_fill_pdb(dpx_grid g, int64_t n_atoms, const float* atoms, int atoms
 
 int dpx_grid_compute_splines(dpx_grid g) {
     if (!g) return fail(DPX_ERR_ARG, "grid is NULL");
+    if (g->splines_current) return DPX_OK;  // written with the values, the same bits
     if (int rc = set_device(g->ctx)) return rc;
     cudaError_t e = g->precision == DPX_FP64 ? dpx::launch_splines_f64(g->ctx->stream, g->g, (double4_32a*)g->cells)
                                              : dpx::launch_splines_f32(g->ctx->stream, g->g, (float4*)g->cells);
     if (e != cudaSuccess) return cuda_fail(e, "spline launch");
+    g->splines_current = true;
     return DPX_OK;
 }
 
@@ -580,6 +592,7 @@ int dpx_grid_read(dpx_grid g, double* values, double* coeffs) {
 
 int dpx_grid_write(dpx_grid g, const double* values, const double* coeffs) {
     if (!g || !values) return fail(DPX_ERR_ARG, "NULL argument");
+    g->splines_current = false;
     dpx_ctx ctx = g->ctx;
     if (int rc = set_device(ctx)) return rc;
     const size_t n = (size_t)g->g.P * 2 * sizeof(double);
@@ -1018,6 +1031,7 @@ int dpx_grid_assemble(dpx_grid dst, int n_models, const dpx_grid* grids, const d
             return fail(DPX_ERR_ARG, "source grids must share the destination's grid_size, qmax and precision");
         if (grids[m] == dst) return fail(DPX_ERR_ARG, "the destination cannot also be a source");
     }
+    dst->splines_current = false;
     dpx_ctx ctx = dst->ctx;
     if (int rc = set_device(ctx)) return rc;
     cudaStream_t s = ctx->stream;

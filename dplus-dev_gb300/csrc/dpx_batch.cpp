@@ -284,7 +284,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
                 e = dpx::launch_origin_intensity(s, !fp32, grid, r);
                 launches++;
             }
-            launches += 3;
+            launches += 4;  // splines, bracket tables, average, finalize
         }
         const size_t r0 = b->res_off[j0], r1 = (j1 < n) ? b->res_off[j1] : b->res_total;
         if (e == cudaSuccess)

@@ -34,6 +34,7 @@
 //                n voxels is exactly the sum of its voxels), the centring
 //                phase e^{i q.c} in FP64, and the Friedel mirror row.
 #include "dpx_internal.h"
+#include "dpx_spline.cuh"
 
 #include <cstdint>
 
@@ -289,25 +290,60 @@ __global__ void __launch_bounds__(kBinThreads) vx_expand(const float4* __restric
     for (int b = threadIdx.x; b < nbins; b += blockDim.x) hist[(int64_t)b * nblk + blockIdx.x] = sh[b];
 }
 
-// thread per bin: its total over the blocks
-__global__ void vx_totals(const int* __restrict__ hist, int nbins, int nblk, int64_t* __restrict__ total) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbins) return;
-    int64_t t = 0;
-    for (int k = 0; k < nblk; ++k) t += hist[(int64_t)b * nblk + k];
-    total[b] = t;
+// Block-wide exclusive scan of one int64 per thread; returns the thread's
+// prefix, *total the block's sum.
+__device__ __forceinline__ int64_t block_scan_excl(int64_t v, int64_t* total) {
+    __shared__ int64_t ws[kBinThreads / 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    int64_t before = 0, all = 0;
+    for (int k = 0; k < kBinThreads / 32; ++k) {
+        if (k < w) before += ws[k];
+        all += ws[k];
+    }
+    __syncthreads();
+    *total = all;
+    return before + x - v;
 }
 
-// thread per bin: off[b][blk] = start of bin b + the counts of its earlier blocks
-__global__ void vx_offsets(const int* __restrict__ hist, const int64_t* __restrict__ total, int nbins, int nblk,
-                           int64_t* __restrict__ off) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbins) return;
-    int64_t run = 0;
-    for (int c = 0; c < b; ++c) run += total[c];
-    for (int k = 0; k < nblk; ++k) {
+// block per bin: its total over the expand blocks
+__global__ void __launch_bounds__(kBinThreads) vx_totals(const int* __restrict__ hist, int nbins, int nblk,
+                                                         int64_t* __restrict__ total) {
+    const int b = blockIdx.x;
+    int64_t v = 0;
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) v += hist[(int64_t)b * nblk + k];
+    int64_t all;
+    block_scan_excl(v, &all);
+    if (threadIdx.x == 0) total[b] = all;
+}
+
+// block per bin: off[b][blk] = start of bin b + the counts of its earlier
+// blocks (a contiguous run of blocks per thread, then a block scan)
+__global__ void __launch_bounds__(kBinThreads) vx_offsets(const int* __restrict__ hist,
+                                                          const int64_t* __restrict__ total, int nbins, int nblk,
+                                                          int64_t* __restrict__ off) {
+    const int b = blockIdx.x;
+    int64_t before = 0;
+    for (int c = threadIdx.x; c < b; c += blockDim.x) before += total[c];
+    int64_t start;
+    block_scan_excl(before, &start);
+    const int per = (nblk + kBinThreads - 1) / kBinThreads;
+    const int k0 = min(nblk, (int)threadIdx.x * per), k1 = min(nblk, k0 + per);
+    const int* hb = hist + (int64_t)b * nblk;
+    int64_t mine = 0;
+    for (int k = k0; k < k1; ++k) mine += hb[k];
+    int64_t dummy;
+    int64_t run = start + block_scan_excl(mine, &dummy);
+    for (int k = k0; k < k1; ++k) {
         off[(int64_t)b * nblk + k] = run;
-        run += hist[(int64_t)b * nblk + k];
+        run += hb[k];
     }
 }
 
@@ -422,10 +458,12 @@ __device__ __forceinline__ float sinc_h(float h) {
 //   F(s i + j) = sum_{r < 6} e^{2 pi i r s / 6} D_r(j),
 //   D_r(j) = sum_{m = r mod 6} G_m w^{mj},
 // so a thread per column j sums the G_m once into six residue classes and
-// finishes its six cells with a 6-point DFT.
+// finishes its six cells with a 6-point DFT.  The row's phi-spline
+// derivatives (row_spline, as the spline pass computes them) are written with
+// the values; the Friedel mirror row gets the conjugates of both.
 // Dynamic shared memory: P column values [K_i], G (atoms, voxels) over
 // m in [m0, m0 + nG) with zero padding (m0 = -6 ceil(l_i/6)), the 6i roots
-// of unity.
+// of unity, the row's 6i values.
 // ---------------------------------------------------------------------------
 constexpr int kSynthThreads = 128;
 
@@ -466,6 +504,7 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(const int2* __restrict
     float2* sG = reinterpret_cast<float2*>(smem + ((size_t)Ki * 4 + 15) / 16 * 16);
     float2* sGv = sG + nG;
     float2* sW = sGv + nG;
+    float2* sF = sW + nph;
     float st, ct;
     sincospif((float)t / (float)h, &st, &ct);
     // Legendre column m per thread
@@ -607,13 +646,20 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(const int2* __restrict
                 sincospif(2.f * rt, &s1n, &c1n);
                 F = make_float2(F.x * c1n - F.y * s1n, F.x * s1n + F.y * c1n);
             }
-            grid[base + (int64_t)t * nph + p] = make_float4(F.x, F.y, 0.f, 0.f);
-            // Friedel: the antipode (3i - t, p + 3i) holds the conjugate (the
-            // equator row is its own mirror and is written once per cell)
-            if (2 * t != h) {
-                const int pm = p < h ? p + h : p - h;
-                grid[base + (int64_t)(h - t) * nph + pm] = make_float4(F.x, -F.y, 0.f, 0.f);
-            }
+            sF[p] = F;
+        }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < nph; p += blockDim.x) {
+        const float2 F = sF[p];
+        float dr, di;
+        row_spline<float, 14>(nph, p, [&](int k) { return sF[k]; }, dr, di);
+        grid[base + (int64_t)t * nph + p] = make_float4(F.x, F.y, dr, di);
+        // Friedel: the antipode (3i - t, p + 3i) holds the conjugate (the
+        // equator row is its own mirror and is written once per cell)
+        if (2 * t != h) {
+            const int pm = p < h ? p + h : p - h;
+            grid[base + (int64_t)(h - t) * nph + pm] = make_float4(F.x, -F.y, dr, -di);
         }
     }
     if (i == 1 && t == 0 && threadIdx.x == 0) grid[0] = make_float4((float)origin, 0.f, 0.f, 0.f);
@@ -677,8 +723,8 @@ cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
     if (a.nbins > kMaxBins) return cudaErrorInvalidValue;
     vx_expand<<<nblk, kBinThreads, 0, s>>>(a.boxes, a.vstart, a.nb, a.nv, a.vs, a.delta, a.nbins, a.tmp, a.vbin,
                                            a.hist, nblk);
-    vx_totals<<<(a.nbins + 127) / 128, 128, 0, s>>>(a.hist, a.nbins, nblk, a.total);
-    vx_offsets<<<(a.nbins + 127) / 128, 128, 0, s>>>(a.hist, a.total, a.nbins, nblk, a.off);
+    vx_totals<<<a.nbins, kBinThreads, 0, s>>>(a.hist, a.nbins, nblk, a.total);
+    vx_offsets<<<a.nbins, kBinThreads, 0, s>>>(a.hist, a.total, a.nbins, nblk, a.off);
     vx_scatter<<<nblk, kBinThreads, 0, s>>>(a.tmp, a.vbin, a.nv, a.nbins, nblk, a.off, a.out);
     return cudaGetLastError();
 }
@@ -689,7 +735,7 @@ cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
     const int nph = 6 * a.Lp;
     const int nG = 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6);
     const size_t smem = ((size_t)((li + 1) * (li + 2) / 2) * 4 + 15) / 16 * 16 + (size_t)2 * nG * sizeof(float2) +
-                        (size_t)nph * sizeof(float2);
+                        (size_t)2 * nph * sizeof(float2);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

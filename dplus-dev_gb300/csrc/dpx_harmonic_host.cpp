@@ -69,8 +69,14 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
                std::vector<int4>& units, std::vector<int2>& groups, std::vector<int>& gu, const float4** out,
                int64_t* n_out) {
     const int64_t nb = t.n_boxes;
-    std::vector<float4> hb((size_t)2 * nb);
-    std::vector<int64_t> vstart(nb);
+    // staging: the boxes about the centre [2 nb] float4, the first voxel of each box [nb]
+    const size_t oB = 0;
+    const size_t oS = al16((size_t)2 * nb * sizeof(float4));
+    const size_t staged = al16(oS + (size_t)nb * sizeof(int64_t));
+    char* hp = nullptr;
+    DPX_CUDA(ctx->pin_boxes.get(staged, &hp));
+    float4* hb = reinterpret_cast<float4*>(hp + oB);
+    int64_t* vstart = reinterpret_cast<int64_t*>(hp + oS);
     int64_t nv = 0;
     for (int64_t b = 0; b < nb; ++b) {
         const float* r = d.boxes + 8 * b;
@@ -82,10 +88,6 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
     }
     if (nv > INT32_MAX) return fail(DPX_ERR_ARG, "harmonic fill: %lld voxels", (long long)nv);
     const int nblk = (int)((nv + 255) / 256);
-    std::vector<char> h;
-    const size_t oB = put(h, hb.data(), hb.size() * sizeof(float4));
-    const size_t oS = put(h, vstart.data(), vstart.size() * sizeof(int64_t));
-    const size_t staged = al16(h.size());
     const size_t oTmp = staged;
     const size_t oBin = al16(oTmp + (size_t)nv * sizeof(float4));
     const size_t oHist = al16(oBin + (size_t)nv * sizeof(int));
@@ -99,7 +101,8 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
     }
     char* base = static_cast<char*>(ctx->voxels.p);
     cudaStream_t st = ctx->stream;
-    DPX_CUDA(cudaMemcpyAsync(base, h.data(), staged, cudaMemcpyHostToDevice, st));
+    DPX_CUDA(cudaMemcpyAsync(base, hp, staged, cudaMemcpyHostToDevice, st));
+    DPX_CUDA(ctx->pin_boxes.copied(st));
     dpx::VoxelBinArgs a{};
     a.boxes = reinterpret_cast<const float4*>(base + oB);
     a.vstart = reinterpret_cast<const int64_t*>(base + oS);
@@ -138,7 +141,7 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
 }  // namespace
 
 bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, std::vector<float>& host_atoms,
-                      int* status) {
+                      double* R_out, int* status) {
     *status = DPX_OK;
     if (d.n_boxes > 0 && d.boxes && !(d.voxel_step > 0.0)) return false;
     const float* src = d.atoms;
@@ -180,7 +183,9 @@ bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, st
         }
         r2 = std::max(r2, q);
     }
-    const double R = std::sqrt(r2) * (1.0 + 1e-6);  // the fill measures R on the rounded points
+    // the fill's points are rounded to FP32 about the centre: a relative margin
+    const double R = std::sqrt(r2) * (1.0 + 1e-6);
+    *R_out = R;
     if (order_of(G.Lp * G.step * R) > dpx::harmonic_max_l()) return false;
     const double delta = kBinWidthTimesQmax / (G.Lp * G.step);
     if (nb > 0 && (int)(R / delta) + 1 > dpx::harmonic_max_bins()) return false;
@@ -188,8 +193,16 @@ bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, st
 }
 
 int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid, const std::vector<float>& host_atoms) {
+                  void* grid, const std::vector<float>& host_atoms, double R) {
     const int Lp = G.Lp;
+    cudaStream_t st = ctx->stream;
+    cudaEvent_t* ev = nullptr;  // [0, 1] atoms' moments, [2, 3] voxels' moments, [4, 5] synthesis, [6, 7] fill
+    if (ctx->timing) {
+        for (cudaEvent_t& e : ctx->tev)
+            if (!e) DPX_CUDA(cudaEventCreate(&e));
+        ev = ctx->tev;
+        DPX_CUDA(cudaEventRecord(ev[6], st));
+    }
     // ---- point sets about the leaf's centre t.cen (device atoms arrive shifted) ----
     const float* src = d.atoms_on_device ? host_atoms.data() : d.atoms;
     const double sh[3] = {d.atoms_on_device ? 0.0 : t.cen[0], d.atoms_on_device ? 0.0 : t.cen[1],
@@ -202,19 +215,8 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
                 atoms[j] = make_float4((float)((double)src[4 * j] - sh[0]), (float)((double)src[4 * j + 1] - sh[1]),
                                        (float)((double)src[4 * j + 2] - sh[2]), (float)u);
     }
-    // ---- R: the atoms and the corners of the solvent boxes ----
+    // R (from harmonic_accepts): the atoms and the corners of the solvent boxes
     const double s = d.voxel_step;
-    double R = 0.0;
-    for (const float4& p : atoms) R = std::max(R, std::sqrt((double)p.x * p.x + (double)p.y * p.y + (double)p.z * p.z));
-    for (int64_t b = 0; b < t.n_boxes; ++b) {
-        const float* r = d.boxes + 8 * b;
-        double q = 0.0;
-        for (int k = 0; k < 3; ++k) {
-            const double e = std::fabs((double)r[k] - t.cen[k]) + 0.5 * r[4 + k];
-            q += e * e;
-        }
-        R = std::max(R, std::sqrt(q));
-    }
     // ---- orders ----
     std::vector<int> lmax(Lp + 1, 0);
     for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * R);
@@ -324,18 +326,16 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         return fail(DPX_ERR_OOM, "harmonic fill needs %zu bytes (%s)", total, cudaGetErrorString(e));
     }
     char* base = static_cast<char*>(ctx->harmonic.p);
-    cudaStream_t st = ctx->stream;
-    cudaEvent_t* ev = nullptr;  // [0, 1] atoms' moments, [2, 3] voxels' moments, [4, 5] synthesis, [6, 7] fill
-    if (ctx->timing) {
-        for (cudaEvent_t& e : ctx->tev)
-            if (!e) DPX_CUDA(cudaEventCreate(&e));
-        ev = ctx->tev;
+    if (ev) {
         ctx->tev_used = n_vox ? 8 : 6;
         ctx->stage_points = (double)atoms.size() + (double)n_vox;
         ctx->stage_k = K;
-        DPX_CUDA(cudaEventRecord(ev[6], st));
     }
-    DPX_CUDA(cudaMemcpyAsync(base, h.data(), staged, cudaMemcpyHostToDevice, st));
+    char* hp = nullptr;
+    DPX_CUDA(ctx->pin_plan.get(staged, &hp));
+    std::memcpy(hp, h.data(), staged);
+    DPX_CUDA(cudaMemcpyAsync(base, hp, staged, cudaMemcpyHostToDevice, st));
+    DPX_CUDA(ctx->pin_plan.copied(st));
     const int* d_lmax = reinterpret_cast<const int*>(base + oL);
     dpx::HarmonicTables tb{};
     tb.Lp = Lp;
@@ -404,8 +404,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         DPX_CUDA(cudaEventRecord(ev[5], st));
         DPX_CUDA(cudaEventRecord(ev[7], st));
     }
-    // the staging vector was copied from pageable memory (the call returns once
-    // it is staged); the arena stays owned by the context
+    // the arena and the pinned staging stay owned by the context
     return DPX_OK;
 }
 

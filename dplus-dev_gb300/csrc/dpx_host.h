@@ -47,6 +47,48 @@ struct DevBuf {
 
 inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// Grow-only pinned host staging buffer owned by a context.  get() waits for
+// the copy that last read it (the event recorded by copied()) before handing
+// it out again.
+struct HostPinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    cudaError_t get(size_t n, char** out) {
+        if (pending) {
+            if (cudaError_t e = cudaEventSynchronize(done)) return e;
+            pending = false;
+        }
+        if (n > bytes) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            bytes = 0;
+            if (cudaError_t e = cudaMallocHost(&p, n)) return e;
+            bytes = n;
+        }
+        *out = static_cast<char*>(p);
+        return cudaSuccess;
+    }
+    // the stream's copies out of the buffer have been issued
+    cudaError_t copied(cudaStream_t s) {
+        if (!done)
+            if (cudaError_t e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming)) return e;
+        if (cudaError_t e = cudaEventRecord(done, s)) return e;
+        pending = true;
+        return cudaSuccess;
+    }
+    void release() {
+        if (pending && done) cudaEventSynchronize(done);
+        if (p) cudaFreeHost(p);
+        if (done) cudaEventDestroy(done);
+        p = nullptr;
+        done = nullptr;
+        bytes = 0;
+        pending = false;
+    }
+};
+
 }  // namespace dpxh
 
 struct dpx_ctx_s {
@@ -68,6 +110,7 @@ struct dpx_ctx_s {
     double stage_points = 0, stage_k = 0;
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
+    dpxh::HostPinned pin_boxes, pin_plan;  // the harmonic fill's host staging
     std::vector<char> host_stage;
 };
 
@@ -78,6 +121,10 @@ struct dpx_grid_s {
     int precision;
     dpx::Geom g;
     void* cells;
+    // the phi-spline derivatives match the values: set by a fill that writes
+    // them (the harmonic synthesis) and by dpx_grid_compute_splines, cleared
+    // by every other write and whenever the device pointer is handed out
+    bool splines_current = false;
 };
 
 namespace dpxh {
@@ -134,11 +181,12 @@ dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* db
 // Harmonic (multipole) FP32 fill of a staged leaf (dpx_harmonic_host.cpp).
 // harmonic_accepts decides before the staging: boxes need their voxel step,
 // and the expansion order and the radial bins must stay within the kernels'
-// limits (device atoms are copied to `host_atoms` to measure them).
+// limits (device atoms are copied to `host_atoms` to measure them).  *R
+// receives the radius of the point sets about the leaf's centre.
 bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, std::vector<float>& host_atoms,
-                      int* status);
+                      double* R, int* status);
 int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid, const std::vector<float>& host_atoms);
+                  void* grid, const std::vector<float>& host_atoms, double R);
 // The FP64 fill launch of a staged leaf.
 cudaError_t launch_leaf_f64(cudaStream_t s, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase,
                             const dpx::Geom& G, void* grid);

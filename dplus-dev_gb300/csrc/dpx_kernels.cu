@@ -12,6 +12,7 @@
 // Grid cells are stored interleaved {re, im, d_re, d_im} (float4 or double4_32a) so
 // that one interpolation node is one 16 B / 32 B sector.
 #include "dpx_internal.h"
+#include "dpx_spline.cuh"
 
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -43,12 +44,8 @@ __device__ __forceinline__ void cell_indices(int64_t idx, int& qi, int& ti, int&
 
 
 // --------------------------------------------------------------------------
-// Periodic cubic-spline derivatives along each theta row.  The inverse of the
-// circulant circ(1,4,1) is a two-sided geometric kernel G(m) = C(a^m + a^(n-m))
-// / (1 - a^n), a = sqrt(3) - 2, C = 1/(2 sqrt 3); folding the right-hand side
-// 3(y[k+1]-y[k-1]) into it gives d_k = sum_s H(s) (y[k-s] - y[k+s]) with
-// H(s) = 3C a^(s-1) (a^2 - 1).  Long rows use the K-term truncation (|a|^K
-// below the type's epsilon); short rows use the exact periodic kernel.
+// Periodic cubic-spline derivatives along each theta row (row_spline,
+// dpx_spline.cuh), one cell per thread.
 // --------------------------------------------------------------------------
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; typedef float2 half; };
@@ -66,36 +63,9 @@ __global__ void splines_kernel(typename Vec4<T>::type* __restrict__ grid, int64_
     int qi, ti, pi;
     cell_indices(idx, qi, ti, pi);
     const int n = 6 * qi;
-    const int64_t row = shell_base(qi) + (int64_t)ti * n;
-    const double alpha = -0.26794919243112270647;  // sqrt(3) - 2
-    const double C = 0.28867513459481288225;        // 1 / (2 sqrt 3)
-    T dr = 0, di = 0;
-    if (n > 2 * K + 2) {
-        double w = 3.0 * C * (alpha * alpha - 1.0);
-        for (int s = 1; s <= K; ++s) {
-            int lo = pi - s; if (lo < 0) lo += n;
-            int hi = pi + s; if (hi >= n) hi -= n;
-            const typename Vec4<T>::type a = grid[row + lo];
-            const typename Vec4<T>::type b = grid[row + hi];
-            dr += T(w) * (a.x - b.x);
-            di += T(w) * (a.y - b.y);
-            w *= alpha;
-        }
-    } else {
-        const double an = pow(alpha, (double)n);
-        const double denom = 1.0 / (1.0 - an);
-        for (int s = 0; s < n; ++s) {
-            int m1 = s + 1; if (m1 >= n) m1 -= n;
-            int m0 = s - 1; if (m0 < 0) m0 += n;
-            const double g1 = C * (pow(alpha, (double)m1) + pow(alpha, (double)(n - m1))) * denom;
-            const double g0 = C * (pow(alpha, (double)m0) + pow(alpha, (double)(n - m0))) * denom;
-            const double h = 3.0 * (g1 - g0);
-            int k = pi - s; if (k < 0) k += n;
-            const typename Vec4<T>::type a = grid[row + k];
-            dr += T(h) * a.x;
-            di += T(h) * a.y;
-        }
-    }
+    const typename Vec4<T>::type* row = grid + shell_base(qi) + (int64_t)ti * n;
+    T dr, di;
+    row_spline<T, K>(n, pi, [&](int k) { return row[k]; }, dr, di);
     reinterpret_cast<H2*>(grid + idx)[1] = H2{dr, di};
 }
 

@@ -45,7 +45,8 @@ def _compile(src: str) -> str:
 def build_libdpx(force: bool = False) -> str:
     """Compile libdpx.so if any source is newer than the library."""
     srcs = [os.path.join(SRC_DIR, s) for s in SOURCES] + [
-        os.path.join(SRC_DIR, "dpx_internal.h"), os.path.join(SRC_DIR, "dpx_host.h"), os.path.join(INCLUDE_DIR, "dpx.h")]
+        os.path.join(SRC_DIR, "dpx_internal.h"), os.path.join(SRC_DIR, "dpx_host.h"),
+        os.path.join(SRC_DIR, "dpx_spline.cuh"), os.path.join(INCLUDE_DIR, "dpx.h")]
     if (not force and os.path.exists(LIB_PATH)
             and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs)):
         return LIB_PATH

@@ -65,3 +65,37 @@ def test_harmonic_and_direct_fill_agree_in_a_batch(ctx):
     ctx.set_fill_method(before)
     for x, y in zip(got[_lib.DPX_FILL_DIRECT], got[_lib.DPX_FILL_HARMONIC]):
         assert rel_to_max(y, x) <= 2e-6
+
+
+@pytest.mark.parametrize("extra,gs", [(LAYER, 40), (SOLVENT, 12)])
+def test_harmonic_fill_writes_the_spline_pass_derivatives(harmonic, extra, gs):
+    """The synthesis writes each row's phi-spline derivatives with its values
+    (and their conjugates on the Friedel mirror row): bit for bit those of the
+    spline pass, long rows and the short rows of the exact periodic kernel
+    (grid_size 12: shells 1-5 have rows of 30 cells or fewer)."""
+    amp = globule(800, 1.6, seed=146, extra=extra)
+    amp.xyz = amp.xyz + np.array([0.3, -0.2, 0.5])
+    g = amp.calculateGrid(harmonic, 4.0, gs, M.FP32)
+    g.compute_splines()  # a no-op: the fill wrote them
+    v0, d0 = g.read(True, True)
+    _ = g.device_ptr  # handing out the pointer clears the flag: the pass recomputes
+    g.compute_splines()
+    v1, d1 = g.read(True, True)
+    assert np.array_equal(v0, v1)
+    assert np.array_equal(d0, d1)
+    assert np.abs(d0).max() > 0
+
+
+def test_grid_write_clears_the_fill_derivatives(harmonic):
+    """A write after a harmonic fill: compute_splines derives the new values."""
+    amp = globule(500, 1.4, seed=147, extra=VACUUM)
+    g = amp.calculateGrid(harmonic, 4.0, 30, M.FP32)
+    v, _ = g.read(True, False)
+    g.write(2.0 * v)
+    g.compute_splines()
+    _, d2 = g.read(False, True)
+    ref = M.Grid(harmonic, 30, 4.0, M.FP32)
+    ref.write(2.0 * v)
+    ref.compute_splines()
+    _, dr = ref.read(False, True)
+    assert np.array_equal(d2, dr)
