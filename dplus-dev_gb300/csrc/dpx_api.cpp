@@ -200,8 +200,10 @@ void ctx_release(dpx_ctx ctx) {
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
                       &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels})
         b->release();
-    ctx->pin_boxes.release();
+    for (DevBuf& b : ctx->leaf_boxes) b.release();
     ctx->pin_plan.release();
+    ctx->pin_totals.release();
+    ctx->pin_small.release();
     for (cudaEvent_t e : ctx->tev)
         if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -423,12 +425,12 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     std::vector<LeafTables> lt(n);
     std::vector<char> harm(n, 0);  // FP32 leaves the harmonic method takes
     std::vector<std::vector<float>> host_atoms(n);
-    std::vector<double> harm_R(n, 0.0);
+    std::vector<HarmLeaf> harm_leaf(n);
     if (ctx->fill_method == DPX_FILL_HARMONIC)
         for (int j = 0; j < n; ++j) {
             if (grids[j]->precision != DPX_FP32) continue;
             int status = DPX_OK;
-            harm[j] = harmonic_accepts(ctx, pdbs[j], grids[j]->g, host_atoms[j], &harm_R[j], &status);
+            harm[j] = harmonic_accepts(ctx, j, pdbs[j], grids[j]->g, host_atoms[j], harm_leaf[j], &status);
             if (status) return status;
         }
     for (int j = 0; j < n; ++j) {
@@ -446,7 +448,7 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     for (int j = 0; j < n; ++j)
         if (harm[j])
             if (int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, host_atoms[j],
-                                       harm_R[j]))
+                                       harm_leaf[j]))
                 return rc;
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;

@@ -24,15 +24,17 @@
 // Kernels:
 //   hm_nodes     j_l at the Chebyshev nodes of every (shell, bin), FP64
 //   hm_fit       T_n(i, b, l) from the node values (inverse Vandermonde)
-//   hm_moments   per unit of <= 1024 points of one group: basis values of a
-//                tile of points in shared memory, then M_unit[n][k] (FP32)
-//   hm_groups    M_g = sum of its units, FP64, stored FP32
-//   hm_contract  C[i][k] = sum_g F_g(q_i) sum_n T_n M_g[n][k], FP64 across groups
+//   hm_moments   per unit of <= 1024 points of one group: M_unit[n][k] on the
+//                tensor cores (split TF32, FP32 sums), the basis values in
+//                registers by scaled Legendre recurrences
+//   hm_groups    M_g = sum of its units, compensated FP32
+//   hm_contract  C[i][k] = sum_g F_g(q_i) sum_n T_n M_g[n][k], compensated FP32
 //   hm_synth     per theta row t <= 3i/2: the B_m of both exponentials, the 6i
 //                cells by a table of 6i-th roots of unity, the voxel form
 //                factor prod_a s sinc(q_a s / 2) on the solvent part (a box of
 //                n voxels is exactly the sum of its voxels), the centring
-//                phase e^{i q.c} in FP64, and the Friedel mirror row.
+//                phase e^{i q.c} in double-float, the Friedel mirror row and
+//                the rows' phi-spline derivatives.
 #include "dpx_internal.h"
 #include "dpx_spline.cuh"
 
@@ -44,8 +46,6 @@ namespace {
 constexpr float kFourPi = 12.566370614359172954f;
 constexpr int kNodes = 6;       // Chebyshev nodes per bin = polynomial degree + 1
 constexpr int kMaxL = 192;      // local recurrence arrays
-constexpr int kMomThreads = 512;  // threads per moments block
-constexpr int kSliceK = 2560;      // (l, m) per moments block: 5 per thread
 
 __device__ __forceinline__ int k_of(int l, int m) { return l * (l + 1) / 2 + m; }
 __device__ __forceinline__ int l_of(int k) {
@@ -135,113 +135,265 @@ __global__ void hm_fit(int Lp, int nbins, int LM, const int* __restrict__ lmax, 
 }
 
 // ---------------------------------------------------------------------------
-// hm_moments: block (unit, k slice); units[u] = {first point, count, bin, 0}.
-// Points: float4 (x, y, z, weight) about the centre, sorted by group.
-// MP[u][n][k] (FP32) = sum over the unit's points of w u^n Pbar_lm e^{-i m phi}.
-// Dynamic shared memory (16-byte aligned regions): the recurrence
-// coefficients of the slice's orders, tp x kk float2 basis values (kk = the
-// slice width rounded to 1 mod 16: rows without bank conflicts), tp x 8
-// weights w u^n and tp angle records.
+// hm_moments: MP[u][n][k] (FP32) = sum over the points of unit u of
+// w u^n Pbar_lm(cos theta) e^{-i m phi}, k = (l, m), n < 6, on the tensor cores.
+//
+// One warp per (unit, pair of column quartets): quartet q holds the orders
+// m = 4q .. 4q+3, and the pair {q, Q-1-q} gives every warp about l_max + 2
+// rows of work.  Per quartet the warp walks the unit's points in chunks of 32
+// (four k-steps of 8) and, per order l, issues
+//   D[16 x 8] += A[16 x 8] B[8 x 8]     (mma.sync m16n8k8, TF32 in, FP32 out)
+// with A the weights (rows n: w u^n rounded to TF32; rows 8 + n: the
+// remainder, so that both halves of the split weight are applied) and B the
+// basis values of the chunk's points (columns: the quartet's 4 orders m x
+// {re, im}), B split the same way over two MMAs: every product carries the
+// hi*hi + hi*lo + lo*hi + lo*lo terms of the FP32 operands.  Lane (g, t)
+// builds the basis values of column g (order m0 + g/2, component g%2) at the
+// points 8j + t and 8j + t + 4 of k-step j: eight Legendre recurrences in
+// registers.  The recurrence is scaled, q_l = Pbar_lm / r_lm with
+// r_lm = prod_{j=m+1..l} a_jm / 2, so that one step is
+//   q_l = 2x q_{l-1} - c_lm q_{l-2},   c_lm = 4 b_lm / a_{l-1,m}
+// (cr[k] = {c_lm, r_lm}); r_lm is applied once per moment at the store.  The
+// start q_m = nmm[m] (-sin theta)^m e^{-i m phi} = nmm[m] z^m with
+// z = (-x + i y) / r (binary powering: no angles).  The D rows of lane (g, t),
+// n = g (hi and remainder rows summed), columns 2t, 2t+1, are the complex
+// moment of order m0 + t; they are summed over the chunks in shared memory.
 // ---------------------------------------------------------------------------
-template <bool FULL>
-__global__ void __launch_bounds__(kMomThreads) hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units,
-                                                          int LM, int K, int kk, int tp, float delta,
-                                                          const float2* __restrict__ ab, const float* __restrict__ nmm,
-                                                          float2* __restrict__ MP) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    float2* sAb = reinterpret_cast<float2*>(smem);
-    const size_t oY = ((size_t)K * sizeof(float2) + 15) / 16 * 16;
-    float2* sY = reinterpret_cast<float2*>(smem + oY);
-    const size_t oW = oY + ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16;
-    float4* sW = reinterpret_cast<float4*>(smem + oW);  // two float4 per point: w u^0 .. w u^5, 0, 0
-    float4* sA = reinterpret_cast<float4*>(smem + oW + (size_t)tp * 2 * sizeof(float4));
-    const int4 un = units[blockIdx.x];
-    const int k_lo = FULL ? 0 : blockIdx.y * kSliceK, k_hi = FULL ? K : min(K, k_lo + kSliceK);
-    const float rb = (un.z + 0.5f) * delta, ih = 2.f / delta;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) sAb[k] = ab[k];
-    float2 acc[kSliceK / kMomThreads][kNodes];
+constexpr int kChunk = 32;  // points per chunk: four k-steps of the m16n8k8 MMA
+
+__device__ __forceinline__ uint32_t tf32_rna(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Packed FP32 pairs (the f32x2 arithmetic of sm_100 and later): two chains
+// per instruction, each lane of the pair an IEEE FP32 operation.
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x pk2(float a, float b) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(f2x v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+    f2x r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+    f2x r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+    f2x r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__device__ __forceinline__ float2 cpow(float2 z, int e) {  // z^e, e >= 0, by binary powering
+    float2 r = make_float2(1.f, 0.f);
+    for (; e > 0; e >>= 1) {
+        if (e & 1) r = cmulf(r, z);
+        z = cmulf(z, z);
+    }
+    return r;
+}
+
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+    return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// One order l of a quartet: the eight recurrences in four packed pairs (the
+// pair of k-step j = the points 8j + t and 8j + t + 4; q_old holds q_{l-2} on
+// entry and q_l on exit, q_new holds q_{l-1}), the TF32 split of the basis
+// values (the high part by truncation, the exact remainder), then the chunk's
+// MMAs into the running sums sDl[lane].  PRO: the first four orders, where a
+// column starts (q_m = its start value) or has not started yet.
+template <bool PRO>
+__device__ __forceinline__ void moment_order(int l, int m, bool col_ok, int kc, const float2* __restrict__ cr,
+                                             f2x (&q_old)[4], const f2x (&q_new)[4], const f2x (&x2)[4],
+                                             const f2x (&st)[4], const uint32_t (&A)[4][4], float2* sDl,
+                                             bool drow, int lane) {
+    float cl;
+    if (PRO) cl = (col_ok && l >= m + 2) ? __ldg(&cr[kc].x) : 0.f;
+    else cl = __ldg(&cr[kc].x);
+    const f2x ncl = pk2(-cl, -cl);
+    const bool start = PRO && col_ok && l == m;
 #pragma unroll
-    for (int s = 0; s < kSliceK / kMomThreads; ++s)
+    for (int j = 0; j < 4; ++j) {
+        const f2x v = fma2(x2[j], q_new[j], mul2(ncl, q_old[j]));
+        q_old[j] = start ? st[j] : v;
+    }
+    // one accumulator per k-step: four independent chains of two MMAs
+    float d[4][4];
 #pragma unroll
-        for (int n = 0; n < kNodes; ++n) acc[s][n] = make_float2(0.f, 0.f);
-    for (int p0 = 0; p0 < un.y; p0 += tp) {
-        const int np = min(tp, un.y - p0);
-        __syncthreads();
-        // per point: angles and the weights w u^n
-        for (int p = threadIdx.x; p < np; p += blockDim.x) {
-            const float4 q = pts[un.x + p0 + p];
-            const float rxy = sqrtf(fmaf(q.x, q.x, q.y * q.y));
-            const float r = sqrtf(fmaf(q.z, q.z, rxy * rxy));
-            float4 a = make_float4(1.f, 0.f, 0.f, 0.f);  // cos theta, sin theta, phi
-            if (r > 0.f) a = make_float4(q.z / r, rxy / r, atan2f(q.y, q.x), 0.f);
-            sA[p] = a;
-            const float u = (r - rb) * ih;
-            float wn[8];
-            wn[0] = q.w;
-#pragma unroll
-            for (int n = 1; n < kNodes; ++n) wn[n] = wn[n - 1] * u;
-            wn[6] = wn[7] = 0.f;
-            sW[2 * p] = make_float4(wn[0], wn[1], wn[2], wn[3]);
-            sW[2 * p + 1] = make_float4(wn[4], wn[5], wn[6], wn[7]);
-        }
-        __syncthreads();
-        // items (column pair c, point p), p fastest: the lanes of a warp share
-        // one or two columns (broadcast coefficient loads) and write rows p of
-        // stride kk = 1 mod 16 float2 (no bank conflicts)
-        const int half = LM / 2 + 1;
-        for (int it = threadIdx.x; it < np * half; it += blockDim.x) {
-            const int p = it % np, cpair = it / np;
-            const float4 a = sA[p];
-            float2* y = sY + (size_t)p * kk - k_lo;
-            for (int side = 0; side < 2; ++side) {
-                const int m = side == 0 ? cpair : LM - cpair;
-                if (side == 1 && m == cpair) break;
-                if (!FULL && (k_of(LM, m) < k_lo || k_of(m, m) >= k_hi)) continue;
-                float pw = nmm[m];
-                for (int mm = 0; mm < m; ++mm) pw *= -a.y;
-                float sm, cm;
-                sincosf((float)m * a.z, &sm, &cm);
-                float p2 = 0.f, p1 = pw;
-                int k = k_of(m, m);
-                if (FULL || k >= k_lo) y[k] = make_float2(p1 * cm, -p1 * sm);
-                // orders l = m+1 .. lend whose k stays below k_hi
-                int lend = LM;
-                if (!FULL)
-                    while (lend > m && k_of(lend, m) >= k_hi) --lend;
-                for (int l = m + 1; l <= lend; ++l) {
-                    k += l;  // k_of(l, m) = k_of(l - 1, m) + l
-                    const float2 c = sAb[k];
-                    const float pn = c.x * fmaf(a.x, p1, -c.y * p2);
-                    if (FULL || k >= k_lo) y[k] = make_float2(pn * cm, -pn * sm);
-                    p2 = p1;
-                    p1 = pn;
-                }
-            }
-        }
-        __syncthreads();
-        for (int p = 0; p < np; ++p) {
-            const float4 w0 = sW[2 * p], w1 = sW[2 * p + 1];
-            const float w[kNodes] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y};
-            const float2* yp = sY + (size_t)p * kk;
-#pragma unroll
-            for (int s = 0; s < kSliceK / kMomThreads; ++s) {
-                const int kl = s * kMomThreads + threadIdx.x;
-                if (k_lo + kl >= k_hi) break;
-                const float2 yv = yp[kl];
-#pragma unroll
-                for (int n = 0; n < kNodes; ++n) {
-                    acc[s][n].x = fmaf(w[n], yv.x, acc[s][n].x);
-                    acc[s][n].y = fmaf(w[n], yv.y, acc[s][n].y);
-                }
-            }
-        }
+    for (int j = 0; j < 4; ++j) d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
+    if (drow) {
+        const float2 prev = sDl[lane];
+        d[0][0] = prev.x;
+        d[0][1] = prev.y;
     }
 #pragma unroll
-    for (int s = 0; s < kSliceK / kMomThreads; ++s) {
-        const int k = k_lo + s * kMomThreads + threadIdx.x;
-        if (k >= k_hi) break;
+    for (int j = 0; j < 4; ++j) {
+        float v0, v1;
+        upk2(q_old[j], v0, v1);
+        const uint32_t h0 = __float_as_uint(v0) & 0xffffe000u, h1 = __float_as_uint(v1) & 0xffffe000u;
+        float r0, r1;
+        upk2(sub2(q_old[j], pk2(__uint_as_float(h0), __uint_as_float(h1))), r0, r1);
+        mma_tf32(d[j], A[j], h0, h1);
+        mma_tf32(d[j], A[j], __float_as_uint(r0), __float_as_uint(r1));
+    }
+    if (drow) {
+        f2x s[4];
 #pragma unroll
-        for (int n = 0; n < kNodes; ++n) MP[((int64_t)blockIdx.x * kNodes + n) * K + k] = acc[s][n];
+        for (int j = 0; j < 4; ++j) s[j] = add2(pk2(d[j][0], d[j][1]), pk2(d[j][2], d[j][3]));
+        float re, im;
+        upk2(add2(add2(s[0], s[1]), add2(s[2], s[3])), re, im);
+        sDl[lane] = make_float2(re, im);
+    }
+}
+
+__global__ void __launch_bounds__(32) hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units,
+                                                 int LM, int K, float delta, const float2* __restrict__ cr,
+                                                 const float* __restrict__ nmm, float2* __restrict__ MP) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* sD = reinterpret_cast<float2*>(smem);  // per quartet [(l - m0) * 24 + lane], lanes < 24
+    const int lane = threadIdx.x;
+    const int g = lane >> 2, t = lane & 3;
+    const int4 un = units[blockIdx.x];
+    const int Q = (LM + 4) / 4;  // quartets
+    const int nq = (Q - 1 - (int)blockIdx.y > (int)blockIdx.y) ? 2 : 1;
+    const int m0a = 4 * blockIdx.y, m0b = 4 * (Q - 1 - blockIdx.y);
+    const int nla = LM - m0a + 1, nlb = nq == 2 ? LM - m0b + 1 : 0;
+    const float rb = (un.z + 0.5f) * delta, ih = 2.f / delta;
+    const bool drow = lane < 24;  // D rows n = g < 6
+    for (int e = lane; e < (nla + nlb) * 24; e += 32) sD[e] = make_float2(0.f, 0.f);
+    __syncwarp();
+
+    for (int c0 = 0; c0 < un.y; c0 += kChunk) {
+        // ---- point c0 + lane: geometry and the powers z^m0 of the pair's quartets ----
+        float ct = 1.f, u = 0.f, w = 0.f;
+        float2 z = make_float2(0.f, 0.f);
+        if (c0 + lane < un.y) {
+            const float4 P = pts[un.x + c0 + lane];
+            const float r = sqrtf(fmaf(P.z, P.z, fmaf(P.x, P.x, P.y * P.y)));
+            if (r > 0.f) {
+                const float ir = 1.f / r;
+                ct = P.z * ir;
+                z = make_float2(-P.x * ir, P.y * ir);
+            }
+            u = (r - rb) * ih;
+            w = P.w;
+        }
+        const float2 zq0 = cpow(z, m0a);
+        const float2 zq1 = nq == 2 ? cpow(z, m0b) : make_float2(0.f, 0.f);
+        // ---- the lane's eight points 8j + t + 4h: recurrence inputs, weight fragments ----
+        f2x x2[4];
+        uint32_t A[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float xx[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int src = 8 * j + t + 4 * h;
+                xx[h] = 2.f * __shfl_sync(0xffffffffu, ct, src);
+                const float us = __shfl_sync(0xffffffffu, u, src);
+                float wv = __shfl_sync(0xffffffffu, w, src);
+                // weight w u^n of row n = g, split into TF32 and remainder
+                if (g >= 6) wv = 0.f;
+                for (int n = 0; n < g; ++n) wv *= us;
+                const uint32_t wh = tf32_rna(wv);
+                A[j][2 * h] = wh;                                          // a0 / a2: row g
+                A[j][2 * h + 1] = __float_as_uint(wv - __uint_as_float(wh));  // a1 / a3: row g + 8
+            }
+            x2[j] = pk2(xx[0], xx[1]);
+        }
+        // ---- the pair's quartets ----
+#pragma unroll 1
+        for (int qi = 0; qi < nq; ++qi) {
+            const int m0 = qi == 0 ? m0a : m0b;
+            const float2 zq = qi == 0 ? zq0 : zq1;
+            const int c = g >> 1;  // this lane's column m0 + c, component g & 1
+            const int m = m0 + c;
+            const bool col_ok = m <= LM;
+            const float nm = col_ok ? nmm[m] : 0.f;
+            f2x st[4], qa_[4], qb_[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float sv[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int src = 8 * j + t + 4 * h;
+                    const float2 zp = shfl2(z, src);
+                    float2 zm = shfl2(zq, src);  // z^m0 of the point, times z^c
+                    if (c >= 1) zm = cmulf(zm, zp);
+                    if (c >= 2) zm = cmulf(zm, zp);
+                    if (c >= 3) zm = cmulf(zm, zp);
+                    sv[h] = nm * ((g & 1) ? zm.y : zm.x);
+                }
+                st[j] = pk2(sv[0], sv[1]);
+                qa_[j] = 0ull;
+                qb_[j] = 0ull;
+            }
+            float2* sDq = sD + (qi == 0 ? 0 : nla * 24);
+            int kc = col_ok ? m0 * (m0 + 1) / 2 + m : 0;  // k(l, m) at l = m0 (read once l >= m + 2)
+            int l = m0;
+            // orders m0 .. m0 + 3: the columns start
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2) {
+                if (l <= LM) moment_order<true>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+                if (col_ok) kc += l + 1;
+                ++l;
+                if (l <= LM) moment_order<true>(l, m, col_ok, kc, cr, qb_, qa_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+                if (col_ok) kc += l + 1;
+                ++l;
+            }
+            // the rest, two orders per iteration
+            for (; l + 1 <= LM; l += 2) {
+                moment_order<false>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+                if (col_ok) kc += l + 1;
+                moment_order<false>(l + 1, m, col_ok, kc, cr, qb_, qa_, x2, st, A, sDq + (l + 1 - m0) * 24, drow, lane);
+                if (col_ok) kc += l + 2;
+            }
+            if (l <= LM) moment_order<false>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+        }
+    }
+    __syncwarp();
+    // ---- store: lane (g < 6, t) holds the moment n = g of order m0 + t ----
+    for (int qi = 0; qi < nq; ++qi) {
+        const int m0 = qi == 0 ? m0a : m0b;
+        const int mo = m0 + t;
+        if (!drow || mo > LM) continue;
+        const float2* sDq = sD + (qi == 0 ? 0 : nla * 24);
+        float2* out = MP + ((int64_t)blockIdx.x * kNodes + g) * K;
+        int k = mo * (mo + 1) / 2 + mo;
+        for (int l = mo; l <= LM; ++l) {
+            const float2 v = sDq[(l - m0) * 24 + lane];
+            const float sc = __ldg(&cr[k].y);
+            out[k] = make_float2(v.x * sc, v.y * sc);
+            k += l + 1;
+        }
     }
 }
 
@@ -293,8 +445,8 @@ __global__ void __launch_bounds__(kBinThreads) vx_expand(const float4* __restric
 // Block-wide exclusive scan of one int64 per thread; returns the thread's
 // prefix, *total the block's sum.
 __device__ __forceinline__ int64_t block_scan_excl(int64_t v, int64_t* total) {
-    __shared__ int64_t ws[kBinThreads / 32];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ int64_t ws[32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     int64_t x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -304,13 +456,83 @@ __device__ __forceinline__ int64_t block_scan_excl(int64_t v, int64_t* total) {
     if (lane == 31) ws[w] = x;
     __syncthreads();
     int64_t before = 0, all = 0;
-    for (int k = 0; k < kBinThreads / 32; ++k) {
+    for (int k = 0; k < nw; ++k) {
         if (k < w) before += ws[k];
         all += ws[k];
     }
     __syncthreads();
     *total = all;
     return before + x - v;
+}
+
+// The leaf's solvent boxes (raw D+ records {cx, cy, cz, w, Lx, Ly, Lz, -}) about
+// the centre c: the float4 pair {centre - c, w}, {L, 0}; each box's voxel
+// count (its edges over the voxel step, rounded as vx_expand rounds them); the
+// largest squared distance of a box corner from c (rounded up to FP32) and
+// the total voxel count, reduced into scal = {r2 bits, total}.
+__global__ void __launch_bounds__(kBinThreads) vx_prepare(const float* __restrict__ raw, int64_t nb, double cx,
+                                                          double cy, double cz, float vs, float4* __restrict__ boxes,
+                                                          int64_t* __restrict__ counts,
+                                                          unsigned long long* __restrict__ scal) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float q = 0.f;
+    int64_t n = 0;
+    if (b < nb) {
+        const float* r = raw + 8 * b;
+        const double c[3] = {cx, cy, cz};
+        double e2 = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const double e = fabs((double)r[k] - c[k]) + 0.5 * (double)r[4 + k];
+            e2 += e * e;
+        }
+        q = __double2float_ru(e2);
+        boxes[2 * b] = make_float4((float)((double)r[0] - cx), (float)((double)r[1] - cy), (float)((double)r[2] - cz),
+                                   r[3]);
+        boxes[2 * b + 1] = make_float4(r[4], r[5], r[6], 0.f);
+        n = (int64_t)__float2int_rn(r[4] / vs) * __float2int_rn(r[5] / vs) * __float2int_rn(r[6] / vs);
+        counts[b] = n;
+    }
+    // block reduction, then one atomic each
+    unsigned qb = __float_as_uint(q);  // q >= 0: the bits order as the values
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        qb = max(qb, __shfl_down_sync(0xffffffffu, qb, o));
+        n += __shfl_down_sync(0xffffffffu, n, o);
+    }
+    __shared__ unsigned sq[kBinThreads / 32];
+    __shared__ int64_t sn[kBinThreads / 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sq[w] = qb;
+        sn[w] = n;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned qm = 0;
+        int64_t nt = 0;
+        for (int k = 0; k < kBinThreads / 32; ++k) {
+            qm = max(qm, sq[k]);
+            nt += sn[k];
+        }
+        atomicMax(scal, (unsigned long long)qm);
+        atomicAdd(scal + 1, (unsigned long long)nt);
+    }
+}
+
+// vstart = exclusive prefix of the box voxel counts: one block, a contiguous
+// run of boxes per thread
+__global__ void __launch_bounds__(1024) vx_vstart(const int64_t* __restrict__ counts, int64_t nb,
+                                                  int64_t* __restrict__ vstart) {
+    const int64_t per = (nb + blockDim.x - 1) / blockDim.x;
+    const int64_t b0 = min(nb, (int64_t)threadIdx.x * per), b1 = min(nb, b0 + per);
+    int64_t mine = 0;
+    for (int64_t b = b0; b < b1; ++b) mine += counts[b];
+    int64_t all;
+    int64_t run = block_scan_excl(mine, &all);
+    for (int64_t b = b0; b < b1; ++b) {
+        vstart[b] = run;
+        run += counts[b];
+    }
 }
 
 // block per bin: its total over the expand blocks
@@ -451,7 +673,7 @@ __device__ __forceinline__ float sinc_h(float h) {
 }
 
 // ---------------------------------------------------------------------------
-// hm_synth: one block per theta row (i, t <= 3i/2); rows[] lists (i, t).
+// hm_synth: one block per theta row (i, t <= 3i/2), shell-major.
 // The row's 6i cells are F(p) = sum_{|m| <= l_i} G_m w^{mp}, w = e^{2 pi i/6i},
 // with G_m = 4 pi sum_l i^l P_lm C_lm and G_-m = 4 pi sum_l i^l P_lm conj(C_lm)
 // (m > 0).  Writing p = s i + j (sextant s < 6, column j < i):
@@ -484,7 +706,10 @@ __device__ __forceinline__ float2 split_ff(double x) {
     return make_float2(hi, (float)(x - (double)hi));
 }
 
-__global__ void __launch_bounds__(kSynthThreads) hm_synth(const int2* __restrict__ rows, const float2* __restrict__ Ca,
+// Rows of shells 1..n: S(n) = sum_{j <= n} (floor(3j/2) + 1) = n(n+1)/2 + floor(n/2) ceil(n/2) + n.
+__device__ __forceinline__ int rows_through(int n) { return n * (n + 1) / 2 + (n / 2) * ((n + 1) / 2) + n; }
+
+__global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* __restrict__ Ca,
                                                           const float2* __restrict__ Cv, int K,
                                                           const int* __restrict__ lmax, const float2* __restrict__ ab,
                                                           const float* __restrict__ nmm, double step, float vox_s,
@@ -492,8 +717,14 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(const int2* __restrict
                                                           double origin, float4* __restrict__ grid) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float2 sRow[3];
-    const int2 row = rows[blockIdx.x];
-    const int i = row.x, t = row.y;
+    // block -> (shell i, row t): the smallest i with rows_through(i) > block
+    int lo = 1, hi = Lp;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (rows_through(mid) > (int)blockIdx.x) hi = mid;
+        else lo = mid + 1;
+    }
+    const int i = lo, t = (int)blockIdx.x - rows_through(i - 1);
     const int li = lmax[i];
     const int Ki = k_of(li, li) + 1;
     const int nph = 6 * i, h = 3 * i;
@@ -679,32 +910,22 @@ cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a) {
 }
 
 cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C) {
-    const int slices = (a.K + kSliceK - 1) / kSliceK;
-    int kk = a.K < kSliceK ? a.K : kSliceK;
-    kk += (17 - kk % 16) % 16;  // row stride = 1 mod 16 float2
-    const size_t oY = ((size_t)a.K * sizeof(float2) + 15) / 16 * 16;
-    // points per tile: the basis rows within 200 KB of shared memory with the coefficients
-    const size_t budget = 200 * 1024 > oY + 4096 ? 200 * 1024 - oY : 4096;
-    int tp = (int)(budget / ((size_t)kk * sizeof(float2) + 48));
-    tp = tp < 1 ? 1 : (tp > 16 ? 16 : tp);
-    const size_t smem = oY + ((size_t)tp * kk * sizeof(float2) + 15) / 16 * 16 + (size_t)tp * 2 * sizeof(float4) +
-                        (size_t)tp * sizeof(float4);
-    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    // one warp per (unit, quartet pair); the running sums of both quartets:
+    // (LM - 4y + 1) + (LM - 4(Q-1-y) + 1) = 2 LM + 6 - 4Q orders for a pair,
+    // LM + 1 for the single quartet of Q = 1
+    const int Q = (a.LM + 4) / 4;
+    const int pairs = (Q + 1) / 2;
+    const int orders = Q >= 2 ? 2 * a.LM + 6 - 4 * Q : a.LM + 1;
+    const size_t smem = (size_t)orders * 24 * sizeof(float2);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     if (a.ev0) {
         cudaError_t e = cudaEventRecord(a.ev0, s);
         if (e != cudaSuccess) return e;
     }
-    if (slices == 1) {
-        cudaError_t e = cudaFuncSetAttribute(hm_moments<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        hm_moments<true><<<dim3(a.n_units, 1), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp,
-                                                                      (float)a.delta, a.ab, a.nmm, a.MP);
-    } else {
-        cudaError_t e = cudaFuncSetAttribute(hm_moments<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        hm_moments<false><<<dim3(a.n_units, slices), kMomThreads, smem, s>>>(a.pts, a.units, a.LM, a.K, kk, tp,
-                                                                           (float)a.delta, a.ab, a.nmm, a.MP);
-    }
+    hm_moments<<<dim3(a.n_units, pairs), 32, smem, s>>>(a.pts, a.units, a.LM, a.K, (float)a.delta, a.cr, a.nmm, a.MP);
     if (a.ev1) {
         cudaError_t e = cudaEventRecord(a.ev1, s);
         if (e != cudaSuccess) return e;
@@ -718,9 +939,19 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C)
 
 int harmonic_max_bins() { return kMaxBins; }
 
+cudaError_t launch_voxel_prepare(cudaStream_t s, const VoxelPrepArgs& a) {
+    if (a.nb <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(a.scal, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    vx_prepare<<<(unsigned)((a.nb + kBinThreads - 1) / kBinThreads), kBinThreads, 0, s>>>(
+        a.raw, a.nb, a.cx, a.cy, a.cz, a.vs, a.boxes, a.counts, a.scal);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
     const int nblk = (int)((a.nv + kBinThreads - 1) / kBinThreads);
     if (a.nbins > kMaxBins) return cudaErrorInvalidValue;
+    vx_vstart<<<1, 1024, 0, s>>>(a.counts, a.nb, a.vstart);
     vx_expand<<<nblk, kBinThreads, 0, s>>>(a.boxes, a.vstart, a.nb, a.nv, a.vs, a.delta, a.nbins, a.tmp, a.vbin,
                                            a.hist, nblk);
     vx_totals<<<a.nbins, kBinThreads, 0, s>>>(a.hist, a.nbins, nblk, a.total);
@@ -740,8 +971,9 @@ cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
         cudaError_t e = cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    hm_synth<<<a.n_rows, kSynthThreads, smem, s>>>(a.rows, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step, a.vox_s, a.cx,
-                                                   a.cy, a.cz, a.use_center, a.scale, a.origin, a.grid);
+    const int n_rows = a.Lp * (a.Lp + 1) / 2 + (a.Lp / 2) * ((a.Lp + 1) / 2) + a.Lp;
+    hm_synth<<<n_rows, kSynthThreads, smem, s>>>(a.Lp, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step, a.vox_s, a.cx,
+                                                 a.cy, a.cz, a.use_center, a.scale, a.origin, a.grid);
     return cudaGetLastError();
 }
 

@@ -61,34 +61,16 @@ void chebyshev_fit(double nodes[6], double vinv[36]) {
         for (int c = 0; c < 6; ++c) vinv[n * 6 + c] = a[n][6 + c];
 }
 
-// The voxels of the solvent boxes about the centre t.cen, expanded and
-// sorted by radius bin (bin width delta) on the device, in box order within a
-// bin (dpx::launch_voxel_bins); the bin totals come back to build the units of
-// <= kUnitPoints voxels per bin.
-int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s, double delta, int nbins,
-               std::vector<int4>& units, std::vector<int2>& groups, std::vector<int>& gu, const float4** out,
-               int64_t* n_out) {
-    const int64_t nb = t.n_boxes;
-    // staging: the boxes about the centre [2 nb] float4, the first voxel of each box [nb]
-    const size_t oB = 0;
-    const size_t oS = al16((size_t)2 * nb * sizeof(float4));
-    const size_t staged = al16(oS + (size_t)nb * sizeof(int64_t));
-    char* hp = nullptr;
-    DPX_CUDA(ctx->pin_boxes.get(staged, &hp));
-    float4* hb = reinterpret_cast<float4*>(hp + oB);
-    int64_t* vstart = reinterpret_cast<int64_t*>(hp + oS);
-    int64_t nv = 0;
-    for (int64_t b = 0; b < nb; ++b) {
-        const float* r = d.boxes + 8 * b;
-        hb[2 * b] = make_float4((float)((double)r[0] - t.cen[0]), (float)((double)r[1] - t.cen[1]),
-                                (float)((double)r[2] - t.cen[2]), r[3]);
-        hb[2 * b + 1] = make_float4(r[4], r[5], r[6], 0.f);
-        vstart[b] = nv;
-        nv += (int64_t)std::lround(r[4] / s) * std::lround(r[5] / s) * std::lround(r[6] / s);
-    }
+// The voxels of the leaf's solvent boxes (centred and counted on the device by
+// harmonic_accepts), expanded and sorted by radius bin (bin width delta) on
+// the device, in box order within a bin (dpx::launch_voxel_bins).  The bin
+// totals come back into pinned memory; bin_voxels_finish waits for them and
+// builds the units of <= kUnitPoints voxels per bin.
+int bin_voxels_launch(dpx_ctx ctx, const HarmLeaf& hl, double s, double delta, int nbins, const float4** out) {
+    const int64_t nb = hl.nb, nv = hl.nv;
     if (nv > INT32_MAX) return fail(DPX_ERR_ARG, "harmonic fill: %lld voxels", (long long)nv);
     const int nblk = (int)((nv + 255) / 256);
-    const size_t oTmp = staged;
+    const size_t oTmp = 0;
     const size_t oBin = al16(oTmp + (size_t)nv * sizeof(float4));
     const size_t oHist = al16(oBin + (size_t)nv * sizeof(int));
     const size_t oOff = al16(oHist + (size_t)nbins * nblk * sizeof(int));
@@ -101,11 +83,10 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
     }
     char* base = static_cast<char*>(ctx->voxels.p);
     cudaStream_t st = ctx->stream;
-    DPX_CUDA(cudaMemcpyAsync(base, hp, staged, cudaMemcpyHostToDevice, st));
-    DPX_CUDA(ctx->pin_boxes.copied(st));
     dpx::VoxelBinArgs a{};
-    a.boxes = reinterpret_cast<const float4*>(base + oB);
-    a.vstart = reinterpret_cast<const int64_t*>(base + oS);
+    a.boxes = hl.boxes;
+    a.counts = hl.counts;
+    a.vstart = hl.vstart;
     a.nb = nb;
     a.nv = nv;
     a.vs = (float)s;
@@ -118,9 +99,19 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
     a.total = reinterpret_cast<int64_t*>(base + oTot);
     a.out = reinterpret_cast<float4*>(base + oOut);
     DPX_CUDA(dpx::launch_voxel_bins(st, a));
-    std::vector<int64_t> tot(nbins);
-    DPX_CUDA(cudaMemcpyAsync(tot.data(), a.total, (size_t)nbins * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    DPX_CUDA(cudaStreamSynchronize(st));
+    char* hp = nullptr;
+    DPX_CUDA(ctx->pin_totals.get((size_t)nbins * sizeof(int64_t), &hp));
+    DPX_CUDA(cudaMemcpyAsync(hp, a.total, (size_t)nbins * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    DPX_CUDA(ctx->pin_totals.copied(st));
+    *out = a.out;
+    return DPX_OK;
+}
+
+int bin_voxels_finish(dpx_ctx ctx, int nbins, std::vector<int4>& units, std::vector<int2>& groups,
+                      std::vector<int>& gu) {
+    char* hp = nullptr;
+    DPX_CUDA(ctx->pin_totals.get((size_t)nbins * sizeof(int64_t), &hp));  // waits for the copy
+    const int64_t* tot = reinterpret_cast<const int64_t*>(hp);
     int64_t start = 0;
     for (int bin = 0; bin < nbins; ++bin) {
         const int64_t c = tot[bin];
@@ -133,16 +124,15 @@ int bin_voxels(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, double s
         start += c;
     }
     gu.push_back((int)units.size());
-    *out = a.out;
-    *n_out = nv;
     return DPX_OK;
 }
 
 }  // namespace
 
-bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, std::vector<float>& host_atoms,
-                      double* R_out, int* status) {
+bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::Geom& G,
+                      std::vector<float>& host_atoms, HarmLeaf& hl, int* status) {
     *status = DPX_OK;
+    hl = HarmLeaf{};
     if (d.n_boxes > 0 && d.boxes && !(d.voxel_step > 0.0)) return false;
     const float* src = d.atoms;
     if (d.atoms_on_device) {  // atoms already shifted by the centre
@@ -173,19 +163,56 @@ bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, st
         for (int k = 0; k < 3; ++k) q += (src[4 * a + k] - ca[k]) * (src[4 * a + k] - ca[k]);
         r2 = std::max(r2, q);
     }
+    // the solvent boxes: uploaded once, centred and counted on the device, with
+    // their largest corner distance and the voxel total read back
     const int64_t nb = d.n_boxes > 0 && d.boxes ? d.n_boxes : 0;
-    for (int64_t b = 0; b < nb; ++b) {
-        const float* r = d.boxes + 8 * b;
-        double q = 0;
-        for (int k = 0; k < 3; ++k) {
-            const double e = std::fabs((double)r[k] - c[k]) + 0.5 * r[4 + k];
-            q += e * e;
+    if (nb > 0) {
+        if ((int)ctx->leaf_boxes.size() <= slot) ctx->leaf_boxes.resize(slot + 1);
+        dpxh::DevBuf& B = ctx->leaf_boxes[slot];
+        const size_t oRaw = 0;
+        const size_t oBox = al16((size_t)8 * nb * sizeof(float));
+        const size_t oCnt = al16(oBox + (size_t)2 * nb * sizeof(float4));
+        const size_t oVs = al16(oCnt + (size_t)nb * sizeof(int64_t));
+        const size_t oSc = al16(oVs + (size_t)nb * sizeof(int64_t));
+        cudaError_t e = B.reserve(oSc + 2 * sizeof(unsigned long long));
+        char* base = static_cast<char*>(B.p);
+        cudaStream_t st = ctx->stream;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(base + oRaw, d.boxes, (size_t)8 * nb * sizeof(float), cudaMemcpyHostToDevice, st);
+        dpx::VoxelPrepArgs a{};
+        a.raw = reinterpret_cast<const float*>(base + oRaw);
+        a.nb = nb;
+        a.cx = c[0];
+        a.cy = c[1];
+        a.cz = c[2];
+        a.vs = (float)d.voxel_step;
+        a.boxes = reinterpret_cast<float4*>(base + oBox);
+        a.counts = reinterpret_cast<int64_t*>(base + oCnt);
+        a.scal = reinterpret_cast<unsigned long long*>(base + oSc);
+        if (e == cudaSuccess) e = dpx::launch_voxel_prepare(st, a);
+        char* hp = nullptr;
+        if (e == cudaSuccess) e = ctx->pin_small.get(2 * sizeof(unsigned long long), &hp);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hp, a.scal, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            *status = cuda_fail(e, "harmonic fill: solvent boxes");
+            return false;
         }
-        r2 = std::max(r2, q);
+        const unsigned long long* sc = reinterpret_cast<const unsigned long long*>(hp);
+        const unsigned qbits = (unsigned)sc[0];
+        float qf;
+        std::memcpy(&qf, &qbits, sizeof qf);
+        r2 = std::max(r2, (double)qf);
+        hl.nb = nb;
+        hl.nv = (int64_t)sc[1];
+        hl.boxes = a.boxes;
+        hl.counts = a.counts;
+        hl.vstart = reinterpret_cast<int64_t*>(base + oVs);
     }
     // the fill's points are rounded to FP32 about the centre: a relative margin
     const double R = std::sqrt(r2) * (1.0 + 1e-6);
-    *R_out = R;
+    hl.R = R;
     if (order_of(G.Lp * G.step * R) > dpx::harmonic_max_l()) return false;
     const double delta = kBinWidthTimesQmax / (G.Lp * G.step);
     if (nb > 0 && (int)(R / delta) + 1 > dpx::harmonic_max_bins()) return false;
@@ -193,7 +220,8 @@ bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, st
 }
 
 int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid, const std::vector<float>& host_atoms, double R) {
+                  void* grid, const std::vector<float>& host_atoms, const HarmLeaf& hl) {
+    const double R = hl.R;
     const int Lp = G.Lp;
     cudaStream_t st = ctx->stream;
     cudaEvent_t* ev = nullptr;  // [0, 1] atoms' moments, [2, 3] voxels' moments, [4, 5] synthesis, [6, 7] fill
@@ -202,6 +230,17 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
             if (!e) DPX_CUDA(cudaEventCreate(&e));
         ev = ctx->tev;
         DPX_CUDA(cudaEventRecord(ev[6], st));
+    }
+    // ---- radial bins; the voxels are expanded and binned on the device while
+    // the host plans the rest ----
+    const double delta = kBinWidthTimesQmax / (Lp * G.step);
+    const int nbins = (int)(R / delta) + 1;
+    const double s = d.voxel_step;
+    const float4* vox_dev = nullptr;
+    if (hl.nb > 0) {
+        if (nbins > dpx::harmonic_max_bins())
+            return fail(DPX_ERR_ARG, "harmonic fill: %d radial bins above %d", nbins, dpx::harmonic_max_bins());
+        if (int rc = bin_voxels_launch(ctx, hl, s, delta, nbins, &vox_dev)) return rc;
     }
     // ---- point sets about the leaf's centre t.cen (device atoms arrive shifted) ----
     const float* src = d.atoms_on_device ? host_atoms.data() : d.atoms;
@@ -215,9 +254,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
                 atoms[j] = make_float4((float)((double)src[4 * j] - sh[0]), (float)((double)src[4 * j + 1] - sh[1]),
                                        (float)((double)src[4 * j + 2] - sh[2]), (float)u);
     }
-    // R (from harmonic_accepts): the atoms and the corners of the solvent boxes
-    const double s = d.voxel_step;
-    // ---- orders ----
+    // ---- orders (R from harmonic_accepts: the atoms and the corners of the solvent boxes) ----
     std::vector<int> lmax(Lp + 1, 0);
     for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * R);
     const int LM = lmax[Lp];
@@ -231,6 +268,20 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
             const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
             ab[(size_t)l * (l + 1) / 2 + m] = make_float2((float)a, (float)b);
         }
+    // the moments' scaled recurrence q_l = Pbar_lm / r_lm, r_lm = prod_{j=m+1..l} a_jm / 2:
+    // q_l = 2x q_{l-1} - c_lm q_{l-2}, c_lm = 4 b_lm / a_{l-1,m} (0 for l = m + 1)
+    std::vector<float2> cr(K, make_float2(0.f, 1.f));
+    for (int m = 0; m <= LM; ++m) {
+        double r = 1.0, a_prev = 0.0;
+        for (int l = m + 1; l <= LM; ++l) {
+            const double a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+            const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
+            r *= 0.5 * a;
+            const double c = l >= m + 2 ? 4.0 * b / a_prev : 0.0;
+            cr[(size_t)l * (l + 1) / 2 + m] = make_float2((float)c, (float)r);
+            a_prev = a;
+        }
+    }
     std::vector<float> nmm(LM + 1);  // Pbar_mm = nmm[m] (-sin theta)^m, orthonormal
     {
         double v = 0.28209479177387814347;  // 1 / sqrt(4 pi)
@@ -239,12 +290,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
             nmm[m] = (float)v;
         }
     }
-    std::vector<int2> rows;
-    for (int i = 1; i <= Lp; ++i)
-        for (int tt = 0; tt <= 3 * i / 2; ++tt) rows.push_back(make_int2(i, tt));
-    // ---- radial bins and the degree-5 interpolation on Chebyshev nodes ----
-    const double delta = kBinWidthTimesQmax / (Lp * G.step);
-    const int nbins = (int)(R / delta) + 1;
+    // ---- the degree-5 interpolation of the radial bins on Chebyshev nodes ----
     double nodes[6], vinv[36];
     chebyshev_fit(nodes, vinv);
     // ---- groups: (bin, ion) for atoms, bin for voxels; counting sort ----
@@ -285,22 +331,18 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     };
     Set sa, sv;
     make_set(atoms, false, sa);
-    // voxels: expanded and binned on the device
-    int64_t n_vox = 0;
-    const float4* vox_dev = nullptr;
-    if (t.n_boxes > 0) {
-        if (nbins > dpx::harmonic_max_bins())
-            return fail(DPX_ERR_ARG, "harmonic fill: %d radial bins above %d", nbins, dpx::harmonic_max_bins());
-        if (int rc = bin_voxels(ctx, d, t, s, delta, nbins, sv.units, sv.groups, sv.gu, &vox_dev, &n_vox)) return rc;
-    }
+    // voxels: their bin totals (the binning launched above)
+    const int64_t n_vox = hl.nb > 0 ? hl.nv : 0;
+    if (hl.nb > 0)
+        if (int rc = bin_voxels_finish(ctx, nbins, sv.units, sv.groups, sv.gu)) return rc;
     const size_t cell_set = (size_t)(Lp + 1) * K * sizeof(float2);
     const size_t moments_per_unit = (size_t)6 * K * sizeof(float2);
     // ---- device arena ----
     std::vector<char> h;
     const size_t oL = put(h, lmax.data(), lmax.size() * sizeof(int));
     const size_t oAb = put(h, ab.data(), ab.size() * sizeof(float2));
+    const size_t oCr = put(h, cr.data(), cr.size() * sizeof(float2));
     const size_t oNm = put(h, nmm.data(), nmm.size() * sizeof(float));
-    const size_t oR = put(h, rows.data(), rows.size() * sizeof(int2));
     const size_t oNo = put(h, nodes, sizeof nodes);
     const size_t oVi = put(h, vinv, sizeof vinv);
     size_t oP[2], oU[2], oG[2], oGu[2];
@@ -368,6 +410,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         a.nbins = nbins;
         a.delta = delta;
         a.ab = reinterpret_cast<const float2*>(base + oAb);
+        a.cr = reinterpret_cast<const float2*>(base + oCr);
         a.nmm = reinterpret_cast<const float*>(base + oNm);
         a.T = tb.T;
         a.lmax = d_lmax;
@@ -379,8 +422,6 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
     }
     dpx::HarmonicSynth y{};
-    y.rows = reinterpret_cast<const int2*>(base + oR);
-    y.n_rows = (int)rows.size();
     y.Ca = Ca;
     y.Cv = Cv;
     y.K = K;

@@ -110,7 +110,8 @@ struct dpx_ctx_s {
     double stage_points = 0, stage_k = 0;
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
-    dpxh::HostPinned pin_boxes, pin_plan;  // the harmonic fill's host staging
+    dpxh::HostPinned pin_plan, pin_totals, pin_small;  // the harmonic fill's host staging
+    std::vector<dpxh::DevBuf> leaf_boxes;  // the harmonic fill's solvent boxes, per leaf of a batch
     std::vector<char> host_stage;
 };
 
@@ -181,12 +182,21 @@ dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* db
 // Harmonic (multipole) FP32 fill of a staged leaf (dpx_harmonic_host.cpp).
 // harmonic_accepts decides before the staging: boxes need their voxel step,
 // and the expansion order and the radial bins must stay within the kernels'
-// limits (device atoms are copied to `host_atoms` to measure them).  *R
-// receives the radius of the point sets about the leaf's centre.
-bool harmonic_accepts(dpx_ctx ctx, const dpx_pdb_desc& d, const dpx::Geom& G, std::vector<float>& host_atoms,
-                      double* R, int* status);
+// limits (device atoms are copied to `host_atoms` to measure them).  It
+// stages the leaf's solvent boxes on the device (context buffer `slot`:
+// centred, counted) and fills `hl`: the radius of the point sets about the
+// leaf's centre, the voxel total and the staged arrays harmonic_fill bins.
+struct HarmLeaf {
+    double R = 0.0;
+    int64_t nb = 0, nv = 0;
+    const float4* boxes = nullptr;
+    const int64_t* counts = nullptr;
+    int64_t* vstart = nullptr;
+};
+bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::Geom& G,
+                      std::vector<float>& host_atoms, HarmLeaf& hl, int* status);
 int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid, const std::vector<float>& host_atoms, double R);
+                  void* grid, const std::vector<float>& host_atoms, const HarmLeaf& hl);
 // The FP64 fill launch of a staged leaf.
 cudaError_t launch_leaf_f64(cudaStream_t s, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase,
                             const dpx::Geom& G, void* grid);

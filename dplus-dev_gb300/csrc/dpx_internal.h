@@ -162,6 +162,7 @@ struct HarmonicSet {
     int LM, K, Lp, nbins;
     double delta;
     const float2* ab;       // [K] Legendre recurrence coefficients
+    const float2* cr;       // [K] scaled recurrence: {c_lm, r_lm} (hm_moments)
     const float* nmm;       // [LM+1] Pbar_mm = nmm[m] (-sin theta)^m
     const float* T;
     const int* lmax;
@@ -171,8 +172,6 @@ struct HarmonicSet {
     cudaEvent_t ev0, ev1;   // recorded around the moments launch when not null
 };
 struct HarmonicSynth {
-    const int2* rows;       // (i, t) of every theta row t <= 3i/2, i >= 1
-    int n_rows;
     const float2* Ca;       // [Lp+1][K] atoms
     const float2* Cv;       // [Lp+1][K] voxels or nullptr
     int K, Lp, lmax_host_outer;
@@ -191,9 +190,21 @@ int harmonic_max_l();
 int harmonic_nodes();
 int harmonic_max_bins();
 // Solvent boxes expanded into voxels and sorted by radius bin on the device.
+// A leaf's raw solvent boxes staged on the device: centred, counted, and R.
+struct VoxelPrepArgs {
+    const float* raw;       // [8 nb] D+ box records
+    int64_t nb;
+    double cx, cy, cz;      // the leaf's centre
+    float vs;               // voxel edge (nm)
+    float4* boxes;          // out [2 nb] {centre - c, w}, {L, 0}
+    int64_t* counts;        // out [nb] voxels per box
+    unsigned long long* scal;  // out {bits of the largest squared corner distance (FP32), total voxels}
+};
+cudaError_t launch_voxel_prepare(cudaStream_t s, const VoxelPrepArgs& a);
 struct VoxelBinArgs {
     const float4* boxes;    // [2 nb] {cx, cy, cz, w} about the centre, {Lx, Ly, Lz, 0}
-    const int64_t* vstart;  // [nb] first voxel of each box
+    const int64_t* counts;  // [nb] voxels per box
+    int64_t* vstart;        // [nb] first voxel of each box (written)
     int64_t nb, nv;
     float vs, delta;        // voxel edge, bin width (nm)
     int nbins;
