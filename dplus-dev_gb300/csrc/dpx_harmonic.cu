@@ -618,51 +618,71 @@ __global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// hm_contract: block (k slice of 128, tile of 8 shells); thread k.
-// groups[g] = {bin, ion (< 0: factor 1)}; C[i][k] = sum_g F sum_n T M,
-// summed across groups with compensation.
+// hm_contract: block (k slice of 32, tile of 8 shells), four warps; lane k,
+// warp w sums the groups [w G / 4, (w + 1) G / 4) (compensated), and the four
+// partial sums are combined in a fixed order with the same compensation.
+// groups[g] = {bin, ion (< 0: factor 1)}; C[i][k] = sum_g F sum_n T M.
 // ---------------------------------------------------------------------------
 constexpr int kContractShells = 8;
+constexpr int kContractK = 32;
+constexpr int kContractWarps = 4;
 
-__global__ void __launch_bounds__(128) hm_contract(const float2* __restrict__ M, const int2* __restrict__ groups, int G,
-                                                   const float* __restrict__ T, int nbins, int LM, int K, int Lp,
-                                                   const int* __restrict__ lmax, const float* __restrict__ aff,
-                                                   float2* __restrict__ C) {
-    const int k = blockIdx.x * 128 + threadIdx.x;
+__global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract(
+    const float2* __restrict__ M, const int2* __restrict__ groups, int G, const float* __restrict__ T, int nbins,
+    int LM, int K, int Lp, const int* __restrict__ lmax, const float* __restrict__ aff, float2* __restrict__ C) {
+    __shared__ float4 part[kContractWarps][kContractShells][kContractK];  // {s_re, c_re, s_im, c_im}
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int k = blockIdx.x * kContractK + lane;
     const int i0 = 1 + blockIdx.y * kContractShells;
-    if (k >= K) return;
-    const int l = l_of(k);
+    const bool kok = k < K;
+    const int l = kok ? l_of(k) : 0;
     float cr[kContractShells], ci[kContractShells], er[kContractShells], ei[kContractShells];
 #pragma unroll
     for (int a = 0; a < kContractShells; ++a) cr[a] = ci[a] = er[a] = ei[a] = 0.f;
-    for (int g = 0; g < G; ++g) {
-        const int2 gb = groups[g];
-        float2 mv[kNodes];
+    const int g0 = (int)((int64_t)G * w / kContractWarps), g1 = (int)((int64_t)G * (w + 1) / kContractWarps);
+    if (kok) {
+        for (int g = g0; g < g1; ++g) {
+            const int2 gb = groups[g];
+            float2 mv[kNodes];
 #pragma unroll
-        for (int n = 0; n < kNodes; ++n) mv[n] = M[((int64_t)g * kNodes + n) * K + k];
+            for (int n = 0; n < kNodes; ++n) mv[n] = M[((int64_t)g * kNodes + n) * K + k];
 #pragma unroll
-        for (int a = 0; a < kContractShells; ++a) {
-            const int i = i0 + a;
-            if (i > Lp || lmax[i] < l) continue;
-            const float4* t4 = reinterpret_cast<const float4*>(T + (((int64_t)i * nbins + gb.x) * (LM + 1) + l) * 8);
-            const float4 ta = t4[0], tb = t4[1];
-            const float t[kNodes] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y};
-            float sr = 0.f, si = 0.f;
+            for (int a = 0; a < kContractShells; ++a) {
+                const int i = i0 + a;
+                if (i > Lp || lmax[i] < l) continue;
+                const float4* t4 = reinterpret_cast<const float4*>(T + (((int64_t)i * nbins + gb.x) * (LM + 1) + l) * 8);
+                const float4 ta = t4[0], tb = t4[1];
+                const float t[kNodes] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y};
+                float sr = 0.f, si = 0.f;
 #pragma unroll
-            for (int n = 0; n < kNodes; ++n) {
-                sr = fmaf(t[n], mv[n].x, sr);
-                si = fmaf(t[n], mv[n].y, si);
+                for (int n = 0; n < kNodes; ++n) {
+                    sr = fmaf(t[n], mv[n].x, sr);
+                    si = fmaf(t[n], mv[n].y, si);
+                }
+                const float f = gb.y < 0 ? 1.f : aff[(int64_t)gb.y * (Lp + 1) + i];
+                sum2(cr[a], er[a], __fmul_rn(f, sr));
+                sum2(ci[a], ei[a], __fmul_rn(f, si));
             }
-            const float f = gb.y < 0 ? 1.f : aff[(int64_t)gb.y * (Lp + 1) + i];
-            sum2(cr[a], er[a], f * sr);
-            sum2(ci[a], ei[a], f * si);
         }
     }
 #pragma unroll
-    for (int a = 0; a < kContractShells; ++a) {
-        const int i = i0 + a;
-        if (i > Lp) continue;
-        C[(int64_t)i * K + k] = make_float2(cr[a] + er[a], ci[a] + ei[a]);
+    for (int a = 0; a < kContractShells; ++a) part[w][a][lane] = make_float4(cr[a], er[a], ci[a], ei[a]);
+    __syncthreads();
+    // warp a' < kContractShells / ... : thread (shell a, lane) combines the four warps
+    for (int e = threadIdx.x; e < kContractShells * kContractK; e += blockDim.x) {
+        const int a = e / kContractK, kl = e % kContractK;
+        const int i = i0 + a, kk = blockIdx.x * kContractK + kl;
+        if (i > Lp || kk >= K) continue;
+        float sr = 0.f, srr = 0.f, si = 0.f, sii = 0.f;
+#pragma unroll
+        for (int ww = 0; ww < kContractWarps; ++ww) {
+            const float4 p = part[ww][a][kl];
+            sum2(sr, srr, p.x);
+            srr += p.y;
+            sum2(si, sii, p.z);
+            sii += p.w;
+        }
+        C[(int64_t)i * K + kk] = make_float2(sr + srr, si + sii);
     }
 }
 
@@ -673,21 +693,29 @@ __device__ __forceinline__ float sinc_h(float h) {
 }
 
 // ---------------------------------------------------------------------------
-// hm_synth: one block per theta row (i, t <= 3i/2), shell-major.
-// The row's 6i cells are F(p) = sum_{|m| <= l_i} G_m w^{mp}, w = e^{2 pi i/6i},
-// with G_m = 4 pi sum_l i^l P_lm C_lm and G_-m = 4 pi sum_l i^l P_lm conj(C_lm)
-// (m > 0).  Writing p = s i + j (sextant s < 6, column j < i):
-//   F(s i + j) = sum_{r < 6} e^{2 pi i r s / 6} D_r(j),
-//   D_r(j) = sum_{m = r mod 6} G_m w^{mj},
-// so a thread per column j sums the G_m once into six residue classes and
-// finishes its six cells with a 6-point DFT.  The row's phi-spline
-// derivatives (row_spline, as the spline pass computes them) are written with
-// the values; the Friedel mirror row gets the conjugates of both.
-// Dynamic shared memory: P column values [K_i], G (atoms, voxels) over
-// m in [m0, m0 + nG) with zero padding (m0 = -6 ceil(l_i/6)), the 6i roots
-// of unity, the row's 6i values.
+// hm_synth: block (row group, shell i): up to kSynthRows theta rows t <= 3i/2
+// of one shell.  A row's 6i cells are F(p) = sum_{|m| <= l_i} G_m w^{mp},
+// w = e^{2 pi i/6i}, with G_m = 4 pi sum_l i^l P_lm C_lm and
+// G_-m = 4 pi sum_l i^l P_lm conj(C_lm) (m > 0).
+//   G stage: a warp takes four orders m x eight rows (lane = m, row), runs the
+//   Legendre recurrence of its (m, row) in registers and sums against the
+//   shell's C_lm (the eight lanes of an order read one address, a warp one
+//   32-byte sector); the quartets are dealt to the warps from both ends.
+//   Cell stage: writing p = s i + j (sextant s < 6, column j < i),
+//     F(s i + j) = sum_{r < 6} e^{2 pi i r s / 6} D_r(j),
+//     D_r(j) = sum_{m = r mod 6} G_m w^{mj},
+//   so a thread per (row, column j) sums the G_m once into six residue
+//   classes and finishes its six cells with a 6-point DFT; as many rows run at
+//   once as 256 threads have columns for.  Then the voxel form factor, the
+//   centring phase (double-float), and the rows' phi-spline derivatives
+//   (row_spline, as the spline pass computes them) written with the values;
+//   the Friedel mirror row gets the conjugates of both.
+// Dynamic shared memory: G (atoms, voxels) per row over m in [m0, m0 + nG)
+// with zero padding (m0 = -6 ceil(l_i/6)), the 6i roots of unity, the values
+// of the rows in flight (6 max(256, Lp) cells).
 // ---------------------------------------------------------------------------
-constexpr int kSynthThreads = 128;
+constexpr int kSynthThreads = 256;
+constexpr int kSynthRows = 8;
 
 __device__ __forceinline__ int synth_pad(int li) { return 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6); }
 
@@ -706,9 +734,6 @@ __device__ __forceinline__ float2 split_ff(double x) {
     return make_float2(hi, (float)(x - (double)hi));
 }
 
-// Rows of shells 1..n: S(n) = sum_{j <= n} (floor(3j/2) + 1) = n(n+1)/2 + floor(n/2) ceil(n/2) + n.
-__device__ __forceinline__ int rows_through(int n) { return n * (n + 1) / 2 + (n / 2) * ((n + 1) / 2) + n; }
-
 __global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* __restrict__ Ca,
                                                           const float2* __restrict__ Cv, int K,
                                                           const int* __restrict__ lmax, const float2* __restrict__ ab,
@@ -716,184 +741,208 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* 
                                                           double cx, double cy, double cz, int use_center, float scale,
                                                           double origin, float4* __restrict__ grid) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ float2 sRow[3];
-    // block -> (shell i, row t): the smallest i with rows_through(i) > block
-    int lo = 1, hi = Lp;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (rows_through(mid) > (int)blockIdx.x) hi = mid;
-        else lo = mid + 1;
-    }
-    const int i = lo, t = (int)blockIdx.x - rows_through(i - 1);
+    __shared__ float2 sRow[kSynthRows][4];  // per row: {st, ct}, A, B, Z (double-float)
+    const int i = blockIdx.y + 1;
+    const int h = 3 * i, nph = 6 * i;
+    const int rows_i = h / 2 + 1;  // rows t = 0 .. floor(3i/2)
+    const int t0 = blockIdx.x * kSynthRows;
+    if (t0 >= rows_i) return;
+    const int nr = min(kSynthRows, rows_i - t0);
     const int li = lmax[i];
-    const int Ki = k_of(li, li) + 1;
-    const int nph = 6 * i, h = 3 * i;
     const int nG = synth_pad(li);
-    const int m0 = -6 * ((li + 5) / 6);
+    const int m0p = -6 * ((li + 5) / 6);
     const bool vox = Cv != nullptr;
-    float* sP = reinterpret_cast<float*>(smem);
-    float2* sG = reinterpret_cast<float2*>(smem + ((size_t)Ki * 4 + 15) / 16 * 16);
-    float2* sGv = sG + nG;
-    float2* sW = sGv + nG;
-    float2* sF = sW + nph;
-    float st, ct;
-    sincospif((float)t / (float)h, &st, &ct);
-    // Legendre column m per thread
-    for (int m = threadIdx.x; m <= li; m += blockDim.x) {
-        float pmm = nmm[m];
-        for (int mm = 0; mm < m; ++mm) pmm *= -st;
-        float p2 = 0.f, p1 = pmm;
-        sP[k_of(m, m)] = p1;
-        for (int l = m + 1; l <= li; ++l) {
-            const float2 c = ab[k_of(l, m)];
-            const float p0 = c.x * fmaf(ct, p1, -c.y * p2);
-            sP[k_of(l, m)] = p0;
-            p2 = p1;
-            p1 = p0;
-        }
-    }
-    for (int n = threadIdx.x; n < nph; n += blockDim.x) {
+    float2* sG = reinterpret_cast<float2*>(smem);      // [row][2][nG]
+    float2* sW = sG + (size_t)kSynthRows * 2 * nG;     // [6i]
+    float2* sF = sW + nph;                              // [6 max(256, Lp)]
+    const int tid = threadIdx.x;
+    for (int n = tid; n < nph; n += blockDim.x) {
         float sw, cw;
         sincospif(2.f * (float)n / (float)nph, &sw, &cw);
         sW[n] = make_float2(cw, sw);
     }
-    if (threadIdx.x == 0) {
+    for (int e = tid; e < nr * 2 * nG; e += blockDim.x) {  // the padding beyond |m| <= l_i
+        const int m = m0p + e % nG;
+        if (m > li || m < -li) sG[e] = make_float2(0.f, 0.f);
+    }
+    const float qI = (float)((double)i * step);
+    if (tid < nr) {
+        const int t = t0 + tid;
+        float st, ct;
+        sincospif((float)t / (float)h, &st, &ct);
+        sRow[tid][0] = make_float2(st, ct);
+        // centring phase q.c / 2 pi = A cos(phi) + B sin(phi) + Z per cell, the
+        // row constants in FP64, held as FP32 pairs
         const double inv2pi = 0.15915494309189533577;
         double sd, cd;
         sincospi((double)t / (double)h, &sd, &cd);
         const double qd = (double)i * step;
-        sRow[0] = split_ff(qd * sd * cx * inv2pi);
-        sRow[1] = split_ff(qd * sd * cy * inv2pi);
-        sRow[2] = split_ff(qd * cd * cz * inv2pi);
-    }
-    for (int n = threadIdx.x; n < nG; n += blockDim.x) {  // the padding beyond |m| <= l_i
-        const int m = m0 + n;
-        if (m > li || m < -li) {
-            sG[n] = make_float2(0.f, 0.f);
-            sGv[n] = make_float2(0.f, 0.f);
-        }
+        sRow[tid][1] = split_ff(qd * sd * cx * inv2pi);
+        sRow[tid][2] = split_ff(qd * sd * cy * inv2pi);
+        sRow[tid][3] = split_ff(qd * cd * cz * inv2pi);
     }
     __syncthreads();
-    const float2* Cai = Ca + (int64_t)i * K;
-    const float2* Cvi = vox ? Cv + (int64_t)i * K : nullptr;
-    for (int m = threadIdx.x; m <= li; m += blockDim.x) {
-        float br = 0.f, bi = 0.f, pr = 0.f, pi_ = 0.f;
-        float vr = 0.f, vi = 0.f, qr = 0.f, qi = 0.f;
-        for (int l = m; l <= li; ++l) {
-            const int k = k_of(l, m);
-            const float p = sP[k];
-            const float2 c = Cai[k];
-            const float2 a = i_pow_times(l, c), e = i_pow_times(l, make_float2(c.x, -c.y));
-            br = fmaf(p, a.x, br);
-            bi = fmaf(p, a.y, bi);
-            pr = fmaf(p, e.x, pr);
-            pi_ = fmaf(p, e.y, pi_);
-            if (vox) {
-                const float2 d = Cvi[k];
-                const float2 av = i_pow_times(l, d), ev = i_pow_times(l, make_float2(d.x, -d.y));
-                vr = fmaf(p, av.x, vr);
-                vi = fmaf(p, av.y, vi);
-                qr = fmaf(p, ev.x, qr);
-                qi = fmaf(p, ev.y, qi);
+    // ---- G stage ----
+    {
+        const int warp = tid >> 5, lane = tid & 31;
+        const int mq = lane >> 3, r = lane & 7;  // order 4q + mq, row t0 + r
+        const int nq = (li + 4) / 4;
+        const float2 sc = sRow[min(r, nr - 1)][0];
+        const float st = sc.x, ct = sc.y;
+        const float2* Cai = Ca + (int64_t)i * K;
+        const float2* Cvi = vox ? Cv + (int64_t)i * K : nullptr;
+        for (int o = warp; o < nq; o += kSynthThreads / 32) {
+            const int q = (o & 1) ? nq - 1 - (o >> 1) : (o >> 1);  // 0, nq-1, 1, nq-2, ...
+            const int m = 4 * q + mq;
+            const bool ok = m <= li && r < nr;
+            // Pbar_mm = nmm[m] (-sin theta)^m by binary powering
+            float pmm = ok ? nmm[m] : 0.f, base = -st;
+            for (int e = ok ? m : 0; e > 0; e >>= 1) {
+                if (e & 1) pmm *= base;
+                base *= base;
+            }
+            float p1 = 0.f, p2 = 0.f;
+            float br = 0.f, bi = 0.f, pr = 0.f, pi_ = 0.f, vr = 0.f, vi = 0.f, qr = 0.f, qi = 0.f;
+            int k = ok ? m * (m + 1) / 2 + m : 0;  // k(l, m) from l = m
+            for (int l = 4 * q; l <= li; ++l) {
+                float p = 0.f;
+                if (ok && l >= m) {
+                    if (l == m) {
+                        p = pmm;
+                    } else {
+                        const float2 c = __ldg(&ab[k]);
+                        p = c.x * fmaf(ct, p1, -c.y * p2);
+                    }
+                    const float2 cA = __ldg(&Cai[k]);
+                    const float2 a = i_pow_times(l, cA), e = i_pow_times(l, make_float2(cA.x, -cA.y));
+                    br = fmaf(p, a.x, br);
+                    bi = fmaf(p, a.y, bi);
+                    pr = fmaf(p, e.x, pr);
+                    pi_ = fmaf(p, e.y, pi_);
+                    if (vox) {
+                        const float2 cV = __ldg(&Cvi[k]);
+                        const float2 av = i_pow_times(l, cV), ev = i_pow_times(l, make_float2(cV.x, -cV.y));
+                        vr = fmaf(p, av.x, vr);
+                        vi = fmaf(p, av.y, vi);
+                        qr = fmaf(p, ev.x, qr);
+                        qi = fmaf(p, ev.y, qi);
+                    }
+                    p2 = p1;
+                    p1 = p;
+                    k += l + 1;  // k(l + 1, m)
+                }
+            }
+            if (ok) {
+                float2* g = sG + (size_t)r * 2 * nG;
+                g[m - m0p] = make_float2(kFourPi * br, kFourPi * bi);
+                if (m > 0) g[-m - m0p] = make_float2(kFourPi * pr, kFourPi * pi_);
+                if (vox) {
+                    g[nG + m - m0p] = make_float2(kFourPi * vr, kFourPi * vi);
+                    if (m > 0) g[nG - m - m0p] = make_float2(kFourPi * qr, kFourPi * qi);
+                }
             }
         }
-        sG[m - m0] = make_float2(kFourPi * br, kFourPi * bi);
-        if (m > 0) sG[-m - m0] = make_float2(kFourPi * pr, kFourPi * pi_);
-        if (vox) {
-            sGv[m - m0] = make_float2(kFourPi * vr, kFourPi * vi);
-            if (m > 0) sGv[-m - m0] = make_float2(kFourPi * qr, kFourPi * qi);
-        }
     }
     __syncthreads();
-    const float qI = (float)((double)i * step);
+    // ---- cell stage: rpp rows at a time ----
     const int64_t base = shell_base(i);
-    // centring phase q.c / 2 pi = A cos(phi) + B sin(phi) + Z per cell, the
-    // row constants A, B, Z in FP64 (set before the barrier above), held as
-    // FP32 pairs
-    const float2 A2 = sRow[0], B2 = sRow[1], Z2 = sRow[2];
     constexpr float kS3 = 0.86602540378443865f;  // sin(pi/3)
     const float wr6[6] = {1.f, 0.5f, -0.5f, -1.f, -0.5f, 0.5f};
     const float wi6[6] = {0.f, kS3, kS3, 0.f, -kS3, -kS3};
-    for (int j = threadIdx.x; j < i; j += blockDim.x) {
-        float2 D[6], Dv[6];
+    const int rpp = max(1, min(nr, kSynthThreads / i));
+    for (int r0 = 0; r0 < nr; r0 += rpp) {
+        const int nrp = min(rpp, nr - r0);
+        for (int it = tid; it < nrp * i; it += blockDim.x) {
+            const int rr = it / i, j = it - rr * i;
+            const int r = r0 + rr;
+            const float2* gA = sG + (size_t)r * 2 * nG;
+            const float2* gV = gA + nG;
+            float2 D[6], Dv[6];
 #pragma unroll
-        for (int r = 0; r < 6; ++r) D[r] = Dv[r] = make_float2(0.f, 0.f);
-        int idx = (int)(((int64_t)m0 * j) % nph);
-        if (idx < 0) idx += nph;
-        for (int u = 0; u < nG; u += 6) {
+            for (int c = 0; c < 6; ++c) D[c] = Dv[c] = make_float2(0.f, 0.f);
+            int idx = (int)(((int64_t)m0p * j) % nph);
+            if (idx < 0) idx += nph;
+            for (int u = 0; u < nG; u += 6) {
 #pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const float2 w = sW[idx];
-                const float2 g = sG[u + r];
-                D[r].x = fmaf(g.x, w.x, fmaf(-g.y, w.y, D[r].x));
-                D[r].y = fmaf(g.x, w.y, fmaf(g.y, w.x, D[r].y));
-                if (vox) {
-                    const float2 gv = sGv[u + r];
-                    Dv[r].x = fmaf(gv.x, w.x, fmaf(-gv.y, w.y, Dv[r].x));
-                    Dv[r].y = fmaf(gv.x, w.y, fmaf(gv.y, w.x, Dv[r].y));
-                }
-                idx += j;  // idx, j < 6i
-                if (idx >= nph) idx -= nph;
-            }
-        }
-#pragma unroll
-        for (int sx = 0; sx < 6; ++sx) {
-            float ar = 0.f, ai = 0.f, vr = 0.f, vi = 0.f;
-#pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const int e = (r * sx) % 6;
-                ar += D[r].x * wr6[e] - D[r].y * wi6[e];
-                ai += D[r].x * wi6[e] + D[r].y * wr6[e];
-                if (vox) {
-                    vr += Dv[r].x * wr6[e] - Dv[r].y * wi6[e];
-                    vi += Dv[r].x * wi6[e] + Dv[r].y * wr6[e];
+                for (int c = 0; c < 6; ++c) {
+                    const float2 w = sW[idx];
+                    const float2 g = gA[u + c];
+                    D[c].x = fmaf(g.x, w.x, fmaf(-g.y, w.y, D[c].x));
+                    D[c].y = fmaf(g.x, w.y, fmaf(g.y, w.x, D[c].y));
+                    if (vox) {
+                        const float2 gv = gV[u + c];
+                        Dv[c].x = fmaf(gv.x, w.x, fmaf(-gv.y, w.y, Dv[c].x));
+                        Dv[c].y = fmaf(gv.x, w.y, fmaf(gv.y, w.x, Dv[c].y));
+                    }
+                    idx += j;  // idx, j < 6i
+                    if (idx >= nph) idx -= nph;
                 }
             }
-            const int p = sx * i + j;
-            const float2 w = sW[p];  // (cos, sin) of the cell's phi = p pi / 3i
-            const float cp = w.x, sp = w.y;
-            const float qx = qI * st * cp, qy = qI * st * sp, qz = qI * ct;
-            if (vox) {
-                const float f = vox_s * sinc_h(0.5f * qx * vox_s) * vox_s * sinc_h(0.5f * qy * vox_s) * vox_s *
-                                sinc_h(0.5f * qz * vox_s);
-                ar = fmaf(f, vr, ar);
-                ai = fmaf(f, vi, ai);
+            const float st = sRow[r][0].x, ct = sRow[r][0].y;
+            const float2 A2 = sRow[r][1], B2 = sRow[r][2], Z2 = sRow[r][3];
+#pragma unroll
+            for (int sx = 0; sx < 6; ++sx) {
+                float ar = 0.f, ai = 0.f, vr = 0.f, vi = 0.f;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    const int e = (c * sx) % 6;
+                    ar += D[c].x * wr6[e] - D[c].y * wi6[e];
+                    ai += D[c].x * wi6[e] + D[c].y * wr6[e];
+                    if (vox) {
+                        vr += Dv[c].x * wr6[e] - Dv[c].y * wi6[e];
+                        vi += Dv[c].x * wi6[e] + Dv[c].y * wr6[e];
+                    }
+                }
+                const int p = sx * i + j;
+                const float2 w = sW[p];  // (cos, sin) of the cell's phi = p pi / 3i
+                const float cp = w.x, sp = w.y;
+                const float qx = qI * st * cp, qy = qI * st * sp, qz = qI * ct;
+                if (vox) {
+                    const float f = vox_s * sinc_h(0.5f * qx * vox_s) * vox_s * sinc_h(0.5f * qy * vox_s) * vox_s *
+                                    sinc_h(0.5f * qz * vox_s);
+                    ar = fmaf(f, vr, ar);
+                    ai = fmaf(f, vi, ai);
+                }
+                float2 F = make_float2(ar * scale, ai * scale);
+                if (use_center) {
+                    // turns = A cp + B sp + Z in double-float (Dekker's two-product,
+                    // Knuth's two-sum), reduced by its nearest integer
+                    const float p1 = __fmul_rn(A2.x, cp), e1 = fmaf(A2.x, cp, -p1);
+                    const float p2 = __fmul_rn(B2.x, sp), e2 = fmaf(B2.x, sp, -p2);
+                    const float s1 = __fadd_rn(p1, p2);
+                    const float b1 = __fsub_rn(s1, p1);
+                    const float f1 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s1, b1)), __fsub_rn(p2, b1));
+                    const float s2 = __fadd_rn(s1, Z2.x);
+                    const float b2 = __fsub_rn(s2, s1);
+                    const float f2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(Z2.x, b2));
+                    const float lo = e1 + e2 + f1 + f2 + Z2.y + A2.y * cp + B2.y * sp;
+                    const float rt = __fsub_rn(s2, rintf(s2)) + lo;
+                    float s1n, c1n;
+                    sincospif(2.f * rt, &s1n, &c1n);
+                    F = make_float2(F.x * c1n - F.y * s1n, F.x * s1n + F.y * c1n);
+                }
+                sF[rr * nph + p] = F;
             }
-            float2 F = make_float2(ar * scale, ai * scale);
-            if (use_center) {
-                // turns = A cp + B sp + Z in double-float (Dekker's two-product,
-                // Knuth's two-sum), reduced by its nearest integer
-                const float p1 = __fmul_rn(A2.x, cp), e1 = fmaf(A2.x, cp, -p1);
-                const float p2 = __fmul_rn(B2.x, sp), e2 = fmaf(B2.x, sp, -p2);
-                const float s1 = __fadd_rn(p1, p2);
-                const float b1 = __fsub_rn(s1, p1);
-                const float f1 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s1, b1)), __fsub_rn(p2, b1));
-                const float s2 = __fadd_rn(s1, Z2.x);
-                const float b2 = __fsub_rn(s2, s1);
-                const float f2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(Z2.x, b2));
-                const float lo = e1 + e2 + f1 + f2 + Z2.y + A2.y * cp + B2.y * sp;
-                const float rt = __fsub_rn(s2, rintf(s2)) + lo;
-                float s1n, c1n;
-                sincospif(2.f * rt, &s1n, &c1n);
-                F = make_float2(F.x * c1n - F.y * s1n, F.x * s1n + F.y * c1n);
+        }
+        __syncthreads();
+        for (int it = tid; it < nrp * nph; it += blockDim.x) {
+            const int rr = it / nph, p = it - rr * nph;
+            const int t = t0 + r0 + rr;
+            const float2* row = sF + rr * nph;
+            const float2 F = row[p];
+            float dr, di;
+            row_spline<float, 14>(nph, p, [&](int k) { return row[k]; }, dr, di);
+            grid[base + (int64_t)t * nph + p] = make_float4(F.x, F.y, dr, di);
+            // Friedel: the antipode (3i - t, p + 3i) holds the conjugate (the
+            // equator row is its own mirror and is written once per cell)
+            if (2 * t != h) {
+                const int pm = p < h ? p + h : p - h;
+                grid[base + (int64_t)(h - t) * nph + pm] = make_float4(F.x, -F.y, dr, -di);
             }
-            sF[p] = F;
         }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int p = threadIdx.x; p < nph; p += blockDim.x) {
-        const float2 F = sF[p];
-        float dr, di;
-        row_spline<float, 14>(nph, p, [&](int k) { return sF[k]; }, dr, di);
-        grid[base + (int64_t)t * nph + p] = make_float4(F.x, F.y, dr, di);
-        // Friedel: the antipode (3i - t, p + 3i) holds the conjugate (the
-        // equator row is its own mirror and is written once per cell)
-        if (2 * t != h) {
-            const int pm = p < h ? p + h : p - h;
-            grid[base + (int64_t)(h - t) * nph + pm] = make_float4(F.x, -F.y, dr, -di);
-        }
-    }
-    if (i == 1 && t == 0 && threadIdx.x == 0) grid[0] = make_float4((float)origin, 0.f, 0.f, 0.f);
+    if (i == 1 && t0 == 0 && tid == 0) grid[0] = make_float4((float)origin, 0.f, 0.f, 0.f);
 }
 
 }  // namespace
@@ -932,7 +981,8 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C)
     }
     const int64_t ng = (int64_t)a.G * kNodes * a.K;
     hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.G, a.K, a.M);
-    hm_contract<<<dim3((a.K + 127) / 128, (a.Lp + kContractShells - 1) / kContractShells), 128, 0, s>>>(
+    hm_contract<<<dim3((a.K + kContractK - 1) / kContractK, (a.Lp + kContractShells - 1) / kContractShells),
+                  kContractK * kContractWarps, 0, s>>>(
         a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.aff, C);
     return cudaGetLastError();
 }
@@ -961,19 +1011,21 @@ cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
 }
 
 cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
-    // one launch; dynamic shared memory sized for the outermost shell
+    // one launch: blocks (row group, shell), dynamic shared memory sized for the outermost shell
     const int li = a.lmax_host_outer;
     const int nph = 6 * a.Lp;
     const int nG = 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6);
-    const size_t smem = ((size_t)((li + 1) * (li + 2) / 2) * 4 + 15) / 16 * 16 + (size_t)2 * nG * sizeof(float2) +
-                        (size_t)2 * nph * sizeof(float2);
+    // rows in flight: rpp x 6i cells with rpp x i <= 256, or one row of 6i > 1,536 cells
+    const size_t cells = (size_t)6 * (a.Lp > kSynthThreads ? a.Lp : kSynthThreads);
+    const size_t smem = ((size_t)kSynthRows * 2 * nG + (size_t)nph + cells) * sizeof(float2);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    const int n_rows = a.Lp * (a.Lp + 1) / 2 + (a.Lp / 2) * ((a.Lp + 1) / 2) + a.Lp;
-    hm_synth<<<n_rows, kSynthThreads, smem, s>>>(a.Lp, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step, a.vox_s, a.cx,
-                                                 a.cy, a.cz, a.use_center, a.scale, a.origin, a.grid);
+    const int groups = (3 * a.Lp / 2 + 1 + kSynthRows - 1) / kSynthRows;
+    hm_synth<<<dim3(groups, a.Lp), kSynthThreads, smem, s>>>(a.Lp, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step,
+                                                             a.vox_s, a.cx, a.cy, a.cz, a.use_center, a.scale,
+                                                             a.origin, a.grid);
     return cudaGetLastError();
 }
 
