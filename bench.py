@@ -343,7 +343,8 @@ def run_dpx(args):
                         "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 flops x max SM clock): "
                                      "no measured FP32 peak is on file",
                         "note": "flops = points (atoms + solvent voxels) x K x 6 moments x 4 (complex "
-                                "multiply-add); the fill also holds the synthesis and the radial tables",
+                                "multiply-add), K the mean over the points of the (l, m) their radial bins "
+                                "carry; the fill also holds the synthesis and the radial tables",
                         "points": n_pts, "K": kk,
                         "stage_ms": {"moments": mom_ms, "synthesis": syn_ms, "harmonic_fill": harm_ms},
                         "equivalent_direct_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)}

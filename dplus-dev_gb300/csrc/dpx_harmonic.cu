@@ -275,14 +275,17 @@ __device__ __forceinline__ void moment_order(int l, int m, bool col_ok, int kc, 
 }
 
 __global__ void __launch_bounds__(32) hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units,
-                                                 int LM, int K, float delta, const float2* __restrict__ cr,
-                                                 const float* __restrict__ nmm, float2* __restrict__ MP) {
+                                                 int K, float delta, const int* __restrict__ lmb,
+                                                 const float2* __restrict__ cr, const float* __restrict__ nmm,
+                                                 float2* __restrict__ MP) {
     extern __shared__ __align__(16) unsigned char smem[];
     float2* sD = reinterpret_cast<float2*>(smem);  // per quartet [(l - m0) * 24 + lane], lanes < 24
     const int lane = threadIdx.x;
     const int g = lane >> 2, t = lane & 3;
     const int4 un = units[blockIdx.x];
+    const int LM = lmb[un.z];    // the orders of the unit's bin
     const int Q = (LM + 4) / 4;  // quartets
+    if ((int)blockIdx.y >= (Q + 1) / 2) return;
     const int nq = (Q - 1 - (int)blockIdx.y > (int)blockIdx.y) ? 2 : 1;
     const int m0a = 4 * blockIdx.y, m0b = 4 * (Q - 1 - blockIdx.y);
     const int nla = LM - m0a + 1, nlb = nq == 2 ? LM - m0b + 1 : 0;
@@ -601,13 +604,18 @@ __device__ __forceinline__ void sum2(float& s, float& c, float x) {
 
 // hm_groups: M[g][n][k] = sum of MP over the units [gu[g], gu[g+1]) of group g,
 // compensated.
-__global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, int G, int K,
-                          float2* __restrict__ M) {
+__global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, const int2* __restrict__ groups,
+                          const int* __restrict__ lmb, int G, int K, float2* __restrict__ M) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t per = (int64_t)kNodes * K;
     if (e >= (int64_t)G * per) return;
     const int g = (int)(e / per);
     const int64_t r = e % per;
+    const int lb = lmb[groups[g].x];
+    if ((int)(r % K) >= (lb + 1) * (lb + 2) / 2) {  // orders the group's bin does not carry
+        M[e] = make_float2(0.f, 0.f);
+        return;
+    }
     float re = 0.f, rc = 0.f, im = 0.f, ic = 0.f;
     for (int u = gu[g]; u < gu[g + 1]; ++u) {
         const float2 v = MP[(int64_t)u * per + r];
@@ -629,7 +637,8 @@ constexpr int kContractWarps = 4;
 
 __global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract(
     const float2* __restrict__ M, const int2* __restrict__ groups, int G, const float* __restrict__ T, int nbins,
-    int LM, int K, int Lp, const int* __restrict__ lmax, const float* __restrict__ aff, float2* __restrict__ C) {
+    int LM, int K, int Lp, const int* __restrict__ lmax, const int* __restrict__ lmb, const float* __restrict__ aff,
+    float2* __restrict__ C) {
     __shared__ float4 part[kContractWarps][kContractShells][kContractK];  // {s_re, c_re, s_im, c_im}
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int k = blockIdx.x * kContractK + lane;
@@ -643,6 +652,7 @@ __global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract(
     if (kok) {
         for (int g = g0; g < g1; ++g) {
             const int2 gb = groups[g];
+            if (l > lmb[gb.x]) continue;  // zero moments: the bin needs no order l
             float2 mv[kNodes];
 #pragma unroll
             for (int n = 0; n < kNodes; ++n) mv[n] = M[((int64_t)g * kNodes + n) * K + k];
@@ -959,12 +969,13 @@ cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a) {
 }
 
 cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C) {
-    // one warp per (unit, quartet pair); the running sums of both quartets:
-    // (LM - 4y + 1) + (LM - 4(Q-1-y) + 1) = 2 LM + 6 - 4Q orders for a pair,
-    // LM + 1 for the single quartet of Q = 1
+    // one warp per (unit, quartet pair); the running sums of both quartets.  A
+    // unit of order L (its bin's, <= LM) holds (L - 4y + 1) + (L - 4(Q-1-y) + 1)
+    // = 2L + 6 - 4Q = L + 2 + (L mod 4) orders for a pair, L + 1 for the single
+    // quartet of Q = 1: at most LM + 5 whatever L.
     const int Q = (a.LM + 4) / 4;
     const int pairs = (Q + 1) / 2;
-    const int orders = Q >= 2 ? 2 * a.LM + 6 - 4 * Q : a.LM + 1;
+    const int orders = a.LM + 5;
     const size_t smem = (size_t)orders * 24 * sizeof(float2);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -974,16 +985,17 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C)
         cudaError_t e = cudaEventRecord(a.ev0, s);
         if (e != cudaSuccess) return e;
     }
-    hm_moments<<<dim3(a.n_units, pairs), 32, smem, s>>>(a.pts, a.units, a.LM, a.K, (float)a.delta, a.cr, a.nmm, a.MP);
+    hm_moments<<<dim3(a.n_units, pairs), 32, smem, s>>>(a.pts, a.units, a.K, (float)a.delta, a.lmb, a.cr, a.nmm,
+                                                       a.MP);
     if (a.ev1) {
         cudaError_t e = cudaEventRecord(a.ev1, s);
         if (e != cudaSuccess) return e;
     }
     const int64_t ng = (int64_t)a.G * kNodes * a.K;
-    hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.G, a.K, a.M);
+    hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.groups, a.lmb, a.G, a.K, a.M);
     hm_contract<<<dim3((a.K + kContractK - 1) / kContractK, (a.Lp + kContractShells - 1) / kContractShells),
                   kContractK * kContractWarps, 0, s>>>(
-        a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.aff, C);
+        a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.lmb, a.aff, C);
     return cudaGetLastError();
 }
 

@@ -254,42 +254,6 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
                 atoms[j] = make_float4((float)((double)src[4 * j] - sh[0]), (float)((double)src[4 * j + 1] - sh[1]),
                                        (float)((double)src[4 * j + 2] - sh[2]), (float)u);
     }
-    // ---- orders (R from harmonic_accepts: the atoms and the corners of the solvent boxes) ----
-    std::vector<int> lmax(Lp + 1, 0);
-    for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * R);
-    const int LM = lmax[Lp];
-    if (LM > dpx::harmonic_max_l()) return fail(DPX_ERR_ARG, "harmonic fill: order %d above %d", LM,
-                                                dpx::harmonic_max_l());
-    const int K = (LM + 1) * (LM + 2) / 2;
-    std::vector<float2> ab(K, make_float2(0.f, 0.f));
-    for (int m = 0; m <= LM; ++m)
-        for (int l = m + 1; l <= LM; ++l) {
-            const double a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
-            const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
-            ab[(size_t)l * (l + 1) / 2 + m] = make_float2((float)a, (float)b);
-        }
-    // the moments' scaled recurrence q_l = Pbar_lm / r_lm, r_lm = prod_{j=m+1..l} a_jm / 2:
-    // q_l = 2x q_{l-1} - c_lm q_{l-2}, c_lm = 4 b_lm / a_{l-1,m} (0 for l = m + 1)
-    std::vector<float2> cr(K, make_float2(0.f, 1.f));
-    for (int m = 0; m <= LM; ++m) {
-        double r = 1.0, a_prev = 0.0;
-        for (int l = m + 1; l <= LM; ++l) {
-            const double a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
-            const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
-            r *= 0.5 * a;
-            const double c = l >= m + 2 ? 4.0 * b / a_prev : 0.0;
-            cr[(size_t)l * (l + 1) / 2 + m] = make_float2((float)c, (float)r);
-            a_prev = a;
-        }
-    }
-    std::vector<float> nmm(LM + 1);  // Pbar_mm = nmm[m] (-sin theta)^m, orthonormal
-    {
-        double v = 0.28209479177387814347;  // 1 / sqrt(4 pi)
-        for (int m = 0; m <= LM; ++m) {
-            if (m > 0) v *= std::sqrt((2.0 * m + 1.0) / (2.0 * m));
-            nmm[m] = (float)v;
-        }
-    }
     // ---- the degree-5 interpolation of the radial bins on Chebyshev nodes ----
     double nodes[6], vinv[36];
     chebyshev_fit(nodes, vinv);
@@ -335,11 +299,57 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     const int64_t n_vox = hl.nb > 0 ? hl.nv : 0;
     if (hl.nb > 0)
         if (int rc = bin_voxels_finish(ctx, nbins, sv.units, sv.groups, sv.gu)) return rc;
+    // ---- orders.  R (harmonic_accepts) bounds the atoms and the corners of the
+    // solvent boxes; every point of bin b lies within (b + 1) delta, so the
+    // last occupied bin bounds them more tightly.  Bin b needs the orders
+    // l <= order_of(q_max (b + 1) delta) only. ----
+    int b_last = 0;
+    for (const Set* S : {&sa, &sv})
+        for (const int2& gb : S->groups) b_last = std::max(b_last, gb.x);
+    const double Reff = std::min(R, (b_last + 1) * delta * (1.0 + 1e-6));
+    std::vector<int> lmax(Lp + 1, 0);
+    for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * Reff);
+    const int LM = lmax[Lp];
+    if (LM > dpx::harmonic_max_l()) return fail(DPX_ERR_ARG, "harmonic fill: order %d above %d", LM,
+                                                dpx::harmonic_max_l());
+    const int K = (LM + 1) * (LM + 2) / 2;
+    std::vector<int> lmb(nbins);
+    for (int b = 0; b < nbins; ++b) lmb[b] = std::min(LM, order_of(Lp * G.step * (b + 1) * delta * (1.0 + 1e-6)));
+    std::vector<float2> ab(K, make_float2(0.f, 0.f));
+    for (int m = 0; m <= LM; ++m)
+        for (int l = m + 1; l <= LM; ++l) {
+            const double a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+            const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
+            ab[(size_t)l * (l + 1) / 2 + m] = make_float2((float)a, (float)b);
+        }
+    // the moments' scaled recurrence q_l = Pbar_lm / r_lm, r_lm = prod_{j=m+1..l} a_jm / 2:
+    // q_l = 2x q_{l-1} - c_lm q_{l-2}, c_lm = 4 b_lm / a_{l-1,m} (0 for l = m + 1)
+    std::vector<float2> cr(K, make_float2(0.f, 1.f));
+    for (int m = 0; m <= LM; ++m) {
+        double r = 1.0, a_prev = 0.0;
+        for (int l = m + 1; l <= LM; ++l) {
+            const double a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+            const double b = std::sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
+            r *= 0.5 * a;
+            const double c = l >= m + 2 ? 4.0 * b / a_prev : 0.0;
+            cr[(size_t)l * (l + 1) / 2 + m] = make_float2((float)c, (float)r);
+            a_prev = a;
+        }
+    }
+    std::vector<float> nmm(LM + 1);  // Pbar_mm = nmm[m] (-sin theta)^m, orthonormal
+    {
+        double v = 0.28209479177387814347;  // 1 / sqrt(4 pi)
+        for (int m = 0; m <= LM; ++m) {
+            if (m > 0) v *= std::sqrt((2.0 * m + 1.0) / (2.0 * m));
+            nmm[m] = (float)v;
+        }
+    }
     const size_t cell_set = (size_t)(Lp + 1) * K * sizeof(float2);
     const size_t moments_per_unit = (size_t)6 * K * sizeof(float2);
     // ---- device arena ----
     std::vector<char> h;
     const size_t oL = put(h, lmax.data(), lmax.size() * sizeof(int));
+    const size_t oLb = put(h, lmb.data(), lmb.size() * sizeof(int));
     const size_t oAb = put(h, ab.data(), ab.size() * sizeof(float2));
     const size_t oCr = put(h, cr.data(), cr.size() * sizeof(float2));
     const size_t oNm = put(h, nmm.data(), nmm.size() * sizeof(float));
@@ -370,8 +380,12 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     char* base = static_cast<char*>(ctx->harmonic.p);
     if (ev) {
         ctx->tev_used = n_vox ? 8 : 6;
+        // K per point as the moments compute it: its bin's (l_b + 1)(l_b + 2) / 2
+        double pk = 0.0;
+        for (const Set* S : {&sa, &sv})
+            for (const int4& u : S->units) pk += (double)u.y * (lmb[u.z] + 1) * (lmb[u.z] + 2) / 2;
         ctx->stage_points = (double)atoms.size() + (double)n_vox;
-        ctx->stage_k = K;
+        ctx->stage_k = ctx->stage_points > 0 ? pk / ctx->stage_points : 0.0;
     }
     char* hp = nullptr;
     DPX_CUDA(ctx->pin_plan.get(staged, &hp));
@@ -414,6 +428,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         a.nmm = reinterpret_cast<const float*>(base + oNm);
         a.T = tb.T;
         a.lmax = d_lmax;
+        a.lmb = reinterpret_cast<const int*>(base + oLb);
         a.aff = reinterpret_cast<const float*>(dbase + t.aff);
         a.MP = reinterpret_cast<float2*>(base + oMP);
         a.M = reinterpret_cast<float2*>(base + oM);

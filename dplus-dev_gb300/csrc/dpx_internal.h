@@ -166,6 +166,7 @@ struct HarmonicSet {
     const float* nmm;       // [LM+1] Pbar_mm = nmm[m] (-sin theta)^m
     const float* T;
     const int* lmax;
+    const int* lmb;         // [nbins] the orders a bin needs (<= LM)
     const float* aff;       // [U][Lp+1] ion form factors (atoms)
     float2* MP;             // [n_units][6][K]
     float2* M;              // [G][6][K]

@@ -92,7 +92,9 @@ int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns);
  * multipole expansion.  Per shell i the plane-wave expansion is cut at order
  * l_i = ceil(q_i R + 3 (q_i R)^(1/3) + 6) (R the largest point distance from
  * the centre); points are grouped by radius and their expansion coefficients
- * summed per group; each theta row is synthesized from the coefficients; solvent
+ * summed per group, a group of radial bin b to the order its largest radius
+ * needs (the same rule at q_max); each theta row is synthesized from the
+ * coefficients; solvent
  * boxes are expanded into their voxels (dpx_pdb_desc.voxel_step).  It serves
  * dpx_grid_fill_pdb and dpx_grid_fill_pdb_batch; leaves it cannot take (boxes
  * without a voxel step, orders above 175, more than 1024 radial bins of
@@ -105,8 +107,10 @@ int dpx_ctx_get_fill_method(dpx_ctx ctx);
 /* Stage timing of harmonic fills (no counterpart in the reference): with
  * timing on, the fill records CUDA events on the context's stream;
  * dpx_ctx_stage_times then gives out[5] = {ms of the moments kernels, ms of
- * the synthesis, ms of the whole harmonic fill, points (atoms + voxels), K}
- * of the last harmonic fill (zeros when there was none). */
+ * the synthesis, ms of the whole harmonic fill, points (atoms + voxels), the
+ * mean over the points of the (l, m) moments each one carries (its radial
+ * bin's (l_b + 1)(l_b + 2) / 2)} of the last harmonic fill (zeros when there
+ * was none). */
 int dpx_ctx_set_timing(dpx_ctx ctx, int on);
 int dpx_ctx_stage_times(dpx_ctx ctx, double* out);
 /* shape[4] = {cells_per_thread, threads, persistent, poly_columns} in use. */
