@@ -522,16 +522,38 @@ __global__ void __launch_bounds__(kBinThreads) vx_prepare(const float* __restric
     }
 }
 
-// vstart = exclusive prefix of the box voxel counts: one block, a contiguous
-// run of boxes per thread
-__global__ void __launch_bounds__(1024) vx_vstart(const int64_t* __restrict__ counts, int64_t nb,
-                                                  int64_t* __restrict__ vstart) {
-    const int64_t per = (nb + blockDim.x - 1) / blockDim.x;
-    const int64_t b0 = min(nb, (int64_t)threadIdx.x * per), b1 = min(nb, b0 + per);
+// vstart = exclusive prefix of the box voxel counts, over runs of
+// kVstartRun boxes: vx_run_sums gives each run's total; vx_vstart adds the
+// totals of the earlier runs and scans its own (kBinThreads threads, a
+// contiguous stretch of the run per thread).
+constexpr int kVstartRun = kVoxelScanRun;
+static_assert(kVstartRun % kBinThreads == 0, "a scan run is whole stretches of the block's threads");
+
+__global__ void __launch_bounds__(kBinThreads) vx_run_sums(const int64_t* __restrict__ counts, int64_t nb,
+                                                           int64_t* __restrict__ sums) {
+    const int64_t r0 = (int64_t)blockIdx.x * kVstartRun;
+    int64_t v = 0;
+    for (int k = threadIdx.x; k < kVstartRun; k += blockDim.x)
+        if (r0 + k < nb) v += counts[r0 + k];
+    int64_t all;
+    block_scan_excl(v, &all);
+    if (threadIdx.x == 0) sums[blockIdx.x] = all;
+}
+
+__global__ void __launch_bounds__(kBinThreads) vx_vstart(const int64_t* __restrict__ counts, int64_t nb,
+                                                         const int64_t* __restrict__ sums,
+                                                         int64_t* __restrict__ vstart) {
+    int64_t before = 0;
+    for (int k = threadIdx.x; k < (int)blockIdx.x; k += blockDim.x) before += sums[k];
+    int64_t start;
+    block_scan_excl(before, &start);
+    const int64_t r0 = (int64_t)blockIdx.x * kVstartRun;
+    const int per = kVstartRun / kBinThreads;
+    const int64_t b0 = min(nb, r0 + (int64_t)threadIdx.x * per), b1 = min(nb, b0 + per);
     int64_t mine = 0;
     for (int64_t b = b0; b < b1; ++b) mine += counts[b];
-    int64_t all;
-    int64_t run = block_scan_excl(mine, &all);
+    int64_t dummy;
+    int64_t run = start + block_scan_excl(mine, &dummy);
     for (int64_t b = b0; b < b1; ++b) {
         vstart[b] = run;
         run += counts[b];
@@ -1013,7 +1035,9 @@ cudaError_t launch_voxel_prepare(cudaStream_t s, const VoxelPrepArgs& a) {
 cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
     const int nblk = (int)((a.nv + kBinThreads - 1) / kBinThreads);
     if (a.nbins > kMaxBins) return cudaErrorInvalidValue;
-    vx_vstart<<<1, 1024, 0, s>>>(a.counts, a.nb, a.vstart);
+    const int runs = (int)((a.nb + kVstartRun - 1) / kVstartRun);
+    vx_run_sums<<<runs, kBinThreads, 0, s>>>(a.counts, a.nb, a.run_sums);
+    vx_vstart<<<runs, kBinThreads, 0, s>>>(a.counts, a.nb, a.run_sums, a.vstart);
     vx_expand<<<nblk, kBinThreads, 0, s>>>(a.boxes, a.vstart, a.nb, a.nv, a.vs, a.delta, a.nbins, a.tmp, a.vbin,
                                            a.hist, nblk);
     vx_totals<<<a.nbins, kBinThreads, 0, s>>>(a.hist, a.nbins, nblk, a.total);

@@ -87,6 +87,7 @@ int bin_voxels_launch(dpx_ctx ctx, const HarmLeaf& hl, double s, double delta, i
     a.boxes = hl.boxes;
     a.counts = hl.counts;
     a.vstart = hl.vstart;
+    a.run_sums = hl.run_sums;
     a.nb = nb;
     a.nv = nv;
     a.vs = (float)s;
@@ -173,7 +174,8 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
         const size_t oBox = al16((size_t)8 * nb * sizeof(float));
         const size_t oCnt = al16(oBox + (size_t)2 * nb * sizeof(float4));
         const size_t oVs = al16(oCnt + (size_t)nb * sizeof(int64_t));
-        const size_t oSc = al16(oVs + (size_t)nb * sizeof(int64_t));
+        const size_t oRs = al16(oVs + (size_t)nb * sizeof(int64_t));
+        const size_t oSc = al16(oRs + (size_t)((nb + dpx::kVoxelScanRun - 1) / dpx::kVoxelScanRun) * sizeof(int64_t));
         cudaError_t e = B.reserve(oSc + 2 * sizeof(unsigned long long));
         char* base = static_cast<char*>(B.p);
         cudaStream_t st = ctx->stream;
@@ -209,6 +211,7 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
         hl.boxes = a.boxes;
         hl.counts = a.counts;
         hl.vstart = reinterpret_cast<int64_t*>(base + oVs);
+        hl.run_sums = reinterpret_cast<int64_t*>(base + oRs);
     }
     // the fill's points are rounded to FP32 about the centre: a relative margin
     const double R = std::sqrt(r2) * (1.0 + 1e-6);

@@ -192,6 +192,7 @@ struct HarmLeaf {
     const float4* boxes = nullptr;
     const int64_t* counts = nullptr;
     int64_t* vstart = nullptr;
+    int64_t* run_sums = nullptr;
 };
 bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::Geom& G,
                       std::vector<float>& host_atoms, HarmLeaf& hl, int* status);

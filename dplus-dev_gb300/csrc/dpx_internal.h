@@ -191,6 +191,9 @@ int harmonic_max_l();
 int harmonic_nodes();
 int harmonic_max_bins();
 // Solvent boxes expanded into voxels and sorted by radius bin on the device.
+// Boxes per run of the voxel-start scan (launch_voxel_bins); VoxelBinArgs::run_sums
+// holds ceil(nb / kVoxelScanRun) entries.
+constexpr int kVoxelScanRun = 1024;
 // A leaf's raw solvent boxes staged on the device: centred, counted, and R.
 struct VoxelPrepArgs {
     const float* raw;       // [8 nb] D+ box records
@@ -206,6 +209,7 @@ struct VoxelBinArgs {
     const float4* boxes;    // [2 nb] {cx, cy, cz, w} about the centre, {Lx, Ly, Lz, 0}
     const int64_t* counts;  // [nb] voxels per box
     int64_t* vstart;        // [nb] first voxel of each box (written)
+    int64_t* run_sums;      // [ceil(nb / kVoxelScanRun)] scratch of the vstart scan
     int64_t nb, nv;
     float vs, delta;        // voxel edge, bin width (nm)
     int nbins;
