@@ -136,9 +136,14 @@ def fill_launches(ctx, n_boxes):
     return 1 + 1
 
 
+# one average: the angular order of the directions (keys, totals, offsets,
+# scatter: eps = 0 and one direction set), bracket tables, average, finalize
+AVERAGE_LAUNCHES = 4 + 3
+
+
 def launches_per_solve(ctx, n_boxes):
-    """One solve: the fill and the average (bracket tables, average, finalize)."""
-    return fill_launches(ctx, n_boxes) + 3
+    """One solve: the fill and the average."""
+    return fill_launches(ctx, n_boxes) + AVERAGE_LAUNCHES
 
 
 def shape_label(shape) -> str:
@@ -608,8 +613,8 @@ def run_assembly(args):
         "e2e": {"value": 2 * world / e2e_s, "unit": "solves/s",
                 "h2d_bytes_per_step": int(2 * dirs.nbytes + 16 * len(xyz) + 48 * (60 + 1300)),
                 "d2h_bytes_per_step": int(2 * Q.nbytes)},
-        # the subunit fill, then two averages of 3 launches (bracket tables, average, finalize)
-        "gpu_launches": (fill_launches(ctx, 0) + 2 * 3) * args.steps,
+        # the subunit fill, then two averages
+        "gpu_launches": (fill_launches(ctx, 0) + 2 * AVERAGE_LAUNCHES) * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_extras:
@@ -721,8 +726,8 @@ def run_serve(args):
                 "h2d_bytes_per_step": int(sum(16 * len(r.leaf.xyz) + (0 if r.copies is None else 48 * len(r.copies[1]))
                                               for r in stream)),
                 "d2h_bytes_per_step": int(sum(r.Q.nbytes for r in stream))},
-        # per grid: its splines (+1); per request: bracket tables, average, finalize, I(0)
-        "gpu_launches": int(st["fill_launches"] + 2 * st["grid_fills"] + 4 * st["completed"]),
+        # per grid: its splines (+1); per request: the average and I(0)
+        "gpu_launches": int(st["fill_launches"] + 2 * st["grid_fills"] + (AVERAGE_LAUNCHES + 1) * st["completed"]),
         "server": st, "generation_s": gen_s, "clocks": clk.summary(),
     }
     if args.fp64_sample > 0 and rank == 0:

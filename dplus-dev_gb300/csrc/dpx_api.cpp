@@ -198,7 +198,7 @@ void ctx_release(dpx_ctx ctx) {
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
-                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels})
+                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels, &ctx->dirsort})
         b->release();
     for (DevBuf& b : ctx->leaf_boxes) b.release();
     ctx->pin_plan.release();
@@ -883,6 +883,11 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
     const size_t part = ((size_t)nbr * plan.n_chunks + (size_t)nbr * 5) * max_q * sizeof(double) + 64;
     DPX_CUDA(ctx->partial.reserve(part));
     plan.partial = (double*)ctx->partial.p;
+    // eps = 0 with one direction set: the samples in angular order (the same mean)
+    if (eps == 0.0 && dir_layer_stride == 0) {
+        DPX_CUDA(ctx->dirsort.reserve(dpx::dir_sort_bytes(n_samples)));
+        plan.sort_scratch = (int*)ctx->dirsort.p;
+    }
     DPX_CUDA(ctx->result.reserve((size_t)nq * sizeof(double)));
     DPX_CUDA(cudaMemcpyAsync(ctx->plan.p, stage.data(), o, cudaMemcpyHostToDevice, s));
     DPX_CUDA(cudaMemcpyAsync(ctx->groups.p, gstage.data(), gstage.size(), cudaMemcpyHostToDevice, s));

@@ -202,7 +202,11 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     int rc = DPX_OK;
     cudaError_t e = cudaMalloc(&b->arena, st.h.size());
     if (e == cudaSuccess) e = cudaMalloc(&b->pool, b->pool_bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->partial, partial_max);
+    // with eps = 0 the averages take the shared directions in angular order (one
+    // sort scratch behind the partial sums, used by one average at a time)
+    const size_t sort_off = al16(partial_max);
+    const size_t sort_bytes = eps == 0.0 ? dpx::dir_sort_bytes(n_samples) : 0;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->partial, sort_off + sort_bytes);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_res, b->res_total * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_res, b->res_total * sizeof(double));
     if (e != cudaSuccess) {
@@ -232,6 +236,8 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
             P.br_qidx = reinterpret_cast<const int*>(A + p.o_bi);
             P.dirs = reinterpret_cast<const double*>(A + o_dirs);
             P.partial = b->partial;
+            P.sort_scratch = sort_bytes ? reinterpret_cast<int*>(reinterpret_cast<char*>(b->partial) + sort_off)
+                                        : nullptr;
         }
         if (!jobs.empty()) std::memcpy(st.h.data() + o_jobs[w], jobs.data(), jobs.size() * sizeof(dpx::FillJob));
         wave_tiles[w] = tiles;
@@ -284,7 +290,9 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
                 e = dpx::launch_origin_intensity(s, !fp32, grid, r);
                 launches++;
             }
-            launches += 4;  // splines, bracket tables, average, finalize
+            // splines, bracket tables, average, finalize; the angular order of the
+            // directions (keys, totals, offsets, scatter) when it applies
+            launches += 4 + (p.plan.sort_scratch && n_samples >= 512 ? 4 : 0);
         }
         const size_t r0 = b->res_off[j0], r1 = (j1 < n) ? b->res_off[j1] : b->res_total;
         if (e == cudaSuccess)

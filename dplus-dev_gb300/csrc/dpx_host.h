@@ -110,6 +110,7 @@ struct dpx_ctx_s {
     double stage_points = 0, stage_k = 0;
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
+    dpxh::DevBuf dirsort;  // the average's angular-order scratch
     dpxh::HostPinned pin_plan, pin_totals, pin_small;  // the harmonic fill's host staging
     std::vector<dpxh::DevBuf> leaf_boxes;  // the harmonic fill's solvent boxes, per leaf of a batch
     std::vector<char> host_stage;

@@ -71,7 +71,13 @@ struct AvgPlan {
     int need_dir;            // some model is placed or docked: the kernel needs the direction vector
     int one_leaf;            // one model without docked copies (ModelDev::n_groups == 0): with a
                              // shared direction set the average slides its plane window
+    int* sort_scratch;       // dir_sort_bytes(n_samples) of device scratch, or nullptr: with eps = 0
+                             // and a shared direction set the samples are taken in an angular order
+                             // (the mean is the same; neighbouring threads gather neighbouring cells)
+    const int* dir_order;    // the sample order in use (set by launch_average; nullptr: as given)
 };
+// Bytes of AvgPlan::sort_scratch for n samples.
+size_t dir_sort_bytes(int64_t n);
 
 // host helpers (dpx_api.cpp)
 void q_brackets(int grid_size, double qmax, int nq, const double* Q, int* layer_of_q);

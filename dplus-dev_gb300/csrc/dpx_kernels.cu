@@ -591,6 +591,7 @@ __device__ __forceinline__ void avg_slot(AvgSums<MQ>& S, int& nslot, const Cx<T>
 
 __device__ __forceinline__ void sample_direction(const AvgPlan& plan, int layer, int64_t s, double& theta,
                                                  double& phi, double dir[3]) {
+    if (plan.dir_order) s = plan.dir_order[s];  // a shared direction set in angular order
     const double* d = plan.dirs + 2 * ((int64_t)layer * plan.dir_stride + s);
     theta = d[0];
     phi = d[1];
@@ -729,6 +730,113 @@ __global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelD
         }
     }
     avg_flush<MQ>(S, nslot, plan, chunk);
+}
+
+// --------------------------------------------------------------------------
+// Angular order of a shared direction set (eps = 0 only: the mean does not
+// depend on the order): key = theta band (32) x phi bin (32), the phi bins
+// reversed in odd bands; a stable counting sort (per-block histograms, one
+// scan, ranks within a block by warp match) gives the sample order, so that
+// the threads of a warp interpolate nearby cells.
+// --------------------------------------------------------------------------
+constexpr int kDirBands = 32, kDirPhi = 32, kDirKeys = kDirBands * kDirPhi;
+constexpr int kDirBlock = 256;
+
+__global__ void __launch_bounds__(kDirBlock) dir_keys(const double* __restrict__ dirs, int64_t n, int* __restrict__ key,
+                                                      int* __restrict__ hist, int nblk) {
+    __shared__ int sh[kDirKeys];
+    for (int k = threadIdx.x; k < kDirKeys; k += blockDim.x) sh[k] = 0;
+    __syncthreads();
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) {
+        const double th = dirs[2 * s], ph = dirs[2 * s + 1];
+        int band = (int)(th * (kDirBands / kPi));
+        band = band < 0 ? 0 : (band >= kDirBands ? kDirBands - 1 : band);
+        int pb = (int)(ph * (kDirPhi / k2Pi));
+        pb = pb < 0 ? 0 : (pb >= kDirPhi ? kDirPhi - 1 : pb);
+        if (band & 1) pb = kDirPhi - 1 - pb;
+        const int k = band * kDirPhi + pb;
+        key[s] = k;
+        atomicAdd(&sh[k], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kDirKeys; k += blockDim.x) hist[(int64_t)k * nblk + blockIdx.x] = sh[k];
+}
+
+// Block-wide exclusive scan of one int per thread (blockDim a multiple of 32);
+// *total gets the block's sum.
+__device__ __forceinline__ int block_scan_excl_int(int v, int* total) {
+    __shared__ int ws[32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    int before = 0, all = 0;
+    for (int k = 0; k < nw; ++k) {
+        if (k < w) before += ws[k];
+        all += ws[k];
+    }
+    __syncthreads();
+    *total = all;
+    return before + x - v;
+}
+
+// block per key: its total over the sort blocks
+__global__ void __launch_bounds__(128) dir_totals(const int* __restrict__ hist, int nblk, int* __restrict__ total) {
+    const int* hk = hist + (int64_t)blockIdx.x * nblk;
+    int v = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += hk[b];
+    int all;
+    block_scan_excl_int(v, &all);
+    if (threadIdx.x == 0) total[blockIdx.x] = all;
+}
+
+// block per key k: off[k][blk] = start of key k + its counts in the earlier blocks
+__global__ void __launch_bounds__(128) dir_offsets(const int* __restrict__ hist, const int* __restrict__ total,
+                                                   int nblk, int* __restrict__ off) {
+    const int k = blockIdx.x;
+    int before = 0;
+    for (int j = threadIdx.x; j < k; j += blockDim.x) before += total[j];
+    int start;
+    block_scan_excl_int(before, &start);
+    const int per = (nblk + blockDim.x - 1) / blockDim.x;
+    const int b0 = min(nblk, (int)threadIdx.x * per), b1 = min(nblk, b0 + per);
+    const int* hk = hist + (int64_t)k * nblk;
+    int mine = 0;
+    for (int b = b0; b < b1; ++b) mine += hk[b];
+    int dummy;
+    int run = start + block_scan_excl_int(mine, &dummy);
+    int* ok = off + (int64_t)k * nblk;
+    for (int b = b0; b < b1; ++b) {
+        ok[b] = run;
+        run += hk[b];
+    }
+}
+
+__global__ void __launch_bounds__(kDirBlock) dir_scatter(const int* __restrict__ key, int64_t n,
+                                                         const int* __restrict__ off, int nblk,
+                                                         int* __restrict__ order) {
+    __shared__ int wc[kDirBlock / 32][kDirKeys];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int e = threadIdx.x; e < (kDirBlock / 32) * kDirKeys; e += blockDim.x) wc[e / kDirKeys][e % kDirKeys] = 0;
+    __syncthreads();
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = s < n;
+    const int k = valid ? key[s] : -1 - lane;  // invalid lanes form groups of one
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank == 0) wc[w][k] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+        int pre = 0;
+        for (int j = 0; j < w; ++j) pre += wc[j][k];
+        order[off[(int64_t)k * nblk + blockIdx.x] + pre + rank] = (int)s;
+    }
 }
 
 // eps = 0: the sum of each bracket's chunk partials, in a fixed order.
@@ -1261,10 +1369,34 @@ cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid)
     return cudaGetLastError();
 }
 
+// Scratch of the angular sort: keys [n], histograms and offsets [kDirKeys][blocks], key totals
+// [kDirKeys], the order [n].
+size_t dir_sort_bytes(int64_t n) {
+    const int64_t nblk = (n + kDirBlock - 1) / kDirBlock;
+    return ((size_t)2 * n + (size_t)2 * kDirKeys * nblk + kDirKeys) * sizeof(int) + 256;
+}
+
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
-                           const AvgPlan& plan) {
-    if (plan.n_brackets == 0 || plan.n_chunks == 0) return cudaSuccess;
-    if (plan.n_chunks > 0x7fffffff) return cudaErrorInvalidValue;
+                           const AvgPlan& plan_in) {
+    if (plan_in.n_brackets == 0 || plan_in.n_chunks == 0) return cudaSuccess;
+    if (plan_in.n_chunks > 0x7fffffff) return cudaErrorInvalidValue;
+    AvgPlan plan = plan_in;
+    plan.dir_order = nullptr;
+    if (plan.sort_scratch && plan.dir_stride == 0 && plan.n_samples >= 2 * kDirBlock &&
+        plan.n_samples <= 0x7fffffff) {
+        const int64_t n = plan.n_samples;
+        const int nblk = (int)((n + kDirBlock - 1) / kDirBlock);
+        int* key = plan.sort_scratch;
+        int* hist = key + n;
+        int* off = hist + (size_t)kDirKeys * nblk;
+        int* tot = off + (size_t)kDirKeys * nblk;
+        int* order = tot + kDirKeys;
+        dir_keys<<<nblk, kDirBlock, 0, s>>>(plan.dirs, n, key, hist, nblk);
+        dir_totals<<<kDirKeys, 128, 0, s>>>(hist, nblk, tot);
+        dir_offsets<<<kDirKeys, 128, 0, s>>>(hist, tot, nblk, off);
+        dir_scatter<<<nblk, kDirBlock, 0, s>>>(key, n, off, nblk, order);
+        plan.dir_order = order;
+    }
     // segments of consecutive brackets: enough blocks to fill the GPU a few
     // times over, at most 64 brackets a segment
     int dev = 0, sms = 152;

@@ -453,7 +453,10 @@ int launch_request(dpx_server_s* S, Request* r) {
     h.resize(oR + (size_t)r->nq * sizeof(double));
     const size_t oP = al16(h.size());
     const size_t part = ((size_t)P.n_brackets * P.n_chunks + (size_t)P.n_brackets * 5) * P.max_q * sizeof(double);
-    const size_t total = oP + part + 64;
+    // with eps = 0 the shared directions are taken in angular order
+    const size_t oS = al16(oP + part);
+    const size_t sort_bytes = r->eps == 0.0 ? dpx::dir_sort_bytes(r->n_samples) : 0;
+    const size_t total = oS + sort_bytes + 64;
     char* d = nullptr;
     DPX_CUDA(cudaMallocAsync((void**)&d, total, s));
     place_models(T, d + oG);
@@ -463,6 +466,7 @@ int launch_request(dpx_server_s* S, Request* r) {
     P.br_q_off = reinterpret_cast<const int*>(d + oO);
     P.br_qidx = reinterpret_cast<const int*>(d + oI);
     P.partial = reinterpret_cast<double*>(d + oP);
+    P.sort_scratch = sort_bytes ? reinterpret_cast<int*>(d + oS) : nullptr;
     size_t cap = 0;
     const size_t stage = oR + (size_t)r->nq * sizeof(double);
     char* hp = static_cast<char*>(S->pinned.get(stage, &cap));
@@ -696,7 +700,8 @@ int dpx_server_submit(dpx_server S, const dpx_request* q, uint64_t* ticket) {
                               sizeof(int) * ((size_t)copies + (size_t)nm) + nm * sizeof(dpx::ModelDev) +
                               B.q.size() * (sizeof(double) + sizeof(int)) + 2 * B.layer.size() * sizeof(int) + 1024;
         r->scratch_bytes = al16(tables) + al16((size_t)r->nq * sizeof(double)) +
-                           ((size_t)B.layer.size() * n_chunks + B.layer.size() * 5) * B.max_q * sizeof(double) + 256;
+                           ((size_t)B.layer.size() * n_chunks + B.layer.size() * 5) * B.max_q * sizeof(double) + 256 +
+                           (r->eps == 0.0 ? dpx::dir_sort_bytes(r->n_samples) : 0);
     }
     r->t_submit = Clock::now();
     {
