@@ -700,6 +700,7 @@ __global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelD
             }
         }
     }
+    const bool phased = dotR != 0.0;  // a placed leaf: its phase per q
     PlaneWindow<T> win;
     win.f = -2;
     for (int b = b0; b < b1; ++b) {
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelD
                 A[k] = {T(0), T(0)};
                 if (valid && k < mq) {
                     Cx<T> v = hermite<T>(pl1, pl2, d1, d2, frac_tab[q0 + qc + k]);
-                    if (dotR != 0.0) v = cmul(v, expi<T>(dotR * plan.br_q[q0 + qc + k]));
+                    if (phased) v = cmul(v, expi<T>(dotR * plan.br_q[q0 + qc + k]));
                     A[k] = cadd(A[k], v);
                 }
             }
