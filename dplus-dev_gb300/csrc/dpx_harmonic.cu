@@ -471,24 +471,29 @@ __device__ __forceinline__ int64_t block_scan_excl(int64_t v, int64_t* total) {
 // The leaf's solvent boxes (raw D+ records {cx, cy, cz, w, Lx, Ly, Lz, -}) about
 // the centre c: the float4 pair {centre - c, w}, {L, 0}; each box's voxel
 // count (its edges over the voxel step, rounded as vx_expand rounds them); the
-// largest squared distance of a box corner from c (rounded up to FP32) and
-// the total voxel count, reduced into scal = {r2 bits, total}.
+// largest squared distance of a box corner from c and of a voxel centre (the
+// corner of the box shrunk by half a voxel), rounded up to FP32, and the total
+// voxel count, reduced into scal = {corner r2 bits, total, centre r2 bits}.
 __global__ void __launch_bounds__(kBinThreads) vx_prepare(const float* __restrict__ raw, int64_t nb, double cx,
                                                           double cy, double cz, float vs, float4* __restrict__ boxes,
                                                           int64_t* __restrict__ counts,
                                                           unsigned long long* __restrict__ scal) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    float q = 0.f;
+    float q = 0.f, qv = 0.f;
     int64_t n = 0;
     if (b < nb) {
         const float* r = raw + 8 * b;
         const double c[3] = {cx, cy, cz};
-        double e2 = 0.0;
+        double e2 = 0.0, v2 = 0.0;
         for (int k = 0; k < 3; ++k) {
-            const double e = fabs((double)r[k] - c[k]) + 0.5 * (double)r[4 + k];
+            const double d = fabs((double)r[k] - c[k]);
+            const double e = d + 0.5 * (double)r[4 + k];
+            const double v = d + 0.5 * fmax((double)r[4 + k] - (double)vs, 0.0);
             e2 += e * e;
+            v2 += v * v;
         }
         q = __double2float_ru(e2);
+        qv = __double2float_ru(v2);
         boxes[2 * b] = make_float4((float)((double)r[0] - cx), (float)((double)r[1] - cy), (float)((double)r[2] - cz),
                                    r[3]);
         boxes[2 * b + 1] = make_float4(r[4], r[5], r[6], 0.f);
@@ -496,29 +501,33 @@ __global__ void __launch_bounds__(kBinThreads) vx_prepare(const float* __restric
         counts[b] = n;
     }
     // block reduction, then one atomic each
-    unsigned qb = __float_as_uint(q);  // q >= 0: the bits order as the values
+    unsigned qb = __float_as_uint(q), qvb = __float_as_uint(qv);  // >= 0: the bits order as the values
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         qb = max(qb, __shfl_down_sync(0xffffffffu, qb, o));
+        qvb = max(qvb, __shfl_down_sync(0xffffffffu, qvb, o));
         n += __shfl_down_sync(0xffffffffu, n, o);
     }
-    __shared__ unsigned sq[kBinThreads / 32];
+    __shared__ unsigned sq[kBinThreads / 32], sqv[kBinThreads / 32];
     __shared__ int64_t sn[kBinThreads / 32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
         sq[w] = qb;
+        sqv[w] = qvb;
         sn[w] = n;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned qm = 0;
+        unsigned qm = 0, qvm = 0;
         int64_t nt = 0;
         for (int k = 0; k < kBinThreads / 32; ++k) {
             qm = max(qm, sq[k]);
+            qvm = max(qvm, sqv[k]);
             nt += sn[k];
         }
         atomicMax(scal, (unsigned long long)qm);
         atomicAdd(scal + 1, (unsigned long long)nt);
+        atomicMax(scal + 2, (unsigned long long)qvm);
     }
 }
 
@@ -1025,7 +1034,7 @@ int harmonic_max_bins() { return kMaxBins; }
 
 cudaError_t launch_voxel_prepare(cudaStream_t s, const VoxelPrepArgs& a) {
     if (a.nb <= 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(a.scal, 0, 2 * sizeof(unsigned long long), s);
+    cudaError_t e = cudaMemsetAsync(a.scal, 0, 3 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     vx_prepare<<<(unsigned)((a.nb + kBinThreads - 1) / kBinThreads), kBinThreads, 0, s>>>(
         a.raw, a.nb, a.cx, a.cy, a.cz, a.vs, a.boxes, a.counts, a.scal);

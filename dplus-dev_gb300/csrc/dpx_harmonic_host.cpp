@@ -164,6 +164,7 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
         for (int k = 0; k < 3; ++k) q += (src[4 * a + k] - ca[k]) * (src[4 * a + k] - ca[k]);
         r2 = std::max(r2, q);
     }
+    double r2_pts = r2;  // the points themselves: atoms and voxel centres
     // the solvent boxes: uploaded once, centred and counted on the device, with
     // their largest corner distance and the voxel total read back
     const int64_t nb = d.n_boxes > 0 && d.boxes ? d.n_boxes : 0;
@@ -176,7 +177,7 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
         const size_t oVs = al16(oCnt + (size_t)nb * sizeof(int64_t));
         const size_t oRs = al16(oVs + (size_t)nb * sizeof(int64_t));
         const size_t oSc = al16(oRs + (size_t)((nb + dpx::kVoxelScanRun - 1) / dpx::kVoxelScanRun) * sizeof(int64_t));
-        cudaError_t e = B.reserve(oSc + 2 * sizeof(unsigned long long));
+        cudaError_t e = B.reserve(oSc + 3 * sizeof(unsigned long long));
         char* base = static_cast<char*>(B.p);
         cudaStream_t st = ctx->stream;
         if (e == cudaSuccess)
@@ -193,8 +194,8 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
         a.scal = reinterpret_cast<unsigned long long*>(base + oSc);
         if (e == cudaSuccess) e = dpx::launch_voxel_prepare(st, a);
         char* hp = nullptr;
-        if (e == cudaSuccess) e = ctx->pin_small.get(2 * sizeof(unsigned long long), &hp);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(hp, a.scal, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = ctx->pin_small.get(3 * sizeof(unsigned long long), &hp);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hp, a.scal, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -202,9 +203,11 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
             return false;
         }
         const unsigned long long* sc = reinterpret_cast<const unsigned long long*>(hp);
-        const unsigned qbits = (unsigned)sc[0];
-        float qf;
+        const unsigned qbits = (unsigned)sc[0], vbits = (unsigned)sc[2];
+        float qf, vf;
         std::memcpy(&qf, &qbits, sizeof qf);
+        std::memcpy(&vf, &vbits, sizeof vf);
+        r2_pts = std::max(r2_pts, (double)vf);
         r2 = std::max(r2, (double)qf);
         hl.nb = nb;
         hl.nv = (int64_t)sc[1];
@@ -216,6 +219,7 @@ bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::G
     // the fill's points are rounded to FP32 about the centre: a relative margin
     const double R = std::sqrt(r2) * (1.0 + 1e-6);
     hl.R = R;
+    hl.R_pts = std::min(R, std::sqrt(r2_pts) * (1.0 + 1e-6));
     if (order_of(G.Lp * G.step * R) > dpx::harmonic_max_l()) return false;
     const double delta = kBinWidthTimesQmax / (G.Lp * G.step);
     if (nb > 0 && (int)(R / delta) + 1 > dpx::harmonic_max_bins()) return false;
@@ -298,18 +302,11 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     };
     Set sa, sv;
     make_set(atoms, false, sa);
-    // voxels: their bin totals (the binning launched above)
     const int64_t n_vox = hl.nb > 0 ? hl.nv : 0;
-    if (hl.nb > 0)
-        if (int rc = bin_voxels_finish(ctx, nbins, sv.units, sv.groups, sv.gu)) return rc;
-    // ---- orders.  R (harmonic_accepts) bounds the atoms and the corners of the
-    // solvent boxes; every point of bin b lies within (b + 1) delta, so the
-    // last occupied bin bounds them more tightly.  Bin b needs the orders
-    // l <= order_of(q_max (b + 1) delta) only. ----
-    int b_last = 0;
-    for (const Set* S : {&sa, &sv})
-        for (const int2& gb : S->groups) b_last = std::max(b_last, gb.x);
-    const double Reff = std::min(R, (b_last + 1) * delta * (1.0 + 1e-6));
+    // ---- orders.  hl.R_pts bounds the atoms and the voxel centres (R, the box
+    // corners, bounds the bins).  Bin b needs the orders l <= order_of(q_max
+    // (b + 1) delta) only. ----
+    const double Reff = hl.R_pts;
     std::vector<int> lmax(Lp + 1, 0);
     for (int i = 1; i <= Lp; ++i) lmax[i] = order_of(i * G.step * Reff);
     const int LM = lmax[Lp];
@@ -360,18 +357,23 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     const size_t oVi = put(h, vinv, sizeof vinv);
     size_t oP[2], oU[2], oG[2], oGu[2];
     Set* sets[2] = {&sa, &sv};
-    for (int k = 0; k < 2; ++k) {
-        oP[k] = put(h, sets[k]->pts.data(), sets[k]->pts.size() * sizeof(float4));  // voxels: empty here
-        oU[k] = put(h, sets[k]->units.data(), sets[k]->units.size() * sizeof(int4));
-        oG[k] = put(h, sets[k]->groups.data(), sets[k]->groups.size() * sizeof(int2));
-        oGu[k] = put(h, sets[k]->gu.data(), sets[k]->gu.size() * sizeof(int));
-    }
+    oP[0] = put(h, sa.pts.data(), sa.pts.size() * sizeof(float4));
+    oU[0] = put(h, sa.units.data(), sa.units.size() * sizeof(int4));
+    oG[0] = put(h, sa.groups.data(), sa.groups.size() * sizeof(int2));
+    oGu[0] = put(h, sa.gu.data(), sa.gu.size() * sizeof(int));
     const size_t staged = al16(h.size());
-    const size_t oJn = staged;
+    // the voxels' units, groups and group starts come with their bin totals:
+    // a region sized for at most one partial unit per bin
+    const size_t vox_units_max = n_vox ? (size_t)(n_vox + kUnitPoints - 1) / kUnitPoints + nbins : 0;
+    oU[1] = staged;
+    oG[1] = al16(oU[1] + vox_units_max * sizeof(int4));
+    oGu[1] = al16(oG[1] + (size_t)nbins * sizeof(int2));
+    oP[1] = 0;
+    const size_t oJn = al16(oGu[1] + (size_t)(nbins + 1) * sizeof(int));
     const size_t oT = al16(oJn + (size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double));
     const size_t oMP = al16(oT + (size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float));
-    const size_t max_units = std::max(sa.units.size(), sv.units.size());
-    const size_t max_groups = std::max(sa.groups.size(), sv.groups.size());
+    const size_t max_units = std::max(sa.units.size(), vox_units_max);
+    const size_t max_groups = std::max(sa.groups.size(), n_vox ? (size_t)nbins : (size_t)0);
     const size_t oM = al16(oMP + max_units * moments_per_unit);
     const size_t oCa = al16(oM + max_groups * moments_per_unit);
     const size_t oCv = al16(oCa + cell_set);
@@ -381,15 +383,6 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         return fail(DPX_ERR_OOM, "harmonic fill needs %zu bytes (%s)", total, cudaGetErrorString(e));
     }
     char* base = static_cast<char*>(ctx->harmonic.p);
-    if (ev) {
-        ctx->tev_used = n_vox ? 8 : 6;
-        // K per point as the moments compute it: its bin's (l_b + 1)(l_b + 2) / 2
-        double pk = 0.0;
-        for (const Set* S : {&sa, &sv})
-            for (const int4& u : S->units) pk += (double)u.y * (lmb[u.z] + 1) * (lmb[u.z] + 2) / 2;
-        ctx->stage_points = (double)atoms.size() + (double)n_vox;
-        ctx->stage_k = ctx->stage_points > 0 ? pk / ctx->stage_points : 0.0;
-    }
     char* hp = nullptr;
     DPX_CUDA(ctx->pin_plan.get(staged, &hp));
     std::memcpy(hp, h.data(), staged);
@@ -411,9 +404,9 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     float2* Ca = reinterpret_cast<float2*>(base + oCa);
     float2* Cv = n_vox == 0 ? nullptr : reinterpret_cast<float2*>(base + oCv);
     DPX_CUDA(cudaMemsetAsync(Ca, 0, cell_set * (n_vox == 0 ? 1 : 2), st));
-    for (int k = 0; k < 2; ++k) {
+    auto launch_set = [&](int k) -> int {
         const Set& S = *sets[k];
-        if (S.units.empty()) continue;
+        if (S.units.empty()) return DPX_OK;
         dpx::HarmonicSet a{};
         a.pts = k == 0 ? reinterpret_cast<const float4*>(base + oP[0]) : vox_dev;
         a.units = reinterpret_cast<const int4*>(base + oU[k]);
@@ -438,6 +431,33 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         a.ev0 = ev ? ev[2 * k] : nullptr;
         a.ev1 = ev ? ev[2 * k + 1] : nullptr;
         DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
+        return DPX_OK;
+    };
+    if (int rc = launch_set(0)) return rc;
+    // ---- the voxels: their bin totals (the binning launched first) give the units ----
+    if (n_vox) {
+        if (int rc = bin_voxels_finish(ctx, nbins, sv.units, sv.groups, sv.gu)) return rc;
+        if (sv.units.size() > vox_units_max || sv.groups.size() > (size_t)nbins)
+            return fail(DPX_ERR_ARG, "harmonic fill: %zu voxel units above the %zu planned", sv.units.size(),
+                        vox_units_max);
+        const size_t bytes = oJn - oU[1];
+        char* vp = nullptr;
+        DPX_CUDA(ctx->pin_units.get(bytes, &vp));
+        std::memcpy(vp, sv.units.data(), sv.units.size() * sizeof(int4));
+        std::memcpy(vp + (oG[1] - oU[1]), sv.groups.data(), sv.groups.size() * sizeof(int2));
+        std::memcpy(vp + (oGu[1] - oU[1]), sv.gu.data(), sv.gu.size() * sizeof(int));
+        DPX_CUDA(cudaMemcpyAsync(base + oU[1], vp, bytes, cudaMemcpyHostToDevice, st));
+        DPX_CUDA(ctx->pin_units.copied(st));
+        if (int rc = launch_set(1)) return rc;
+    }
+    if (ev) {
+        ctx->tev_used = n_vox ? 8 : 6;
+        // K per point as the moments compute it: its bin's (l_b + 1)(l_b + 2) / 2
+        double pk = 0.0;
+        for (const Set* S : {&sa, &sv})
+            for (const int4& u : S->units) pk += (double)u.y * (lmb[u.z] + 1) * (lmb[u.z] + 2) / 2;
+        ctx->stage_points = (double)atoms.size() + (double)n_vox;
+        ctx->stage_k = ctx->stage_points > 0 ? pk / ctx->stage_points : 0.0;
     }
     dpx::HarmonicSynth y{};
     y.Ca = Ca;

@@ -111,7 +111,7 @@ struct dpx_ctx_s {
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
     dpxh::DevBuf dirsort;  // the average's angular-order scratch
-    dpxh::HostPinned pin_plan, pin_totals, pin_small;  // the harmonic fill's host staging
+    dpxh::HostPinned pin_plan, pin_totals, pin_small, pin_units;  // the harmonic fill's host staging
     std::vector<dpxh::DevBuf> leaf_boxes;  // the harmonic fill's solvent boxes, per leaf of a batch
     std::vector<char> host_stage;
 };
@@ -188,7 +188,8 @@ dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* db
 // centred, counted) and fills `hl`: the radius of the point sets about the
 // leaf's centre, the voxel total and the staged arrays harmonic_fill bins.
 struct HarmLeaf {
-    double R = 0.0;
+    double R = 0.0;      // bounds the atoms and the solvent boxes' corners
+    double R_pts = 0.0;  // bounds the atoms and the voxel centres (<= R)
     int64_t nb = 0, nv = 0;
     const float4* boxes = nullptr;
     const int64_t* counts = nullptr;

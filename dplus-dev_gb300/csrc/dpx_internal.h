@@ -208,7 +208,8 @@ struct VoxelPrepArgs {
     float vs;               // voxel edge (nm)
     float4* boxes;          // out [2 nb] {centre - c, w}, {L, 0}
     int64_t* counts;        // out [nb] voxels per box
-    unsigned long long* scal;  // out {bits of the largest squared corner distance (FP32), total voxels}
+    unsigned long long* scal;  // out {bits of the largest squared corner distance (FP32), total voxels,
+                               //      bits of the largest squared voxel-centre distance (FP32)}
 };
 cudaError_t launch_voxel_prepare(cudaStream_t s, const VoxelPrepArgs& a);
 struct VoxelBinArgs {
