@@ -205,6 +205,7 @@ void ctx_release(dpx_ctx ctx) {
     ctx->pin_totals.release();
     ctx->pin_small.release();
     ctx->pin_units.release();
+    ctx->pin_atomset.release();
     for (cudaEvent_t e : ctx->tev)
         if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);

@@ -253,14 +253,15 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     const float* src = d.atoms_on_device ? host_atoms.data() : d.atoms;
     const double sh[3] = {d.atoms_on_device ? 0.0 : t.cen[0], d.atoms_on_device ? 0.0 : t.cen[1],
                           d.atoms_on_device ? 0.0 : t.cen[2]};
-    std::vector<float4> atoms(d.n_atoms);
-    {
+    auto centred_atoms = [&]() {
+        std::vector<float4> atoms(d.n_atoms);
         int64_t j = 0;
         for (int u = 0; u < d.n_ions; ++u)
             for (int k = 0; k < d.atoms_per_ion[u]; ++k, ++j)
                 atoms[j] = make_float4((float)((double)src[4 * j] - sh[0]), (float)((double)src[4 * j + 1] - sh[1]),
                                        (float)((double)src[4 * j + 2] - sh[2]), (float)u);
-    }
+        return atoms;
+    };
     // ---- the degree-5 interpolation of the radial bins on Chebyshev nodes ----
     double nodes[6], vinv[36];
     chebyshev_fit(nodes, vinv);
@@ -300,8 +301,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         }
         out.gu.push_back((int)out.units.size());
     };
-    Set sa, sv;
-    make_set(atoms, false, sa);
+    Set sa, sv;  // built after the tables and the voxels' moments are launched
     const int64_t n_vox = hl.nb > 0 ? hl.nv : 0;
     // ---- orders.  hl.R_pts bounds the atoms and the voxel centres (R, the box
     // corners, bounds the bins).  Bin b needs the orders l <= order_of(q_max
@@ -357,23 +357,26 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     const size_t oVi = put(h, vinv, sizeof vinv);
     size_t oP[2], oU[2], oG[2], oGu[2];
     Set* sets[2] = {&sa, &sv};
-    oP[0] = put(h, sa.pts.data(), sa.pts.size() * sizeof(float4));
-    oU[0] = put(h, sa.units.data(), sa.units.size() * sizeof(int4));
-    oG[0] = put(h, sa.groups.data(), sa.groups.size() * sizeof(int2));
-    oGu[0] = put(h, sa.gu.data(), sa.gu.size() * sizeof(int));
     const size_t staged = al16(h.size());
-    // the voxels' units, groups and group starts come with their bin totals:
-    // a region sized for at most one partial unit per bin
+    // the voxels' units, groups and group starts come with their bin totals,
+    // the atoms' set once the voxels' moments run: regions sized for at most
+    // one partial unit per group
     const size_t vox_units_max = n_vox ? (size_t)(n_vox + kUnitPoints - 1) / kUnitPoints + nbins : 0;
     oU[1] = staged;
     oG[1] = al16(oU[1] + vox_units_max * sizeof(int4));
     oGu[1] = al16(oG[1] + (size_t)nbins * sizeof(int2));
     oP[1] = 0;
-    const size_t oJn = al16(oGu[1] + (size_t)(nbins + 1) * sizeof(int));
+    const size_t atom_groups_max = (size_t)nbins * d.n_ions;
+    const size_t atom_units_max = (size_t)(d.n_atoms + kUnitPoints - 1) / kUnitPoints + atom_groups_max;
+    oP[0] = al16(oGu[1] + (size_t)(nbins + 1) * sizeof(int));
+    oU[0] = al16(oP[0] + (size_t)d.n_atoms * sizeof(float4));
+    oG[0] = al16(oU[0] + atom_units_max * sizeof(int4));
+    oGu[0] = al16(oG[0] + atom_groups_max * sizeof(int2));
+    const size_t oJn = al16(oGu[0] + (atom_groups_max + 1) * sizeof(int));
     const size_t oT = al16(oJn + (size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double));
     const size_t oMP = al16(oT + (size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float));
-    const size_t max_units = std::max(sa.units.size(), vox_units_max);
-    const size_t max_groups = std::max(sa.groups.size(), n_vox ? (size_t)nbins : (size_t)0);
+    const size_t max_units = std::max(atom_units_max, vox_units_max);
+    const size_t max_groups = std::max(atom_groups_max, n_vox ? (size_t)nbins : (size_t)0);
     const size_t oM = al16(oMP + max_units * moments_per_unit);
     const size_t oCa = al16(oM + max_groups * moments_per_unit);
     const size_t oCv = al16(oCa + cell_set);
@@ -433,7 +436,6 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
         return DPX_OK;
     };
-    if (int rc = launch_set(0)) return rc;
     // ---- the voxels: their bin totals (the binning launched first) give the units ----
     if (n_vox) {
         if (int rc = bin_voxels_finish(ctx, nbins, sv.units, sv.groups, sv.gu)) return rc;
@@ -450,13 +452,32 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         DPX_CUDA(ctx->pin_units.copied(st));
         if (int rc = launch_set(1)) return rc;
     }
+    // ---- the atoms, grouped by (bin, ion) while the voxels' moments run ----
+    make_set(centred_atoms(), false, sa);
+    if (sa.units.size() > atom_units_max || sa.groups.size() > atom_groups_max)
+        return fail(DPX_ERR_ARG, "harmonic fill: %zu atom units above the %zu planned", sa.units.size(),
+                    atom_units_max);
+    if (!sa.units.empty()) {
+        const size_t bytes = oJn - oP[0];
+        char* ap = nullptr;
+        DPX_CUDA(ctx->pin_atomset.get(bytes, &ap));
+        std::memcpy(ap, sa.pts.data(), sa.pts.size() * sizeof(float4));
+        std::memcpy(ap + (oU[0] - oP[0]), sa.units.data(), sa.units.size() * sizeof(int4));
+        std::memcpy(ap + (oG[0] - oP[0]), sa.groups.data(), sa.groups.size() * sizeof(int2));
+        std::memcpy(ap + (oGu[0] - oP[0]), sa.gu.data(), sa.gu.size() * sizeof(int));
+        DPX_CUDA(cudaMemcpyAsync(base + oP[0], ap, bytes, cudaMemcpyHostToDevice, st));
+        DPX_CUDA(ctx->pin_atomset.copied(st));
+        if (int rc = launch_set(0)) return rc;
+    }
+    // F(0) with the solvent boxes' volumes, summed while the moments run
+    const double origin = t.origin + d.scale * box_volume_sum(d);
     if (ev) {
         ctx->tev_used = n_vox ? 8 : 6;
         // K per point as the moments compute it: its bin's (l_b + 1)(l_b + 2) / 2
         double pk = 0.0;
         for (const Set* S : {&sa, &sv})
             for (const int4& u : S->units) pk += (double)u.y * (lmb[u.z] + 1) * (lmb[u.z] + 2) / 2;
-        ctx->stage_points = (double)atoms.size() + (double)n_vox;
+        ctx->stage_points = (double)sa.pts.size() + (double)n_vox;
         ctx->stage_k = ctx->stage_points > 0 ? pk / ctx->stage_points : 0.0;
     }
     dpx::HarmonicSynth y{};
@@ -475,7 +496,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     y.cz = t.cen[2];
     y.use_center = (t.cen[0] != 0.0 || t.cen[1] != 0.0 || t.cen[2] != 0.0);
     y.scale = (float)d.scale;
-    y.origin = t.origin;
+    y.origin = origin;
     y.grid = reinterpret_cast<float4*>(grid);
     if (ev) DPX_CUDA(cudaEventRecord(ev[4], st));
     DPX_CUDA(dpx::launch_harmonic_synth(st, y));

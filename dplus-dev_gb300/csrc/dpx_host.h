@@ -111,7 +111,7 @@ struct dpx_ctx_s {
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
     dpxh::DevBuf dirsort;  // the average's angular-order scratch
-    dpxh::HostPinned pin_plan, pin_totals, pin_small, pin_units;  // the harmonic fill's host staging
+    dpxh::HostPinned pin_plan, pin_totals, pin_small, pin_units, pin_atomset;  // the harmonic fill's host staging
     std::vector<dpxh::DevBuf> leaf_boxes;  // the harmonic fill's solvent boxes, per leaf of a batch
     std::vector<char> host_stage;
 };
@@ -173,10 +173,13 @@ struct LeafTables {
     double origin = 0;  // F(0) = scale (sum_u aff_u(0) N_u + sum_b w_b V_b), FP64
 };
 // Appends leaf d's tables for grid G (FP32 with cpt cells per item, or FP64).
-// direct_boxes = false leaves the boxes out of the staging (the harmonic fill
-// reads them from the descriptor); F(0) counts them either way.
+// direct_boxes = false leaves the boxes out of the staging and out of F(0):
+// the harmonic fill reads them from the descriptor and adds
+// scale * box_volume_sum(d) to F(0) while its moments run.
 void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G, bool fp32, int cpt, LeafTables& t,
                 bool direct_boxes = true);
+// sum_b w_b Lx_b Ly_b Lz_b over d's solvent boxes, in their order, FP64.
+double box_volume_sum(const dpx_pdb_desc& d);
 // The FP32 fill job of a staged leaf whose buffer sits at device address dbase.
 dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
                       int64_t tile_start);

@@ -82,11 +82,18 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
             b[2 * i + 1] = make_float4(s[4], s[5], s[6], 0.f);
         }
     }
-    for (int64_t i = 0; i < t.n_boxes; ++i) {
-        const float* s = d.boxes + 8 * i;
-        origin += (double)s[3] * (double)s[4] * (double)s[5] * (double)s[6];
-    }
+    if (direct_boxes) origin += box_volume_sum(d);
     t.origin = origin * d.scale;
+}
+
+double box_volume_sum(const dpx_pdb_desc& d) {
+    double v = 0.0;
+    const int64_t nb = d.n_boxes > 0 && d.boxes ? d.n_boxes : 0;
+    for (int64_t i = 0; i < nb; ++i) {
+        const float* s = d.boxes + 8 * i;
+        v += (double)s[3] * (double)s[4] * (double)s[5] * (double)s[6];
+    }
+    return v;
 }
 
 dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
