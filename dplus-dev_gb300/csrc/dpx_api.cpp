@@ -129,8 +129,10 @@ void dpx::q_brackets(int grid_size, double qmax, int nq, const double* Q, int* l
     if (nq == 0) return;
     int tmp = 0;
     while (Q[0] > (tmp + 1) * step) tmp++;
+    // qb = the length of the prefix of Q at or below layer * step: it only
+    // grows with the layer (for any Q), so each layer's scan continues the last
+    int qb = 0;
     for (int layer = tmp; layer < L; ++layer) {
-        int qb = 0;
         while (qb < nq && Q[qb] <= layer * step) qb++;
         if (qb >= nq) continue;
         int qe = qb + 1;
@@ -622,19 +624,26 @@ void make_brackets(const dpx::Geom& G, int grid_size, double qmax, int nq, const
     std::vector<int> layer_of_q(nq);
     dpx::q_brackets(grid_size, qmax, nq, Q, layer_of_q.data());
     b = Brackets{};
+    // the q of each layer in ascending layer order, each layer's in index order
+    // (a stable counting pass)
+    std::vector<int> start(G.L + 1, 0);
+    for (int k = 0; k < nq; ++k)
+        if (layer_of_q[k] >= 0 && layer_of_q[k] < G.L) start[layer_of_q[k] + 1]++;
+    for (int l = 0; l < G.L; ++l) start[l + 1] += start[l];
+    std::vector<int> order(start[G.L]);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int k = 0; k < nq; ++k)
+        if (layer_of_q[k] >= 0 && layer_of_q[k] < G.L) order[fill[layer_of_q[k]]++] = k;
     for (int l = 0; l < G.L; ++l) {
-        int cnt = 0;
-        for (int k = 0; k < nq; ++k)
-            if (layer_of_q[k] == l) {
-                b.q.push_back(Q[k]);
-                b.qidx.push_back(k);
-                cnt++;
-            }
-        if (cnt) {
-            b.layer.push_back(l);
-            b.off.push_back((int)b.q.size());
-            b.max_q = std::max(b.max_q, cnt);
+        const int cnt = start[l + 1] - start[l];
+        if (!cnt) continue;
+        for (int j = start[l]; j < start[l + 1]; ++j) {
+            b.q.push_back(Q[order[j]]);
+            b.qidx.push_back(order[j]);
         }
+        b.layer.push_back(l);
+        b.off.push_back((int)b.q.size());
+        b.max_q = std::max(b.max_q, cnt);
     }
 }
 

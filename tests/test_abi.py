@@ -60,6 +60,25 @@ def test_brackets_match_oracle(gs, qmax, nq, q0):
     assert np.array_equal(out, O.q_brackets(gs, qmax, Q))
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_brackets_match_oracle_ragged(seed):
+    """Clustered, repeated, grid-aligned and unsorted q lists (the reference's
+    bracket scan has no sortedness requirement) give the oracle's layers."""
+    rng = np.random.default_rng(seed)
+    gs, qmax = int(rng.integers(4, 120)), float(rng.uniform(1.0, 8.0))
+    step = 2 * qmax / gs
+    nq = int(rng.integers(1, 300))
+    Q = np.sort(rng.uniform(0, qmax, nq))
+    if seed % 3 == 1:  # repeats and exact layer boundaries
+        Q = np.sort(np.concatenate([Q[: nq // 2], Q[: nq // 4], step * rng.integers(0, gs // 2, nq // 4 + 1)]))
+    elif seed % 3 == 2:
+        Q = rng.permutation(Q)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    out = np.zeros(len(Q), dtype=np.int32)
+    _lib.check(dpx.lib().dpx_q_brackets(gs, qmax, len(Q), _lib.dptr(Q), _lib.iptr(out)))
+    assert np.array_equal(out, O.q_brackets(gs, qmax, Q))
+
+
 def test_grid_geometry():
     assert dpx.lib().dpx_grid_cells(120) == 1548289
     assert dpx.lib().dpx_grid_bytes(400, M.FP32) == 50688289 * 16
