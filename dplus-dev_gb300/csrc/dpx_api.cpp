@@ -210,6 +210,12 @@ void ctx_release(dpx_ctx ctx) {
     ctx->pin_atomset.release();
     for (cudaEvent_t e : ctx->tev)
         if (e) cudaEventDestroy(e);
+    if (ctx->aux) {
+        cudaStreamSynchronize(ctx->aux);
+        cudaStreamDestroy(ctx->aux);
+    }
+    for (cudaEvent_t e : {ctx->aux_go, ctx->aux_done})
+        if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }

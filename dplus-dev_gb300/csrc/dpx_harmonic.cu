@@ -1024,6 +1024,10 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C)
     }
     const int64_t ng = (int64_t)a.G * kNodes * a.K;
     hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.groups, a.lmb, a.G, a.K, a.M);
+    if (a.contract_wait) {
+        cudaError_t e = cudaStreamWaitEvent(s, a.contract_wait, 0);
+        if (e != cudaSuccess) return e;
+    }
     hm_contract<<<dim3((a.K + kContractK - 1) / kContractK, (a.Lp + kContractShells - 1) / kContractShells),
                   kContractK * kContractWarps, 0, s>>>(
         a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.lmb, a.aff, C);

@@ -403,7 +403,14 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     tb.vinv = reinterpret_cast<const double*>(base + oVi);
     tb.Jn = reinterpret_cast<double*>(base + oJn);
     tb.T = reinterpret_cast<float*>(base + oT);
-    DPX_CUDA(dpx::launch_harmonic_tables(st, tb));
+    // the tables on the side stream, beside the binning and the moments
+    if (!ctx->aux) DPX_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    if (!ctx->aux_go) DPX_CUDA(cudaEventCreateWithFlags(&ctx->aux_go, cudaEventDisableTiming));
+    if (!ctx->aux_done) DPX_CUDA(cudaEventCreateWithFlags(&ctx->aux_done, cudaEventDisableTiming));
+    DPX_CUDA(cudaEventRecord(ctx->aux_go, st));
+    DPX_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->aux_go, 0));
+    DPX_CUDA(dpx::launch_harmonic_tables(ctx->aux, tb));
+    DPX_CUDA(cudaEventRecord(ctx->aux_done, ctx->aux));
     float2* Ca = reinterpret_cast<float2*>(base + oCa);
     float2* Cv = n_vox == 0 ? nullptr : reinterpret_cast<float2*>(base + oCv);
     DPX_CUDA(cudaMemsetAsync(Ca, 0, cell_set * (n_vox == 0 ? 1 : 2), st));
@@ -433,6 +440,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         a.M = reinterpret_cast<float2*>(base + oM);
         a.ev0 = ev ? ev[2 * k] : nullptr;
         a.ev1 = ev ? ev[2 * k + 1] : nullptr;
+        a.contract_wait = ctx->aux_done;
         DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
         return DPX_OK;
     };

@@ -177,6 +177,7 @@ struct HarmonicSet {
     float2* MP;             // [n_units][6][K]
     float2* M;              // [G][6][K]
     cudaEvent_t ev0, ev1;   // recorded around the moments launch when not null
+    cudaEvent_t contract_wait;  // the radial tables' completion, waited on before hm_contract when not null
 };
 struct HarmonicSynth {
     const float2* Ca;       // [Lp+1][K] atoms
