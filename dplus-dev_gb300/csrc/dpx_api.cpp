@@ -214,7 +214,7 @@ void ctx_release(dpx_ctx ctx) {
         cudaStreamSynchronize(ctx->aux);
         cudaStreamDestroy(ctx->aux);
     }
-    for (cudaEvent_t e : {ctx->aux_go, ctx->aux_done})
+    for (cudaEvent_t e : {ctx->aux_go, ctx->aux_done, ctx->aux_atoms})
         if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;

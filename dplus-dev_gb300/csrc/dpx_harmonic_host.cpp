@@ -375,10 +375,12 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     const size_t oJn = al16(oGu[0] + (atom_groups_max + 1) * sizeof(int));
     const size_t oT = al16(oJn + (size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double));
     const size_t oMP = al16(oT + (size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float));
-    const size_t max_units = std::max(atom_units_max, vox_units_max);
-    const size_t max_groups = std::max(atom_groups_max, n_vox ? (size_t)nbins : (size_t)0);
-    const size_t oM = al16(oMP + max_units * moments_per_unit);
-    const size_t oCa = al16(oM + max_groups * moments_per_unit);
+    // moments scratch: the voxels' at oMP / oM, the atoms' (on the side
+    // stream, at the same time) at oMPa / oMa
+    const size_t oM = al16(oMP + vox_units_max * moments_per_unit);
+    const size_t oMPa = al16(oM + (n_vox ? (size_t)nbins : (size_t)0) * moments_per_unit);
+    const size_t oMa = al16(oMPa + atom_units_max * moments_per_unit);
+    const size_t oCa = al16(oMa + atom_groups_max * moments_per_unit);
     const size_t oCv = al16(oCa + cell_set);
     const size_t total = oCv + (n_vox == 0 ? 0 : cell_set);
     if (cudaError_t e = ctx->harmonic.reserve(total)) {
@@ -403,17 +405,20 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     tb.vinv = reinterpret_cast<const double*>(base + oVi);
     tb.Jn = reinterpret_cast<double*>(base + oJn);
     tb.T = reinterpret_cast<float*>(base + oT);
-    // the tables on the side stream, beside the binning and the moments
-    if (!ctx->aux) DPX_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
-    if (!ctx->aux_go) DPX_CUDA(cudaEventCreateWithFlags(&ctx->aux_go, cudaEventDisableTiming));
-    if (!ctx->aux_done) DPX_CUDA(cudaEventCreateWithFlags(&ctx->aux_done, cudaEventDisableTiming));
-    DPX_CUDA(cudaEventRecord(ctx->aux_go, st));
-    DPX_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->aux_go, 0));
-    DPX_CUDA(dpx::launch_harmonic_tables(ctx->aux, tb));
-    DPX_CUDA(cudaEventRecord(ctx->aux_done, ctx->aux));
     float2* Ca = reinterpret_cast<float2*>(base + oCa);
     float2* Cv = n_vox == 0 ? nullptr : reinterpret_cast<float2*>(base + oCv);
     DPX_CUDA(cudaMemsetAsync(Ca, 0, cell_set * (n_vox == 0 ? 1 : 2), st));
+    // the side stream: the tables, then the atoms' set, beside the binning and
+    // the voxels' moments (the voxels' contractions wait for aux_done, the
+    // synthesis for aux_atoms)
+    if (!ctx->aux) DPX_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ctx->aux_go, &ctx->aux_done, &ctx->aux_atoms})
+        if (!*e) DPX_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    cudaStream_t ax = ctx->aux;
+    DPX_CUDA(cudaEventRecord(ctx->aux_go, st));
+    DPX_CUDA(cudaStreamWaitEvent(ax, ctx->aux_go, 0));
+    DPX_CUDA(dpx::launch_harmonic_tables(ax, tb));
+    DPX_CUDA(cudaEventRecord(ctx->aux_done, ax));
     auto launch_set = [&](int k) -> int {
         const Set& S = *sets[k];
         if (S.units.empty()) return DPX_OK;
@@ -436,12 +441,12 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         a.lmax = d_lmax;
         a.lmb = reinterpret_cast<const int*>(base + oLb);
         a.aff = reinterpret_cast<const float*>(dbase + t.aff);
-        a.MP = reinterpret_cast<float2*>(base + oMP);
-        a.M = reinterpret_cast<float2*>(base + oM);
+        a.MP = reinterpret_cast<float2*>(base + (k == 0 ? oMPa : oMP));
+        a.M = reinterpret_cast<float2*>(base + (k == 0 ? oMa : oM));
         a.ev0 = ev ? ev[2 * k] : nullptr;
         a.ev1 = ev ? ev[2 * k + 1] : nullptr;
-        a.contract_wait = ctx->aux_done;
-        DPX_CUDA(dpx::launch_harmonic_set(st, a, k == 0 ? Ca : Cv));
+        a.contract_wait = k == 0 ? nullptr : ctx->aux_done;  // the atoms run on the tables' stream
+        DPX_CUDA(dpx::launch_harmonic_set(k == 0 ? ax : st, a, k == 0 ? Ca : Cv));
         return DPX_OK;
     };
     // ---- the voxels: their bin totals (the binning launched first) give the units ----
@@ -473,10 +478,12 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         std::memcpy(ap + (oU[0] - oP[0]), sa.units.data(), sa.units.size() * sizeof(int4));
         std::memcpy(ap + (oG[0] - oP[0]), sa.groups.data(), sa.groups.size() * sizeof(int2));
         std::memcpy(ap + (oGu[0] - oP[0]), sa.gu.data(), sa.gu.size() * sizeof(int));
-        DPX_CUDA(cudaMemcpyAsync(base + oP[0], ap, bytes, cudaMemcpyHostToDevice, st));
-        DPX_CUDA(ctx->pin_atomset.copied(st));
+        DPX_CUDA(cudaMemcpyAsync(base + oP[0], ap, bytes, cudaMemcpyHostToDevice, ax));
+        DPX_CUDA(ctx->pin_atomset.copied(ax));
         if (int rc = launch_set(0)) return rc;
     }
+    DPX_CUDA(cudaEventRecord(ctx->aux_atoms, ax));
+    DPX_CUDA(cudaStreamWaitEvent(st, ctx->aux_atoms, 0));
     // F(0) with the solvent boxes' volumes, summed while the moments run
     const double origin = t.origin + d.scale * box_volume_sum(d);
     if (ev) {

@@ -97,10 +97,11 @@ struct dpx_ctx_s {
     bool closed = false;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
-    // the harmonic fill's radial tables run on aux beside its moments:
-    // aux waits for aux_go (the plan's upload), the contractions for aux_done
+    // the harmonic fill's radial tables and atoms' set run on aux beside the
+    // voxels' moments: aux waits for aux_go (the plan's upload), the voxels'
+    // contractions for aux_done (the tables), the synthesis for aux_atoms
     cudaStream_t aux = nullptr;
-    cudaEvent_t aux_go = nullptr, aux_done = nullptr;
+    cudaEvent_t aux_go = nullptr, aux_done = nullptr, aux_atoms = nullptr;
     int fill_cpt = 8, fill_threads = 128;  // FP32 fill shape (dpx_autotune_fill)
     bool fill_persistent = false;
     int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
