@@ -68,7 +68,10 @@ int dpx_version(void);
 /* ---- context: one device, one stream, grow-only device scratch ---- */
 int dpx_ctx_create(int device, dpx_ctx* out);
 int dpx_ctx_destroy(dpx_ctx ctx);
-/* Use an external cudaStream_t (NULL = the context's own stream). */
+/* Use an external cudaStream_t (NULL = the context's own stream).  The
+ * harmonic fill also runs its radial tables and its atoms' moments on a second
+ * stream the context owns, forked from and joined back into this one by
+ * events; the fill returns with both drained. */
 int dpx_ctx_set_stream(dpx_ctx ctx, void* stream);
 void* dpx_ctx_get_stream(dpx_ctx ctx);
 int dpx_ctx_synchronize(dpx_ctx ctx);
