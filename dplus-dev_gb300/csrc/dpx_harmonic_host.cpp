@@ -416,6 +416,18 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
         if (!*e) DPX_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     cudaStream_t ax = ctx->aux;
     DPX_CUDA(cudaEventRecord(ctx->aux_go, st));
+    // from here on every return joins the side stream back into st, so that a
+    // later call's staging on st cannot overwrite the arena while the tables or
+    // the atoms' set still use it
+    struct JoinAux {
+        cudaStream_t st, ax;
+        cudaEvent_t ev;
+        bool joined = false;
+        ~JoinAux() {
+            if (joined) return;
+            if (cudaEventRecord(ev, ax) == cudaSuccess) cudaStreamWaitEvent(st, ev, 0);
+        }
+    } join{st, ax, ctx->aux_atoms};
     DPX_CUDA(cudaStreamWaitEvent(ax, ctx->aux_go, 0));
     DPX_CUDA(dpx::launch_harmonic_tables(ax, tb));
     DPX_CUDA(cudaEventRecord(ctx->aux_done, ax));
@@ -484,6 +496,7 @@ int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const
     }
     DPX_CUDA(cudaEventRecord(ctx->aux_atoms, ax));
     DPX_CUDA(cudaStreamWaitEvent(st, ctx->aux_atoms, 0));
+    join.joined = true;
     // F(0) with the solvent boxes' volumes, summed while the moments run
     const double origin = t.origin + d.scale * box_volume_sum(d);
     if (ev) {

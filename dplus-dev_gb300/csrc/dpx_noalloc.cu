@@ -12,7 +12,7 @@
 // The kernels are the same as dpx_orientation_average's; only where their
 // bracket tables and per-chunk partial sums live differs.
 #include "dpx.h"
-#include "dpx_internal.h"
+#include "dpx_host.h"
 
 #include <cuda_runtime.h>
 
@@ -89,25 +89,13 @@ extern "C" int dpx_mc_average_noalloc(const void* grid_cells, int grid_size, dou
     if (Q[nq - 1] > G.L * G.step * (1.0 + 1e-12)) return dpx::set_error(DPX_ERR_ARG, "q beyond the grid's qmax");
 
     // bracket tables, as dpx_orientation_average builds them
-    std::vector<int> layer_of_q(nq);
-    dpx::q_brackets(grid_size, qmax, nq, Q, layer_of_q.data());
-    std::vector<int> br_layer, br_off{0}, br_qidx;
-    std::vector<double> br_q;
-    int max_q = 1;
-    for (int l = 0; l < G.L; ++l) {
-        int cnt = 0;
-        for (int k = 0; k < nq; ++k)
-            if (layer_of_q[k] == l) {
-                br_q.push_back(Q[k]);
-                br_qidx.push_back(k);
-                cnt++;
-            }
-        if (cnt) {
-            br_layer.push_back(l);
-            br_off.push_back((int)br_q.size());
-            if (cnt > max_q) max_q = cnt;
-        }
-    }
+    dpxh::Brackets B;
+    dpxh::make_brackets(G, grid_size, qmax, nq, Q, B);
+    const std::vector<int>& br_layer = B.layer;
+    const std::vector<int>& br_off = B.off;
+    const std::vector<int>& br_qidx = B.qidx;
+    const std::vector<double>& br_q = B.q;
+    const int max_q = B.max_q;
     dpx::AvgPlan plan{};
     plan.n_brackets = (int)br_layer.size();
     plan.max_q = max_q;

@@ -59,11 +59,21 @@ def build_libdpx(force: bool = False) -> str:
     return LIB_PATH
 
 
+def reference_root() -> str | None:
+    """The reference checkout the oracle's pin library is built from:
+    DPX_REF_ROOT, else a checkout named ``reference`` beside this repository;
+    None where neither exists (the GPU machine runs without it)."""
+    for cand in (os.environ.get("DPX_REF_ROOT"), os.path.join(os.path.dirname(REPO_DIR), "reference")):
+        if cand and os.path.isdir(os.path.join(cand, "Backend")):
+            return cand
+    return None
+
+
 def build_oracle(with_reference: bool = True) -> None:
     """Compile the CPU oracle (test infrastructure) and, where the reference
     checkout exists, the reference-backed pin library."""
     oracle_dir = os.path.join(REPO_DIR, "oracle")
     subprocess.run(["make", "-s", "-C", oracle_dir], check=True)
-    ref_root = os.environ.get("DPX_REF_ROOT", "/root/reference")
-    if with_reference and os.path.isdir(ref_root):
+    ref_root = reference_root()
+    if with_reference and ref_root:
         subprocess.run(["make", "-s", "-C", oracle_dir, "ref", f"REF_ROOT={ref_root}"], check=True)

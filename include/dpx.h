@@ -477,7 +477,10 @@ int dpx_server_destroy(dpx_server s);
  * Requests needing more (about 8 B x brackets x ceil(n_samples/128) x max q per
  * bracket) return DPX_ERR_ARG.  The first call on a device looks up the scratch
  * array's device address (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture.  All calls on a device share the
+ * that first call before any stream capture.  The address is kept per device
+ * ordinal, i.e. for the CUDA runtime's primary context of that device: callers
+ * that switch the thread to another driver-API context of the same device must
+ * not use this entry point there.  All calls on a device share the
  * array and it keeps the last call's contents: calls whose work overlaps on the
  * GPU (different streams, or different host threads) race on it and must be
  * serialized by the caller. */

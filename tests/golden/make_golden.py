@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures under tests/golden/ from the reference checkout.
 
-Run in a container that holds the reference (default /root/reference, or
-DPX_REF_ROOT); the GPU machine and the tests only read the committed JSON files.
+Run in a container that holds the reference checkout, given as the first
+argument (or DPX_REF_ROOT); the GPU machine and the tests only read the committed JSON files.
 
 * grid_index.json   — cell index <-> (i, j, k) <-> (q, theta, phi) from the
   reference's own Python Grid class (PythonInterface/dplus/Amplitudes.py:48-200).
@@ -19,7 +19,9 @@ import os
 import re
 import sys
 
-REF = os.environ.get("DPX_REF_ROOT", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DPX_REF_ROOT", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: %s REFERENCE_ROOT (or set DPX_REF_ROOT)" % sys.argv[0])
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIX = os.path.join(REF, "PythonInterface/tests/reviewer_tests/files_for_tests/generate/cpu/short")
 

@@ -1,7 +1,7 @@
 """Regenerate tests/golden/lysozyme.json from the reference's lysozyme example.
 
-Run in a container that holds the reference (default /root/reference, or
-DPX_REF_ROOT); the GPU machine and the tests only read the committed JSON file.
+Run in a container that holds the reference checkout, given as the first
+argument (or DPX_REF_ROOT); the GPU machine and the tests only read the committed JSON file.
 
 Source: "Example Files/Examples/CPU/Fast_CPU/6_Lysozyme/" of the reference:
 
@@ -21,9 +21,12 @@ from __future__ import annotations
 
 import json
 import os
+import sys
 import re
 
-REF = os.environ.get("DPX_REF_ROOT", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DPX_REF_ROOT", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: %s REFERENCE_ROOT (or set DPX_REF_ROOT)" % sys.argv[0])
 HERE = os.path.dirname(os.path.abspath(__file__))
 EX = os.path.join(REF, "Example Files", "Examples", "CPU", "Fast_CPU", "6_Lysozyme")
 

@@ -59,9 +59,12 @@ def test_noalloc_rejects_requests_beyond_its_scratch(ctx):
     import torch
     amp = globule(100, 0.8, seed=78)
     grid = amp.calculateGrid(ctx, 4.0, 40, M.FP32)
-    Q = np.linspace(0, 4.0, 400)
-    n = 4_000_000  # about 40 MB of partial sums: above the static limit
-    d_dirs = torch.zeros((1, 2), dtype=torch.float64, device="cuda")
+    # few samples but 400,000 q values over 20 brackets: about 42 MB of partial
+    # sums, above the static limit.  Every buffer is backed in full, so even a
+    # request that slipped past the check would read and write valid memory.
+    Q = np.linspace(0, 4.0, 400_000)
+    n = 1000
+    d_dirs = torch.from_numpy(M.mc_directions(9, n)).cuda()
     d_res = torch.zeros(len(Q), dtype=torch.float64, device="cuda")
     rc = dpx.lib().dpx_mc_average_noalloc(C.c_void_p(grid.device_ptr), 40, 4.0, M.FP32, len(Q), _lib.dptr(Q),
                                           C.c_void_p(d_dirs.data_ptr()), n, 0.0, C.c_void_p(d_res.data_ptr()), None)
