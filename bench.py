@@ -390,8 +390,8 @@ def run_dpx(args):
         }
         if tune:
             out["autotune"] = tune
-        if args.check_error:
-            out["max_rel_err_vs_fp64"] = fp64_error(ctx, amp, Q, dirs, I_fp32)
+        if not args.no_error:
+            out.update(error_report(ctx, stream, amp, Q, dirs, d_dirs, I_fp32, grid, dev_ms / args.steps))
         if not args.no_cpu_baseline and world == 1:
             out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     grid.close()
@@ -770,12 +770,73 @@ def max_over_ranks(ms, world):
     return out if isinstance(ms, (list, tuple)) else out[0]
 
 
-def fp64_error(ctx, amp, Q, dirs, I32):
-    """FP32-bulk I(q) against the plain FP64 GPU path on the same inputs."""
+DIRECT_Q_STRIDE, DIRECT_DIRS = 25, 2000
+
+
+def error_report(ctx, stream, amp, Q, dirs, d_dirs, I32, grid32, ms32):
+    """The error every result reports, and the plain FP64 GPU path beside it.
+
+    (1) The plain FP64 path on the same inputs (FP64 direct-sum fill with the
+    solvent boxes, FP64 splines and Monte Carlo average over the same 1e5
+    directions), timed as one solve with CUDA events: max relative I(q) error
+    of the FP32-bulk result against it, and its solves/s.
+    (2) The FP64 direct sum with no grid (dpx_direct_intensity) at every 25th
+    q and the first 2,000 directions, against the FP32 grid and the FP64 grid
+    averaged over the same sample: the FP32 figure is what the result reports;
+    the FP64 grid's shows how much of it is the grid method's own
+    (interpolation) error."""
+    import ctypes as C
+    import torch
+    from dpx import _lib
     from dpx import models as M
-    dom = M.DomainModel([amp], GRID_SIZE, QMAX, M.FP64)
-    I64 = dom.CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
-    return float(np.max(np.abs(I32 - I64) / np.abs(I64)))
+    L = M.lib()
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))  # noqa: E731
+    g64 = M.Grid(ctx, GRID_SIZE, QMAX, M.FP64)
+    gh = (C.c_void_p * 1)(g64.handle.value)
+    desc, keep = M.pdb_descs([amp])
+    I64 = np.zeros(len(Q))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    _lib.check(L.dpx_grid_fill_pdb_batch(1, gh, desc))
+    _lib.check(L.dpx_grid_compute_splines(g64.handle))
+    _lib.check(L.dpx_orientation_average(ctx.handle, 1, gh, None, None, None, None, None, None, len(Q), _lib.dptr(Q),
+                                         C.c_void_p(d_dirs.data_ptr()), 1, 0, len(dirs), 0.0, _lib.dptr(I64)))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1)
+    Qs = np.ascontiguousarray(Q[12::DIRECT_Q_STRIDE])
+    ds = np.ascontiguousarray(dirs[:DIRECT_DIRS])
+
+    def sample_average(g):
+        r = np.zeros(len(Qs))
+        h = (C.c_void_p * 1)(g.handle.value)
+        _lib.check(L.dpx_orientation_average(ctx.handle, 1, h, None, None, None, None, None, None, len(Qs),
+                                             _lib.dptr(Qs), ds.ctypes.data_as(C.c_void_p), 0, 0, len(ds), 0.0,
+                                             _lib.dptr(r)))
+        return r
+
+    a32, a64 = sample_average(grid32), sample_average(g64)
+    g64.close()
+    direct = np.zeros(len(Qs))
+    desc[0].center = None  # the frame as given
+    t0 = time.perf_counter()
+    _lib.check(L.dpx_direct_intensity(ctx.handle, desc, 0, None, None, len(Qs), _lib.dptr(Qs), len(ds),
+                                      _lib.dptr(ds), _lib.dptr(direct)))
+    t_direct = time.perf_counter() - t0
+    del keep
+    return {"max_rel_err_vs_fp64": rel(I32, I64),
+            "max_rel_err_vs_direct_sum": rel(a32, direct),
+            "error": {"vs_fp64": "FP32-bulk I(q) against the plain FP64 GPU path, all %d q, the same %d directions"
+                                 % (len(Q), len(dirs)),
+                      "vs_direct_sum": "FP64 direct sum (no grid, dpx_direct_intensity) at %d q (every %dth) x the "
+                                       "first %d directions, against the grid averaged over the same sample"
+                                       % (len(Qs), DIRECT_Q_STRIDE, len(ds)),
+                      "fp32_grid_vs_direct_sum": rel(a32, direct), "fp64_grid_vs_direct_sum": rel(a64, direct),
+                      "direct_sum_s": t_direct},
+            "fp64_plain": {"ms_per_solve": ms64, "solves_per_s": 1e3 / ms64, "speedup_fp32_vs_fp64": ms64 / ms32,
+                           "note": "plain FP64 GPU path (FP64 direct-sum fill, splines, MC average), same inputs, "
+                                   "one solve timed with CUDA events"}}
 
 
 def _every(s, k):
@@ -791,6 +852,43 @@ def _every(s, k):
     return O.Struct(np.concatenate(xyz), api, s.coeffs, s.rads, s.flags, s.sol_ed, s.c1, s.scale, boxes)
 
 
+_CPU_STRUCT = None
+
+
+def cpu_struct():
+    """The workload's leaf for the CPU baseline, built without libdpx: the
+    oracle's globule generator (the library's dpx_make_globule, bit for bit),
+    the form-factor tables of dpx.elements (Python data), and the oracle's
+    numpy voxelizer for the solvation layer (box for box the library's C++
+    voxelizer).  Built once per process (about 20 s of host work, outside
+    every timed sample)."""
+    global _CPU_STRUCT
+    if _CPU_STRUCT is None:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        import voxel as OV
+        from dpx import models as M
+        from dpx.elements import GLOBULE_CODES
+        el, xyz = O.make_globule(N_ATOMS, RADIUS, SEED)
+        amp = M.PDBAmplitude([GLOBULE_CODES[e] for e in el], xyz.astype(np.float64), EXTRA)
+        ec, ed, lc, ld, _ = OV.voxel_solvent(amp.xyz, amp.atom_radii(), amp.voxelStep, amp.solventRad,
+                                             amp.solvationThickness, amp.fillHoles)
+        step = np.float32(amp.voxelStep)
+        parts = []
+        for on, com, dims, w in ((amp.voxel_excluded, ec, ed, -amp.solventED),
+                                 (amp.voxel_layer, lc, ld, amp.outerSolventED - amp.solventED)):
+            if on and len(com):
+                b = np.zeros((len(com), 8), dtype=np.float32)
+                b[:, :3] = com
+                b[:, 3] = np.float32(w)
+                b[:, 4:7] = step * dims.astype(np.float32)
+                parts.append(b)
+        boxes = np.concatenate(parts) if parts else None
+        _CPU_STRUCT = O.Struct(amp.xyz, amp.atoms_per_ion, amp.coeffs, amp.ion_rads, amp.flags, amp.solventED,
+                               amp.c1, amp.scale, boxes)
+    return _CPU_STRUCT
+
+
 def cpu_baseline(seconds: float):
     """The reference's CPU algorithm (oracle, reference-exact precision, all host
     threads) on a bounded sample: the outermost shell of the grid fill for every
@@ -800,8 +898,7 @@ def cpu_baseline(seconds: float):
     average is < 1 % of a CPU solve."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    amp, Q, dirs = build_inputs()
-    s = O.Struct.from_pdb(amp)
+    s = cpu_struct()
     Lp = GRID_SIZE // 2 + 3
     cores = os.cpu_count() or 1
     P = O.grid_cells(GRID_SIZE)
@@ -831,7 +928,8 @@ def cpu_baseline(seconds: float):
             "sample": f"outer shell of the grid fill ({cells} cells) for every {k}-th atom and solvent box "
                       f"({points(sample)} of {points(s)} points, {dt:.1f} s), scaled by point-cell pairs to "
                       f"{P} cells; splines timed in full ({t_spl:.1f} s); orientation average not included "
-                      f"(<1%); voxelization (host, once per structure) not included"}
+                      f"(<1%); voxelization (host, once per structure) not included; inputs built without the "
+                      f"library (oracle globule generator and numpy voxelizer)"}
 
 
 def run_reference(args):
@@ -866,7 +964,8 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="sweep the fill shapes first and use the fastest")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--check-error", action="store_true")
+    ap.add_argument("--no-error", action="store_true",
+                    help="skip the error report (plain FP64 solve and FP64 direct-sum sample)")
     ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
     ap.add_argument("--workload", default="subunit", choices=["subunit", "batch", "serve", "assembly"])
     ap.add_argument("--no-extras", action="store_true", help="assembly: skip the VEGAS / GK / FP64 extras")
@@ -880,6 +979,7 @@ def main():
     if args.profile_shape:
         apply_profile_shape(args.profile_shape)
         args.no_cpu_baseline = True
+        args.no_error = True
     if args.impl == "reference":
         out = run_reference(args)
     else:

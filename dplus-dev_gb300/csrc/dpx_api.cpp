@@ -200,7 +200,8 @@ void ctx_release(dpx_ctx ctx) {
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
-                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels, &ctx->dirsort})
+                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels, &ctx->dirsort,
+                      &ctx->direct})
         b->release();
     for (DevBuf& b : ctx->leaf_boxes) b.release();
     ctx->pin_plan.release();

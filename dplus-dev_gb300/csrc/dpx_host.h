@@ -116,6 +116,7 @@ struct dpx_ctx_s {
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
     dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
     dpxh::DevBuf dirsort;  // the average's angular-order scratch
+    dpxh::DevBuf direct;   // the FP64 direct sum's tables and partial amplitudes
     dpxh::HostPinned pin_plan, pin_totals, pin_small, pin_units, pin_atomset;  // the harmonic fill's host staging
     std::vector<dpxh::DevBuf> leaf_boxes;  // the harmonic fill's solvent boxes, per leaf of a batch
     std::vector<char> host_stage;

@@ -331,6 +331,22 @@ int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
                              const double* const* inD, const double* trans, const double* rots, int numGrids,
                              double* outAmpData, int precision, int* pStop);
 
+/* ---- FP64 direct-sum orientation average: the error reference of every grid
+ * result (no counterpart as one call in the reference; it evaluates
+ * PDBAmplitude::calcAmplitude, Backend/Backend/PDBAmplitude.cpp:243-317, with
+ * its solvent boxes :277-314, point by point in FP64, with no grid) ----
+ *   I(q_k) = (1/D) sum_d |F(q_k n_d)|^2,
+ *   F(q) = scale [sum_u aff_u(|q|) sum_{j in u} e^{i q.r_j}
+ *                 + sum_b w_b prod_a L_a sinc(q_a L_a / 2) e^{i q.c_b}]
+ * for the leaf d (host atoms and boxes, in the frame given: no centring), or
+ * with n_copies > 0 the docked sum sum_c e^{i q.t_c} F(R_c^T q) (copy_rot
+ * [3 n] radians as EulerD, copy_tr [3 n] nm; ManualSymmetry, Symmetries.cpp:
+ * 1079-1166).  Q [nq] any order; dirs [D] (theta, phi) pairs, host; res [nq]
+ * host.  FP64 throughout, deterministic (fixed-order sums); cost N x nq x D
+ * FP64 sincos, so callers use it on a sample of q values and directions. */
+int dpx_direct_intensity(dpx_ctx ctx, const dpx_pdb_desc* d, int n_copies, const double* copy_rot,
+                         const double* copy_tr, int nq, const double* Q, int64_t D, const double* dirs, double* res);
+
 /* SFU calibration (no counterpart in the reference): times a kernel of
  * independent __sincosf chains and returns the MUFU operations per second this
  * GPU sustains (sin and cos count one each) — the denominator of the amplitude

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <array>
 #include <climits>
+#include <unordered_map>
 #include <omp.h>
 
 namespace {
@@ -801,11 +802,37 @@ int orc_integrate_layers(int grid_size, double qmax, int n_leaves, const orc_lea
     return 0;
 }
 
+namespace {
+/* The voxelized-solvent boxes' amplitude at q in FP64 (PDBAmplitude.cpp:277-314,
+ * the FP64 branch of orc_grid_add_boxes_shells), times scale. */
+cd boxes_fp64(int64_t n_boxes, const float* boxes, double scale, double qx, double qy, double qz) {
+    const double q[3] = {qx, qy, qz};
+    double re = 0, im = 0;
+    for (int64_t b = 0; b < n_boxes; b++) {
+        const float* B = boxes + 8 * b;
+        double va = B[3], ph = 0;
+        for (int a = 0; a < 3; a++) {
+            const double L = B[4 + a], x = 0.5 * q[a] * L;
+            va *= L * (x == 0.0 ? 1.0 : std::sin(x) / x);
+            ph += q[a] * double(B[a]);
+        }
+        re += va * std::cos(ph);
+        im += va * std::sin(ph);
+    }
+    return cd(re, im) * scale;
+}
+}  // namespace
+
 void orc_direct_intensity(int64_t N, const double* xyz, int U, const int* atoms_per_ion, const double* coeffs,
-                          const double* ion_rads, int flags, double sol_ed, double c1, double scale, int n_copies,
-                          const double* copy_rot, const double* copy_tr, int nq, const double* Q, int64_t D,
-                          const double* dirs, int nthreads, double* res) {
+                          const double* ion_rads, int flags, double sol_ed, double c1, double scale, int64_t n_boxes,
+                          const float* boxes, int n_copies, const double* copy_rot, const double* copy_tr, int nq,
+                          const double* Q, int64_t D, const double* dirs, int nthreads, double* res) {
     Structure s{N, xyz, U, atoms_per_ion, coeffs, ion_rads, flags, sol_ed, c1, scale};
+    auto leaf_amp = [&](double rm_, double qx, double qy, double qz) {
+        cd f = amp_fp64(s, rm_, qx, qy, qz);
+        if (n_boxes > 0) f += boxes_fp64(n_boxes, boxes, scale, qx, qy, qz);
+        return f;
+    };
     double rm = mean_radius<double>(U, atoms_per_ion, ion_rads);
     std::vector<std::array<double, 9>> Rk;
     for (int c = 0; c < n_copies; c++) {
@@ -823,12 +850,12 @@ void orc_direct_intensity(int64_t N, const double* xyz, int U, const int* atoms_
             double q = Q[k];
             cd F(0, 0);
             if (n_copies == 0) {
-                F = amp_fp64(s, rm, q * n[0], q * n[1], q * n[2]);
+                F = leaf_amp(rm, q * n[0], q * n[1], q * n[2]);
             } else {
                 for (int c = 0; c < n_copies; c++) {
                     double nn[3];
                     row_times(n, Rk[c].data(), nn);
-                    cd f = amp_fp64(s, rm, q * nn[0], q * nn[1], q * nn[2]);
+                    cd f = leaf_amp(rm, q * nn[0], q * nn[1], q * nn[2]);
                     double a = q * (n[0] * copy_tr[3 * c] + n[1] * copy_tr[3 * c + 1] + n[2] * copy_tr[3 * c + 2]);
                     F += f * std::exp(cd(0., 1.) * a);
                 }
@@ -1105,6 +1132,73 @@ double orc_gk_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf
     GKCtx C{&models};
     /* GaussKron2DSphereRecurs (Amplitude.cpp:1416-1419): theta in [0, pi/2], / 2pi */
     return gk_theta(C, q, 0.0, kPi / 2, eps, max_depth - 1, -1) / (2.0 * kPi);
+}
+
+/* Synthetic workload structures: the seeded globule every configuration is
+ * built from (a self-avoiding random walk of 0.15 nm steps folded into a
+ * sphere, no two atoms closer than 0.1 nm, elements C 63 / N 17 / O 19 / S 1 %),
+ * the same generator the library's dpx_make_globule runs, so that the CPU
+ * baseline builds its inputs without loading the library. */
+int orc_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xyz, int* elem) {
+    if (n_atoms <= 0 || !(radius_nm > 0) || !xyz || !elem) return -1;
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U01(0.0, 1.0);
+    const double step = 0.15, min_d = 0.1, cell = 0.2, R = radius_nm;
+    const int64_t nc = (int64_t)std::ceil(2 * R / cell) + 2;
+    auto cell_of = [&](double v) { return (int64_t)std::floor((v + R) / cell) + 1; };
+    std::unordered_map<int64_t, std::vector<int64_t>> cells;
+    cells.reserve((size_t)n_atoms * 2);
+    auto free_at = [&](double x, double y, double z) {
+        const int64_t ix = cell_of(x), iy = cell_of(y), iz = cell_of(z);
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dz = -1; dz <= 1; ++dz) {
+                    auto it = cells.find(((ix + dx) * nc + (iy + dy)) * nc + (iz + dz));
+                    if (it == cells.end()) continue;
+                    for (int64_t j : it->second) {
+                        const double ex = xyz[3 * j] - x, ey = xyz[3 * j + 1] - y, ez = xyz[3 * j + 2] - z;
+                        if (ex * ex + ey * ey + ez * ez < min_d * min_d) return false;
+                    }
+                }
+        return true;
+    };
+    double px = 0, py = 0, pz = 0;
+    for (int64_t i = 0; i < n_atoms; ++i) {
+        double x = px, y = py, z = pz;
+        if (i > 0) {
+            bool placed = false;
+            for (int attempt = 0; attempt < 64 && !placed; ++attempt) {
+                const double ct = 2 * U01(rng) - 1, ph = 2 * kPi * U01(rng), st = std::sqrt(1 - ct * ct);
+                x = px + step * st * std::cos(ph);
+                y = py + step * st * std::sin(ph);
+                z = pz + step * ct;
+                if (x * x + y * y + z * z > R * R) continue;
+                placed = free_at(x, y, z);
+            }
+            if (!placed) {  /* a dead end restarts the walk at a random free point */
+                for (int attempt = 0; attempt < 100000; ++attempt) {
+                    x = (2 * U01(rng) - 1) * R;
+                    y = (2 * U01(rng) - 1) * R;
+                    z = (2 * U01(rng) - 1) * R;
+                    if (x * x + y * y + z * z <= R * R && free_at(x, y, z)) {
+                        placed = true;
+                        break;
+                    }
+                }
+                if (!placed) return -1;
+            }
+        }
+        xyz[3 * i] = (float)x;
+        xyz[3 * i + 1] = (float)y;
+        xyz[3 * i + 2] = (float)z;
+        cells[(cell_of(x) * nc + cell_of(y)) * nc + cell_of(z)].push_back(i);
+        px = x;
+        py = y;
+        pz = z;
+        const double r = U01(rng);
+        elem[i] = r < 0.63 ? 0 : (r < 0.80 ? 1 : (r < 0.99 ? 2 : 3));
+    }
+    return 0;
 }
 
 }  // extern "C"

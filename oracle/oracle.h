@@ -130,11 +130,15 @@ void orc_assemble_grid(int grid_size, double qmax, int n_leaves, const orc_leaf*
                        double scale, int nthreads, double* out);
 
 /* ---- FP64 direct-sum oracle (no grid) ----
- * F(q n) = sum_j f_j(q) e^{i q n.r_j} for a placed leaf with optional docked
- * copies; I(q) = mean over the given directions of |F|^2. */
+ * F(q n) = scale [sum_j f_j(q) e^{i q n.r_j} + sum_b w_b prod_a L_a sinc(q_a L_a/2)
+ * e^{i q n.c_b}] for a leaf (PDBAmplitude::calcAmplitude, PDBAmplitude.cpp:243-317,
+ * every float promoted to double) with optional voxelized-solvent boxes
+ * {cx, cy, cz, w, Lx, Ly, Lz, 0} and docked copies (sum_c e^{i q n.t_c}
+ * F(R_c^T q n), Symmetries.cpp:1079-1166); I(q) = mean over the given
+ * directions of |F|^2. */
 void orc_direct_intensity(int64_t N, const double* xyz, int U, const int* atoms_per_ion,
                           const double* coeffs, const double* ion_rads, int flags,
-                          double sol_ed, double c1, double scale,
+                          double sol_ed, double c1, double scale, int64_t n_boxes, const float* boxes,
                           int n_copies, const double* copy_rot, const double* copy_tr,
                           int nq, const double* Q, int64_t D, const double* dirs,
                           int nthreads, double* res);
@@ -150,6 +154,13 @@ double orc_gk_intensity(int grid_size, double qmax, int n_leaves, const orc_leaf
 void orc_debye(int64_t N, const double* xyz, int U, const int* atoms_per_ion, const double* coeffs,
                const double* ion_rads, int flags, double sol_ed, double c1, const double* bfactor,
                const double* anom, int nq, const double* Q, int mode, int nthreads, double* out);
+
+/* ---- synthetic workload structures (shared by the CPU baseline and the tests) ----
+ * Seeded globule: a self-avoiding walk of 0.15 nm steps folded into a sphere of
+ * radius_nm, elements C 63 / N 17 / O 19 / S 1 % (codes 0..3); the generator of
+ * the library's dpx_make_globule.  Returns 0, or -1 when the sphere cannot hold
+ * the atoms. */
+int orc_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xyz, int* elem);
 
 #ifdef __cplusplus
 }

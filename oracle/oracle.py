@@ -70,7 +70,8 @@ def lib():
                                            C.c_int64, C.c_int64, C.c_double, C.c_int, _D]
         L.orc_q_brackets.argtypes = [C.c_int, C.c_double, C.c_int, _D, _I]
         L.orc_direct_intensity.argtypes = [C.c_int64, _D, C.c_int, _I, _D, _D, C.c_int, C.c_double, C.c_double,
-                                           C.c_double, C.c_int, _D, _D, C.c_int, _D, C.c_int64, _D, C.c_int, _D]
+                                           C.c_double, C.c_int64, _F, C.c_int, _D, _D, C.c_int, _D, C.c_int64, _D,
+                                           C.c_int, _D]
         L.orc_debye.argtypes = [C.c_int64, _D, C.c_int, _I, _D, _D, C.c_int, C.c_double, C.c_double, _D, _D,
                                 C.c_int, _D, C.c_int, C.c_int, _D]
         L.orc_gk_intensity.restype = C.c_double
@@ -118,6 +119,19 @@ class Struct:
     def from_pdb(cls, amp):
         return cls(amp.xyz, amp.atoms_per_ion, amp.coeffs, amp.ion_rads, amp.flags, amp.solventED, amp.c1,
                    amp.scale, getattr(amp, "solvent_boxes", lambda: None)())
+
+
+def make_globule(n_atoms, radius_nm, seed):
+    """(element codes 0..3 for C, N, O, S, xyz [n, 3] float32 nm) of the seeded
+    globule generator, without the library."""
+    L = lib()
+    L.orc_make_globule.restype = C.c_int
+    L.orc_make_globule.argtypes = [C.c_int64, C.c_double, C.c_uint64, _F, _I]
+    xyz = np.empty((n_atoms, 3), dtype=np.float32)
+    el = np.empty(n_atoms, dtype=np.int32)
+    if L.orc_make_globule(n_atoms, radius_nm, seed, xyz.ctypes.data_as(_F), el.ctypes.data_as(_I)) != 0:
+        raise ValueError("globule of radius %g nm cannot hold %d atoms" % (radius_nm, n_atoms))
+    return el, xyz
 
 
 def grid_cells(grid_size):
@@ -224,12 +238,17 @@ def integrate_layers(grid_size, qmax, leaves, Q, dirs, dir_layer_stride, max_ite
 
 
 def direct_intensity(s: Struct, Q, dirs, copy_rot=None, copy_tr=None, nthreads=0):
+    """FP64 direct sum (no grid) at the given directions, with the leaf's
+    solvent boxes and optional docked copies (radians, nm)."""
     Q = np.ascontiguousarray(Q, dtype=np.float64)
     dirs = np.ascontiguousarray(dirs, dtype=np.float64)
     res = np.zeros(len(Q))
     nc = 0 if copy_rot is None else len(np.ravel(copy_rot)) // 3
+    nb = 0 if s.boxes is None else len(s.boxes)
+    bx = None if s.boxes is None else s.boxes.ctypes.data_as(_F)
     lib().orc_direct_intensity(len(s.xyz), _d(s.xyz), len(s.api), s.api.ctypes.data_as(_I), _d(s.coeffs),
-                               _d(s.rads), s.flags, s.sol_ed, s.c1, s.scale, nc, _d(copy_rot), _d(copy_tr), len(Q),
+                               _d(s.rads), s.flags, s.sol_ed, s.c1, s.scale, nb, bx, nc, _d(copy_rot), _d(copy_tr),
+                               len(Q),
                                Q.ctypes.data_as(_D), len(dirs), dirs.ctypes.data_as(_D), nthreads,
                                res.ctypes.data_as(_D))
     return res

@@ -61,3 +61,16 @@ def test_request_stream_shape():
             assert base.leaf is r.leaf and base.grid_size == r.grid_size and r.repeat_of < j
         assert r.Q[-1] <= r.qmax + 1e-12
     assert 0 < sum(r.repeat_of >= 0 for r in s) < len(s)
+
+
+def test_oracle_globule_is_the_library_globule():
+    """The CPU baseline builds its structure with the oracle's generator (no
+    library loaded); it must be the library's globule bit for bit."""
+    import oracle as O
+    from dpx import models as M
+    from dpx.elements import GLOBULE_CODES
+    for n, r, seed in ((2000, 2.5, 20250), (5000, 3.0, 2020), (700, 1.4, 9)):
+        el, xyz = O.make_globule(n, r, seed)
+        sym, xyz_lib = M.make_globule(n, r, seed)
+        assert np.array_equal(xyz.astype(np.float64), xyz_lib)
+        assert [GLOBULE_CODES[e] for e in el] == sym
