@@ -270,6 +270,16 @@ int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns) {
                 poly_columns);
 }
 
+int dpx_ctx_set_convergence(dpx_ctx ctx, int rule, int64_t samples_per_step) {
+    if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
+    if (rule != DPX_CONV_CPU && rule != DPX_CONV_GPU) return fail(DPX_ERR_ARG, "unknown convergence rule %d", rule);
+    if (rule == DPX_CONV_GPU && (samples_per_step < 128 || samples_per_step % 128 != 0))
+        return fail(DPX_ERR_ARG, "samples_per_step must be a positive multiple of 128");
+    ctx->conv_rule = rule;
+    if (rule == DPX_CONV_GPU) ctx->conv_samples = samples_per_step;
+    return DPX_OK;
+}
+
 int dpx_ctx_set_timing(dpx_ctx ctx, int on) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
     ctx->timing = on != 0;
@@ -858,9 +868,11 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
     plan.n_brackets = nbr;
     plan.max_q = max_q;
     plan.n_samples = n_samples;
-    plan.chunk = eps > 0.0 ? 100 : 128;
-    plan.chunk_off = eps > 0.0 ? 99 : 0;
+    const bool gpu_rule = eps > 0.0 && ctx->conv_rule == DPX_CONV_GPU;
+    plan.chunk = eps > 0.0 && !gpu_rule ? 100 : 128;
+    plan.chunk_off = eps > 0.0 && !gpu_rule ? 99 : 0;
     plan.n_chunks = (n_samples + plan.chunk_off + plan.chunk - 1) / plan.chunk;
+    plan.conv_group = gpu_rule ? (int)(ctx->conv_samples / 128) : 0;
     plan.dir_stride = dir_layer_stride;
     plan.need_dir = 0;
     for (const auto& M : md)

@@ -106,6 +106,8 @@ struct dpx_ctx_s {
     bool fill_persistent = false;
     int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
     int fill_method = 1;  // DPX_FILL_HARMONIC (default) / DPX_FILL_DIRECT
+    int conv_rule = 0;              // DPX_CONV_CPU (default) / DPX_CONV_GPU (dpx_ctx_set_convergence)
+    int64_t conv_samples = 8192;    // samples per step of DPX_CONV_GPU
     // stage timing of the last harmonic fill (dpx_ctx_set_timing): events
     // around the moments of the atoms and of the voxels, the synthesis and the
     // whole fill; the points and K of that fill

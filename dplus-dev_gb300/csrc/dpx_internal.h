@@ -75,6 +75,11 @@ struct AvgPlan {
                              // and a shared direction set the samples are taken in an angular order
                              // (the mean is the same; neighbouring threads gather neighbouring cells)
     const int* dir_order;    // the sample order in use (set by launch_average; nullptr: as given)
+    int conv_group;          // eps > 0 only.  0: the reference CPU's convergence test (4-column history
+                             // every 100 samples, AverageIntensitiesBetweenLayers); > 0: the reference
+                             // GPU paths' test (OAJacob.cu:320-337, GPUHybridCalc.cu:705-720) on steps of
+                             // conv_group chunks: after 4 steps, every q of the bracket within eps of its
+                             // mean at each of the 3 steps before
 };
 // Bytes of AvgPlan::sort_scratch for n samples.
 size_t dir_sort_bytes(int64_t n);

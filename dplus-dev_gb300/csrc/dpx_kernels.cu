@@ -873,6 +873,37 @@ __global__ void finalize_kernel(AvgPlan plan, double eps, double* __restrict__ r
     double* run = out;
     double* hist = out + plan.max_q;
     for (int k = 0; k < m; ++k) run[k] = 0.0;
+    if (plan.conv_group > 0) {
+        // the reference GPU paths' test: the running mean after every step of
+        // conv_group chunks; from the 4th step on, converged when every q is
+        // within eps of its mean at each of the three steps before
+        int64_t step = 0;
+        for (int64_t c = 0; c < plan.n_chunks; ++c) {
+            for (int k = 0; k < m; ++k) run[k] += part[c * plan.max_q + k];
+            if ((c + 1) % plan.conv_group != 0 && c + 1 != plan.n_chunks) continue;
+            const int64_t done = min((c + 1) * (int64_t)plan.chunk, plan.n_samples);
+            const int pos = (int)(step % 4);
+            for (int k = 0; k < m; ++k) hist[pos * plan.max_q + k] = run[k] / (double)done;
+            if (step > 2) {
+                bool conv = true;
+                for (int j = 1; conv && j <= 3; ++j) {
+                    const int pj = (int)((step - j) % 4);
+                    for (int k = 0; k < m; ++k)
+                        if (!(fabs(1.0 - hist[pos * plan.max_q + k] / hist[pj * plan.max_q + k]) <= eps)) {
+                            conv = false;
+                            break;
+                        }
+                }
+                if (conv) {
+                    for (int k = 0; k < m; ++k) res[plan.br_qidx[q0 + k]] = hist[pos * plan.max_q + k];
+                    return;
+                }
+            }
+            ++step;
+        }
+        for (int k = 0; k < m; ++k) res[plan.br_qidx[q0 + k]] = run[k] / (double)plan.n_samples;
+        return;
+    }
     for (int64_t c = 0; c < plan.n_chunks; ++c) {
         for (int k = 0; k < m; ++k) run[k] += part[c * plan.max_q + k];
         if (eps > 0.0) {

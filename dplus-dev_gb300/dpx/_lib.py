@@ -18,6 +18,7 @@ DPX_FP32 = 1
 DPX_CALC_ATOMIC_FORMFACTORS = 1
 DPX_CALC_DUMMY_SOLVENT = 2
 DPX_FILL_DIRECT, DPX_FILL_HARMONIC = 0, 1
+DPX_CONV_CPU, DPX_CONV_GPU = 0, 1
 
 _STATUS = {-1: "DPX_ERR_ARG", -2: "DPX_ERR_CUDA", -3: "DPX_ERR_OOM", -4: "DPX_ERR_STOPPED",
            -5: "DPX_ERR_NODEVICE"}
@@ -76,6 +77,7 @@ _SIGS = {
     "dpx_ctx_set_fill_poly": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_set_fill_method": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_get_fill_method": (C.c_int, [_P]),
+    "dpx_ctx_set_convergence": (C.c_int, [_P, C.c_int, C.c_int64]),
     "dpx_ctx_set_timing": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_stage_times": (C.c_int, [_P, _D]),
     "dpx_ctx_get_fill_shape": (C.c_int, [_P, _I]),

@@ -65,6 +65,12 @@ class Context:
     def fill_method(self) -> int:
         return int(lib().dpx_ctx_get_fill_method(self.handle))
 
+    def set_convergence(self, rule: int, samples_per_step: int = 8192) -> None:
+        """Monte Carlo convergence test: _lib.DPX_CONV_CPU (the reference's CPU
+        rule) or _lib.DPX_CONV_GPU (its GPU averages' rule, samples_per_step
+        samples a step: 8192 on the grid path, 4096 on the hybrid path)."""
+        check(lib().dpx_ctx_set_convergence(self.handle, rule, samples_per_step))
+
     def synchronize(self) -> None:
         check(lib().dpx_ctx_synchronize(self.handle))
 
@@ -497,14 +503,15 @@ def _pack_models(placements):
 
 class ManualSymmetry:
     """Docked copies of one child: rows (x, y, z [nm], alpha, beta, gamma [degrees]),
-    as ManualSymmetry::PreCalculate reads them (Symmetries.cpp:670-695).
+    as ManualSymmetry::PreCalculate reads them (Symmetries.cpp:670-695).  The
+    child is a PDB leaf or another ManualSymmetry that uses its grid.
 
     ``use_grid=False`` is the hybrid path: the docked sum is evaluated per
     orientation sample (HybridOA.cu, Symmetries.cpp:1079-1166).  ``use_grid=True``
     builds the assembly grid once (ManualSymmetry::calculateGrid,
     Symmetries.cpp:879-962) and averages it like a leaf."""
 
-    def __init__(self, child: PDBAmplitude, rows: Sequence[Sequence[float]], scale: float = 1.0,
+    def __init__(self, child, rows: Sequence[Sequence[float]], scale: float = 1.0,
                  use_grid: bool = False, location: Sequence[float] = (0, 0, 0, 0, 0, 0)):
         r = np.asarray(rows, dtype=np.float64).reshape(-1, 6)
         self.child = child
@@ -515,6 +522,14 @@ class ManualSymmetry:
         self.location = tuple(float(v) for v in location)
         self._grid = None
         self._grid_key = None
+
+    def hash(self) -> str:
+        """Content key of the assembly: the child's, the rows, scale and placement."""
+        h = hashlib.sha1(self.child.hash().encode())
+        h.update(np.ascontiguousarray(self.trans).tobytes())
+        h.update(np.ascontiguousarray(self.rot).tobytes())
+        h.update(repr((self.scale, self.use_grid, self.location, self.child.location)).encode())
+        return h.hexdigest()
 
     def calculateGrid(self, ctx: Context, qmax: float, gridSize: int, precision: int = FP32) -> Grid:
         child = self.child.calculateGrid(ctx, qmax, gridSize, precision)

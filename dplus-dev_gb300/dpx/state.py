@@ -28,6 +28,7 @@ from typing import Sequence
 
 import numpy as np
 
+from . import _lib
 from . import models as M
 from . import pdb as P
 
@@ -84,9 +85,11 @@ class Job:
         return [(w, M.DomainModel(amps, self.grid_size, self.qmax, precision)) for w, amps in self.populations]
 
     def intensity(self, ctx, Q, dirs=None, precision=M.FP32, seed=0, points_per_iter=4096,
-                  iterations: int | None = None):
+                  iterations: int | None = None, mc_rule: str = "cpu"):
         """I(q) of the state (MC needs the direction set, as dpx's averages take
-        directions explicitly)."""
+        directions explicitly).  ``mc_rule`` picks the Monte Carlo convergence
+        test: "cpu" (the reference's CPU rule) or "gpu" (its GPU averages'
+        rule: 8192 samples a step on the grid path, 4096 on the hybrid path)."""
         Q = np.ascontiguousarray(Q, dtype=np.float64)
         n = self.iterations if iterations is None else int(iterations)
         total = np.zeros(len(Q))
@@ -94,7 +97,14 @@ class Job:
             if self.method == "MC":
                 if dirs is None:
                     raise ValueError("Monte Carlo needs a direction set")
-                I = dom.CalculateIntensityVector(ctx, Q, self.convergence, min(n, len(dirs)), dirs)
+                if mc_rule == "gpu":
+                    hybrid = any(isinstance(a, M.ManualSymmetry) and not a.use_grid for a in dom.amps)
+                    ctx.set_convergence(_lib.DPX_CONV_GPU, 4096 if hybrid else 8192)
+                try:
+                    I = dom.CalculateIntensityVector(ctx, Q, self.convergence, min(n, len(dirs)), dirs)
+                finally:
+                    if mc_rule == "gpu":
+                        ctx.set_convergence(_lib.DPX_CONV_CPU)
             elif self.method == "VEGAS":
                 I = dom.CalculateIntensityVector(ctx, Q, self.convergence, n, method="VEGAS", seed=seed,
                                                  points_per_iter=points_per_iter)
@@ -133,10 +143,24 @@ class _Decoder:
         raise NotImplementedError(f"model type {t!r} is outside the scattering path (geometric form factors, "
                                   "Lua-scripted symmetries and electron PDBs are not carried)")
 
-    def node(self, node, copies=None, grid_ok=True):
-        """Amplitudes of one node; ``copies`` = [(R, t)] applied above it."""
+    def grid_subtree(self, node) -> bool:
+        """The node and every node under it use grids (the reference's
+        GetUseGridWithChildren); with the preferences' UseGrid off nothing does."""
+        return (self.use_grid and bool(node.get("Use_Grid", True))
+                and all(self.grid_subtree(c) for c in node.get("Children", [])))
+
+    def node(self, node, copies=None):
+        """Amplitudes of one node; ``copies`` = [(R, t)] applied above it.
+
+        As the reference's hybrid FlattenTree (Backend/Backend/Amplitude.cpp:
+        577-691) does, a ManualSymmetry whose subtree uses grids stays one
+        object: its assembly grid (ManualSymmetry::calculateGrid over its
+        children's grids, Symmetries.cpp:879-962); the copies above it dock that
+        grid per orientation.  A symmetry that does not use grids is flattened:
+        its rows (and its own placement) compose into the copies of its
+        children."""
         t = node.get("Type")
-        if t == ",26":  # ManualSymmetry: compose its rows (and its own placement) into the copies
+        if t == ",26":
             rows = np.asarray(node.get("Parameters", []), dtype=np.float64).reshape(-1, 6)
             Rn, tn = _transform(_location(node))
             scale = float((node.get("ExtraParameters") or [1.0])[0])
@@ -144,10 +168,19 @@ class _Decoder:
             for r in rows:
                 Rr = _euler_matrix(*np.radians(r[3:6]))
                 mine.append((Rn @ Rr, Rn @ r[:3] + tn))
+            if self.grid_subtree(node):
+                # one assembly grid of this node's rows over each child's grid
+                out = []
+                for child in node.get("Children", []):
+                    for kid in self.node(child, None):
+                        g = M.ManualSymmetry(kid, _rows(mine), scale=scale, use_grid=True)
+                        out.append(g if copies is None else
+                                   M.ManualSymmetry(g, _rows(copies), scale=1.0, use_grid=False))
+                return out
             composed = mine if copies is None else [(Ro @ Ri, Ro @ ti + to) for Ro, to in copies for Ri, ti in mine]
             out = []
             for child in node.get("Children", []):
-                for a in self.node(child, composed, grid_ok and bool(node.get("Use_Grid", True))):
+                for a in self.node(child, composed):
                     out.append(a if scale == 1.0 else _scaled(a, scale))
             return out
         if t == ",25":  # space-filling symmetry of its children (grid path)
@@ -155,7 +188,7 @@ class _Decoder:
             scale = float((node.get("ExtraParameters") or [1.0])[0])
             kids = []
             for child in node.get("Children", []):
-                kids += self.node(child, None, True)
+                kids += self.node(child, None)
             sf = M.SpaceFillingSymmetry(kids, rows[0, 0], rows[1, 0], rows[2, 0], rows[0, 1], rows[1, 1],
                                         rows[2, 1], rows[0, 2], rows[1, 2], rows[2, 2], scale=scale,
                                         location=_location(node))
@@ -165,13 +198,20 @@ class _Decoder:
         leaf = self.leaf(node)
         if copies is None:
             return [leaf]
-        rows = []
-        for R, tt in copies:
-            a, b, c = _euler_angles(R)
-            rows.append([tt[0], tt[1], tt[2], math.degrees(a), math.degrees(b), math.degrees(c)])
         if isinstance(leaf, M.AmpGridAmplitude):
             raise NotImplementedError("docked copies of an amplitude-file leaf are not carried")
-        return [M.ManualSymmetry(leaf, rows, scale=1.0, use_grid=grid_ok and self.use_grid)]
+        # copies reach a leaf only from symmetries that do not use grids: the
+        # leaf's grid is docked per orientation
+        return [M.ManualSymmetry(leaf, _rows(copies), scale=1.0, use_grid=False)]
+
+
+def _rows(copies):
+    """ManualSymmetry rows (x, y, z nm, alpha, beta, gamma degrees) of [(R, t)]."""
+    rows = []
+    for R, tt in copies:
+        a, b, c = _euler_angles(R)
+        rows.append([tt[0], tt[1], tt[2], math.degrees(a), math.degrees(b), math.degrees(c)])
+    return rows
 
 
 def _scaled(a, s):

@@ -107,6 +107,19 @@ int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns);
 enum { DPX_FILL_DIRECT = 0, DPX_FILL_HARMONIC = 1 };
 int dpx_ctx_set_fill_method(dpx_ctx ctx, int method);
 int dpx_ctx_get_fill_method(dpx_ctx ctx);
+/* Convergence test of the Monte Carlo average (eps > 0) for this context's
+ * dpx_orientation_average calls.  DPX_CONV_CPU (the default): the reference's
+ * CPU rule (DomainModel::AverageIntensitiesBetweenLayers, Backend/Backend/
+ * Amplitude.cpp:2773-2815): every 100th sample from the 400th on, each q's
+ * running mean within eps of the 4 last recorded.  DPX_CONV_GPU: the rule of
+ * the reference's GPU averages (GPUCalcMCOAJacobSphrDD, Backend/GPU/OAJacob.cu:
+ * 244-346, 8192 samples a step; the hybrid GPUHybridCalculator::
+ * MonteCarloOrientationFunc, GPUHybridCalc.cu:467-578 with checkConvergenceOA
+ * :705-720, 4096 a step): the running mean after every samples_per_step
+ * samples (a multiple of 128); from the 4th step on, converged when every q of
+ * the bracket is within eps of its mean at each of the 3 steps before. */
+enum { DPX_CONV_CPU = 0, DPX_CONV_GPU = 1 };
+int dpx_ctx_set_convergence(dpx_ctx ctx, int rule, int64_t samples_per_step);
 /* Stage timing of harmonic fills (no counterpart in the reference): with
  * timing on, the fill records CUDA events on the context's stream;
  * dpx_ctx_stage_times then gives out[5] = {ms of the moments kernels, ms of

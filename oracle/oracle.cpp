@@ -732,9 +732,31 @@ void orc_q_brackets(int grid_size, double qmax, int nq, const double* Q, int* la
     }
 }
 
+namespace {
+int integrate_layers_impl(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq, const double* Q,
+                          const double* dirs, int64_t dir_layer_stride, int64_t max_iter, double eps, int nthreads,
+                          int64_t gpu_step, double* res);
+}  // namespace
+
 int orc_integrate_layers(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq, const double* Q,
                          const double* dirs, int64_t dir_layer_stride, int64_t max_iter, double eps, int nthreads,
                          double* res) {
+    return integrate_layers_impl(grid_size, qmax, n_leaves, leaves, nq, Q, dirs, dir_layer_stride, max_iter, eps,
+                                 nthreads, 0, res);
+}
+
+int orc_integrate_layers_gpu_rule(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq,
+                                  const double* Q, const double* dirs, int64_t dir_layer_stride, int64_t max_iter,
+                                  double eps, int64_t samples_per_step, int nthreads, double* res) {
+    if (samples_per_step <= 0) return -1;
+    return integrate_layers_impl(grid_size, qmax, n_leaves, leaves, nq, Q, dirs, dir_layer_stride, max_iter, eps,
+                                 nthreads, samples_per_step, res);
+}
+
+namespace {
+int integrate_layers_impl(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq, const double* Q,
+                          const double* dirs, int64_t dir_layer_stride, int64_t max_iter, double eps, int nthreads,
+                          int64_t gpu_step, double* res) {
     std::vector<LeafModel> models;
     for (int l = 0; l < n_leaves; l++) models.push_back(make_model(grid_size, qmax, leaves[l]));
     const int L = grid_size / 2;
@@ -781,6 +803,28 @@ int orc_integrate_layers(int grid_size, double qmax, int n_leaves, const orc_lea
                 for (int k = 0; k < m; k++) sums[k] += one[k];
             }
             for (int k = 0; k < m; k++) run[k] += std::real(sums[k] * std::conj(sums[k]));
+            if (eps > 0.0 && gpu_step > 0) {
+                /* the reference GPU averages' test (OAJacob.cu:320-337, GPUHybridCalc.cu:705-720):
+                 * the running mean after every gpu_step samples; from the 4th step on, converged
+                 * when every q is within eps of its mean at each of the 3 steps before */
+                if ((i + 1) % gpu_step != 0) continue;
+                const int64_t step = (i + 1) / gpu_step - 1;
+                const int pos = int(step % 4);
+                for (int k = 0; k < m; k++) hist[pos * m + k] = run[k] / double(i + 1);
+                if (step > 2) {
+                    bool conv = true;
+                    for (int j = 1; conv && j <= 3; j++) {
+                        const int pj = int((step - j) % 4);
+                        for (int k = 0; k < m; k++)
+                            if (!(std::fabs(1.0 - hist[pos * m + k] / hist[pj * m + k]) <= eps)) { conv = false; break; }
+                    }
+                    if (conv) {
+                        for (int k = 0; k < m; k++) res[idx[k]] = hist[pos * m + k];
+                        done = true;
+                    }
+                }
+                continue;
+            }
             if (eps > 0.0 && i % 100 == 0) {
                 int pos = int((i / 100) % 4);
                 for (int k = 0; k < m; k++) hist[pos * m + k] = run[k] / double(i + 1);
@@ -801,6 +845,7 @@ int orc_integrate_layers(int grid_size, double qmax, int n_leaves, const orc_lea
     }
     return 0;
 }
+}  // namespace
 
 namespace {
 /* The voxelized-solvent boxes' amplitude at q in FP64 (PDBAmplitude.cpp:277-314,

@@ -106,6 +106,14 @@ int orc_integrate_layers(int grid_size, double qmax, int n_leaves, const orc_lea
                          int nq, const double* Q, const double* dirs, int64_t dir_layer_stride,
                          int64_t max_iter, double eps, int nthreads, double* res);
 
+/* The same with the reference GPU averages' convergence test (GPUCalcMCOAJacobSphrDD,
+ * OAJacob.cu:244-346; GPUHybridCalc.cu:467-578, 705-720): with eps > 0 the running
+ * mean after every samples_per_step samples, converged from the 4th step on when
+ * every q of the bracket is within eps of its mean at each of the 3 steps before. */
+int orc_integrate_layers_gpu_rule(int grid_size, double qmax, int n_leaves, const orc_leaf* leaves, int nq,
+                                  const double* Q, const double* dirs, int64_t dir_layer_stride, int64_t max_iter,
+                                  double eps, int64_t samples_per_step, int nthreads, double* res);
+
 /* Bracket assignment of IntegrateLayersTogether (Amplitude.cpp:1184-1217):
  * for each q index, the layer whose bracket computes it (-1 for q == 0), later
  * layers win where two brackets claim the same q. */

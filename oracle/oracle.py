@@ -237,6 +237,23 @@ def integrate_layers(grid_size, qmax, leaves, Q, dirs, dir_layer_stride, max_ite
     return res
 
 
+def integrate_layers_gpu_rule(grid_size, qmax, leaves, Q, dirs, dir_layer_stride, max_iter, eps, samples_per_step,
+                              nthreads=0):
+    """integrate_layers with the reference GPU averages' convergence test."""
+    L = lib()
+    L.orc_integrate_layers_gpu_rule.restype = C.c_int
+    L.orc_integrate_layers_gpu_rule.argtypes = [C.c_int, C.c_double, C.c_int, C.POINTER(Leaf), C.c_int, _D, _D,
+                                                C.c_int64, C.c_int64, C.c_double, C.c_int64, C.c_int, _D]
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float64)
+    arr = (Leaf * len(leaves))(*leaves)
+    res = np.zeros(len(Q))
+    L.orc_integrate_layers_gpu_rule(grid_size, qmax, len(leaves), arr, len(Q), Q.ctypes.data_as(_D),
+                                    dirs.ctypes.data_as(_D), dir_layer_stride, max_iter, eps, samples_per_step,
+                                    nthreads, res.ctypes.data_as(_D))
+    return res
+
+
 def direct_intensity(s: Struct, Q, dirs, copy_rot=None, copy_tr=None, nthreads=0):
     """FP64 direct sum (no grid) at the given directions, with the leaf's
     solvent boxes and optional docked copies (radians, nm)."""

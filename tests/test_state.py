@@ -95,3 +95,25 @@ def test_space_filling_rows(tmp_path):
     (w, amps), = S.decode(_state([sf])).populations
     ref = M.SpaceFillingSymmetry([], 3.0, 3.5, 4.0, 90, 80, 100, 2, 3, 4)
     assert np.allclose(amps[0].lattice, ref.lattice) and amps[0].scale == 0.7 and math.isclose(w, 1.5)
+
+
+def test_grid_subtree_stays_one_assembly_grid(tmp_path):
+    """As the reference's hybrid FlattenTree: a symmetry whose subtree uses grids
+    is one assembly grid; a symmetry above it that does not use grids docks
+    that grid per orientation; with grids all the way up, grid of grid."""
+    p = str(tmp_path / "sub.pdb")
+    _pdb(p, [("C", 0, 0, 0), ("O", 1.2, 0, 0)])
+    leaf = _node("PDB", Filename=p, ExtraParameters=[1, 0, 1, 0.05, 0.14, 0.28, 0, 0, 0, 0])
+    inner = _node(",26", Parameters=[[-4, -2, -8.13, 90, 0, 0]], ExtraParameters=[1], Children=[leaf])
+    for outer_grid in (False, True):
+        outer = _node(",26", Parameters=[[0, 0, 0, 0, 0, 0], [4, 0, 0, 0, 0, 0], [8, 0, 0, 0, 0, 0]],
+                      ExtraParameters=[1], Children=[inner], Use_Grid=outer_grid)
+        st = _state([outer])
+        st["DomainPreferences"]["UseGrid"] = True
+        (w, amps), = S.decode(st, base_dir=str(tmp_path)).populations
+        ms, = amps
+        assert isinstance(ms, M.ManualSymmetry) and ms.use_grid is outer_grid and len(ms.trans) == 3
+        assert isinstance(ms.child, M.ManualSymmetry) and ms.child.use_grid and len(ms.child.trans) == 1
+        assert isinstance(ms.child.child, M.PDBAmplitude)
+        assert np.allclose(ms.child.trans[0], [-4, -2, -8.13]) and np.allclose(ms.child.rot[0], [np.pi / 2, 0, 0])
+        assert np.allclose(ms.trans[:, 0], [0, 4, 8])
