@@ -200,15 +200,8 @@ void ctx_release(dpx_ctx ctx) {
     set_device(ctx);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->atoms, &ctx->table, &ctx->ions, &ctx->models, &ctx->groups, &ctx->plan, &ctx->partial,
-                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->voxels, &ctx->dirsort,
-                      &ctx->direct})
+                      &ctx->result, &ctx->dirs, &ctx->debye, &ctx->harmonic, &ctx->dirsort, &ctx->direct})
         b->release();
-    for (DevBuf& b : ctx->leaf_boxes) b.release();
-    ctx->pin_plan.release();
-    ctx->pin_totals.release();
-    ctx->pin_small.release();
-    ctx->pin_units.release();
-    ctx->pin_atomset.release();
     for (cudaEvent_t e : ctx->tev)
         if (e) cudaEventDestroy(e);
     if (ctx->aux) {
@@ -424,6 +417,30 @@ int check_pdb(const dpx_pdb_desc& d) {
     return DPX_OK;
 }
 
+int ctx_harmonic_streams(dpx_ctx ctx, HarmStreams& S) {
+    if (!ctx->aux) DPX_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ctx->aux_go, &ctx->aux_done, &ctx->aux_atoms})
+        if (!*e) DPX_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    if (ctx->timing)
+        for (cudaEvent_t& e : ctx->tev)
+            if (!e) DPX_CUDA(cudaEventCreate(&e));
+    S = HarmStreams{};
+    S.st = ctx->stream;
+    S.ax = ctx->aux;
+    S.go = ctx->aux_go;
+    S.tables = ctx->aux_done;
+    S.atoms = ctx->aux_atoms;
+    S.tev = ctx->timing ? ctx->tev : nullptr;
+    return DPX_OK;
+}
+
+void ctx_stage_record(dpx_ctx ctx, const HarmPlan& p) {
+    if (!ctx->timing) return;
+    ctx->tev_used = p.n_vox ? 8 : 6;
+    ctx->stage_points = p.stage_points;
+    ctx->stage_k = p.stage_k;
+}
+
 // Batched fill with an explicit FP32 launch shape; ev0/ev1 (optional) bracket
 // the FP32 fill launch on the context's stream.
 int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int cpt, int threads, int poly,
@@ -440,37 +457,56 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     cudaStream_t s = ctx->stream;
     for (int j = 0; j < n; ++j) grids[j]->splines_current = false;
 
-    // host staging of every leaf, then the FP32 job table and the tile counter
-    std::vector<char>& h = ctx->host_stage;
-    h.clear();
-    std::vector<LeafTables> lt(n);
-    std::vector<char> harm(n, 0);  // FP32 leaves the harmonic method takes
-    std::vector<std::vector<float>> host_atoms(n);
-    std::vector<HarmLeaf> harm_leaf(n);
+    // the harmonic method plans the FP32 leaves it takes (host work and
+    // synchronizations), the rest are staged for the direct sum
+    std::vector<char> harm(n, 0);
+    std::vector<HarmPlan> plans(n);
+    struct Release {
+        std::vector<HarmPlan>& p;
+        ~Release() {
+            for (HarmPlan& x : p) harmonic_plan_release(x);
+        }
+    } release{plans};
     if (ctx->fill_method == DPX_FILL_HARMONIC)
         for (int j = 0; j < n; ++j) {
             if (grids[j]->precision != DPX_FP32) continue;
-            int status = DPX_OK;
-            harm[j] = harmonic_accepts(ctx, j, pdbs[j], grids[j]->g, host_atoms[j], harm_leaf[j], &status);
-            if (status) return status;
+            const int rc = harmonic_plan(s, pdbs[j], grids[j]->g, plans[j]);
+            if (rc < 0) return rc;
+            harm[j] = rc == DPX_OK;
         }
+    // host staging of every direct leaf, then the FP32 job table and the tile counter
+    std::vector<char>& h = ctx->host_stage;
+    h.clear();
+    std::vector<LeafTables> lt(n);
     for (int j = 0; j < n; ++j) {
+        if (harm[j]) continue;
         const bool fp32 = grids[j]->precision == DPX_FP32;
-        stage_leaf(h, pdbs[j], grids[j]->g, fp32, fp32 ? cpt : dpx::kFill64Cells, lt[j], !harm[j]);
+        stage_leaf(h, pdbs[j], grids[j]->g, fp32, fp32 ? cpt : dpx::kFill64Cells, lt[j]);
     }
     const size_t jobs_off = al16(h.size());
     const size_t counter_off = al16(jobs_off + (size_t)n * sizeof(dpx::FillJob));
     h.resize(counter_off + 64, 0);
     DPX_CUDA(ctx->atoms.reserve(h.size()));
     const char* dbase = (const char*)ctx->atoms.p;
-    // the leaf tables first: the harmonic fills read their form factors
     DPX_CUDA(cudaMemcpyAsync(ctx->atoms.p, h.data(), jobs_off, cudaMemcpyHostToDevice, s));
     if (ev0) DPX_CUDA(cudaEventRecord(ev0, s));
+    size_t scratch = 0;
     for (int j = 0; j < n; ++j)
-        if (harm[j])
-            if (int rc = harmonic_fill(ctx, pdbs[j], lt[j], dbase, grids[j]->g, grids[j]->cells, host_atoms[j],
-                                       harm_leaf[j]))
+        if (harm[j]) scratch = std::max(scratch, plans[j].scratch_bytes);
+    if (scratch) {
+        if (cudaError_t e = ctx->harmonic.reserve(scratch)) {
+            cudaGetLastError();
+            return fail(DPX_ERR_OOM, "harmonic fill needs %zu bytes of scratch (%s)", scratch, cudaGetErrorString(e));
+        }
+        HarmStreams S;
+        if (int rc = ctx_harmonic_streams(ctx, S)) return rc;
+        for (int j = 0; j < n; ++j) {
+            if (!harm[j]) continue;
+            if (int rc = harmonic_launch(S, plans[j], ctx->harmonic.p, reinterpret_cast<float4*>(grids[j]->cells)))
                 return rc;
+            ctx_stage_record(ctx, plans[j]);
+        }
+    }
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
     for (int j = 0; j < n; ++j) {

@@ -7,8 +7,12 @@
 // 1168-1247, 2746-2822), which the reference runs one structure at a time.
 // Here the solves are packed into waves whose grids fit a device-memory
 // budget.  Each wave is one CUDA graph:
-//   one FP32 fill launch over every structure of the wave (FP64: one per structure),
-//   per structure: splines, MC average, finalize, the q = 0 term,
+//   FP32 with the harmonic method (the default): per structure the harmonic
+//   fill planned at creation (tables, moments, contraction, synthesis with the
+//   phi-spline derivatives), one scratch shared by the fills in order;
+//   FP32 leaves the harmonic method declines: one direct-sum launch over all of
+//   them, then their splines; FP64: the direct sum per structure and splines;
+//   per structure: MC average, finalize, the q = 0 term;
 //   one device-to-host copy of the wave's I(q) into pinned memory.
 // All inputs (atoms, form-factor tables, item prefixes, bracket tables and the
 // shared direction set) are uploaded once at creation; the grids of a wave
@@ -41,6 +45,8 @@ struct dpx_batch_s {
     double* h_res = nullptr;  // pinned
     std::vector<cudaGraph_t> graphs;
     std::vector<cudaGraphExec_t> execs;
+    std::vector<dpxh::HarmPlan> plans;  // FP32 solves the harmonic method fills (arena != nullptr)
+    void* hscratch = nullptr;           // their launch scratch, shared (the fills run in order)
 };
 
 namespace {
@@ -56,6 +62,9 @@ void batch_free(dpx_batch b) {
     if (b->partial) cudaFree(b->partial);
     if (b->d_res) cudaFree(b->d_res);
     if (b->h_res) cudaFreeHost(b->h_res);
+    for (dpxh::HarmPlan& p : b->plans) dpxh::harmonic_plan_release(p);
+    if (b->hscratch) cudaFree(b->hscratch);
+    cudaStreamSynchronize(b->ctx->stream);
     ctx_release(b->ctx);
     delete b;
 }
@@ -143,6 +152,21 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     b->wave_first.push_back(n);
     const int n_waves = (int)b->wave_first.size() - 1;
 
+    // the harmonic method plans the FP32 solves it takes (host work and
+    // synchronizations here, at creation); the graphs then only replay kernels
+    b->plans.resize(n);
+    size_t hscratch = 0;
+    if (fp32 && ctx->fill_method == DPX_FILL_HARMONIC)
+        for (int j = 0; j < n; ++j) {
+            const int rc = harmonic_plan(ctx->stream, solves[j].pdb, sp[j].G, b->plans[j]);
+            if (rc < 0) {
+                batch_free(b);
+                return rc;
+            }
+            if (rc == DPX_OK) hscratch = std::max(hscratch, b->plans[j].scratch_bytes);
+        }
+    auto harmonic = [&](int j) { return b->plans[j].arena != nullptr; };
+
     // staging of every input table
     Stage st;
     size_t partial_max = 0;
@@ -151,7 +175,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         const dpx_pdb_desc& pd = d.pdb;
         SolvePlan& p = sp[j];
         const Geom& G = p.G;
-        stage_leaf(st.h, pd, G, fp32, cpt, p.lt);
+        if (!harmonic(j)) stage_leaf(st.h, pd, G, fp32, cpt, p.lt);
         // brackets and the plain identity model
         Brackets B;
         make_brackets(G, p.grid_size, p.qmax, d.nq, d.Q, B);
@@ -209,6 +233,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->partial, sort_off + sort_bytes);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_res, b->res_total * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_res, b->res_total * sizeof(double));
+    if (e == cudaSuccess && hscratch) e = cudaMalloc(&b->hscratch, hscratch);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "batch allocation");
         batch_free(b);
@@ -225,7 +250,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
             SolvePlan& p = sp[j];
             dpx::ModelDev* M = reinterpret_cast<dpx::ModelDev*>(st.h.data() + p.o_model);
             M->grid = pool + p.grid_off;
-            if (fp32) {
+            if (fp32 && !harmonic(j)) {
                 jobs.push_back(make_job(solves[j].pdb, p.lt, A, p.G, pool + p.grid_off, tiles));
                 tiles += (p.lt.items + threads - 1) / threads;
             }
@@ -262,12 +287,27 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         int64_t launches = 0;
         const int j0 = b->wave_first[w], j1 = b->wave_first[w + 1];
         if (fp32) {
+            HarmStreams hs;
+            hs.st = s;  // the fills run in order on one stream and share the scratch
+            for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
+                if (!harmonic(j)) continue;
+                if (harmonic_launch(hs, b->plans[j], b->hscratch, reinterpret_cast<float4*>(pool + sp[j].grid_off)))
+                    e = cudaErrorUnknown;
+                launches += harmonic_launches(b->plans[j]);
+            }
             bool boxes = false;
-            for (int j = j0; j < j1; ++j) boxes |= sp[j].lt.n_boxes > 0;
-            e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(A + o_jobs[w]), j1 - j0,
-                                           wave_tiles[w], reinterpret_cast<unsigned long long*>(A + o_counter[w]),
-                                           cpt, threads, poly, persistent, boxes);
-            launches++;
+            int direct = 0;
+            for (int j = j0; j < j1; ++j)
+                if (!harmonic(j)) {
+                    boxes |= sp[j].lt.n_boxes > 0;
+                    direct++;
+                }
+            if (e == cudaSuccess && direct) {
+                e = dpx::launch_fill_f32_batch(s, reinterpret_cast<const dpx::FillJob*>(A + o_jobs[w]), direct,
+                                               wave_tiles[w], reinterpret_cast<unsigned long long*>(A + o_counter[w]),
+                                               cpt, threads, poly, persistent, boxes);
+                launches++;
+            }
         } else {
             for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
                 const SolvePlan& p = sp[j];
@@ -278,8 +318,11 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
             const SolvePlan& p = sp[j];
             void* grid = pool + p.grid_off;
-            e = fp32 ? dpx::launch_splines_f32(s, p.G, reinterpret_cast<float4*>(grid))
-                     : dpx::launch_splines_f64(s, p.G, reinterpret_cast<double4_32a*>(grid));
+            if (!harmonic(j)) {  // the harmonic synthesis writes the derivatives itself
+                e = fp32 ? dpx::launch_splines_f32(s, p.G, reinterpret_cast<float4*>(grid))
+                         : dpx::launch_splines_f64(s, p.G, reinterpret_cast<double4_32a*>(grid));
+                launches++;
+            }
             double* r = b->d_res + b->res_off[j];
             if (e == cudaSuccess) e = cudaMemsetAsync(r, 0, (size_t)b->nq[j] * sizeof(double), s);
             if (e == cudaSuccess)
@@ -290,9 +333,9 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
                 e = dpx::launch_origin_intensity(s, !fp32, grid, r);
                 launches++;
             }
-            // splines, bracket tables, average, finalize; the angular order of the
+            // bracket tables, average, finalize; the angular order of the
             // directions (keys, totals, offsets, scatter) when it applies
-            launches += 4 + (p.plan.sort_scratch && n_samples >= 512 ? 4 : 0);
+            launches += 3 + (p.plan.sort_scratch && n_samples >= 512 ? 4 : 0);
         }
         const size_t r0 = b->res_off[j0], r1 = (j1 < n) ? b->res_off[j1] : b->res_total;
         if (e == cudaSuccess)

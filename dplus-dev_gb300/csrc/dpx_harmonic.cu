@@ -36,6 +36,8 @@
 //                phase e^{i q.c} in double-float, the Friedel mirror row and
 //                the rows' phi-spline derivatives.
 #include "dpx_internal.h"
+
+#include <mutex>
 #include "dpx_spline.cuh"
 
 #include <cstdint>
@@ -991,6 +993,40 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* 
 int harmonic_max_l() { return kMaxL - 17; }
 int harmonic_nodes() { return kNodes; }
 
+namespace {
+// Dynamic shared memory of hm_moments: running sums of at most LM + 5 orders
+// (a unit's quartet pair) x 24 values.
+size_t moments_smem(int LM) { return (size_t)(LM + 5) * 24 * sizeof(float2); }
+// Dynamic shared memory of hm_synth for shells up to Lp and outer order li:
+// the G_m of kSynthRows rows, the phi phases of the outer shell, and the rows
+// in flight (rpp x 6i cells with rpp x i <= 256, or one row of 6i > 1,536 cells).
+size_t synth_smem(int Lp, int li) {
+    const int nph = 6 * Lp;
+    const int nG = 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6);
+    const size_t cells = (size_t)6 * (Lp > kSynthThreads ? Lp : kSynthThreads);
+    return ((size_t)kSynthRows * 2 * nG + (size_t)nph + cells) * sizeof(float2);
+}
+std::mutex g_smem_mu;
+size_t g_smem_set[2][64] = {};  // per device: the limits set for hm_moments, hm_synth
+}  // namespace
+
+cudaError_t harmonic_reserve_smem(int Lp, int LM) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    const size_t need[2] = {moments_smem(LM), synth_smem(Lp, LM)};
+    std::lock_guard<std::mutex> lock(g_smem_mu);
+    for (int k = 0; k < 2; ++k) {
+        if (need[k] <= 48 * 1024 || need[k] <= g_smem_set[k][dev]) continue;
+        e = k == 0 ? cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k])
+                   : cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k]);
+        if (e != cudaSuccess) return e;
+        g_smem_set[k][dev] = need[k];
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a) {
     const int64_t nn = (int64_t)a.Lp * a.nbins * kNodes;
     hm_nodes<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a.Lp, a.nbins, a.LM, a.step, a.delta, a.lmax, a.nodes, a.Jn);
@@ -1006,12 +1042,7 @@ cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C)
     // quartet of Q = 1: at most LM + 5 whatever L.
     const int Q = (a.LM + 4) / 4;
     const int pairs = (Q + 1) / 2;
-    const int orders = a.LM + 5;
-    const size_t smem = (size_t)orders * 24 * sizeof(float2);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    const size_t smem = moments_smem(a.LM);  // the limit is raised by harmonic_reserve_smem
     if (a.ev0) {
         cudaError_t e = cudaEventRecord(a.ev0, s);
         if (e != cudaSuccess) return e;
@@ -1061,16 +1092,7 @@ cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
 
 cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
     // one launch: blocks (row group, shell), dynamic shared memory sized for the outermost shell
-    const int li = a.lmax_host_outer;
-    const int nph = 6 * a.Lp;
-    const int nG = 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6);
-    // rows in flight: rpp x 6i cells with rpp x i <= 256, or one row of 6i > 1,536 cells
-    const size_t cells = (size_t)6 * (a.Lp > kSynthThreads ? a.Lp : kSynthThreads);
-    const size_t smem = ((size_t)kSynthRows * 2 * nG + (size_t)nph + cells) * sizeof(float2);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    const size_t smem = synth_smem(a.Lp, a.lmax_host_outer);  // the limit is raised by harmonic_reserve_smem
     const int groups = (3 * a.Lp / 2 + 1 + kSynthRows - 1) / kSynthRows;
     hm_synth<<<dim3(groups, a.Lp), kSynthThreads, smem, s>>>(a.Lp, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step,
                                                              a.vox_s, a.cx, a.cy, a.cz, a.use_center, a.scale,

@@ -115,12 +115,10 @@ struct dpx_ctx_s {
     cudaEvent_t tev[8] = {};
     int tev_used = 0;
     double stage_points = 0, stage_k = 0;
-    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye, harmonic;
-    dpxh::DevBuf voxels;   // the harmonic fill's voxels, binned
+    dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye;
+    dpxh::DevBuf harmonic; // the harmonic fill's launch scratch
     dpxh::DevBuf dirsort;  // the average's angular-order scratch
     dpxh::DevBuf direct;   // the FP64 direct sum's tables and partial amplitudes
-    dpxh::HostPinned pin_plan, pin_totals, pin_small, pin_units, pin_atomset;  // the harmonic fill's host staging
-    std::vector<dpxh::DevBuf> leaf_boxes;  // the harmonic fill's solvent boxes, per leaf of a batch
     std::vector<char> host_stage;
 };
 
@@ -191,26 +189,54 @@ double box_volume_sum(const dpx_pdb_desc& d);
 // The FP32 fill job of a staged leaf whose buffer sits at device address dbase.
 dpx::FillJob make_job(const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G, void* grid,
                       int64_t tile_start);
-// Harmonic (multipole) FP32 fill of a staged leaf (dpx_harmonic_host.cpp).
-// harmonic_accepts decides before the staging: boxes need their voxel step,
-// and the expansion order and the radial bins must stay within the kernels'
-// limits (device atoms are copied to `host_atoms` to measure them).  It
-// stages the leaf's solvent boxes on the device (context buffer `slot`:
-// centred, counted) and fills `hl`: the radius of the point sets about the
-// leaf's centre, the voxel total and the staged arrays harmonic_fill bins.
-struct HarmLeaf {
-    double R = 0.0;      // bounds the atoms and the solvent boxes' corners
-    double R_pts = 0.0;  // bounds the atoms and the voxel centres (<= R)
-    int64_t nb = 0, nv = 0;
-    const float4* boxes = nullptr;
-    const int64_t* counts = nullptr;
-    int64_t* vstart = nullptr;
-    int64_t* run_sums = nullptr;
+// Harmonic (multipole) FP32 fill of one leaf (dpx_harmonic_host.cpp), planned
+// once and launched any number of times.  harmonic_plan (host work and
+// synchronizations on stream st) returns DPX_OK, a negative status, or
+// kHarmDeclined when the method does not take the leaf (boxes without their
+// voxel step, orders or radial bins beyond the kernels' limits): the caller
+// then fills with the direct sum.  The plan owns a device arena (stream-ordered
+// on st) with its tables and point sets; harmonic_launch queues only kernels
+// and memsets, so a graph can record it.
+constexpr int kHarmDeclined = 1;
+struct HarmPlan {
+    dpx::Geom G{};
+    cudaStream_t stream = nullptr;  // the arena is freed on it
+    int nbins = 0, LM = 0, K = 0;
+    double delta = 0.0;
+    int64_t n_vox = 0;
+    int n_units[2] = {0, 0}, n_groups[2] = {0, 0};  // [0] atoms, [1] solvent voxels
+    double cen[3] = {0, 0, 0};   // the centring translation restored per cell
+    float scale = 1.f, vox_s = 0.f;
+    double origin = 0.0;         // F(0), FP64, scaled
+    double stage_points = 0.0, stage_k = 0.0;  // points and mean (l, m) per point (stage timing)
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    size_t o_lmax = 0, o_lmb = 0, o_ab = 0, o_cr = 0, o_nmm = 0, o_nodes = 0, o_vinv = 0, o_aff = 0;
+    size_t o_pts[2] = {0, 0}, o_units[2] = {0, 0}, o_groups[2] = {0, 0}, o_gu[2] = {0, 0};
+    // scratch of a launch (offsets from the caller's scratch, 256-byte aligned)
+    size_t s_Jn = 0, s_T = 0, s_MP[2] = {0, 0}, s_M[2] = {0, 0}, s_C[2] = {0, 0};
+    size_t scratch_bytes = 0;
 };
-bool harmonic_accepts(dpx_ctx ctx, int slot, const dpx_pdb_desc& d, const dpx::Geom& G,
-                      std::vector<float>& host_atoms, HarmLeaf& hl, int* status);
-int harmonic_fill(dpx_ctx ctx, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase, const dpx::Geom& G,
-                  void* grid, const std::vector<float>& host_atoms, const HarmLeaf& hl);
+// Streams of a launch: ax (may be null or st) runs the radial tables and the
+// atoms' set beside the voxels' moments on st, forked and joined by the events
+// go, tables and atoms; tev (null: no timing) receives the stage events.
+struct HarmStreams {
+    cudaStream_t st = nullptr, ax = nullptr;
+    cudaEvent_t go = nullptr, tables = nullptr, atoms = nullptr;
+    cudaEvent_t* tev = nullptr;
+};
+int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, HarmPlan& p);
+void harmonic_plan_release(HarmPlan& p);
+// Fills grid (FP32 cells with their phi-spline derivatives) from the plan.
+int harmonic_launch(const HarmStreams& S, const HarmPlan& p, void* scratch, float4* grid);
+// Kernel launches of one harmonic_launch.
+int harmonic_launches(const HarmPlan& p);
+// The context's streams for a harmonic launch: its stream, its side stream and
+// fork/join events (created on first use, so call it outside stream capture),
+// and the stage-timing events when timing is on; ctx_stage_record keeps the
+// plan's figures for dpx_ctx_stage_times.
+int ctx_harmonic_streams(dpx_ctx ctx, HarmStreams& S);
+void ctx_stage_record(dpx_ctx ctx, const HarmPlan& p);
 // The FP64 fill launch of a staged leaf.
 cudaError_t launch_leaf_f64(cudaStream_t s, const dpx_pdb_desc& d, const LeafTables& t, const char* dbase,
                             const dpx::Geom& G, void* grid);

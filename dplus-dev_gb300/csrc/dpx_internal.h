@@ -234,6 +234,11 @@ struct VoxelBinArgs {
     float4* out;            // [nv] voxels sorted by bin
 };
 cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a);
+// Raises hm_moments' and hm_synth's dynamic shared-memory limits on the current
+// device to what a fill of shells up to Lp and orders up to LM needs (never
+// lowers them).  Called when a fill is planned, outside any stream capture;
+// the launches below do not touch the limits.
+cudaError_t harmonic_reserve_smem(int Lp, int LM);
 cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a);
 // C [Lp+1][K] (FP64) = the expansion coefficients of one point set.
 cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C);

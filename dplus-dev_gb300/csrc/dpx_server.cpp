@@ -58,6 +58,7 @@ struct LeafCopy {
     bool has_center = false;
     double center[3] = {0, 0, 0};
     std::vector<float> boxes;  // 8 per voxelized-solvent box
+    double voxel_step = 0;     // the voxel edge the boxes were built on (the harmonic fill needs it)
     uint64_t key = 0;  // content (or caller) key, before the grid parameters
 };
 
@@ -359,11 +360,31 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
         d.center = l.has_center ? l.center : nullptr;
         d.n_boxes = (int64_t)l.boxes.size() / 8;
         d.boxes = l.boxes.empty() ? nullptr : l.boxes.data();
+        d.voxel_step = l.voxel_step;
         const bool fp32 = g.precision == DPX_FP32;
         stage_leaf(h, d, g.G, fp32, fp32 ? cpt32 : dpx::kFill64Cells, lt[j]);
     }
+    // the harmonic method plans the FP32 leaves it takes (on the fill stream;
+    // this worker waits for the planning's device steps), the rest are staged
+    // for one direct-sum launch
+    std::vector<HarmPlan> plans(fresh.size());
+    struct Release {
+        std::vector<HarmPlan>& p;
+        ~Release() {
+            for (HarmPlan& x : p) harmonic_plan_release(x);
+        }
+    } release{plans};
+    std::vector<char> harm(fresh.size(), 0);
+    if (ctx->fill_method == DPX_FILL_HARMONIC)
+        for (size_t j = 0; j < fresh.size(); ++j) {
+            if (fresh[j]->precision != DPX_FP32) continue;
+            const int rc = harmonic_plan(s, descs[j], fresh[j]->G, plans[j]);
+            if (rc < 0) return rc;
+            harm[j] = rc == DPX_OK;
+        }
     const size_t jobs_at = al16(h.size());
-    const size_t n32 = std::count_if(fresh.begin(), fresh.end(), [](GridEntry* g) { return g->precision == DPX_FP32; });
+    size_t n32 = 0;
+    for (size_t j = 0; j < fresh.size(); ++j) n32 += fresh[j]->precision == DPX_FP32 && !harm[j];
     h.resize(jobs_at + n32 * sizeof(dpx::FillJob));
     const size_t counter_at = al16(h.size());
     h.resize(counter_at + 64, 0);
@@ -374,7 +395,7 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
     std::vector<dpx::FillJob> jobs;
     int64_t tiles = 0;
     for (size_t j = 0; j < fresh.size(); ++j) {
-        if (fresh[j]->precision != DPX_FP32) continue;
+        if (fresh[j]->precision != DPX_FP32 || harm[j]) continue;
         jobs.push_back(make_job(descs[j], lt[j], d, fresh[j]->G, fresh[j]->cells, tiles));
         tiles += (lt[j].items + threads - 1) / threads;
     }
@@ -399,9 +420,22 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
         dl.fill_launches++;
     }
     DPX_CUDA(cudaFreeAsync(d, s));
-    for (GridEntry* g : fresh) {
-        e = g->precision == DPX_FP32 ? dpx::launch_splines_f32(s, g->G, reinterpret_cast<float4*>(g->cells))
-                                     : dpx::launch_splines_f64(s, g->G, reinterpret_cast<double4_32a*>(g->cells));
+    for (size_t j = 0; j < fresh.size(); ++j) {  // harmonic fills, one scratch each, in stream order
+        if (!harm[j]) continue;
+        void* scratch = nullptr;
+        DPX_CUDA(cudaMallocAsync(&scratch, plans[j].scratch_bytes, s));
+        HarmStreams hs;
+        hs.st = s;
+        const int rc = harmonic_launch(hs, plans[j], scratch, reinterpret_cast<float4*>(fresh[j]->cells));
+        cudaFreeAsync(scratch, s);
+        if (rc) return rc;
+        dl.fill_launches += harmonic_launches(plans[j]);
+    }
+    for (size_t j = 0; j < fresh.size(); ++j) {
+        GridEntry* g = fresh[j];
+        e = harm[j] ? cudaSuccess  // the harmonic synthesis writes the phi-spline derivatives
+            : g->precision == DPX_FP32 ? dpx::launch_splines_f32(s, g->G, reinterpret_cast<float4*>(g->cells))
+                                       : dpx::launch_splines_f64(s, g->G, reinterpret_cast<double4_32a*>(g->cells));
         if (e != cudaSuccess) return cuda_fail(e, "splines launch");
         DPX_CUDA(cudaEventCreateWithFlags(&g->ready, cudaEventDisableTiming));
         DPX_CUDA(cudaEventRecord(g->ready, s));
@@ -634,6 +668,7 @@ int dpx_server_submit(dpx_server S, const dpx_request* q, uint64_t* ticket) {
         if (d.center)
             for (int k = 0; k < 3; ++k) c.center[k] = d.center[k];
         if (d.n_boxes > 0 && d.boxes) c.boxes.assign(d.boxes, d.boxes + 8 * d.n_boxes);
+        c.voxel_step = d.voxel_step;
         uint64_t h = q->leaf_keys && q->leaf_keys[l] ? q->leaf_keys[l] : 0;
         if (!h) {  // content key
             h = 1469598103934665603ull;
@@ -645,6 +680,7 @@ int dpx_server_submit(dpx_server S, const dpx_request* q, uint64_t* ticket) {
             h = fnv(h, p, sizeof p);
             if (c.has_center) h = fnv(h, c.center, sizeof c.center);
             h = fnv(h, c.boxes.data(), c.boxes.size() * sizeof(float));
+            h = fnv(h, &c.voxel_step, sizeof c.voxel_step);
         }
         c.key = h;
     }

@@ -92,6 +92,10 @@ _SIGS = {
                                     C.c_double, C.c_double, _D]),
     "dpx_grid_fill_pdb_batch": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(PdbDesc)]),
     "dpx_autotune_fill": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(PdbDesc), C.c_int, _I, _F]),
+    "dpx_leaf_create": (C.c_int, [_P, C.POINTER(PdbDesc), C.POINTER(_P)]),
+    "dpx_leaf_fill": (C.c_int, [_P]),
+    "dpx_leaf_info": (C.c_int, [_P, _I, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "dpx_leaf_destroy": (C.c_int, [_P]),
     "dpx_grid_compute_splines": (C.c_int, [_P]),
     "dpx_grid_read": (C.c_int, [_P, _D, _D]),
     "dpx_grid_write": (C.c_int, [_P, _D, _D]),

@@ -195,6 +195,25 @@ int dpx_grid_fill_pdb_batch(int n, const dpx_grid* grids, const dpx_pdb_desc* pd
  * (optional) the average time of each.  The grids end up filled. */
 int dpx_autotune_fill(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int repeats, int* best,
                       float* times_ms);
+/* ---- prepared leaves (the reference's PDBAmplitude after PreCalculate,
+ * Backend/Backend/PDBAmplitude.cpp:1199-1336: what does not change between
+ * fills, done once) ----
+ * dpx_leaf_create prepares the fill of grid g from leaf d (host or device atoms,
+ * as dpx_grid_fill_pdb_batch reads them; host arrays are read only here): for
+ * an FP32 grid with the harmonic method, the harmonic fill's plan (points
+ * grouped by radius and ion, solvent boxes expanded and binned on the device,
+ * recurrence tables) and its launch scratch, in device memory the leaf owns;
+ * otherwise the direct sum's staged tables.  It synchronizes the context's
+ * stream.  dpx_leaf_fill queues the fill of g, with its phi-spline derivatives,
+ * on the context's stream and returns without waiting: no host work, no copies
+ * from the host and no synchronization, so a stream capture can record it.
+ * The grid must outlive the leaf.  dpx_leaf_info: harmonic (1) or direct (0),
+ * kernel launches per fill, device bytes the leaf holds. */
+typedef struct dpx_leaf_s* dpx_leaf;
+int dpx_leaf_create(dpx_grid g, const dpx_pdb_desc* d, dpx_leaf* out);
+int dpx_leaf_fill(dpx_leaf leaf);
+int dpx_leaf_info(dpx_leaf leaf, int* harmonic, int64_t* launches, int64_t* device_bytes);
+int dpx_leaf_destroy(dpx_leaf leaf);
 /* Periodic cubic-spline phi derivatives of every theta row. */
 int dpx_grid_compute_splines(dpx_grid g);
 /* Host copies in the reference's layout: interleaved complex double [2P] each;

@@ -99,3 +99,96 @@ def test_grid_write_clears_the_fill_derivatives(harmonic):
     ref.compute_splines()
     _, dr = ref.read(False, True)
     assert np.array_equal(d2, dr)
+
+
+def _leaf(grid, desc):
+    import ctypes as C
+    import dpx
+    h = C.c_void_p()
+    _lib.check(dpx.lib().dpx_leaf_create(grid.handle, desc, C.byref(h)))
+    return h
+
+
+@pytest.mark.parametrize("method,prec", [(_lib.DPX_FILL_HARMONIC, M.FP32), (_lib.DPX_FILL_DIRECT, M.FP32),
+                                         (_lib.DPX_FILL_HARMONIC, M.FP64)])
+@pytest.mark.parametrize("extra", [LAYER, SOLVENT])
+def test_prepared_leaf_fill_equals_batch_fill(ctx, method, prec, extra):
+    """dpx_leaf_fill (planned once, queue-only fills) writes the same bits as
+    dpx_grid_fill_pdb_batch, for host atoms and for centred device atoms, and
+    again on a second fill."""
+    import ctypes as C
+    import dpx
+    import torch
+    L = dpx.lib()
+    amp = globule(900, 1.7, seed=148, extra=extra)
+    gs, qmax = 30, 4.0
+    before = ctx.fill_method()
+    ctx.set_fill_method(method)
+    try:
+        ref = M.Grid(ctx, gs, qmax, prec)
+        descs, keep = M.pdb_descs([amp])
+        _lib.check(L.dpx_grid_fill_pdb_batch(1, (C.c_void_p * 1)(ref.handle.value), descs))
+        ref.compute_splines()
+        v0, d0 = ref.read(True, True)
+        g = M.Grid(ctx, gs, qmax, prec)
+        leaf = _leaf(g, descs)
+        for _ in range(2):
+            _lib.check(L.dpx_leaf_fill(leaf))
+            g.compute_splines()
+            v, d = g.read(True, True)
+            assert np.array_equal(v, v0) and np.array_equal(d, d0)
+        harm = C.c_int()
+        _lib.check(L.dpx_leaf_info(leaf, C.byref(harm), None, None))
+        assert harm.value == (1 if method == _lib.DPX_FILL_HARMONIC and prec == M.FP32 else 0)
+        _lib.check(L.dpx_leaf_destroy(leaf))
+        if prec == M.FP32:  # device atoms, centred by the caller
+            cen = amp.xyz.mean(0)
+            at = amp.atoms_float4()
+            at[:, :3] = (amp.xyz - cen).astype(np.float32)
+            d_at = torch.from_numpy(at).cuda()
+            c = np.ascontiguousarray(cen)
+            descs[0].atoms, descs[0].atoms_on_device, descs[0].center = d_at.data_ptr(), 1, _lib.dptr(c)
+            _lib.check(L.dpx_grid_fill_pdb_batch(1, (C.c_void_p * 1)(ref.handle.value), descs))
+            ref.compute_splines()
+            v1, _ = ref.read(True, False)
+            leaf = _leaf(g, descs)
+            _lib.check(L.dpx_leaf_fill(leaf))
+            v2, _ = g.read(True, False)
+            assert np.array_equal(v1, v2)
+            assert rel_to_max(v2, v0) <= 2e-6
+            _lib.check(L.dpx_leaf_destroy(leaf))
+        del keep
+    finally:
+        ctx.set_fill_method(before)
+
+
+def test_prepared_leaf_fill_replays_in_a_cuda_graph(harmonic):
+    """A stream capture records dpx_leaf_fill (side stream joined back by
+    events); replaying the graph refills the grid with the same bits."""
+    import ctypes as C
+    import dpx
+    import torch
+    L = dpx.lib()
+    amp = globule(700, 1.6, seed=149, extra=LAYER)
+    g = M.Grid(harmonic, 30, 4.0, M.FP32)
+    descs, keep = M.pdb_descs([amp])
+    leaf = _leaf(g, descs)
+    _lib.check(L.dpx_leaf_fill(leaf))
+    harmonic.synchronize()
+    v0, d0 = g.read(True, True)
+    s = torch.cuda.Stream()
+    old = C.c_void_p(L.dpx_ctx_get_stream(harmonic.handle))
+    harmonic.set_stream(s.cuda_stream)
+    try:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=s):
+            _lib.check(L.dpx_leaf_fill(leaf))
+        g.write(np.zeros_like(v0))  # the replay must write every cell again
+        graph.replay()
+        torch.cuda.synchronize()
+    finally:
+        harmonic.set_stream(old.value)
+    v1, d1 = g.read(True, True)
+    assert np.array_equal(v1, v0) and np.array_equal(d1, d0)
+    _lib.check(L.dpx_leaf_destroy(leaf))
+    del keep

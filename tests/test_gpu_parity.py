@@ -567,26 +567,28 @@ def _batch_case(seed0=80):
     return leaves, gss, qms, Qs
 
 
-@pytest.mark.parametrize("prec", [M.FP32, M.FP64])
-def test_solve_batch_equals_single_solves(ctx, prec):
-    """dpx_batch (one graph per wave, one fill launch per wave) gives the same
-    I(q) as one DomainModel solve per structure, also when the grid budget
+@pytest.mark.parametrize("prec,method", [(M.FP32, _lib.DPX_FILL_HARMONIC), (M.FP32, _lib.DPX_FILL_DIRECT),
+                                         (M.FP64, _lib.DPX_FILL_HARMONIC)])
+def test_solve_batch_equals_single_solves(ctx, prec, method):
+    """dpx_batch (one graph per wave: the harmonic fills planned at creation,
+    or one direct-sum launch per wave) gives the same I(q) as one DomainModel
+    solve per structure with the same fill method, also when the grid budget
     splits the batch into several waves; replaying the graphs is stable."""
     leaves, gss, qms, Qs = _batch_case()
     dirs = M.mc_directions(9, 500)
-    with fill_method(ctx, _lib.DPX_FILL_DIRECT):  # the batch fills with the direct sum
+    with fill_method(ctx, method):
         singles = [M.DomainModel([a], gs, qm, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
                    for a, gs, qm, Q in zip(leaves, gss, qms, Qs)]
-    for budget in (0, 1):  # 1 byte: every structure is its own wave
-        b = M.SolveBatch(ctx, leaves, gss, qms, Qs, dirs, precision=prec, grid_budget_bytes=budget)
-        waves, launches, _ = b.info()
-        assert waves == (5 if budget == 1 else 1)
-        assert launches > 0
-        for _ in range(2):
-            b.run()
-            for r, s in zip(b.results(), singles):
-                assert np.allclose(r, s, rtol=1e-12, atol=0)
-        b.close()
+        for budget in (0, 1):  # 1 byte: every structure is its own wave
+            b = M.SolveBatch(ctx, leaves, gss, qms, Qs, dirs, precision=prec, grid_budget_bytes=budget)
+            waves, launches, _ = b.info()
+            assert waves == (5 if budget == 1 else 1)
+            assert launches > 0
+            for _ in range(2):
+                b.run()
+                for r, s in zip(b.results(), singles):
+                    assert np.allclose(r, s, rtol=1e-12, atol=0)
+            b.close()
     if prec == M.FP64:  # pin one structure to the oracle
         data, co = oracle_grid(leaves[0], gss[0], qms[0])
         ref = O.integrate_layers(gss[0], qms[0], [O.make_leaf(data, co)], Qs[0], dirs, 0, len(dirs), 0.0)

@@ -38,21 +38,28 @@ def _mix():
     return reqs
 
 
-def _direct(ctx, req, dirs):
-    """One DomainModel solve, filled with the direct sum as the server fills."""
+def _direct(ctx, req, dirs, method):
+    """One DomainModel solve, filled with the fill method the server uses."""
     amps, gs, qmax, Q, prec = req
     for a in amps:
         for leaf in (a, getattr(a, "child", None)):
             if leaf is not None:
                 leaf._grid = None
-    with fill_method(ctx, _lib.DPX_FILL_DIRECT):
+    with fill_method(ctx, method):
         return M.DomainModel(amps, gs, qmax, prec).CalculateIntensityVector(ctx, Q, 0.0, len(dirs), dirs)
 
 
-def test_server_same_alone_and_in_the_mix(ctx):
+@pytest.fixture(params=[_lib.DPX_FILL_HARMONIC, _lib.DPX_FILL_DIRECT], ids=["harmonic", "direct"])
+def method(request, ctx):
+    """The server fills with the context's FP32 fill method."""
+    with fill_method(ctx, request.param):
+        yield request.param
+
+
+def test_server_same_alone_and_in_the_mix(ctx, method):
     dirs = M.mc_directions(13, 640)
     reqs = _mix()
-    direct = [_direct(ctx, r, dirs) for r in reqs]
+    direct = [_direct(ctx, r, dirs, method) for r in reqs]
     # alone: one request at a time through a fresh server
     alone = []
     for r in reqs:
@@ -75,13 +82,14 @@ def test_server_same_alone_and_in_the_mix(ctx):
     # filled once within the same turn); no (leaf, grid) is filled twice:
     # FP32 a@24, b@20, c@28, b@28, d@24 and FP64 a@24, d@16
     assert st["grid_fills"] == 7
-    assert st["fill_launches"] <= st["grid_fills"]
+    if method == _lib.DPX_FILL_DIRECT:  # one batched launch per turn, FP64 one per grid
+        assert st["fill_launches"] <= st["grid_fills"]
 
 
-def test_server_budget_evicts_and_rejects(ctx):
+def test_server_budget_evicts_and_rejects(ctx, method):
     dirs = M.mc_directions(14, 256)
     reqs = _mix()[:4]
-    direct = [_direct(ctx, r, dirs) for r in reqs]
+    direct = [_direct(ctx, r, dirs, method) for r in reqs]
     import dpx
     g28 = dpx.lib().dpx_grid_bytes(28, M.FP32)
     # room for about two grids: later requests evict earlier, unpinned grids
