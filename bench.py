@@ -410,7 +410,41 @@ def run_dpx(args):
     _lib.check(L.dpx_leaf_destroy(leaf))
     grid.close()
     ctx.close()
+    if out is not None and world == 1 and not args.no_extras:
+        out.update(headline_extras(args))
     return out
+
+
+def headline_extras(args):
+    """The metric's other two workloads, as keys of the default line: the
+    uneven batch of 512 structures (one graph per wave) and the served Poisson
+    stream, each FP32-bulk against the plain FP64 GPU path on a seeded
+    subsample of the same work (solves/s ratio and max relative I(q) error),
+    the stream with its p50 / p99 latency.  Each runs on its own context after
+    the subunit's is closed."""
+    import argparse as _ap
+    import torch
+    torch.cuda.synchronize()
+    b = run_batch(_ap.Namespace(**dict(vars(args), steps=min(args.steps, 5), warmup=1, fp64_sample=8,
+                                       autotune=False, e2e_steps=1, batch_size=512)))
+    torch.cuda.synchronize()
+    v = run_serve(_ap.Namespace(**dict(vars(args), requests=200, rate=200.0, fp64_sample=8, warmup=3)))
+    f64b, f64s = b.get("fp64_plain", {}), v.get("fp64_plain", {})
+    return {
+        "batch": {"workload": b["config"]["workload"], "value": b["value"], "unit": "solves/s", "steps": b["steps"],
+                  "ms_per_step": b["ms_per_step"], "e2e": b["e2e"]["value"], "waves": b["config"]["waves"],
+                  "gpu_launches_per_step": b["gpu_launches"] // max(1, b["steps"]),
+                  "fp64_plain_solves_per_s_on_sample": f64b.get("fp64_solves_per_s"),
+                  "speedup_fp32_vs_fp64_same_sample": f64b.get("speedup_fp32_vs_fp64"),
+                  "max_rel_err_vs_fp64": f64b.get("max_rel_err_fp32_vs_fp64"),
+                  "fp64_sample": f64b.get("sample"), "clocks": b["clocks"]},
+        "serve": {"workload": v["config"]["workload"], "value": v["value"], "unit": "solves/s",
+                  "arrival_rate_hz": 200.0, "latency_ms": v["latency_ms"], "server": v["server"],
+                  "fp64_plain_solves_per_s_on_sample": f64s.get("fp64_solves_per_s"),
+                  "speedup_served_vs_fp64": f64s.get("speedup_served_vs_fp64"),
+                  "max_rel_err_vs_fp64": f64s.get("max_rel_err_fp32_vs_fp64"),
+                  "fp64_sample": f64s.get("sample"), "clocks": v["clocks"]},
+    }
 
 
 BATCH_NQ, BATCH_DIRS = 200, 100_000
@@ -418,7 +452,7 @@ BATCH_NQ, BATCH_DIRS = 200, 100_000
 
 def run_batch(args):
     """Independent solves of uneven size in one batch (dpx_batch: one CUDA graph
-    per wave, one FP32 fill launch per wave); FP32-bulk for the whole mix, the
+    per wave with the harmonic fills planned at creation); FP32-bulk for the whole mix, the
     plain FP64 path on a seeded subsample of it for the speed ratio and the
     error."""
     import torch
@@ -498,12 +532,16 @@ def run_batch(args):
                    "structures": len(mix), "atom_cell_pairs": pairs, "waves": waves, "grid_pool_bytes": pool,
                    "l2": "every grid >= 8 MB and the wave's grids together >> 129 MB L2"},
         "e2e": {"value": n_tot / e2e_s, "unit": "solves/s",
-                "h2d_bytes_per_step": int(sum(16 * s.atoms for s in mix) + dirs.nbytes + sum(q.nbytes for q in Qs)),
-                "d2h_bytes_per_step": int(sum(q.nbytes for q in Qs))},
+                "h2d_bytes_per_step": int(sum(16 * s.atoms for s in mix) + dirs.nbytes + sum(q.nbytes for q in Qs)
+                                          + sum(0 if lf.solvent_boxes() is None else lf.solvent_boxes().nbytes
+                                                for lf in leaves)),
+                "d2h_bytes_per_step": int(sum(q.nbytes for q in Qs)),
+                "note": "per step: the batch created from host leaves (upload, harmonic plans, graph recording), "
+                        "run, and its I(q) read back"},
         "gpu_launches": int(launches) * args.steps,
-        "roofline": {"bound": "sfu", "kernel": "fill_f32_%s" % ("persistent" if ctx.fill_shape()[2] else "flat"),
-                     "algorithmic_pairs_per_s": pairs * args.steps / (dev_ms / 1e3),
-                     "note": "whole-batch time (fill + splines + average); per-kernel split in the subunit line"},
+        "fill_method": "harmonic" if ctx.fill_method() == 1 else "direct",
+        "roofline": {"note": "whole-batch time (fill + average per structure); per-kernel rooflines in the "
+                             "subunit line", "equivalent_direct_pairs_per_s": pairs * args.steps / (dev_ms / 1e3)},
         "generation_s": gen_s,
     }
     if tune:
@@ -740,8 +778,9 @@ def run_serve(args):
                 "h2d_bytes_per_step": int(sum(16 * len(r.leaf.xyz) + (0 if r.copies is None else 48 * len(r.copies[1]))
                                               for r in stream)),
                 "d2h_bytes_per_step": int(sum(r.Q.nbytes for r in stream))},
-        # per grid: its splines (+1); per request: the average and I(0)
-        "gpu_launches": int(st["fill_launches"] + 2 * st["grid_fills"] + (AVERAGE_LAUNCHES + 1) * st["completed"]),
+        # the fills' kernels (harmonic: tables, moments, contractions, the synthesis,
+        # which writes the spline derivatives); per request: the average and I(0)
+        "gpu_launches": int(st["fill_launches"] + (AVERAGE_LAUNCHES + 1) * st["completed"]),
         "server": st, "generation_s": gen_s, "clocks": clk.summary(),
     }
     if args.fp64_sample > 0 and rank == 0:
@@ -989,7 +1028,8 @@ def main():
                     help="skip the error report (plain FP64 solve and FP64 direct-sum sample)")
     ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
     ap.add_argument("--workload", default="subunit", choices=["subunit", "batch", "serve", "assembly"])
-    ap.add_argument("--no-extras", action="store_true", help="assembly: skip the VEGAS / GK / FP64 extras")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="subunit: skip the batch and serving keys; assembly: skip the VEGAS / GK / FP64 extras")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--inflight", type=int, default=32)
@@ -1001,6 +1041,7 @@ def main():
         apply_profile_shape(args.profile_shape)
         args.no_cpu_baseline = True
         args.no_error = True
+        args.no_extras = True
     if args.impl == "reference":
         out = run_reference(args)
     else:
