@@ -18,6 +18,8 @@
 
 #include <complex>
 #include <cstring>
+#include <fstream>
+#include <string>
 #include <vector>
 
 extern "C" {
@@ -113,6 +115,34 @@ int ref_aff_qmajor(int U, const int* atoms_per_ion, const float* coeffs, const f
     /* GetQMajorAFFMatrix maps an [nq x U] column-major array; return it q-major */
     for (int k = 0; k < nq; k++)
         for (int u = 0; u < U; u++) out[k * U + u] = m[k + u * nq];
+    return 0;
+}
+
+/* The reference's binary amplitude file, version 13: JacobianSphereGrid::
+ * ExportBinaryData (Grid.cpp:847-890) of the given values. */
+int ref_amp_write(const char* path, const char* header, int grid_size, double qmax, const double* data) {
+    JacobianSphereGrid grid((unsigned short)grid_size, qmax);
+    long long n = (long long)(grid.GetRealSize() / sizeof(double));
+    std::memcpy(grid.GetDataPointer(), data, sizeof(double) * n);
+    std::ofstream f(path, std::ios::binary);
+    return grid.ExportBinaryData(f, std::string(header ? header : "")) ? 0 : -1;
+}
+
+/* JacobianSphereGrid::ImportBinaryData (Grid.cpp:892-963) into a grid of
+ * (grid_size, qmax): the values, the step it read and the header text. */
+int ref_amp_read(const char* path, int grid_size, double qmax, double* out_data, double* step, char* header,
+                 int header_cap) {
+    JacobianSphereGrid grid((unsigned short)grid_size, qmax);
+    std::ifstream f(path, std::ios::binary);
+    std::string head;
+    if (!grid.ImportBinaryData(f, head)) return -1;
+    long long n = (long long)(grid.GetRealSize() / sizeof(double));
+    std::memcpy(out_data, grid.GetDataPointer(), sizeof(double) * n);
+    *step = grid.GetStepSize();
+    if (header && header_cap > 0) {
+        std::strncpy(header, head.c_str(), (size_t)header_cap - 1);
+        header[header_cap - 1] = 0;
+    }
     return 0;
 }
 

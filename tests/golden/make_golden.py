@@ -8,8 +8,10 @@ argument (or DPX_REF_ROOT); the GPU machine and the tests only read the committed JS
 * single_atom.json  — the deterministic single-atom known-answer fixtures
   (PythonInterface/tests/reviewer_tests/files_for_tests/generate/cpu/short/
   {c,n,o,h}_explicit_*, {ch,ch2,ch3,nh,nh2,nh3,oh}_implicit_*): state
-  parameters and the reference's I(q) columns, plus the reference's own
-  coefficient rows and dummy radii for those ions (PDBReaderLib.cpp).
+  parameters, the state document itself (without its viewport and fitting
+  blocks) with its one-atom PDB record, and the reference's I(q) columns,
+  plus the reference's own coefficient rows and dummy radii for those ions
+  (PDBReaderLib.cpp).
 * points.json       — the six-atom statistical fixture points_explicit_* (q, I, sigma).
 """
 from __future__ import annotations
@@ -108,7 +110,14 @@ def main():
         d = os.path.join(FIX, name)
         st = read_state(os.path.join(d, name + ".state"))
         q, I, s = read_out(os.path.join(d, name + "TestStandard.out"))
-        fixtures.append(dict(name=name, ion=GROUPS[m.group(1)], q=q, I=I, sigma=s, **st))
+        doc = json.load(open(os.path.join(d, name + ".state")))
+        doc.pop("Viewport", None)
+        doc.pop("FittingPreferences", None)
+        pdbs = [x for x in os.listdir(d) if x.lower().endswith(".pdb")]
+        pdb_lines = [ln for ln in open(os.path.join(d, pdbs[0])).read().split("\n")
+                     if ln[:6] in ("ATOM  ", "HETATM")] if pdbs else []
+        fixtures.append(dict(name=name, ion=GROUPS[m.group(1)], q=q, I=I, sigma=s, state=doc,
+                             pdb_name=pdbs[0] if pdbs else None, pdb_lines=pdb_lines, **st))
     json.dump(dict(ions=ions, fixtures=fixtures), open(os.path.join(HERE, "single_atom.json"), "w"))
 
     pts = []

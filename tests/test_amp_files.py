@@ -71,3 +71,39 @@ def test_ampj_layout_is_read(tmp_path):
         z.writestr("header.json", json.dumps({"Old Header:": "hdr", "Header": {}}))
     g2, q2, h2, v2 = M.read_amp(p)
     assert (g2, q2, h2) == (gs, qmax, "hdr") and np.array_equal(v2, v)
+
+
+def _ref():
+    import oracle as O
+    if not O.have_ref():
+        pytest.skip("the reference's own Grid.cpp pin library is built only where the reference checkout is")
+    import ctypes as C
+    L = O.ref()
+    D = C.POINTER(C.c_double)
+    L.ref_amp_write.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_double, D]
+    L.ref_amp_read.argtypes = [C.c_char_p, C.c_int, C.c_double, D, D, C.c_char_p, C.c_int]
+    return L
+
+
+@pytest.mark.parametrize("gs,qmax,header", [(20, 5.0, "made by dpx"), (36, 7.5, "a header"), (12, 2.0, "")])
+def test_amp_files_pinned_to_the_reference_both_ways(tmp_path, gs, qmax, header):
+    """The library's .amp writer and reader against the reference's own
+    JacobianSphereGrid::ExportBinaryData / ImportBinaryData (Grid.cpp:847-963),
+    compiled from the reference's sources: each reads the other's file to the
+    bit, with the same step and header."""
+    import ctypes as C
+    L = _ref()
+    v = _values(gs, 7 + gs)
+    step = qmax / (gs // 2)
+    ours = str(tmp_path / "dpx.amp")
+    _lib.check(dpx.lib().dpx_amp_write(ours.encode(), header.encode(), gs, step, _lib.dptr(v)))
+    got = np.zeros_like(v)
+    st = C.c_double()
+    buf = C.create_string_buffer(256)
+    assert L.ref_amp_read(ours.encode(), gs, qmax, _lib.dptr(got), C.byref(st), buf, 256) == 0
+    assert np.array_equal(got, v) and st.value == step
+    theirs = str(tmp_path / "ref.amp")
+    assert L.ref_amp_write(theirs.encode(), header.encode(), gs, qmax, _lib.dptr(v)) == 0
+    g2, q2, h2, v2 = M.read_amp(theirs)
+    assert g2 == gs and abs(q2 - qmax) < 1e-12 and h2 == header and np.array_equal(v2, v)
+    assert open(ours, "rb").read() == open(theirs, "rb").read()  # the same bytes

@@ -763,3 +763,19 @@ def test_json_state_runs_end_to_end(ctx, tmp_path):
     ref = 2.0 * (by_hand1.CalculateIntensityVector(ctx, Q, 0.0, 300, dirs)
                  + 0.5 * by_hand2.CalculateIntensityVector(ctx, Q, 0.0, 300, dirs)) + 0.25
     assert rel(I, ref) <= 1e-9
+
+
+@pytest.mark.parametrize("idx", [0, 5, 9, 13, 21])
+def test_single_atom_states_through_the_decoder(ctx, idx):
+    """The reference's single-atom state documents decoded by dpx.state and run
+    through the Job: I(q) equals the reference's within its printed digits
+    (amplitudes within 2e-6 of the largest), FP64 and FP32 bulk."""
+    from dpx import state as S
+    with open(os.path.join(GOLD, "single_atom.json")) as f:
+        fx = json.load(f)["fixtures"][idx]
+    job = S.decode(fx["state"], files={fx["pdb_name"]: fx["pdb_lines"]})
+    dirs = M.mc_directions(42, 600)
+    ref = np.array(fx["I"])
+    for prec in (M.FP64, M.FP32):
+        I = job.intensity(ctx, np.array(fx["q"]), dirs=dirs, precision=prec, iterations=600)
+        assert np.max(np.abs(np.sqrt(I) - np.sqrt(ref))) <= 2e-6 * np.sqrt(ref.max()), fx["name"]

@@ -117,3 +117,25 @@ def test_grid_subtree_stays_one_assembly_grid(tmp_path):
         assert isinstance(ms.child.child, M.PDBAmplitude)
         assert np.allclose(ms.child.trans[0], [-4, -2, -8.13]) and np.allclose(ms.child.rot[0], [np.pi / 2, 0, 0])
         assert np.allclose(ms.trans[:, 0], [0, 4, 8])
+
+
+def test_reference_single_atom_states_decode():
+    """The reference's own single-atom state documents (generate/cpu/short/
+    {c,n,o,h}_explicit_*, {ch,...,oh}_implicit_*, kept in tests/golden with their
+    one-atom PDB records) decode to the grid, method and leaf they describe."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "single_atom.json")) as f:
+        fixtures = json.load(f)["fixtures"]
+    assert len(fixtures) == 22
+    for fx in fixtures:
+        job = S.decode(fx["state"], files={fx["pdb_name"]: fx["pdb_lines"]})
+        assert (job.grid_size, job.qmax, job.convergence) == (fx["gridSize"], fx["qMax"], fx["convergence"])
+        assert job.method == S.METHODS[fx["method"]]
+        (w, amps), = job.populations
+        leaf, = amps
+        assert isinstance(leaf, M.PDBAmplitude) and leaf.symbols == [fx["ion"]], fx["name"]
+        e = fx["extra"]
+        assert (leaf.scale, leaf.solventED, leaf.c1, leaf.outerSolventED) == (e[0], e[1], e[2], e[6])
+        if fx["centered"]:
+            assert np.allclose(leaf.xyz, 0.0)
