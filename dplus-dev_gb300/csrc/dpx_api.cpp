@@ -107,6 +107,22 @@ void aff_table(int U, const int* api, const double* coeffs, const double* rads, 
     aff_at(U, api, coeffs, rads, flags, sol_ed, c1, Lp + 1, q.data(), out);
 }
 
+void leaf_aff_table(const dpx_pdb_desc& d, int Lp, double step, std::vector<double>& out) {
+    if (!d.aff) {
+        aff_table(d.n_ions, d.atoms_per_ion, d.coeffs, d.ion_rads, d.flags, d.solvent_ed, d.c1, Lp, step, out);
+        return;
+    }
+    out.assign((size_t)d.n_ions * (Lp + 1), 0.0);
+    for (int u = 0; u < d.n_ions; ++u)
+        for (int k = 0; k <= Lp && k < d.aff_n; ++k) out[(size_t)u * (Lp + 1) + k] = d.aff[(size_t)u * d.aff_n + k];
+}
+
+int check_leaf_grid(const dpx_pdb_desc& d, const dpx::Geom& G) {
+    if (d.aff && d.aff_n < G.Lp + 1)
+        return fail(DPX_ERR_ARG, "the tabulated form factors cover %d shells; the grid has %d", d.aff_n, G.Lp + 1);
+    return DPX_OK;
+}
+
 // Tait-Bryan X1Y2Z3 rotation (the reference's EulerD, Amplitude.h:557-573).
 void euler(double a, double b, double c, double R[9]) {
     const double c1 = std::cos(a), s1 = std::sin(a), c2 = std::cos(b), s2 = std::sin(b), c3 = std::cos(c),
@@ -146,7 +162,9 @@ void dpx::q_brackets(int grid_size, double qmax, int nq, const double* Q, int* l
 namespace {
 using dpx::q_brackets;
 
-int grid_from_voxels(int64_t voxels, int thDivs, int phDivs, double stepSize, int* grid_size, double* qmax) {
+}  // namespace
+
+int dpxh::grid_from_voxels(int64_t voxels, int thDivs, int phDivs, double stepSize, int* grid_size, double* qmax) {
     if (thDivs != 3 || phDivs != 6) return fail(DPX_ERR_ARG, "only thDivs=3, phDivs=6 grids exist");
     for (int lp = 4; lp < 4096; ++lp) {
         const int64_t P = 6 * (int64_t)lp * (lp + 1) * (lp + 1) + 1;
@@ -159,8 +177,6 @@ int grid_from_voxels(int64_t voxels, int thDivs, int phDivs, double stepSize, in
     }
     return fail(DPX_ERR_ARG, "voxels=%lld is not a Jacobian sphere grid size", (long long)voxels);
 }
-
-}  // namespace
 
 extern "C" {
 
@@ -405,8 +421,9 @@ namespace dpxh {
 int check_pdb(const dpx_pdb_desc& d) {
     if (d.n_atoms <= 0 || !d.atoms) return fail(DPX_ERR_ARG, "no atoms");
     if (d.n_atoms > INT_MAX) return fail(DPX_ERR_ARG, "too many atoms (%lld)", (long long)d.n_atoms);
-    if (d.n_ions <= 0 || d.n_ions > 256 || !d.atoms_per_ion || !d.coeffs || !d.ion_rads)
+    if (d.n_ions <= 0 || d.n_ions > 256 || !d.atoms_per_ion || (!d.aff && (!d.coeffs || !d.ion_rads)))
         return fail(DPX_ERR_ARG, "bad ion description");
+    if (d.aff && d.aff_n <= 0) return fail(DPX_ERR_ARG, "aff_n must be positive with a tabulated aff");
     int64_t tot = 0;
     for (int u = 0; u < d.n_ions; ++u) {
         if (d.atoms_per_ion[u] < 0) return fail(DPX_ERR_ARG, "negative atoms_per_ion");
@@ -450,6 +467,7 @@ int fill_batch_impl(int n, const dpx_grid* grids, const dpx_pdb_desc* pdbs, int 
     for (int j = 0; j < n; ++j) {
         if (!grids[j] || grids[j]->ctx != ctx) return fail(DPX_ERR_ARG, "every grid of a batch needs the same context");
         if (int rc = check_pdb(pdbs[j])) return rc;
+        if (int rc = check_leaf_grid(pdbs[j], grids[j]->g)) return rc;
         for (int k = 0; k < j; ++k)
             if (grids[k] == grids[j]) return fail(DPX_ERR_ARG, "a grid appears twice in one batch");
     }
@@ -1389,6 +1407,17 @@ int dpx_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xy
     return DPX_OK;
 }
 
+namespace {
+// The body of both grid-amplitude drop-ins: form factors from coefficients
+// (coeffs, ionRads) or tabulated (affs, nq).
+int pdb_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
+                       const float* atomLocations, int64_t numAtoms, int numUniqueIons, const int* atomsPerIon,
+                       const float* coeffs, const float* ionRads, const float* affs, int nq, int bitCombination,
+                       float solventED, float c1, const float* solCOM, const int* solDims, int64_t nSol,
+                       double voxStep, const float* outSolCOM, const int* outSolDims, int64_t nOutSol,
+                       double outerSolED, double scale, int precision, int* pStop);
+}  // namespace
+
 int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
                                     const float* atomLocations, int64_t numAtoms, int numUniqueIons,
                                     const int* atomsPerIon, const float* coeffs, const float* ionRads,
@@ -1396,7 +1425,37 @@ int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, dou
                                     const int* solDims, int64_t nSol, double voxStep, const float* outSolCOM,
                                     const int* outSolDims, int64_t nOutSol, double outerSolED, double scale,
                                     int precision, int* pStop) {
+    if (!coeffs) return fail(DPX_ERR_ARG, "NULL coefficients");
+    return pdb_grid_amplitude(voxels, thDivs, phDivs, stepSize, outData, atomLocations, numAtoms, numUniqueIons,
+                              atomsPerIon, coeffs, ionRads, nullptr, 0, bitCombination, solventED, c1, solCOM,
+                              solDims, nSol, voxStep, outSolCOM, outSolDims, nOutSol, outerSolED, scale, precision,
+                              pStop);
+}
+
+int dpx_pdb_jacobian_grid_amplitude_aff(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
+                                        const float* atomLocations, int64_t numAtoms, int numUniqueIons,
+                                        const int* atomsPerIon, const float* affs, int nq, int bitCombination,
+                                        float solventED, const float* solCOM, const int* solDims, int64_t nSol,
+                                        double voxStep, const float* outSolCOM, const int* outSolDims,
+                                        int64_t nOutSol, double outerSolED, double scale, int precision, int* pStop) {
+    if (!affs || nq <= 0) return fail(DPX_ERR_ARG, "NULL form-factor table");
+    return pdb_grid_amplitude(voxels, thDivs, phDivs, stepSize, outData, atomLocations, numAtoms, numUniqueIons,
+                              atomsPerIon, nullptr, nullptr, affs, nq, bitCombination, solventED, 1.0f, solCOM,
+                              solDims, nSol, voxStep, outSolCOM, outSolDims, nOutSol, outerSolED, scale, precision,
+                              pStop);
+}
+
+}  // extern "C"
+
+namespace {
+int pdb_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
+                       const float* atomLocations, int64_t numAtoms, int numUniqueIons, const int* atomsPerIon,
+                       const float* coeffs, const float* ionRads, const float* affs, int nq, int bitCombination,
+                       float solventED, float c1, const float* solCOM, const int* solDims, int64_t nSol,
+                       double voxStep, const float* outSolCOM, const int* outSolDims, int64_t nOutSol,
+                       double outerSolED, double scale, int precision, int* pStop) {
     if (!outData || !atomLocations) return fail(DPX_ERR_ARG, "NULL buffer");
+    if (numUniqueIons <= 0 || numUniqueIons > 256 || !atomsPerIon) return fail(DPX_ERR_ARG, "bad ion description");
     if ((nSol > 0 && (!solCOM || !solDims)) || (nOutSol > 0 && (!outSolCOM || !outSolDims)))
         return fail(DPX_ERR_ARG, "NULL voxel arrays");
     // voxel boxes as PDBJacobianGridAmplitudeCalculation applies them
@@ -1425,12 +1484,12 @@ int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, dou
     dpx_grid g;
     int rc = dpx_grid_create(ctx, grid_size, qmax, precision, &g);
     if (rc) { dpx_ctx_destroy(ctx); return rc; }
-    std::vector<double> cd(9 * numUniqueIons), rd(numUniqueIons);
-    for (int k = 0; k < 9 * numUniqueIons; ++k) cd[k] = coeffs[k];
-    for (int k = 0; k < numUniqueIons; ++k) rd[k] = ionRads ? ionRads[k] : 0.0;
-    dpx_pdb_desc d{numAtoms, atomLocations, 0, numUniqueIons, atomsPerIon, cd.data(), rd.data(),
-                   bitCombination & 3, solventED, c1, scale, nullptr, (int64_t)boxes.size() / 8,
-                   boxes.empty() ? nullptr : boxes.data(), voxStep};
+    std::vector<double> cd(coeffs ? 9 * numUniqueIons : 0), rd(coeffs ? numUniqueIons : 0);
+    for (size_t k = 0; k < cd.size(); ++k) cd[k] = coeffs[k];
+    for (size_t k = 0; k < rd.size(); ++k) rd[k] = ionRads ? ionRads[k] : 0.0;
+    dpx_pdb_desc d{numAtoms, atomLocations, 0, numUniqueIons, atomsPerIon, coeffs ? cd.data() : nullptr,
+                   coeffs ? rd.data() : nullptr, bitCombination & 3, solventED, c1, scale, nullptr,
+                   (int64_t)boxes.size() / 8, boxes.empty() ? nullptr : boxes.data(), voxStep, affs, nq};
     rc = dpx_grid_fill_pdb_batch(1, &g, &d);
     if (!rc && pStop && *pStop) rc = fail(DPX_ERR_STOPPED, "stopped");
     if (!rc) rc = dpx_grid_read(g, outData, nullptr);
@@ -1438,6 +1497,9 @@ int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, dou
     dpx_ctx_destroy(ctx);
     return rc;
 }
+}  // namespace
+
+extern "C" {
 
 int dpx_calc_mcoa_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double stepSz, const double* inAmp,
                              const double* inD, const double* qs, double* intensities, int qPoints, int64_t maxIters,

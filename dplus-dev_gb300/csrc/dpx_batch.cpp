@@ -105,6 +105,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         const dpx_solve_desc& d = solves[j];
         if (int rc = check_pdb(d.pdb)) return rc;
         if (d.grid_size < 2 || (d.grid_size & 1)) return fail(DPX_ERR_ARG, "solve %d: grid_size must be even", j);
+        if (int rc = check_leaf_grid(d.pdb, dpx::make_geom(d.grid_size, d.qmax))) return rc;
         if (!(d.qmax > 0)) return fail(DPX_ERR_ARG, "solve %d: qmax must be positive", j);
         if (d.nq <= 0 || !d.Q) return fail(DPX_ERR_ARG, "solve %d: no q values", j);
         for (int k = 1; k < d.nq; ++k)

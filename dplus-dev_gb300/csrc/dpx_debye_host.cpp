@@ -29,6 +29,7 @@ int dpx_debye_intensity(dpx_ctx ctx, const dpx_pdb_desc* d, const float* bfactor
     if (nq < 0) return fail(DPX_ERR_ARG, "nq < 0");
     if (precision != DPX_FP32 && precision != DPX_FP64) return fail(DPX_ERR_ARG, "bad precision %d", precision);
     if (int rc = check_pdb(*d)) return rc;
+    if (d->aff) return fail(DPX_ERR_ARG, "the Debye sum needs the form-factor coefficients, not a table");
     if (d->n_boxes > 0) return fail(DPX_ERR_ARG, "the Debye sum takes no voxelized-solvent boxes");
     for (int k = 0; k < nq; ++k)
         if (!(Q[k] >= 0.0) || !std::isfinite(Q[k])) return fail(DPX_ERR_ARG, "q[%d] is negative or not finite", k);

@@ -160,6 +160,7 @@ extern "C" int dpx_direct_intensity(dpx_ctx ctx, const dpx_pdb_desc* d, int n_co
     if (!ctx || !d || !Q || !dirs || !res) return fail(DPX_ERR_ARG, "NULL argument");
     if (int rc = check_pdb(*d)) return rc;
     if (d->atoms_on_device) return fail(DPX_ERR_ARG, "the direct sum takes host atoms");
+    if (d->aff) return fail(DPX_ERR_ARG, "the direct sum needs the form-factor coefficients, not a table");
     if (nq <= 0 || D <= 0) return fail(DPX_ERR_ARG, "nq and D must be positive");
     if (D > INT32_MAX) return fail(DPX_ERR_ARG, "too many directions");
     if (n_copies < 0 || (n_copies > 0 && (!copy_rot || !copy_tr))) return fail(DPX_ERR_ARG, "bad copy list");

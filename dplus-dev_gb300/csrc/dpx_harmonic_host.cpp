@@ -251,7 +251,7 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
     double nodes[6], vinv[36];
     chebyshev_fit(nodes, vinv);
     std::vector<double> affd;
-    aff_table(d.n_ions, d.atoms_per_ion, d.coeffs, d.ion_rads, d.flags, d.solvent_ed, d.c1, Lp, G.step, affd);
+    leaf_aff_table(d, Lp, G.step, affd);
     std::vector<float> aff(affd.begin(), affd.end());
     double origin = 0.0;  // F(0): the form factors at shell 0 times the ion counts, plus the box volumes
     for (int u = 0; u < d.n_ions; ++u) origin += affd[(size_t)u * (Lp + 1)] * d.atoms_per_ion[u];

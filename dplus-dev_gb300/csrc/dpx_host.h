@@ -150,9 +150,17 @@ void aff_table(int U, const int* api, const double* coeffs, const double* rads, 
 // The same at the nq values q[k], [U][nq].
 void aff_at(int U, const int* api, const double* coeffs, const double* rads, int flags, double sol_ed, double c1,
             int nq, const double* q, std::vector<double>& out);
+// A leaf's form factors on shells 0..Lp, [U][Lp+1]: its tabulated ones
+// (dpx_pdb_desc::aff) or aff_table of its coefficients.  check_leaf_grid
+// rejects a tabulated leaf whose table is shorter than the grid's shells.
+void leaf_aff_table(const dpx_pdb_desc& d, int Lp, double step, std::vector<double>& out);
+int check_leaf_grid(const dpx_pdb_desc& d, const dpx::Geom& G);
 // Tait-Bryan X1Y2Z3 rotation (EulerD).
 void euler(double a, double b, double c, double R[9]);
 int check_pdb(const dpx_pdb_desc& d);
+// grid_size and qmax of the reference's (voxels, thDivs, phDivs, stepSize)
+// description of a Jacobian sphere grid (voxels = complex cells).
+int grid_from_voxels(int64_t voxels, int thDivs, int phDivs, double stepSize, int* grid_size, double* qmax);
 
 // Model structs of one average and their docked-copy group tables.  build_models
 // stages the tables on the host (gstage) with offsets; place_models points the

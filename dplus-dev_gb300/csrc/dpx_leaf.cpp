@@ -52,6 +52,7 @@ int dpx_leaf_create(dpx_grid g, const dpx_pdb_desc* d, dpx_leaf* out) {
     if (!g || !d || !out) return fail(DPX_ERR_ARG, "NULL argument");
     *out = nullptr;
     if (int rc = check_pdb(*d)) return rc;
+    if (int rc = check_leaf_grid(*d, g->g)) return rc;
     dpx_ctx ctx = g->ctx;
     if (int rc = set_device(ctx)) return rc;
     auto* L = new dpx_leaf_s;

@@ -654,6 +654,10 @@ int dpx_server_submit(dpx_server S, const dpx_request* q, uint64_t* ticket) {
             delete r;
             return fail(DPX_ERR_ARG, "server requests take host atoms");
         }
+        if (d.aff) {
+            delete r;
+            return fail(DPX_ERR_ARG, "server requests take leaves with form-factor coefficients");
+        }
         LeafCopy& c = r->leaves[l];
         c.atoms.assign(d.atoms, d.atoms + 4 * d.n_atoms);
         c.api.assign(d.atoms_per_ion, d.atoms_per_ion + d.n_ions);

@@ -47,7 +47,7 @@ void stage_leaf(std::vector<char>& h, const dpx_pdb_desc& d, const dpx::Geom& G,
     for (int u = 0; u < d.n_ions; ++u) off[u + 1] = off[u] + d.atoms_per_ion[u];
     t.off = put(h, off.data(), off.size() * sizeof(int));
     std::vector<double> aff;
-    aff_table(d.n_ions, d.atoms_per_ion, d.coeffs, d.ion_rads, d.flags, d.solvent_ed, d.c1, G.Lp, G.step, aff);
+    leaf_aff_table(d, G.Lp, G.step, aff);
     if (fp32) {
         std::vector<float> af(aff.begin(), aff.end());
         t.aff = put(h, af.data(), af.size() * sizeof(float));

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libdpx.so")
 SOURCES = ["dpx_fill.cu", "dpx_kernels.cu", "dpx_api.cpp", "dpx_batch.cpp", "dpx_server.cpp", "dpx_stage.cpp",
            "dpx_voxel.cpp", "dpx_amp.cpp", "dpx_noalloc.cu", "dpx_debye.cu", "dpx_debye_host.cpp",
            "dpx_harmonic.cu", "dpx_harmonic_host.cpp", "dpx_direct.cu",
-           "dpx_leaf.cpp"]
+           "dpx_leaf.cpp", "dpx_hybrid.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

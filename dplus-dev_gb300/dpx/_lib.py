@@ -19,6 +19,7 @@ DPX_CALC_ATOMIC_FORMFACTORS = 1
 DPX_CALC_DUMMY_SOLVENT = 2
 DPX_FILL_DIRECT, DPX_FILL_HARMONIC = 0, 1
 DPX_CONV_CPU, DPX_CONV_GPU = 0, 1
+DPX_OA_MC, DPX_OA_VEGAS = 0, 1
 
 _STATUS = {-1: "DPX_ERR_ARG", -2: "DPX_ERR_CUDA", -3: "DPX_ERR_OOM", -4: "DPX_ERR_STOPPED",
            -5: "DPX_ERR_NODEVICE"}
@@ -42,7 +43,7 @@ class PdbDesc(C.Structure):
     _fields_ = [("n_atoms", C.c_int64), ("atoms", _P), ("atoms_on_device", C.c_int), ("n_ions", C.c_int),
                 ("atoms_per_ion", _I), ("coeffs", _D), ("ion_rads", _D), ("flags", C.c_int),
                 ("solvent_ed", C.c_double), ("c1", C.c_double), ("scale", C.c_double), ("center", _D),
-                ("n_boxes", C.c_int64), ("boxes", _F), ("voxel_step", C.c_double)]
+                ("n_boxes", C.c_int64), ("boxes", _F), ("voxel_step", C.c_double), ("aff", _F), ("aff_n", C.c_int)]
 
 class SolveDesc(C.Structure):
     """dpx_solve_desc: one solve of a dpx_batch."""
@@ -114,6 +115,10 @@ _SIGS = {
                                                   C.c_int, _I, _F, _F, C.c_int, C.c_float, C.c_float, _F, _I,
                                                   C.c_int64, C.c_double, _F, _I, C.c_int64, C.c_double, C.c_double,
                                                   C.c_int, _I]),
+    "dpx_pdb_jacobian_grid_amplitude_aff": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.c_double, _D, _F, C.c_int64,
+                                                      C.c_int, _I, _F, C.c_int, C.c_int, C.c_float, _F, _I,
+                                                      C.c_int64, C.c_double, _F, _I, C.c_int64, C.c_double,
+                                                      C.c_double, C.c_int, _I]),
     "dpx_calc_mcoa_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, C.c_int,
                                            C.c_int64, C.c_double, _D, C.c_int64, C.c_int, _I]),
     "dpx_calc_man_sym_jacob_sphr": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D, _D,
@@ -141,6 +146,15 @@ _SIGS = {
     "dpx_boxes_get": (C.c_int, [_P, C.c_int, _F, _I]),
     "dpx_boxes_space": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dpx_boxes_free": (C.c_int, [_P]),
+    "dpx_hybrid_create": (C.c_int, [_P, C.c_int, _F, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    C.c_int, C.POINTER(_P)]),
+    "dpx_hybrid_set_num_children": (C.c_int, [_P, C.c_int]),
+    "dpx_hybrid_child_pdb": (C.c_int, [_P, C.c_int, C.POINTER(PdbDesc)]),
+    "dpx_hybrid_child_amp": (C.c_int, [_P, C.c_int, _D]),
+    "dpx_hybrid_add_rotations": (C.c_int, [_P, C.c_int, C.c_int, _F]),
+    "dpx_hybrid_add_translations": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _F]),
+    "dpx_hybrid_compute_intensity": (C.c_int, [_P, C.c_int, _D, C.c_double, C.c_int64, C.c_uint64, _I]),
+    "dpx_hybrid_destroy": (C.c_int, [_P]),
     "dpx_measure_sfu_peak": (C.c_int, [_P, _D]),
     "dpx_debye_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), _F, _F, C.c_int, _D, C.c_int, _D]),
     "dpx_direct_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), C.c_int, _D, _D, C.c_int, _D, C.c_int64, _D, _D]),

@@ -31,6 +31,13 @@
  *                                       (Backend/Backend/PDBAmplitude.cpp:1652-1716, 1789-1967)
  *   dpx_calc_debye_v2                <- GPUCalcDebyeV2 (Backend/GPU/InternalGPUHeaders.h:61,
  *                                       DebyeCalculator.cu:164-372)
+ *   dpx_pdb_jacobian_grid_amplitude_aff <- PDBJacobianGridAmplitudeCalculation with the
+ *                                       form factors as its atomicFFCalculator tabulates them
+ *                                       (PDBAmplitudeCUDA.cu:224-284)
+ *   dpx_hybrid_*                     <- IGPUGridCalculator of GPUCreateCalculatorHybrid
+ *                                       (Backend/GPU/GPUInterface.h:203-222, GPUHeader.cpp:39-42)
+ *                                       and GPUHybrid_SetPDB / GPUHybrid_PDBAmplitude
+ *                                       (HybridPDB.cu:168-379)
  */
 #ifndef DPX_H
 #define DPX_H
@@ -181,6 +188,16 @@ typedef struct dpx_pdb_desc {
     /* the voxel edge (nm) the boxes were built on; 0 = unknown.  The
      * harmonic fill expands boxes into voxels and needs it. */
     double voxel_step;
+    /* optional: the ions' form factors already tabulated on the grid's
+     * shells, as the reference's atomicFFCalculator::GetQMajorAFFMatrix(aff,
+     * aff_n, step) writes them (Backend/GPU/Atomic Form Factor.cpp:58-64, called
+     * so by PDBAmplitudeCUDA.cu:284): aff[u * aff_n + k] at q = k * step, the
+     * dummy-atom solvent included, aff_n >= the grid's layers + 4.  When set,
+     * coeffs, ion_rads, flags, solvent_ed and c1 are not read; the FP64 direct
+     * sum and the Debye sum, which need form factors at any q, reject such a
+     * leaf.  NULL: the form factors are computed from the coefficients. */
+    const float* aff;
+    int aff_n;
 } dpx_pdb_desc;
 /* Fills n grids (distinct, one context) from n leaves.  The FP32 grids of the
  * batch share ONE launch over the tiles of every leaf (flat: one CTA per tile;
@@ -300,6 +317,18 @@ int dpx_make_globule(int64_t n_atoms, double radius_nm, uint64_t seed, float* xy
  * outerSolED - solventED, each set only with more than four boxes.  Returns 0
  * or a negative status (the reference returns -3000-err / -1000-err; callers
  * test != 0). */
+/* The same with the form factors as the reference's call site has them: affs
+ * [numUniqueIons][nq] from atomicFFCalculator::GetQMajorAFFMatrix(affs, nq,
+ * stepSize) with nq = the grid's layers + 4 (numQLayers + 1 of
+ * PDBAmplitudeCUDA.cu:224-284), the dummy-atom solvent folded in; atomsPerIon
+ * from GetNumAtomsPerIon; bitCombination from GetBitCombination (its
+ * CALC_VOXELIZED_SOLVENT bit selects the excluded-volume boxes). */
+int dpx_pdb_jacobian_grid_amplitude_aff(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
+                                        const float* atomLocations, int64_t numAtoms, int numUniqueIons,
+                                        const int* atomsPerIon, const float* affs, int nq, int bitCombination,
+                                        float solventED, const float* solCOM, const int* solDims, int64_t nSol,
+                                        double voxStep, const float* outSolCOM, const int* outSolDims,
+                                        int64_t nOutSol, double outerSolED, double scale, int precision, int* pStop);
 int dpx_pdb_jacobian_grid_amplitude(uint64_t voxels, int thDivs, int phDivs, double stepSize, double* outData,
                                     const float* atomLocations, int64_t numAtoms, int numUniqueIons,
                                     const int* atomsPerIon, const float* coeffs, const float* ionRads,
@@ -378,6 +407,43 @@ int dpx_sum_grids_jacob_sphr(int64_t voxels, int thDivs, int phDivs, double step
  * FP64 sincos, so callers use it on a sample of q values and directions. */
 int dpx_direct_intensity(dpx_ctx ctx, const dpx_pdb_desc* d, int n_copies, const double* copy_rot,
                          const double* copy_tr, int nq, const double* Q, int64_t D, const double* dirs, double* res);
+
+/* ---- the hybrid calculator: IGPUGridCalculator (Backend/GPU/GPUInterface.h:
+ * 203-222) made by GPUCreateCalculatorHybrid (GPUHeader.cpp:39-42) and driven by
+ * DomainModel::PerformGPUHybridComputation (Backend/Backend/Amplitude.cpp:
+ * 2044-2289), with its leaf hooks GPUHybrid_SetPDB / GPUHybrid_PDBAmplitude
+ * (HybridPDB.cu:168-379) and GPUHybrid_AmpGridAmplitude ----
+ * dpx_hybrid_create = GPUCreateCalculatorHybrid + Initialize of the master
+ * workspace: the q points as the reference passes them (float, ascending,
+ * within qMax), totalSize = 2 x cells, thetaDivisions 3, phiDivisions 6,
+ * qLayers = layers + 4, qMax, stepSize; FP32 bulk or plain FP64 grids.
+ * A child is one distinct leaf: its amplitude grid comes from a PDB leaf (the
+ * fill of dpx_grid_fill_pdb_batch, with its phi-spline derivatives) or from
+ * given amplitudes [2 cells] (derivatives computed).  AddRotations gives a
+ * child's rotations as float4 {alpha, beta, gamma (radians, EulerD), scale}
+ * and AddTranslations, per rotation index, its translations as float4
+ * {x, y, z (nm), 0} (the flattened tree, Amplitude.cpp:2151-2183).
+ * ComputeIntensity: I(q) = < |sum_children sum_rotations scale sum_translations
+ * e^{i q.t} A_child(R^T q)|^2 > over orientations, outData [nq]:
+ *   DPX_OA_MC     seeded mt19937 directions (min(iterations, 2^22) of them,
+ *                 shared by the brackets) and the reference GPU averages'
+ *                 convergence test at epsi, 4096 samples a step
+ *                 (GPUHybridCalc.cu:467-578, 705-720);
+ *   DPX_OA_VEGAS  dpx_vegas_intensity with 4096 points an iteration up to
+ *                 iterations points (GPUHybridCalc.cu:581-703).
+ * pStop is read before and after.  dpx_hybrid_destroy = FreeWorkspace + delete. */
+enum { DPX_OA_MC = 0, DPX_OA_VEGAS = 1 };
+typedef struct dpx_hybrid_s* dpx_hybrid;
+int dpx_hybrid_create(dpx_ctx ctx, int nq, const float* qPoints, int64_t totalSize, int thetaDivs, int phiDivs,
+                      int qLayers, double qMax, double stepSize, int precision, dpx_hybrid* out);
+int dpx_hybrid_set_num_children(dpx_hybrid h, int n);
+int dpx_hybrid_child_pdb(dpx_hybrid h, int child, const dpx_pdb_desc* d);
+int dpx_hybrid_child_amp(dpx_hybrid h, int child, const double* amp);
+int dpx_hybrid_add_rotations(dpx_hybrid h, int child, int n, const float* rotations);
+int dpx_hybrid_add_translations(dpx_hybrid h, int child, int rotation, int n, const float* translations);
+int dpx_hybrid_compute_intensity(dpx_hybrid h, int method, double* outData, double epsi, int64_t iterations,
+                                 uint64_t seed, int* pStop);
+int dpx_hybrid_destroy(dpx_hybrid h);
 
 /* SFU calibration (no counterpart in the reference): times a kernel of
  * independent __sincosf chains and returns the MUFU operations per second this

@@ -779,3 +779,69 @@ def test_single_atom_states_through_the_decoder(ctx, idx):
     for prec in (M.FP64, M.FP32):
         I = job.intensity(ctx, np.array(fx["q"]), dirs=dirs, precision=prec, iterations=600)
         assert np.max(np.abs(np.sqrt(I) - np.sqrt(ref))) <= 2e-6 * np.sqrt(ref.max()), fx["name"]
+
+
+@pytest.mark.parametrize("prec,tol", [(M.FP64, TOL64), (M.FP32, TOL32)])
+def test_hybrid_calculator_matches_oracle(ctx, prec, tol):
+    """The IGPUGridCalculator drop-in (dpx_hybrid_*): one PDB child with three
+    rotations of two translations each, Monte Carlo with the reference GPU
+    averages' convergence test, against the oracle's docked sum of the same
+    copies over the same seeded directions."""
+    amp = globule(300, 1.2, seed=61, extra=SOLVENT)
+    gs, qmax = 24, 4.0
+    L = dpx.lib()
+    P = L.dpx_grid_cells(gs)
+    Q = (np.arange(1, 49) / 12.0).astype(np.float32)  # exact in float
+    h = C.c_void_p()
+    _lib.check(L.dpx_hybrid_create(ctx.handle, len(Q), _lib.fptr(Q), 2 * P, 3, 6, gs // 2 + 4, qmax, qmax / (gs // 2),
+                                   prec, C.byref(h)))
+    _lib.check(L.dpx_hybrid_set_num_children(h, 1))
+    descs, keep = M.pdb_descs([amp])
+    _lib.check(L.dpx_hybrid_child_pdb(h, 0, descs))
+    rots = np.array([[0.0, 0.0, 0.0, 1.0], [0.3, -0.4, 1.1, 1.0], [1.2, 0.2, -0.7, 1.0]], dtype=np.float32)
+    _lib.check(L.dpx_hybrid_add_rotations(h, 0, 3, _lib.fptr(rots)))
+    trans = [np.array([[0, 0, 0, 0], [2.5, 0, 0, 0]], dtype=np.float32),
+             np.array([[0, 1.5, 0.5, 0], [-1, -1, 2, 0]], dtype=np.float32),
+             np.array([[0.5, 0.5, -2, 0], [3, 0, 1, 0]], dtype=np.float32)]
+    for r, t in enumerate(trans):
+        _lib.check(L.dpx_hybrid_add_translations(h, 0, r, 2, _lib.fptr(t)))
+    seed, iters, eps = 77, 40_000, 2e-3
+    out = np.zeros(len(Q))
+    _lib.check(L.dpx_hybrid_compute_intensity(h, _lib.DPX_OA_MC, _lib.dptr(out), eps, iters, seed, None))
+    _lib.check(L.dpx_hybrid_destroy(h))
+    crot = np.repeat(rots[:, :3].astype(np.float64), 2, axis=0)
+    ctr = np.concatenate([t[:, :3] for t in trans]).astype(np.float64)
+    data, co = oracle_grid(amp, gs, qmax)
+    kp = []
+    leaf = O.make_leaf(data, co, copy_rot=crot, copy_tr=ctr, keep=kp)
+    dirs = O.mc_directions(seed, iters)
+    ref = O.integrate_layers_gpu_rule(gs, qmax, [leaf], Q.astype(np.float64), dirs, 0, iters, eps, 4096)
+    assert rel(out, ref) <= tol
+    del keep
+
+
+def test_grid_amplitude_with_tabulated_form_factors(ctx):
+    """dpx_pdb_jacobian_grid_amplitude_aff takes the form factors as the
+    reference's atomicFFCalculator::GetQMajorAFFMatrix tabulates them ([U][nq],
+    q fastest, dummy-atom solvent folded in): the FP64 grid equals the
+    coefficient entry's within the table's float rounding."""
+    amp = globule(250, 1.1, seed=62, extra=SOLVENT)
+    gs, qmax = 20, 5.0
+    L = dpx.lib()
+    P = L.dpx_grid_cells(gs)
+    step = qmax / (gs // 2)
+    nq = gs // 2 + 4
+    s = O.Struct.from_pdb(amp)
+    aff = O.aff_table(s, nq, 0.0, step, O.FP64)  # [nq, U]
+    tab = np.ascontiguousarray(aff.T.astype(np.float32))  # [U][nq]
+    a = amp.atoms_float4()
+    out = np.zeros(2 * P)
+    _lib.check(L.dpx_pdb_jacobian_grid_amplitude_aff(P, 3, 6, step, _lib.dptr(out), _lib.fptr(a), len(a),
+                                                     len(amp.unique), _lib.iptr(amp.atoms_per_ion), _lib.fptr(tab),
+                                                     nq, amp.flags, amp.solventED, None, None, 0, 0.0, None, None, 0,
+                                                     0.0, amp.scale, M.FP64, None))
+    assert rel_to_max(out, O.grid_fill(s, gs, qmax, O.FP64)) <= 2e-7
+    assert L.dpx_pdb_jacobian_grid_amplitude_aff(P, 3, 6, step, _lib.dptr(out), _lib.fptr(a), len(a),
+                                                 len(amp.unique), _lib.iptr(amp.atoms_per_ion), _lib.fptr(tab),
+                                                 nq - 1, amp.flags, amp.solventED, None, None, 0, 0.0, None, None, 0,
+                                                 0.0, amp.scale, M.FP64, None) == -1
