@@ -202,6 +202,8 @@ def run_dpx(args):
     sfu_c = C.c_double()
     _lib.check(L.dpx_measure_sfu_peak(ctx.handle, C.byref(sfu_c)))
     sfu_measured = sfu_c.value
+    pipes = np.zeros(3)  # FP32 FMA scalar, FP32 FMA f32x2, TF32 mma.sync: flops/s on this GPU
+    _lib.check(L.dpx_measure_pipe_peaks(ctx.handle, _lib.dptr(pipes)))
     tune = None
     if args.autotune:  # sweep every fill shape on this workload's leaf, keep the fastest
         best, table = M.autotune_fill(ctx, [amp], QMAX, GRID_SIZE, repeats=1)
@@ -349,16 +351,25 @@ def run_dpx(args):
             mom_ms, syn_ms, harm_ms, n_pts, kk = (float(v) for v in st5)
             # moments: per point and (l, m) six weights times a complex basis value = 24 flops
             flops = n_pts * kk * 24.0
-            fp32_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+            fp32_peak = float(max(pipes[0], pipes[1])) / 1e12
+            # executed on the tensor path: per 32 points, order l and quartet of 4 m,
+            # 8 m16n8k8 MMAs (hi and remainder of both operands) = 128 flops per point-(l, m)
+            mma_flops = n_pts * kk * 128.0
             roofline = {"bound": "fp32", "kernel": "hm_moments", "method": "harmonic",
                         "achieved": flops / (mom_ms / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                         "frac": flops / (mom_ms / 1e3) / 1e12 / fp32_peak,
                         "traffic": MOMENTS_BYTES_PER_POINT * n_pts,
-                        "peak_kind": "nominal FP32 (152 SMs x 128 lanes x 2 flops x max SM clock): "
-                                     "no measured FP32 peak is on file",
+                        "peak_kind": "measured on this GPU (dpx_measure_pipe_peaks: independent FP32 FMA chains, "
+                                     "the faster of scalar and packed f32x2)",
+                        "pipes_measured_tflops": {"fp32_fma": pipes[0] / 1e12, "fp32_fma_f32x2": pipes[1] / 1e12,
+                                                  "tf32_mma_sync": pipes[2] / 1e12},
+                        "tensor_path": {"executed_tflops": mma_flops / (mom_ms / 1e3) / 1e12,
+                                        "peak": pipes[2] / 1e12,
+                                        "frac": mma_flops / (mom_ms / 1e3) / pipes[2]},
                         "note": "flops = points (atoms + solvent voxels) x K x 6 moments x 4 (complex "
                                 "multiply-add), K the mean over the points of the (l, m) their radial bins "
-                                "carry; the fill also holds the synthesis and the radial tables",
+                                "carry; time = the hm_moments launches alone (stage events around them); the "
+                                "fill also holds the synthesis and the radial tables",
                         "points": n_pts, "K": kk,
                         "stage_ms": {"moments": mom_ms, "synthesis": syn_ms, "harmonic_fill": harm_ms},
                         "equivalent_direct_pairs_per_s": float(N_ATOMS + n_boxes) * P / (fill_ms / 1e3)}

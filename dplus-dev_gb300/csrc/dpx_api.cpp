@@ -1312,6 +1312,47 @@ int dpx_measure_sfu_peak(dpx_ctx ctx, double* ops_per_s) {
     return DPX_OK;
 }
 
+int dpx_measure_pipe_peaks(dpx_ctx ctx, double* flops_per_s) {
+    if (!ctx || !flops_per_s) return fail(DPX_ERR_ARG, "NULL argument");
+    if (int rc = set_device(ctx)) return rc;
+    int dev = 0, sms = 0;
+    DPX_CUDA(cudaGetDevice(&dev));
+    DPX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaStream_t s = ctx->stream;
+    DPX_CUDA(ctx->result.reserve(64));
+    cudaEvent_t e0, e1;
+    DPX_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(DPX_ERR_CUDA, "cudaEventCreate");
+    }
+    cudaError_t e = cudaSuccess;
+    const int blocks = sms * 8;
+    for (int kind = 0; kind < 3 && e == cudaSuccess; ++kind) {
+        const int iters = kind == 2 ? 2048 : 8192;
+        e = dpx::launch_pipe_probe(s, kind, blocks, 64, (float*)ctx->result.p);  // warm-up
+        float best = 0.f;
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
+            cudaEventRecord(e0, s);
+            e = dpx::launch_pipe_probe(s, kind, blocks, iters, (float*)ctx->result.p);
+            cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && (best == 0.f || ms < best)) best = ms;
+        }
+        const double threads = double(blocks) * 256.0;
+        const double flops = kind == 0 ? threads * iters * 8 * 2
+                             : kind == 1 ? threads * iters * 8 * 4
+                                         : threads / 32.0 * iters * 4 * 2048.0;
+        if (e == cudaSuccess) flops_per_s[kind] = flops / (best * 1e-3);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(e, "pipe probe");
+    return DPX_OK;
+}
+
 int dpx_mc_directions(uint32_t seed, int64_t D, double* theta_phi) {
     if (D < 0 || (D > 0 && !theta_phi)) return fail(DPX_ERR_ARG, "bad direction buffer");
     std::mt19937 rng;

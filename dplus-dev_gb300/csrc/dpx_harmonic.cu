@@ -403,6 +403,57 @@ __global__ void __launch_bounds__(32) hm_moments(const float4* __restrict__ pts,
 }
 
 // ---------------------------------------------------------------------------
+// Pipe calibration (the denominators of the moments' roofline): independent
+// chains per thread, long enough that launch costs vanish.
+//   kind 0: scalar FP32 FMA, 8 chains        (2 flops per FMA)
+//   kind 1: packed fma.rn.f32x2, 8 chains    (4 flops per instruction)
+//   kind 2: mma.sync m16n8k8 TF32, 4 independent accumulators per warp
+//           (2 x 16 x 8 x 8 = 2,048 flops per MMA)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) pipe_probe_kernel(int kind, int iters, float* out) {
+    float acc = 0.f;
+    if (kind == 0) {
+        float x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = 1e-3f * (threadIdx.x + 1) + 0.1f * c;
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) x[c] = fmaf(x[c], 0.999f, 1e-4f);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc += x[c];
+    } else if (kind == 1) {
+        f2x x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = pk2(1e-3f * (threadIdx.x + 1) + 0.1f * c, 0.2f * c);
+        const f2x m = pk2(0.999f, 0.998f), a = pk2(1e-4f, 2e-4f);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) x[c] = fma2(x[c], m, a);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            float u, v;
+            upk2(x[c], u, v);
+            acc += u + v;
+        }
+    } else {
+        float d[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
+        const uint32_t a[4] = {tf32_rna(1e-3f * threadIdx.x), tf32_rna(0.5f), tf32_rna(0.25f), tf32_rna(0.125f)};
+        const uint32_t b0 = tf32_rna(1e-3f), b1 = tf32_rna(2e-3f);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) mma_tf32(d[j], a, b0, b1);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc += d[j][0] + d[j][1] + d[j][2] + d[j][3];
+    }
+    if (acc == 12345.678f) out[0] = acc;  // keeps the chains live; never true for these inputs
+}
+
+// ---------------------------------------------------------------------------
 // Solvent boxes to voxels, binned by radius with a stable counting sort:
 // vx_expand (voxel v of box b: centre, weight; its bin; per-block histograms),
 // vx_bins (per bin: the total and its blocks' offsets), vx_scatter (the rank of
@@ -1009,6 +1060,11 @@ size_t synth_smem(int Lp, int li) {
 std::mutex g_smem_mu;
 size_t g_smem_set[2][64] = {};  // per device: the limits set for hm_moments, hm_synth
 }  // namespace
+
+cudaError_t launch_pipe_probe(cudaStream_t s, int kind, int blocks, int iters, float* out) {
+    pipe_probe_kernel<<<blocks, 256, 0, s>>>(kind, iters, out);
+    return cudaGetLastError();
+}
 
 cudaError_t harmonic_reserve_smem(int Lp, int LM) {
     int dev = 0;

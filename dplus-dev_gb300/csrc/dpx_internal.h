@@ -239,6 +239,10 @@ cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a);
 // lowers them).  Called when a fill is planned, outside any stream capture;
 // the launches below do not touch the limits.
 cudaError_t harmonic_reserve_smem(int Lp, int LM);
+// Pipe calibration kernels: kind 0 scalar FP32 FMA, 1 packed f32x2 FMA, 2
+// mma.sync m16n8k8 TF32 (256 threads a block, iters steps of 8 / 8 / 4
+// independent operations per thread or warp).
+cudaError_t launch_pipe_probe(cudaStream_t s, int kind, int blocks, int iters, float* out);
 cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a);
 // C [Lp+1][K] (FP64) = the expansion coefficients of one point set.
 cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C);

@@ -156,6 +156,7 @@ _SIGS = {
     "dpx_hybrid_compute_intensity": (C.c_int, [_P, C.c_int, _D, C.c_double, C.c_int64, C.c_uint64, _I]),
     "dpx_hybrid_destroy": (C.c_int, [_P]),
     "dpx_measure_sfu_peak": (C.c_int, [_P, _D]),
+    "dpx_measure_pipe_peaks": (C.c_int, [_P, _D]),
     "dpx_debye_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), _F, _F, C.c_int, _D, C.c_int, _D]),
     "dpx_direct_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), C.c_int, _D, _D, C.c_int, _D, C.c_int64, _D, _D]),
     "dpx_calc_debye_v2": (C.c_int, [C.c_int, C.c_float, C.c_float, _D, C.c_int, _I, _F, C.POINTER(C.c_uint8), _F,

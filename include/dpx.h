@@ -450,6 +450,11 @@ int dpx_hybrid_destroy(dpx_hybrid h);
  * GPU sustains (sin and cos count one each) — the denominator of the amplitude
  * fill's roofline. */
 int dpx_measure_sfu_peak(dpx_ctx ctx, double* ops_per_s);
+/* Pipe calibration (no counterpart in the reference): flops_per_s[3] = the
+ * FP32 FMA pipe with scalar FMAs, with packed f32x2 FMAs, and the TF32
+ * mma.sync (m16n8k8) tensor path this GPU sustains, each from a kernel of
+ * independent chains — the denominators of the harmonic moments' roofline. */
+int dpx_measure_pipe_peaks(dpx_ctx ctx, double* flops_per_s);
 
 /* ---- amplitude-grid files (D+'s binary .amp, version 13: JacobianSphereGrid::
  * ExportBinaryData / ImportBinaryData, Backend/Backend/Grid.cpp:847-963) ----
