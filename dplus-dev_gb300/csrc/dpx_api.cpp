@@ -220,6 +220,8 @@ void ctx_release(dpx_ctx ctx) {
         b->release();
     for (cudaEvent_t e : ctx->tev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->aev)
+        if (e) cudaEventDestroy(e);
     if (ctx->aux) {
         cudaStreamSynchronize(ctx->aux);
         cudaStreamDestroy(ctx->aux);
@@ -293,6 +295,19 @@ int dpx_ctx_set_timing(dpx_ctx ctx, int on) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
     ctx->timing = on != 0;
     ctx->tev_used = 0;
+    ctx->aev_used = false;
+    return DPX_OK;
+}
+
+int dpx_ctx_average_kernel_ms(dpx_ctx ctx, double* ms) {
+    if (!ctx || !ms) return fail(DPX_ERR_ARG, "NULL argument");
+    *ms = 0.0;
+    if (!ctx->aev_used) return DPX_OK;
+    if (int rc = set_device(ctx)) return rc;
+    DPX_CUDA(cudaEventSynchronize(ctx->aev[1]));
+    float f = 0.f;
+    DPX_CUDA(cudaEventElapsedTime(&f, ctx->aev[0], ctx->aev[1]));
+    *ms = f;
     return DPX_OK;
 }
 
@@ -326,6 +341,12 @@ int dpx_ctx_set_fill_method(dpx_ctx ctx, int method) {
 }
 
 int dpx_ctx_get_fill_method(dpx_ctx ctx) { return ctx ? ctx->fill_method : DPX_ERR_ARG; }
+
+int dpx_set_average_shape(int directions_per_thread) {
+    if (dpx::set_average_dpt(directions_per_thread) != 0)
+        return fail(DPX_ERR_ARG, "directions per thread must be 1 or 2, got %d", directions_per_thread);
+    return DPX_OK;
+}
 
 int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
@@ -977,8 +998,13 @@ int dpx_orientation_average(dpx_ctx ctx, int n_models, const dpx_grid* grids, co
     DPX_CUDA(cudaMemcpyAsync(ctx->groups.p, gstage.data(), gstage.size(), cudaMemcpyHostToDevice, s));
     DPX_CUDA(cudaMemsetAsync(ctx->result.p, 0, (size_t)nq * sizeof(double), s));
 
-    cudaError_t e = dpx::launch_average(s, prec == DPX_FP64, G, n_models, d_models, plan);
+    if (ctx->timing)
+        for (cudaEvent_t& ev : ctx->aev)
+            if (!ev) DPX_CUDA(cudaEventCreate(&ev));
+    cudaError_t e = dpx::launch_average(s, prec == DPX_FP64, G, n_models, d_models, plan,
+                                        ctx->timing ? ctx->aev : nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "average launch");
+    ctx->aev_used = ctx->timing;
     e = dpx::launch_finalize(s, plan, eps, (double*)ctx->result.p);
     if (e != cudaSuccess) return cuda_fail(e, "finalize launch");
     DPX_CUDA(cudaMemcpyAsync(res, ctx->result.p, (size_t)nq * sizeof(double), cudaMemcpyDeviceToHost, s));

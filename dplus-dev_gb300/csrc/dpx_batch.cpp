@@ -12,11 +12,13 @@
 //   phi-spline derivatives), one scratch shared by the fills in order;
 //   FP32 leaves the harmonic method declines: one direct-sum launch over all of
 //   them, then their splines; FP64: the direct sum per structure and splines;
-//   per structure: MC average, finalize, the q = 0 term;
+//   the MC averages of all the wave's structures in three launches (bracket
+//   tables, average, finalize with the q = 0 terms: launch_average_batch),
+//   each structure with its own partial sums;
 //   one device-to-host copy of the wave's I(q) into pinned memory.
 // All inputs (atoms, form-factor tables, item prefixes, bracket tables and the
-// shared direction set) are uploaded once at creation; the grids of a wave
-// live in one pool reused by every wave.
+// shared direction set, sorted once into its angular order) are uploaded once
+// at creation; the grids of a wave live in one pool reused by every wave.
 #include "dpx_host.h"
 
 #include <algorithm>
@@ -47,6 +49,8 @@ struct dpx_batch_s {
     std::vector<cudaGraphExec_t> execs;
     std::vector<dpxh::HarmPlan> plans;  // FP32 solves the harmonic method fills (arena != nullptr)
     void* hscratch = nullptr;           // their launch scratch, shared (the fills run in order)
+    dpx::AvgJob* jobs = nullptr;        // [n] the batched averages' solves (device)
+    int* dsort = nullptr;               // the shared directions' angular order (eps = 0), sorted once
 };
 
 namespace {
@@ -64,6 +68,8 @@ void batch_free(dpx_batch b) {
     if (b->h_res) cudaFreeHost(b->h_res);
     for (dpxh::HarmPlan& p : b->plans) dpxh::harmonic_plan_release(p);
     if (b->hscratch) cudaFree(b->hscratch);
+    if (b->jobs) cudaFree(b->jobs);
+    if (b->dsort) cudaFree(b->dsort);
     cudaStreamSynchronize(b->ctx->stream);
     ctx_release(b->ctx);
     delete b;
@@ -89,6 +95,7 @@ struct SolvePlan {
     size_t o_model, o_bq, o_bl, o_bo, o_bi;
     bool origin;  // Q[0] == 0
     dpx::AvgPlan plan;  // pointers filled once the arena exists
+    size_t part_off;    // its partial sums and bracket tables in the wave's region
 };
 
 }  // namespace
@@ -170,7 +177,8 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
 
     // staging of every input table
     Stage st;
-    size_t partial_max = 0;
+    size_t partial_max = 0, wave_part = 0;
+    int wave = 0;
     for (int j = 0; j < n; ++j) {
         const dpx_solve_desc& d = solves[j];
         const dpx_pdb_desc& pd = d.pdb;
@@ -200,8 +208,15 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         P.dir_stride = 0;
         P.need_dir = 0;
         P.one_leaf = 1;
-        partial_max = std::max(partial_max, ((size_t)P.n_brackets * P.n_chunks + (size_t)P.n_brackets * 5) *
-                                                P.max_q * sizeof(double) + 64);
+        // the solves of a wave average in one launch: each its own partial sums
+        if (j == b->wave_first[wave + 1]) {
+            ++wave;
+            wave_part = 0;
+        }
+        p.part_off = wave_part;
+        wave_part += (((size_t)P.n_brackets * P.n_chunks + (size_t)P.n_brackets * 5) * P.max_q * sizeof(double) +
+                      64 + 255) & ~size_t(255);
+        partial_max = std::max(partial_max, wave_part);
         p.origin = d.Q[0] == 0.0;
         b->nq.push_back(d.nq);
         b->res_off.push_back(b->res_total);
@@ -227,11 +242,12 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     int rc = DPX_OK;
     cudaError_t e = cudaMalloc(&b->arena, st.h.size());
     if (e == cudaSuccess) e = cudaMalloc(&b->pool, b->pool_bytes);
-    // with eps = 0 the averages take the shared directions in angular order (one
-    // sort scratch behind the partial sums, used by one average at a time)
-    const size_t sort_off = al16(partial_max);
+    // with eps = 0 the averages take the shared directions in angular order,
+    // sorted once here
     const size_t sort_bytes = eps == 0.0 ? dpx::dir_sort_bytes(n_samples) : 0;
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->partial, sort_off + sort_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->partial, partial_max);
+    if (e == cudaSuccess && sort_bytes) e = cudaMalloc((void**)&b->dsort, sort_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->jobs, (size_t)n * sizeof(dpx::AvgJob));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_res, b->res_total * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_res, b->res_total * sizeof(double));
     if (e == cudaSuccess && hscratch) e = cudaMalloc(&b->hscratch, hscratch);
@@ -261,15 +277,40 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
             P.br_q_off = reinterpret_cast<const int*>(A + p.o_bo);
             P.br_qidx = reinterpret_cast<const int*>(A + p.o_bi);
             P.dirs = reinterpret_cast<const double*>(A + o_dirs);
-            P.partial = b->partial;
-            P.sort_scratch = sort_bytes ? reinterpret_cast<int*>(reinterpret_cast<char*>(b->partial) + sort_off)
-                                        : nullptr;
+            P.partial = reinterpret_cast<double*>(reinterpret_cast<char*>(b->partial) + p.part_off);
         }
         if (!jobs.empty()) std::memcpy(st.h.data() + o_jobs[w], jobs.data(), jobs.size() * sizeof(dpx::FillJob));
         wave_tiles[w] = tiles;
     }
     cudaStream_t s = ctx->stream;
     e = cudaMemcpyAsync(b->arena, st.h.data(), st.h.size(), cudaMemcpyHostToDevice, s);
+    const int* order = nullptr;
+    if (e == cudaSuccess && b->dsort) {
+        order = dpx::launch_dir_order(s, reinterpret_cast<const double*>(A + o_dirs), n_samples, b->dsort);
+        e = cudaGetLastError();
+    }
+    // the batched averages' solves
+    std::vector<dpx::AvgJob> jobs(n);
+    std::vector<int> wave_nbr(n_waves, 0);
+    std::vector<int64_t> wave_blocks(n_waves, 0);
+    for (int w = 0; w < n_waves; ++w) {
+        for (int j = b->wave_first[w]; j < b->wave_first[w + 1]; ++j) {
+            dpx::AvgJob& J = jobs[j];
+            J = dpx::AvgJob{};
+            J.plan = sp[j].plan;
+            J.plan.dir_order = order;
+            J.model = reinterpret_cast<const dpx::ModelDev*>(A + sp[j].o_model);
+            J.res = b->d_res + b->res_off[j];
+            J.step = sp[j].G.step;
+            J.Lp = sp[j].G.Lp;
+            J.origin = sp[j].origin ? 1 : 0;
+            wave_nbr[w] = std::max(wave_nbr[w], J.plan.n_brackets);
+        }
+        wave_blocks[w] = dpx::plan_average_batch(jobs.data() + b->wave_first[w],
+                                                 b->wave_first[w + 1] - b->wave_first[w], !fp32);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->jobs, jobs.data(), jobs.size() * sizeof(dpx::AvgJob),
+                                              cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "batch upload");
@@ -324,21 +365,14 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
                          : dpx::launch_splines_f64(s, p.G, reinterpret_cast<double4_32a*>(grid));
                 launches++;
             }
-            double* r = b->d_res + b->res_off[j];
-            if (e == cudaSuccess) e = cudaMemsetAsync(r, 0, (size_t)b->nq[j] * sizeof(double), s);
-            if (e == cudaSuccess)
-                e = dpx::launch_average(s, !fp32, p.G, 1, reinterpret_cast<const dpx::ModelDev*>(A + p.o_model),
-                                        p.plan);
-            if (e == cudaSuccess) e = dpx::launch_finalize(s, p.plan, eps, r);
-            if (e == cudaSuccess && p.origin) {
-                e = dpx::launch_origin_intensity(s, !fp32, grid, r);
-                launches++;
-            }
-            // bracket tables, average, finalize; the angular order of the
-            // directions (keys, totals, offsets, scatter) when it applies
-            launches += 3 + (p.plan.sort_scratch && n_samples >= 512 ? 4 : 0);
         }
+        // the wave's averages: bracket tables, average and finalize (with the
+        // q = 0 terms), each one launch over all its solves
         const size_t r0 = b->res_off[j0], r1 = (j1 < n) ? b->res_off[j1] : b->res_total;
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->d_res + r0, 0, (r1 - r0) * sizeof(double), s);
+        if (e == cudaSuccess)
+            e = dpx::launch_average_batch(s, !fp32, b->jobs + j0, j1 - j0, wave_nbr[w], wave_blocks[w], eps);
+        launches += 3;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(b->h_res + r0, b->d_res + r0, (r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost, s);
         const cudaError_t ec = cudaStreamEndCapture(s, &g);

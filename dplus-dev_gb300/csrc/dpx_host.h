@@ -115,6 +115,9 @@ struct dpx_ctx_s {
     cudaEvent_t tev[8] = {};
     int tev_used = 0;
     double stage_points = 0, stage_k = 0;
+    // with timing on, events around the last orientation average's main kernel
+    cudaEvent_t aev[2] = {};
+    bool aev_used = false;
     dpxh::DevBuf atoms, table, ions, models, groups, plan, partial, result, dirs, debye;
     dpxh::DevBuf harmonic; // the harmonic fill's launch scratch
     dpxh::DevBuf dirsort;  // the average's angular-order scratch

@@ -145,8 +145,34 @@ cudaError_t launch_assemble(cudaStream_t s, bool fp64, const Geom& g, int n_mode
 // other kernels (dpx_kernels.cu)
 cudaError_t launch_splines_f32(cudaStream_t s, const Geom& g, float4* grid);
 cudaError_t launch_splines_f64(cudaStream_t s, const Geom& g, double4_32a* grid);
+// Directions per thread of the FP32 slide average (1 or 2; -1: other values).
+int set_average_dpt(int dpt);
+// One solve of a batched average (launch_average_batch): a plain leaf on its
+// grid with its own brackets and partial-sum region, every solve on the same
+// shared direction set (plan.dir_order: its angular order, or nullptr).
+struct AvgJob {
+    AvgPlan plan;
+    const ModelDev* model;  // the plain leaf (identity placement) on its grid
+    double* res;            // [nq] I(q)
+    double step;            // the grid's radial step
+    int Lp;
+    int origin;             // the first q is 0: res[0] = |F(0)|^2 from the origin cell
+    int seg_len, n_seg;     // set by plan_average_batch
+    int64_t bx;             // blocks along the chunks (plan_average_batch)
+    int64_t block0;         // the solve's first block in the batched average (plan_average_batch)
+};
+// Host: the launch shape of every job; returns the total blocks of the average.
+int64_t plan_average_batch(AvgJob* jobs, int n, bool fp64);
+// Bracket tables, average and finalize (with the q = 0 terms) of n_jobs solves
+// in three launches; max_brackets = the largest n_brackets.
+cudaError_t launch_average_batch(cudaStream_t s, bool fp64, const AvgJob* d_jobs, int n_jobs, int max_brackets,
+                                 int64_t total_blocks, double eps);
+// The angular order of a shared direction set (dir_sort_bytes(n) of scratch),
+// or nullptr when the set is too small to sort.
+const int* launch_dir_order(cudaStream_t s, const double* dirs, int64_t n, int* scratch);
+// kev (optional): two events recorded just before and after the main average kernel
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
-                           const AvgPlan& plan);
+                           const AvgPlan& plan, cudaEvent_t* kev = nullptr);
 cudaError_t launch_finalize(cudaStream_t s, const AvgPlan& plan, double eps, double* d_res);
 // SFU calibration: blocks x 256 threads x iters x 8 __sincosf (2 MUFU ops each)
 cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);

@@ -354,14 +354,48 @@ __device__ void sample_amps(const ModelDev* __restrict__ models, int n_models, i
 constexpr float kPiF = 3.14159265358979f;
 constexpr float k2PiF = 6.28318530717959f;
 
-__device__ Cx<float> interp_plane_f(const float4* __restrict__ g, int ri, float theta, float phi) {
-    const int64_t base = shell_base(ri);
-    const int phiPoints = 6 * ri, thePoints = 3 * ri;
-    // clamped as in interp_plane: every node index stays inside shell ri
+// Cubic Hermite on [0, 1] as weights of its four inputs: p(t) = h00 p1 + h10 d1
+// + h01 p2 + h11 d2 (the same polynomial as hermite(), evaluated as one dot
+// product per component).
+struct HermiteW {
+    float h00, h10, h01, h11;
+};
+__device__ __forceinline__ HermiteW hermite_w(float t) {
+    const float t2 = t * t;
+    const float h01 = t2 * (3.f - 2.f * t);
+    const float h11 = t2 * (t - 1.f);
+    return {1.f - h01, h11 + t * (1.f - t), h01, h11};
+}
+// Hermite through y2, y3 with the four-point slopes of four_point() (Ginsburg
+// et al. 2019, eqs 35-36) folded in: y(t) = sum_k w_k y_k.  With d2 = (-7 y1 -
+// 3 y2 + 12 y3 - 2 y4) / 15 and d3 = (2 y1 - 12 y2 + 3 y3 + 7 y4) / 15.
+__device__ __forceinline__ float4 four_point_w(float t) {
+    const HermiteW h = hermite_w(t);
+    constexpr float r = 1.f / 15.f;
+    return make_float4(r * (-7.f * h.h10 + 2.f * h.h11), h.h00 + r * (-3.f * h.h10 - 12.f * h.h11),
+                       h.h01 + r * (12.f * h.h10 + 3.f * h.h11), r * (-2.f * h.h10 + 7.f * h.h11));
+}
+__device__ __forceinline__ Cx<float> dot4(float4 w, Cx<float> a, Cx<float> b, Cx<float> c, Cx<float> d) {
+    return {fmaf(w.w, d.r, fmaf(w.z, c.r, fmaf(w.y, b.r, w.x * a.r))),
+            fmaf(w.w, d.i, fmaf(w.z, c.i, fmaf(w.y, b.i, w.x * a.i)))};
+}
+
+// Angles clamped as interp_plane clamps them: every node index of a plane
+// interpolation stays inside its shell.
+__device__ __forceinline__ void clamp_angles_f(float& theta, float& phi) {
     if (!(theta >= 0.f)) theta = 0.f;
     if (theta > kPiF) theta = kPiF;
     if (!(phi >= 0.f)) phi = 0.f;
     if (phi > k2PiF) phi = k2PiF;
+}
+
+// One theta-phi plane at shell ri >= 1 for clamped angles: the 4 rows x 2 phi
+// nodes of interp_plane (Grid.cpp:61-134, IndicesFromRadians :1220-1256) as
+// 32-bit offsets into the shell, the phi Hermite and the theta four-point
+// Hermite as weights.  Rows away from the poles take no wrap logic.
+__device__ __forceinline__ Cx<float> plane_clamped_f(const float4* __restrict__ g, int ri, float theta, float phi) {
+    const float4* __restrict__ sh = g + shell_base(ri);
+    const int phiPoints = 6 * ri, thePoints = 3 * ri;
     const float cells_per_rad = (float)thePoints * (1.f / kPiF);
     const float xt = theta * cells_per_rad, xp = phi * cells_per_rad;
     int tI = (int)xt;
@@ -374,30 +408,45 @@ __device__ Cx<float> interp_plane_f(const float4* __restrict__ g, int ri, float 
         tPh = 0.f;
     }
     const int pI1 = (pI + 1 == phiPoints) ? 0 : pI + 1;
+    int o1[4], o2[4];
+    if (tI >= 1 && tI + 2 <= thePoints) {
+        const int r0 = (tI - 1) * phiPoints;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            o1[i] = r0 + i * phiPoints + pI;
+            o2[i] = r0 + i * phiPoints + pI1;
+        }
+    } else {
+        // a row past a pole is the row mirrored through it, half a turn round
+        const int h1 = ((2 * pI >= phiPoints) ? -phiPoints : phiPoints) / 2;
+        const int h2 = ((2 * pI1 >= phiPoints) ? -phiPoints : phiPoints) / 2;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int v = tI + i - 1;
+            const bool wrap = v < 0 || v > thePoints;
+            const int row = v < 0 ? v + thePoints + 1 : (v > thePoints ? v - (thePoints + 1) : v);
+            o1[i] = row * phiPoints + pI + (wrap ? h1 : 0);
+            o2[i] = row * phiPoints + pI1 + (wrap ? h2 : 0);
+        }
+    }
+    float4 c1[4], c2[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        c1[i] = __ldg(sh + o1[i]);
+        c2[i] = __ldg(sh + o2[i]);
+    }
+    const HermiteW h = hermite_w(tPh);
     Cx<float> nodes[4];
 #pragma unroll
-    for (int i = -1; i < 3; ++i) {
-        const int v = tI + i;
-        int theInd = v < 0 ? v + thePoints + 1 : (v > thePoints ? v - (thePoints + 1) : v);
-        int64_t c1, c2;
-        if (theInd == tI + i) {
-            c1 = base + phiPoints * theInd + pI;
-            c2 = base + phiPoints * theInd + pI1;
-        } else {
-            if (tI + i > thePoints) theInd = (tI + i) - (thePoints + 1);
-            c1 = base + phiPoints * theInd + pI;
-            c2 = base + phiPoints * theInd + pI1;
-            c1 += ((2 * pI >= phiPoints) ? -phiPoints : phiPoints) / 2;
-            c2 += ((2 * pI1 >= phiPoints) ? -phiPoints : phiPoints) / 2;
-        }
-        Cx<float> v1, d1, v2, d2;
-        load_cell<float>(g, c1, v1, d1);
-        load_cell<float>(g, c2, v2, d2);
-        nodes[i + 1] = hermite<float>(v1, v2, d1, d2, tPh);
-    }
-    Cx<float> ds1, ds2;
-    four_point<float>(nodes[0], nodes[1], nodes[2], nodes[3], ds1, ds2);
-    return hermite<float>(nodes[1], nodes[2], ds1, ds2, tTh);
+    for (int i = 0; i < 4; ++i)
+        nodes[i] = {fmaf(h.h11, c2[i].z, fmaf(h.h01, c2[i].x, fmaf(h.h10, c1[i].z, h.h00 * c1[i].x))),
+                    fmaf(h.h11, c2[i].w, fmaf(h.h01, c2[i].y, fmaf(h.h10, c1[i].w, h.h00 * c1[i].y)))};
+    return dot4(four_point_w(tTh), nodes[0], nodes[1], nodes[2], nodes[3]);
+}
+
+__device__ Cx<float> interp_plane_f(const float4* __restrict__ g, int ri, float theta, float phi) {
+    clamp_angles_f(theta, phi);
+    return plane_clamped_f(g, ri, theta, phi);
 }
 
 // window_plane in FP32 angles.
@@ -501,13 +550,17 @@ __device__ void sample_amps_f32(const ModelDev* __restrict__ models, int n_model
 // Grid.cpp:149-150), in the precision of the interpolation.
 // --------------------------------------------------------------------------
 template <typename T>
-__global__ void bracket_tables_kernel(AvgPlan plan, double step, int* __restrict__ find, T* __restrict__ frac) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= plan.n_brackets) return;
+__device__ __forceinline__ void bracket_tables_at(const AvgPlan& plan, double step, int b, int* __restrict__ find,
+                                                  T* __restrict__ frac) {
     const int q0 = plan.br_q_off[b], q1 = plan.br_q_off[b + 1];
     const int f = (q1 > q0) ? (int)bump8(plan.br_q[q0] / step) : 0;
     find[b] = f;
     for (int k = q0; k < q1; ++k) frac[k] = (T)(bump8(plan.br_q[k] / step) - (double)f);
+}
+template <typename T>
+__global__ void bracket_tables_kernel(AvgPlan plan, double step, int* __restrict__ find, T* __restrict__ frac) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < plan.n_brackets) bracket_tables_at<T>(plan, step, b, find, frac);
 }
 
 // The four radial planes of the bracket a thread is on.  Consecutive brackets
@@ -653,51 +706,36 @@ __global__ void __launch_bounds__(128) average_kernel(int Lp, const ModelDev* __
 // One undocked leaf with one direction set for all layers: a thread walks
 // the brackets of its direction in order and keeps the leaf's planes in a
 // sliding window, one plane interpolation per bracket.  The planes, the
-// radial Hermite and the leaf phase are those of sample_amps /
-// sample_amps_f32, so the amplitudes are the same.
+// radial Hermite and the leaf phase are those of sample_amps, so the
+// amplitudes are the same.  FP64 grids; FP32 grids take
+// average_slide_f32_kernel.
 template <typename T, int MQ>
-__global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelDev* __restrict__ models,
-                                                            AvgPlan plan, int seg_len, const int* __restrict__ find,
-                                                            const T* __restrict__ frac_tab) {
+__device__ __forceinline__ void slide_f64(const ModelDev& M, int Lp, const AvgPlan& plan, int seg_len,
+                                          const int* __restrict__ find, const T* __restrict__ frac_tab,
+                                          int64_t chunk, int by) {
     typedef typename Vec4<T>::type V4;
-    const int64_t chunk = blockIdx.x;
-    const int b0 = blockIdx.y * seg_len;
+    const int b0 = by * seg_len;
     const int b1 = min(plan.n_brackets, b0 + seg_len);
     const int64_t s = chunk * plan.chunk - plan.chunk_off + threadIdx.x;
     const bool valid = (threadIdx.x < plan.chunk) && s >= 0 && s < plan.n_samples;
     __shared__ AvgSums<MQ> S;
     int nslot = 0;
 
-    const ModelDev& M = models[0];
     const V4* g = reinterpret_cast<const V4*>(M.grid);
+    static_assert(sizeof(T) == 8, "FP64 grids only");
     // the leaf's direction (Amplitude.cpp:3553-3579)
     double th = 0, ph = 0, dotR = 0;
-    float thf = 0.f, phf = 0.f;
     if (valid) {
         double theta, phi, dir[3] = {0.0, 0.0, 1.0};
         sample_direction(plan, 0, s, theta, phi, dir);
         th = theta;
         ph = phi;
-        thf = (float)theta;
-        phf = (float)phi;
         if (!M.plain) {
-            if constexpr (sizeof(T) == 4) {
-                const float n0 = (float)dir[0], n1 = (float)dir[1], n2 = (float)dir[2];
-                const float* C = M.Rf;
-                const float t0 = n0 * C[0] + n1 * C[3] + n2 * C[6];
-                const float t1 = n0 * C[1] + n1 * C[4] + n2 * C[7];
-                const float t2 = n0 * C[2] + n1 * C[5] + n2 * C[8];
-                dotR = dir[0] * M.w[0] + dir[1] * M.w[1] + dir[2] * M.w[2];
-                thf = atan2f(sqrtf(t0 * t0 + t1 * t1), t2);
-                phf = atan2f(t1, t0);
-                if (phf < 0.f) phf += k2PiF;
-            } else {
-                const double t0 = dir[0] * M.R[0] + dir[1] * M.R[3] + dir[2] * M.R[6];
-                const double t1 = dir[0] * M.R[1] + dir[1] * M.R[4] + dir[2] * M.R[7];
-                const double t2 = dir[0] * M.R[2] + dir[1] * M.R[5] + dir[2] * M.R[8];
-                dotR = t0 * M.tr[0] + t1 * M.tr[1] + t2 * M.tr[2];
-                dir_angles(t0, t1, t2, th, ph);
-            }
+            const double t0 = dir[0] * M.R[0] + dir[1] * M.R[3] + dir[2] * M.R[6];
+            const double t1 = dir[0] * M.R[1] + dir[1] * M.R[4] + dir[2] * M.R[7];
+            const double t2 = dir[0] * M.R[2] + dir[1] * M.R[5] + dir[2] * M.R[8];
+            dotR = t0 * M.tr[0] + t1 * M.tr[1] + t2 * M.tr[2];
+            dir_angles(t0, t1, t2, th, ph);
         }
     }
     const bool phased = dotR != 0.0;  // a placed leaf: its phase per q
@@ -707,10 +745,7 @@ __global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelD
         const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
         Cx<T> pl1{}, pl2{}, d1{}, d2{};
         if (valid) {
-            if constexpr (sizeof(T) == 4)
-                window_to(win, find[b], Lp, [&](int j) { return window_plane_f(g, j, thf, phf); });
-            else
-                window_to(win, find[b], Lp, [&](int j) { return window_plane<T>(g, j, th, ph); });
+            window_to(win, find[b], Lp, [&](int j) { return window_plane<T>(g, j, th, ph); });
             four_point<T>(win.p[0], win.p[1], win.p[2], win.p[3], d1, d2);
             pl1 = win.p[1];
             pl2 = win.p[2];
@@ -731,6 +766,217 @@ __global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelD
         }
     }
     avg_flush<MQ>(S, nslot, plan, chunk);
+}
+
+template <typename T, int MQ>
+__global__ void __launch_bounds__(128) average_slide_kernel(int Lp, const ModelDev* __restrict__ models,
+                                                            AvgPlan plan, int seg_len, const int* __restrict__ find,
+                                                            const T* __restrict__ frac_tab) {
+    slide_f64<T, MQ>(models[0], Lp, plan, seg_len, find, frac_tab, blockIdx.x, blockIdx.y);
+}
+
+// --------------------------------------------------------------------------
+// FP32 slide average.  The same planes and radial Hermite as
+// average_slide_kernel<float>, reorganised for the issue rate:
+//   * the radial four-point Hermite of every q is a weight table (4 floats a
+//     q, bracket_weights_kernel), so a q costs one broadcast load and 8 FMAs;
+//   * no phase: one leaf without docked copies has |e^{i q n.t} A|^2 = |A|^2
+//     (Amplitude.cpp:3553-3579 multiplies by it; the intensity does not see it);
+//   * the warp sums of |A|^2 stay FP32 in shared memory until a flush, where
+//     the four warps are added in FP64 (one conversion per slot and q, not one
+//     per bracket and warp: FP64 runs at 1/64 of the FP32 rate on this part);
+//   * the per-q warp sums are one transpose-reduce (V values over 32 lanes in
+//     log2(V) + 5 - log2(V) shuffle rounds, 2 V - 1 shuffles instead of 5 V);
+//   * DPT directions per thread, from DPT consecutive chunks, for more
+//     independent gathers in flight.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void bracket_weights_at(const AvgPlan& plan, double step, int b, int* __restrict__ find,
+                                                   float4* __restrict__ wq) {
+    const int q0 = plan.br_q_off[b], q1 = plan.br_q_off[b + 1];
+    const int f = (q1 > q0) ? (int)bump8(plan.br_q[q0] / step) : 0;
+    find[b] = f;
+    for (int k = q0; k < q1; ++k) wq[k] = four_point_w((float)(bump8(plan.br_q[k] / step) - (double)f));
+}
+__global__ void bracket_weights_kernel(AvgPlan plan, double step, int* __restrict__ find, float4* __restrict__ wq) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < plan.n_brackets) bracket_weights_at(plan, step, b, find, wq);
+}
+
+// Sums over the warp of each of V values (V a power of two <= 32): lane l
+// returns the sum of value l / (32 / V).
+template <int V>
+__device__ __forceinline__ float warp_sums(float (&v)[V], int lane) {
+#pragma unroll
+    for (int n = V, o = 16; n > 1; n >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < n / 2; ++k) {
+            const float keep = up ? v[k + n / 2] : v[k];
+            const float send = up ? v[k] : v[k + n / 2];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    float s = v[0];
+#pragma unroll
+    for (int o = 16 / V; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
+template <int V>
+struct SlideSums {
+    float red[kAvgSlots][4][V];
+    int b[kAvgSlots], q[kAvgSlots], m[kAvgSlots];
+};
+
+// Stores the block's filled slots: value v of a slot is q (v mod 4) of chunk
+// chunk0 + v / 4.  Called block-uniformly.
+template <int V>
+__device__ __forceinline__ void slide_flush(SlideSums<V>& S, int& nslot, const AvgPlan& plan, int64_t chunk0) {
+    if (nslot == 0) return;
+    __syncthreads();
+    for (int t = threadIdx.x; t < nslot * V; t += blockDim.x) {
+        const int sl = t / V, v = t - sl * V;
+        const int k = v & 3;
+        const int64_t chunk = chunk0 + (v >> 2);
+        if (k < S.m[sl] && chunk < plan.n_chunks) {
+            const double x = (((double)S.red[sl][0][v] + (double)S.red[sl][1][v]) + (double)S.red[sl][2][v]) +
+                             (double)S.red[sl][3][v];
+            plan.partial[((int64_t)S.b[sl] * plan.n_chunks + chunk) * plan.max_q + S.q[sl] + k] = x;
+        }
+    }
+    __syncthreads();
+    nslot = 0;
+}
+
+// The window's plane j: the mirrored first shell at j = -1 (Grid.cpp:513-537),
+// the origin cell at j = 0, else shell j (angles clamped by the caller).
+struct SlideDir {
+    float th, ph;    // clamped
+    float thm, phm;  // the mirrored first shell's, clamped
+};
+__device__ __forceinline__ Cx<float> slide_plane(const float4* __restrict__ g, int j, const SlideDir& a) {
+    if (j == -1) return plane_clamped_f(g, 1, a.thm, a.phm);
+    if (j == 0) {
+        const float4 o = __ldg(g);
+        return {o.x, o.y};
+    }
+    return plane_clamped_f(g, j, a.th, a.ph);
+}
+
+// window_to with shifts of up to three planes.
+__device__ __forceinline__ void slide_window_to(PlaneWindow<float>& w, int f, int Lp, const float4* __restrict__ g,
+                                                const SlideDir& a) {
+    const int d = f - w.f;
+    if (d == 0) return;
+    const bool top = w.f >= -1 && w.f + 2 < Lp;  // w.p[3] is plane w.f + 2, not the repeated last one
+    if (top && d == 1) {
+        w.p[0] = w.p[1];
+        w.p[1] = w.p[2];
+        w.p[2] = w.p[3];
+    } else if (top && d == 2) {
+        w.p[0] = w.p[2];
+        w.p[1] = w.p[3];
+        w.p[2] = slide_plane(g, f + 1, a);
+    } else if (top && d == 3) {
+        w.p[0] = w.p[3];
+        w.p[1] = slide_plane(g, f, a);
+        w.p[2] = slide_plane(g, f + 1, a);
+    } else {
+        w.p[0] = slide_plane(g, f - 1, a);
+        w.p[1] = slide_plane(g, f, a);
+        w.p[2] = slide_plane(g, f + 1, a);
+    }
+    w.p[3] = (f + 2 < Lp) ? slide_plane(g, f + 2, a) : w.p[2];
+    w.f = f;
+}
+
+// The block (bx, by) of the average of leaf M: chunks [bx DPT, bx DPT + DPT) x
+// brackets [by seg_len, by seg_len + seg_len).  Called block-uniformly.
+template <int DPT>
+__device__ __forceinline__ void slide_f32(const ModelDev& M, int Lp, const AvgPlan& plan, int seg_len,
+                                          const int* __restrict__ find, const float4* __restrict__ wq, int64_t bx,
+                                          int by) {
+    constexpr int MQ = 4, V = MQ * DPT;
+    const int64_t chunk0 = bx * DPT;
+    const int b0 = by * seg_len;
+    const int b1 = min(plan.n_brackets, b0 + seg_len);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ SlideSums<V> S;
+    int nslot = 0;
+    const float4* g = reinterpret_cast<const float4*>(M.grid);
+    SlideDir a[DPT];
+    bool valid[DPT];
+    PlaneWindow<float> win[DPT];
+#pragma unroll
+    for (int d = 0; d < DPT; ++d) {
+        const int64_t s = (chunk0 + d) * plan.chunk - plan.chunk_off + threadIdx.x;
+        valid[d] = (threadIdx.x < plan.chunk) && s >= 0 && s < plan.n_samples;
+        float th = 0.f, ph = 0.f;
+        if (valid[d]) {
+            const int64_t si = plan.dir_order ? plan.dir_order[s] : s;
+            const double* dd = plan.dirs + 2 * si;
+            th = (float)dd[0];
+            ph = (float)dd[1];
+            if (!M.plain) {  // the leaf's rotated direction (Amplitude.cpp:3553-3579)
+                float st, ct, sp, cp;
+                sincosf(th, &st, &ct);
+                sincosf(ph, &sp, &cp);
+                const float n0 = st * cp, n1 = st * sp, n2 = ct;
+                const float* C = M.Rf;
+                const float t0 = n0 * C[0] + n1 * C[3] + n2 * C[6];
+                const float t1 = n0 * C[1] + n1 * C[4] + n2 * C[7];
+                const float t2 = n0 * C[2] + n1 * C[5] + n2 * C[8];
+                th = atan2f(sqrtf(t0 * t0 + t1 * t1), t2);
+                ph = atan2f(t1, t0);
+                if (ph < 0.f) ph += k2PiF;
+            }
+        }
+        float thm = kPiF - th, phm = ph + kPiF;
+        if (phm >= k2PiF) phm -= k2PiF;
+        clamp_angles_f(th, ph);
+        clamp_angles_f(thm, phm);
+        a[d] = {th, ph, thm, phm};
+        win[d].f = -2;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) win[d].p[k] = {0.f, 0.f};
+    }
+    for (int b = b0; b < b1; ++b) {
+        const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
+        const int f = find[b];
+#pragma unroll
+        for (int d = 0; d < DPT; ++d)
+            if (valid[d]) slide_window_to(win[d], f, Lp, g, a[d]);
+        for (int qc = 0; qc < m; qc += MQ) {
+            const int mq = min(MQ, m - qc);
+            float v[V];
+#pragma unroll
+            for (int k = 0; k < MQ; ++k) {
+                const float4 w = (k < mq) ? wq[q0 + qc + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int d = 0; d < DPT; ++d) {
+                    const Cx<float> A = dot4(w, win[d].p[0], win[d].p[1], win[d].p[2], win[d].p[3]);
+                    v[d * MQ + k] = valid[d] ? fmaf(A.r, A.r, A.i * A.i) : 0.f;
+                }
+            }
+            const float sum = warp_sums<V>(v, lane);
+            if ((lane & (32 / V - 1)) == 0) S.red[nslot][warp][lane / (32 / V)] = sum;
+            if (threadIdx.x == 0) {
+                S.b[nslot] = b;
+                S.q[nslot] = qc;
+                S.m[nslot] = mq;
+            }
+            if (++nslot == kAvgSlots) slide_flush<V>(S, nslot, plan, chunk0);
+        }
+    }
+    slide_flush<V>(S, nslot, plan, chunk0);
+}
+
+template <int DPT>
+__global__ void __launch_bounds__(128) average_slide_f32_kernel(int Lp, const ModelDev* __restrict__ models,
+                                                                AvgPlan plan, int seg_len,
+                                                                const int* __restrict__ find,
+                                                                const float4* __restrict__ wq) {
+    slide_f32<DPT>(models[0], Lp, plan, seg_len, find, wq, blockIdx.x, blockIdx.y);
 }
 
 // --------------------------------------------------------------------------
@@ -840,9 +1086,8 @@ __global__ void __launch_bounds__(kDirBlock) dir_scatter(const int* __restrict__
     }
 }
 
-// eps = 0: the sum of each bracket's chunk partials, in a fixed order.
-__global__ void __launch_bounds__(128) finalize_sum_kernel(AvgPlan plan, double* __restrict__ res) {
-    const int b = blockIdx.x;
+// eps = 0: the sum of bracket b's chunk partials, in a fixed order (a block of 128).
+__device__ __forceinline__ void finalize_sum_at(const AvgPlan& plan, int b, double* __restrict__ res) {
     const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
     const double* part = plan.partial + (int64_t)b * plan.n_chunks * plan.max_q;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -859,13 +1104,14 @@ __global__ void __launch_bounds__(128) finalize_sum_kernel(AvgPlan plan, double*
         __syncthreads();
     }
 }
+__global__ void __launch_bounds__(128) finalize_sum_kernel(AvgPlan plan, double* __restrict__ res) {
+    finalize_sum_at(plan, blockIdx.x, res);
+}
 
 // Sequential convergence scan per bracket (AverageIntensitiesBetweenLayers,
 // Amplitude.cpp:2773-2815): running sums chunk by chunk; with eps > 0 the
 // reference's 4-column history is tested at every 100th sample.
-__global__ void finalize_kernel(AvgPlan plan, double eps, double* __restrict__ res) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= plan.n_brackets) return;
+__device__ void finalize_scan_at(const AvgPlan& plan, double eps, int b, double* __restrict__ res) {
     const int q0 = plan.br_q_off[b], m = plan.br_q_off[b + 1] - q0;
     const double* part = plan.partial + (int64_t)b * plan.n_chunks * plan.max_q;
     double* out = plan.partial + ((int64_t)plan.n_brackets * plan.n_chunks) * plan.max_q +
@@ -924,6 +1170,10 @@ __global__ void finalize_kernel(AvgPlan plan, double eps, double* __restrict__ r
         }
     }
     for (int k = 0; k < m; ++k) res[plan.br_qidx[q0 + k]] = run[k] / (double)plan.n_samples;
+}
+__global__ void finalize_kernel(AvgPlan plan, double eps, double* __restrict__ res) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < plan.n_brackets) finalize_scan_at(plan, eps, b, res);
 }
 
 template <typename V4>
@@ -1408,57 +1658,215 @@ size_t dir_sort_bytes(int64_t n) {
     return ((size_t)2 * n + (size_t)2 * kDirKeys * nblk + kDirKeys) * sizeof(int) + 256;
 }
 
+// Directions per thread of the FP32 slide average (1 or 2), process-wide.
+static int g_avg_dpt = 1;
+
+namespace {
+int device_sms() {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+// Segments of consecutive brackets: enough blocks to fill the GPU a few times
+// over, at most 64 brackets a segment.  bx = blocks along the chunks.
+struct AvgShape {
+    bool slide;
+    int64_t bx, n_seg;
+    int seg_len;
+};
+AvgShape avg_shape(const AvgPlan& plan, bool fp64, int n_models, int sms) {
+    AvgShape a;
+    const int64_t nbr = plan.n_brackets;
+    a.slide = plan.one_leaf && n_models == 1 && plan.dir_stride == 0;
+    a.bx = (a.slide && !fp64) ? (plan.n_chunks + g_avg_dpt - 1) / g_avg_dpt : plan.n_chunks;
+    const int64_t target = (int64_t)sms * 16;
+    int64_t n_seg = std::max<int64_t>((nbr + 63) / 64, (target + a.bx - 1) / a.bx);
+    n_seg = std::min<int64_t>(n_seg, nbr);
+    a.seg_len = (int)((nbr + n_seg - 1) / n_seg);
+    a.n_seg = (nbr + a.seg_len - 1) / a.seg_len;
+    return a;
+}
+
+// The bracket tables live in the finalize scratch behind the partial sums
+// (5 n_brackets max_q doubles, unused until the finalize): plane indices,
+// then the fractions of every q (FP64, and FP32 outside the slide) or, 16 B
+// aligned, the FP32 slide's radial weights (at most 2 n_brackets max_q doubles).
+struct AvgTables {
+    int* find;
+    double* frac;
+    float4* wq;
+};
+__host__ __device__ inline AvgTables avg_tables(const AvgPlan& plan) {
+    AvgTables t;
+    double* tab = plan.partial + (size_t)plan.n_brackets * plan.n_chunks * plan.max_q;
+    t.find = reinterpret_cast<int*>(tab);
+    t.frac = tab + (plan.n_brackets + 1) / 2;
+    t.wq = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(t.frac) + 15) & ~uintptr_t(15));
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// Batched averages: every solve of a batch in one launch per stage (tables,
+// average, finalize with the q = 0 term).  A block of the average finds its
+// solve by a binary search over the solves' first blocks.
+// ---------------------------------------------------------------------------
+template <bool FP64>
+__global__ void batch_tables_kernel(const AvgJob* __restrict__ jobs) {
+    const AvgJob& J = jobs[blockIdx.y];
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= J.plan.n_brackets) return;
+    const AvgTables t = avg_tables(J.plan);
+    if (FP64) bracket_tables_at<double>(J.plan, J.step, b, t.find, t.frac);
+    else bracket_weights_at(J.plan, J.step, b, t.find, t.wq);
+}
+
+__device__ __forceinline__ int batch_job_of(const AvgJob* __restrict__ jobs, int n_jobs, int64_t block) {
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block0 <= block) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int DPT>
+__global__ void __launch_bounds__(128) batch_average_f32_kernel(const AvgJob* __restrict__ jobs, int n_jobs) {
+    const AvgJob& J = jobs[batch_job_of(jobs, n_jobs, blockIdx.x)];
+    const int64_t local = (int64_t)blockIdx.x - J.block0;
+    const AvgTables t = avg_tables(J.plan);
+    slide_f32<DPT>(*J.model, J.Lp, J.plan, J.seg_len, t.find, t.wq, local % J.bx, (int)(local / J.bx));
+}
+
+__global__ void __launch_bounds__(128) batch_average_f64_kernel(const AvgJob* __restrict__ jobs, int n_jobs) {
+    const AvgJob& J = jobs[batch_job_of(jobs, n_jobs, blockIdx.x)];
+    const int64_t local = (int64_t)blockIdx.x - J.block0;
+    const AvgTables t = avg_tables(J.plan);
+    slide_f64<double, 4>(*J.model, J.Lp, J.plan, J.seg_len, t.find, t.frac, local % J.bx, (int)(local / J.bx));
+}
+
+// Block (b, j): bracket b of solve j (eps = 0: the block's sum; eps > 0: the
+// sequential scan on thread 0); block (0, j) also writes I(0) = |F(0)|^2 of
+// the solve's plain leaf (Amplitude.cpp:1176-1182) when its first q is 0.
+__global__ void __launch_bounds__(128) batch_finalize_kernel(const AvgJob* __restrict__ jobs, double eps, int fp64) {
+    const AvgJob& J = jobs[blockIdx.y];
+    const int b = blockIdx.x;
+    if (b == 0 && threadIdx.x == 0 && J.origin) {
+        double re, im;
+        if (fp64) {
+            const double* g = static_cast<const double*>(J.model->grid);
+            re = g[0];
+            im = g[1];
+        } else {
+            const float* g = static_cast<const float*>(J.model->grid);
+            re = g[0];
+            im = g[1];
+        }
+        J.res[0] = re * re + im * im;
+    }
+    if (b >= J.plan.n_brackets) return;
+    if (eps > 0.0) {
+        if (threadIdx.x == 0) finalize_scan_at(J.plan, eps, b, J.res);
+    } else {
+        finalize_sum_at(J.plan, b, J.res);
+    }
+}
+}  // namespace
+
+const int* launch_dir_order(cudaStream_t s, const double* dirs, int64_t n, int* scratch) {
+    if (!scratch || n < 2 * kDirBlock || n > 0x7fffffff) return nullptr;
+    const int nblk = (int)((n + kDirBlock - 1) / kDirBlock);
+    int* key = scratch;
+    int* hist = key + n;
+    int* off = hist + (size_t)kDirKeys * nblk;
+    int* tot = off + (size_t)kDirKeys * nblk;
+    int* order = tot + kDirKeys;
+    dir_keys<<<nblk, kDirBlock, 0, s>>>(dirs, n, key, hist, nblk);
+    dir_totals<<<kDirKeys, 128, 0, s>>>(hist, nblk, tot);
+    dir_offsets<<<kDirKeys, 128, 0, s>>>(hist, tot, nblk, off);
+    dir_scatter<<<nblk, kDirBlock, 0, s>>>(key, n, off, nblk, order);
+    return order;
+}
+
 cudaError_t launch_average(cudaStream_t s, bool fp64, const Geom& g, int n_models, const ModelDev* d_models,
-                           const AvgPlan& plan_in) {
+                           const AvgPlan& plan_in, cudaEvent_t* kev) {
     if (plan_in.n_brackets == 0 || plan_in.n_chunks == 0) return cudaSuccess;
     if (plan_in.n_chunks > 0x7fffffff) return cudaErrorInvalidValue;
     AvgPlan plan = plan_in;
-    plan.dir_order = nullptr;
-    if (plan.sort_scratch && plan.dir_stride == 0 && plan.n_samples >= 2 * kDirBlock &&
-        plan.n_samples <= 0x7fffffff) {
-        const int64_t n = plan.n_samples;
-        const int nblk = (int)((n + kDirBlock - 1) / kDirBlock);
-        int* key = plan.sort_scratch;
-        int* hist = key + n;
-        int* off = hist + (size_t)kDirKeys * nblk;
-        int* tot = off + (size_t)kDirKeys * nblk;
-        int* order = tot + kDirKeys;
-        dir_keys<<<nblk, kDirBlock, 0, s>>>(plan.dirs, n, key, hist, nblk);
-        dir_totals<<<kDirKeys, 128, 0, s>>>(hist, nblk, tot);
-        dir_offsets<<<kDirKeys, 128, 0, s>>>(hist, tot, nblk, off);
-        dir_scatter<<<nblk, kDirBlock, 0, s>>>(key, n, off, nblk, order);
-        plan.dir_order = order;
-    }
-    // segments of consecutive brackets: enough blocks to fill the GPU a few
-    // times over, at most 64 brackets a segment
-    int dev = 0, sms = 152;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // a shared direction set in angular order (sorted here, or given sorted)
+    if (plan.sort_scratch && plan.dir_stride == 0) plan.dir_order = launch_dir_order(s, plan.dirs, plan.n_samples,
+                                                                                      plan.sort_scratch);
+    const AvgShape a = avg_shape(plan, fp64, n_models, device_sms());
+    if (a.n_seg > 65535) return cudaErrorInvalidValue;
     const int64_t nbr = plan.n_brackets;
-    const int64_t target = (int64_t)sms * 16;
-    int64_t n_seg = std::max<int64_t>((nbr + 63) / 64, (target + plan.n_chunks - 1) / plan.n_chunks);
-    n_seg = std::min<int64_t>(n_seg, nbr);
-    const int seg_len = (int)((nbr + n_seg - 1) / n_seg);
-    n_seg = (nbr + seg_len - 1) / seg_len;
-    if (n_seg > 65535) return cudaErrorInvalidValue;
-    // the bracket tables live in the finalize scratch behind the partial sums
-    // (5 n_brackets max_q doubles, unused until the finalize): plane indices,
-    // then the fractions of every q
-    double* tab = plan.partial + (size_t)nbr * plan.n_chunks * plan.max_q;
-    int* find = reinterpret_cast<int*>(tab);
-    double* frac = tab + (nbr + 1) / 2;
-    dim3 grid((unsigned)plan.n_chunks, (unsigned)n_seg);
-    const bool slide = plan.one_leaf && n_models == 1 && plan.dir_stride == 0;
-    if (fp64) {
-        bracket_tables_kernel<double><<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, find, frac);
-        if (slide) average_slide_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, seg_len, find, frac);
-        else average_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, n_models, plan, seg_len, find, frac);
-    } else {
-        float* fracf = reinterpret_cast<float*>(frac);
-        bracket_tables_kernel<float><<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, find, fracf);
-        if (slide) average_slide_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, seg_len, find, fracf);
-        else average_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, n_models, plan, seg_len, find, fracf);
+    const AvgTables t = avg_tables(plan);
+    float* fracf = reinterpret_cast<float*>(t.frac);
+    if (fp64) bracket_tables_kernel<double><<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, t.find, t.frac);
+    else if (a.slide) bracket_weights_kernel<<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, t.find, t.wq);
+    else bracket_tables_kernel<float><<<blocks_for(nbr, 128), 128, 0, s>>>(plan, g.step, t.find, fracf);
+    const dim3 grid((unsigned)a.bx, (unsigned)a.n_seg);
+    if (kev) cudaEventRecord(kev[0], s);
+    if (fp64 && a.slide)
+        average_slide_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, a.seg_len, t.find, t.frac);
+    else if (fp64)
+        average_kernel<double, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, n_models, plan, a.seg_len, t.find, t.frac);
+    else if (a.slide && g_avg_dpt == 2)
+        average_slide_f32_kernel<2><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, a.seg_len, t.find, t.wq);
+    else if (a.slide)
+        average_slide_f32_kernel<1><<<grid, 128, 0, s>>>(g.Lp, d_models, plan, a.seg_len, t.find, t.wq);
+    else
+        average_kernel<float, 4><<<grid, 128, 0, s>>>(g.Lp, d_models, n_models, plan, a.seg_len, t.find, fracf);
+    if (kev) cudaEventRecord(kev[1], s);
+    return cudaGetLastError();
+}
+
+int64_t plan_average_batch(AvgJob* jobs, int n, bool fp64) {
+    const int sms = device_sms();
+    int64_t blocks = 0;
+    for (int j = 0; j < n; ++j) {
+        AvgJob& J = jobs[j];
+        J.block0 = blocks;
+        J.bx = J.n_seg = J.seg_len = 0;
+        if (J.plan.n_brackets == 0 || J.plan.n_chunks == 0) continue;
+        const AvgShape a = avg_shape(J.plan, fp64, 1, sms);
+        J.bx = a.bx;
+        J.n_seg = (int)a.n_seg;
+        J.seg_len = a.seg_len;
+        blocks += a.bx * a.n_seg;
+    }
+    return blocks;
+}
+
+cudaError_t launch_average_batch(cudaStream_t s, bool fp64, const AvgJob* d_jobs, int n_jobs, int max_brackets,
+                                 int64_t total_blocks, double eps) {
+    if (n_jobs <= 0) return cudaSuccess;
+    if (total_blocks > 0x7fffffff) return cudaErrorInvalidValue;
+    for (int j0 = 0; j0 < n_jobs; j0 += 65535) {
+        const int nj = std::min(65535, n_jobs - j0);
+        if (max_brackets > 0) {
+            const dim3 g((unsigned)blocks_for(max_brackets, 128), (unsigned)nj);
+            if (fp64) batch_tables_kernel<true><<<g, 128, 0, s>>>(d_jobs + j0);
+            else batch_tables_kernel<false><<<g, 128, 0, s>>>(d_jobs + j0);
+        }
+    }
+    if (total_blocks > 0) {
+        if (fp64) batch_average_f64_kernel<<<(unsigned)total_blocks, 128, 0, s>>>(d_jobs, n_jobs);
+        else if (g_avg_dpt == 2) batch_average_f32_kernel<2><<<(unsigned)total_blocks, 128, 0, s>>>(d_jobs, n_jobs);
+        else batch_average_f32_kernel<1><<<(unsigned)total_blocks, 128, 0, s>>>(d_jobs, n_jobs);
+    }
+    for (int j0 = 0; j0 < n_jobs; j0 += 65535) {
+        const int nj = std::min(65535, n_jobs - j0);
+        const dim3 g((unsigned)std::max(1, max_brackets), (unsigned)nj);
+        batch_finalize_kernel<<<g, 128, 0, s>>>(d_jobs + j0, eps, fp64 ? 1 : 0);
     }
     return cudaGetLastError();
+}
+
+int set_average_dpt(int dpt) {
+    if (dpt != 1 && dpt != 2) return -1;
+    g_avg_dpt = dpt;
+    return 0;
 }
 
 namespace {

@@ -75,12 +75,14 @@ _SIGS = {
     "dpx_ctx_synchronize": (C.c_int, [_P]),
     "dpx_ctx_set_fill_shape": (C.c_int, [_P, C.c_int, C.c_int]),
     "dpx_ctx_set_fill_schedule": (C.c_int, [_P, C.c_int]),
+    "dpx_set_average_shape": (C.c_int, [C.c_int]),
     "dpx_ctx_set_fill_poly": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_set_fill_method": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_get_fill_method": (C.c_int, [_P]),
     "dpx_ctx_set_convergence": (C.c_int, [_P, C.c_int, C.c_int64]),
     "dpx_ctx_set_timing": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_stage_times": (C.c_int, [_P, _D]),
+    "dpx_ctx_average_kernel_ms": (C.c_int, [_P, _D]),
     "dpx_ctx_get_fill_shape": (C.c_int, [_P, _I]),
     "dpx_fill_shapes": (C.c_int, [_I]),
     "dpx_grid_cells": (C.c_int64, [C.c_int]),

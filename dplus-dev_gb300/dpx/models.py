@@ -373,6 +373,12 @@ def pdb_descs(leaves: Sequence[PDBAmplitude]):
     return descs, keep
 
 
+def set_average_shape(directions_per_thread: int) -> None:
+    """Directions per thread (1 or 2) of the FP32 average of one undocked leaf
+    over a shared direction set, process-wide (dpx_set_average_shape)."""
+    check(lib().dpx_set_average_shape(int(directions_per_thread)))
+
+
 def autotune_fill(ctx: Context, leaves: Sequence[PDBAmplitude], qmax: float, gridSize: int, repeats: int = 2):
     """Project autotuner: time every FP32 fill shape on these leaves and keep
     the fastest in the context.  Returns (best (cpt, threads, persistent,

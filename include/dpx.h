@@ -112,6 +112,11 @@ int dpx_ctx_set_fill_poly(dpx_ctx ctx, int poly_columns);
  * serving fills.  dpx_autotune_fill times it beside the direct shapes (the
  * row {0, 0, 0, 0} of dpx_fill_shapes). */
 enum { DPX_FILL_DIRECT = 0, DPX_FILL_HARMONIC = 1 };
+/* Directions per thread (1, the default, or 2) of the FP32 orientation average
+ * of one undocked leaf over a shared direction set, for every context of the
+ * process: 2 gives each thread the samples of two neighbouring chunks, twice
+ * the independent gathers in flight at a higher register count. */
+int dpx_set_average_shape(int directions_per_thread);
 int dpx_ctx_set_fill_method(dpx_ctx ctx, int method);
 int dpx_ctx_get_fill_method(dpx_ctx ctx);
 /* Convergence test of the Monte Carlo average (eps > 0) for this context's
@@ -136,6 +141,9 @@ int dpx_ctx_set_convergence(dpx_ctx ctx, int rule, int64_t samples_per_step);
  * was none). */
 int dpx_ctx_set_timing(dpx_ctx ctx, int on);
 int dpx_ctx_stage_times(dpx_ctx ctx, double* out);
+/* With timing on: *ms = the device time of the last dpx_orientation_average's
+ * main kernel alone (CUDA events around that launch; 0 when there was none). */
+int dpx_ctx_average_kernel_ms(dpx_ctx ctx, double* ms);
 /* shape[4] = {cells_per_thread, threads, persistent, poly_columns} in use. */
 int dpx_ctx_get_fill_shape(dpx_ctx ctx, int* shape);
 /* The shapes the autotuner sweeps: writes 4 ints per shape (if shapes != NULL)

@@ -130,6 +130,36 @@ def test_placed_leaf_rotation_translation(ctx):
     assert rel(I, ref) <= TOL64
 
 
+@pytest.mark.parametrize("dpt", [1, 2])
+def test_fp32_slide_average_matches_oracle(ctx, dpt):
+    """The FP32 average of one undocked leaf over a shared direction set (the
+    plane window with the radial weight table), at one and two directions per
+    thread: a plain leaf with an odd chunk count (the two-direction blocks'
+    last chunk runs past the samples), a placed leaf, q sets whose brackets
+    skip one and two planes (the window's shifts by 2 and 3), and eps > 0
+    (chunks of 100 samples)."""
+    amp = globule(600, 1.6, seed=81, extra=SOLVENT)
+    gs, qmax = 48, 5.0
+    data, co = oracle_grid(amp, gs, qmax)
+    dirs = M.mc_directions(83, 128 * 7 + 45)
+    cases = [(np.linspace(0, qmax, 157), None, 0.0),
+             (np.linspace(0.05, 4.9, 61), (0.4, -0.8, 1.5, 0.3, -0.7, 1.9), 0.0),
+             (np.linspace(0.02, 4.95, 13), None, 0.0),
+             (np.concatenate([np.linspace(0.1, 1.0, 4), np.linspace(1.3, 4.8, 7)]), None, 0.0),
+             (np.linspace(0.1, 4.9, 90), None, 2e-3)]
+    try:
+        M.set_average_shape(dpt)
+        for Q, loc, eps in cases:
+            amp.location = loc or (0, 0, 0, 0, 0, 0)
+            I = _avg(ctx, amp, gs, qmax, Q, dirs, M.FP32, eps=eps)
+            leaf = O.make_leaf(data, co) if loc is None else O.make_leaf(data, co, rot=loc[3:], tr=loc[:3])
+            ref = O.integrate_layers(gs, qmax, [leaf], Q, dirs, 0, len(dirs), eps)
+            assert rel(I, ref) <= TOL32, (len(Q), loc, eps)
+    finally:
+        M.set_average_shape(1)
+        amp.location = (0, 0, 0, 0, 0, 0)
+
+
 @pytest.mark.parametrize("prec,tol", [(M.FP64, TOL64), (M.FP32, TOL32)])
 def test_docked_sum_matches_oracle(ctx, prec, tol):
     """ManualSymmetry docked copies (hybrid per-orientation sum), incl. two
