@@ -170,7 +170,7 @@ __device__ __forceinline__ uint32_t tf32_rna(float v) {
 }
 
 __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
+    asm(
         "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
@@ -799,7 +799,9 @@ __device__ __forceinline__ float sinc_h(float h) {
 //     F(s i + j) = sum_{r < 6} e^{2 pi i r s / 6} D_r(j),
 //     D_r(j) = sum_{m = r mod 6} G_m w^{mj},
 //   so a thread per (row, column j) sums the G_m once into six residue
-//   classes and finishes its six cells with a 6-point DFT; as many rows run at
+//   classes (each by Horner's rule in z = w^{6j}: D_r(j) = w^{m_r j}
+//   sum_k G_{m_r + 6k} z^k, m_r the class's lowest order) and finishes its six
+//   cells with a 6-point DFT; as many rows run at
 //   once as 256 threads have columns for.  Then the voxel form factor, the
 //   centring phase (double-float), and the rows' phi-spline derivatives
 //   (row_spline, as the spline pass computes them) written with the values;
@@ -954,23 +956,39 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* 
             float2 D[6], Dv[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) D[c] = Dv[c] = make_float2(0.f, 0.f);
-            int idx = (int)(((int64_t)m0p * j) % nph);
-            if (idx < 0) idx += nph;
-            for (int u = 0; u < nG; u += 6) {
+            // D_c = w^{(m0 + c) j} sum_k G_{m0 + c + 6k} z^k with z = w^{6j}: Horner
+            // over k (no twiddle lookups in the loop), then one twiddle per class
+            const float2 z = sW[6 * j];
+            const int top = nG - 6;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                D[c] = gA[top + c];
+                if (vox) Dv[c] = gV[top + c];
+            }
+            for (int u = top - 6; u >= 0; u -= 6) {
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
-                    const float2 w = sW[idx];
                     const float2 g = gA[u + c];
-                    D[c].x = fmaf(g.x, w.x, fmaf(-g.y, w.y, D[c].x));
-                    D[c].y = fmaf(g.x, w.y, fmaf(g.y, w.x, D[c].y));
+                    const float2 a = D[c];
+                    D[c].x = fmaf(a.x, z.x, fmaf(-a.y, z.y, g.x));
+                    D[c].y = fmaf(a.x, z.y, fmaf(a.y, z.x, g.y));
                     if (vox) {
                         const float2 gv = gV[u + c];
-                        Dv[c].x = fmaf(gv.x, w.x, fmaf(-gv.y, w.y, Dv[c].x));
-                        Dv[c].y = fmaf(gv.x, w.y, fmaf(gv.y, w.x, Dv[c].y));
+                        const float2 b = Dv[c];
+                        Dv[c].x = fmaf(b.x, z.x, fmaf(-b.y, z.y, gv.x));
+                        Dv[c].y = fmaf(b.x, z.y, fmaf(b.y, z.x, gv.y));
                     }
-                    idx += j;  // idx, j < 6i
-                    if (idx >= nph) idx -= nph;
                 }
+            }
+            int idx = (int)(((int64_t)m0p * j) % nph);
+            if (idx < 0) idx += nph;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const float2 w = sW[idx];
+                D[c] = make_float2(fmaf(D[c].x, w.x, -D[c].y * w.y), fmaf(D[c].x, w.y, D[c].y * w.x));
+                if (vox) Dv[c] = make_float2(fmaf(Dv[c].x, w.x, -Dv[c].y * w.y), fmaf(Dv[c].x, w.y, Dv[c].y * w.x));
+                idx += j;  // idx, j < 6i
+                if (idx >= nph) idx -= nph;
             }
             const float st = sRow[r][0].x, ct = sRow[r][0].y;
             const float2 A2 = sRow[r][1], B2 = sRow[r][2], Z2 = sRow[r][3];

@@ -971,8 +971,13 @@ __device__ __forceinline__ void slide_f32(const ModelDev& M, int Lp, const AvgPl
     slide_flush<V>(S, nslot, plan, chunk0);
 }
 
+// The gathers' latency is hidden by resident warps: one direction per thread
+// is capped at 64 registers (8 blocks of 128 per SM, no spills) instead of
+// the 76 it takes uncapped (6 blocks).
+constexpr int slide_min_blocks(int dpt) { return dpt == 1 ? 8 : 1; }
+
 template <int DPT>
-__global__ void __launch_bounds__(128) average_slide_f32_kernel(int Lp, const ModelDev* __restrict__ models,
+__global__ void __launch_bounds__(128, slide_min_blocks(DPT)) average_slide_f32_kernel(int Lp, const ModelDev* __restrict__ models,
                                                                 AvgPlan plan, int seg_len,
                                                                 const int* __restrict__ find,
                                                                 const float4* __restrict__ wq) {
@@ -1732,7 +1737,7 @@ __device__ __forceinline__ int batch_job_of(const AvgJob* __restrict__ jobs, int
 }
 
 template <int DPT>
-__global__ void __launch_bounds__(128) batch_average_f32_kernel(const AvgJob* __restrict__ jobs, int n_jobs) {
+__global__ void __launch_bounds__(128, slide_min_blocks(DPT)) batch_average_f32_kernel(const AvgJob* __restrict__ jobs, int n_jobs) {
     const AvgJob& J = jobs[batch_job_of(jobs, n_jobs, blockIdx.x)];
     const int64_t local = (int64_t)blockIdx.x - J.block0;
     const AvgTables t = avg_tables(J.plan);
