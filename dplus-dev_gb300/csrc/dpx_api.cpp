@@ -222,12 +222,6 @@ void ctx_release(dpx_ctx ctx) {
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->aev)
         if (e) cudaEventDestroy(e);
-    if (ctx->aux) {
-        cudaStreamSynchronize(ctx->aux);
-        cudaStreamDestroy(ctx->aux);
-    }
-    for (cudaEvent_t e : {ctx->aux_go, ctx->aux_done, ctx->aux_atoms})
-        if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -456,25 +450,18 @@ int check_pdb(const dpx_pdb_desc& d) {
 }
 
 int ctx_harmonic_streams(dpx_ctx ctx, HarmStreams& S) {
-    if (!ctx->aux) DPX_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&ctx->aux_go, &ctx->aux_done, &ctx->aux_atoms})
-        if (!*e) DPX_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     if (ctx->timing)
         for (cudaEvent_t& e : ctx->tev)
             if (!e) DPX_CUDA(cudaEventCreate(&e));
     S = HarmStreams{};
     S.st = ctx->stream;
-    S.ax = ctx->aux;
-    S.go = ctx->aux_go;
-    S.tables = ctx->aux_done;
-    S.atoms = ctx->aux_atoms;
     S.tev = ctx->timing ? ctx->tev : nullptr;
     return DPX_OK;
 }
 
 void ctx_stage_record(dpx_ctx ctx, const HarmPlan& p) {
     if (!ctx->timing) return;
-    ctx->tev_used = p.n_vox ? 8 : 6;
+    ctx->tev_used = 6;  // moments (both point sets in one launch), synthesis, the whole fill
     ctx->stage_points = p.stage_points;
     ctx->stage_k = p.stage_k;
 }

@@ -7,9 +7,11 @@
 // 1168-1247, 2746-2822), which the reference runs one structure at a time.
 // Here the solves are packed into waves whose grids fit a device-memory
 // budget.  Each wave is one CUDA graph:
-//   FP32 with the harmonic method (the default): per structure the harmonic
-//   fill planned at creation (tables, moments, contraction, synthesis with the
-//   phi-spline derivatives), one scratch shared by the fills in order;
+//   FP32 with the harmonic method (the default): the fills planned at
+//   creation, run in fill batches (as many structures as 8 GiB of scratch
+//   holds, each its own part of it): five launches per batch over its job
+//   table (radial nodes, moments, radial fit + group sums, contraction,
+//   synthesis with the phi-spline derivatives: launch_harmonic_jobs);
 //   FP32 leaves the harmonic method declines: one direct-sum launch over all of
 //   them, then their splines; FP64: the direct sum per structure and splines;
 //   the MC averages of all the wave's structures in three launches (bracket
@@ -48,7 +50,13 @@ struct dpx_batch_s {
     std::vector<cudaGraph_t> graphs;
     std::vector<cudaGraphExec_t> execs;
     std::vector<dpxh::HarmPlan> plans;  // FP32 solves the harmonic method fills (arena != nullptr)
-    void* hscratch = nullptr;           // their launch scratch, shared (the fills run in order)
+    void* hscratch = nullptr;           // the scratch of one fill batch (each fill its own part)
+    dpx::HarmJob* hjobs = nullptr;      // [harmonic solves] the fill batches' job tables (device)
+    struct FillBatch {
+        int wave, first, n;             // jobs [first, first + n) of hjobs
+        dpx::HarmShape shape;
+    };
+    std::vector<FillBatch> fbatches;
     dpx::AvgJob* jobs = nullptr;        // [n] the batched averages' solves (device)
     int* dsort = nullptr;               // the shared directions' angular order (eps = 0), sorted once
 };
@@ -68,6 +76,7 @@ void batch_free(dpx_batch b) {
     if (b->h_res) cudaFreeHost(b->h_res);
     for (dpxh::HarmPlan& p : b->plans) dpxh::harmonic_plan_release(p);
     if (b->hscratch) cudaFree(b->hscratch);
+    if (b->hjobs) cudaFree(b->hjobs);
     if (b->jobs) cudaFree(b->jobs);
     if (b->dsort) cudaFree(b->dsort);
     cudaStreamSynchronize(b->ctx->stream);
@@ -163,7 +172,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     // the harmonic method plans the FP32 solves it takes (host work and
     // synchronizations here, at creation); the graphs then only replay kernels
     b->plans.resize(n);
-    size_t hscratch = 0;
+    size_t hmax = 0;
     if (fp32 && ctx->fill_method == DPX_FILL_HARMONIC)
         for (int j = 0; j < n; ++j) {
             const int rc = harmonic_plan(ctx->stream, solves[j].pdb, sp[j].G, b->plans[j]);
@@ -171,9 +180,32 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
                 batch_free(b);
                 return rc;
             }
-            if (rc == DPX_OK) hscratch = std::max(hscratch, b->plans[j].scratch_bytes);
+            if (rc == DPX_OK) hmax = std::max(hmax, b->plans[j].scratch_bytes);
         }
     auto harmonic = [&](int j) { return b->plans[j].arena != nullptr; };
+    // fill batches: a wave's harmonic fills in order, each batch's scratch (the
+    // sum of its fills') within 8 GiB or the largest single fill's
+    const size_t fb_budget = std::max(hmax, (size_t)8 << 30);
+    size_t hscratch = 0;
+    std::vector<size_t> sc_off(n, 0);
+    std::vector<int> hjob_of(n, -1);
+    int n_hjobs = 0;
+    for (int w = 0; w < n_waves; ++w) {
+        size_t used = 0;
+        for (int j = b->wave_first[w]; j < b->wave_first[w + 1]; ++j) {
+            if (!harmonic(j)) continue;
+            const size_t need = (b->plans[j].scratch_bytes + 255) & ~size_t(255);
+            if (b->fbatches.empty() || b->fbatches.back().wave != w || used + need > fb_budget) {
+                b->fbatches.push_back({w, n_hjobs, 0, {}});
+                used = 0;
+            }
+            sc_off[j] = used;
+            used += need;
+            hscratch = std::max(hscratch, used);
+            hjob_of[j] = n_hjobs++;
+            b->fbatches.back().n++;
+        }
+    }
 
     // staging of every input table
     Stage st;
@@ -251,6 +283,7 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_res, b->res_total * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_res, b->res_total * sizeof(double));
     if (e == cudaSuccess && hscratch) e = cudaMalloc(&b->hscratch, hscratch);
+    if (e == cudaSuccess && n_hjobs) e = cudaMalloc((void**)&b->hjobs, (size_t)n_hjobs * sizeof(dpx::HarmJob));
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "batch allocation");
         batch_free(b);
@@ -311,6 +344,13 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->jobs, jobs.data(), jobs.size() * sizeof(dpx::AvgJob),
                                               cudaMemcpyHostToDevice, s);
+    // the fill batches' job tables: scratch offsets in the batch scratch, grids in the wave's pool
+    std::vector<dpx::HarmJob> hjobs(n_hjobs);
+    for (int j = 0; j < n; ++j)
+        if (hjob_of[j] >= 0) hjobs[hjob_of[j]] = harmonic_job(b->plans[j], sc_off[j], sp[j].grid_off);
+    for (auto& fb : b->fbatches) fb.shape = dpx::plan_harmonic_jobs(hjobs.data() + fb.first, fb.n);
+    if (e == cudaSuccess && n_hjobs)
+        e = cudaMemcpyAsync(b->hjobs, hjobs.data(), hjobs.size() * sizeof(dpx::HarmJob), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "batch upload");
@@ -329,13 +369,13 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         int64_t launches = 0;
         const int j0 = b->wave_first[w], j1 = b->wave_first[w + 1];
         if (fp32) {
-            HarmStreams hs;
-            hs.st = s;  // the fills run in order on one stream and share the scratch
-            for (int j = j0; j < j1 && e == cudaSuccess; ++j) {
-                if (!harmonic(j)) continue;
-                if (harmonic_launch(hs, b->plans[j], b->hscratch, reinterpret_cast<float4*>(pool + sp[j].grid_off)))
-                    e = cudaErrorUnknown;
-                launches += harmonic_launches(b->plans[j]);
+            // the wave's harmonic fills: five launches per fill batch
+            for (const auto& fb : b->fbatches) {
+                if (fb.wave != w || e != cudaSuccess) continue;
+                e = dpx::launch_harmonic_jobs(s, b->hjobs + fb.first, fb.n, fb.shape,
+                                              static_cast<char*>(b->hscratch), pool, nullptr);
+                launches += (fb.shape.nodes > 0) + (fb.shape.moments > 0) + (fb.shape.fit + fb.shape.groups > 0) +
+                            (fb.shape.contract > 0) + (fb.shape.synth > 0);
             }
             bool boxes = false;
             int direct = 0;

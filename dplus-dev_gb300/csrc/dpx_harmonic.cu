@@ -63,9 +63,8 @@ __device__ __forceinline__ int l_of(int k) {
 // r_l = x / (2l + 1 - x r_{l+1}) (started 16 orders above) for the ratios above.
 // Jn[((i * nbins + b) * kNodes + c) * (LM + 1) + l].
 // ---------------------------------------------------------------------------
-__global__ void hm_nodes(int Lp, int nbins, int LM, double step, double delta, const int* __restrict__ lmax,
-                         const double* __restrict__ nodes, double* __restrict__ Jn) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void hm_nodes(int Lp, int nbins, int LM, double step, double delta, const int* __restrict__ lmax,
+                         const double* __restrict__ nodes, double* __restrict__ Jn, int64_t e) {
     const int64_t total = (int64_t)Lp * nbins * kNodes;
     if (e >= total) return;
     const int c = (int)(e % kNodes);
@@ -112,9 +111,8 @@ __global__ void hm_nodes(int Lp, int nbins, int LM, double step, double delta, c
 }
 
 // hm_fit: thread (shell i >= 1, bin b, l <= l_i): T[((i nbins + b)(LM+1) + l) * 8 + n].
-__global__ void hm_fit(int Lp, int nbins, int LM, const int* __restrict__ lmax, const double* __restrict__ vinv,
-                       const double* __restrict__ Jn, float* __restrict__ T) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void hm_fit(int Lp, int nbins, int LM, const int* __restrict__ lmax, const double* __restrict__ vinv,
+                       const double* __restrict__ Jn, float* __restrict__ T, int64_t e) {
     const int64_t total = (int64_t)Lp * nbins * (LM + 1);
     if (e >= total) return;
     const int l = (int)(e % (LM + 1));
@@ -276,20 +274,19 @@ __device__ __forceinline__ void moment_order(int l, int m, bool col_ok, int kc, 
     }
 }
 
-__global__ void __launch_bounds__(32) hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units,
-                                                 int K, float delta, const int* __restrict__ lmb,
-                                                 const float2* __restrict__ cr, const float* __restrict__ nmm,
-                                                 float2* __restrict__ MP) {
+__device__ void hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units, int K, float delta,
+                           const int* __restrict__ lmb, const float2* __restrict__ cr, const float* __restrict__ nmm,
+                           float2* __restrict__ MP, int bx, int by) {
     extern __shared__ __align__(16) unsigned char smem[];
     float2* sD = reinterpret_cast<float2*>(smem);  // per quartet [(l - m0) * 24 + lane], lanes < 24
     const int lane = threadIdx.x;
     const int g = lane >> 2, t = lane & 3;
-    const int4 un = units[blockIdx.x];
+    const int4 un = units[bx];
     const int LM = lmb[un.z];    // the orders of the unit's bin
     const int Q = (LM + 4) / 4;  // quartets
-    if ((int)blockIdx.y >= (Q + 1) / 2) return;
-    const int nq = (Q - 1 - (int)blockIdx.y > (int)blockIdx.y) ? 2 : 1;
-    const int m0a = 4 * blockIdx.y, m0b = 4 * (Q - 1 - blockIdx.y);
+    if (by >= (Q + 1) / 2) return;
+    const int nq = (Q - 1 - by > by) ? 2 : 1;
+    const int m0a = 4 * by, m0b = 4 * (Q - 1 - by);
     const int nla = LM - m0a + 1, nlb = nq == 2 ? LM - m0b + 1 : 0;
     const float rb = (un.z + 0.5f) * delta, ih = 2.f / delta;
     const bool drow = lane < 24;  // D rows n = g < 6
@@ -391,7 +388,7 @@ __global__ void __launch_bounds__(32) hm_moments(const float4* __restrict__ pts,
         const int mo = m0 + t;
         if (!drow || mo > LM) continue;
         const float2* sDq = sD + (qi == 0 ? 0 : nla * 24);
-        float2* out = MP + ((int64_t)blockIdx.x * kNodes + g) * K;
+        float2* out = MP + ((int64_t)bx * kNodes + g) * K;
         int k = mo * (mo + 1) / 2 + mo;
         for (int l = mo; l <= LM; ++l) {
             const float2 v = sDq[(l - m0) * 24 + lane];
@@ -688,9 +685,8 @@ __device__ __forceinline__ void sum2(float& s, float& c, float x) {
 
 // hm_groups: M[g][n][k] = sum of MP over the units [gu[g], gu[g+1]) of group g,
 // compensated.
-__global__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, const int2* __restrict__ groups,
-                          const int* __restrict__ lmb, int G, int K, float2* __restrict__ M) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void hm_groups(const float2* __restrict__ MP, const int* __restrict__ gu, const int2* __restrict__ groups,
+                          const int* __restrict__ lmb, int G, int K, float2* __restrict__ M, int64_t e) {
     const int64_t per = (int64_t)kNodes * K;
     if (e >= (int64_t)G * per) return;
     const int g = (int)(e / per);
@@ -719,14 +715,14 @@ constexpr int kContractShells = 8;
 constexpr int kContractK = 32;
 constexpr int kContractWarps = 4;
 
-__global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract(
-    const float2* __restrict__ M, const int2* __restrict__ groups, int G, const float* __restrict__ T, int nbins,
-    int LM, int K, int Lp, const int* __restrict__ lmax, const int* __restrict__ lmb, const float* __restrict__ aff,
-    float2* __restrict__ C) {
+__device__ void hm_contract(const float2* __restrict__ M, const int2* __restrict__ groups, int G,
+                            const float* __restrict__ T, int nbins, int LM, int K, int Lp, const int* __restrict__ lmax,
+                            const int* __restrict__ lmb, const float* __restrict__ aff, float2* __restrict__ C, int bx,
+                            int by) {
     __shared__ float4 part[kContractWarps][kContractShells][kContractK];  // {s_re, c_re, s_im, c_im}
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int k = blockIdx.x * kContractK + lane;
-    const int i0 = 1 + blockIdx.y * kContractShells;
+    const int k = bx * kContractK + lane;
+    const int i0 = 1 + by * kContractShells;
     const bool kok = k < K;
     const int l = kok ? l_of(k) : 0;
     float cr[kContractShells], ci[kContractShells], er[kContractShells], ei[kContractShells];
@@ -765,7 +761,7 @@ __global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract(
     // warp a' < kContractShells / ... : thread (shell a, lane) combines the four warps
     for (int e = threadIdx.x; e < kContractShells * kContractK; e += blockDim.x) {
         const int a = e / kContractK, kl = e % kContractK;
-        const int i = i0 + a, kk = blockIdx.x * kContractK + kl;
+        const int i = i0 + a, kk = bx * kContractK + kl;
         if (i > Lp || kk >= K) continue;
         float sr = 0.f, srr = 0.f, si = 0.f, sii = 0.f;
 #pragma unroll
@@ -830,18 +826,18 @@ __device__ __forceinline__ float2 split_ff(double x) {
     return make_float2(hi, (float)(x - (double)hi));
 }
 
-__global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* __restrict__ Ca,
+__device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
                                                           const float2* __restrict__ Cv, int K,
                                                           const int* __restrict__ lmax, const float2* __restrict__ ab,
                                                           const float* __restrict__ nmm, double step, float vox_s,
                                                           double cx, double cy, double cz, int use_center, float scale,
-                                                          double origin, float4* __restrict__ grid) {
+                                                          double origin, float4* __restrict__ grid, int bx, int by) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float2 sRow[kSynthRows][4];  // per row: {st, ct}, A, B, Z (double-float)
-    const int i = blockIdx.y + 1;
+    const int i = by + 1;
     const int h = 3 * i, nph = 6 * i;
     const int rows_i = h / 2 + 1;  // rows t = 0 .. floor(3i/2)
-    const int t0 = blockIdx.x * kSynthRows;
+    const int t0 = bx * kSynthRows;
     if (t0 >= rows_i) return;
     const int nr = min(kSynthRows, rows_i - t0);
     const int li = lmax[i];
@@ -1057,6 +1053,100 @@ __global__ void __launch_bounds__(kSynthThreads) hm_synth(int Lp, const float2* 
     if (i == 1 && t0 == 0 && tid == 0) grid[0] = make_float4((float)origin, 0.f, 0.f, 0.f);
 }
 
+// ---------------------------------------------------------------------------
+// Batched launches over a job table (HarmJob): a block finds its job (or its
+// job's point set) by a binary search over the first blocks, then runs the
+// body above with its local block index: the radial nodes of every job; the
+// moments of every (job, set); the radial fit, then the group sums, in one
+// launch; the contraction of every (job, set) whose coefficient set the
+// synthesis reads; the synthesis of every job.
+// ---------------------------------------------------------------------------
+constexpr int kNodesThreads = 128, kFitThreads = 256;
+
+__device__ __forceinline__ int job_of(const HarmJob* __restrict__ J, int n, int64_t blk, int64_t HarmJob::*key) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (J[mid].*key <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+// (job, set) 2j + k of a per-set launch: the last with its first block <= blk
+__device__ __forceinline__ int set_of(const HarmJob* __restrict__ J, int n, int64_t blk, int64_t (HarmJob::*key)[2]) {
+    int lo = 0, hi = 2 * n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((J[mid >> 1].*key)[mid & 1] <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int synth_groups(int Lp) { return (3 * Lp / 2 + 1 + kSynthRows - 1) / kSynthRows; }
+
+__global__ void __launch_bounds__(kNodesThreads) hm_nodes_jobs(const HarmJob* __restrict__ J, int n,
+                                                              char* __restrict__ scratch) {
+    const HarmJob& h = J[job_of(J, n, blockIdx.x, &HarmJob::b_nodes)];
+    const int64_t e = ((int64_t)blockIdx.x - h.b_nodes) * kNodesThreads + threadIdx.x;
+    hm_nodes(h.Lp, h.nbins, h.LM, h.step, h.delta, h.lmax, h.nodes, reinterpret_cast<double*>(scratch + h.s_Jn), e);
+}
+
+__global__ void __launch_bounds__(32) hm_moments_jobs(const HarmJob* __restrict__ J, int n,
+                                                      char* __restrict__ scratch) {
+    const int64_t b = blockIdx.x;
+    const int js = set_of(J, n, b, &HarmJob::b_mom);
+    const HarmJob& h = J[js >> 1];
+    const int k = js & 1;
+    const int64_t local = b - h.b_mom[k];
+    const int nu = h.n_units[k];
+    hm_moments(h.pts[k], h.units[k], h.K, (float)h.delta, h.lmb, h.cr, h.nmm,
+               reinterpret_cast<float2*>(scratch + h.s_MP[k]), (int)(local % nu), (int)(local / nu));
+}
+
+__global__ void __launch_bounds__(kFitThreads) hm_fit_groups(const HarmJob* __restrict__ J, int n, int64_t fit_blocks,
+                                                             char* __restrict__ scratch) {
+    const int64_t blk = blockIdx.x;
+    if (blk < fit_blocks) {
+        const HarmJob& h = J[job_of(J, n, blk, &HarmJob::b_fit)];
+        const int64_t e = (blk - h.b_fit) * kFitThreads + threadIdx.x;
+        hm_fit(h.Lp, h.nbins, h.LM, h.lmax, h.vinv, reinterpret_cast<const double*>(scratch + h.s_Jn),
+               reinterpret_cast<float*>(scratch + h.s_T), e);
+        return;
+    }
+    const int64_t b = blk - fit_blocks;
+    const int js = set_of(J, n, b, &HarmJob::b_grp);
+    const HarmJob& h = J[js >> 1];
+    const int k = js & 1;
+    const int64_t e = (b - h.b_grp[k]) * kFitThreads + threadIdx.x;
+    hm_groups(reinterpret_cast<const float2*>(scratch + h.s_MP[k]), h.gu[k], h.groups[k], h.lmb, h.G[k], h.K,
+              reinterpret_cast<float2*>(scratch + h.s_M[k]), e);
+}
+
+__global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract_jobs(const HarmJob* __restrict__ J, int n,
+                                                                               char* __restrict__ scratch) {
+    const int js = set_of(J, n, blockIdx.x, &HarmJob::b_con);
+    const HarmJob& h = J[js >> 1];
+    const int k = js & 1;
+    const int64_t local = (int64_t)blockIdx.x - h.b_con[k];
+    const int gx = (h.K + kContractK - 1) / kContractK;
+    hm_contract(reinterpret_cast<const float2*>(scratch + h.s_M[k]), h.groups[k], h.G[k],
+                reinterpret_cast<const float*>(scratch + h.s_T), h.nbins, h.LM, h.K, h.Lp, h.lmax, h.lmb, h.aff,
+                reinterpret_cast<float2*>(scratch + h.s_C[k]), (int)(local % gx), (int)(local / gx));
+}
+
+__global__ void __launch_bounds__(kSynthThreads) hm_synth_jobs(const HarmJob* __restrict__ J, int n,
+                                                               char* __restrict__ scratch, char* __restrict__ grid) {
+    const HarmJob& h = J[job_of(J, n, blockIdx.x, &HarmJob::b_syn)];
+    const int64_t local = (int64_t)blockIdx.x - h.b_syn;
+    const int gx = synth_groups(h.Lp);
+    hm_synth(h.Lp, reinterpret_cast<const float2*>(scratch + h.s_C[0]),
+             h.vox ? reinterpret_cast<const float2*>(scratch + h.s_C[1]) : nullptr, h.K, h.lmax, h.ab, h.nmm, h.step,
+             h.vox_s, h.cx, h.cy, h.cz, h.use_center, h.scale, h.origin,
+             h.grid_ptr ? h.grid_ptr : reinterpret_cast<float4*>(grid + h.grid_off), (int)(local % gx),
+             (int)(local / gx));
+}
+
 }  // namespace
 
 int harmonic_max_l() { return kMaxL - 17; }
@@ -1093,50 +1183,12 @@ cudaError_t harmonic_reserve_smem(int Lp, int LM) {
     std::lock_guard<std::mutex> lock(g_smem_mu);
     for (int k = 0; k < 2; ++k) {
         if (need[k] <= 48 * 1024 || need[k] <= g_smem_set[k][dev]) continue;
-        e = k == 0 ? cudaFuncSetAttribute(hm_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k])
-                   : cudaFuncSetAttribute(hm_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k]);
+        e = k == 0 ? cudaFuncSetAttribute(hm_moments_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k])
+                   : cudaFuncSetAttribute(hm_synth_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k]);
         if (e != cudaSuccess) return e;
         g_smem_set[k][dev] = need[k];
     }
     return cudaSuccess;
-}
-
-cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a) {
-    const int64_t nn = (int64_t)a.Lp * a.nbins * kNodes;
-    hm_nodes<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(a.Lp, a.nbins, a.LM, a.step, a.delta, a.lmax, a.nodes, a.Jn);
-    const int64_t nf = (int64_t)a.Lp * a.nbins * (a.LM + 1);
-    hm_fit<<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(a.Lp, a.nbins, a.LM, a.lmax, a.vinv, a.Jn, a.T);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C) {
-    // one warp per (unit, quartet pair); the running sums of both quartets.  A
-    // unit of order L (its bin's, <= LM) holds (L - 4y + 1) + (L - 4(Q-1-y) + 1)
-    // = 2L + 6 - 4Q = L + 2 + (L mod 4) orders for a pair, L + 1 for the single
-    // quartet of Q = 1: at most LM + 5 whatever L.
-    const int Q = (a.LM + 4) / 4;
-    const int pairs = (Q + 1) / 2;
-    const size_t smem = moments_smem(a.LM);  // the limit is raised by harmonic_reserve_smem
-    if (a.ev0) {
-        cudaError_t e = cudaEventRecord(a.ev0, s);
-        if (e != cudaSuccess) return e;
-    }
-    hm_moments<<<dim3(a.n_units, pairs), 32, smem, s>>>(a.pts, a.units, a.K, (float)a.delta, a.lmb, a.cr, a.nmm,
-                                                       a.MP);
-    if (a.ev1) {
-        cudaError_t e = cudaEventRecord(a.ev1, s);
-        if (e != cudaSuccess) return e;
-    }
-    const int64_t ng = (int64_t)a.G * kNodes * a.K;
-    hm_groups<<<(unsigned)((ng + 255) / 256), 256, 0, s>>>(a.MP, a.gu, a.groups, a.lmb, a.G, a.K, a.M);
-    if (a.contract_wait) {
-        cudaError_t e = cudaStreamWaitEvent(s, a.contract_wait, 0);
-        if (e != cudaSuccess) return e;
-    }
-    hm_contract<<<dim3((a.K + kContractK - 1) / kContractK, (a.Lp + kContractShells - 1) / kContractShells),
-                  kContractK * kContractWarps, 0, s>>>(
-        a.M, a.groups, a.G, a.T, a.nbins, a.LM, a.K, a.Lp, a.lmax, a.lmb, a.aff, C);
-    return cudaGetLastError();
 }
 
 int harmonic_max_bins() { return kMaxBins; }
@@ -1164,14 +1216,58 @@ cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a) {
-    // one launch: blocks (row group, shell), dynamic shared memory sized for the outermost shell
-    const size_t smem = synth_smem(a.Lp, a.lmax_host_outer);  // the limit is raised by harmonic_reserve_smem
-    const int groups = (3 * a.Lp / 2 + 1 + kSynthRows - 1) / kSynthRows;
-    hm_synth<<<dim3(groups, a.Lp), kSynthThreads, smem, s>>>(a.Lp, a.Ca, a.Cv, a.K, a.lmax, a.ab, a.nmm, a.step,
-                                                             a.vox_s, a.cx, a.cy, a.cz, a.use_center, a.scale,
-                                                             a.origin, a.grid);
-    return cudaGetLastError();
+
+HarmShape plan_harmonic_jobs(HarmJob* J, int n) {
+    HarmShape sh{};
+    for (int j = 0; j < n; ++j) {
+        HarmJob& h = J[j];
+        const int pairs = ((h.LM + 4) / 4 + 1) / 2;
+        const int64_t gx = (h.K + kContractK - 1) / kContractK, gy = (h.Lp + kContractShells - 1) / kContractShells;
+        h.b_nodes = sh.nodes;
+        sh.nodes += ((int64_t)h.Lp * h.nbins * kNodes + kNodesThreads - 1) / kNodesThreads;
+        h.b_fit = sh.fit;
+        sh.fit += ((int64_t)h.Lp * h.nbins * (h.LM + 1) + kFitThreads - 1) / kFitThreads;
+        for (int k = 0; k < 2; ++k) {
+            h.b_mom[k] = sh.moments;
+            sh.moments += (int64_t)h.n_units[k] * pairs;
+            h.b_grp[k] = sh.groups;
+            sh.groups += ((int64_t)h.G[k] * kNodes * h.K + kFitThreads - 1) / kFitThreads;
+            h.b_con[k] = sh.contract;
+            if (k == 0 || h.vox) sh.contract += gx * gy;  // the coefficient sets the synthesis reads
+        }
+        h.b_syn = sh.synth;
+        sh.synth += (int64_t)((3 * h.Lp / 2 + 1 + kSynthRows - 1) / kSynthRows) * h.Lp;
+        sh.maxLp = std::max(sh.maxLp, h.Lp);
+        sh.maxLM = std::max(sh.maxLM, h.LM);
+    }
+    return sh;
+}
+
+int harmonic_launches_per_batch() { return 5; }
+
+cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, const HarmShape& sh, char* scratch,
+                                 char* grid, cudaEvent_t* ev) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t b = sh.fit + sh.groups;
+    if (sh.nodes > 0x7fffffff || sh.moments > 0x7fffffff || b > 0x7fffffff || sh.contract > 0x7fffffff ||
+        sh.synth > 0x7fffffff)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaSuccess;
+    if (sh.nodes > 0) hm_nodes_jobs<<<(unsigned)sh.nodes, kNodesThreads, 0, s>>>(d_jobs, n, scratch);
+    // the limits were raised by harmonic_reserve_smem when the jobs were planned
+    if (ev && ev[0]) e = cudaEventRecord(ev[0], s);
+    if (e == cudaSuccess && sh.moments > 0)
+        hm_moments_jobs<<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
+    if (e == cudaSuccess && ev && ev[1]) e = cudaEventRecord(ev[1], s);
+    if (e == cudaSuccess && b > 0) hm_fit_groups<<<(unsigned)b, kFitThreads, 0, s>>>(d_jobs, n, sh.fit, scratch);
+    if (e == cudaSuccess && sh.contract > 0)
+        hm_contract_jobs<<<(unsigned)sh.contract, kContractK * kContractWarps, 0, s>>>(d_jobs, n, scratch);
+    if (e == cudaSuccess && ev && ev[2]) e = cudaEventRecord(ev[2], s);
+    if (e == cudaSuccess && sh.synth > 0)
+        hm_synth_jobs<<<(unsigned)sh.synth, kSynthThreads, synth_smem(sh.maxLp, sh.maxLM), s>>>(d_jobs, n, scratch,
+                                                                                                grid);
+    if (e == cudaSuccess && ev && ev[3]) e = cudaEventRecord(ev[3], s);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace dpx

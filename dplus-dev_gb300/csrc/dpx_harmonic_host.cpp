@@ -280,7 +280,8 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
     p.o_groups[1] = al16(p.o_units[1] + vox_units_max * sizeof(int4));
     p.o_gu[1] = al16(p.o_groups[1] + (size_t)nbins * sizeof(int2));
     p.o_pts[1] = al16(p.o_gu[1] + (size_t)(nbins + 1) * sizeof(int));
-    p.arena_bytes = (nv ? al16(p.o_pts[1] + (size_t)nv * sizeof(float4)) : staged) + 16;
+    p.o_job = al16(nv ? p.o_pts[1] + (size_t)nv * sizeof(float4) : staged);
+    p.arena_bytes = p.o_job + sizeof(dpx::HarmJob) + 16;
     DPX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p.arena), p.arena_bytes, st));
     DPX_CUDA(cudaMemcpyAsync(p.arena, h.data(), staged, cudaMemcpyHostToDevice, st));
     // ---- the voxels: expanded and sorted by bin on the device, units from the totals ----
@@ -376,6 +377,10 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
     p.s_C[0] = take(cell_set);
     p.s_C[1] = take(nv ? cell_set : 0);
     p.scratch_bytes = o + 256;
+    // the plan's own job: its scratch and grid at the launch's bases
+    dpx::HarmJob job = harmonic_job(p, 0, 0);
+    p.shape = dpx::plan_harmonic_jobs(&job, 1);
+    DPX_CUDA(cudaMemcpyAsync(p.arena + p.o_job, &job, sizeof job, cudaMemcpyHostToDevice, st));
     // the pageable staging above must stay valid until its copy is done
     DPX_CUDA(cudaStreamSynchronize(st));
     return DPX_OK;
@@ -387,116 +392,62 @@ void harmonic_plan_release(HarmPlan& p) {
     p.arena_bytes = 0;
 }
 
-int harmonic_launch(const HarmStreams& S, const HarmPlan& p, void* scratch_v, float4* grid) {
+dpx::HarmJob harmonic_job(const HarmPlan& p, size_t scratch_off, size_t grid_off) {
+    const char* base = p.arena;
+    dpx::HarmJob J{};
+    J.Lp = p.G.Lp;
+    J.nbins = p.nbins;
+    J.LM = p.LM;
+    J.K = p.K;
+    J.step = p.G.step;
+    J.delta = p.delta;
+    J.lmax = reinterpret_cast<const int*>(base + p.o_lmax);
+    J.lmb = reinterpret_cast<const int*>(base + p.o_lmb);
+    J.nodes = reinterpret_cast<const double*>(base + p.o_nodes);
+    J.vinv = reinterpret_cast<const double*>(base + p.o_vinv);
+    J.ab = reinterpret_cast<const float2*>(base + p.o_ab);
+    J.cr = reinterpret_cast<const float2*>(base + p.o_cr);
+    J.nmm = reinterpret_cast<const float*>(base + p.o_nmm);
+    J.aff = reinterpret_cast<const float*>(base + p.o_aff);
+    for (int k = 0; k < 2; ++k) {
+        J.pts[k] = reinterpret_cast<const float4*>(base + p.o_pts[k]);
+        J.units[k] = reinterpret_cast<const int4*>(base + p.o_units[k]);
+        J.groups[k] = reinterpret_cast<const int2*>(base + p.o_groups[k]);
+        J.gu[k] = reinterpret_cast<const int*>(base + p.o_gu[k]);
+        J.n_units[k] = p.n_units[k];
+        J.G[k] = p.n_groups[k];
+        J.s_MP[k] = scratch_off + p.s_MP[k];
+        J.s_M[k] = scratch_off + p.s_M[k];
+        J.s_C[k] = scratch_off + p.s_C[k];
+    }
+    J.vox = p.n_vox > 0;
+    J.use_center = (p.cen[0] != 0.0 || p.cen[1] != 0.0 || p.cen[2] != 0.0);
+    J.vox_s = p.vox_s;
+    J.scale = p.scale;
+    J.cx = p.cen[0];
+    J.cy = p.cen[1];
+    J.cz = p.cen[2];
+    J.origin = p.origin;
+    J.s_Jn = scratch_off + p.s_Jn;
+    J.s_T = scratch_off + p.s_T;
+    J.grid_off = grid_off;
+    return J;
+}
+
+int harmonic_launch(const HarmStreams& S, const HarmPlan& p, void* scratch, float4* grid) {
     if (!p.arena) return fail(DPX_ERR_ARG, "harmonic fill: no plan");
-    char* base = p.arena;
-    char* scratch = static_cast<char*>(scratch_v);
-    const int Lp = p.G.Lp;
-    cudaStream_t st = S.st;
-    const bool side = S.ax && S.ax != st;
-    cudaStream_t ax = side ? S.ax : st;
-    cudaEvent_t* ev = S.tev;  // [0, 1] atoms' moments, [2, 3] voxels' moments, [4, 5] synthesis, [6, 7] fill
-    if (ev) DPX_CUDA(cudaEventRecord(ev[6], st));
-    const size_t cell_set = (size_t)(Lp + 1) * p.K * sizeof(float2);
-    float2* C[2] = {reinterpret_cast<float2*>(scratch + p.s_C[0]),
-                    p.n_vox ? reinterpret_cast<float2*>(scratch + p.s_C[1]) : nullptr};
-    DPX_CUDA(cudaMemsetAsync(C[0], 0, cell_set, st));
-    if (C[1]) DPX_CUDA(cudaMemsetAsync(C[1], 0, cell_set, st));
-    const int* d_lmax = reinterpret_cast<const int*>(base + p.o_lmax);
-    dpx::HarmonicTables tb{};
-    tb.Lp = Lp;
-    tb.nbins = p.nbins;
-    tb.LM = p.LM;
-    tb.step = p.G.step;
-    tb.delta = p.delta;
-    tb.lmax = d_lmax;
-    tb.nodes = reinterpret_cast<const double*>(base + p.o_nodes);
-    tb.vinv = reinterpret_cast<const double*>(base + p.o_vinv);
-    tb.Jn = reinterpret_cast<double*>(scratch + p.s_Jn);
-    tb.T = reinterpret_cast<float*>(scratch + p.s_T);
-    // with a side stream: the radial tables, then the atoms' set, run beside the
-    // voxels' moments (the voxels' contractions wait for the tables, the
-    // synthesis for the atoms)
-    if (side) {
-        DPX_CUDA(cudaEventRecord(S.go, st));
-        DPX_CUDA(cudaStreamWaitEvent(ax, S.go, 0));
-    }
-    struct Join {  // every return after the fork joins the side stream back into st
-        cudaStream_t st, ax;
-        cudaEvent_t ev;
-        bool on;
-        ~Join() {
-            if (on && cudaEventRecord(ev, ax) == cudaSuccess) cudaStreamWaitEvent(st, ev, 0);
-        }
-    } join{st, ax, S.atoms, side};
-    DPX_CUDA(dpx::launch_harmonic_tables(ax, tb));
-    if (side) DPX_CUDA(cudaEventRecord(S.tables, ax));
-    for (int k : {1, 0}) {
-        if (p.n_units[k] == 0) continue;
-        dpx::HarmonicSet a{};
-        a.pts = reinterpret_cast<const float4*>(base + p.o_pts[k]);
-        a.units = reinterpret_cast<const int4*>(base + p.o_units[k]);
-        a.n_units = p.n_units[k];
-        a.groups = reinterpret_cast<const int2*>(base + p.o_groups[k]);
-        a.gu = reinterpret_cast<const int*>(base + p.o_gu[k]);
-        a.G = p.n_groups[k];
-        a.LM = p.LM;
-        a.K = p.K;
-        a.Lp = Lp;
-        a.nbins = p.nbins;
-        a.delta = p.delta;
-        a.ab = reinterpret_cast<const float2*>(base + p.o_ab);
-        a.cr = reinterpret_cast<const float2*>(base + p.o_cr);
-        a.nmm = reinterpret_cast<const float*>(base + p.o_nmm);
-        a.T = tb.T;
-        a.lmax = d_lmax;
-        a.lmb = reinterpret_cast<const int*>(base + p.o_lmb);
-        a.aff = reinterpret_cast<const float*>(base + p.o_aff);
-        a.MP = reinterpret_cast<float2*>(scratch + p.s_MP[k]);
-        a.M = reinterpret_cast<float2*>(scratch + p.s_M[k]);
-        a.ev0 = ev ? ev[2 * k] : nullptr;
-        a.ev1 = ev ? ev[2 * k + 1] : nullptr;
-        // the voxels run on st and wait for the tables by event; the atoms follow
-        // the tables on their stream
-        a.contract_wait = (k == 1 && side) ? S.tables : nullptr;
-        DPX_CUDA(dpx::launch_harmonic_set(k == 0 ? ax : st, a, C[k]));
-    }
-    if (side) {
-        DPX_CUDA(cudaEventRecord(S.atoms, ax));
-        DPX_CUDA(cudaStreamWaitEvent(st, S.atoms, 0));
-        join.on = false;
-    }
-    dpx::HarmonicSynth y{};
-    y.Ca = C[0];
-    y.Cv = C[1];
-    y.K = p.K;
-    y.Lp = Lp;
-    y.lmax_host_outer = p.LM;
-    y.lmax = d_lmax;
-    y.ab = reinterpret_cast<const float2*>(base + p.o_ab);
-    y.nmm = reinterpret_cast<const float*>(base + p.o_nmm);
-    y.step = p.G.step;
-    y.vox_s = p.vox_s;
-    y.cx = p.cen[0];
-    y.cy = p.cen[1];
-    y.cz = p.cen[2];
-    y.use_center = (p.cen[0] != 0.0 || p.cen[1] != 0.0 || p.cen[2] != 0.0);
-    y.scale = p.scale;
-    y.origin = p.origin;
-    y.grid = grid;
-    if (ev) DPX_CUDA(cudaEventRecord(ev[4], st));
-    DPX_CUDA(dpx::launch_harmonic_synth(st, y));
-    if (ev) {
-        DPX_CUDA(cudaEventRecord(ev[5], st));
-        DPX_CUDA(cudaEventRecord(ev[7], st));
-    }
+    cudaEvent_t* ev = S.tev;  // [0, 1] moments, [4, 5] synthesis, [6, 7] the whole fill
+    cudaEvent_t stage[4] = {ev ? ev[0] : nullptr, ev ? ev[1] : nullptr, ev ? ev[4] : nullptr, ev ? ev[5] : nullptr};
+    if (ev) DPX_CUDA(cudaEventRecord(ev[6], S.st));
+    DPX_CUDA(dpx::launch_harmonic_jobs(S.st, reinterpret_cast<const dpx::HarmJob*>(p.arena + p.o_job), 1, p.shape,
+                                       static_cast<char*>(scratch), reinterpret_cast<char*>(grid), stage));
+    if (ev) DPX_CUDA(cudaEventRecord(ev[7], S.st));
     return DPX_OK;
 }
 
 int harmonic_launches(const HarmPlan& p) {
-    // the radial tables (2), moments + group sums + contraction per point set
-    // (3 each), the synthesis (1); the coefficient sets' memsets are not kernels
-    return 2 + 3 * ((p.n_units[0] > 0) + (p.n_units[1] > 0)) + 1;
+    const dpx::HarmShape& h = p.shape;
+    return (h.nodes > 0) + (h.moments > 0) + (h.fit + h.groups > 0) + (h.contract > 0) + (h.synth > 0);
 }
 
 }  // namespace dpxh

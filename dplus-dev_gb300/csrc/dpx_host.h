@@ -97,11 +97,6 @@ struct dpx_ctx_s {
     bool closed = false;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
-    // the harmonic fill's radial tables and atoms' set run on aux beside the
-    // voxels' moments: aux waits for aux_go (the plan's upload), the voxels'
-    // contractions for aux_done (the tables), the synthesis for aux_atoms
-    cudaStream_t aux = nullptr;
-    cudaEvent_t aux_go = nullptr, aux_done = nullptr, aux_atoms = nullptr;
     int fill_cpt = 8, fill_threads = 128;  // FP32 fill shape (dpx_autotune_fill)
     bool fill_persistent = false;
     int fill_poly = 0;  // phi columns per work item whose sincos run on the FMA pipe
@@ -227,13 +222,12 @@ struct HarmPlan {
     // scratch of a launch (offsets from the caller's scratch, 256-byte aligned)
     size_t s_Jn = 0, s_T = 0, s_MP[2] = {0, 0}, s_M[2] = {0, 0}, s_C[2] = {0, 0};
     size_t scratch_bytes = 0;
+    size_t o_job = 0;       // the plan's own job (scratch and grid at offset 0) in the arena
+    dpx::HarmShape shape{};  // its launch layout
 };
-// Streams of a launch: ax (may be null or st) runs the radial tables and the
-// atoms' set beside the voxels' moments on st, forked and joined by the events
-// go, tables and atoms; tev (null: no timing) receives the stage events.
+// The stream of a launch; tev (null: no timing) receives the stage events.
 struct HarmStreams {
-    cudaStream_t st = nullptr, ax = nullptr;
-    cudaEvent_t go = nullptr, tables = nullptr, atoms = nullptr;
+    cudaStream_t st = nullptr;
     cudaEvent_t* tev = nullptr;
 };
 int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, HarmPlan& p);
@@ -242,10 +236,13 @@ void harmonic_plan_release(HarmPlan& p);
 int harmonic_launch(const HarmStreams& S, const HarmPlan& p, void* scratch, float4* grid);
 // Kernel launches of one harmonic_launch.
 int harmonic_launches(const HarmPlan& p);
-// The context's streams for a harmonic launch: its stream, its side stream and
-// fork/join events (created on first use, so call it outside stream capture),
-// and the stage-timing events when timing is on; ctx_stage_record keeps the
-// plan's figures for dpx_ctx_stage_times.
+// The device job of a plan with its scratch at scratch_off from a launch's
+// scratch base and its grid at grid_off from the launch's grid base (the
+// block layout is set by dpx::plan_harmonic_jobs over the job table).
+dpx::HarmJob harmonic_job(const HarmPlan& p, size_t scratch_off, size_t grid_off);
+// The context's stream for a harmonic launch and the stage-timing events when
+// timing is on (created on first use, so call it outside stream capture);
+// ctx_stage_record keeps the plan's figures for dpx_ctx_stage_times.
 int ctx_harmonic_streams(dpx_ctx ctx, HarmStreams& S);
 void ctx_stage_record(dpx_ctx ctx, const HarmPlan& p);
 // The FP64 fill launch of a staged leaf.

@@ -180,51 +180,51 @@ cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);
 // Harmonic (multipole) FP32 fill of one leaf (dpx_harmonic.cu).  Points are
 // float4 (x, y, z nm about the centre, weight), sorted by group (radial bin,
 // and ion for atoms); a unit is <= 1024 points of one group.
-struct HarmonicTables {
-    int Lp, nbins, LM;
-    double step, delta;     // q step, bin width (nm)
-    const int* lmax;        // [Lp+1] l_i
-    const double* nodes;    // [6] Chebyshev nodes on [-1, 1]
-    const double* vinv;     // [6][6] inverse Vandermonde of the nodes
-    double* Jn;             // [Lp+1][nbins][6][LM+1] scratch
-    float* T;               // [Lp+1][nbins][LM+1][8] polynomial coefficients
-};
-struct HarmonicSet {
-    const float4* pts;
-    const int4* units;      // {first point, count, bin, 0}
-    int n_units;
-    const int2* groups;     // {bin, ion or -1}
-    const int* gu;          // [G+1] first unit of each group
-    int G;
-    int LM, K, Lp, nbins;
-    double delta;
-    const float2* ab;       // [K] Legendre recurrence coefficients
-    const float2* cr;       // [K] scaled recurrence: {c_lm, r_lm} (hm_moments)
-    const float* nmm;       // [LM+1] Pbar_mm = nmm[m] (-sin theta)^m
-    const float* T;
-    const int* lmax;
-    const int* lmb;         // [nbins] the orders a bin needs (<= LM)
-    const float* aff;       // [U][Lp+1] ion form factors (atoms)
-    float2* MP;             // [n_units][6][K]
-    float2* M;              // [G][6][K]
-    cudaEvent_t ev0, ev1;   // recorded around the moments launch when not null
-    cudaEvent_t contract_wait;  // the radial tables' completion, waited on before hm_contract when not null
-};
-struct HarmonicSynth {
-    const float2* Ca;       // [Lp+1][K] atoms
-    const float2* Cv;       // [Lp+1][K] voxels or nullptr
-    int K, Lp, lmax_host_outer;
-    const int* lmax;
-    const float2* ab;
-    const float* nmm;
-    double step;
-    float vox_s;            // voxel edge (nm)
-    double cx, cy, cz;
+// One structure's harmonic fill in the batched launches (launch_harmonic_jobs).
+// Table pointers are absolute (the structure's plan arena); scratch and grid
+// are byte offsets from the launch's scratch and grid bases, so one table
+// serves any scratch and grid.  Set 0: atoms, set 1: solvent voxels.
+struct HarmJob {
+    int Lp, nbins, LM, K;
+    double step, delta;        // q step, radial bin width (nm)
+    const int* lmax;           // [Lp+1] l_i
+    const int* lmb;            // [nbins] the orders a bin needs (<= LM)
+    const double* nodes;       // [6] Chebyshev nodes on [-1, 1]
+    const double* vinv;        // [6][6] inverse Vandermonde of the nodes
+    const float2* ab;          // [K] Legendre recurrence coefficients
+    const float2* cr;          // [K] scaled recurrence {c_lm, r_lm} (moments)
+    const float* nmm;          // [LM+1] Pbar_mm = nmm[m] (-sin theta)^m
+    const float* aff;          // [U][Lp+1] ion form factors (atoms)
+    const float4* pts[2];
+    const int4* units[2];      // {first point, count, bin, 0}
+    const int2* groups[2];     // {bin, ion or -1}
+    const int* gu[2];          // [G+1] first unit of each group
+    int n_units[2], G[2];
+    int vox;                   // the voxel set exists
     int use_center;
-    float scale;
-    double origin;
-    float4* grid;
+    float vox_s, scale;        // voxel edge (nm), scale
+    double cx, cy, cz;         // the centring translation restored per cell
+    double origin;             // F(0)
+    size_t s_Jn, s_T, s_MP[2], s_M[2], s_C[2];  // scratch offsets (bytes)
+    size_t grid_off;           // grid offset (bytes)
+    float4* grid_ptr;          // the grid itself when not null (grid_off unused)
+    // the job's first blocks in each launch (plan_harmonic_jobs)
+    int64_t b_nodes, b_mom[2], b_fit, b_grp[2], b_con[2], b_syn;
 };
+// Blocks of the launches and the largest shell count and order (shared
+// memory) of a job table.
+struct HarmShape {
+    int64_t nodes, moments, fit, groups, contract, synth;
+    int maxLp, maxLM;
+};
+// Host: the block layout of n jobs (sets their b_* fields).
+HarmShape plan_harmonic_jobs(HarmJob* jobs, int n);
+// The harmonic fills of n jobs in five launches: radial nodes, moments, radial
+// fit + group sums, contraction, synthesis.  ev[0..1] (when not null) are
+// recorded around the moments, ev[2..3] around the synthesis.
+cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, const HarmShape& sh, char* scratch,
+                                 char* grid, cudaEvent_t* ev);
+int harmonic_launches_per_batch();
 int harmonic_max_l();
 int harmonic_nodes();
 int harmonic_max_bins();
@@ -269,10 +269,6 @@ cudaError_t harmonic_reserve_smem(int Lp, int LM);
 // mma.sync m16n8k8 TF32 (256 threads a block, iters steps of 8 / 8 / 4
 // independent operations per thread or warp).
 cudaError_t launch_pipe_probe(cudaStream_t s, int kind, int blocks, int iters, float* out);
-cudaError_t launch_harmonic_tables(cudaStream_t s, const HarmonicTables& a);
-// C [Lp+1][K] (FP64) = the expansion coefficients of one point set.
-cudaError_t launch_harmonic_set(cudaStream_t s, const HarmonicSet& a, float2* C);
-cudaError_t launch_harmonic_synth(cudaStream_t s, const HarmonicSynth& a);
 
 // Debye sum of one leaf (dpx_debye.cu).  Atoms padded to a multiple of the
 // 128-atom tile; F tables [nq][npad] of the path's type; partial sums

@@ -72,7 +72,7 @@ int dpx_leaf_create(dpx_grid g, const dpx_pdb_desc* d, dpx_leaf* out) {
     }
     int rc = DPX_OK;
     if (L->harmonic) {
-        HarmStreams hs;  // creates the context's side stream and events now, outside any capture
+        HarmStreams hs;  // creates the timing events now, outside any capture
         rc = ctx_harmonic_streams(ctx, hs);
         cudaError_t e = rc ? cudaSuccess : cudaMalloc(&L->scratch, L->plan.scratch_bytes);
         if (e != cudaSuccess) {
@@ -124,7 +124,7 @@ int dpx_leaf_fill(dpx_leaf L) {
     dpx_grid g = L->grid;
     g->splines_current = false;
     if (L->harmonic) {
-        HarmStreams hs;  // the radial tables and the atoms' set on the side stream, forked and joined by events
+        HarmStreams hs;
         if (int rc = ctx_harmonic_streams(ctx, hs)) return rc;
         if (int rc = harmonic_launch(hs, L->plan, L->scratch, reinterpret_cast<float4*>(g->cells))) return rc;
         ctx_stage_record(ctx, L->plan);

@@ -400,6 +400,20 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
         tiles += (lt[j].items + threads - 1) / threads;
     }
     if (!jobs.empty()) std::memcpy(h.data() + jobs_at, jobs.data(), jobs.size() * sizeof(dpx::FillJob));
+    // the harmonic fills' job table: one scratch block, each fill its own part
+    std::vector<dpx::HarmJob> hj;
+    size_t hscratch = 0;
+    for (size_t j = 0; j < fresh.size(); ++j) {
+        if (!harm[j]) continue;
+        dpx::HarmJob J = harmonic_job(plans[j], hscratch, 0);
+        J.grid_ptr = reinterpret_cast<float4*>(fresh[j]->cells);
+        hj.push_back(J);
+        hscratch += (plans[j].scratch_bytes + 255) & ~size_t(255);
+    }
+    const dpx::HarmShape hshape = dpx::plan_harmonic_jobs(hj.data(), (int)hj.size());
+    const size_t hjobs_at = al16(h.size());
+    h.resize(hjobs_at + hj.size() * sizeof(dpx::HarmJob));
+    if (!hj.empty()) std::memcpy(h.data() + hjobs_at, hj.data(), hj.size() * sizeof(dpx::HarmJob));
     size_t cap = 0;
     void* hp = S->pinned.get(h.size(), &cap);
     if (!hp) return fail(DPX_ERR_OOM, "pinned staging");
@@ -419,18 +433,17 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
         if (e != cudaSuccess) return cuda_fail(e, "fill launch");
         dl.fill_launches++;
     }
-    DPX_CUDA(cudaFreeAsync(d, s));
-    for (size_t j = 0; j < fresh.size(); ++j) {  // harmonic fills, one scratch each, in stream order
-        if (!harm[j]) continue;
-        void* scratch = nullptr;
-        DPX_CUDA(cudaMallocAsync(&scratch, plans[j].scratch_bytes, s));
-        HarmStreams hs;
-        hs.st = s;
-        const int rc = harmonic_launch(hs, plans[j], scratch, reinterpret_cast<float4*>(fresh[j]->cells));
+    if (!hj.empty()) {  // the harmonic fills: five launches over their job table
+        char* scratch = nullptr;
+        DPX_CUDA(cudaMallocAsync((void**)&scratch, hscratch, s));
+        e = dpx::launch_harmonic_jobs(s, reinterpret_cast<const dpx::HarmJob*>(d + hjobs_at), (int)hj.size(), hshape,
+                                      scratch, nullptr, nullptr);
         cudaFreeAsync(scratch, s);
-        if (rc) return rc;
-        dl.fill_launches += harmonic_launches(plans[j]);
+        if (e != cudaSuccess) return cuda_fail(e, "harmonic fill launch");
+        dl.fill_launches += (hshape.nodes > 0) + (hshape.moments > 0) + (hshape.fit + hshape.groups > 0) +
+                            (hshape.contract > 0) + (hshape.synth > 0);
     }
+    DPX_CUDA(cudaFreeAsync(d, s));
     for (size_t j = 0; j < fresh.size(); ++j) {
         GridEntry* g = fresh[j];
         e = harm[j] ? cudaSuccess  // the harmonic synthesis writes the phi-spline derivatives
