@@ -844,8 +844,10 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
     const int nG = synth_pad(li);
     const int m0p = -6 * ((li + 5) / 6);
     const bool vox = Cv != nullptr;
-    float2* sG = reinterpret_cast<float2*>(smem);      // [row][2][nG]
-    float2* sW = sG + (size_t)kSynthRows * 2 * nG;     // [6i]
+    // G per row: [set (atoms, voxels)][component (re, im)][nG] floats, so that
+    // two neighbouring orders of one component load as one f32x2 pair
+    float* sG = reinterpret_cast<float*>(smem);
+    float2* sW = reinterpret_cast<float2*>(sG + (size_t)kSynthRows * 4 * nG);  // [6i]
     float2* sF = sW + nph;                              // [6 max(256, Lp)]
     const int tid = threadIdx.x;
     for (int n = tid; n < nph; n += blockDim.x) {
@@ -853,9 +855,9 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
         sincospif(2.f * (float)n / (float)nph, &sw, &cw);
         sW[n] = make_float2(cw, sw);
     }
-    for (int e = tid; e < nr * 2 * nG; e += blockDim.x) {  // the padding beyond |m| <= l_i
+    for (int e = tid; e < nr * 4 * nG; e += blockDim.x) {  // the padding beyond |m| <= l_i
         const int m = m0p + e % nG;
-        if (m > li || m < -li) sG[e] = make_float2(0.f, 0.f);
+        if (m > li || m < -li) sG[e] = 0.f;
     }
     const float qI = (float)((double)i * step);
     if (tid < nr) {
@@ -925,12 +927,20 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
                 }
             }
             if (ok) {
-                float2* g = sG + (size_t)r * 2 * nG;
-                g[m - m0p] = make_float2(kFourPi * br, kFourPi * bi);
-                if (m > 0) g[-m - m0p] = make_float2(kFourPi * pr, kFourPi * pi_);
+                float* g = sG + (size_t)r * 4 * nG;
+                g[m - m0p] = kFourPi * br;
+                g[nG + m - m0p] = kFourPi * bi;
+                if (m > 0) {
+                    g[-m - m0p] = kFourPi * pr;
+                    g[nG - m - m0p] = kFourPi * pi_;
+                }
                 if (vox) {
-                    g[nG + m - m0p] = make_float2(kFourPi * vr, kFourPi * vi);
-                    if (m > 0) g[nG - m - m0p] = make_float2(kFourPi * qr, kFourPi * qi);
+                    g[2 * nG + m - m0p] = kFourPi * vr;
+                    g[3 * nG + m - m0p] = kFourPi * vi;
+                    if (m > 0) {
+                        g[2 * nG - m - m0p] = kFourPi * qr;
+                        g[3 * nG - m - m0p] = kFourPi * qi;
+                    }
                 }
             }
         }
@@ -947,33 +957,50 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
         for (int it = tid; it < nrp * i; it += blockDim.x) {
             const int rr = it / i, j = it - rr * i;
             const int r = r0 + rr;
-            const float2* gA = sG + (size_t)r * 2 * nG;
-            const float2* gV = gA + nG;
+            const float* gx = sG + (size_t)r * 4 * nG;  // atoms re, im; voxels re, im
             float2 D[6], Dv[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) D[c] = Dv[c] = make_float2(0.f, 0.f);
             // D_c = w^{(m0 + c) j} sum_k G_{m0 + c + 6k} z^k with z = w^{6j}: Horner
-            // over k (no twiddle lookups in the loop), then one twiddle per class
+            // over k (no twiddle lookups in the loop), then one twiddle per class.
+            // Classes in pairs (c, c + 1) as f32x2: X = re, Y = im of both,
+            //   X' = X z.x + (Y (-z.y) + G.re),  Y' = X z.y + (Y z.x + G.im)
+            // (per lane the same FP32 FMAs as the complex Horner step).
             const float2 z = sW[6 * j];
+            const f2x ZX = pk2(z.x, z.x), ZY = pk2(z.y, z.y), NZY = pk2(-z.y, -z.y);
             const int top = nG - 6;
+            auto ld2 = [](const float* p) { return *reinterpret_cast<const f2x*>(p); };
+            f2x XA[3], YA[3], XV[3], YV[3];
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                D[c] = gA[top + c];
-                if (vox) Dv[c] = gV[top + c];
+            for (int q = 0; q < 3; ++q) {
+                XA[q] = ld2(gx + top + 2 * q);
+                YA[q] = ld2(gx + nG + top + 2 * q);
+                XV[q] = YV[q] = 0ull;
+                if (vox) {
+                    XV[q] = ld2(gx + 2 * nG + top + 2 * q);
+                    YV[q] = ld2(gx + 3 * nG + top + 2 * q);
+                }
             }
             for (int u = top - 6; u >= 0; u -= 6) {
 #pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    const float2 g = gA[u + c];
-                    const float2 a = D[c];
-                    D[c].x = fmaf(a.x, z.x, fmaf(-a.y, z.y, g.x));
-                    D[c].y = fmaf(a.x, z.y, fmaf(a.y, z.x, g.y));
+                for (int q = 0; q < 3; ++q) {
+                    const f2x xa = XA[q], ya = YA[q];
+                    XA[q] = fma2(xa, ZX, fma2(ya, NZY, ld2(gx + u + 2 * q)));
+                    YA[q] = fma2(xa, ZY, fma2(ya, ZX, ld2(gx + nG + u + 2 * q)));
                     if (vox) {
-                        const float2 gv = gV[u + c];
-                        const float2 b = Dv[c];
-                        Dv[c].x = fmaf(b.x, z.x, fmaf(-b.y, z.y, gv.x));
-                        Dv[c].y = fmaf(b.x, z.y, fmaf(b.y, z.x, gv.y));
+                        const f2x xv = XV[q], yv = YV[q];
+                        XV[q] = fma2(xv, ZX, fma2(yv, NZY, ld2(gx + 2 * nG + u + 2 * q)));
+                        YV[q] = fma2(xv, ZY, fma2(yv, ZX, ld2(gx + 3 * nG + u + 2 * q)));
                     }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                upk2(XA[q], D[2 * q].x, D[2 * q + 1].x);
+                upk2(YA[q], D[2 * q].y, D[2 * q + 1].y);
+                if (vox) {
+                    upk2(XV[q], Dv[2 * q].x, Dv[2 * q + 1].x);
+                    upk2(YV[q], Dv[2 * q].y, Dv[2 * q + 1].y);
                 }
             }
             int idx = (int)(((int64_t)m0p * j) % nph);

@@ -10,13 +10,15 @@ decoded into this package's model tree, for the scattering path:
   (CompositeModel::CalculateVector, Backend/Backend/CompositeModel.cpp:165-176);
 * model nodes: ``PDB`` (a PDB file: ExtraParameters, Centered, Location),
   ``AMP`` (an amplitude-grid file, ExtraParameters [scale]), ``,26``
-  ManualSymmetry (rows x, y, z, alpha, beta, gamma in degrees; scale) and
+  ManualSymmetry (rows x, y, z, alpha, beta, gamma in degrees; scale),
+  ``Scripted Symmetry`` (a Lua script whose Populate(p, nlayers) gives those
+  rows, run by dpx.lua; LuaSymmetry, Backend/Backend/Symmetry.cpp:404-521) and
   ``,25`` space-filling symmetry (three rows of distance, angle, repetitions).
 
-Nested ManualSymmetry nodes are flattened (FlattenTree, Backend/Backend/
+Nested symmetry nodes are flattened (FlattenTree, Backend/Backend/
 Amplitude.cpp:577-691): every leaf gets the composition of the symmetry copies
-and node placements above it.  Geometric form-factor models, Lua-scripted
-symmetries and electron PDBs are outside the scattering path and are rejected.
+and node placements above it.  Geometric form-factor models and electron PDBs
+are outside the scattering path and are rejected.
 """
 from __future__ import annotations
 
@@ -29,6 +31,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
+from . import lua as L
 from . import models as M
 from . import pdb as P
 
@@ -140,8 +143,8 @@ class _Decoder:
             extra = node.get("ExtraParameters", [1])
             return M.AmpGridAmplitude(self.resolve(node["Filename"]), scale=float(extra[0] if extra else 1.0),
                                       location=_location(node))
-        raise NotImplementedError(f"model type {t!r} is outside the scattering path (geometric form factors, "
-                                  "Lua-scripted symmetries and electron PDBs are not carried)")
+        raise NotImplementedError(f"model type {t!r} is outside the scattering path (geometric form factors "
+                                  "and electron PDBs are not carried)")
 
     def grid_subtree(self, node) -> bool:
         """The node and every node under it use grids (the reference's
@@ -160,8 +163,20 @@ class _Decoder:
         its rows (and its own placement) compose into the copies of its
         children."""
         t = node.get("Type")
-        if t == ",26":
-            rows = np.asarray(node.get("Parameters", []), dtype=np.float64).reshape(-1, 6)
+        if t in (",26", "Scripted Symmetry"):
+            if t == ",26":
+                rows = np.asarray(node.get("Parameters", []), dtype=np.float64).reshape(-1, 6)
+            else:  # the script's Populate(p, nlayers) gives the rows (LuaSymmetry, Symmetry.cpp:463-521)
+                if not node.get("Filename"):
+                    raise ValueError("a scripted symmetry needs its script (Filename)")
+                script = self.resolve(node["Filename"])  # a path, or the text given in ``files``
+                if isinstance(script, (list, tuple)):
+                    script = "\n".join(script)
+                elif os.path.exists(script):
+                    with open(script) as f:
+                        script = f.read()
+                params = node.get("Parameters", [])
+                rows = L.populate(script, params, int(node.get("nLayers", len(params))))
             Rn, tn = _transform(_location(node))
             scale = float((node.get("ExtraParameters") or [1.0])[0])
             mine = []

@@ -5,7 +5,11 @@ reference's generate/gpu/short/Man_Symm_Impl_No_Charges_* fixtures) is a
 two-level ManualSymmetry of the 3J6F tubulin dimer (18 docked copies, 6,763
 atoms with implicit hydrogens, dummy-atom solvent, with or without a
 voxelized hydration layer) averaged by Monte Carlo, VEGAS or Gauss-Kronrod on
-the grid or by the hybrid per-orientation docked sum.  The state document goes
+the grid or by the hybrid per-orientation docked sum.  Each case of
+tests/golden/scripted.json.gz (make_scripted.py, from the
+Scripted_Symm_Impl_No_Charges_* fixtures) is the same dimer under a
+Lua-scripted symmetry (a 3 x 2 x 3 lattice of copies) over a ManualSymmetry:
+its script runs through dpx.lua.  The state document goes
 through dpx.state.decode (this package's JSON state reader) and the PDB
 records through dpx.pdb.read_pdb; the I(q) of the FP32-bulk path must pass
 the reference's acceptance of its generate tests
@@ -48,16 +52,17 @@ from dpx import models as M
 from dpx import state as S
 
 pytestmark = pytest.mark.gpu
-GOLD = os.path.join(os.path.dirname(__file__), "golden", "mansymm.json.gz")
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
 
-def _load():
-    with gzip.open(GOLD, "rt") as f:
+def _load(name):
+    with gzip.open(os.path.join(GOLD, name), "rt") as f:
         return json.load(f)
 
 
-DATA = _load()
-CASES = sorted(DATA["cases"])
+DATA = _load("mansymm.json.gz")
+SCRIPTED = _load("scripted.json.gz")
+CASES = [("man", n) for n in sorted(DATA["cases"])] + [("lua", n) for n in sorted(SCRIPTED["cases"])]
 
 
 # ---- the reference's acceptance (test_generate_results.py:99-199), restated ----
@@ -89,11 +94,16 @@ def div_test(calc, exp):
     return all(abs(c / e) >= 0.999999 for c, e in zip(calc, exp))
 
 
-@pytest.mark.parametrize("name", CASES)
-def test_reference_docked_sum_golden(ctx, name):
-    case = DATA["cases"][name]
+@pytest.mark.parametrize("kind,name", CASES)
+def test_reference_docked_sum_golden(ctx, kind, name):
+    files = {DATA["pdb_name"]: DATA["pdb_lines"]}
+    if kind == "man":
+        case = DATA["cases"][name]
+    else:  # the same PDB records (make_scripted.py checks them), the scripted symmetry's Lua source
+        case = SCRIPTED["cases"][name]
+        files[SCRIPTED["script_name"]] = SCRIPTED["script"]
     std = case["standard"]
-    job = S.decode(case["state"], files={DATA["pdb_name"]: DATA["pdb_lines"]})
+    job = S.decode(case["state"], files=files)
     Q = np.asarray(std["q"])
     exp, sig = np.asarray(std["I"]), np.asarray(std["sigma"])
     dirs = M.mc_directions(20260, 1_000_000) if job.method == "MC" else None

@@ -81,7 +81,7 @@ def test_methods_populations_and_rejections(tmp_path):
     assert S.decode(_state([leaf], "Adaptive Gauss Kronrod")).method == "GK"
     with pytest.raises(NotImplementedError):
         S.decode(_state([_node(",2", Parameters=[[1, 333]])]))
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(ValueError):  # a scripted symmetry without its script
         S.decode(_state([_node("Scripted Symmetry", Children=[leaf])]))
     with pytest.raises(FileNotFoundError):
         S.decode(_state([_node("PDB", Filename="nowhere.pdb")]), base_dir=str(tmp_path))
