@@ -29,6 +29,7 @@
 #include <deque>
 #include <list>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -88,6 +89,7 @@ struct Request {
     std::vector<double> Q;
     // runtime
     int status = 1;  // 1 pending / running, 0 done, < 0 error
+    std::string why;  // the worker's message for a failed request
     std::vector<double> res;
     Clock::time_point t_submit, t_done;
     std::vector<GridEntry*> grids;  // per leaf
@@ -233,6 +235,7 @@ void admit_locked(dpx_server_s* S, std::vector<Request*>& admitted) {
         }
         if (need > S->budget) {  // can never fit
             r->status = DPX_ERR_OOM;
+            r->why = "the request needs more device memory than the server's budget";
             r->t_done = Clock::now();
             S->st.failed++;
             it = S->pending.erase(it);
@@ -303,6 +306,7 @@ void retire_locked(dpx_server_s* S) {
             S->st.completed++;
         } else {
             r->status = cuda_fail(q, "request");
+            r->why = dpx_last_error();
             S->st.failed++;
         }
         r->t_done = Clock::now();
@@ -388,6 +392,12 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
     h.resize(jobs_at + n32 * sizeof(dpx::FillJob));
     const size_t counter_at = al16(h.size());
     h.resize(counter_at + 64, 0);
+    // the harmonic fills' job table goes last; its room is counted before the
+    // staging block is allocated
+    size_t n_harm = 0;
+    for (size_t j = 0; j < fresh.size(); ++j) n_harm += harm[j] != 0;
+    const size_t hjobs_at = al16(h.size());
+    h.resize(hjobs_at + n_harm * sizeof(dpx::HarmJob), 0);
     // device: grids, then one staging block (freed in stream order after the launches)
     for (GridEntry* g : fresh) DPX_CUDA(cudaMallocAsync(&g->cells, g->bytes, s));
     char* d = nullptr;
@@ -411,8 +421,7 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
         hscratch += (plans[j].scratch_bytes + 255) & ~size_t(255);
     }
     const dpx::HarmShape hshape = dpx::plan_harmonic_jobs(hj.data(), (int)hj.size());
-    const size_t hjobs_at = al16(h.size());
-    h.resize(hjobs_at + hj.size() * sizeof(dpx::HarmJob));
+    if (hj.size() != n_harm) return fail(DPX_ERR_ARG, "harmonic job count changed while staging");
     if (!hj.empty()) std::memcpy(h.data() + hjobs_at, hj.data(), hj.size() * sizeof(dpx::HarmJob));
     size_t cap = 0;
     void* hp = S->pinned.get(h.size(), &cap);
@@ -564,8 +573,12 @@ void worker_main(dpx_server_s* S) {
         Delta dl;
         int rc = launch_fills(S, fresh, dl);
         std::vector<int> rcs(admitted.size(), rc);
+        std::vector<std::string> why(admitted.size(), rc ? std::string(dpx_last_error()) : std::string());
         for (size_t k = 0; k < admitted.size(); ++k)
-            if (!rc) rcs[k] = launch_request(S, admitted[k]);
+            if (!rc) {
+                rcs[k] = launch_request(S, admitted[k]);
+                if (rcs[k]) why[k] = dpx_last_error();
+            }
         lk.lock();
         S->st.fill_launches += dl.fill_launches;
         S->st.grid_fills += dl.grid_fills;
@@ -584,6 +597,7 @@ void worker_main(dpx_server_s* S) {
             S->st.bytes_in_use -= (int64_t)r->scratch_bytes;
             S->inflight.remove(r);
             r->status = rcs[k];
+            r->why = why[k];
             r->t_done = Clock::now();
             S->st.failed++;
         }
@@ -795,8 +809,9 @@ int dpx_server_wait(dpx_server S, uint64_t ticket, double* res, double* latency_
     const int status = r->status;
     if (status == DPX_OK && res) std::memcpy(res, r->res.data(), r->res.size() * sizeof(double));
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    const std::string why = r->why;
     delete r;
-    if (status != DPX_OK) return fail(status, "request failed (status %d)", status);
+    if (status != DPX_OK) return fail(status, "request failed (status %d): %s", status, why.c_str());
     return DPX_OK;
 }
 
