@@ -197,6 +197,8 @@ def run_dpx(args):
     if args.fill_shape:
         apply_fill_shape(ctx, args.fill_shape)
     ctx.set_fill_method(_lib.DPX_FILL_HARMONIC if args.fill_method == "harmonic" else _lib.DPX_FILL_DIRECT)
+    moments_tc = args.moments == "tcgen05"
+    _lib.check(L.dpx_set_moments_kernel(_lib.DPX_MOMENTS_TCGEN05 if moments_tc else _lib.DPX_MOMENTS_MMA_SYNC))
 
     amp, Q, dirs = build_inputs()
     sfu_c = C.c_double()
@@ -356,10 +358,14 @@ def run_dpx(args):
             # moments: per point and (l, m) six weights times a complex basis value = 24 flops
             flops = n_pts * kk * 24.0
             fp32_peak = float(max(pipes[0], pipes[1])) / 1e12
-            # executed on the tensor path: per 32 points, order l and quartet of 4 m,
-            # 8 m16n8k8 MMAs (hi and remainder of both operands) = 128 flops per point-(l, m)
+            # executed on the tensor path, 128 flops per point-(l, m) either way: mma.sync, per
+            # 32 points, order l and quartet of 4 m, 8 m16n8k8 TF32 MMAs (hi and remainder of
+            # both operands); tcgen05, per 64 points and 128 rows (64 (l, m)), 8 M128 N16 K16
+            # FP16 MMAs (hi and remainder of the basis; the weights' halves in N)
             mma_flops = n_pts * kk * 128.0
-            roofline = {"bound": "fp32", "kernel": "hm_moments", "method": "harmonic",
+            tensor_peak = (peaks["bf16_tflops"] * 1e12) if moments_tc else pipes[2]
+            roofline = {"bound": "fp32", "kernel": "hm_moments_tc" if moments_tc else "hm_moments",
+                        "method": "harmonic",
                         "achieved": flops / (mom_ms / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                         "frac": flops / (mom_ms / 1e3) / 1e12 / fp32_peak,
                         "traffic": MOMENTS_BYTES_PER_POINT * n_pts,
@@ -368,8 +374,10 @@ def run_dpx(args):
                         "pipes_measured_tflops": {"fp32_fma": pipes[0] / 1e12, "fp32_fma_f32x2": pipes[1] / 1e12,
                                                   "tf32_mma_sync": pipes[2] / 1e12},
                         "tensor_path": {"executed_tflops": mma_flops / (mom_ms / 1e3) / 1e12,
-                                        "peak": pipes[2] / 1e12,
-                                        "frac": mma_flops / (mom_ms / 1e3) / pipes[2]},
+                                        "peak": tensor_peak / 1e12,
+                                        "peak_kind": ("dense bf16/fp16 tcgen05 rate, MEASURED_PEAKS bf16_tflops"
+                                                      if moments_tc else "TF32 mma.sync, dpx_measure_pipe_peaks"),
+                                        "frac": mma_flops / (mom_ms / 1e3) / tensor_peak},
                         "note": "flops = points (atoms + solvent voxels) x K x 6 moments x 4 (complex "
                                 "multiply-add), K the mean over the points of the (l, m) their radial bins "
                                 "carry; time = the hm_moments launches alone (stage events around them); the "
@@ -1046,6 +1054,8 @@ def main():
     ap.add_argument("--no-error", action="store_true",
                     help="skip the error report (plain FP64 solve and FP64 direct-sum sample)")
     ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
+    ap.add_argument("--moments", default="mma", choices=["tcgen05", "mma"],
+                    help="harmonic moments kernel: the mma.sync kernel (default) or tcgen05.mma")
     ap.add_argument("--workload", default="subunit", choices=["subunit", "batch", "serve", "assembly"])
     ap.add_argument("--no-extras", action="store_true",
                     help="subunit: skip the batch and serving keys; assembly: skip the VEGAS / GK / FP64 extras")

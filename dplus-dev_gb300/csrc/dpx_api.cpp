@@ -342,6 +342,22 @@ int dpx_set_average_shape(int directions_per_thread) {
     return DPX_OK;
 }
 
+int dpx_set_moments_kernel(int kind) {
+    if (kind != DPX_MOMENTS_TCGEN05 && kind != DPX_MOMENTS_MMA_SYNC)
+        return fail(DPX_ERR_ARG, "unknown moments kernel %d", kind);
+    dpx::set_moments_kernel(kind);
+    return DPX_OK;
+}
+
+int dpx_get_moments_kernel(void) { return dpx::moments_kernel(); }
+
+int dpx_take_device_faults(unsigned* flags) {
+    if (!flags) return fail(DPX_ERR_ARG, "NULL argument");
+    *flags = 0;
+    DPX_CUDA(dpx::harmonic_take_faults(flags));
+    return DPX_OK;
+}
+
 int dpx_ctx_set_fill_schedule(dpx_ctx ctx, int persistent) {
     if (!ctx) return fail(DPX_ERR_ARG, "ctx is NULL");
     ctx->fill_persistent = persistent != 0;

@@ -37,10 +37,12 @@
 //                the rows' phi-spline derivatives.
 #include "dpx_internal.h"
 
+#include <atomic>
 #include <mutex>
 #include "dpx_spline.cuh"
 
 #include <cstdint>
+#include <cuda_fp16.h>
 
 namespace dpx {
 namespace {
@@ -396,6 +398,503 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
             out[k] = make_float2(v.x * sc, v.y * sc);
             k += l + 1;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// hm_moments_tc: the same moments MP[u][n][k] on the fifth-generation tensor
+// cores: tcgen05.mma kind::f16 with FP16 operands and FP32 accumulators in
+// tensor memory.  Per tile of 64 points and 128 rows (a row = one (l, m) and
+// re or im):
+//   D[row][col] += A[row][p] B[col][p]            (M = 128, N = 16, K = 16 per MMA)
+// A = the rows' basis values at the 64 points, written into tensor memory by
+// the producer warps (tcgen05.st), twice: the FP16 value (hi) and the FP16
+// remainder (lo), one MMA each per K-step; B = the weights w u^n of the points
+// in shared memory (K-major, 128-byte swizzle): rows n < 6 hi, rows 6 + n lo,
+// rows 12..15 zero.  So D[row][n] + D[row][6 + n] carries all four products
+// hi*hi + hi*lo + lo*hi + lo*lo of the FP32 operands (about 22 bits), and the
+// basis values never pass through shared memory.  The basis values are the
+// orthonormal Pbar_lm(cos theta) e^{-i m phi} (at most about 5.3 in magnitude
+// for l <= 175), the scaled recurrence of hm_moments times r_lm 2^11; the
+// weights are scaled by 2^(14 - e) per unit, 2^e above the unit's largest |w|:
+// both halves of both operands stay in the FP16 normal range (the remainders
+// too, down to operands 2^-14 of their scale), and the epilogue multiplies by
+// 2^(e - 25).
+//
+// CTA = 4 producer warps, 1 warp that owns the tensor memory (all 512
+// columns: two A slots of 64 columns, 24 accumulator tiles of 16) and issues
+// the MMAs from one thread, and 4 drain warps.  Producer warp w writes tensor-memory lanes
+// 32w .. 32w + 31 of a tile: two consecutive steps (lanes 32w + 16h), in
+// each the rows of one octet of orders m = 8o + g (lane 16h + g: re,
+// 16h + 8 + g: im); thread (g, t4) holds its row pair at the points
+// 16 rep + 4 t4 + i (the 16x256b fragment: two FP16 points per register).
+// Step d of octet o is l = m + d for every order of the octet, so the eight
+// recurrences of a warp start together (one start per octet, from the
+// per-chunk tables z^(8o) and z^g: z^m = z^(8o) z^g), and an order's last
+// l = LM ends its row early (zeros after it).  The unit's steps (octets end
+// to end) are cut evenly over the 4 P producer slots of its P CTAs; a slot
+// that starts inside an octet runs the recurrences silently up to its first
+// step.  Pipeline: producer slot fill -> mbarrier full[s] (128 arrivals) ->
+// MMA thread issues the tile's 8 MMAs (the tile's accumulator restarts every
+// chunk) and commits to empty[s] and done[tile] -> producers refill slot s;
+// the four drain warps (warp w reads tensor-memory lanes 32 (w % 4) ..) add the
+// tile into FP32 sums in shared memory (round to nearest) and arrive on
+// drained[tile], which the tile's next MMAs wait for.  A chain of 8 MMAs per
+// accumulator: the tensor cores' accumulation over a whole unit of 1,024
+// points (128 MMAs) measured 2.6e-6 of the largest amplitude on voxel leaves,
+// against 7e-7 for the mma.sync kernel.  Every wait is bounded (kTcWaitLimit
+// polls); a wait that gives up sets g_tc_fault and the CTA drains its MMAs,
+// frees tensor memory and returns.
+// ---------------------------------------------------------------------------
+constexpr int kTcProducers = 4;
+constexpr int kTcMmaWarp = kTcProducers;              // warp 4: tensor memory and the MMAs
+constexpr int kTcDrainers = 4;                        // warps 5..8: accumulator drains
+constexpr int kTcThreads = 32 * (kTcProducers + 1 + kTcDrainers);
+constexpr int kTcChunk = 64;                          // points per tile
+constexpr int kTcTiles = kTcSlotSteps / 2;            // accumulator tiles
+constexpr int kTcUnit = 1024;                         // points per unit at most
+constexpr int kTcOctets = kMaxL / 8 + 1;
+constexpr uint32_t kTcCols = 512;                     // tensor-memory columns held
+constexpr uint32_t kTcAcc0 = 128;                     // first accumulator column
+constexpr int kTcWaitLimit = 1 << 22;
+constexpr float kTcBasisScale = 2048.f;    // 2^11
+constexpr int kTcWeightExp = 14;           // weights scaled to below 2^14
+static_assert(kTcAcc0 + 16 * kTcTiles <= kTcCols, "accumulators fit tensor memory");
+// shared memory from a 1024-byte aligned base
+constexpr size_t kTcOffP = (size_t)kTcUnit / kTcChunk * 2048;           // weights: 16 chunks x 2 KB
+constexpr size_t kTcOffZ8 = kTcOffP + (size_t)kTcUnit * sizeof(float4);  // points
+constexpr size_t kTcOffZg = kTcOffZ8 + (size_t)kTcOctets * kTcChunk * sizeof(float2);  // z^(8o) per point
+constexpr size_t kTcOffAcc = kTcOffZg + (size_t)8 * kTcChunk * sizeof(float2);         // z^g per point
+constexpr size_t kTcOffBar = kTcOffAcc + (size_t)kTcTiles * 128 * kNodes * sizeof(float);  // sums [tile][row][n]
+constexpr int kTcBars = 4 + 2 * kTcTiles;  // full[2], empty[2], done[tiles], drained[tiles]
+constexpr size_t kTcSmemUse = 1024 + kTcOffBar + (size_t)kTcBars * 8 + 16;
+// requested per CTA: more than half of an SM's shared memory, so that one CTA
+// (which holds all of tensor memory) runs per SM
+constexpr size_t kTcSmemLaunch = 150 * 1024;
+static_assert(kTcSmemUse <= kTcSmemLaunch, "tensor-core moments shared memory");
+
+__device__ unsigned int g_tc_fault;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Waits for the completion of the barrier's phase of this parity; false when
+// kTcWaitLimit polls pass first.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    const uint32_t a = smem_u32(b);
+    for (int it = 0; it < kTcWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * kTcProducers) : "memory"); }
+
+// 16 lanes x 256 bits, repeated over 4 column groups: register 4r + j of thread
+// (g, t4) goes to lane base + g + 8 (j / 2), column 8r + 2 t4 + (j % 2).
+__device__ __forceinline__ void tmem_st_16x256b_x4(uint32_t taddr, const uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.16x256b.x4.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+// 32 lanes x 32 bits, 16 columns: thread i reads lane base + i.
+__device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+        "[%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr)
+        : "memory");
+}
+// D[tmem] (+)= A[tmem] B[smem descriptor]
+__device__ __forceinline__ void mma_f16_ts(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+        "r"(a), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
+                 : "memory");
+}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1,024 bytes apart (start address and offsets in 16-byte units).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// Instruction descriptor of kind::f16: FP32 accumulator, FP16 A and B, both
+// K-major, N = 16, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+// Weight w u^n of chunk point p (< 64) in row r of the swizzled B tile.
+__device__ __forceinline__ void tc_put_weight(unsigned char* tile, int r, int p, __half v) {
+    const int off = (r >> 3) * 1024 + (r & 7) * 128 + (((p >> 3) ^ (r & 7)) << 4) + (p & 7) * 2;
+    *reinterpret_cast<__half*>(tile + off) = v;
+}
+
+__device__ __forceinline__ void tc_geom(const float4 P, float& ct, float2& z) {
+    const float r = sqrtf(fmaf(P.z, P.z, fmaf(P.x, P.x, P.y * P.y)));
+    ct = 1.f;
+    z = make_float2(0.f, 0.f);
+    if (r > 0.f) {
+        const float ir = 1.f / r;
+        ct = P.z * ir;
+        z = make_float2(-P.x * ir, P.y * ir);
+    }
+}
+
+// Octet of a step of the unit's sequence and the step within it.
+__device__ __forceinline__ void tc_decode(int LM, int gs, int& o, int& d) {
+    const int O = LM / 8 + 1;
+    o = 0;
+    while (o + 1 < O && tc_octet_first(LM, o + 1) <= gs) ++o;
+    d = gs - tc_octet_first(LM, o);
+}
+
+// FP16 pair (x0 in the low half: the lower K index) as one register.
+__device__ __forceinline__ uint32_t h2u(float x0, float x1) {
+    const __half2 h = __floats2half2_rn(x0, x1);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__device__ void hm_moments_tc(const float4* __restrict__ pts, const int4* __restrict__ units, int n_units, int K,
+                              float delta, const int* __restrict__ lmb, const float2* __restrict__ cr,
+                              const float* __restrict__ nmm, float2* __restrict__ MP, int64_t local) {
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char* sm = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
+    unsigned char* sB = sm;
+    float4* sP = reinterpret_cast<float4*>(sm + kTcOffP);
+    float2* sZ8 = reinterpret_cast<float2*>(sm + kTcOffZ8);  // [o][64]
+    float2* sZg = reinterpret_cast<float2*>(sm + kTcOffZg);  // [g][64]
+    float* sAcc = reinterpret_cast<float*>(sm + kTcOffAcc);  // [tile][row][n]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kTcOffBar);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + 2;
+    uint64_t* done = bars + 4;
+    uint64_t* drained = bars + 4 + kTcTiles;
+    volatile uint32_t* s_taddr = reinterpret_cast<volatile uint32_t*>(bars + kTcBars);
+    volatile int* s_abort = reinterpret_cast<volatile int*>(bars + kTcBars) + 1;
+    unsigned int* s_wmax = reinterpret_cast<unsigned int*>(bars + kTcBars + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // ---- the CTA's unit (the last whose first CTA <= local) and part ----
+    int lo = 0, hi = n_units - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (units[mid].w <= local) lo = mid;
+        else hi = mid - 1;
+    }
+    const int4 un = units[lo];
+    const int LM = lmb[un.z];
+    const int S = tc_steps(LM), P = tc_parts(LM), W = 4 * P;
+    const int part = (int)(local - un.w);
+    if (part < 0 || part >= P || un.y > kTcUnit) return;  // (uniform over the CTA)
+    const int T = ((S + W - 1) / W + 1) / 2;  // tiles per chunk, every slot of the unit
+    const int nch = (un.y + kTcChunk - 1) / kTcChunk;
+    const int total = nch * T;
+
+    if (tid == 0) {
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(&full[k], 32 * kTcProducers);
+            mbar_init(&empty[k], 1);
+        }
+        for (int k = 0; k < kTcTiles; ++k) {
+            mbar_init(&done[k], 1);
+            mbar_init(&drained[k], 32 * kTcDrainers);
+        }
+        *s_abort = 0;
+        *s_wmax = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == kTcMmaWarp) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32((const void*)s_taddr)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int j = tid; j < kTcUnit; j += kTcThreads) sP[j] = j < un.y ? pts[un.x + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = tid; e < (int)(kTcOffP / 16); e += kTcThreads) reinterpret_cast<uint4*>(sB)[e] = make_uint4(0, 0, 0, 0);
+    for (int e = tid; e < T * 128 * kNodes; e += kTcThreads) sAcc[e] = 0.f;
+    __syncthreads();
+    for (int j = tid; j < un.y; j += kTcThreads) atomicMax(s_wmax, __float_as_uint(fabsf(sP[j].w)));
+    __syncthreads();
+    int wexp = 0;
+    frexpf(__uint_as_float(*s_wmax), &wexp);  // max |w| < 2^wexp
+    const float wsc = ldexpf(1.f, kTcWeightExp - wexp), wback = ldexpf(1.f, wexp - kTcWeightExp - 11);
+    {
+        const float rb = (un.z + 0.5f) * delta, ih = 2.f / delta;
+        for (int j = tid; j < un.y; j += kTcThreads) {
+            const float4 Pt = sP[j];
+            const float r = sqrtf(fmaf(Pt.z, Pt.z, fmaf(Pt.x, Pt.x, Pt.y * Pt.y)));
+            const float u = (r - rb) * ih;
+            unsigned char* tile = sB + (j / kTcChunk) * 2048;
+            const int p = j % kTcChunk;
+            float wv = Pt.w;  // w u^n, as hm_moments forms it, then scaled by 2^(14 - wexp)
+            for (int n = 0; n < kNodes; ++n) {
+                const float v = wv * wsc;
+                const __half h = __float2half_rn(v);
+                tc_put_weight(tile, n, p, h);
+                tc_put_weight(tile, 6 + n, p, __float2half_rn(v - __half2float(h)));
+                wv *= u;
+            }
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the weights are read by the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *s_taddr;
+
+    if (warp == kTcMmaWarp) {
+        // ---- MMA issue: one thread ----
+        if (lane == 0) {
+            int issued = -1;
+            for (int t = 0; t < total; ++t) {
+                if (*s_abort) break;
+                const int s = t & 1;
+                const int c = t / T, tau = t - c * T;
+                // the slot's basis values are in, and the tile's last sums were drained
+                if (!mbar_wait(&full[s], (uint32_t)((t >> 1) & 1)) ||
+                    (c > 0 && !mbar_wait(&drained[tau], (uint32_t)((c - 1) & 1)))) {
+                    *s_abort = 1;
+                    atomicOr(&g_tc_fault, 1u);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tbase + kTcAcc0 + 16u * (uint32_t)tau;
+                const uint32_t a = tbase + 64u * (uint32_t)s;
+                const uint64_t bd = sw128_desc(smem_u32(sB + c * 2048));
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    mma_f16_ts(d, a + 8u * k, bd + 2u * k, kTcIdesc, k > 0 ? 1u : 0u);
+                    mma_f16_ts(d, a + 32u + 8u * k, bd + 2u * k, kTcIdesc, 1u);
+                }
+                mma_commit(&empty[s]);
+                mma_commit(&done[tau]);
+                issued = t;
+            }
+            // the last commit covers every MMA this thread issued
+            if (issued >= 0 && !mbar_wait(&empty[issued & 1], (uint32_t)((issued >> 1) & 1)))
+                atomicOr(&g_tc_fault, 2u);
+        }
+        __syncwarp();
+    } else if (warp > kTcMmaWarp) {
+        // ---- drains: tile tau of chunk c into the FP32 sums, then free it ----
+        const int qd = warp & 3;  // the lane quarter this warp may read
+        for (int t = 0; t < total; ++t) {
+            const int c = t / T, tau = t - c * T;
+            if (!__all_sync(0xffffffffu, mbar_wait(&done[tau], (uint32_t)(c & 1)))) {
+                *s_abort = 1;
+                atomicOr(&g_tc_fault, 16u);
+                break;
+            }
+            tc_fence_after();
+            uint32_t v[16];
+            tmem_ld_32x32b_x16(tbase + ((uint32_t)(32 * qd) << 16) + kTcAcc0 + 16u * (uint32_t)tau, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float* acc = sAcc + ((size_t)tau * 128 + 32 * qd + lane) * kNodes;
+#pragma unroll
+            for (int n = 0; n < kNodes; ++n) acc[n] += __uint_as_float(v[n]) + __uint_as_float(v[6 + n]);
+            tc_fence_before();
+            mbar_arrive(&drained[tau]);
+        }
+    } else {
+        // ---- producers ----
+        const int g = lane >> 2, t4 = lane & 3;
+        const int sid = 4 * part + warp;
+        const int g0 = (int)((int64_t)sid * S / W), g1 = (int)((int64_t)(sid + 1) * S / W);
+        const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+        bool ok = true;
+        // every producer warp passes the two named barriers of every chunk (an
+        // abort only skips the chunk's tiles), so no warp waits on one that left
+        for (int c = 0; c < nch; ++c) {
+            // the chunk's power tables: z^g (g < 8) and z^(8o)
+            producers_sync();
+            if (tid < kTcChunk) {
+                float ct;
+                float2 z;
+                tc_geom(sP[c * kTcChunk + tid], ct, z);
+                float2 zp = make_float2(1.f, 0.f);
+                for (int k = 0; k < 8; ++k) {
+                    sZg[k * kTcChunk + tid] = zp;
+                    zp = cmulf(zp, z);
+                }
+                float2 zo = make_float2(1.f, 0.f);
+                const int O = LM / 8 + 1;
+                for (int o = 0; o < O; ++o) {
+                    sZ8[o * kTcChunk + tid] = zo;
+                    zo = cmulf(zo, zp);
+                }
+            }
+            producers_sync();
+            if (__any_sync(0xffffffffu, !ok || *s_abort)) {  // (warp-uniform)
+                ok = false;
+                continue;
+            }
+            // the thread's 16 points: 16 rep + 4 t4 + i, as q = 4 rep + i
+            f2x x2[16], q1[16], q2[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                float ct;
+                float2 z;
+                tc_geom(sP[c * kTcChunk + 16 * (q >> 2) + 4 * t4 + (q & 3)], ct, z);
+                x2[q] = pk2(2.f * ct, 2.f * ct);
+                q1[q] = q2[q] = 0ull;
+            }
+            int o = 0, d = 0;
+            if (g0 < g1) tc_decode(LM, g0, o, d);
+            int m = 8 * o + g;
+            int Lo = LM + 1 - 8 * o;  // steps of octet o
+            // one step of the recurrences at (o, d): q_l with l = m + d into q1
+            auto advance = [&](float c_lm) {
+                if (d == 0) {  // the octet's start: q_m = nmm[m] z^m, z^m = z^(8o) z^g
+                    const float nm = m <= LM ? nmm[m] : 0.f;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int pc = 16 * (q >> 2) + 4 * t4 + (q & 3);
+                        const float2 zm = cmulf(sZ8[o * kTcChunk + pc], sZg[g * kTcChunk + pc]);
+                        q2[q] = 0ull;
+                        q1[q] = pk2(nm * zm.x, nm * zm.y);
+                    }
+                } else {
+                    const f2x nc = pk2(-c_lm, -c_lm);
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const f2x v = fma2(x2[q], q1[q], mul2(nc, q2[q]));
+                        q2[q] = q1[q];
+                        q1[q] = v;
+                    }
+                }
+            };
+            // silent steps up to the slot's first
+            {
+                const int d0 = d;
+                for (d = 0; d < d0; ++d) {
+                    const int l = m + d;
+                    const float c_lm = (d >= 2 && m <= LM && l <= LM) ? __ldg(&cr[l * (l + 1) / 2 + m].x) : 0.f;
+                    advance(c_lm);
+                }
+            }
+            int gs = g0;
+            for (int tau = 0; tau < T; ++tau) {
+                const int t = c * T + tau, s = t & 1;
+                if (__any_sync(0xffffffffu, *s_abort != 0)) {
+                    ok = false;
+                    break;
+                }
+                // the warp decides together (the .sync.aligned stores below need every lane)
+                const bool free = __all_sync(0xffffffffu, t < 2 || mbar_wait(&empty[s], (uint32_t)(((t >> 1) - 1) & 1)));
+                if (!free) {
+                    *s_abort = 1;
+                    atomicOr(&g_tc_fault, 4u);
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+#pragma unroll 1
+                for (int h = 0; h < 2; ++h, ++gs) {
+                    uint32_t H[16], L[16];
+                    if (gs < g1) {
+                        if (d == Lo) {  // next octet
+                            ++o;
+                            d = 0;
+                            m = 8 * o + g;
+                            Lo = LM + 1 - 8 * o;
+                        }
+                        const int l = m + d;
+                        const bool act = m <= LM && l <= LM;
+                        float2 cv = make_float2(0.f, 0.f);
+                        if (act) cv = __ldg(&cr[l * (l + 1) / 2 + m]);
+                        advance(d >= 2 ? cv.x : 0.f);
+                        // r_lm 2^11 (0 for rows past their last order)
+                        const f2x r2 = pk2(cv.y * kTcBasisScale, cv.y * kTcBasisScale);
+#pragma unroll
+                        for (int rep = 0; rep < 4; ++rep) {
+                            float hr[4], hi_[4], lr[4], li[4];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const f2x v = mul2(q1[4 * rep + i], r2);
+                                float vr, vi;
+                                upk2(v, vr, vi);
+                                const float ar = __uint_as_float(__float_as_uint(vr) & 0xffffe000u);
+                                const float ai = __uint_as_float(__float_as_uint(vi) & 0xffffe000u);
+                                float br, bi;
+                                upk2(sub2(v, pk2(ar, ai)), br, bi);
+                                hr[i] = ar;
+                                hi_[i] = ai;
+                                lr[i] = br;
+                                li[i] = bi;
+                            }
+                            H[4 * rep + 0] = h2u(hr[0], hr[1]);
+                            H[4 * rep + 1] = h2u(hr[2], hr[3]);
+                            H[4 * rep + 2] = h2u(hi_[0], hi_[1]);
+                            H[4 * rep + 3] = h2u(hi_[2], hi_[3]);
+                            L[4 * rep + 0] = h2u(lr[0], lr[1]);
+                            L[4 * rep + 1] = h2u(lr[2], lr[3]);
+                            L[4 * rep + 2] = h2u(li[0], li[1]);
+                            L[4 * rep + 3] = h2u(li[2], li[3]);
+                        }
+                        ++d;
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) H[e] = L[e] = 0u;
+                    }
+                    const uint32_t ta = tbase + lane_base + ((uint32_t)(16 * h) << 16) + 64u * (uint32_t)s;
+                    tmem_st_16x256b_x4(ta, H);
+                    tmem_st_16x256b_x4(ta + 32u, L);
+                }
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                tc_fence_before();
+                mbar_arrive(&full[s]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp < kTcProducers && !*s_abort) {
+        // ---- epilogue: row 32w + 16h + 8c + g of tile tau = (order of row g of
+        // producer slot w's step 2 tau + h, component c) ----
+        const int sid = 4 * part + warp;
+        const int g0 = (int)((int64_t)sid * S / W), g1 = (int)((int64_t)(sid + 1) * S / W);
+        const int h = lane >> 4, c = (lane >> 3) & 1, g = lane & 7;
+        float* out = reinterpret_cast<float*>(MP);
+        for (int tau = 0; tau < T; ++tau) {
+            const int gs = g0 + 2 * tau + h;
+            if (gs >= g1) continue;
+            int o, d;
+            tc_decode(LM, gs, o, d);
+            const int m = 8 * o + g, l = m + d;
+            if (m > LM || l > LM) continue;
+            const int64_t k = (int64_t)l * (l + 1) / 2 + m;
+            const float* acc = sAcc + ((size_t)tau * 128 + 32 * warp + lane) * kNodes;
+#pragma unroll
+            for (int n = 0; n < kNodes; ++n) out[(((int64_t)lo * kNodes + n) * K + k) * 2 + c] = acc[n] * wback;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == kTcMmaWarp) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTcCols) : "memory");
     }
 }
 
@@ -1131,6 +1630,18 @@ __global__ void __launch_bounds__(32) hm_moments_jobs(const HarmJob* __restrict_
                reinterpret_cast<float2*>(scratch + h.s_MP[k]), (int)(local % nu), (int)(local / nu));
 }
 
+// The tensor-core moments of every (job, set): a set's CTAs are its units'
+// parts (units[].w: the unit's first CTA in the set).
+__global__ void __launch_bounds__(kTcThreads, 1) hm_moments_tc_jobs(const HarmJob* __restrict__ J, int n,
+                                                                    char* __restrict__ scratch) {
+    const int64_t b = blockIdx.x;
+    const int js = set_of(J, n, b, &HarmJob::b_mom);
+    const HarmJob& h = J[js >> 1];
+    const int k = js & 1;
+    hm_moments_tc(h.pts[k], h.units[k], h.n_units[k], h.K, (float)h.delta, h.lmb, h.cr, h.nmm,
+                  reinterpret_cast<float2*>(scratch + h.s_MP[k]), b - h.b_mom[k]);
+}
+
 __global__ void __launch_bounds__(kFitThreads) hm_fit_groups(const HarmJob* __restrict__ J, int n, int64_t fit_blocks,
                                                              char* __restrict__ scratch) {
     const int64_t blk = blockIdx.x;
@@ -1193,8 +1704,24 @@ size_t synth_smem(int Lp, int li) {
     return ((size_t)kSynthRows * 2 * nG + (size_t)nph + cells) * sizeof(float2);
 }
 std::mutex g_smem_mu;
-size_t g_smem_set[2][64] = {};  // per device: the limits set for hm_moments, hm_synth
+size_t g_smem_set[3][64] = {};  // per device: the limits set for hm_moments, hm_synth, hm_moments_tc
+std::atomic<int> g_moments_kind{1};
 }  // namespace
+
+void set_moments_kernel(int kind) { g_moments_kind.store(kind == 1 ? 1 : 0); }
+int moments_kernel() { return g_moments_kind.load(); }
+
+cudaError_t harmonic_take_faults(unsigned* flags) {
+    unsigned v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_tc_fault, sizeof v);
+    if (e != cudaSuccess) return e;
+    if (v) {
+        const unsigned zero = 0;
+        e = cudaMemcpyToSymbol(g_tc_fault, &zero, sizeof zero);
+    }
+    if (flags) *flags = v;
+    return e;
+}
 
 cudaError_t launch_pipe_probe(cudaStream_t s, int kind, int blocks, int iters, float* out) {
     pipe_probe_kernel<<<blocks, 256, 0, s>>>(kind, iters, out);
@@ -1206,12 +1733,14 @@ cudaError_t harmonic_reserve_smem(int Lp, int LM) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    const size_t need[2] = {moments_smem(LM), synth_smem(Lp, LM)};
+    const size_t need[3] = {moments_smem(LM), synth_smem(Lp, LM), kTcSmemLaunch};
     std::lock_guard<std::mutex> lock(g_smem_mu);
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
         if (need[k] <= 48 * 1024 || need[k] <= g_smem_set[k][dev]) continue;
-        e = k == 0 ? cudaFuncSetAttribute(hm_moments_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k])
-                   : cudaFuncSetAttribute(hm_synth_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k]);
+        const void* f = k == 0 ? (const void*)hm_moments_jobs
+                        : k == 1 ? (const void*)hm_synth_jobs
+                                 : (const void*)hm_moments_tc_jobs;
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k]);
         if (e != cudaSuccess) return e;
         g_smem_set[k][dev] = need[k];
     }
@@ -1246,6 +1775,7 @@ cudaError_t launch_voxel_bins(cudaStream_t s, const VoxelBinArgs& a) {
 
 HarmShape plan_harmonic_jobs(HarmJob* J, int n) {
     HarmShape sh{};
+    sh.moments_kind = moments_kernel();
     for (int j = 0; j < n; ++j) {
         HarmJob& h = J[j];
         const int pairs = ((h.LM + 4) / 4 + 1) / 2;
@@ -1256,7 +1786,7 @@ HarmShape plan_harmonic_jobs(HarmJob* J, int n) {
         sh.fit += ((int64_t)h.Lp * h.nbins * (h.LM + 1) + kFitThreads - 1) / kFitThreads;
         for (int k = 0; k < 2; ++k) {
             h.b_mom[k] = sh.moments;
-            sh.moments += (int64_t)h.n_units[k] * pairs;
+            sh.moments += sh.moments_kind == 0 ? (int64_t)h.n_parts[k] : (int64_t)h.n_units[k] * pairs;
             h.b_grp[k] = sh.groups;
             sh.groups += ((int64_t)h.G[k] * kNodes * h.K + kFitThreads - 1) / kFitThreads;
             h.b_con[k] = sh.contract;
@@ -1267,6 +1797,9 @@ HarmShape plan_harmonic_jobs(HarmJob* J, int n) {
         sh.maxLp = std::max(sh.maxLp, h.Lp);
         sh.maxLM = std::max(sh.maxLM, h.LM);
     }
+    // the launches size their shared memory for the table's largest shell count
+    // and order together, which can exceed what any one job's plan reserved
+    if (n > 0) sh.reserve_error = harmonic_reserve_smem(sh.maxLp, sh.maxLM);
     return sh;
 }
 
@@ -1275,6 +1808,7 @@ int harmonic_launches_per_batch() { return 5; }
 cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, const HarmShape& sh, char* scratch,
                                  char* grid, cudaEvent_t* ev) {
     if (n <= 0) return cudaSuccess;
+    if (sh.reserve_error != cudaSuccess) return sh.reserve_error;
     const int64_t b = sh.fit + sh.groups;
     if (sh.nodes > 0x7fffffff || sh.moments > 0x7fffffff || b > 0x7fffffff || sh.contract > 0x7fffffff ||
         sh.synth > 0x7fffffff)
@@ -1283,8 +1817,12 @@ cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, c
     if (sh.nodes > 0) hm_nodes_jobs<<<(unsigned)sh.nodes, kNodesThreads, 0, s>>>(d_jobs, n, scratch);
     // the limits were raised by harmonic_reserve_smem when the jobs were planned
     if (ev && ev[0]) e = cudaEventRecord(ev[0], s);
-    if (e == cudaSuccess && sh.moments > 0)
-        hm_moments_jobs<<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
+    if (e == cudaSuccess && sh.moments > 0) {
+        if (sh.moments_kind == 0)
+            hm_moments_tc_jobs<<<(unsigned)sh.moments, kTcThreads, kTcSmemLaunch, s>>>(d_jobs, n, scratch);
+        else
+            hm_moments_jobs<<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
+    }
     if (e == cudaSuccess && ev && ev[1]) e = cudaEventRecord(ev[1], s);
     if (e == cudaSuccess && b > 0) hm_fit_groups<<<(unsigned)b, kFitThreads, 0, s>>>(d_jobs, n, sh.fit, scratch);
     if (e == cudaSuccess && sh.contract > 0)

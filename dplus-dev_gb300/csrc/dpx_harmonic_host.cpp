@@ -118,6 +118,17 @@ void make_atom_set(const std::vector<float4>& in, int n_ions, int nbins, double 
     out.gu.push_back((int)out.units.size());
 }
 
+// The tensor-core moments' CTAs of a set: units[].w = the unit's first CTA
+// (dpx::tc_parts of its bin's order per unit); returns the set's total.
+int number_parts(std::vector<int4>& units, const std::vector<int>& lmb) {
+    int n = 0;
+    for (int4& u : units) {
+        u.w = n;
+        n += dpx::tc_parts(lmb[u.z]);
+    }
+    return n;
+}
+
 }  // namespace
 
 int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, HarmPlan& p) {
@@ -260,6 +271,7 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
     Set sa;
     make_atom_set(atoms, d.n_ions, nbins, delta, sa);
     // ---- the device arena: tables, the atoms' set, the voxels (binned below) ----
+    p.n_parts[0] = number_parts(sa.units, lmb);
     std::vector<char> h;
     p.o_lmax = put(h, lmax.data(), lmax.size() * sizeof(int));
     p.o_lmb = put(h, lmb.data(), lmb.size() * sizeof(int));
@@ -330,6 +342,7 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
             start += cnt;
         }
         sv.gu.push_back((int)sv.units.size());
+        p.n_parts[1] = number_parts(sv.units, lmb);
         if (sv.units.size() > vox_units_max || start != nv)
             return fail(DPX_ERR_ARG, "harmonic fill: %zu voxel units above the %zu planned", sv.units.size(),
                         vox_units_max);
@@ -415,6 +428,7 @@ dpx::HarmJob harmonic_job(const HarmPlan& p, size_t scratch_off, size_t grid_off
         J.groups[k] = reinterpret_cast<const int2*>(base + p.o_groups[k]);
         J.gu[k] = reinterpret_cast<const int*>(base + p.o_gu[k]);
         J.n_units[k] = p.n_units[k];
+        J.n_parts[k] = p.n_parts[k];
         J.G[k] = p.n_groups[k];
         J.s_MP[k] = scratch_off + p.s_MP[k];
         J.s_M[k] = scratch_off + p.s_M[k];

@@ -211,6 +211,7 @@ struct HarmPlan {
     double delta = 0.0;
     int64_t n_vox = 0;
     int n_units[2] = {0, 0}, n_groups[2] = {0, 0};  // [0] atoms, [1] solvent voxels
+    int n_parts[2] = {0, 0};  // CTAs of the tensor-core moments per set
     double cen[3] = {0, 0, 0};   // the centring translation restored per cell
     float scale = 1.f, vox_s = 0.f;
     double origin = 0.0;         // F(0), FP64, scaled

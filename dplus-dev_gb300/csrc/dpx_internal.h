@@ -184,6 +184,25 @@ cudaError_t launch_sfu_probe(cudaStream_t s, int blocks, int iters, float* out);
 // Table pointers are absolute (the structure's plan arena); scratch and grid
 // are byte offsets from the launch's scratch and grid bases, so one table
 // serves any scratch and grid.  Set 0: atoms, set 1: solvent voxels.
+// Tensor-core moments (hm_moments_tc): the (l, m) steps of a unit whose bin
+// carries orders l <= LM, laid out as octets o of the orders m = 8o .. 8o + 7
+// (octet o takes LM + 1 - 8o steps: step d holds l = m + d for each of its
+// orders m), cut evenly over 4 P producer-warp slots of at most
+// kTcSlotSteps steps each, P CTAs per unit.  units[].w holds a unit's first
+// CTA within its set.
+constexpr int kTcSlotSteps = 48;
+__host__ __device__ inline int tc_octet_first(int LM, int o) { return o * (LM + 1) - 4 * o * (o - 1); }
+__host__ __device__ inline int tc_steps(int LM) { return tc_octet_first(LM, LM / 8 + 1); }
+__host__ __device__ inline int tc_parts(int LM) { return (tc_steps(LM) + 4 * kTcSlotSteps - 1) / (4 * kTcSlotSteps); }
+// Which moments kernel the harmonic launches use (process-wide): 0 tcgen05.mma
+// (FP16 hi + lo operands, accumulators in tensor memory), 1 (the default)
+// mma.sync TF32 (split operands, sums in shared memory).
+void set_moments_kernel(int kind);
+int moments_kernel();
+// Faults recorded by the tensor-core moments kernel (a wait that ran past its
+// limit): reads and clears the device flag (synchronous).
+cudaError_t harmonic_take_faults(unsigned* flags);
+
 struct HarmJob {
     int Lp, nbins, LM, K;
     double step, delta;        // q step, radial bin width (nm)
@@ -200,6 +219,7 @@ struct HarmJob {
     const int2* groups[2];     // {bin, ion or -1}
     const int* gu[2];          // [G+1] first unit of each group
     int n_units[2], G[2];
+    int n_parts[2];            // CTAs of the tensor-core moments per set (sum over units of tc_parts)
     int vox;                   // the voxel set exists
     int use_center;
     float vox_s, scale;        // voxel edge (nm), scale
@@ -216,6 +236,8 @@ struct HarmJob {
 struct HarmShape {
     int64_t nodes, moments, fit, groups, contract, synth;
     int maxLp, maxLM;
+    int moments_kind;  // moments_kernel() when planned
+    cudaError_t reserve_error;  // raising the launches' shared-memory limits (on the planning device)
 };
 // Host: the block layout of n jobs (sets their b_* fields).
 HarmShape plan_harmonic_jobs(HarmJob* jobs, int n);

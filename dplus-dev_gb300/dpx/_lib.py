@@ -19,6 +19,7 @@ DPX_CALC_ATOMIC_FORMFACTORS = 1
 DPX_CALC_DUMMY_SOLVENT = 2
 DPX_FILL_DIRECT, DPX_FILL_HARMONIC = 0, 1
 DPX_CONV_CPU, DPX_CONV_GPU = 0, 1
+DPX_MOMENTS_TCGEN05, DPX_MOMENTS_MMA_SYNC = 0, 1
 DPX_OA_MC, DPX_OA_VEGAS = 0, 1
 
 _STATUS = {-1: "DPX_ERR_ARG", -2: "DPX_ERR_CUDA", -3: "DPX_ERR_OOM", -4: "DPX_ERR_STOPPED",
@@ -78,6 +79,9 @@ _SIGS = {
     "dpx_set_average_shape": (C.c_int, [C.c_int]),
     "dpx_ctx_set_fill_poly": (C.c_int, [_P, C.c_int]),
     "dpx_ctx_set_fill_method": (C.c_int, [_P, C.c_int]),
+    "dpx_set_moments_kernel": (C.c_int, [C.c_int]),
+    "dpx_get_moments_kernel": (C.c_int, []),
+    "dpx_take_device_faults": (C.c_int, [C.POINTER(C.c_uint)]),
     "dpx_ctx_get_fill_method": (C.c_int, [_P]),
     "dpx_ctx_set_convergence": (C.c_int, [_P, C.c_int, C.c_int64]),
     "dpx_ctx_set_timing": (C.c_int, [_P, C.c_int]),

@@ -117,6 +117,22 @@ enum { DPX_FILL_DIRECT = 0, DPX_FILL_HARMONIC = 1 };
  * process: 2 gives each thread the samples of two neighbouring chunks, twice
  * the independent gathers in flight at a higher register count. */
 int dpx_set_average_shape(int directions_per_thread);
+/* Moments kernel of the harmonic fill, for every context of the process (no
+ * counterpart in the reference): DPX_MOMENTS_MMA_SYNC (the default) computes the
+ * moments with the warp-level mma.sync TF32 path (operands in registers);
+ * DPX_MOMENTS_TCGEN05 on the fifth-generation tensor cores (tcgen05.mma with
+ * FP16 operands split into value and remainder, accumulators in tensor
+ * memory).  Harmonic plans made after the call use it (prepared leaves and
+ * batches keep the kernel they were planned with). */
+enum { DPX_MOMENTS_TCGEN05 = 0, DPX_MOMENTS_MMA_SYNC = 1 };
+int dpx_set_moments_kernel(int kind);
+int dpx_get_moments_kernel(void);
+/* Faults recorded by this library's kernels on the current device since the
+ * last call (no counterpart in the reference): *flags = 0 when there were none;
+ * bits 0-3: a wait of the tensor-core moments kernel ran past its limit (that
+ * kernel then leaves its moments unwritten and returns).  Reads and clears the
+ * flags; synchronous. */
+int dpx_take_device_faults(unsigned* flags);
 int dpx_ctx_set_fill_method(dpx_ctx ctx, int method);
 int dpx_ctx_get_fill_method(dpx_ctx ctx);
 /* Convergence test of the Monte Carlo average (eps > 0) for this context's
