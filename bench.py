@@ -198,13 +198,14 @@ def run_dpx(args):
         apply_fill_shape(ctx, args.fill_shape)
     ctx.set_fill_method(_lib.DPX_FILL_HARMONIC if args.fill_method == "harmonic" else _lib.DPX_FILL_DIRECT)
     moments_tc = args.moments == "tcgen05"
-    _lib.check(L.dpx_set_moments_kernel(_lib.DPX_MOMENTS_TCGEN05 if moments_tc else _lib.DPX_MOMENTS_MMA_SYNC))
+    _lib.check(L.dpx_set_moments_kernel({"tcgen05": _lib.DPX_MOMENTS_TCGEN05, "mma": _lib.DPX_MOMENTS_MMA_SYNC,
+                                         "mma16": _lib.DPX_MOMENTS_MMA_F16}[args.moments]))
 
     amp, Q, dirs = build_inputs()
     sfu_c = C.c_double()
     _lib.check(L.dpx_measure_sfu_peak(ctx.handle, C.byref(sfu_c)))
     sfu_measured = sfu_c.value
-    pipes = np.zeros(3)  # FP32 FMA scalar, FP32 FMA f32x2, TF32 mma.sync: flops/s on this GPU
+    pipes = np.zeros(4)  # FP32 FMA scalar, FP32 FMA f32x2, TF32 and FP16 mma.sync: flops/s on this GPU
     _lib.check(L.dpx_measure_pipe_peaks(ctx.handle, _lib.dptr(pipes)))
     tune = None
     if args.autotune:  # sweep every fill shape on this workload's leaf, keep the fastest
@@ -363,8 +364,9 @@ def run_dpx(args):
             # both operands); tcgen05, per 64 points and 128 rows (64 (l, m)), 8 M128 N16 K16
             # FP16 MMAs (hi and remainder of the basis; the weights' halves in N)
             mma_flops = n_pts * kk * 128.0
-            tensor_peak = (peaks["bf16_tflops"] * 1e12) if moments_tc else pipes[2]
-            roofline = {"bound": "fp32", "kernel": "hm_moments_tc" if moments_tc else "hm_moments",
+            tensor_peak = {"tcgen05": peaks["bf16_tflops"] * 1e12, "mma": pipes[2], "mma16": pipes[3]}[args.moments]
+            roofline = {"bound": "fp32", "kernel": {"tcgen05": "hm_moments_tc_jobs", "mma": "hm_moments_jobs<TF32>",
+                                                   "mma16": "hm_moments_jobs<FP16>"}[args.moments],
                         "method": "harmonic",
                         "achieved": flops / (mom_ms / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                         "frac": flops / (mom_ms / 1e3) / 1e12 / fp32_peak,
@@ -372,11 +374,15 @@ def run_dpx(args):
                         "peak_kind": "measured on this GPU (dpx_measure_pipe_peaks: independent FP32 FMA chains, "
                                      "the faster of scalar and packed f32x2)",
                         "pipes_measured_tflops": {"fp32_fma": pipes[0] / 1e12, "fp32_fma_f32x2": pipes[1] / 1e12,
-                                                  "tf32_mma_sync": pipes[2] / 1e12},
+                                                  "tf32_mma_sync": pipes[2] / 1e12,
+                                                  "fp16_mma_sync": pipes[3] / 1e12},
                         "tensor_path": {"executed_tflops": mma_flops / (mom_ms / 1e3) / 1e12,
                                         "peak": tensor_peak / 1e12,
-                                        "peak_kind": ("dense bf16/fp16 tcgen05 rate, MEASURED_PEAKS bf16_tflops"
-                                                      if moments_tc else "TF32 mma.sync, dpx_measure_pipe_peaks"),
+                                        "peak_kind": {"tcgen05": "dense bf16/fp16 tcgen05 rate, MEASURED_PEAKS "
+                                                                     "bf16_tflops",
+                                                      "mma": "TF32 mma.sync m16n8k8, dpx_measure_pipe_peaks",
+                                                      "mma16": "FP16 mma.sync m16n8k16, dpx_measure_pipe_peaks"
+                                                      }[args.moments],
                                         "frac": mma_flops / (mom_ms / 1e3) / tensor_peak},
                         "note": "flops = points (atoms + solvent voxels) x K x 6 moments x 4 (complex "
                                 "multiply-add), K the mean over the points of the (l, m) their radial bins "
@@ -1054,8 +1060,8 @@ def main():
     ap.add_argument("--no-error", action="store_true",
                     help="skip the error report (plain FP64 solve and FP64 direct-sum sample)")
     ap.add_argument("--profile-shape", default="", help="atoms,layers,dirs,nq (ncu captures only)")
-    ap.add_argument("--moments", default="mma", choices=["tcgen05", "mma"],
-                    help="harmonic moments kernel: the mma.sync kernel (default) or tcgen05.mma")
+    ap.add_argument("--moments", default="mma16", choices=["tcgen05", "mma", "mma16"],
+                    help="harmonic moments kernel: mma.sync FP16 (default), mma.sync TF32 or tcgen05.mma")
     ap.add_argument("--workload", default="subunit", choices=["subunit", "batch", "serve", "assembly"])
     ap.add_argument("--no-extras", action="store_true",
                     help="subunit: skip the batch and serving keys; assembly: skip the VEGAS / GK / FP64 extras")

@@ -343,7 +343,7 @@ int dpx_set_average_shape(int directions_per_thread) {
 }
 
 int dpx_set_moments_kernel(int kind) {
-    if (kind != DPX_MOMENTS_TCGEN05 && kind != DPX_MOMENTS_MMA_SYNC)
+    if (kind != DPX_MOMENTS_TCGEN05 && kind != DPX_MOMENTS_MMA_SYNC && kind != DPX_MOMENTS_MMA_F16)
         return fail(DPX_ERR_ARG, "unknown moments kernel %d", kind);
     dpx::set_moments_kernel(kind);
     return DPX_OK;
@@ -1341,6 +1341,23 @@ int dpx_measure_sfu_peak(dpx_ctx ctx, double* ops_per_s) {
     return DPX_OK;
 }
 
+int dpx_measure_tcgen05_issue(dpx_ctx ctx, double* cycles_per_mma) {
+    if (!ctx || !cycles_per_mma) return fail(DPX_ERR_ARG, "NULL argument");
+    if (int rc = set_device(ctx)) return rc;
+    DPX_CUDA(ctx->result.reserve(64));
+    char* d = static_cast<char*>(ctx->result.p);
+    DPX_CUDA(cudaMemsetAsync(d, 0, 64, ctx->stream));
+    DPX_CUDA(dpx::launch_tc_issue_probe(ctx->stream, reinterpret_cast<long long*>(d), reinterpret_cast<int*>(d + 16)));
+    long long c[2] = {0, 0};
+    int st = 0;
+    DPX_CUDA(cudaMemcpyAsync(c, d, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+    DPX_CUDA(cudaMemcpyAsync(&st, d + 16, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+    DPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st) return fail(DPX_ERR_CUDA, "tcgen05 issue probe: a wait ran past its limit");
+    for (int k = 0; k < 2; ++k) cycles_per_mma[k] = (double)c[k] / dpx::tc_issue_probe_mmas();
+    return DPX_OK;
+}
+
 int dpx_measure_pipe_peaks(dpx_ctx ctx, double* flops_per_s) {
     if (!ctx || !flops_per_s) return fail(DPX_ERR_ARG, "NULL argument");
     if (int rc = set_device(ctx)) return rc;
@@ -1357,8 +1374,8 @@ int dpx_measure_pipe_peaks(dpx_ctx ctx, double* flops_per_s) {
     }
     cudaError_t e = cudaSuccess;
     const int blocks = sms * 8;
-    for (int kind = 0; kind < 3 && e == cudaSuccess; ++kind) {
-        const int iters = kind == 2 ? 2048 : 8192;
+    for (int kind = 0; kind < 4 && e == cudaSuccess; ++kind) {
+        const int iters = kind >= 2 ? 2048 : 8192;
         e = dpx::launch_pipe_probe(s, kind, blocks, 64, (float*)ctx->result.p);  // warm-up
         float best = 0.f;
         for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
@@ -1373,7 +1390,8 @@ int dpx_measure_pipe_peaks(dpx_ctx ctx, double* flops_per_s) {
         const double threads = double(blocks) * 256.0;
         const double flops = kind == 0 ? threads * iters * 8 * 2
                              : kind == 1 ? threads * iters * 8 * 4
-                                         : threads / 32.0 * iters * 4 * 2048.0;
+                             : kind == 2 ? threads / 32.0 * iters * 4 * 2048.0
+                                         : threads / 32.0 * iters * 4 * 4096.0;
         if (e == cudaSuccess) flops_per_s[kind] = flops / (best * 1e-3);
     }
     cudaEventDestroy(e0);

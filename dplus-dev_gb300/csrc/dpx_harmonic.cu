@@ -276,6 +276,91 @@ __device__ __forceinline__ void moment_order(int l, int m, bool col_ok, int kc, 
     }
 }
 
+// FP16 variant of one order (the H kernel below): the basis values are the
+// true Pbar_lm e^{-i m phi} times 2^11 (the scaled recurrence times r_lm 2^11:
+// both FP16 halves stay in the normal range), split into the FP16 value (the
+// FP32 value truncated to 11 significant bits) and the FP16 remainder; the
+// pairs are the points (2t, 2t + 1) and (2t + 8, 2t + 9) of the k-steps of 16
+// points, one f16x2 register each, and each k-step takes two m16n8k16 MMAs
+// (value and remainder against the weights' value and remainder rows).
+__device__ __forceinline__ void mma_f16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t h2pack(float x0, float x1) {  // x0 in the low half (the lower k)
+    const __half2 h = __floats2half2_rn(x0, x1);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+template <bool PRO>
+__device__ __forceinline__ void moment_order_h(int l, int m, bool col_ok, int kc, const float2* __restrict__ cr,
+                                               f2x (&q_old)[4], const f2x (&q_new)[4], const f2x (&x2)[4],
+                                               const f2x (&st)[4], const uint32_t (&A)[2][4], float2* sDl,
+                                               bool drow, int lane) {
+    const float2 cv = col_ok ? __ldg(&cr[kc]) : make_float2(0.f, 0.f);
+    const float cl = (PRO && l < m + 2) ? 0.f : cv.x;
+    const f2x ncl = pk2(-cl, -cl);
+    const bool start = PRO && col_ok && l == m;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const f2x v = fma2(x2[j], q_new[j], mul2(ncl, q_old[j]));
+        q_old[j] = start ? st[j] : v;
+    }
+    const float rs = cv.y * 2048.f;  // r_lm 2^11 (1 at l = m)
+    const f2x rs2 = pk2(rs, rs);
+    uint32_t Bh[4], Bl[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const f2x v = mul2(q_old[j], rs2);
+        float v0, v1;
+        upk2(v, v0, v1);
+        const float h0 = __uint_as_float(__float_as_uint(v0) & 0xffffe000u);
+        const float h1 = __uint_as_float(__float_as_uint(v1) & 0xffffe000u);
+        float r0, r1;
+        upk2(sub2(v, pk2(h0, h1)), r0, r1);
+        Bh[j] = h2pack(h0, h1);
+        Bl[j] = h2pack(r0, r1);
+    }
+    // one accumulator per k-step: two independent chains of two MMAs, started
+    // at zero (the running sum is added in FP32 afterwards: the FP16 MMAs'
+    // accumulation rounds less finely, measured 2.9e-6 against 1.5e-6 for the
+    // bench subunit's I(q) when the running sum went through them)
+    float d[2][4];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
+    const float2 prev = drow ? sDl[lane] : make_float2(0.f, 0.f);  // loaded while the MMAs run
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        mma_f16(d[j], A[j], Bh[2 * j], Bh[2 * j + 1]);
+        mma_f16(d[j], A[j], Bl[2 * j], Bl[2 * j + 1]);
+    }
+    if (drow) {
+        const f2x s0 = add2(pk2(d[0][0], d[0][1]), pk2(d[0][2], d[0][3]));
+        const f2x s1 = add2(pk2(d[1][0], d[1][1]), pk2(d[1][2], d[1][3]));
+        float re, im;
+        upk2(add2(pk2(prev.x, prev.y), add2(s0, s1)), re, im);
+        sDl[lane] = make_float2(re, im);
+    }
+}
+
+template <bool H, bool PRO>
+__device__ __forceinline__ void order_step(int l, int m, bool col_ok, int kc, const float2* __restrict__ cr,
+                                           f2x (&q_old)[4], const f2x (&q_new)[4], const f2x (&x2)[4],
+                                           const f2x (&st)[4], const uint32_t (&A)[4][4], float2* sDl, bool drow,
+                                           int lane) {
+    if (H)
+        moment_order_h<PRO>(l, m, col_ok, kc, cr, q_old, q_new, x2, st,
+                            *reinterpret_cast<const uint32_t(*)[2][4]>(&A[0][0]), sDl, drow, lane);
+    else
+        moment_order<PRO>(l, m, col_ok, kc, cr, q_old, q_new, x2, st, A, sDl, drow, lane);
+}
+
+// H = false: TF32 operands (moment_order); H = true: FP16 operands
+// (moment_order_h), the weights w u^n scaled by 2^(14 - e) per unit (2^e above
+// the unit's largest |w|), the moments stored times 2^(e - 25).
+template <bool H>
 __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restrict__ units, int K, float delta,
                            const int* __restrict__ lmb, const float2* __restrict__ cr, const float* __restrict__ nmm,
                            float2* __restrict__ MP, int bx, int by) {
@@ -294,6 +379,17 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
     const bool drow = lane < 24;  // D rows n = g < 6
     for (int e = lane; e < (nla + nlb) * 24; e += 32) sD[e] = make_float2(0.f, 0.f);
     __syncwarp();
+    float wsc = 1.f, wback = 1.f;
+    if (H) {  // the unit's largest |w|: the FP16 weights' scale
+        float wm = 0.f;
+        for (int j = lane; j < un.y; j += 32) wm = fmaxf(wm, fabsf(__ldg(&pts[un.x + j]).w));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+        int e = 0;
+        frexpf(wm, &e);
+        wsc = ldexpf(1.f, 14 - e);
+        wback = ldexpf(1.f, e - 25);
+    }
 
     for (int c0 = 0; c0 < un.y; c0 += kChunk) {
         // ---- point c0 + lane: geometry and the powers z^m0 of the pair's quartets ----
@@ -314,22 +410,33 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
         const float2 zq1 = nq == 2 ? cpow(z, m0b) : make_float2(0.f, 0.f);
         // ---- the lane's eight points 8j + t + 4h: recurrence inputs, weight fragments ----
         f2x x2[4];
-        uint32_t A[4][4];
+        uint32_t A[4][4];  // H: [k-step][a0..a3], k-steps 0, 1
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            float xx[2];
+            float xx[2], wh2[2], wl2[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int src = 8 * j + t + 4 * h;
+                const int src = H ? 16 * (j >> 1) + 2 * t + 8 * (j & 1) + h : 8 * j + t + 4 * h;
                 xx[h] = 2.f * __shfl_sync(0xffffffffu, ct, src);
                 const float us = __shfl_sync(0xffffffffu, u, src);
                 float wv = __shfl_sync(0xffffffffu, w, src);
-                // weight w u^n of row n = g, split into TF32 and remainder
+                // weight w u^n of row n = g, split into the value (row g) and remainder (row g + 8)
                 if (g >= 6) wv = 0.f;
                 for (int n = 0; n < g; ++n) wv *= us;
-                const uint32_t wh = tf32_rna(wv);
-                A[j][2 * h] = wh;                                          // a0 / a2: row g
-                A[j][2 * h + 1] = __float_as_uint(wv - __uint_as_float(wh));  // a1 / a3: row g + 8
+                if (H) {
+                    wv *= wsc;
+                    const float vh = __half2float(__float2half_rn(wv));
+                    wh2[h] = vh;
+                    wl2[h] = wv - vh;
+                } else {
+                    const uint32_t wh = tf32_rna(wv);
+                    A[j][2 * h] = wh;                                          // a0 / a2: row g
+                    A[j][2 * h + 1] = __float_as_uint(wv - __uint_as_float(wh));  // a1 / a3: row g + 8
+                }
+            }
+            if (H) {  // a0 / a1: rows g, g + 8 at the k-step's points 2t, 2t + 1; a2 / a3 at 2t + 8, 2t + 9
+                A[j >> 1][2 * (j & 1)] = h2pack(wh2[0], wh2[1]);
+                A[j >> 1][2 * (j & 1) + 1] = h2pack(wl2[0], wl2[1]);
             }
             x2[j] = pk2(xx[0], xx[1]);
         }
@@ -348,7 +455,7 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
                 float sv[2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int src = 8 * j + t + 4 * h;
+                    const int src = H ? 16 * (j >> 1) + 2 * t + 8 * (j & 1) + h : 8 * j + t + 4 * h;
                     const float2 zp = shfl2(z, src);
                     float2 zm = shfl2(zq, src);  // z^m0 of the point, times z^c
                     if (c >= 1) zm = cmulf(zm, zp);
@@ -366,21 +473,21 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
             // orders m0 .. m0 + 3: the columns start
 #pragma unroll
             for (int s2 = 0; s2 < 2; ++s2) {
-                if (l <= LM) moment_order<true>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+                if (l <= LM) order_step<H, true>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
                 if (col_ok) kc += l + 1;
                 ++l;
-                if (l <= LM) moment_order<true>(l, m, col_ok, kc, cr, qb_, qa_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+                if (l <= LM) order_step<H, true>(l, m, col_ok, kc, cr, qb_, qa_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
                 if (col_ok) kc += l + 1;
                 ++l;
             }
             // the rest, two orders per iteration
             for (; l + 1 <= LM; l += 2) {
-                moment_order<false>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+                order_step<H, false>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
                 if (col_ok) kc += l + 1;
-                moment_order<false>(l + 1, m, col_ok, kc, cr, qb_, qa_, x2, st, A, sDq + (l + 1 - m0) * 24, drow, lane);
+                order_step<H, false>(l + 1, m, col_ok, kc, cr, qb_, qa_, x2, st, A, sDq + (l + 1 - m0) * 24, drow, lane);
                 if (col_ok) kc += l + 2;
             }
-            if (l <= LM) moment_order<false>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
+            if (l <= LM) order_step<H, false>(l, m, col_ok, kc, cr, qa_, qb_, x2, st, A, sDq + (l - m0) * 24, drow, lane);
         }
     }
     __syncwarp();
@@ -394,7 +501,7 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
         int k = mo * (mo + 1) / 2 + mo;
         for (int l = mo; l <= LM; ++l) {
             const float2 v = sDq[(l - m0) * 24 + lane];
-            const float sc = __ldg(&cr[k].y);
+            const float sc = H ? wback : __ldg(&cr[k].y);
             out[k] = make_float2(v.x * sc, v.y * sc);
             k += l + 1;
         }
@@ -899,12 +1006,74 @@ __device__ void hm_moments_tc(const float4* __restrict__ pts, const int4* __rest
 }
 
 // ---------------------------------------------------------------------------
+// tcgen05 issue calibration: one thread issues R = 32 MMAs of kind::f16,
+// M = 128 (A in tensor memory, B in shared memory, zeros), N = 16 or 256, into
+// one accumulator, and times (clock64) from the first issue to the commit's
+// mbarrier completion: cycles[0] for N = 16, cycles[1] for N = 256, the best of
+// 4 repetitions.  Bounded waits; status 1 when a wait ran out.
+// ---------------------------------------------------------------------------
+constexpr int kIssueProbeMmas = 32;
+__global__ void __launch_bounds__(128, 1) tc_issue_probe_kernel(long long* cycles, int* status) {
+    extern __shared__ __align__(1024) unsigned char pr_raw[];
+    unsigned char* sm = pr_raw + ((1024u - (smem_u32(pr_raw) & 1023u)) & 1023u);
+    unsigned char* sB = sm;  // 256 rows x 128 B of zeros
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 32768);
+    volatile uint32_t* sta = reinterpret_cast<volatile uint32_t*>(sm + 32768 + 16);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int e = tid; e < 32768 / 16; e += blockDim.x) reinterpret_cast<uint4*>(sB)[e] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32((const void*)sta)),
+                     "r"(512u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tb = *sta;
+    if (tid == 0) {
+        const uint64_t bd = sw128_desc(smem_u32(sB));
+        int phase = 0;
+        for (int v = 0; v < 2; ++v) {
+            const uint32_t n = v == 0 ? 16u : 256u;
+            const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+            long long best = -1;
+            for (int rep = 0; rep < 4; ++rep) {
+                const long long t0 = clock64();
+                for (int r = 0; r < kIssueProbeMmas; ++r)
+                    mma_f16_ts(tb + 256u, tb + 8u * (uint32_t)(r & 3), bd, idesc, r > 0 ? 1u : 0u);
+                mma_commit(bar);
+                if (!mbar_wait(bar, (uint32_t)(phase & 1))) *status = 1;
+                ++phase;
+                const long long dt = clock64() - t0;
+                if (best < 0 || dt < best) best = dt;
+            }
+            cycles[v] = best;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tb), "r"(512u) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Pipe calibration (the denominators of the moments' roofline): independent
 // chains per thread, long enough that launch costs vanish.
 //   kind 0: scalar FP32 FMA, 8 chains        (2 flops per FMA)
 //   kind 1: packed fma.rn.f32x2, 8 chains    (4 flops per instruction)
 //   kind 2: mma.sync m16n8k8 TF32, 4 independent accumulators per warp
 //           (2 x 16 x 8 x 8 = 2,048 flops per MMA)
+//   kind 3: mma.sync m16n8k16 FP16 with FP32 accumulators, 4 independent
+//           accumulators per warp (4,096 flops per MMA)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) pipe_probe_kernel(int kind, int iters, float* out) {
     float acc = 0.f;
@@ -933,7 +1102,7 @@ __global__ void __launch_bounds__(256) pipe_probe_kernel(int kind, int iters, fl
             upk2(x[c], u, v);
             acc += u + v;
         }
-    } else {
+    } else if (kind == 2) {
         float d[4][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
@@ -942,6 +1111,19 @@ __global__ void __launch_bounds__(256) pipe_probe_kernel(int kind, int iters, fl
         for (int it = 0; it < iters; ++it) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) mma_tf32(d[j], a, b0, b1);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc += d[j][0] + d[j][1] + d[j][2] + d[j][3];
+    } else {
+        float d[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
+        const uint32_t a[4] = {h2pack(1e-3f * threadIdx.x, 0.5f), h2pack(0.25f, 0.125f), h2pack(0.5f, 0.25f),
+                               h2pack(0.125f, 1e-3f)};
+        const uint32_t b0 = h2pack(1e-3f, 2e-3f), b1 = h2pack(3e-3f, 4e-3f);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) mma_f16(d[j], a, b0, b1);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc += d[j][0] + d[j][1] + d[j][2] + d[j][3];
@@ -1325,6 +1507,34 @@ __device__ __forceinline__ float2 split_ff(double x) {
     return make_float2(hi, (float)(x - (double)hi));
 }
 
+// X[s] = sum_{c < 6} D[c] e^{2 pi i c s / 6}: E = DFT3 of the even classes,
+// O = DFT3 of the odd ones (e^{2 pi i / 3} steps), X[s] = E[s mod 3] +
+// e^{i pi s / 3} O[s mod 3], X[s + 3] = E[s] - e^{i pi s / 3} O[s].
+__device__ __forceinline__ void dft3(float2 a, float2 b, float2 c, float2& x0, float2& x1, float2& x2) {
+    constexpr float kS3 = 0.86602540378443865f;  // sin(pi/3)
+    const float2 t1 = make_float2(b.x + c.x, b.y + c.y);
+    const float2 t2 = make_float2(fmaf(-0.5f, t1.x, a.x), fmaf(-0.5f, t1.y, a.y));
+    const float2 t3 = make_float2(-kS3 * (b.y - c.y), kS3 * (b.x - c.x));  // i sin(pi/3) (b - c)
+    x0 = make_float2(a.x + t1.x, a.y + t1.y);
+    x1 = make_float2(t2.x + t3.x, t2.y + t3.y);
+    x2 = make_float2(t2.x - t3.x, t2.y - t3.y);
+}
+__device__ __forceinline__ void dft6(const float2 (&D)[6], float2 (&X)[6]) {
+    constexpr float kS3 = 0.86602540378443865f;
+    float2 E[3], O[3];
+    dft3(D[0], D[2], D[4], E[0], E[1], E[2]);
+    dft3(D[1], D[3], D[5], O[0], O[1], O[2]);
+    // twiddles e^{i pi s / 3}: 1, (1/2, sin(pi/3)), (-1/2, sin(pi/3))
+    const float2 o1 = make_float2(0.5f * O[1].x - kS3 * O[1].y, kS3 * O[1].x + 0.5f * O[1].y);
+    const float2 o2 = make_float2(-0.5f * O[2].x - kS3 * O[2].y, kS3 * O[2].x - 0.5f * O[2].y);
+    X[0] = make_float2(E[0].x + O[0].x, E[0].y + O[0].y);
+    X[3] = make_float2(E[0].x - O[0].x, E[0].y - O[0].y);
+    X[1] = make_float2(E[1].x + o1.x, E[1].y + o1.y);
+    X[4] = make_float2(E[1].x - o1.x, E[1].y - o1.y);
+    X[2] = make_float2(E[2].x + o2.x, E[2].y + o2.y);
+    X[5] = make_float2(E[2].x - o2.x, E[2].y - o2.y);
+}
+
 __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
                                                           const float2* __restrict__ Cv, int K,
                                                           const int* __restrict__ lmax, const float2* __restrict__ ab,
@@ -1447,9 +1657,6 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
     __syncthreads();
     // ---- cell stage: rpp rows at a time ----
     const int64_t base = shell_base(i);
-    constexpr float kS3 = 0.86602540378443865f;  // sin(pi/3)
-    const float wr6[6] = {1.f, 0.5f, -0.5f, -1.f, -0.5f, 0.5f};
-    const float wi6[6] = {0.f, kS3, kS3, 0.f, -kS3, -kS3};
     const int rpp = max(1, min(nr, kSynthThreads / i));
     for (int r0 = 0; r0 < nr; r0 += rpp) {
         const int nrp = min(rpp, nr - r0);
@@ -1514,28 +1721,24 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
             }
             const float st = sRow[r][0].x, ct = sRow[r][0].y;
             const float2 A2 = sRow[r][1], B2 = sRow[r][2], Z2 = sRow[r][3];
+            // the six sextants X[sx] = sum_c D_c e^{2 pi i c sx / 6} as two 3-point
+            // DFTs (even and odd classes) and one radix-2 step
+            float2 X[6], Xv[6];
+            dft6(D, X);
+            if (vox) dft6(Dv, Xv);
+            const float qz = qI * ct;
+            const float sz = vox ? sinc_h(0.5f * qz * vox_s) : 0.f;  // the row's z factor
 #pragma unroll
             for (int sx = 0; sx < 6; ++sx) {
-                float ar = 0.f, ai = 0.f, vr = 0.f, vi = 0.f;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    const int e = (c * sx) % 6;
-                    ar += D[c].x * wr6[e] - D[c].y * wi6[e];
-                    ai += D[c].x * wi6[e] + D[c].y * wr6[e];
-                    if (vox) {
-                        vr += Dv[c].x * wr6[e] - Dv[c].y * wi6[e];
-                        vi += Dv[c].x * wi6[e] + Dv[c].y * wr6[e];
-                    }
-                }
+                float ar = X[sx].x, ai = X[sx].y;
                 const int p = sx * i + j;
                 const float2 w = sW[p];  // (cos, sin) of the cell's phi = p pi / 3i
                 const float cp = w.x, sp = w.y;
-                const float qx = qI * st * cp, qy = qI * st * sp, qz = qI * ct;
+                const float qx = qI * st * cp, qy = qI * st * sp;
                 if (vox) {
-                    const float f = vox_s * sinc_h(0.5f * qx * vox_s) * vox_s * sinc_h(0.5f * qy * vox_s) * vox_s *
-                                    sinc_h(0.5f * qz * vox_s);
-                    ar = fmaf(f, vr, ar);
-                    ai = fmaf(f, vi, ai);
+                    const float f = vox_s * sinc_h(0.5f * qx * vox_s) * vox_s * sinc_h(0.5f * qy * vox_s) * vox_s * sz;
+                    ar = fmaf(f, Xv[sx].x, ar);
+                    ai = fmaf(f, Xv[sx].y, ai);
                 }
                 float2 F = make_float2(ar * scale, ai * scale);
                 if (use_center) {
@@ -1618,6 +1821,7 @@ __global__ void __launch_bounds__(kNodesThreads) hm_nodes_jobs(const HarmJob* __
     hm_nodes(h.Lp, h.nbins, h.LM, h.step, h.delta, h.lmax, h.nodes, reinterpret_cast<double*>(scratch + h.s_Jn), e);
 }
 
+template <bool H>
 __global__ void __launch_bounds__(32) hm_moments_jobs(const HarmJob* __restrict__ J, int n,
                                                       char* __restrict__ scratch) {
     const int64_t b = blockIdx.x;
@@ -1626,8 +1830,8 @@ __global__ void __launch_bounds__(32) hm_moments_jobs(const HarmJob* __restrict_
     const int k = js & 1;
     const int64_t local = b - h.b_mom[k];
     const int nu = h.n_units[k];
-    hm_moments(h.pts[k], h.units[k], h.K, (float)h.delta, h.lmb, h.cr, h.nmm,
-               reinterpret_cast<float2*>(scratch + h.s_MP[k]), (int)(local % nu), (int)(local / nu));
+    hm_moments<H>(h.pts[k], h.units[k], h.K, (float)h.delta, h.lmb, h.cr, h.nmm,
+                  reinterpret_cast<float2*>(scratch + h.s_MP[k]), (int)(local % nu), (int)(local / nu));
 }
 
 // The tensor-core moments of every (job, set): a set's CTAs are its units'
@@ -1704,11 +1908,11 @@ size_t synth_smem(int Lp, int li) {
     return ((size_t)kSynthRows * 2 * nG + (size_t)nph + cells) * sizeof(float2);
 }
 std::mutex g_smem_mu;
-size_t g_smem_set[3][64] = {};  // per device: the limits set for hm_moments, hm_synth, hm_moments_tc
-std::atomic<int> g_moments_kind{1};
+size_t g_smem_set[4][64] = {};  // per device: the limits set for hm_moments (TF32), hm_synth, hm_moments_tc, hm_moments (FP16)
+std::atomic<int> g_moments_kind{2};
 }  // namespace
 
-void set_moments_kernel(int kind) { g_moments_kind.store(kind == 1 ? 1 : 0); }
+void set_moments_kernel(int kind) { g_moments_kind.store(kind >= 0 && kind <= 2 ? kind : 2); }
 int moments_kernel() { return g_moments_kind.load(); }
 
 cudaError_t harmonic_take_faults(unsigned* flags) {
@@ -1728,18 +1932,28 @@ cudaError_t launch_pipe_probe(cudaStream_t s, int kind, int blocks, int iters, f
     return cudaGetLastError();
 }
 
+cudaError_t launch_tc_issue_probe(cudaStream_t s, long long* cycles, int* status) {
+    constexpr int smem = 1024 + 32768 + 64;
+    cudaError_t e = cudaFuncSetAttribute(tc_issue_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    tc_issue_probe_kernel<<<1, 128, smem, s>>>(cycles, status);
+    return cudaGetLastError();
+}
+int tc_issue_probe_mmas() { return kIssueProbeMmas; }
+
 cudaError_t harmonic_reserve_smem(int Lp, int LM) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    const size_t need[3] = {moments_smem(LM), synth_smem(Lp, LM), kTcSmemLaunch};
+    const size_t need[4] = {moments_smem(LM), synth_smem(Lp, LM), kTcSmemLaunch, moments_smem(LM)};
     std::lock_guard<std::mutex> lock(g_smem_mu);
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         if (need[k] <= 48 * 1024 || need[k] <= g_smem_set[k][dev]) continue;
-        const void* f = k == 0 ? (const void*)hm_moments_jobs
+        const void* f = k == 0 ? (const void*)hm_moments_jobs<false>
                         : k == 1 ? (const void*)hm_synth_jobs
-                                 : (const void*)hm_moments_tc_jobs;
+                        : k == 2 ? (const void*)hm_moments_tc_jobs
+                                 : (const void*)hm_moments_jobs<true>;
         e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need[k]);
         if (e != cudaSuccess) return e;
         g_smem_set[k][dev] = need[k];
@@ -1820,8 +2034,10 @@ cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, c
     if (e == cudaSuccess && sh.moments > 0) {
         if (sh.moments_kind == 0)
             hm_moments_tc_jobs<<<(unsigned)sh.moments, kTcThreads, kTcSmemLaunch, s>>>(d_jobs, n, scratch);
+        else if (sh.moments_kind == 2)
+            hm_moments_jobs<true><<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
         else
-            hm_moments_jobs<<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
+            hm_moments_jobs<false><<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
     }
     if (e == cudaSuccess && ev && ev[1]) e = cudaEventRecord(ev[1], s);
     if (e == cudaSuccess && b > 0) hm_fit_groups<<<(unsigned)b, kFitThreads, 0, s>>>(d_jobs, n, sh.fit, scratch);

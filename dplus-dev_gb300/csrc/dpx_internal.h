@@ -195,8 +195,9 @@ __host__ __device__ inline int tc_octet_first(int LM, int o) { return o * (LM + 
 __host__ __device__ inline int tc_steps(int LM) { return tc_octet_first(LM, LM / 8 + 1); }
 __host__ __device__ inline int tc_parts(int LM) { return (tc_steps(LM) + 4 * kTcSlotSteps - 1) / (4 * kTcSlotSteps); }
 // Which moments kernel the harmonic launches use (process-wide): 0 tcgen05.mma
-// (FP16 hi + lo operands, accumulators in tensor memory), 1 (the default)
-// mma.sync TF32 (split operands, sums in shared memory).
+// (FP16 hi + lo operands, accumulators in tensor memory), 1 mma.sync TF32
+// m16n8k8, 2 (the default) mma.sync FP16 m16n8k16 (split operands, sums in
+// shared memory).
 void set_moments_kernel(int kind);
 int moments_kernel();
 // Faults recorded by the tensor-core moments kernel (a wait that ran past its
@@ -291,6 +292,10 @@ cudaError_t harmonic_reserve_smem(int Lp, int LM);
 // mma.sync m16n8k8 TF32 (256 threads a block, iters steps of 8 / 8 / 4
 // independent operations per thread or warp).
 cudaError_t launch_pipe_probe(cudaStream_t s, int kind, int blocks, int iters, float* out);
+// cycles[2]: one thread issuing tc_issue_probe_mmas() tcgen05 MMAs (M = 128,
+// N = 16 and N = 256) until their commit completes; *status 1 on a wait limit.
+cudaError_t launch_tc_issue_probe(cudaStream_t s, long long* cycles, int* status);
+int tc_issue_probe_mmas();
 
 // Debye sum of one leaf (dpx_debye.cu).  Atoms padded to a multiple of the
 // 128-atom tile; F tables [nq][npad] of the path's type; partial sums

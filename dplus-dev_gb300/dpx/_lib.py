@@ -19,7 +19,7 @@ DPX_CALC_ATOMIC_FORMFACTORS = 1
 DPX_CALC_DUMMY_SOLVENT = 2
 DPX_FILL_DIRECT, DPX_FILL_HARMONIC = 0, 1
 DPX_CONV_CPU, DPX_CONV_GPU = 0, 1
-DPX_MOMENTS_TCGEN05, DPX_MOMENTS_MMA_SYNC = 0, 1
+DPX_MOMENTS_TCGEN05, DPX_MOMENTS_MMA_SYNC, DPX_MOMENTS_MMA_F16 = 0, 1, 2
 DPX_OA_MC, DPX_OA_VEGAS = 0, 1
 
 _STATUS = {-1: "DPX_ERR_ARG", -2: "DPX_ERR_CUDA", -3: "DPX_ERR_OOM", -4: "DPX_ERR_STOPPED",
@@ -163,6 +163,7 @@ _SIGS = {
     "dpx_hybrid_destroy": (C.c_int, [_P]),
     "dpx_measure_sfu_peak": (C.c_int, [_P, _D]),
     "dpx_measure_pipe_peaks": (C.c_int, [_P, _D]),
+    "dpx_measure_tcgen05_issue": (C.c_int, [_P, _D]),
     "dpx_debye_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), _F, _F, C.c_int, _D, C.c_int, _D]),
     "dpx_direct_intensity": (C.c_int, [_P, C.POINTER(PdbDesc), C.c_int, _D, _D, C.c_int, _D, C.c_int64, _D, _D]),
     "dpx_calc_debye_v2": (C.c_int, [C.c_int, C.c_float, C.c_float, _D, C.c_int, _I, _F, C.POINTER(C.c_uint8), _F,

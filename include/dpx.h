@@ -118,13 +118,15 @@ enum { DPX_FILL_DIRECT = 0, DPX_FILL_HARMONIC = 1 };
  * the independent gathers in flight at a higher register count. */
 int dpx_set_average_shape(int directions_per_thread);
 /* Moments kernel of the harmonic fill, for every context of the process (no
- * counterpart in the reference): DPX_MOMENTS_MMA_SYNC (the default) computes the
- * moments with the warp-level mma.sync TF32 path (operands in registers);
- * DPX_MOMENTS_TCGEN05 on the fifth-generation tensor cores (tcgen05.mma with
- * FP16 operands split into value and remainder, accumulators in tensor
- * memory).  Harmonic plans made after the call use it (prepared leaves and
- * batches keep the kernel they were planned with). */
-enum { DPX_MOMENTS_TCGEN05 = 0, DPX_MOMENTS_MMA_SYNC = 1 };
+ * counterpart in the reference): DPX_MOMENTS_MMA_F16 (the default) computes the
+ * moments with the warp-level mma.sync path, FP16 operands split into value and
+ * remainder (m16n8k16); DPX_MOMENTS_MMA_SYNC the same with TF32 split operands
+ * (m16n8k8: twice the MMAs); DPX_MOMENTS_TCGEN05 on the fifth-generation tensor
+ * cores (tcgen05.mma with FP16 split operands, accumulators in tensor memory).
+ * All three give the same amplitudes within the FP32 bound.  Harmonic plans
+ * made after the call use it (prepared leaves and batches keep the kernel they
+ * were planned with). */
+enum { DPX_MOMENTS_TCGEN05 = 0, DPX_MOMENTS_MMA_SYNC = 1, DPX_MOMENTS_MMA_F16 = 2 };
 int dpx_set_moments_kernel(int kind);
 int dpx_get_moments_kernel(void);
 /* Faults recorded by this library's kernels on the current device since the
@@ -474,11 +476,18 @@ int dpx_hybrid_destroy(dpx_hybrid h);
  * GPU sustains (sin and cos count one each) — the denominator of the amplitude
  * fill's roofline. */
 int dpx_measure_sfu_peak(dpx_ctx ctx, double* ops_per_s);
-/* Pipe calibration (no counterpart in the reference): flops_per_s[3] = the
- * FP32 FMA pipe with scalar FMAs, with packed f32x2 FMAs, and the TF32
- * mma.sync (m16n8k8) tensor path this GPU sustains, each from a kernel of
- * independent chains — the denominators of the harmonic moments' roofline. */
+/* Pipe calibration (no counterpart in the reference): flops_per_s[4] = the
+ * FP32 FMA pipe with scalar FMAs, with packed f32x2 FMAs, the TF32 mma.sync
+ * (m16n8k8) and the FP16 mma.sync (m16n8k16, FP32 accumulators) tensor paths
+ * this GPU sustains, each from a kernel of independent chains — the
+ * denominators of the harmonic moments' roofline. */
 int dpx_measure_pipe_peaks(dpx_ctx ctx, double* flops_per_s);
+/* tcgen05 issue calibration (no counterpart in the reference): one thread
+ * issues 32 MMAs of kind::f16, M = 128 (A in tensor memory, B in shared
+ * memory) into one accumulator; cycles_per_mma[2] = SM cycles per MMA from the
+ * first issue to the commit's completion at N = 16 and at N = 256 — the
+ * evidence for which shapes the fifth-generation tensor cores can be fed at. */
+int dpx_measure_tcgen05_issue(dpx_ctx ctx, double* cycles_per_mma);
 
 /* ---- amplitude-grid files (D+'s binary .amp, version 13: JacobianSphereGrid::
  * ExportBinaryData / ImportBinaryData, Backend/Backend/Grid.cpp:847-963) ----

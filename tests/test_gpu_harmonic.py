@@ -197,11 +197,11 @@ def test_prepared_leaf_fill_replays_in_a_cuda_graph(harmonic):
 def test_pipe_calibration_is_plausible(ctx):
     """dpx_measure_pipe_peaks: the FP32 FMA pipe (scalar and f32x2) within a
     factor of two of 152 SMs x 128 lanes x 2 flops at 1.0-2.1 GHz, and the TF32
-    mma.sync path measured."""
+    and FP16 mma.sync paths measured."""
     import dpx
-    p = np.zeros(3)
+    p = np.zeros(4)
     _lib.check(dpx.lib().dpx_measure_pipe_peaks(ctx.handle, _lib.dptr(p)))
     nominal_lo, nominal_hi = 152 * 128 * 2 * 1.0e9, 152 * 128 * 2 * 2.1e9
     for v in p[:2]:
         assert nominal_lo / 2 <= v <= nominal_hi * 2
-    assert p[2] > 1e12
+    assert p[2] > 1e12 and p[3] > 1e12
