@@ -124,15 +124,15 @@ def build_inputs():
 
 
 def fill_launches(ctx, n_boxes):
-    """Kernel launches of one leaf's fill with its spline derivatives.
-    Harmonic fill: radial tables (2), moments + group sums + contraction per
-    point set (3 each), synthesis (1, which also writes the spline
-    derivatives), and with solvent voxels their expansion and binning (4);
-    direct fill: one launch (the boxes are sorted on the host), then the
-    spline pass (1)."""
+    """Kernel launches of one leaf's fill with its spline derivatives, planned
+    and launched in one call.  Harmonic fill: the plan's radial tables (2) and,
+    with solvent voxels, their preparation, expansion and binning (7); the
+    launch: moments, group sums, contraction, synthesis (4, the synthesis also
+    writes the spline derivatives); direct fill: one launch (the boxes are
+    sorted on the host), then the spline pass (1)."""
     from dpx import _lib
     if ctx.fill_method() == _lib.DPX_FILL_HARMONIC:
-        return 2 + 3 + 1 + ((4 + 3) if n_boxes else 0)
+        return 2 + 4 + (7 if n_boxes else 0)
     return 1 + 1
 
 

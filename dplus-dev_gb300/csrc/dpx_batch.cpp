@@ -9,9 +9,9 @@
 // budget.  Each wave is one CUDA graph:
 //   FP32 with the harmonic method (the default): the fills planned at
 //   creation, run in fill batches (as many structures as 8 GiB of scratch
-//   holds, each its own part of it): five launches per batch over its job
-//   table (radial nodes, moments, radial fit + group sums, contraction,
-//   synthesis with the phi-spline derivatives: launch_harmonic_jobs);
+//   holds, each its own part of it): four launches per batch over its job
+//   table (moments, group sums, contraction, synthesis with the phi-spline
+//   derivatives: launch_harmonic_jobs; the radial tables are the plans');
 //   FP32 leaves the harmonic method declines: one direct-sum launch over all of
 //   them, then their splines; FP64: the direct sum per structure and splines;
 //   the MC averages of all the wave's structures in three launches (bracket
@@ -369,12 +369,12 @@ int dpx_batch_create(dpx_ctx ctx, int n, const dpx_solve_desc* solves, int preci
         int64_t launches = 0;
         const int j0 = b->wave_first[w], j1 = b->wave_first[w + 1];
         if (fp32) {
-            // the wave's harmonic fills: five launches per fill batch
+            // the wave's harmonic fills: four launches per fill batch
             for (const auto& fb : b->fbatches) {
                 if (fb.wave != w || e != cudaSuccess) continue;
                 e = dpx::launch_harmonic_jobs(s, b->hjobs + fb.first, fb.n, fb.shape,
                                               static_cast<char*>(b->hscratch), pool, nullptr);
-                launches += (fb.shape.nodes > 0) + (fb.shape.moments > 0) + (fb.shape.fit + fb.shape.groups > 0) +
+                launches += (fb.shape.moments > 0) + (fb.shape.groups > 0) +
                             (fb.shape.contract > 0) + (fb.shape.synth > 0);
             }
             bool boxes = false;

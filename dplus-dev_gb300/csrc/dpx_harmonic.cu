@@ -22,8 +22,8 @@
 // (shell, bin, node) instead of once per (shell, point).
 //
 // Kernels:
-//   hm_nodes     j_l at the Chebyshev nodes of every (shell, bin), FP64
-//   hm_fit       T_n(i, b, l) from the node values (inverse Vandermonde)
+//   hm_nodes     j_l at the Chebyshev nodes of every (shell, bin), FP64   } once per plan
+//   hm_fit       T_n(i, b, l) from the node values (inverse Vandermonde)  } (launch_radial_tables)
 //   hm_moments   per unit of <= 1024 points of one group: M_unit[n][k] on the
 //                tensor cores (split TF32, FP32 sums), the basis values in
 //                registers by scaled Legendre recurrences
@@ -1485,7 +1485,7 @@ __device__ __forceinline__ float sinc_h(float h) {
 //   the Friedel mirror row gets the conjugates of both.
 // Dynamic shared memory: G (atoms, voxels) per row over m in [m0, m0 + nG)
 // with zero padding (m0 = -6 ceil(l_i/6)), the 6i roots of unity, the values
-// of the rows in flight (6 max(256, Lp) cells).
+// of the rows in flight (6 max(256, 2 Lp) cells).
 // ---------------------------------------------------------------------------
 constexpr int kSynthThreads = 256;
 constexpr int kSynthRows = 8;
@@ -1557,7 +1557,7 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
     // two neighbouring orders of one component load as one f32x2 pair
     float* sG = reinterpret_cast<float*>(smem);
     float2* sW = reinterpret_cast<float2*>(sG + (size_t)kSynthRows * 4 * nG);  // [6i]
-    float2* sF = sW + nph;                              // [6 max(256, Lp)]
+    float2* sF = sW + nph;                              // [6 max(256, 2 Lp)]
     const int tid = threadIdx.x;
     for (int n = tid; n < nph; n += blockDim.x) {
         float sw, cw;
@@ -1657,7 +1657,9 @@ __device__ void hm_synth(int Lp, const float2* __restrict__ Ca,
     __syncthreads();
     // ---- cell stage: rpp rows at a time ----
     const int64_t base = shell_base(i);
-    const int rpp = max(1, min(nr, kSynthThreads / i));
+    // rows in flight: as many as 256 threads have columns for, and at least
+    // two (so that a large shell keeps more than i of the 256 threads busy)
+    const int rpp = min(nr, max(2, kSynthThreads / i));
     for (int r0 = 0; r0 < nr; r0 += rpp) {
         const int nrp = min(rpp, nr - r0);
         for (int it = tid; it < nrp * i; it += blockDim.x) {
@@ -1814,11 +1816,13 @@ __device__ __forceinline__ int set_of(const HarmJob* __restrict__ J, int n, int6
 
 __device__ __forceinline__ int synth_groups(int Lp) { return (3 * Lp / 2 + 1 + kSynthRows - 1) / kSynthRows; }
 
-__global__ void __launch_bounds__(kNodesThreads) hm_nodes_jobs(const HarmJob* __restrict__ J, int n,
-                                                              char* __restrict__ scratch) {
-    const HarmJob& h = J[job_of(J, n, blockIdx.x, &HarmJob::b_nodes)];
-    const int64_t e = ((int64_t)blockIdx.x - h.b_nodes) * kNodesThreads + threadIdx.x;
-    hm_nodes(h.Lp, h.nbins, h.LM, h.step, h.delta, h.lmax, h.nodes, reinterpret_cast<double*>(scratch + h.s_Jn), e);
+// The radial tables of one plan (launch_radial_tables).
+__global__ void __launch_bounds__(kNodesThreads) hm_nodes_plan(RadialTableArgs a) {
+    hm_nodes(a.Lp, a.nbins, a.LM, a.step, a.delta, a.lmax, a.nodes, a.Jn,
+             (int64_t)blockIdx.x * kNodesThreads + threadIdx.x);
+}
+__global__ void __launch_bounds__(kFitThreads) hm_fit_plan(RadialTableArgs a) {
+    hm_fit(a.Lp, a.nbins, a.LM, a.lmax, a.vinv, a.Jn, a.T, (int64_t)blockIdx.x * kFitThreads + threadIdx.x);
 }
 
 template <bool H>
@@ -1846,17 +1850,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) hm_moments_tc_jobs(const HarmJo
                   reinterpret_cast<float2*>(scratch + h.s_MP[k]), b - h.b_mom[k]);
 }
 
-__global__ void __launch_bounds__(kFitThreads) hm_fit_groups(const HarmJob* __restrict__ J, int n, int64_t fit_blocks,
-                                                             char* __restrict__ scratch) {
-    const int64_t blk = blockIdx.x;
-    if (blk < fit_blocks) {
-        const HarmJob& h = J[job_of(J, n, blk, &HarmJob::b_fit)];
-        const int64_t e = (blk - h.b_fit) * kFitThreads + threadIdx.x;
-        hm_fit(h.Lp, h.nbins, h.LM, h.lmax, h.vinv, reinterpret_cast<const double*>(scratch + h.s_Jn),
-               reinterpret_cast<float*>(scratch + h.s_T), e);
-        return;
-    }
-    const int64_t b = blk - fit_blocks;
+__global__ void __launch_bounds__(kFitThreads) hm_groups_jobs(const HarmJob* __restrict__ J, int n,
+                                                              char* __restrict__ scratch) {
+    const int64_t b = blockIdx.x;
     const int js = set_of(J, n, b, &HarmJob::b_grp);
     const HarmJob& h = J[js >> 1];
     const int k = js & 1;
@@ -1873,7 +1869,7 @@ __global__ void __launch_bounds__(kContractK * kContractWarps) hm_contract_jobs(
     const int64_t local = (int64_t)blockIdx.x - h.b_con[k];
     const int gx = (h.K + kContractK - 1) / kContractK;
     hm_contract(reinterpret_cast<const float2*>(scratch + h.s_M[k]), h.groups[k], h.G[k],
-                reinterpret_cast<const float*>(scratch + h.s_T), h.nbins, h.LM, h.K, h.Lp, h.lmax, h.lmb, h.aff,
+                h.T, h.nbins, h.LM, h.K, h.Lp, h.lmax, h.lmb, h.aff,
                 reinterpret_cast<float2*>(scratch + h.s_C[k]), (int)(local % gx), (int)(local / gx));
 }
 
@@ -1900,11 +1896,11 @@ namespace {
 size_t moments_smem(int LM) { return (size_t)(LM + 5) * 24 * sizeof(float2); }
 // Dynamic shared memory of hm_synth for shells up to Lp and outer order li:
 // the G_m of kSynthRows rows, the phi phases of the outer shell, and the rows
-// in flight (rpp x 6i cells with rpp x i <= 256, or one row of 6i > 1,536 cells).
+// in flight (rpp x 6i cells with rpp x i <= 256, or two rows of 6i cells).
 size_t synth_smem(int Lp, int li) {
     const int nph = 6 * Lp;
     const int nG = 6 * ((li + 5) / 6) + 6 * ((li + 6) / 6);
-    const size_t cells = (size_t)6 * (Lp > kSynthThreads ? Lp : kSynthThreads);
+    const size_t cells = (size_t)6 * (2 * Lp > kSynthThreads ? 2 * Lp : kSynthThreads);
     return ((size_t)kSynthRows * 2 * nG + (size_t)nph + cells) * sizeof(float2);
 }
 std::mutex g_smem_mu;
@@ -1963,6 +1959,17 @@ cudaError_t harmonic_reserve_smem(int Lp, int LM) {
 
 int harmonic_max_bins() { return kMaxBins; }
 
+cudaError_t launch_radial_tables(cudaStream_t s, const RadialTableArgs& a) {
+    const int64_t nodes = (int64_t)a.Lp * a.nbins * kNodes, fits = (int64_t)a.Lp * a.nbins * (a.LM + 1);
+    if (nodes <= 0) return cudaSuccess;
+    if ((nodes + kNodesThreads - 1) / kNodesThreads > 0x7fffffff || (fits + kFitThreads - 1) / kFitThreads > 0x7fffffff)
+        return cudaErrorInvalidValue;
+    // rows of shell 0 (never read) stay as they are; shells 1..Lp are written
+    hm_nodes_plan<<<(unsigned)((nodes + kNodesThreads - 1) / kNodesThreads), kNodesThreads, 0, s>>>(a);
+    hm_fit_plan<<<(unsigned)((fits + kFitThreads - 1) / kFitThreads), kFitThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_voxel_prepare(cudaStream_t s, const VoxelPrepArgs& a) {
     if (a.nb <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(a.scal, 0, 3 * sizeof(unsigned long long), s);
@@ -1994,10 +2001,6 @@ HarmShape plan_harmonic_jobs(HarmJob* J, int n) {
         HarmJob& h = J[j];
         const int pairs = ((h.LM + 4) / 4 + 1) / 2;
         const int64_t gx = (h.K + kContractK - 1) / kContractK, gy = (h.Lp + kContractShells - 1) / kContractShells;
-        h.b_nodes = sh.nodes;
-        sh.nodes += ((int64_t)h.Lp * h.nbins * kNodes + kNodesThreads - 1) / kNodesThreads;
-        h.b_fit = sh.fit;
-        sh.fit += ((int64_t)h.Lp * h.nbins * (h.LM + 1) + kFitThreads - 1) / kFitThreads;
         for (int k = 0; k < 2; ++k) {
             h.b_mom[k] = sh.moments;
             sh.moments += sh.moments_kind == 0 ? (int64_t)h.n_parts[k] : (int64_t)h.n_units[k] * pairs;
@@ -2017,18 +2020,15 @@ HarmShape plan_harmonic_jobs(HarmJob* J, int n) {
     return sh;
 }
 
-int harmonic_launches_per_batch() { return 5; }
+int harmonic_launches_per_batch() { return 4; }
 
 cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, const HarmShape& sh, char* scratch,
                                  char* grid, cudaEvent_t* ev) {
     if (n <= 0) return cudaSuccess;
     if (sh.reserve_error != cudaSuccess) return sh.reserve_error;
-    const int64_t b = sh.fit + sh.groups;
-    if (sh.nodes > 0x7fffffff || sh.moments > 0x7fffffff || b > 0x7fffffff || sh.contract > 0x7fffffff ||
-        sh.synth > 0x7fffffff)
+    if (sh.moments > 0x7fffffff || sh.groups > 0x7fffffff || sh.contract > 0x7fffffff || sh.synth > 0x7fffffff)
         return cudaErrorInvalidValue;
     cudaError_t e = cudaSuccess;
-    if (sh.nodes > 0) hm_nodes_jobs<<<(unsigned)sh.nodes, kNodesThreads, 0, s>>>(d_jobs, n, scratch);
     // the limits were raised by harmonic_reserve_smem when the jobs were planned
     if (ev && ev[0]) e = cudaEventRecord(ev[0], s);
     if (e == cudaSuccess && sh.moments > 0) {
@@ -2040,7 +2040,7 @@ cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, c
             hm_moments_jobs<false><<<(unsigned)sh.moments, 32, moments_smem(sh.maxLM), s>>>(d_jobs, n, scratch);
     }
     if (e == cudaSuccess && ev && ev[1]) e = cudaEventRecord(ev[1], s);
-    if (e == cudaSuccess && b > 0) hm_fit_groups<<<(unsigned)b, kFitThreads, 0, s>>>(d_jobs, n, sh.fit, scratch);
+    if (e == cudaSuccess && sh.groups > 0) hm_groups_jobs<<<(unsigned)sh.groups, kFitThreads, 0, s>>>(d_jobs, n, scratch);
     if (e == cudaSuccess && sh.contract > 0)
         hm_contract_jobs<<<(unsigned)sh.contract, kContractK * kContractWarps, 0, s>>>(d_jobs, n, scratch);
     if (e == cudaSuccess && ev && ev[2]) e = cudaEventRecord(ev[2], s);

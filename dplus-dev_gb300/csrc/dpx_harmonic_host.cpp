@@ -293,9 +293,28 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
     p.o_gu[1] = al16(p.o_groups[1] + (size_t)nbins * sizeof(int2));
     p.o_pts[1] = al16(p.o_gu[1] + (size_t)(nbins + 1) * sizeof(int));
     p.o_job = al16(nv ? p.o_pts[1] + (size_t)nv * sizeof(float4) : staged);
-    p.arena_bytes = p.o_job + sizeof(dpx::HarmJob) + 16;
+    // the radial tables T_n(i, b, l): they depend on the grid's shells and the
+    // radial bins only, so they are computed here once, not in every fill
+    p.o_T = al16(p.o_job + sizeof(dpx::HarmJob));
+    p.arena_bytes = p.o_T + (size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float) + 16;
     DPX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p.arena), p.arena_bytes, st));
     DPX_CUDA(cudaMemcpyAsync(p.arena, h.data(), staged, cudaMemcpyHostToDevice, st));
+    {
+        TmpDev jn(st);  // j_l at the nodes, FP64, freed in stream order after the fit
+        DPX_CUDA(jn.get((size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double)));
+        dpx::RadialTableArgs ra{};
+        ra.Lp = Lp;
+        ra.nbins = nbins;
+        ra.LM = LM;
+        ra.step = G.step;
+        ra.delta = delta;
+        ra.lmax = reinterpret_cast<const int*>(p.arena + p.o_lmax);
+        ra.nodes = reinterpret_cast<const double*>(p.arena + p.o_nodes);
+        ra.vinv = reinterpret_cast<const double*>(p.arena + p.o_vinv);
+        ra.Jn = static_cast<double*>(jn.p);
+        ra.T = reinterpret_cast<float*>(p.arena + p.o_T);
+        DPX_CUDA(dpx::launch_radial_tables(st, ra));
+    }
     // ---- the voxels: expanded and sorted by bin on the device, units from the totals ----
     Set sv;
     if (nv > 0) {
@@ -381,8 +400,6 @@ int harmonic_plan(cudaStream_t st, const dpx_pdb_desc& d, const dpx::Geom& G, Ha
         o = at + n;
         return at;
     };
-    p.s_Jn = take((size_t)(Lp + 1) * nbins * 6 * (LM + 1) * sizeof(double));
-    p.s_T = take((size_t)(Lp + 1) * nbins * (LM + 1) * 8 * sizeof(float));
     for (int k = 0; k < 2; ++k) {
         p.s_MP[k] = take((size_t)p.n_units[k] * mpu);
         p.s_M[k] = take((size_t)p.n_groups[k] * mpu);
@@ -442,8 +459,7 @@ dpx::HarmJob harmonic_job(const HarmPlan& p, size_t scratch_off, size_t grid_off
     J.cy = p.cen[1];
     J.cz = p.cen[2];
     J.origin = p.origin;
-    J.s_Jn = scratch_off + p.s_Jn;
-    J.s_T = scratch_off + p.s_T;
+    J.T = reinterpret_cast<const float*>(base + p.o_T);
     J.grid_off = grid_off;
     return J;
 }
@@ -461,7 +477,7 @@ int harmonic_launch(const HarmStreams& S, const HarmPlan& p, void* scratch, floa
 
 int harmonic_launches(const HarmPlan& p) {
     const dpx::HarmShape& h = p.shape;
-    return (h.nodes > 0) + (h.moments > 0) + (h.fit + h.groups > 0) + (h.contract > 0) + (h.synth > 0);
+    return (h.moments > 0) + (h.groups > 0) + (h.contract > 0) + (h.synth > 0);
 }
 
 }  // namespace dpxh

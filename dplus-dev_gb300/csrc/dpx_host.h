@@ -221,9 +221,10 @@ struct HarmPlan {
     size_t o_lmax = 0, o_lmb = 0, o_ab = 0, o_cr = 0, o_nmm = 0, o_nodes = 0, o_vinv = 0, o_aff = 0;
     size_t o_pts[2] = {0, 0}, o_units[2] = {0, 0}, o_groups[2] = {0, 0}, o_gu[2] = {0, 0};
     // scratch of a launch (offsets from the caller's scratch, 256-byte aligned)
-    size_t s_Jn = 0, s_T = 0, s_MP[2] = {0, 0}, s_M[2] = {0, 0}, s_C[2] = {0, 0};
+    size_t s_MP[2] = {0, 0}, s_M[2] = {0, 0}, s_C[2] = {0, 0};
     size_t scratch_bytes = 0;
     size_t o_job = 0;       // the plan's own job (scratch and grid at offset 0) in the arena
+    size_t o_T = 0;         // the radial tables T_n(i, b, l) in the arena (computed when planned)
     dpx::HarmShape shape{};  // its launch layout
 };
 // The stream of a launch; tev (null: no timing) receives the stage events.

@@ -226,28 +226,42 @@ struct HarmJob {
     float vox_s, scale;        // voxel edge (nm), scale
     double cx, cy, cz;         // the centring translation restored per cell
     double origin;             // F(0)
-    size_t s_Jn, s_T, s_MP[2], s_M[2], s_C[2];  // scratch offsets (bytes)
+    const float* T;            // radial polynomial tables T_n(i, b, l), computed when planned
+    size_t s_MP[2], s_M[2], s_C[2];  // scratch offsets (bytes)
     size_t grid_off;           // grid offset (bytes)
     float4* grid_ptr;          // the grid itself when not null (grid_off unused)
     // the job's first blocks in each launch (plan_harmonic_jobs)
-    int64_t b_nodes, b_mom[2], b_fit, b_grp[2], b_con[2], b_syn;
+    int64_t b_mom[2], b_grp[2], b_con[2], b_syn;
 };
 // Blocks of the launches and the largest shell count and order (shared
 // memory) of a job table.
 struct HarmShape {
-    int64_t nodes, moments, fit, groups, contract, synth;
+    int64_t moments, groups, contract, synth;
     int maxLp, maxLM;
     int moments_kind;  // moments_kernel() when planned
     cudaError_t reserve_error;  // raising the launches' shared-memory limits (on the planning device)
 };
 // Host: the block layout of n jobs (sets their b_* fields).
 HarmShape plan_harmonic_jobs(HarmJob* jobs, int n);
-// The harmonic fills of n jobs in five launches: radial nodes, moments, radial
-// fit + group sums, contraction, synthesis.  ev[0..1] (when not null) are
-// recorded around the moments, ev[2..3] around the synthesis.
+// The harmonic fills of n jobs in four launches: moments, group sums,
+// contraction, synthesis (the radial tables are the plans').  ev[0..1] (when
+// not null) are recorded around the moments, ev[2..3] around the synthesis.
 cudaError_t launch_harmonic_jobs(cudaStream_t s, const HarmJob* d_jobs, int n, const HarmShape& sh, char* scratch,
                                  char* grid, cudaEvent_t* ev);
 int harmonic_launches_per_batch();
+// The radial tables of a plan (once per plan): j_l at the Chebyshev nodes of
+// every (shell i >= 1, bin) in FP64 into Jn [(Lp + 1) nbins 6 (LM + 1)], then
+// the interpolation coefficients T [(Lp + 1) nbins (LM + 1) 8] (FP32).
+struct RadialTableArgs {
+    int Lp, nbins, LM;
+    double step, delta;
+    const int* lmax;
+    const double* nodes;
+    const double* vinv;
+    double* Jn;
+    float* T;
+};
+cudaError_t launch_radial_tables(cudaStream_t s, const RadialTableArgs& a);
 int harmonic_max_l();
 int harmonic_nodes();
 int harmonic_max_bins();

@@ -442,14 +442,14 @@ int launch_fills(dpx_server_s* S, const std::vector<GridEntry*>& fresh, Delta& d
         if (e != cudaSuccess) return cuda_fail(e, "fill launch");
         dl.fill_launches++;
     }
-    if (!hj.empty()) {  // the harmonic fills: five launches over their job table
+    if (!hj.empty()) {  // the harmonic fills: four launches over their job table
         char* scratch = nullptr;
         DPX_CUDA(cudaMallocAsync((void**)&scratch, hscratch, s));
         e = dpx::launch_harmonic_jobs(s, reinterpret_cast<const dpx::HarmJob*>(d + hjobs_at), (int)hj.size(), hshape,
                                       scratch, nullptr, nullptr);
         cudaFreeAsync(scratch, s);
         if (e != cudaSuccess) return cuda_fail(e, "harmonic fill launch");
-        dl.fill_launches += (hshape.nodes > 0) + (hshape.moments > 0) + (hshape.fit + hshape.groups > 0) +
+        dl.fill_launches += (hshape.moments > 0) + (hshape.groups > 0) +
                             (hshape.contract > 0) + (hshape.synth > 0);
     }
     DPX_CUDA(cudaFreeAsync(d, s));
