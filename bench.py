@@ -35,10 +35,11 @@ N_DIRS, DIR_SEED = 100_000, 1234
 # ncu dram__bytes_read+write of fill_f32_kernel on the profile shape (2,000 atoms,
 # 120 layers, 11.3 M cells): 335 MB, i.e. 29.6 B per cell; scaled to 50.7 M cells
 FILL_TRAFFIC = 29.6 * 50688289
-# ncu dram__bytes_read+write of the voxel hm_moments launch on the profile shape
-# (about 452,000 voxels): 6.93 MB read, 0 written, i.e. 15.7 B per point (each
-# point read once); scaled to the points of the workload
-MOMENTS_BYTES_PER_POINT = 15.7
+# ncu dram__bytes_read+write of the moments launch (hm_moments_jobs<FP16>, atoms
+# and voxels in one launch) at full size: 137.3 MB read + 144.1 MB written for
+# 2,006,280 points, i.e. 140.3 B per point (each point read once, the moments of
+# every unit written once); scaled to the points of the workload
+MOMENTS_BYTES_PER_POINT = 140.3
 # scale, solventED, c1, voxelStep, probe radius, solvation thickness, outer (layer) ED, fillHoles,
 # solventOnly, radius type 4 (dummy atoms): dummy-atom solvent at 333 e/nm^3 and a 0.3 nm voxelized
 # solvation layer at 400 e/nm^3
