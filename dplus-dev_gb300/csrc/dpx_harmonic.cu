@@ -408,7 +408,9 @@ __device__ void hm_moments(const float4* __restrict__ pts, const int4* __restric
         }
         const float2 zq0 = cpow(z, m0a);
         const float2 zq1 = nq == 2 ? cpow(z, m0b) : make_float2(0.f, 0.f);
-        // ---- the lane's eight points 8j + t + 4h: recurrence inputs, weight fragments ----
+        // ---- the lane's eight points (pair j, member h: 8j + t + 4h for TF32, the
+        // m16n8k8 fragment; 16 (j / 2) + 2t + 8 (j % 2) + h for FP16, m16n8k16):
+        // recurrence inputs, weight fragments ----
         f2x x2[4];
         uint32_t A[4][4];  // H: [k-step][a0..a3], k-steps 0, 1
 #pragma unroll
